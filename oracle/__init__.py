@@ -1,0 +1,249 @@
+"""TEST INFRASTRUCTURE ONLY -- the FP64 CPU oracle for the ReaDDy hot path.
+
+ctypes front end of ``readdy_oracle.cpp``, an FP64 restatement of ReaDDy's CPU kernel
+(kernels/cpu/src: cell-linked list, forces, Euler BD, uncontrolled approximation, Gillespie).
+Only the tests, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` leg of ``bench.py`` may
+use it, and only as the checker; the product path never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libreaddy_oracle.so")
+_lib = None
+_lock = threading.Lock()
+
+UNCONTROLLED_APPROXIMATION = 0
+GILLESPIE = 1
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++, a few seconds)."""
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def _load():
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        build()
+        lib = C.CDLL(_LIB_PATH)
+        d, i, u64, vp = C.c_double, C.c_int, C.c_uint64, C.c_void_p
+        i64 = C.c_int64
+        P = C.POINTER
+        sig = {
+            "orc_create": (vp, [P(d), P(i), d, i, P(d), u64, i, i]),
+            "orc_destroy": (None, [vp]),
+            "orc_last_error": (C.c_char_p, []),
+            "orc_add_harmonic_repulsion": (i, [vp, i, i, d, d]),
+            "orc_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
+            "orc_add_lennard_jones": (i, [vp, i, i, C.c_uint, C.c_uint, d, i, d, d]),
+            "orc_add_screened_electrostatics": (i, [vp, i, i, d, d, d, d, C.c_uint, d]),
+            "orc_add_conversion": (i, [vp, i, i, d]),
+            "orc_add_decay": (i, [vp, i, d]),
+            "orc_add_fusion": (i, [vp, i, i, i, d, d, d, d]),
+            "orc_add_fission": (i, [vp, i, i, i, d, d, d, d]),
+            "orc_add_enzymatic": (i, [vp, i, i, i, d, d]),
+            "orc_add_harmonic_bonds": (i, [vp, i, P(i), P(d), P(d)]),
+            "orc_add_harmonic_angles": (i, [vp, i, P(i), P(d), P(d)]),
+            "orc_add_cosine_dihedrals": (i, [vp, i, P(i), P(d), P(d), P(d)]),
+            "orc_add_particles": (i, [vp, i, P(d), P(i)]),
+            "orc_n_particles": (i, [vp]),
+            "orc_n_entries": (i, [vp]),
+            "orc_get_particles": (i, [vp, P(d), P(i), P(u64), P(d), P(i)]),
+            "orc_calculate_max_cutoff": (d, [vp]),
+            "orc_nl_setup": (i, [vp, d]),
+            "orc_nl_update": (i, [vp]),
+            "orc_nl_pairs": (i64, [vp, d, i64, P(u64)]),
+            "orc_brute_force_pairs": (i64, [vp, d, i64, P(u64)]),
+            "orc_calculate_forces": (d, [vp]),
+            "orc_energy": (d, [vp]),
+            "orc_euler_bd": (i, [vp, d]),
+            "orc_uncontrolled_approximation": (i, [vp, d]),
+            "orc_gillespie": (i, [vp, d]),
+            "orc_run": (i, [vp, i64, d, i, i, P(i64), i64]),
+            "orc_reaction_counts": (i, [vp, P(i64), i]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return lib
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class OracleSystem:
+    """One FP64 CPU system with the reference's CPU-kernel semantics."""
+
+    def __init__(self, box, periodic=(True, True, True), kbt=1.0, diffusion=(1.0,), seed=0,
+                 n_threads=1, cll_radius=1):
+        self._lib = _load()
+        b = np.ascontiguousarray(box, dtype=np.float64)
+        p = np.ascontiguousarray([int(bool(x)) for x in periodic], dtype=np.int32)
+        D = np.ascontiguousarray(diffusion, dtype=np.float64)
+        self.n_types = len(D)
+        self._h = self._lib.orc_create(_ptr(b, C.c_double), _ptr(p, C.c_int), float(kbt), self.n_types,
+                                       _ptr(D, C.c_double), int(seed) & (2**64 - 1), int(n_threads),
+                                       int(cll_radius))
+        if not self._h:
+            raise ValueError(self._lib.orc_last_error().decode())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.orc_destroy(h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc < 0:
+            raise RuntimeError(self._lib.orc_last_error().decode())
+        return rc
+
+    # potentials
+    def add_harmonic_repulsion(self, t1, t2, k, d):
+        return self._check(self._lib.orc_add_harmonic_repulsion(self._h, t1, t2, k, d))
+
+    def add_weak_interaction_piecewise_harmonic(self, t1, t2, k, desired, depth, cutoff):
+        return self._check(self._lib.orc_add_weak_interaction_piecewise_harmonic(self._h, t1, t2, k, desired,
+                                                                                 depth, cutoff))
+
+    def add_lennard_jones(self, t1, t2, m, n, cutoff, shift, epsilon, sigma):
+        return self._check(self._lib.orc_add_lennard_jones(self._h, t1, t2, m, n, cutoff, int(shift),
+                                                           epsilon, sigma))
+
+    def add_screened_electrostatics(self, t1, t2, C_, kappa, D_, sigma, exponent, cutoff):
+        return self._check(self._lib.orc_add_screened_electrostatics(self._h, t1, t2, C_, kappa, D_, sigma,
+                                                                     exponent, cutoff))
+
+    # reactions
+    def add_conversion(self, a, b, rate):
+        return self._check(self._lib.orc_add_conversion(self._h, a, b, rate))
+
+    def add_decay(self, a, rate):
+        return self._check(self._lib.orc_add_decay(self._h, a, rate))
+
+    def add_fusion(self, a, b, c, rate, educt_distance, w1=0.5, w2=0.5):
+        return self._check(self._lib.orc_add_fusion(self._h, a, b, c, rate, educt_distance, w1, w2))
+
+    def add_fission(self, a, b, c, rate, product_distance, w1=0.5, w2=0.5):
+        return self._check(self._lib.orc_add_fission(self._h, a, b, c, rate, product_distance, w1, w2))
+
+    def add_enzymatic(self, catalyst, a, b, rate, educt_distance):
+        return self._check(self._lib.orc_add_enzymatic(self._h, catalyst, a, b, rate, educt_distance))
+
+    # bonded
+    def add_harmonic_bonds(self, idx, k, l0):
+        idx = np.ascontiguousarray(idx, dtype=np.int32).reshape(-1, 2)
+        n = len(idx)
+        k = np.ascontiguousarray(np.broadcast_to(k, (n,)), dtype=np.float64)
+        l0 = np.ascontiguousarray(np.broadcast_to(l0, (n,)), dtype=np.float64)
+        return self._check(self._lib.orc_add_harmonic_bonds(self._h, n, _ptr(idx, C.c_int), _ptr(k, C.c_double),
+                                                            _ptr(l0, C.c_double)))
+
+    def add_harmonic_angles(self, idx, k, theta0):
+        idx = np.ascontiguousarray(idx, dtype=np.int32).reshape(-1, 3)
+        n = len(idx)
+        k = np.ascontiguousarray(np.broadcast_to(k, (n,)), dtype=np.float64)
+        t = np.ascontiguousarray(np.broadcast_to(theta0, (n,)), dtype=np.float64)
+        return self._check(self._lib.orc_add_harmonic_angles(self._h, n, _ptr(idx, C.c_int), _ptr(k, C.c_double),
+                                                             _ptr(t, C.c_double)))
+
+    def add_cosine_dihedrals(self, idx, k, multiplicity, phi0):
+        idx = np.ascontiguousarray(idx, dtype=np.int32).reshape(-1, 4)
+        n = len(idx)
+        k = np.ascontiguousarray(np.broadcast_to(k, (n,)), dtype=np.float64)
+        m = np.ascontiguousarray(np.broadcast_to(multiplicity, (n,)), dtype=np.float64)
+        p = np.ascontiguousarray(np.broadcast_to(phi0, (n,)), dtype=np.float64)
+        return self._check(self._lib.orc_add_cosine_dihedrals(self._h, n, _ptr(idx, C.c_int), _ptr(k, C.c_double),
+                                                              _ptr(m, C.c_double), _ptr(p, C.c_double)))
+
+    # particles
+    def add_particles(self, positions, types):
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(np.broadcast_to(types, (len(pos),)), dtype=np.int32)
+        return self._check(self._lib.orc_add_particles(self._h, len(pos), _ptr(pos, C.c_double),
+                                                       _ptr(t, C.c_int)))
+
+    @property
+    def n_particles(self):
+        return self._lib.orc_n_particles(self._h)
+
+    def particles(self):
+        """(positions[n,3], types[n], ids[n], forces[n,3], storage_index[n]) of active particles."""
+        n = self.n_particles
+        pos = np.zeros((n, 3)); f = np.zeros((n, 3))
+        t = np.zeros(n, np.int32); ids = np.zeros(n, np.uint64); si = np.zeros(n, np.int32)
+        self._lib.orc_get_particles(self._h, _ptr(pos, C.c_double), _ptr(t, C.c_int), _ptr(ids, C.c_uint64),
+                                    _ptr(f, C.c_double), _ptr(si, C.c_int))
+        return pos, t, ids, f, si
+
+    def calculate_max_cutoff(self):
+        return self._lib.orc_calculate_max_cutoff(self._h)
+
+    def nl_setup(self, cutoff):
+        return self._check(self._lib.orc_nl_setup(self._h, cutoff))
+
+    def nl_update(self):
+        return self._check(self._lib.orc_nl_update(self._h))
+
+    def _pairs(self, fn, cutoff):
+        cap = max(1024, 64 * self.n_particles)
+        while True:
+            out = np.zeros((cap, 2), np.uint64)
+            n = fn(self._h, cutoff, cap, _ptr(out, C.c_uint64))
+            if n >= 0:
+                return out[:n].copy()
+            cap *= 4
+
+    def nl_pairs(self, cutoff):
+        return self._pairs(self._lib.orc_nl_pairs, cutoff)
+
+    def brute_force_pairs(self, cutoff):
+        return self._pairs(self._lib.orc_brute_force_pairs, cutoff)
+
+    def calculate_forces(self):
+        e = self._lib.orc_calculate_forces(self._h)
+        if e != e:
+            err = self._lib.orc_last_error().decode()
+            if err:
+                raise RuntimeError(err)
+        return e
+
+    @property
+    def energy(self):
+        return self._lib.orc_energy(self._h)
+
+    def euler_bd(self, dt):
+        return self._check(self._lib.orc_euler_bd(self._h, dt))
+
+    def uncontrolled_approximation(self, dt):
+        return self._check(self._lib.orc_uncontrolled_approximation(self._h, dt))
+
+    def gillespie(self, dt):
+        return self._check(self._lib.orc_gillespie(self._h, dt))
+
+    def run(self, n_steps, dt, handler=UNCONTROLLED_APPROXIMATION, count_stride=0):
+        """SimulationLoop::run; returns per-type counts every count_stride steps (incl. t=0)."""
+        nrec = (n_steps // count_stride + 1) if count_stride > 0 else 0
+        counts = np.zeros((max(nrec, 1), self.n_types), np.int64)
+        r = self._check(self._lib.orc_run(self._h, n_steps, dt, handler, count_stride,
+                                          _ptr(counts, C.c_int64), nrec))
+        return counts[:r]
+
+    def reaction_counts(self, n):
+        out = np.zeros(n, np.int64)
+        k = self._lib.orc_reaction_counts(self._h, _ptr(out, C.c_int64), n)
+        return out[:k]

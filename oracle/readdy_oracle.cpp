@@ -1,0 +1,1114 @@
+/*
+ * TEST INFRASTRUCTURE ONLY -- not part of the product.
+ *
+ * FP64 CPU restatement of the ReaDDy CPU-kernel hot path.  It is the checker that the CUDA path is
+ * compared against (tests/, __graft_entry__.smoke(), and the timed cpu_baseline leg of bench.py).
+ * Every function names the reference file:line whose behaviour it restates.  Paths are relative to
+ * the readdy/readdy project root.
+ *
+ * Differences from the reference, all deliberate and limited to what cannot be reproduced:
+ *   - random numbers come from seeded std::mt19937_64 streams (one per worker thread) instead of
+ *     the unseedable thread_local generators of include/readdy/model/RandomProvider.h:55-97;
+ *   - the serial cell-list fill is used (CellLinkedList.cpp:171-184) so that iteration order is
+ *     reproducible; the parallel CAS fill (:186-228) builds the same cell membership;
+ *   - particle ids come from a per-system counter instead of the process-global one
+ *     (include/readdy/model/Particle.h:112-114).
+ * Build with -ffp-contract=off so that x86-64 and aarch64 round identically.
+ */
+#include "readdy_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <utility>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+
+struct V3 {
+    double x = 0, y = 0, z = 0;
+    double &operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+    double operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator*(double s, V3 a) { return {a.x * s, a.y * s, a.z * s}; }
+inline V3 operator*(V3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline V3 operator/(V3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+inline V3 &operator+=(V3 &a, V3 b) { a.x += b.x; a.y += b.y; a.z += b.z; return a; }
+inline V3 &operator-=(V3 &a, V3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; return a; }
+/* dot product with the accumulation order of std::inner_product (ReaDDyVec3.h:332-334) */
+inline double dot(V3 a, V3 b) { double r = 0; r += a.x * b.x; r += a.y * b.y; r += a.z * b.z; return r; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double norm(V3 a) { return std::sqrt(dot(a, a)); }
+
+/* include/readdy/common/boundary_condition_operations.h:53-80 */
+struct Box {
+    double L[3];
+    bool pbc[3];
+    void fix(V3 &v) const {
+        for (int d = 0; d < 3; ++d) {
+            if (pbc[d]) {
+                while (v[d] >= .5 * L[d]) v[d] -= L[d];
+                while (v[d] < -.5 * L[d]) v[d] += L[d];
+            }
+        }
+    }
+    V3 apply(V3 v) const { fix(v); return v; }
+    V3 shortest(V3 lhs, V3 rhs) const {
+        V3 dv = rhs - lhs;
+        for (int i = 0; i < 3; ++i) {
+            if (pbc[i]) {
+                if (dv[i] > L[i] * .5) dv[i] -= L[i];
+                else if (dv[i] <= -L[i] * .5) dv[i] += L[i];
+            }
+        }
+        return dv;
+    }
+    double dist2(V3 lhs, V3 rhs) const { V3 d = shortest(lhs, rhs); return dot(d, d); }
+};
+
+enum PotKind { HARMONIC_REPULSION = 0, WEAK_PIECEWISE_HARMONIC = 1, LENNARD_JONES = 2, SCREENED_ELECTROSTATICS = 3 };
+
+struct Pot2 {
+    int kind;
+    double p[8];
+    double cutoff2;
+
+    /* include/readdy/model/potentials/PotentialsOrder2.h, one branch per potential class */
+    double energy(V3 x) const {
+        switch (kind) {
+            case HARMONIC_REPULSION: {  // :73-82
+                double k = p[0], d = p[1], d2 = p[2];
+                double s = dot(x, x);
+                if (s < d2) {
+                    s = std::sqrt(s);
+                    s -= d;
+                    s *= s;
+                    return 0.5 * s * k;
+                }
+                return 0;
+            }
+            case WEAK_PIECEWISE_HARMONIC: {  // :131-154
+                double k = p[0], d0 = p[1], depth = p[2], rc = p[3];
+                const double dist = std::sqrt(dot(x, x));
+                const double len2 = rc - d0;
+                if (dist < d0) return .5 * k * (dist - d0) * (dist - d0) - depth;
+                if (dist < d0 + .5 * len2)
+                    return .5 * depth * (1. / (.5 * len2)) * (1. / (.5 * len2)) * (dist - d0) * (dist - d0) - depth;
+                if (dist < rc) return -.5 * depth * (1. / (.5 * len2)) * (1. / (.5 * len2)) * (dist - rc) * (dist - rc);
+                return 0;
+            }
+            case LENNARD_JONES: {  // :240-244, 262-264
+                double m = p[0], n = p[1], rc = p[2], shift = p[3], sigma = p[5], kk = p[6];
+                const double r = norm(x);
+                if (r > rc) return 0;
+                auto e = [&](double rr) { return kk * (std::pow(sigma / rr, m) - std::pow(sigma / rr, n)); };
+                return shift != 0 ? e(r) - e(rc) : e(r);
+            }
+            case SCREENED_ELECTROSTATICS: {  // :291-296
+                double C = p[0], kappa = p[1], D = p[2], sigma = p[3], ex = p[4];
+                const double r = norm(x);
+                double res = C * std::exp(-kappa * r) / r;
+                res += D * std::pow(sigma / r, ex);
+                return res;
+            }
+        }
+        return 0;
+    }
+
+    void force(V3 &f, V3 x) const {
+        switch (kind) {
+            case HARMONIC_REPULSION: {  // :84-91
+                double k = p[0], d = p[1], d2 = p[2];
+                double s = dot(x, x);
+                if (s < d2 && s > 0) {
+                    s = std::sqrt(s);
+                    f += ((k * (s - d)) / s) * x;
+                }
+                return;
+            }
+            case WEAK_PIECEWISE_HARMONIC: {  // :156-183
+                double k = p[0], d0 = p[1], depth = p[2], rc = p[3];
+                const double dist = std::sqrt(dot(x, x));
+                const double len2 = rc - d0;
+                double factor = 0;
+                if (dist < d0) {
+                    factor = -1 * k * (d0 - dist);
+                } else if (dist < d0 + .5 * len2) {
+                    factor = -1. * depth * (1. / (.5 * len2)) * (1. / (.5 * len2)) * (d0 - dist);
+                } else if (dist < rc) {
+                    factor = depth * (1. / (.5 * len2)) * (1. / (.5 * len2)) * (rc - dist);
+                }
+                if (dist > 0 && factor != 0) f += (factor * x) / dist;
+                return;
+            }
+            case LENNARD_JONES: {  // :246-253
+                double m = p[0], n = p[1], rc = p[2], sigma = p[5], kk = p[6];
+                const double r = norm(x);
+                if (r <= rc) {
+                    double s = -1. * kk * (1 / (sigma * sigma)) *
+                               (m * std::pow(sigma / r, m + 2) - n * std::pow(sigma / r, n + 2));
+                    f += s * x;
+                }
+                return;
+            }
+            case SCREENED_ELECTROSTATICS: {  // :298-305
+                double C = p[0], kappa = p[1], D = p[2], sigma = p[3], ex = p[4];
+                double r = norm(x);
+                double ff = C * std::exp(-kappa * r);
+                ff *= (kappa / r + 1. / std::pow(r, 2.));
+                ff += D * ex / sigma * std::pow(sigma / r, ex + 1.);
+                f += ff * ((-1. * x) / r);
+                return;
+            }
+        }
+    }
+};
+
+enum ReactionKind { CONVERSION = 0, FUSION = 1, FISSION = 2, ENZYMATIC = 3, DECAY = 4 };
+
+struct Reaction {
+    int kind, id;
+    int educts[2] = {0, 0}, products[2] = {0, 0};
+    int nEducts, nProducts;
+    double rate, eductDistance = 0, eductDistance2 = 0, productDistance = 0, w1 = .5, w2 = .5;
+};
+
+struct Entry {
+    V3 pos, force;
+    uint64_t id = 0;
+    int type = 0;
+    bool deactivated = false;
+};
+
+struct Event {  // kernels/cpu .. reactions/Event.h:51-67
+    int nEducts, nProducts;
+    size_t idx1, idx2;
+    size_t reactionIndex;
+    int t1, t2;
+    double rate, cumulativeRate;
+};
+
+struct Bond { size_t i, j; double k, l0; };
+struct Angle { size_t i, j, k; double kf, theta0; };
+struct Dihedral { size_t i, j, k, l; double kf, mult, phi0; };
+
+/* a small fork/join pool standing in for ctpl::thread_pool (include/readdy/common/thread/ctpl.h) */
+class Pool {
+public:
+    explicit Pool(int n) : n_(std::max(1, n)) {
+        for (int t = 1; t < n_; ++t) workers_.emplace_back([this, t] { loop(t); });
+    }
+    ~Pool() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto &w : workers_) w.join();
+    }
+    int size() const { return n_; }
+    /* runs fn(tid) on every thread, tid 0 on the caller, and joins */
+    void run(const std::function<void(int)> &fn) {
+        if (n_ == 1) { fn(0); return; }
+        {
+            std::lock_guard<std::mutex> g(m_);
+            job_ = &fn;
+            pending_ = n_ - 1;
+            ++gen_;
+        }
+        cv_.notify_all();
+        fn(0);
+        std::unique_lock<std::mutex> l(m_);
+        done_.wait(l, [this] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    void loop(int tid) {
+        uint64_t seen = 0;
+        for (;;) {
+            const std::function<void(int)> *job;
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+                job = job_;
+            }
+            (*job)(tid);
+            {
+                std::lock_guard<std::mutex> g(m_);
+                if (--pending_ == 0) done_.notify_one();
+            }
+        }
+    }
+    int n_;
+    std::vector<std::thread> workers_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *job_ = nullptr;
+    int pending_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
+inline std::pair<size_t, size_t> chunk(size_t n, int parts, int t) {
+    size_t g = n / parts;
+    size_t b = g * t, e = (t == parts - 1) ? n : b + g;
+    return {b, e};
+}
+
+}  // namespace
+
+struct orc_system {
+    Box box;
+    double kbt;
+    std::vector<double> D;
+    int nTypes;
+    std::map<std::pair<int, int>, std::vector<Pot2>> pot2;          // symmetric key (min,max)
+    std::vector<std::vector<const Reaction *>> o1;                 // by type
+    std::map<std::pair<int, int>, std::vector<const Reaction *>> o2;  // symmetric key
+    std::vector<Reaction *> reactions;
+    std::vector<int64_t> reactionCounts;
+    std::vector<Bond> bonds;
+    std::vector<Angle> angles;
+    std::vector<Dihedral> dihedrals;
+
+    std::vector<Entry> entries;
+    std::vector<size_t> blanks;
+    uint64_t nextId = 0;
+    double energy = 0;
+
+    // CompactCellLinkedList (CellLinkedList.cpp)
+    int radius;
+    bool nlSetUp = false;
+    double nlCutoff = 0;
+    size_t dims[3] = {1, 1, 1};
+    double cellSize[3] = {1, 1, 1};
+    std::vector<std::vector<size_t>> adjacency;
+    std::vector<size_t> head, list;
+
+    Pool pool;
+    std::vector<std::mt19937_64> rng;
+
+    orc_system(const double b[3], const int p[3], double kbt_, int nt, const double *diff, uint64_t seed, int nthreads,
+               int r)
+        : kbt(kbt_), nTypes(nt), radius(r), pool(nthreads) {
+        for (int d = 0; d < 3; ++d) { box.L[d] = b[d]; box.pbc[d] = p[d] != 0; }
+        D.assign(diff, diff + nt);
+        o1.resize(nt);
+        std::seed_seq ss{(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32), 0x5eedu};
+        std::vector<uint32_t> seeds(pool.size());
+        ss.generate(seeds.begin(), seeds.end());
+        for (int t = 0; t < pool.size(); ++t) rng.emplace_back(seeds[t] ^ (uint64_t(t) << 32));
+    }
+    ~orc_system() { for (auto r : reactions) delete r; }
+
+    static std::pair<int, int> key(int a, int b) { return {std::min(a, b), std::max(a, b)}; }
+
+    const std::vector<Pot2> *pots(int a, int b) const {
+        auto it = pot2.find(key(a, b));
+        return it == pot2.end() ? nullptr : &it->second;
+    }
+    const std::vector<const Reaction *> *reac2(int a, int b) const {
+        auto it = o2.find(key(a, b));
+        return it == o2.end() ? nullptr : &it->second;
+    }
+
+    double normal(int tid) { std::normal_distribution<double> nd(0., 1.); return nd(rng[tid]); }
+    V3 normal3(int tid) { V3 v; v.x = normal(tid); v.y = normal(tid); v.z = normal(tid); return v; }
+    double uniform(int tid, double a = 0., double b = 1.) {
+        std::uniform_real_distribution<double> u(a, b);
+        return u(rng[tid]);
+    }
+
+    /* Context::calculateMaxCutoff, readdy/main/model/Context.cpp:126-144 */
+    double maxCutoff() const {
+        double c = 0;
+        for (auto &e : pot2) for (auto &p : e.second) c = std::max(c, std::sqrt(p.cutoff2));
+        for (auto &e : o2) for (auto *r : e.second) c = std::max(c, r->eductDistance);
+        return c;
+    }
+
+    /* DefaultDataContainer::addParticles / addEntry, DefaultDataContainer.h:79-101 */
+    size_t addEntry(const Entry &e) {
+        if (!blanks.empty()) {
+            size_t idx = blanks.back();
+            blanks.pop_back();
+            entries.at(idx) = e;
+            return idx;
+        }
+        entries.push_back(e);
+        return entries.size() - 1;
+    }
+    void removeEntry(size_t idx) {  // DataContainer.h:149-157
+        auto &e = entries.at(idx);
+        if (!e.deactivated) { e.deactivated = true; blanks.push_back(idx); }
+    }
+
+    /* CellLinkedList::setUp, kernels/cpu/src/nl/CellLinkedList.cpp:52-142 */
+    void nlSetup(double cutoff) {
+        if (cutoff <= 0) throw std::logic_error("The cutoff distance for setting up a neighbor list must be > 0");
+        nlCutoff = cutoff;
+        double width = cutoff / static_cast<double>(radius);
+        for (int i = 0; i < 3; ++i) {
+            dims[i] = static_cast<unsigned int>(std::max(1., std::floor(box.L[i] / width)));
+            cellSize[i] = box.L[i] / static_cast<double>(dims[i]);
+        }
+        size_t nCells = dims[0] * dims[1] * dims[2];
+        adjacency.assign(nCells, {});
+        int r = radius;
+        for (int i = 0; i < (int)dims[0]; ++i)
+            for (int j = 0; j < (int)dims[1]; ++j)
+                for (int k = 0; k < (int)dims[2]; ++k) {
+                    size_t self = cellIndex(i, j, k);
+                    std::vector<size_t> adj;
+                    for (int ii = i - r; ii <= i + r; ++ii)
+                        for (int jj = j - r; jj <= j + r; ++jj)
+                            for (int kk = k - r; kk <= k + r; ++kk) {
+                                if (ii == i && jj == j && kk == k) continue;
+                                int a[3] = {ii, jj, kk};
+                                bool ok = true;
+                                for (int d = 0; d < 3; ++d) {
+                                    int c = (int)dims[d];
+                                    if (box.pbc[d]) a[d] = (a[d] % c + c) % c;
+                                    if (a[d] < 0 || a[d] >= c) ok = false;
+                                }
+                                if (ok) adj.push_back(cellIndex(a[0], a[1], a[2]));
+                            }
+                    std::sort(adj.begin(), adj.end());
+                    adj.erase(std::unique(adj.begin(), adj.end()), adj.end());
+                    adj.erase(std::remove(adj.begin(), adj.end(), self), adj.end());
+                    adjacency[self] = std::move(adj);
+                }
+        nlSetUp = true;
+        nlUpdate();
+    }
+    /* row-major Index3D, include/readdy/common/Index.h:130-141 */
+    size_t cellIndex(size_t i, size_t j, size_t k) const { return k + dims[2] * (j + dims[1] * i); }
+
+    /* CompactCellLinkedList::setUpBins + fillBins<true>, CellLinkedList.cpp:161-184, 230-247 */
+    void nlUpdate() {
+        if (!nlSetUp) throw std::logic_error("Attempting to fill neighborlist bins, but cell structure is not set up yet");
+        head.assign(adjacency.size(), 0);
+        list.assign(entries.size() + 1, 0);
+        size_t pidx = 1;
+        for (const auto &e : entries) {
+            const V3 &p = e.pos;
+            bool inBox = -.5 * box.L[0] <= p.x && .5 * box.L[0] > p.x && -.5 * box.L[1] <= p.y &&
+                         .5 * box.L[1] > p.y && -.5 * box.L[2] <= p.z && .5 * box.L[2] > p.z;
+            if (!e.deactivated && inBox) {
+                auto i = static_cast<size_t>(std::floor((p.x + .5 * box.L[0]) / cellSize[0]));
+                auto j = static_cast<size_t>(std::floor((p.y + .5 * box.L[1]) / cellSize[1]));
+                auto k = static_cast<size_t>(std::floor((p.z + .5 * box.L[2]) / cellSize[2]));
+                size_t c = cellIndex(i, j, k);
+                list[pidx] = head.at(c);
+                head[c] = pidx;
+            }
+            ++pidx;
+        }
+    }
+    template <typename F>
+    void forEachInCell(size_t cell, F f) const {
+        for (size_t s = head[cell]; s != 0; s = list[s]) f(s - 1);
+    }
+    /* CompactCellLinkedList::forEachNeighbor, CellLinkedList.h:304-313 */
+    template <typename F>
+    void forEachNeighbor(size_t particle, size_t cell, F f) const {
+        forEachInCell(cell, [&](size_t x) { if (x != particle) f(x); });
+        for (size_t nc : adjacency[cell]) forEachInCell(nc, f);
+    }
+
+    /* CPUCalculateForces::perform, kernels/cpu/src/actions/CPUCalculateForces.cpp:46-212 */
+    double calculateForces() {
+        energy = 0;
+        if (pot2.empty() && bonds.empty() && angles.empty() && dihedrals.empty()) return 0;
+        for (auto &e : entries) e.force = {0, 0, 0};
+        int nt = pool.size();
+        std::vector<double> part(nt, 0.);
+        if (!bonds.empty() || !angles.empty() || !dihedrals.empty()) energy += bondedForces();
+        if (!pot2.empty()) {
+            if (!nlSetUp) throw std::logic_error("neighbor list not set up");
+            size_t nCells = adjacency.size();
+            pool.run([&](int tid) {
+                auto [cb, ce] = chunk(nCells, nt, tid);
+                part[tid] = order2(cb, ce);
+            });
+            for (double p : part) energy += p;
+        }
+        return energy;
+    }
+    /* calculateOrder2<false>, CPUCalculateForces.cpp:214-268 */
+    double order2(size_t cb, size_t ce) {
+        double eUpd = 0;
+        for (size_t cell = cb; cell < ce; ++cell) {
+            forEachInCell(cell, [&](size_t pi) {
+                Entry &entry = entries[pi];
+                if (entry.deactivated) return;
+                forEachNeighbor(pi, cell, [&](size_t ni) {
+                    const Entry &nb = entries[ni];
+                    if (nb.deactivated) return;
+                    double myE = 0;
+                    const auto *ps = pots(entry.type, nb.type);
+                    if (ps) {
+                        V3 xij = box.shortest(entry.pos, nb.pos);
+                        double d2 = dot(xij, xij);
+                        for (const auto &pot : *ps) {
+                            if (d2 < pot.cutoff2) {
+                                V3 upd{0, 0, 0};
+                                myE += pot.energy(xij);
+                                pot.force(upd, xij);
+                                entry.force += upd;
+                            }
+                        }
+                    }
+                    eUpd += 0.5 * myE;
+                });
+            });
+        }
+        return eUpd;
+    }
+
+    /* bonded terms, kernels/cpu/src/actions/topologies/CPUTopologyActions.cpp:55-123 */
+    double bondedForces() {
+        double e = 0;
+        for (const auto &b : bonds) {  // :61-74, BondedPotential.h:105-113
+            if (b.k == 0) continue;
+            Entry &e1 = entries.at(b.i), &e2 = entries.at(b.j);
+            V3 xij = box.shortest(e1.pos, e2.pos);
+            const double nrm = norm(xij);
+            V3 upd = (2. * b.k * (nrm - b.l0) / nrm) * xij;
+            e1.force += upd;
+            e2.force -= upd;
+            const double n2 = std::sqrt(dot(xij, xij));
+            e += b.k * (n2 - b.l0) * (n2 - b.l0);
+        }
+        for (const auto &a : angles) {  // :82-97, AnglePotential.cpp:58-104
+            Entry &e1 = entries.at(a.i), &e2 = entries.at(a.j), &e3 = entries.at(a.k);
+            V3 xji = box.shortest(e2.pos, e1.pos);
+            V3 xjk = box.shortest(e2.pos, e3.pos);
+            e += angleEnergy(xji, xjk, a);
+            angleForce(e1.force, e2.force, e3.force, xji, xjk, a);
+        }
+        for (const auto &d : dihedrals) {  // :106-123, TorsionPotential.cpp:53-159
+            Entry &ei = entries.at(d.i), &ej = entries.at(d.j), &ek = entries.at(d.k), &el = entries.at(d.l);
+            V3 xji = box.shortest(ej.pos, ei.pos);
+            V3 xkj = box.shortest(ek.pos, ej.pos);
+            V3 xkl = box.shortest(ek.pos, el.pos);
+            e += dihedralEnergy(xji, xkj, xkl, d);
+            dihedralForce(ei.force, ej.force, ek.force, el.force, xji, xkj, xkl, d);
+        }
+        return e;
+    }
+
+    static double angleEnergy(V3 xij, V3 xkj, const Angle &a) {  // AnglePotential.cpp:58-65
+        const double sp = dot(xij, xkj);
+        const double th = std::acos(sp / (norm(xij) * norm(xkj)));
+        return a.kf * (th - a.theta0) * (th - a.theta0);
+    }
+    static void angleForce(V3 &fi, V3 &fj, V3 &fk, V3 xji, V3 xjk, const Angle &a) {  // :67-102
+        const double SMALL = 1e-10;
+        const double sp = dot(xji, xjk);
+        double nji2 = dot(xji, xji);
+        if (nji2 < SMALL) nji2 = SMALL;
+        const double nji = std::sqrt(nji2);
+        double njk2 = dot(xjk, xjk);
+        if (njk2 < SMALL) njk2 = SMALL;
+        const double njk = std::sqrt(njk2);
+        double np = nji * njk;
+        if (np < SMALL) np = SMALL;
+        const double inp = 1. / np;
+        double c = inp * sp;
+        c = std::min(1., std::max(-1., c));
+        double sinv = std::sqrt(1. - c * c);
+        if (sinv < SMALL) sinv = SMALL;
+        sinv = 1. / sinv;
+        const double cc = 2. * a.kf * (std::acos(c) - a.theta0) * sinv;
+        const V3 f_i = cc * c * (1. / nji2) * xji - cc * inp * xjk;
+        const V3 f_k = -cc * inp * xji + cc * c * (1. / njk2) * xjk;
+        fi -= f_i;
+        fj += f_i + f_k;
+        fk -= f_k;
+    }
+
+    static double dihedralEnergy(V3 xji, V3 xkj, V3 xkl, const Dihedral &d) {  // TorsionPotential.cpp:53-68
+        const double SMALL = .0001;
+        const V3 xjk = -1. * xkj;
+        double xjkn = norm(xjk);
+        xjkn = xjkn < SMALL ? SMALL : xjkn;
+        const V3 m = cross(xji, xkj);
+        const double mn = norm(m);
+        const V3 n = cross(xkl, xjk);
+        const double nn = norm(n);
+        double mnn = mn * nn;
+        mnn = mnn < SMALL ? SMALL : mnn;
+        const double sinT = dot(cross(m, n), xjk) / (mnn * xjkn);
+        const double cosT = dot(m, n) / mnn;
+        const double dih = -std::atan2(sinT, cosT);
+        return d.kf * (1 + std::cos(d.mult * dih - d.phi0));
+    }
+
+    /* 3x3 "tensor" of three column vectors, include/readdy/common/Vec3Tensor.h */
+    struct T3 { V3 c[3]; };
+    static T3 skew(V3 v) {  // the columns written at TorsionPotential.cpp:111-112
+        return T3{{V3{0, -v[2], v[1]}, V3{v[2], 0, -v[0]}, V3{-v[1], v[0], 0}}};
+    }
+    static T3 add(T3 a, T3 b) { return T3{{a.c[0] + b.c[0], a.c[1] + b.c[1], a.c[2] + b.c[2]}}; }
+    static T3 scale(T3 a, double s) { return T3{{a.c[0] * s, a.c[1] * s, a.c[2] * s}}; }
+    static V3 vecT(V3 v, T3 t) { return {dot(t.c[0], v), dot(t.c[1], v), dot(t.c[2], v)}; }  // Vec3 * Tensor
+
+    static void dihedralForce(V3 &fi, V3 &fj, V3 &fk, V3 &fl, V3 xji, V3 xkj, V3 xkl,
+                              const Dihedral &dh) {  // TorsionPotential.cpp:70-153
+        const double SMALL = .0001;
+        const V3 xjk = -1. * xkj;
+        double xjkn2 = dot(xjk, xjk);
+        xjkn2 = xjkn2 < SMALL ? SMALL : xjkn2;
+        const double xjkn = std::sqrt(xjkn2);
+        const V3 m = cross(xji, xkj);
+        double mn2 = dot(m, m);
+        mn2 = mn2 < SMALL ? SMALL : mn2;
+        const double mn = std::sqrt(mn2);
+        const V3 n = cross(xkl, xjk);
+        double nn2 = dot(n, n);
+        nn2 = nn2 < SMALL ? SMALL : nn2;
+        const double nn = std::sqrt(nn2);
+        double nmn = mn * nn;
+        nmn = nmn < SMALL ? SMALL : nmn;
+        const V3 mxn = cross(m, n);
+        const double n_m = dot(n, m);
+        const double cphi = n_m / nmn;
+        if (std::abs(cphi) < SMALL) return;
+        const double sphi = dot(cross(m, n), xjk) / (nmn * xjkn);
+        const double phi = -std::atan2(sphi, cphi);
+        const double dVdphi = -dh.kf * dh.mult * std::sin(dh.mult * phi - dh.phi0);
+        const V3 dmn2_dxi = 2 * xjkn2 * xji - 2 * dot(xji, xkj) * xkj;
+        const V3 dmn_dxi = dmn2_dxi / (2 * mn);
+        const V3 dmn2_dxk = -2 * dot(xji, xji) * xkj + 2 * dot(xji, xkj) * xji;
+        const V3 dmn_dxk = dmn2_dxk / (2 * mn);
+        const V3 dmn2_dxj = -1. * (dmn2_dxi + dmn2_dxk);
+        const V3 dmn_dxj = dmn2_dxj / (2 * mn);
+        const V3 dnn2_dxl = 2 * xjkn2 * xkl - 2 * dot(xkl, xjk) * xjk;
+        const V3 dnn_dxl = dnn2_dxl / (2 * nn);
+        const V3 dnn2_dxj = -2 * dot(xkl, xkl) * xjk + 2 * dot(xkl, xjk) * xkl;
+        const V3 dnn_dxj = dnn2_dxj / (2 * nn);
+        const V3 dnn2_dxk = -1. * (dnn2_dxl + dnn2_dxj);
+        const V3 dnn_dxk = dnn2_dxk / (2 * nn);
+
+        const T3 dm_dxi = skew(xkj);
+        const T3 dm_dxk = skew(xji);
+        const T3 dm_dxj = scale(add(dm_dxk, dm_dxi), -1.);
+        const T3 dn_dxl = scale(dm_dxi, -1);
+        const T3 dn_dxj = skew(xkl);
+        const T3 dn_dxk = scale(add(dn_dxj, dn_dxl), -1);
+
+        const double cpre = 1. / nmn;
+        const V3 dc_dxi = cpre * (vecT(n, dm_dxi) - (cphi * nn) * dmn_dxi);
+        const V3 dc_dxj = cpre * (vecT(n, dm_dxj) + vecT(m, dn_dxj) - (cphi * nn) * dmn_dxj - (cphi * mn) * dnn_dxj);
+        const V3 dc_dxk = cpre * (vecT(n, dm_dxk) + vecT(m, dn_dxk) - (cphi * nn) * dmn_dxk - (cphi * mn) * dnn_dxk);
+        const V3 dc_dxl = cpre * (vecT(m, dn_dxl) - (cphi * mn) * dnn_dxl);
+
+        auto colCross = [](T3 t, V3 v) { return T3{{cross(t.c[0], v), cross(t.c[1], v), cross(t.c[2], v)}}; };
+        auto crossCol = [](V3 v, T3 t) { return T3{{cross(v, t.c[0]), cross(v, t.c[1]), cross(v, t.c[2])}}; };
+        const T3 dmxn_dxi = colCross(dm_dxi, n);
+        const T3 dmxn_dxj = add(colCross(dm_dxj, n), crossCol(m, dn_dxj));
+        const T3 dmxn_dxk = add(colCross(dm_dxk, n), crossCol(m, dn_dxk));
+        const T3 dmxn_dxl = crossCol(m, dn_dxl);
+
+        const double spre = 1. / (nmn * xjkn);
+        const V3 ds_dxi = spre * (vecT(xjk, dmxn_dxi) - (sphi * nn * xjkn) * dmn_dxi);
+        const V3 ds_dxj = spre * (vecT(xjk, dmxn_dxj) - 1. * mxn - (sphi * nn * xjkn) * dmn_dxj -
+                                  (sphi * mn * xjkn) * dnn_dxj + (sphi * nmn / xjkn) * xjk);
+        const V3 ds_dxk = spre * (vecT(xjk, dmxn_dxk) + mxn - (sphi * nn * xjkn) * dmn_dxk -
+                                  (sphi * mn * xjkn) * dnn_dxk - (sphi * nmn / xjkn) * xjk);
+        const V3 ds_dxl = spre * (vecT(xjk, dmxn_dxl) - (sphi * mn * xjkn) * dnn_dxl);
+
+        const double sbc = sphi / cphi;
+        const double ppre = -1. / (cphi * (1. + sbc * sbc));
+        const V3 dphi_dxi = ppre * (ds_dxi - sbc * dc_dxi);
+        const V3 dphi_dxj = ppre * (ds_dxj - sbc * dc_dxj);
+        const V3 dphi_dxk = ppre * (ds_dxk - sbc * dc_dxk);
+        const V3 dphi_dxl = ppre * (ds_dxl - sbc * dc_dxl);
+        fi += -dVdphi * dphi_dxi;
+        fj += -dVdphi * dphi_dxj;
+        fk += -dVdphi * dphi_dxk;
+        fl += -dVdphi * dphi_dxl;
+    }
+
+    /* CPUEulerBDIntegrator::perform, kernels/cpu/src/actions/CPUEulerBDIntegrator.cpp:51-103 */
+    void eulerBD(double dt) {
+        int nt = pool.size();
+        size_t n = entries.size();
+        pool.run([&](int tid) {
+            auto [b, e] = chunk(n, nt, tid);
+            for (size_t i = b; i < e; ++i) {
+                Entry &en = entries[i];
+                if (en.deactivated) continue;
+                const double Dt = D[en.type];
+                V3 rnd = normal3(tid);
+                V3 det = ((en.force * Dt) * dt) / kbt;
+                rnd = rnd * std::sqrt(2. * Dt * dt);
+                en.pos += rnd + det;
+                box.fix(en.pos);
+            }
+        });
+    }
+
+    /* performReactionEvent<false>, include/readdy/kernel/cpu/actions/reactions/ReactionUtils.h:64-71 */
+    bool coin(int tid, double rate, double dt) { return uniform(tid) < 1 - std::exp(-rate * dt); }
+
+    /* performReaction, ReactionUtils.h:146-227 */
+    void performReaction(size_t idx1, size_t idx2, const Reaction *r, std::vector<Entry> &newEntries,
+                         std::vector<size_t> &decayed) {
+        Entry &e1 = entries.at(idx1);
+        Entry &e2 = entries.at(idx2);
+        switch (r->kind) {
+            case DECAY: decayed.push_back(idx1); break;
+            case CONVERSION: e1.type = r->products[0]; e1.id = nextId++; break;
+            case ENZYMATIC:
+                if (e1.type == r->educts[1]) { e2.type = r->products[0]; e2.id = nextId++; }
+                else { e1.type = r->products[0]; e1.id = nextId++; }
+                break;
+            case FISSION: {
+                V3 n3 = normal3(0);
+                n3 = n3 / std::sqrt(dot(n3, n3));
+                Entry ne;
+                ne.pos = box.apply(e1.pos - (r->w2 * r->productDistance) * n3);
+                ne.type = r->products[1];
+                ne.id = nextId++;
+                newEntries.push_back(ne);
+                e1.type = r->products[0];
+                e1.id = nextId++;
+                e1.pos += (r->w1 * r->productDistance) * n3;   // DefaultDataContainer::displace :141-146
+                box.fix(e1.pos);
+                break;
+            }
+            case FUSION: {
+                V3 diff = box.shortest(e1.pos, e2.pos);
+                Entry ne;
+                ne.pos = box.apply(e1.pos + (r->educts[0] == e1.type ? r->w1 : r->w2) * diff);
+                ne.type = r->products[0];
+                ne.id = nextId++;
+                newEntries.push_back(ne);
+                decayed.push_back(idx1);
+                decayed.push_back(idx2);
+                break;
+            }
+        }
+        reactionCounts[r->id]++;
+    }
+
+    /* DefaultDataContainer::update, DefaultDataContainer.h:121-139 */
+    void commit(std::vector<Entry> &newEntries, std::vector<size_t> &decayed) {
+        auto it = decayed.begin();
+        for (auto &ne : newEntries) {
+            if (it != decayed.end()) { entries.at(*it) = ne; ++it; }
+            else addEntry(ne);
+        }
+        for (; it != decayed.end(); ++it) removeEntry(*it);
+    }
+
+    /* CPUUncontrolledApproximation::perform, kernels/cpu/src/actions/reactions/CPUUncontrolledApproximation.cpp:135-256 */
+    void uncontrolledApproximation(double dt) {
+        if (!nlSetUp) throw std::logic_error("neighbor list not set up");
+        int nt = pool.size();
+        std::vector<std::vector<Event>> parts(nt);
+        size_t n = entries.size(), nCells = adjacency.size();
+        pool.run([&](int tid) {  // findEvents :70-133
+            auto &ev = parts[tid];
+            auto [b, e] = chunk(n, nt, tid);
+            for (size_t i = b; i < e; ++i) {
+                const Entry &en = entries[i];
+                if (en.deactivated) continue;
+                const auto &rs = o1[en.type];
+                for (size_t ri = 0; ri < rs.size(); ++ri) {
+                    double rate = rs[ri]->rate;
+                    if (rate > 0 && coin(tid, rate, dt))
+                        ev.push_back(Event{1, rs[ri]->nProducts, i, i, ri, en.type, 0, rate, 0});
+                }
+            }
+            auto [cb, ce] = chunk(nCells, nt, tid);
+            for (size_t cell = cb; cell < ce; ++cell) {
+                forEachInCell(cell, [&](size_t pi) {
+                    const Entry &en = entries[pi];
+                    if (en.deactivated) return;
+                    forEachNeighbor(pi, cell, [&](size_t ni) {
+                        if (!(pi > ni)) return;
+                        const Entry &nb = entries[ni];
+                        if (nb.deactivated) return;
+                        const auto *rs = reac2(en.type, nb.type);
+                        if (!rs) return;
+                        const double d2 = box.dist2(nb.pos, en.pos);
+                        for (size_t ri = 0; ri < rs->size(); ++ri) {
+                            const Reaction *r = (*rs)[ri];
+                            if (r->rate > 0 && d2 < r->eductDistance2 && coin(tid, r->rate, dt))
+                                ev.push_back(Event{2, r->nProducts, pi, ni, ri, en.type, nb.type, r->rate, 0});
+                        }
+                    });
+                });
+            }
+        });
+        std::vector<Event> events;
+        for (auto &p : parts) events.insert(events.end(), p.begin(), p.end());
+        std::shuffle(events.begin(), events.end(), rng[0]);
+        std::vector<Entry> newEntries;
+        std::vector<size_t> decayed;
+        for (auto it = events.begin(); it != events.end(); ++it) {  // :206-253
+            Event &ev = *it;
+            if (ev.cumulativeRate != 0) continue;
+            size_t e1 = ev.idx1;
+            if (ev.nEducts == 1) {
+                performReaction(e1, e1, o1[ev.t1][ev.reactionIndex], newEntries, decayed);
+                for (auto j = it + 1; j != events.end(); ++j)
+                    if (j->idx1 == e1 || j->idx2 == e1) j->cumulativeRate = 1;
+            } else {
+                performReaction(e1, ev.idx2, (*reac2(ev.t1, ev.t2))[ev.reactionIndex], newEntries, decayed);
+                for (auto j = it + 1; j != events.end(); ++j)
+                    if (j->idx1 == e1 || j->idx2 == e1 || j->idx1 == ev.idx2 || j->idx2 == ev.idx2)
+                        j->cumulativeRate = 1;
+            }
+        }
+        commit(newEntries, decayed);
+    }
+
+    /* CPUGillespie::perform + gatherEvents + handleEventsGillespie + algo::performEvents:
+     * kernels/cpu/src/actions/reactions/CPUGillespie.cpp:53-93, ReactionUtils.h:83-144,
+     * kernels/cpu/src/actions/reactions/ReactionUtils.cpp:55-123, include/readdy/common/algorithm.h:62-136 */
+    void gillespie(double dt) {
+        if (reactions.empty()) return;
+        if (!nlSetUp) throw std::logic_error("neighbor list not set up");
+        double alpha = 0;
+        std::vector<Event> events;
+        for (size_t i = 0; i < entries.size(); ++i) {
+            const Entry &en = entries[i];
+            if (en.deactivated) continue;
+            const auto &rs = o1[en.type];
+            for (size_t ri = 0; ri < rs.size(); ++ri) {
+                double rate = rs[ri]->rate;
+                if (rate > 0) {
+                    alpha += rate;
+                    events.push_back(Event{1, rs[ri]->nProducts, i, 0, ri, en.type, 0, rate, alpha});
+                }
+            }
+        }
+        for (size_t cell = 0; cell < adjacency.size(); ++cell) {
+            forEachInCell(cell, [&](size_t i1) {
+                const Entry &en = entries[i1];
+                if (en.deactivated) return;
+                forEachNeighbor(i1, cell, [&](size_t i2) {
+                    if (i1 > i2) return;
+                    const Entry &nb = entries[i2];
+                    if (nb.deactivated) return;
+                    const auto *rs = reac2(en.type, nb.type);
+                    if (!rs) return;
+                    const double d2 = box.dist2(nb.pos, en.pos);
+                    for (size_t ri = 0; ri < rs->size(); ++ri) {
+                        const Reaction *r = (*rs)[ri];
+                        if (r->rate > 0 && d2 < r->eductDistance2) {
+                            alpha += r->rate;
+                            events.push_back(Event{2, r->nProducts, i1, i2, ri, en.type, nb.type, r->rate, alpha});
+                        }
+                    }
+                });
+            });
+        }
+        std::vector<Entry> newEntries;
+        std::vector<size_t> decayed;
+        auto depending = [](const Event &a, const Event &b) {  // ReactionUtils.cpp:77-80
+            return a.idx1 == b.idx1 || (b.nEducts == 2 && a.idx1 == b.idx2) ||
+                   (a.nEducts == 2 && (a.idx2 == b.idx1 || (b.nEducts == 2 && a.idx2 == b.idx2)));
+        };
+        auto eval = [&](const Event &ev) {
+            if (ev.nEducts == 1) performReaction(ev.idx1, ev.idx1, o1[ev.t1][ev.reactionIndex], newEntries, decayed);
+            else performReaction(ev.idx1, ev.idx2, (*reac2(ev.t1, ev.t2))[ev.reactionIndex], newEntries, decayed);
+        };
+        if (!events.empty()) {  // algo::performEvents
+            size_t nDeact = 0;
+            const size_t nEvents = events.size();
+            double cum = 0;
+            for (auto &ev : events) { ev.cumulativeRate = ev.rate + cum; cum = ev.cumulativeRate; }
+            while (nDeact < nEvents) {
+                const double cr = (events.end() - nDeact - 1)->cumulativeRate;
+                const double x = uniform(0, 0., cr);
+                auto it = std::lower_bound(events.begin(), events.end() - nDeact, x,
+                                           [](const Event &e, double v) { return e.cumulativeRate < v; });
+                if (it == events.end()) throw std::logic_error("performEvents: no event could be selected");
+                if (coin(0, it->rate, dt)) {
+                    eval(*it);
+                    Event done = *it;
+                    auto j = events.begin();
+                    double cs = 0;
+                    while (j < events.end() - nDeact) {
+                        if (depending(*j, done)) {
+                            ++nDeact;
+                            std::iter_swap(j, events.end() - nDeact);
+                        } else {
+                            cs += j->rate;
+                            j->cumulativeRate = cs;
+                            ++j;
+                        }
+                    }
+                } else {
+                    ++nDeact;
+                    std::iter_swap(it, events.end() - nDeact);
+                    it->cumulativeRate = it->rate;
+                    if (it > events.begin()) it->cumulativeRate += (it - 1)->cumulativeRate;
+                    double cs = it->cumulativeRate;
+                    for (auto j = it + 1; j < events.end() - nDeact; ++j) { cs += j->rate; j->cumulativeRate = cs; }
+                }
+            }
+        }
+        commit(newEntries, decayed);
+    }
+
+    void countTypes(int64_t *out) const {
+        for (int t = 0; t < nTypes; ++t) out[t] = 0;
+        for (const auto &e : entries) if (!e.deactivated) out[e.type]++;
+    }
+};
+
+extern "C" {
+
+const char *orc_last_error(void) { return g_err.c_str(); }
+
+orc_system *orc_create(const double box[3], const int periodic[3], double kbt, int n_types, const double *diffusion,
+                       uint64_t seed, int n_threads, int cll_radius) {
+    try {
+        if (n_types <= 0 || cll_radius <= 0) throw std::invalid_argument("bad n_types or cll radius");
+        return new orc_system(box, periodic, kbt, n_types, diffusion, seed, n_threads, cll_radius);
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return nullptr;
+    }
+}
+void orc_destroy(orc_system *s) { delete s; }
+
+static int addPot(orc_system *s, int t1, int t2, Pot2 p) {
+    if (t1 < 0 || t2 < 0 || t1 >= s->nTypes || t2 >= s->nTypes) { g_err = "bad type"; return -1; }
+    s->pot2[orc_system::key(t1, t2)].push_back(p);
+    return 0;
+}
+int orc_add_harmonic_repulsion(orc_system *s, int t1, int t2, double k, double d) {
+    Pot2 p{HARMONIC_REPULSION, {k, d, d * d}, d * d};
+    return addPot(s, t1, t2, p);
+}
+int orc_add_weak_interaction_piecewise_harmonic(orc_system *s, int t1, int t2, double k, double d0, double depth,
+                                                double rc) {
+    Pot2 p{WEAK_PIECEWISE_HARMONIC, {k, d0, depth, rc}, rc * rc};
+    return addPot(s, t1, t2, p);
+}
+int orc_add_lennard_jones(orc_system *s, int t1, int t2, unsigned m, unsigned n, double cutoff, int shift,
+                          double epsilon, double sigma) {
+    if (m <= n) { g_err = "LJ: m must be greater than n"; return -1; }  // Potentials.cpp:163-166
+    double dm = m, dn = n;
+    double rmin = sigma * std::pow(dn / dm, 1. / (dn - dm));            // Potentials.cpp:167-170
+    double kk = -epsilon / (std::pow(sigma / rmin, dm) - std::pow(sigma / rmin, dn));
+    Pot2 p{LENNARD_JONES, {dm, dn, cutoff, shift ? 1. : 0., epsilon, sigma, kk}, cutoff * cutoff};
+    return addPot(s, t1, t2, p);
+}
+int orc_add_screened_electrostatics(orc_system *s, int t1, int t2, double C, double kappa, double D, double sigma,
+                                    unsigned exponent, double cutoff) {
+    if (kappa < 0 || D < 0 || sigma < 0 || cutoff < 0) { g_err = "screened electrostatics: negative parameter"; return -1; }
+    Pot2 p{SCREENED_ELECTROSTATICS, {C, kappa, D, sigma, (double)exponent, cutoff}, cutoff * cutoff};
+    return addPot(s, t1, t2, p);
+}
+
+static int addReaction(orc_system *s, Reaction *r) {
+    r->id = (int)s->reactions.size();
+    s->reactions.push_back(r);
+    s->reactionCounts.push_back(0);
+    if (r->nEducts == 1) s->o1.at(r->educts[0]).push_back(r);
+    else s->o2[orc_system::key(r->educts[0], r->educts[1])].push_back(r);
+    return r->id;
+}
+static void normWeights(Reaction *r) {  // Fusion.h:62-68, Fission.h:64-70
+    double sum = r->w1 + r->w2;
+    if (sum != 1) { r->w1 /= sum; r->w2 /= sum; }
+}
+int orc_add_conversion(orc_system *s, int from, int to, double rate) {
+    auto *r = new Reaction{CONVERSION, 0, {from, 0}, {to, 0}, 1, 1, rate};
+    return addReaction(s, r);
+}
+int orc_add_decay(orc_system *s, int from, double rate) {
+    auto *r = new Reaction{DECAY, 0, {from, 0}, {0, 0}, 1, 0, rate};
+    return addReaction(s, r);
+}
+int orc_add_fusion(orc_system *s, int from1, int from2, int to, double rate, double ed, double w1, double w2) {
+    auto *r = new Reaction{FUSION, 0, {from1, from2}, {to, 0}, 2, 1, rate, ed, ed * ed, 0, w1, w2};
+    normWeights(r);
+    return addReaction(s, r);
+}
+int orc_add_fission(orc_system *s, int from, int to1, int to2, double rate, double pd, double w1, double w2) {
+    auto *r = new Reaction{FISSION, 0, {from, 0}, {to1, to2}, 1, 2, rate, 0, 0, pd, w1, w2};
+    normWeights(r);
+    return addReaction(s, r);
+}
+int orc_add_enzymatic(orc_system *s, int catalyst, int from, int to, double rate, double ed) {
+    auto *r = new Reaction{ENZYMATIC, 0, {from, catalyst}, {to, catalyst}, 2, 2, rate, ed, ed * ed};
+    return addReaction(s, r);
+}
+
+int orc_add_harmonic_bonds(orc_system *s, int n, const int *idx, const double *k, const double *l0) {
+    for (int i = 0; i < n; ++i) s->bonds.push_back(Bond{(size_t)idx[2 * i], (size_t)idx[2 * i + 1], k[i], l0[i]});
+    return 0;
+}
+int orc_add_harmonic_angles(orc_system *s, int n, const int *idx, const double *k, const double *th) {
+    for (int i = 0; i < n; ++i)
+        s->angles.push_back(Angle{(size_t)idx[3 * i], (size_t)idx[3 * i + 1], (size_t)idx[3 * i + 2], k[i], th[i]});
+    return 0;
+}
+int orc_add_cosine_dihedrals(orc_system *s, int n, const int *idx, const double *k, const double *mult,
+                             const double *phi0) {
+    for (int i = 0; i < n; ++i)
+        s->dihedrals.push_back(Dihedral{(size_t)idx[4 * i], (size_t)idx[4 * i + 1], (size_t)idx[4 * i + 2],
+                                        (size_t)idx[4 * i + 3], k[i], mult[i], phi0[i]});
+    return 0;
+}
+
+int orc_add_particles(orc_system *s, int n, const double *pos, const int *types) {
+    for (int i = 0; i < n; ++i) {
+        Entry e;
+        e.pos = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        e.type = types[i];
+        e.id = s->nextId++;
+        s->addEntry(e);
+    }
+    return 0;
+}
+int orc_n_particles(const orc_system *s) {
+    int n = 0;
+    for (auto &e : s->entries) n += !e.deactivated;
+    return n;
+}
+int orc_n_entries(const orc_system *s) { return (int)s->entries.size(); }
+int orc_get_particles(const orc_system *s, double *pos, int *types, uint64_t *ids, double *force, int *sidx) {
+    int k = 0;
+    for (size_t i = 0; i < s->entries.size(); ++i) {
+        const auto &e = s->entries[i];
+        if (e.deactivated) continue;
+        if (pos) { pos[3 * k] = e.pos.x; pos[3 * k + 1] = e.pos.y; pos[3 * k + 2] = e.pos.z; }
+        if (types) types[k] = e.type;
+        if (ids) ids[k] = e.id;
+        if (force) { force[3 * k] = e.force.x; force[3 * k + 1] = e.force.y; force[3 * k + 2] = e.force.z; }
+        if (sidx) sidx[k] = (int)i;
+        ++k;
+    }
+    return k;
+}
+double orc_calculate_max_cutoff(const orc_system *s) { return s->maxCutoff(); }
+
+int orc_nl_setup(orc_system *s, double cutoff) {
+    try { s->nlSetup(cutoff); return 0; } catch (const std::exception &e) { g_err = e.what(); return -1; }
+}
+int orc_nl_update(orc_system *s) {
+    try { s->nlUpdate(); return 0; } catch (const std::exception &e) { g_err = e.what(); return -1; }
+}
+
+static int64_t finishPairs(std::vector<std::pair<uint64_t, uint64_t>> &v, int64_t cap, uint64_t *out) {
+    std::sort(v.begin(), v.end());
+    if ((int64_t)v.size() > cap) return -1;
+    for (size_t i = 0; i < v.size(); ++i) { out[2 * i] = v[i].first; out[2 * i + 1] = v[i].second; }
+    return (int64_t)v.size();
+}
+/* the pair-set contract of the consumers: CPUCalculateForces.cpp:240-243 (d^2 < rc^2 on the minimum image) */
+int64_t orc_nl_pairs(const orc_system *s, double cutoff, int64_t cap, uint64_t *out) {
+    std::vector<std::pair<uint64_t, uint64_t>> v;
+    const double c2 = cutoff * cutoff;
+    for (size_t cell = 0; cell < s->adjacency.size(); ++cell) {
+        s->forEachInCell(cell, [&](size_t i) {
+            const auto &a = s->entries[i];
+            if (a.deactivated) return;
+            s->forEachNeighbor(i, cell, [&](size_t j) {
+                if (i > j) return;
+                const auto &b = s->entries[j];
+                if (b.deactivated) return;
+                V3 x = s->box.shortest(a.pos, b.pos);
+                if (dot(x, x) < c2) v.push_back({std::min(a.id, b.id), std::max(a.id, b.id)});
+            });
+        });
+    }
+    return finishPairs(v, cap, out);
+}
+/* brute force over all in-box pairs, kernels/cpu/test/TestNeighborList.cpp:277-297 */
+int64_t orc_brute_force_pairs(const orc_system *s, double cutoff, int64_t cap, uint64_t *out) {
+    std::vector<std::pair<uint64_t, uint64_t>> v;
+    const double c2 = cutoff * cutoff;
+    auto inBox = [s](const V3 &p) {
+        for (int d = 0; d < 3; ++d) if (!(-.5 * s->box.L[d] <= p[d] && .5 * s->box.L[d] > p[d])) return false;
+        return true;
+    };
+    for (size_t i = 0; i < s->entries.size(); ++i) {
+        const auto &a = s->entries[i];
+        if (a.deactivated || !inBox(a.pos)) continue;
+        for (size_t j = i + 1; j < s->entries.size(); ++j) {
+            const auto &b = s->entries[j];
+            if (b.deactivated || !inBox(b.pos)) continue;
+            V3 x = s->box.shortest(a.pos, b.pos);
+            if (dot(x, x) < c2) v.push_back({std::min(a.id, b.id), std::max(a.id, b.id)});
+        }
+    }
+    return finishPairs(v, cap, out);
+}
+
+double orc_calculate_forces(orc_system *s) {
+    try { return s->calculateForces(); } catch (const std::exception &e) { g_err = e.what(); return NAN; }
+}
+double orc_energy(const orc_system *s) { return s->energy; }
+int orc_euler_bd(orc_system *s, double dt) { s->eulerBD(dt); return 0; }
+int orc_uncontrolled_approximation(orc_system *s, double dt) {
+    try { s->uncontrolledApproximation(dt); return 0; } catch (const std::exception &e) { g_err = e.what(); return -1; }
+}
+int orc_gillespie(orc_system *s, double dt) {
+    try { s->gillespie(dt); return 0; } catch (const std::exception &e) { g_err = e.what(); return -1; }
+}
+
+/* SimulationLoop::run, include/readdy/api/SimulationLoop.h:256-306 (no compartments, no topology reactions) */
+int orc_run(orc_system *s, int64_t n_steps, double dt, int handler, int stride, int64_t *counts, int64_t maxrec) {
+    try {
+        double cutoff = s->maxCutoff();
+        bool nl = cutoff > 0;
+        int64_t rec = 0;
+        auto observe = [&](int64_t t) {
+            if (counts && stride > 0 && t % stride == 0 && rec < maxrec) s->countTypes(counts + rec++ * s->nTypes);
+        };
+        if (nl) s->nlSetup(cutoff);
+        s->calculateForces();
+        observe(0);
+        for (int64_t t = 0; t < n_steps; ++t) {
+            s->eulerBD(dt);
+            if (nl) s->nlUpdate();
+            if (!s->reactions.empty()) {
+                if (handler == ORC_GILLESPIE) s->gillespie(dt);
+                else s->uncontrolledApproximation(dt);
+            }
+            if (nl) s->nlUpdate();
+            s->calculateForces();
+            observe(t + 1);
+        }
+        return (int)rec;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+int orc_reaction_counts(const orc_system *s, int64_t *counts, int cap) {
+    int n = std::min<int>(cap, (int)s->reactionCounts.size());
+    for (int i = 0; i < n; ++i) counts[i] = s->reactionCounts[i];
+    return n;
+}
+
+}  // extern "C"

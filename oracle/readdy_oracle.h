@@ -1,0 +1,85 @@
+/*
+ * TEST INFRASTRUCTURE ONLY -- not part of the product.
+ *
+ * C interface of the FP64 CPU restatement of ReaDDy's CPU-kernel hot path (cell-linked neighbour
+ * list, pair and bonded forces, Euler Brownian dynamics, uncontrolled-approximation and Gillespie
+ * reaction handlers).  Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load it,
+ * as the checker the CUDA path is compared against.
+ *
+ * Indices ("storage indices") follow the reference data container: particles live in a vector with
+ * blanks that are reused LIFO (kernels/cpu .. DefaultDataContainer.h:79-139).
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_system orc_system;
+
+enum orc_handler { ORC_UNCONTROLLED_APPROXIMATION = 0, ORC_GILLESPIE = 1 };
+
+orc_system *orc_create(const double box[3], const int periodic[3], double kbt, int n_types,
+                       const double *diffusion, uint64_t seed, int n_threads, int cll_radius);
+void orc_destroy(orc_system *s);
+const char *orc_last_error(void);
+
+/* pair potentials (PotentialsOrder2.h); return 0 on success */
+int orc_add_harmonic_repulsion(orc_system *s, int t1, int t2, double k, double interaction_distance);
+int orc_add_weak_interaction_piecewise_harmonic(orc_system *s, int t1, int t2, double k, double desired_distance,
+                                                double depth, double no_interaction_distance);
+int orc_add_lennard_jones(orc_system *s, int t1, int t2, unsigned m, unsigned n, double cutoff, int shift,
+                          double epsilon, double sigma);
+int orc_add_screened_electrostatics(orc_system *s, int t1, int t2, double electrostatic_strength,
+                                    double inverse_screening_depth, double repulsion_strength,
+                                    double repulsion_distance, unsigned exponent, double cutoff);
+
+/* reactions (include/readdy/model/reactions); return reaction id >= 0 or -1 */
+int orc_add_conversion(orc_system *s, int from, int to, double rate);
+int orc_add_decay(orc_system *s, int from, double rate);
+int orc_add_fusion(orc_system *s, int from1, int from2, int to, double rate, double educt_distance, double w1,
+                   double w2);
+int orc_add_fission(orc_system *s, int from, int to1, int to2, double rate, double product_distance, double w1,
+                    double w2);
+int orc_add_enzymatic(orc_system *s, int catalyst, int from, int to, double rate, double educt_distance);
+
+/* bonded terms of static topologies, indices are storage indices */
+int orc_add_harmonic_bonds(orc_system *s, int n, const int *idx2, const double *k, const double *l0);
+int orc_add_harmonic_angles(orc_system *s, int n, const int *idx3, const double *k, const double *theta0);
+int orc_add_cosine_dihedrals(orc_system *s, int n, const int *idx4, const double *k, const double *multiplicity,
+                             const double *phi0);
+
+/* particles */
+int orc_add_particles(orc_system *s, int n, const double *pos3, const int *types);
+int orc_n_particles(const orc_system *s);       /* active */
+int orc_n_entries(const orc_system *s);         /* storage size incl. blanks */
+/* active particles in storage order; any output pointer may be NULL */
+int orc_get_particles(const orc_system *s, double *pos3, int *types, uint64_t *ids, double *force3,
+                      int *storage_index);
+double orc_calculate_max_cutoff(const orc_system *s);
+
+/* neighbour list (CellLinkedList.cpp) */
+int orc_nl_setup(orc_system *s, double cutoff);
+int orc_nl_update(orc_system *s);
+/* candidate pairs from the cell list, each unordered pair once, filtered by d^2 < cutoff^2;
+ * writes particle ids (min,max) sorted ascending; returns the number of pairs or -1 if cap too small */
+int64_t orc_nl_pairs(const orc_system *s, double cutoff, int64_t cap, uint64_t *pairs);
+int64_t orc_brute_force_pairs(const orc_system *s, double cutoff, int64_t cap, uint64_t *pairs);
+
+/* actions */
+double orc_calculate_forces(orc_system *s);     /* returns total energy */
+double orc_energy(const orc_system *s);
+int orc_euler_bd(orc_system *s, double dt);
+int orc_uncontrolled_approximation(orc_system *s, double dt);
+int orc_gillespie(orc_system *s, double dt);
+/* SimulationLoop::run step order; counts (n_types per record) every count_stride steps incl. t=0,
+ * returns the number of records written (counts may be NULL) */
+int orc_run(orc_system *s, int64_t n_steps, double dt, int handler, int count_stride, int64_t *counts,
+            int64_t max_records);
+/* per-reaction count of performed events accumulated since creation */
+int orc_reaction_counts(const orc_system *s, int64_t *counts, int cap);
+
+#ifdef __cplusplus
+}
+#endif

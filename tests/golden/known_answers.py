@@ -1,0 +1,172 @@
+"""Known-answer vectors for the hot path, transcribed from ReaDDy's own unit tests.
+
+Each case names the reference test (file:line) whose inputs and expected outputs it carries.
+The CPU oracle is pinned against these (tests/test_oracle_golden.py) and the CUDA path is checked
+against the same cases (tests/test_gpu_golden.py).  Forces the reference computes but does not
+enforce (its vec3eq calls without REQUIRE) are enforced here.
+"""
+import math
+
+PI = math.pi
+
+# ---------------------------------------------------------------------------------------------
+# pair potentials
+# ---------------------------------------------------------------------------------------------
+PAIR_CASES = [
+    dict(
+        name="harmonic_repulsion_two_particles",
+        source="readdy/test/TestStateModel.cpp:57-99",
+        box=(4., 4., 4.), periodic=(False, False, False), diffusion=(1.0,),
+        potentials=[("harmonic_repulsion", 0, 0, dict(k=1.0, d=2.0))],
+        positions=[(0., 0., 0.), (0., 0., 1.8)], types=[0, 0],
+        energy=0.02,
+        forces=[(0, 0, -0.2), (0, 0, 0.2)],
+        force_atol=1e-12,
+    ),
+    dict(
+        name="harmonic_repulsion_six_particles",
+        source="readdy/test/TestStateModel.cpp:101-181",
+        box=(10., 10., 10.), periodic=(True, True, False), diffusion=(1.0, 1.0),
+        potentials=[("harmonic_repulsion", 0, 1, dict(k=1.0, d=3.0))],
+        positions=[(0, 0, 0), (0, 0.8, 0), (0.2, 0, -0.2), (0, 0, 0.1), (-1.8, -4.0, 1.8), (0.5, 0, 0)],
+        types=[0, 0, 0, 1, 1, 1],
+        energy=4.205 + 3.125 + 2.4063226755104354 + 2.1148056603830194 + 3.4833346173608031 * 2,
+        # per-pair forces of the reference test, combined per particle below
+        pair_forces={
+            (0, 3): (0, 0, -2.9), (0, 5): (-2.5, 0, 0),
+            (1, 3): (0, 2.1768336301410027, -0.27210420376762534),
+            (1, 5): (-1.08999682000954, 1.743994912015264, 0),
+            (2, 3): (1.4641005886756873, 0, -2.1961508830135306),
+            (2, 5): (-2.1961508830135306, 0, -1.4641005886756873),
+        },
+        force_atol=1e-12,
+    ),
+    dict(
+        name="lennard_jones_3_2",
+        source="readdy/test/TestPotentials.cpp:379-447",
+        box=(10., 10., 10.), periodic=(True, True, True), diffusion=(1.0,),
+        potentials=[("lennard_jones", 0, 0, dict(m=3, n=2, cutoff=1.0, shift=False, epsilon=1.0, sigma=0.1))],
+        positions=[(0, 0, 0), (0, 0, .09), (2, 0, 0), (2, 0, .09)], types=[0, 0, 0, 0],
+        energy=2.0 * 0.925925925926, energy_rtol=1e-6,
+        forces=[(0, 0, -123.45679012), (0, 0, 123.45679012), (0, 0, -123.45679012), (0, 0, 123.45679012)],
+        force_atol=1e-6,
+    ),
+    dict(
+        name="screened_electrostatics",
+        source="readdy/test/TestPotentials.cpp:448-505",
+        box=(10., 10., 10.), periodic=(False, False, False), diffusion=(1.0,),
+        potentials=[("screened_electrostatics", 0, 0,
+                     dict(C=-1.0, kappa=1.0, D=1.0, sigma=1.0, exponent=6, cutoff=8.0))],
+        positions=[(0, 0, 0), (1.2, 1.5, -1.7)], types=[0, 0],
+        energy=-0.0264715664281, energy_rtol=1e-9,
+        forces=[(0.01565262, 0.01956577, -0.02217454), (-0.01565262, -0.01956577, 0.02217454)],
+        force_atol=1e-8,
+    ),
+]
+
+# ---------------------------------------------------------------------------------------------
+# bonded terms of static topologies
+# ---------------------------------------------------------------------------------------------
+BONDED_CASES = [
+    dict(
+        name="harmonic_bond",
+        source="readdy/test/TestTopologies.cpp:83-128",
+        box=(10., 10., 10.), periodic=(True, True, True),
+        positions=[(4, 0, 0), (1, 0, 0)],
+        bonds=[((0, 1), 10.0, 5.0)], angles=[], dihedrals=[],
+        energy=40.0, energy_rtol=0.0,
+        forces=[(40., 0, 0), (-40., 0, 0)], force_atol=0.0,
+    ),
+    dict(
+        name="harmonic_angle",
+        source="readdy/test/TestTopologies.cpp:130-178",
+        box=(10., 10., 10.), periodic=(True, True, True),
+        positions=[(0, 0, 0), (1, 0, 0), (1, 1, 0)],
+        bonds=[], angles=[((0, 1, 2), 1.0, PI)], dihedrals=[],
+        energy=2.4674011002723395, energy_rtol=1e-5,
+        forces=[(0, -3.14159265, 0), (-3.14159265, 3.14159265, 0), (3.14159265, 0., 0.)], force_atol=1e-6,
+    ),
+    dict(
+        name="harmonic_angle_general",
+        source="readdy/test/TestTopologies.cpp:180-215",
+        box=(10., 10., 10.), periodic=(True, True, True),
+        positions=[(0.1, 0.1, 0.1), (1.0, 0.0, 0.0), (1.0, 0.5, -.3)],
+        bonds=[], angles=[((0, 1, 2), 1.0, PI)], dihedrals=[],
+        energy=2.5871244540347655, energy_rtol=1e-5,
+        forces=[(-0.13142034, -3.01536661, 1.83258358), (-5.32252362, 3.44312692, -1.11964973),
+                (5.45394396, -0.42776031, -0.71293385)], force_atol=1e-6,
+    ),
+    dict(
+        name="cosine_dihedral",
+        source="readdy/test/TestTopologies.cpp:217-273",
+        box=(10., 10., 10.), periodic=(True, True, True),
+        positions=[(-1, 0, 0), (0, 0, 0), (0, 0, 1), (1, .1, 1)],
+        bonds=[], angles=[], dihedrals=[((0, 1, 2, 3), 1.0, 3, PI)],
+        energy=0.044370223263673791, energy_rtol=1e-5,
+        forces=[(0., -0.88371125, 0.), (0., 0.88371125, 0.), (-0.08749616, 0.87496163, 0.),
+                (0.08749616, -0.87496163, 0.)], force_atol=1e-6,
+    ),
+    dict(
+        name="cosine_dihedral_steep",
+        source="readdy/test/TestTopologies.cpp:275-311",
+        box=(10., 10., 10.), periodic=(True, True, True),
+        positions=[(-1, 0, 0), (0, 0, 0), (0, 0, 1), (1, 3, 1)],
+        bonds=[], angles=[], dihedrals=[((0, 1, 2, 3), 1.0, 3, PI)],
+        energy=1.8221921916437787, energy_rtol=1e-5,
+        forces=[(0., 1.70762994, 0.), (0., -1.70762994, 0.), (0.51228898, -0.17076299, 0.),
+                (-0.51228898, 0.17076299, 0.)], force_atol=1e-6,
+    ),
+]
+
+# ---------------------------------------------------------------------------------------------
+# reactions with rates so large that every candidate fires (deterministic outcomes)
+# ---------------------------------------------------------------------------------------------
+REACTION_CASES = [
+    dict(
+        name="fusion_through_periodic_boundary",
+        source="readdy/test/TestReactions.cpp:166-189",
+        box=(10., 10., 10.), periodic=(True, True, True), diffusion=(0.,),
+        reactions=[("fusion", dict(a=0, b=0, c=0, rate=1e16, educt_distance=2.0))],
+        positions=[(4.5, 4.5, 4.5), (-4.7, -4.7, -4.7)], types=[0, 0],
+        expect_n=1, expect_positions=[(4.9, 4.9, 4.9)], pos_rtol=1e-6,
+    ),
+    dict(
+        name="parallel_gillespie_eleven_particles",
+        source="kernels/cpu/test/TestReactions.cpp:250-355",
+        box=(10., 10., 30.), periodic=(True, True, False), diffusion=(.25, .25, .25),
+        reactions=[("fusion", dict(a=0, b=0, c=0, rate=1e16, educt_distance=1.0)),
+                   ("fusion", dict(a=0, b=2, c=0, rate=2.2250738585072014e-308, educt_distance=1.0)),
+                   ("fusion", dict(a=0, b=1, c=0, rate=0.0, educt_distance=1.0))],
+        positions=[(0, 0, 0), (0, 0, -.7), (0, 0, .7), (0, 0, -1.6), (0, 0, 1.6), (0, 0, 1.7), (0, 0, -1.7),
+                   (0, 0, -5), (0, 0, -5.5), (0, 0, 5), (0, 0, 5.5)],
+        types=[0, 0, 2, 2, 0, 0, 1, 0, 0, 0, 0],
+        expect_n=7,
+        # (type, position) of every particle after one step of the handler
+        expect_particles=[(1, (0, 0, -1.7)), (2, (0, 0, .7)), (2, (0, 0, -1.6)), (0, (0, 0, -5.25)),
+                          (0, (0, 0, -.35)), (0, (0, 0, 1.65)), (0, (0, 0, 5.25))],
+        pos_atol=1e-6,
+    ),
+]
+
+# Michaelis-Menten integration test, readdy/test/IntegrationTests.cpp:30-106:
+# <S> over 37,500 steps must lie within 3 % of 665.2.
+MICHAELIS_MENTEN = dict(
+    source="readdy/test/IntegrationTests.cpp:30-106",
+    box=(10., 10., 10.), periodic=(True, True, True),
+    diffusion=(0.5, 0.5, 0.5, 0.5),   # E, S, ES, P
+    k_fwd=0.0023417691399750494, k_back=1.0, k_prod=1.0, educt_distance=1.0, product_distance=1.0,
+    n_e=70, n_s=700, dt=8e-3, n_steps=37500, mean_s=665.2, rel_band=0.03,
+)
+
+
+def per_particle_forces(case):
+    """Expected per-particle forces; pair_forces (i,j): f are forces on i, -f on j."""
+    if "forces" in case:
+        return [tuple(map(float, f)) for f in case["forces"]]
+    n = len(case["positions"])
+    out = [[0.0, 0.0, 0.0] for _ in range(n)]
+    for (i, j), f in case["pair_forces"].items():
+        for d in range(3):
+            out[i][d] += f[d]
+            out[j][d] -= f[d]
+    return [tuple(v) for v in out]

@@ -1,0 +1,161 @@
+"""Pins the FP64 CPU oracle against the known-answer vectors of ReaDDy's own unit tests.
+
+These run without a GPU.  They establish that the oracle restates the reference before any CUDA
+result is compared with it.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests.golden import known_answers as ka
+
+
+def _oracle_from_case(case, seed=1, n_threads=1):
+    n_types = max(len(case.get("diffusion", (1.0,))), max(case.get("types", [0])) + 1)
+    diff = list(case.get("diffusion", (1.0,))) + [1.0] * (n_types - len(case.get("diffusion", (1.0,))))
+    s = oracle.OracleSystem(case["box"], case["periodic"], 1.0, diff, seed=seed, n_threads=n_threads)
+    for kind, t1, t2, p in case.get("potentials", []):
+        if kind == "harmonic_repulsion":
+            s.add_harmonic_repulsion(t1, t2, p["k"], p["d"])
+        elif kind == "lennard_jones":
+            s.add_lennard_jones(t1, t2, p["m"], p["n"], p["cutoff"], p["shift"], p["epsilon"], p["sigma"])
+        elif kind == "screened_electrostatics":
+            s.add_screened_electrostatics(t1, t2, p["C"], p["kappa"], p["D"], p["sigma"], p["exponent"],
+                                          p["cutoff"])
+        elif kind == "weak_interaction_piecewise_harmonic":
+            s.add_weak_interaction_piecewise_harmonic(t1, t2, p["k"], p["desired"], p["depth"], p["cutoff"])
+    return s
+
+
+@pytest.mark.parametrize("case", ka.PAIR_CASES, ids=lambda c: c["name"])
+def test_pair_potential_known_answers(case):
+    s = _oracle_from_case(case)
+    s.add_particles(np.array(case["positions"], float), np.array(case["types"]))
+    s.nl_setup(s.calculate_max_cutoff())
+    e1 = s.calculate_forces()
+    e2 = s.calculate_forces()  # calculating twice must not accumulate (TestStateModel.cpp:80-81)
+    assert e1 == e2
+    rtol = case.get("energy_rtol", 1e-12)
+    assert e1 == pytest.approx(case["energy"], rel=max(rtol, 1e-12))
+    _, _, ids, f, _ = s.particles()
+    exp = np.array(ka.per_particle_forces(case))
+    order = np.argsort(ids)
+    np.testing.assert_allclose(f[order], exp, rtol=0, atol=case["force_atol"] + 1e-12)
+
+
+@pytest.mark.parametrize("case", ka.BONDED_CASES, ids=lambda c: c["name"])
+def test_bonded_known_answers(case):
+    s = oracle.OracleSystem(case["box"], case["periodic"], 1.0, (1.0,), seed=1)
+    s.add_particles(np.array(case["positions"], float), 0)
+    for idx, k, l0 in case["bonds"]:
+        s.add_harmonic_bonds([idx], k, l0)
+    for idx, k, th in case["angles"]:
+        s.add_harmonic_angles([idx], k, th)
+    for idx, k, mult, phi0 in case["dihedrals"]:
+        s.add_cosine_dihedrals([idx], k, mult, phi0)
+    e = s.calculate_forces()
+    assert e == pytest.approx(case["energy"], rel=case["energy_rtol"], abs=1e-14)
+    _, _, _, f, _ = s.particles()
+    np.testing.assert_allclose(f, np.array(case["forces"], float), rtol=0, atol=case["force_atol"] + 1e-14)
+
+
+def _oracle_reaction_case(case, seed):
+    s = oracle.OracleSystem(case["box"], case["periodic"], 1.0, case["diffusion"], seed=seed)
+    for kind, p in case["reactions"]:
+        assert kind == "fusion"
+        s.add_fusion(p["a"], p["b"], p["c"], p["rate"], p["educt_distance"])
+    s.add_particles(np.array(case["positions"], float), np.array(case.get("types", [0] * len(case["positions"]))))
+    return s
+
+
+@pytest.mark.parametrize("handler", [oracle.UNCONTROLLED_APPROXIMATION, oracle.GILLESPIE])
+@pytest.mark.parametrize("case", ka.REACTION_CASES, ids=lambda c: c["name"])
+def test_reaction_known_answers(case, handler):
+    for seed in range(5):
+        s = _oracle_reaction_case(case, seed)
+        s.nl_setup(s.calculate_max_cutoff())
+        (s.gillespie if handler == oracle.GILLESPIE else s.uncontrolled_approximation)(1.0)
+        pos, types, _, _, _ = s.particles()
+        assert len(pos) == case["expect_n"]
+        if "expect_positions" in case:
+            np.testing.assert_allclose(pos, np.array(case["expect_positions"]), rtol=case["pos_rtol"])
+        else:
+            got = sorted((int(t), tuple(np.round(p, 6))) for t, p in zip(types, pos))
+            exp = sorted((t, tuple(np.round(np.array(p, float), 6))) for t, p in case["expect_particles"])
+            assert [g[0] for g in got] == [e[0] for e in exp]
+            np.testing.assert_allclose(np.array([g[1] for g in got]), np.array([e[1] for e in exp]),
+                                       atol=case["pos_atol"])
+
+
+@pytest.mark.parametrize("handler", [oracle.UNCONTROLLED_APPROXIMATION, oracle.GILLESPIE])
+def test_fission_near_boundary(handler):
+    """readdy/test/TestReactions.cpp:191-213: products straddle the periodic boundary."""
+    for seed in range(10):
+        s = oracle.OracleSystem((10., 10., 10.), (True,) * 3, 1.0, (0.,), seed=seed)
+        s.add_fission(0, 0, 0, 1e16, 2.0)
+        s.add_particles([(-4.9999999, 0, 0)], 0)
+        s.nl_setup(1.0)
+        (s.gillespie if handler == oracle.GILLESPIE else s.uncontrolled_approximation)(1.0)
+        pos, _, _, _, _ = s.particles()
+        assert len(pos) == 2
+        assert (pos[0, 0] <= 0) != (pos[1, 0] <= 0)
+        assert np.all(pos >= -5.0) and np.all(pos < 5.0)
+
+
+@pytest.mark.parametrize("box,pbc", [((10, 10, 10), (1, 1, 1)), ((10, 10, 10), (0, 0, 0)),
+                                     ((5, 12, 7), (1, 0, 1)), ((3.3, 3.3, 3.3), (1, 1, 1)),
+                                     ((2.5, 8, 2.5), (1, 1, 0)), ((20, 4, 4), (1, 1, 1)),
+                                     ((6, 6, 30), (0, 1, 1))])
+@pytest.mark.parametrize("radius", [1, 2])
+def test_cell_list_pairs_match_brute_force(box, pbc, radius):
+    """kernels/cpu/test/TestNeighborList.cpp:267-362: cell-list pair set == brute-force pair set."""
+    rng = np.random.default_rng(7)
+    s = oracle.OracleSystem(box, pbc, 1.0, (1.0, 1.0), seed=3, cll_radius=radius)
+    s.add_harmonic_repulsion(0, 1, 1.0, 1.2)
+    s.add_harmonic_repulsion(0, 0, 1.0, 0.9)
+    n = 400
+    pos = (rng.random((n, 3)) - 0.5) * np.array(box, float)
+    s.add_particles(pos, rng.integers(0, 2, n))
+    s.nl_setup(s.calculate_max_cutoff())
+    for step in range(3):
+        a = s.nl_pairs(1.2)
+        b = s.brute_force_pairs(1.2)
+        assert len(a) > 0
+        np.testing.assert_array_equal(a, b)
+        s.euler_bd(0.01)
+        s.nl_update()
+
+
+def test_multithreaded_forces_match_serial():
+    rng = np.random.default_rng(11)
+    pos = (rng.random((3000, 3)) - 0.5) * 15.0
+    types = rng.integers(0, 3, 3000)
+    out = []
+    for nt in (1, 4):
+        s = oracle.OracleSystem((15., 15., 15.), (1, 1, 1), 1.0, (1., .5, .2), seed=1, n_threads=nt)
+        s.add_lennard_jones(0, 0, 12, 6, 2.5, True, 1.0, 1.0)
+        s.add_weak_interaction_piecewise_harmonic(1, 1, 10.0, 1.0, 0.5, 1.5)
+        s.add_harmonic_repulsion(0, 1, 10.0, 1.0)
+        s.add_harmonic_repulsion(0, 2, 10.0, 1.0)
+        s.add_harmonic_repulsion(1, 2, 10.0, 1.0)
+        s.add_harmonic_repulsion(2, 2, 10.0, 1.0)
+        s.add_particles(pos, types)
+        s.nl_setup(s.calculate_max_cutoff())
+        e = s.calculate_forces()
+        out.append((e, s.particles()[3]))
+    assert out[0][0] == pytest.approx(out[1][0], rel=1e-12)
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12, atol=1e-12)
+
+
+def test_brownian_msd_matches_6Dt():
+    """Free diffusion: <|dx|^2> = 6 D t, 60k samples give a 3-sigma band of 1 %."""
+    rng = np.random.default_rng(5)
+    n, steps, dt, D = 20000, 30, 1e-3, 1.0
+    s = oracle.OracleSystem((1000., 1000., 1000.), (1, 1, 1), 1.0, (D,), seed=9, n_threads=2)
+    p0 = (rng.random((n, 3)) - 0.5) * 100.0
+    s.add_particles(p0, 0)
+    for _ in range(steps):
+        s.euler_bd(dt)
+    p1 = s.particles()[0]
+    msd = np.mean(np.sum((p1 - p0) ** 2, axis=1))
+    assert abs(msd / (6 * D * dt * steps) - 1) < 0.01
