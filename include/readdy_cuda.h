@@ -1,0 +1,179 @@
+/*
+ * readdy_cuda.h -- C ABI of the GB300-native ReaDDy compute kernel ("CUDA" kernel plugin).
+ *
+ * libreaddy_cuda_core.so exports these symbols.  They take plain pointers, sizes and PODs, return an
+ * int status (RDC_OK or an RDC_ERR_* code) and never throw; rdc_last_error() returns the message of
+ * the calling thread's last failure.  A ReaDDy kernel plugin (model::Kernel, StateModel,
+ * ActionFactory) binds one call per action; the binding is shown in INTEGRATION.md.
+ *
+ * Each entry point names the reference interface it replaces (paths inside readdy/readdy).
+ * Positions, box sizes and parameters are passed in FP64 like the reference's `scalar`
+ * (include/readdy/common/common.h:62) and are held on the device in FP32; box edges are rounded to
+ * FP32 on entry.  Particle ids are 64-bit on this interface and count per system from 0.
+ */
+#ifndef READDY_CUDA_H
+#define READDY_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; the plugin maps them onto the reference's exception types
+ * (KernelProvider.cpp:188, CellLinkedList.cpp:55,245, CPUActionFactory.cpp:109) */
+#define RDC_OK 0
+#define RDC_ERR_INVALID_ARGUMENT 1 /* std::invalid_argument */
+#define RDC_ERR_LOGIC 2            /* std::logic_error */
+#define RDC_ERR_RUNTIME 3          /* std::runtime_error */
+#define RDC_ERR_CUDA 4             /* a CUDA runtime call failed */
+#define RDC_ERR_CAPACITY 5         /* device buffer capacity exceeded (particles or events) */
+
+#define RDC_UNCONTROLLED_APPROXIMATION 0
+#define RDC_GILLESPIE 1
+
+typedef struct rdc_context rdc_context;
+typedef struct rdc_system rdc_system;
+typedef struct rdc_batch rdc_batch;
+
+/* ---- library ---------------------------------------------------------------------------------- */
+/* message of the calling thread's last failed call ("" if none) */
+const char *rdc_last_error(void);
+/* ABI version of this header (major*1000 + minor) */
+int rdc_version(void);
+/* KernelProvider plugin identity: name() of kernels/cpu .. CPUKernel.h:150-152; returns "CUDA" */
+const char *rdc_kernel_name(void);
+
+/* ---- model::Context (include/readdy/model/Context.h) ------------------------------------------ */
+/* box, periodicity, kBT (Context.h:76-108) and species with diffusion constants
+ * (ParticleTypeRegistry::add, include/readdy/model/ParticleTypeRegistry.h:128-133) */
+int rdc_context_create(rdc_context **out, const double box[3], const int periodic[3], double kbt, int n_types,
+                       const double *diffusion);
+int rdc_context_destroy(rdc_context *ctx);
+/* Context::calculateMaxCutoff, readdy/main/model/Context.cpp:126-144 */
+int rdc_context_max_cutoff(const rdc_context *ctx, double *cutoff);
+
+/* PotentialRegistry::addHarmonicRepulsion (PotentialsOrder2.h:54-103) */
+int rdc_context_add_harmonic_repulsion(rdc_context *ctx, int type1, int type2, double force_constant,
+                                       double interaction_distance);
+/* PotentialRegistry::addWeakInteractionPiecewiseHarmonic (PotentialsOrder2.h:105-194) */
+int rdc_context_add_weak_interaction_piecewise_harmonic(rdc_context *ctx, int type1, int type2,
+                                                        double force_constant, double desired_distance,
+                                                        double depth, double no_interaction_distance);
+/* PotentialRegistry::addLennardJones (PotentialsOrder2.h:199-272, readdy/main/model/potentials/Potentials.cpp:157-171) */
+int rdc_context_add_lennard_jones(rdc_context *ctx, int type1, int type2, unsigned m, unsigned n, double cutoff,
+                                  int shift, double epsilon, double sigma);
+/* PotentialRegistry::addScreenedElectrostatics (PotentialsOrder2.h:274-323, Potentials.cpp:183-202) */
+int rdc_context_add_screened_electrostatics(rdc_context *ctx, int type1, int type2, double electrostatic_strength,
+                                            double inverse_screening_depth, double repulsion_strength,
+                                            double repulsion_distance, unsigned exponent, double cutoff);
+
+/* ReactionRegistry::addConversion / addDecay / addFusion / addFission / addEnzymatic
+ * (include/readdy/model/reactions/{Conversion,Decay,Fusion,Fission,Enzymatic}.h); *reaction_id is the
+ * reaction's index in registration order (Reaction.h:93-96) */
+int rdc_context_add_conversion(rdc_context *ctx, int type_from, int type_to, double rate, int *reaction_id);
+int rdc_context_add_decay(rdc_context *ctx, int type_from, double rate, int *reaction_id);
+int rdc_context_add_fusion(rdc_context *ctx, int type_from1, int type_from2, int type_to, double rate,
+                           double educt_distance, double weight1, double weight2, int *reaction_id);
+int rdc_context_add_fission(rdc_context *ctx, int type_from, int type_to1, int type_to2, double rate,
+                            double product_distance, double weight1, double weight2, int *reaction_id);
+int rdc_context_add_enzymatic(rdc_context *ctx, int type_catalyst, int type_from, int type_to, double rate,
+                              double educt_distance, int *reaction_id);
+
+/* TopologyRegistry::configureBondPotential / configureAnglePotential / configureTorsionPotential
+ * (include/readdy/api/PotentialConfiguration.h:136-161; lookups are reversal-symmetric) */
+int rdc_context_configure_harmonic_bond(rdc_context *ctx, int type1, int type2, double force_constant,
+                                        double length);
+int rdc_context_configure_harmonic_angle(rdc_context *ctx, int type1, int type2, int type3,
+                                         double force_constant, double equilibrium_angle);
+int rdc_context_configure_cosine_dihedral(rdc_context *ctx, int type1, int type2, int type3, int type4,
+                                          double force_constant, double multiplicity, double phi0);
+
+/* ---- model::Kernel + StateModel (include/readdy/model/{Kernel,StateModel}.h) ----------------- */
+/* KernelProvider::create("CUDA") with a copy of ctx (KernelProvider.cpp:183-189); seed keys every
+ * Philox stream of the system */
+int rdc_system_create(rdc_system **out, const rdc_context *ctx, uint64_t seed);
+int rdc_system_destroy(rdc_system *s);
+/* StateModel::addParticles (StateModel.h:69-117); writes the assigned ids if ids_out != NULL */
+int rdc_add_particles(rdc_system *s, int64_t n, const double *positions3, const int *types, uint64_t *ids_out);
+/* StateModel::addTopology with the graph's edges (local vertex indices); builds the bond, angle and
+ * dihedral term lists as GraphTopology::configure does
+ * (readdy/main/model/topologies/GraphTopology.cpp:59-143, include/graphs/bits/Graph_detail.h:39-76) */
+int rdc_add_topology(rdc_system *s, int64_t n, const double *positions3, const int *types, int64_t n_edges,
+                     const int64_t *edges2, uint64_t *ids_out);
+/* active particle count (StateModel::getParticles().size()) */
+int rdc_get_n_particles(rdc_system *s, int64_t *n);
+/* StateModel::getParticles: positions, types and ids of active particles; order is the device's
+ * cell-sorted storage order; any output may be NULL */
+int rdc_get_particles(rdc_system *s, int64_t capacity, double *positions3, int *types, uint64_t *ids,
+                      int64_t *n_out);
+/* Forces observable (CPUObservables.cpp): per-particle forces, same order as rdc_get_particles */
+int rdc_get_forces(rdc_system *s, int64_t capacity, double *forces3, uint64_t *ids, int64_t *n_out);
+/* StateModel::energy() after the last CalculateForces */
+int rdc_get_energy(rdc_system *s, double *energy);
+/* NParticles observable per type (kernels/cpu/src/observables/CPUObservables.cpp:153-171) */
+int rdc_count_types(rdc_system *s, int64_t *counts);
+/* ReactionCounts observable: performed events per reaction id since creation
+ * (kernels/cpu/src/CPUStateModel.cpp:126-144) */
+int rdc_get_reaction_counts(rdc_system *s, int n, int64_t *counts);
+/* particle capacity on the device (reaction products beyond it raise RDC_ERR_CAPACITY) */
+int rdc_reserve(rdc_system *s, int64_t capacity);
+/* cell-list tuning: cells per cutoff (the reference's cll_radius, KernelConfiguration.h:63) */
+int rdc_set_cell_radius(rdc_system *s, int radius);
+
+/* ---- ActionFactory actions (include/readdy/model/actions/Actions.h:81-453) -------------------- */
+/* InitializeKernel: Kernel::initialize, resets reaction counts (kernels/cpu/src/CPUKernel.cpp:63-83) */
+int rdc_initialize(rdc_system *s);
+/* CreateNeighborList(cutoff) = StateModel::initializeNeighborList (CPUStateModel.h:96-99) */
+int rdc_nl_create(rdc_system *s, double cutoff);
+/* UpdateNeighborList (CPUStateModel.h:101-103, CellLinkedList.cpp:230-247) */
+int rdc_nl_update(rdc_system *s);
+/* ClearNeighborList (CPUStateModel.h:170-172) */
+int rdc_nl_clear(rdc_system *s);
+/* CalculateForces (kernels/cpu/src/actions/CPUCalculateForces.cpp:46-212) */
+int rdc_calculate_forces(rdc_system *s);
+/* EulerBDIntegrator(dt) (kernels/cpu/src/actions/CPUEulerBDIntegrator.cpp:51-103) */
+int rdc_euler_bd_integrate(rdc_system *s, double dt);
+/* UncontrolledApproximation(dt) (kernels/cpu/src/actions/reactions/CPUUncontrolledApproximation.cpp:135-256) */
+int rdc_uncontrolled_approximation(rdc_system *s, double dt);
+/* Gillespie(dt) (kernels/cpu/src/actions/reactions/CPUGillespie.cpp:53-93) */
+int rdc_gillespie(rdc_system *s, double dt);
+/* SimulationLoop::run(n_steps) (include/readdy/api/SimulationLoop.h:256-306) on the device, captured
+ * in a CUDA graph.  Per-type counts are recorded every count_stride steps including t=0 when
+ * counts != NULL (n_types values per record, at most max_records records); *n_records receives the
+ * number written. */
+int rdc_run(rdc_system *s, int64_t n_steps, double dt, int handler, int64_t count_stride, int64_t *counts,
+            int64_t max_records, int64_t *n_records);
+/* neighbour pair set of the current cell list for one cutoff: every unordered pair of active
+ * in-box particles with d^2 < cutoff^2 (the consumers' contract, CPUCalculateForces.cpp:240-243),
+ * as (min id, max id) sorted ascending; parity/debug path */
+int rdc_nl_pairs(rdc_system *s, double cutoff, int64_t capacity, uint64_t *pairs2, int64_t *n_pairs);
+/* wait for the system's stream and report device-side status */
+int rdc_synchronize(rdc_system *s);
+
+/* ---- batched replicas (no reference counterpart: thousands of independent copies of one
+ *      Context advanced together, one fused launch per step) ------------------------------------ */
+/* n_replicas systems sharing ctx's species, potentials and reactions; boxes3 gives each replica's
+ * box (FP32-rounded), capacities its particle capacity */
+int rdc_batch_create(rdc_batch **out, const rdc_context *ctx, int n_replicas, const double *boxes3,
+                     const int64_t *capacities, uint64_t seed);
+int rdc_batch_destroy(rdc_batch *b);
+/* initial particles of every replica: offsets (n_replicas+1) into positions3/types */
+int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *positions3, const int *types);
+/* handler, time step and the cell-list knobs (cells per cutoff, threads per block) */
+int rdc_batch_configure(rdc_batch *b, int handler, double dt, int cell_radius, int threads_per_block);
+/* advance every replica n_steps; each step is one fused launch replayed from a CUDA graph */
+int rdc_batch_step(rdc_batch *b, int64_t n_steps);
+/* per-replica, per-type counts (n_replicas * n_types) */
+int rdc_batch_count_types(rdc_batch *b, int64_t *counts);
+/* active particles per replica */
+int rdc_batch_n_particles(rdc_batch *b, int64_t *n_per_replica);
+/* particles of one replica, same layout as rdc_get_particles */
+int rdc_batch_get_particles(rdc_batch *b, int replica, int64_t capacity, double *positions3, int *types,
+                            uint64_t *ids, int64_t *n_out);
+int rdc_batch_synchronize(rdc_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* READDY_CUDA_H */

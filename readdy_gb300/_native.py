@@ -1,0 +1,130 @@
+"""ctypes binding of libreaddy_cuda_core.so (the C ABI declared in include/readdy_cuda.h).
+
+There is no CPU fallback: if the library cannot be built or loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+RDC_OK = 0
+RDC_ERR_INVALID_ARGUMENT = 1
+RDC_ERR_LOGIC = 2
+RDC_ERR_RUNTIME = 3
+RDC_ERR_CUDA = 4
+RDC_ERR_CAPACITY = 5
+
+UNCONTROLLED_APPROXIMATION = 0
+GILLESPIE = 1
+
+_lib = None
+_lock = threading.Lock()
+
+
+class CudaKernelError(RuntimeError):
+    """A CUDA runtime failure or a device-side capacity/status error."""
+
+
+class CapacityError(CudaKernelError):
+    pass
+
+
+def _sig(lib):
+    d, i, u64, i64, vp = C.c_double, C.c_int, C.c_uint64, C.c_int64, C.c_void_p
+    P = C.POINTER
+    vpp = P(vp)
+    table = {
+        "rdc_last_error": (C.c_char_p, []),
+        "rdc_version": (i, []),
+        "rdc_kernel_name": (C.c_char_p, []),
+        "rdc_context_create": (i, [vpp, P(d), P(i), d, i, P(d)]),
+        "rdc_context_destroy": (i, [vp]),
+        "rdc_context_max_cutoff": (i, [vp, P(d)]),
+        "rdc_context_add_harmonic_repulsion": (i, [vp, i, i, d, d]),
+        "rdc_context_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
+        "rdc_context_add_lennard_jones": (i, [vp, i, i, C.c_uint, C.c_uint, d, i, d, d]),
+        "rdc_context_add_screened_electrostatics": (i, [vp, i, i, d, d, d, d, C.c_uint, d]),
+        "rdc_context_add_conversion": (i, [vp, i, i, d, P(i)]),
+        "rdc_context_add_decay": (i, [vp, i, d, P(i)]),
+        "rdc_context_add_fusion": (i, [vp, i, i, i, d, d, d, d, P(i)]),
+        "rdc_context_add_fission": (i, [vp, i, i, i, d, d, d, d, P(i)]),
+        "rdc_context_add_enzymatic": (i, [vp, i, i, i, d, d, P(i)]),
+        "rdc_context_configure_harmonic_bond": (i, [vp, i, i, d, d]),
+        "rdc_context_configure_harmonic_angle": (i, [vp, i, i, i, d, d]),
+        "rdc_context_configure_cosine_dihedral": (i, [vp, i, i, i, i, d, d, d]),
+        "rdc_system_create": (i, [vpp, vp, u64]),
+        "rdc_system_destroy": (i, [vp]),
+        "rdc_add_particles": (i, [vp, i64, P(d), P(i), P(u64)]),
+        "rdc_add_topology": (i, [vp, i64, P(d), P(i), i64, P(i64), P(u64)]),
+        "rdc_get_n_particles": (i, [vp, P(i64)]),
+        "rdc_get_particles": (i, [vp, i64, P(d), P(i), P(u64), P(i64)]),
+        "rdc_get_forces": (i, [vp, i64, P(d), P(u64), P(i64)]),
+        "rdc_get_energy": (i, [vp, P(d)]),
+        "rdc_count_types": (i, [vp, P(i64)]),
+        "rdc_get_reaction_counts": (i, [vp, i, P(i64)]),
+        "rdc_reserve": (i, [vp, i64]),
+        "rdc_set_cell_radius": (i, [vp, i]),
+        "rdc_initialize": (i, [vp]),
+        "rdc_nl_create": (i, [vp, d]),
+        "rdc_nl_update": (i, [vp]),
+        "rdc_nl_clear": (i, [vp]),
+        "rdc_calculate_forces": (i, [vp]),
+        "rdc_euler_bd_integrate": (i, [vp, d]),
+        "rdc_uncontrolled_approximation": (i, [vp, d]),
+        "rdc_gillespie": (i, [vp, d]),
+        "rdc_run": (i, [vp, i64, d, i, i64, P(i64), i64, P(i64)]),
+        "rdc_nl_pairs": (i, [vp, d, i64, P(u64), P(i64)]),
+        "rdc_synchronize": (i, [vp]),
+        "rdc_batch_create": (i, [vpp, vp, i, P(d), P(i64), u64]),
+        "rdc_batch_destroy": (i, [vp]),
+        "rdc_batch_set_particles": (i, [vp, P(i64), P(d), P(i)]),
+        "rdc_batch_configure": (i, [vp, i, d, i, i]),
+        "rdc_batch_step": (i, [vp, i64]),
+        "rdc_batch_count_types": (i, [vp, P(i64)]),
+        "rdc_batch_n_particles": (i, [vp, P(i64)]),
+        "rdc_batch_get_particles": (i, [vp, i, i64, P(d), P(i), P(u64), P(i64)]),
+        "rdc_batch_synchronize": (i, [vp]),
+    }
+    for name, (res, args) in table.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+EXPORTED = None  # filled from the header by tests
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the CUDA core, building it in-tree first if needed (nvcc for sm_103a)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing:
+            _build.build()
+        if not os.path.exists(path):
+            raise CudaKernelError(f"CUDA core library missing: {path} (run readdy_gb300.build.build())")
+        _lib = _sig(C.CDLL(path))
+        return _lib
+
+
+def check(rc: int):
+    if rc == RDC_OK:
+        return
+    msg = _lib.rdc_last_error().decode() if _lib is not None else "unknown error"
+    if rc == RDC_ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    if rc == RDC_ERR_LOGIC:
+        raise RuntimeError(msg)
+    if rc == RDC_ERR_CAPACITY:
+        raise CapacityError(msg)
+    raise CudaKernelError(msg)

@@ -1,0 +1,112 @@
+"""Batched replicas: thousands of independent copies of one Context advanced by one fused launch per
+step (rdc_batch_* in include/readdy_cuda.h), and the autotuner that picks its launch knobs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _native as N
+from .kernel import Context
+
+_M64 = (1 << 64) - 1
+
+
+def _splitmix64(x: int) -> int:
+    x = (x + 0x9E3779B97F4A7C15) & _M64
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & _M64
+    return x ^ (x >> 31)
+
+
+def replica_seed(seed: int, replica: int) -> int:
+    """Seed of replica `replica` inside a batch created with `seed`; a CUDAKernel created with this
+    seed runs the same random streams as that replica."""
+    return _splitmix64((seed ^ ((0x5DEECE66D * (replica + 1)) & _M64)) & _M64)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class ReplicaBatch:
+    def __init__(self, context: Context, boxes, capacities, seed: int = 0):
+        self._lib = N.load()
+        self.context = context
+        boxes = np.ascontiguousarray(boxes, dtype=np.float64).reshape(-1, 3)
+        caps = np.ascontiguousarray(capacities, dtype=np.int64)
+        assert len(caps) == len(boxes)
+        self.n_replicas = len(boxes)
+        h = C.c_void_p()
+        N.check(self._lib.rdc_batch_create(C.byref(h), context.handle, self.n_replicas, _p(boxes, C.c_double),
+                                           _p(caps, C.c_int64), int(seed) & _M64))
+        self._h = h
+        self.seed = seed
+        self.boxes = boxes
+        self.capacities = caps
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.rdc_batch_destroy(h)
+            self._h = None
+
+    def set_particles(self, positions_per_replica, types_per_replica):
+        offs = np.zeros(self.n_replicas + 1, np.int64)
+        offs[1:] = np.cumsum([len(p) for p in positions_per_replica])
+        pos = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1, 3)
+                                                   for p in positions_per_replica]))
+        types = np.ascontiguousarray(np.concatenate([np.asarray(t, np.int32) for t in types_per_replica]))
+        N.check(self._lib.rdc_batch_set_particles(self._h, _p(offs, C.c_int64), _p(pos, C.c_double),
+                                                  _p(types, C.c_int)))
+
+    def configure(self, handler=N.GILLESPIE, dt=1e-3, cell_radius=1, threads_per_block=256):
+        N.check(self._lib.rdc_batch_configure(self._h, int(handler), float(dt), int(cell_radius),
+                                              int(threads_per_block)))
+        self.handler, self.dt, self.cell_radius, self.threads_per_block = handler, dt, cell_radius, threads_per_block
+
+    def step(self, n_steps=1):
+        N.check(self._lib.rdc_batch_step(self._h, int(n_steps)))
+
+    def synchronize(self):
+        N.check(self._lib.rdc_batch_synchronize(self._h))
+
+    def count_types(self):
+        out = np.zeros((self.n_replicas, self.context.n_types), np.int64)
+        N.check(self._lib.rdc_batch_count_types(self._h, _p(out, C.c_int64)))
+        return out
+
+    def n_particles(self):
+        out = np.zeros(self.n_replicas, np.int64)
+        N.check(self._lib.rdc_batch_n_particles(self._h, _p(out, C.c_int64)))
+        return out
+
+    def get_particles(self, replica):
+        n = int(self.n_particles()[replica])
+        pos = np.zeros((n, 3)); t = np.zeros(n, np.int32); ids = np.zeros(n, np.uint64)
+        got = C.c_int64()
+        N.check(self._lib.rdc_batch_get_particles(self._h, int(replica), n, _p(pos, C.c_double), _p(t, C.c_int),
+                                                  _p(ids, C.c_uint64), C.byref(got)))
+        return pos[:got.value], t[:got.value], ids[:got.value]
+
+
+def autotune(make_batch, steps=20, radii=(1, 2), threads=(128, 256, 512), handler=N.GILLESPIE, dt=1e-3):
+    """Times short runs of freshly made batches over cell radius x threads per block and returns the
+    fastest setting as a dict.  `make_batch()` must return a batch with its particles set."""
+    best = None
+    for r in radii:
+        for t in threads:
+            b = make_batch()
+            b.configure(handler=handler, dt=dt, cell_radius=r, threads_per_block=t)
+            b.step(2)
+            b.synchronize()
+            t0 = time.perf_counter()
+            b.step(steps)
+            b.synchronize()
+            dtm = (time.perf_counter() - t0) / steps
+            if best is None or dtm < best["s_per_step"]:
+                best = dict(cell_radius=r, threads_per_block=t, s_per_step=dtm)
+            del b
+    return best

@@ -1,0 +1,1165 @@
+// C ABI of libreaddy_cuda_core.so (include/readdy_cuda.h) and the host orchestration of the
+// per-system path: context registries, device tables, particle storage, the action sequence of
+// SimulationLoop::run (include/readdy/api/SimulationLoop.h:256-306) captured in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/readdy_cuda.h"
+#include "rdc_host.h"
+
+using namespace rdc;
+
+namespace {
+thread_local std::string g_err;
+
+struct InvalidArgument : std::invalid_argument {
+    using std::invalid_argument::invalid_argument;
+};
+struct LogicError : std::logic_error {
+    using std::logic_error::logic_error;
+};
+
+template <typename F>
+int guarded(F &&f) {
+    try {
+        f();
+        g_err.clear();
+        return RDC_OK;
+    } catch (const CapacityError &e) {
+        g_err = e.what();
+        return RDC_ERR_CAPACITY;
+    } catch (const CudaError &e) {
+        g_err = e.what();
+        return RDC_ERR_CUDA;
+    } catch (const std::invalid_argument &e) {
+        g_err = e.what();
+        return RDC_ERR_INVALID_ARGUMENT;
+    } catch (const std::logic_error &e) {
+        g_err = e.what();
+        return RDC_ERR_LOGIC;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return RDC_ERR_RUNTIME;
+    }
+}
+
+void require(bool c, const std::string &msg) {
+    if (!c) throw InvalidArgument(msg);
+}
+
+template <typename T>
+T *dalloc(size_t n) {
+    void *p = nullptr;
+    if (n == 0) n = 1;
+    RDC_CUDA(cudaMalloc(&p, n * sizeof(T)));
+    return static_cast<T *>(p);
+}
+template <typename T>
+void dfree(T *&p) {
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+uint64_t coin_threshold(double rate, double dt) {
+    // acceptance probability 1 - exp(-k dt) (ReactionUtils.h:64-71) as a 64-bit threshold
+    const double p = 1.0 - std::exp(-rate * dt);
+    if (!(p > 0)) return 0;
+    const double x = p * 18446744073709551616.0;
+    if (x >= 18446744073709551615.0) return ~0ull;
+    return (uint64_t)x;
+}
+
+float band_for(double cutoff, const float L[3]) {
+    const double Lmax = std::max(L[0], std::max(L[1], L[2]));
+    const double c2 = cutoff * cutoff;
+    return (float)(1e-5 * c2 + 4e-6 * Lmax * cutoff);
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------------------
+namespace rdc {
+
+double ContextData::max_cutoff() const {
+    double c = 0;
+    for (auto &p : pots) c = std::max(c, p.cutoff);
+    for (auto &r : reactions)
+        if (r.n_educts == 2) c = std::max(c, r.educt_distance);
+    return c;
+}
+
+bool ContextData::structural_reactions() const {
+    for (auto &r : reactions)
+        if (r.kind == R_FUSION || r.kind == R_FISSION || r.kind == R_DECAY) return true;
+    return false;
+}
+
+Geo make_geo(const double box[3], const int pbc[3], double cutoff, int radius) {
+    Geo g{};
+    double Lmax = 0;
+    for (int d = 0; d < 3; ++d) {
+        g.L[d] = (float)box[d];
+        g.hL[d] = g.L[d] * 0.5f;
+        g.Ld[d] = (double)g.L[d];
+        g.pbc[d] = pbc[d] ? 1 : 0;
+        Lmax = std::max(Lmax, g.Ld[d]);
+    }
+    g.exact_always = 0;
+    for (int d = 0; d < 3; ++d) {
+        int dims = 1;
+        if (cutoff > 0) {
+            // cell width >= cutoff/radius with a margin covering FP32 binning error
+            const double w = cutoff / radius + std::ldexp(g.Ld[d], -19) / radius + 1e-6 * cutoff;
+            dims = (int)std::max(1.0, std::floor(g.Ld[d] / w));
+        }
+        g.dims[d] = dims;
+        g.invW[d] = (float)((double)dims / g.Ld[d]);
+        if (g.pbc[d] && cutoff > 0.45 * g.Ld[d]) g.exact_always = 1;
+    }
+    const long long nc = (long long)g.dims[0] * g.dims[1] * g.dims[2];
+    if (nc > (1LL << 28)) throw InvalidArgument("cell grid too large for the box and cutoff");
+    g.ncells = (int)nc;
+    return g;
+}
+
+void set_time_step(const ContextData &c, double dt, Tables &t) {
+    for (int i = 0; i < c.ntypes; ++i) {
+        t.bd_drift[i] = (float)(c.D[i] * dt / c.kbt);
+        t.bd_scale[i] = (float)std::sqrt(2.0 * c.D[i] * dt);
+    }
+    for (int r = 0; r < t.nreactions; ++r) t.reactions[r].coin_threshold = coin_threshold(t.reactions[r].rate, dt);
+}
+
+void build_tables(const ContextData &c, const double box[3], double dt, Tables &t) {
+    std::memset(&t, 0, sizeof(Tables));
+    const int T = c.ntypes;
+    t.ntypes = T;
+    float L[3] = {(float)box[0], (float)box[1], (float)box[2]};
+    // pair potentials grouped by unordered type pair, registration order kept within a pair
+    std::map<std::pair<int, int>, std::vector<const HostPot *>> groups;
+    for (auto &p : c.pots) groups[{std::min(p.t1, p.t2), std::max(p.t1, p.t2)}].push_back(&p);
+    int np = 0;
+    for (auto &kv : groups) {
+        const int first = np;
+        for (auto *hp : kv.second) {
+            if (np >= MAX_PAIR_POTENTIALS) throw InvalidArgument("too many pair potentials");
+            t.pots[np] = hp->pot;
+            t.pots[np].band = band_for(hp->cutoff, L);
+            ++np;
+        }
+        const int cnt = np - first;
+        if (cnt > 255) throw InvalidArgument("too many potentials for one type pair");
+        const int v = (first << 8) | cnt;
+        t.pair_tab[kv.first.first * T + kv.first.second] = v;
+        t.pair_tab[kv.first.second * T + kv.first.first] = v;
+    }
+    t.npots = np;
+    // reactions
+    t.nreactions = (int)c.reactions.size();
+    if (t.nreactions > MAX_REACTIONS) throw InvalidArgument("too many reactions");
+    for (int r = 0; r < t.nreactions; ++r) {
+        const auto &h = c.reactions[r];
+        ReactionDev &d = t.reactions[r];
+        d.kind = h.kind;
+        d.n_educts = h.n_educts;
+        d.n_products = h.n_products;
+        d.educt[0] = h.educt[0]; d.educt[1] = h.educt[1];
+        d.product[0] = h.product[0]; d.product[1] = h.product[1];
+        d.id = r;
+        d.w1 = (float)h.w1; d.w2 = (float)h.w2;
+        d.product_distance = (float)h.product_distance;
+        d.educt_distance2 = h.educt_distance * h.educt_distance;
+        d.educt_distance2f = (float)d.educt_distance2;
+        d.band = band_for(h.educt_distance, L);
+        d.rate = h.rate;
+        d.inv_rate = h.rate > 0 ? (float)(1.0 / h.rate) : 0.f;
+    }
+    std::vector<std::vector<int>> o1(T);
+    std::map<std::pair<int, int>, std::vector<int>> o2;
+    for (int r = 0; r < t.nreactions; ++r) {
+        const auto &h = c.reactions[r];
+        if (h.n_educts == 1) o1[h.educt[0]].push_back(r);
+        else o2[{std::min(h.educt[0], h.educt[1]), std::max(h.educt[0], h.educt[1])}].push_back(r);
+    }
+    int k = 0;
+    for (int ty = 0; ty < T; ++ty) {
+        t.o1_tab[ty] = o1[ty].empty() ? 0 : ((k << 8) | (int)o1[ty].size());
+        for (int r : o1[ty]) t.o1_list[k++] = r;
+    }
+    k = 0;
+    for (auto &kv : o2) {
+        const int v = (k << 8) | (int)kv.second.size();
+        t.o2_tab[kv.first.first * T + kv.first.second] = v;
+        t.o2_tab[kv.first.second * T + kv.first.first] = v;
+        t.o2_any[kv.first.first] = 1;
+        t.o2_any[kv.first.second] = 1;
+        t.has_o2_any = 1;
+        for (int r : kv.second) t.o2_list[k++] = r;
+    }
+    set_time_step(c, dt, t);
+}
+
+}  // namespace rdc
+
+struct rdc_context {
+    ContextData d;
+};
+
+namespace rdc {
+const ContextData &context_data(const rdc_context *ctx) { return ctx->d; }
+void set_last_error(const std::string &m) { g_err = m; }
+}  // namespace rdc
+
+// ---------------------------------------------------------------------------------------------
+// system
+// ---------------------------------------------------------------------------------------------
+struct Topology {
+    // terms refer to topology slots
+    std::vector<int4> bonds;
+    std::vector<float2> bond_par;
+    std::vector<int4> angles;
+    std::vector<float2> angle_par;
+    std::vector<int4> dihedrals;
+    std::vector<float4> dih_par;
+};
+
+struct rdc_system {
+    ContextData ctx;
+    uint64_t seed = 0;
+    cudaStream_t stream = nullptr;
+    SysDev d{};
+    Tables *tab_dev = nullptr;
+    Tables tab{};
+    double tab_dt = 0;
+    int radius = 1;
+    double nl_cutoff = 0;
+    bool nl_ready = false;
+    bool forces_live = false;
+    int n_top = 0;
+    Topology top;
+    int *top_off_dev = nullptr, *top_terms_dev = nullptr;
+    int4 *bond_idx_dev = nullptr, *angle_idx_dev = nullptr, *dih_idx_dev = nullptr;
+    float2 *bond_par_dev = nullptr, *angle_par_dev = nullptr;
+    float4 *dih_par_dev = nullptr;
+    int top_capacity = 0;
+    int ncells_alloc = -1;
+    unsigned long long *count_buf = nullptr;  // MAX_TYPES scratch for count_types
+    int *pairs_n = nullptr;
+    // graph of the run loop (captured per run: device pointers and the recording base are baked in)
+    cudaGraphExec_t graph = nullptr;
+
+    ~rdc_system() { release(); }
+
+    void release() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        dfree(d.pos); dfree(d.id); dfree(d.tslot); dfree(d.force);
+        dfree(d.pos_alt); dfree(d.id_alt); dfree(d.tslot_alt); dfree(d.force_alt);
+        dfree(d.bin); dfree(d.rank); dfree(d.src);
+        dfree(d.cnt); dfree(d.start); dfree(d.scan_blocks);
+        dfree(d.tloc); dfree(d.counters); dfree(d.step);
+        dfree(d.events); dfree(d.claim); dfree(d.taken); dfree(d.reaction_counts);
+        dfree(d.epart); dfree(d.energy); dfree(d.counts_ring);
+        dfree(tab_dev); dfree(count_buf); dfree(pairs_n);
+        dfree(top_off_dev); dfree(top_terms_dev);
+        dfree(bond_idx_dev); dfree(angle_idx_dev); dfree(dih_idx_dev);
+        dfree(bond_par_dev); dfree(angle_par_dev); dfree(dih_par_dev);
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+
+    void sync() { RDC_CUDA(cudaStreamSynchronize(stream)); }
+
+    void read_counters(int *c) {
+        RDC_CUDA(cudaMemcpyAsync(c, d.counters, sizeof(int) * C_COUNT, cudaMemcpyDeviceToHost, stream));
+        sync();
+    }
+
+    // raise device-side status as an error and clear it
+    void check_status() {
+        int c[C_COUNT];
+        read_counters(c);
+        const int st = c[C_STATUS];
+        if (st) {
+            int zero = 0;
+            RDC_CUDA(cudaMemcpyAsync(d.counters + C_STATUS, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
+            sync();
+            if (st & ST_CAPACITY) throw CapacityError("particle capacity exceeded by reaction products (rdc_reserve)");
+            if (st & ST_EVENTS) throw CapacityError("reaction event buffer overflow");
+            if (st & ST_ID_OVERFLOW) throw std::runtime_error("32-bit particle id space exhausted");
+            if (st & ST_RESOLVE_ROUNDS) throw std::runtime_error("reaction conflict resolution did not converge");
+            throw std::runtime_error("device status " + std::to_string(st));
+        }
+    }
+
+    void init(const ContextData &c, uint64_t s) {
+        ctx = c;
+        seed = s;
+        RDC_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        init_kernel_attributes();
+        tab_dev = dalloc<Tables>(1);
+        build_tables(ctx, ctx.box, 0.0, tab);
+        tab_dt = 0;
+        upload_tables();
+        d.tab = tab_dev;
+        d.seed = seed;
+        d.radius = radius;
+        d.counters = dalloc<int>(C_COUNT);
+        RDC_CUDA(cudaMemsetAsync(d.counters, 0, sizeof(int) * C_COUNT, stream));
+        d.step = dalloc<uint64_t>(2);
+        RDC_CUDA(cudaMemsetAsync(d.step, 0, sizeof(uint64_t) * 2, stream));
+        d.reaction_counts = dalloc<unsigned long long>(MAX_REACTIONS);
+        RDC_CUDA(cudaMemsetAsync(d.reaction_counts, 0, sizeof(unsigned long long) * MAX_REACTIONS, stream));
+        d.epart = dalloc<double>(FORCE_BLOCKS + BONDED_BLOCKS);
+        RDC_CUDA(cudaMemsetAsync(d.epart, 0, sizeof(double) * (FORCE_BLOCKS + BONDED_BLOCKS), stream));
+        d.energy = dalloc<double>(1);
+        RDC_CUDA(cudaMemsetAsync(d.energy, 0, sizeof(double), stream));
+        d.event_capacity = 1 << 16;
+        d.events = dalloc<EventRec>(d.event_capacity);
+        count_buf = dalloc<unsigned long long>(MAX_TYPES);
+        pairs_n = dalloc<int>(1);
+        d.geo = make_geo(ctx.box, ctx.pbc, 0.0, 1);
+        alloc_cells(d.geo.ncells);
+        reserve(1024);
+        sync();
+    }
+
+    void upload_tables() {
+        RDC_CUDA(cudaMemcpyAsync(tab_dev, &tab, sizeof(Tables), cudaMemcpyHostToDevice, stream));
+    }
+
+    void set_dt(double dt) {
+        if (dt != tab_dt) {
+            set_time_step(ctx, dt, tab);
+            tab_dt = dt;
+            upload_tables();
+        }
+    }
+
+    void alloc_cells(int ncells) {
+        if (ncells == ncells_alloc) return;
+        dfree(d.cnt); dfree(d.start); dfree(d.scan_blocks);
+        d.cnt = dalloc<int>(ncells + 2);
+        d.start = dalloc<int>(ncells + 3);
+        d.scan_blocks = dalloc<int>(scan_block_count(ncells + 2) + 1);
+        RDC_CUDA(cudaMemsetAsync(d.cnt, 0, sizeof(int) * (ncells + 2), stream));
+        RDC_CUDA(cudaMemsetAsync(d.start, 0, sizeof(int) * (ncells + 3), stream));
+        ncells_alloc = ncells;
+        invalidate_graph();
+    }
+
+    void invalidate_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+
+    // grow the per-particle arrays (host-synchronous)
+    void reserve(int cap) {
+        if (cap <= d.capacity) return;
+        int c[C_COUNT] = {0};
+        if (d.capacity > 0) read_counters(c);
+        const int n = c[C_N_TOTAL];
+        auto grow = [&](auto *&p, int keep) {
+            using T = std::remove_reference_t<decltype(*p)>;
+            T *np = dalloc<T>(cap);
+            if (p && keep > 0) RDC_CUDA(cudaMemcpyAsync(np, p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, stream));
+            sync();
+            dfree(p);
+            p = np;
+        };
+        grow(d.pos, n); grow(d.id, n); grow(d.tslot, n); grow(d.force, n);
+        grow(d.pos_alt, 0); grow(d.id_alt, 0); grow(d.tslot_alt, 0); grow(d.force_alt, 0);
+        grow(d.bin, 0); grow(d.rank, 0); grow(d.src, 0);
+        grow(d.claim, 0); grow(d.taken, 0);
+        RDC_CUDA(cudaMemsetAsync(d.claim, 0x7f, sizeof(int) * cap, stream));
+        RDC_CUDA(cudaMemsetAsync(d.taken, 0, sizeof(int) * cap, stream));
+        d.capacity = cap;
+        sync();
+        invalidate_graph();
+    }
+
+    void swap_buffers() {
+        std::swap(d.pos, d.pos_alt);
+        std::swap(d.id, d.id_alt);
+        std::swap(d.tslot, d.tslot_alt);
+        std::swap(d.force, d.force_alt);
+    }
+
+    // append particles (host-synchronous): they join the cell list at the next sort
+    void append(int64_t n, const double *pos, const int *types, const int *tslots, uint64_t *ids_out) {
+        if (n <= 0) return;
+        for (int64_t i = 0; i < n; ++i)
+            if (types[i] < 0 || types[i] >= ctx.ntypes) throw InvalidArgument("particle type out of range");
+        int c[C_COUNT];
+        read_counters(c);
+        const int64_t need = (int64_t)c[C_N_TOTAL] + n;
+        if (need > INT_MAX / 2) throw InvalidArgument("too many particles");
+        if (need > d.capacity) {
+            int cap = std::max(d.capacity, 1024);
+            while (cap < need) cap *= 2;
+            reserve(cap);
+        }
+        std::vector<float4> hp(n);
+        std::vector<int> ht(n);
+        for (int64_t i = 0; i < n; ++i) {
+            float4 p;
+            p.x = (float)pos[3 * i]; p.y = (float)pos[3 * i + 1]; p.z = (float)pos[3 * i + 2];
+            int ty = types[i];
+            std::memcpy(&p.w, &ty, 4);
+            hp[i] = p;
+            ht[i] = tslots ? tslots[i] : -1;
+        }
+        const int base = c[C_N_TOTAL];
+        RDC_CUDA(cudaMemcpyAsync(d.pos + base, hp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, stream));
+        RDC_CUDA(cudaMemcpyAsync(d.tslot + base, ht.data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream));
+        RDC_CUDA(cudaMemsetAsync(d.force + base, 0, sizeof(float4) * n, stream));
+        launch_fill_ids(d.id + base, (uint32_t)c[C_NEXT_ID], (int)n, stream);
+        int upd[2] = {(int)need, c[C_NEXT_ID] + (int)n};
+        RDC_CUDA(cudaMemcpyAsync(d.counters + C_N_TOTAL, &upd[0], sizeof(int), cudaMemcpyHostToDevice, stream));
+        RDC_CUDA(cudaMemcpyAsync(d.counters + C_NEXT_ID, &upd[1], sizeof(int), cudaMemcpyHostToDevice, stream));
+        if (ids_out)
+            for (int64_t i = 0; i < n; ++i) ids_out[i] = (uint64_t)(c[C_NEXT_ID] + i);
+        sync();
+        // without a neighbour list the storage is one bin; keep the new particles reachable
+        if (!nl_ready) {
+            d.geo = make_geo(ctx.box, ctx.pbc, 0.0, radius);
+            alloc_cells(d.geo.ncells);
+            launch_bin(d, stream);
+            launch_sort(d, true, stream);
+            swap_buffers();
+            sync();
+        }
+    }
+
+    // ---- actions ----
+    void nl_create(double cutoff) {
+        if (!(cutoff > 0)) throw LogicError("The cutoff distance for setting up a neighbor list must be > 0");
+        nl_cutoff = cutoff;
+        d.geo = make_geo(ctx.box, ctx.pbc, cutoff, radius);
+        d.radius = radius;
+        alloc_cells(d.geo.ncells);
+        build_tables(ctx, ctx.box, tab_dt, tab);
+        upload_tables();
+        nl_ready = true;
+        invalidate_graph();
+        nl_update();
+    }
+    void nl_update() {
+        if (!nl_ready) throw LogicError("Attempting to fill neighborlist bins, but cell structure is not set up yet");
+        launch_bin(d, stream);
+        launch_sort(d, forces_live, stream);
+        swap_buffers();
+    }
+    void nl_clear() {
+        nl_ready = false;
+        nl_cutoff = 0;
+    }
+    void calculate_forces() {
+        if (!ctx.pots.empty() && !nl_ready) throw LogicError("calculate forces: the neighbor list is not set up");
+        launch_forces(d, true, n_top > 0, stream);
+        forces_live = true;
+    }
+    void integrate(double dt) {
+        set_dt(dt);
+        // integrate + bin: the bins are refreshed at the next nl_update, so only integrate here
+        integrate_only();
+        forces_live = false;
+    }
+    void integrate_only();
+    void react(double dt, int handler) {
+        if (ctx.reactions.empty()) return;
+        if (!nl_ready) throw LogicError("reactions: the neighbor list is not set up");
+        set_dt(dt);
+        launch_events(d, handler, stream);
+        launch_resolve_apply(d, handler, stream);
+        if (ctx.structural_reactions()) {
+            // reaction products must be in the cell list before the next consumer
+            launch_bin(d, stream);
+            launch_sort(d, false, stream);
+            swap_buffers();
+        }
+    }
+
+    // ---- topology ----
+    void add_topology(int64_t n, const double *pos, const int *types, int64_t n_edges, const int64_t *edges,
+                      uint64_t *ids_out);
+    void upload_topology();
+
+    // ---- SimulationLoop::run ----
+    void run(int64_t n_steps, double dt, int handler, int64_t stride, int64_t *counts, int64_t max_rec,
+             int64_t *n_rec);
+    void step_sequence(int handler, bool reactions, bool structural, int nsteps);
+};
+
+void rdc_system::integrate_only() {
+    // k_integrate_bin with binning into the count array; the bin results are discarded by the
+    // next nl_update, which re-bins. Counting here keeps the launch identical to the fused one.
+    launch_integrate_bin(d, true, stream);
+}
+
+// findNTuples over one topology graph (include/graphs/bits/Graph_detail.h:39-76) and the type-tuple
+// lookup of GraphTopology::configure (readdy/main/model/topologies/GraphTopology.cpp:59-143)
+void rdc_system::add_topology(int64_t n, const double *pos, const int *types, int64_t n_edges, const int64_t *edges,
+                              uint64_t *ids_out) {
+    require(n > 0, "topology needs particles");
+    std::vector<std::vector<int>> adj(n);
+    for (int64_t e = 0; e < n_edges; ++e) {
+        const int64_t a = edges[2 * e], b = edges[2 * e + 1];
+        require(a >= 0 && b >= 0 && a < n && b < n && a != b, "bad topology edge");
+        adj[a].push_back((int)b);
+        adj[b].push_back((int)a);
+    }
+    const int base = n_top;
+    auto ty = [&](int v) { return types[v]; };
+    std::vector<char> visited(n, 0);
+    for (int v1 = 0; v1 < n; ++v1) {
+        visited[v1] = 1;
+        for (int nb : adj[v1]) {
+            if (!visited[nb]) {
+                bool found = false;
+                for (auto &c : ctx.bonds) {
+                    if ((c.t1 == ty(v1) && c.t2 == ty(nb)) || (c.t1 == ty(nb) && c.t2 == ty(v1))) {
+                        top.bonds.push_back(make_int4(base + v1, base + nb, 0, 0));
+                        top.bond_par.push_back(make_float2((float)c.k, (float)c.l0));
+                        found = true;
+                    }
+                }
+                if (!found)
+                    throw InvalidArgument("The edge " + std::to_string(v1) + " -- " + std::to_string(nb) +
+                                          " has no bond configured!");
+                for (int q1 : adj[v1]) {
+                    if (q1 == nb) continue;
+                    for (int q2 : adj[nb]) {
+                        if (q2 == v1 || q2 == q1) continue;
+                        const int tt[4] = {ty(q1), ty(v1), ty(nb), ty(q2)};
+                        for (auto &c : ctx.dihedrals) {
+                            const bool fwd = c.t1 == tt[0] && c.t2 == tt[1] && c.t3 == tt[2] && c.t4 == tt[3];
+                            const bool bwd = c.t1 == tt[3] && c.t2 == tt[2] && c.t3 == tt[1] && c.t4 == tt[0];
+                            if (fwd || bwd) {
+                                top.dihedrals.push_back(make_int4(base + q1, base + v1, base + nb, base + q2));
+                                top.dih_par.push_back(make_float4((float)c.k, (float)c.mult, (float)c.phi0, 0.f));
+                            }
+                        }
+                    }
+                }
+            }
+            for (int nb2 : adj[v1]) {
+                if (nb2 != nb && nb2 < nb) {
+                    const int tt[3] = {ty(nb2), ty(v1), ty(nb)};
+                    for (auto &c : ctx.angles) {
+                        const bool fwd = c.t1 == tt[0] && c.t2 == tt[1] && c.t3 == tt[2];
+                        const bool bwd = c.t1 == tt[2] && c.t2 == tt[1] && c.t3 == tt[0];
+                        if (fwd || bwd) {
+                            top.angles.push_back(make_int4(base + nb2, base + v1, base + nb, 0));
+                            top.angle_par.push_back(make_float2((float)c.k, (float)c.theta0));
+                        }
+                    }
+                }
+            }
+        }
+    }
+    std::vector<int> slots(n);
+    for (int64_t i = 0; i < n; ++i) slots[i] = base + (int)i;
+    n_top += (int)n;
+    append(n, pos, types, slots.data(), ids_out);
+    upload_topology();
+}
+
+void rdc_system::upload_topology() {
+    // CSR: per topology slot, every (kind, role, term) it takes part in
+    std::vector<std::vector<int>> per(n_top);
+    for (size_t i = 0; i < top.bonds.size(); ++i) {
+        per[top.bonds[i].x].push_back((0 << 28) | (0 << 24) | (int)i);
+        per[top.bonds[i].y].push_back((0 << 28) | (1 << 24) | (int)i);
+    }
+    for (size_t i = 0; i < top.angles.size(); ++i) {
+        per[top.angles[i].x].push_back((1 << 28) | (0 << 24) | (int)i);
+        per[top.angles[i].y].push_back((1 << 28) | (1 << 24) | (int)i);
+        per[top.angles[i].z].push_back((1 << 28) | (2 << 24) | (int)i);
+    }
+    for (size_t i = 0; i < top.dihedrals.size(); ++i) {
+        per[top.dihedrals[i].x].push_back((2 << 28) | (0 << 24) | (int)i);
+        per[top.dihedrals[i].y].push_back((2 << 28) | (1 << 24) | (int)i);
+        per[top.dihedrals[i].z].push_back((2 << 28) | (2 << 24) | (int)i);
+        per[top.dihedrals[i].w].push_back((2 << 28) | (3 << 24) | (int)i);
+    }
+    if (top.bonds.size() >= (1u << 24) || top.angles.size() >= (1u << 24) || top.dihedrals.size() >= (1u << 24))
+        throw InvalidArgument("too many bonded terms");
+    std::vector<int> off(n_top + 1, 0), terms;
+    for (int t = 0; t < n_top; ++t) {
+        off[t + 1] = off[t] + (int)per[t].size();
+        terms.insert(terms.end(), per[t].begin(), per[t].end());
+    }
+    auto up = [&](auto *&dptr, const auto &vec) {
+        using T = std::remove_reference_t<decltype(*dptr)>;
+        dfree(dptr);
+        dptr = dalloc<T>(vec.size());
+        if (!vec.empty())
+            RDC_CUDA(cudaMemcpyAsync(dptr, vec.data(), sizeof(T) * vec.size(), cudaMemcpyHostToDevice, stream));
+    };
+    up(top_off_dev, off);
+    up(top_terms_dev, terms);
+    up(bond_idx_dev, top.bonds);
+    up(bond_par_dev, top.bond_par);
+    up(angle_idx_dev, top.angles);
+    up(angle_par_dev, top.angle_par);
+    up(dih_idx_dev, top.dihedrals);
+    up(dih_par_dev, top.dih_par);
+    dfree(d.tloc);
+    d.tloc = dalloc<int>(n_top);
+    d.n_top = n_top;
+    d.top_off = top_off_dev;
+    d.top_terms = top_terms_dev;
+    d.bond_idx = bond_idx_dev; d.bond_par = bond_par_dev;
+    d.angle_idx = angle_idx_dev; d.angle_par = angle_par_dev;
+    d.dih_idx = dih_idx_dev; d.dih_par = dih_par_dev;
+    // tloc is rebuilt by a sort
+    launch_bin(d, stream);
+    launch_sort(d, forces_live, stream);
+    swap_buffers();
+    sync();
+    invalidate_graph();
+}
+
+// One or more loop iterations: integrate, update NL, react, update NL, forces, observables.
+void rdc_system::step_sequence(int handler, bool reactions, bool structural, int nsteps) {
+    for (int k = 0; k < nsteps; ++k) {
+        launch_integrate_bin(d, true, stream);
+        launch_sort(d, false, stream);
+        swap_buffers();
+        if (reactions) {
+            launch_events(d, handler, stream);
+            launch_resolve_apply(d, handler, stream);
+            if (structural) {
+                launch_bin(d, stream);
+                launch_sort(d, false, stream);
+                swap_buffers();
+            }
+        }
+        launch_forces(d, true, n_top > 0, stream);
+        launch_record_counts(d, stream);
+    }
+}
+
+void rdc_system::run(int64_t n_steps, double dt, int handler, int64_t stride, int64_t *counts, int64_t max_rec,
+                     int64_t *n_rec) {
+    require(n_steps >= 0, "n_steps must be >= 0");
+    require(dt > 0, "time step must be > 0");
+    require(handler == H_UNCONTROLLED_APPROXIMATION || handler == H_GILLESPIE, "unknown reaction handler");
+    set_dt(dt);
+    // runInitialize + runInitializeNeighborList + runForces (SimulationLoop.h:257-272)
+    RDC_CUDA(cudaMemsetAsync(d.reaction_counts, 0, sizeof(unsigned long long) * MAX_REACTIONS, stream));
+    const double cutoff = std::max(nl_cutoff, ctx.max_cutoff());
+    const bool need_nl = cutoff > 0;
+    if (need_nl) nl_create(cutoff);
+    else {
+        nl_ready = true;
+        nl_update();
+    }
+    calculate_forces();
+    // observables ring
+    dfree(d.counts_ring);
+    const bool rec = counts != nullptr && stride > 0 && max_rec > 0;
+    d.counts_stride = rec ? (int)std::min<int64_t>(stride, INT_MAX) : 0;
+    d.counts_max = rec ? (int)std::min<int64_t>(max_rec, 1 << 24) : 0;
+    d.counts_ring = dalloc<unsigned long long>((size_t)std::max(1, d.counts_max) * ctx.ntypes);
+    RDC_CUDA(cudaMemsetAsync(d.counts_ring, 0, sizeof(unsigned long long) * std::max(1, d.counts_max) * ctx.ntypes,
+                             stream));
+    {
+        int zero = 0;
+        RDC_CUDA(cudaMemcpyAsync(d.counters + C_REC, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
+    }
+    uint64_t steps_now[2];
+    RDC_CUDA(cudaMemcpyAsync(steps_now, d.step, sizeof(steps_now), cudaMemcpyDeviceToHost, stream));
+    sync();
+    d.rec_base = steps_now[0];
+    if (rec) launch_record_counts(d, stream);  // t = 0
+    const bool reactions = !ctx.reactions.empty();
+    const bool structural = reactions && ctx.structural_reactions();
+    const int swaps = 1 + (structural ? 1 : 0);
+    const int per_graph = (swaps % 2 == 0) ? 1 : 2;
+    // the device state pointers are baked into the graph; a graph of an even number of buffer
+    // swaps starts and ends on the same buffers and can be replayed
+    const int64_t reps = n_steps / per_graph;
+    if (reps > 0) {
+        invalidate_graph();
+        cudaGraph_t g;
+        RDC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        SysDev saved = d;
+        step_sequence(handler, reactions, structural, per_graph);
+        const bool same = d.pos == saved.pos;
+        RDC_CUDA(cudaStreamEndCapture(stream, &g));
+        if (!same) {
+            cudaGraphDestroy(g);
+            throw std::logic_error("graph capture ended on the alternate buffers");
+        }
+        RDC_CUDA(cudaGraphInstantiate(&graph, g, 0));
+        cudaGraphDestroy(g);
+        for (int64_t r = 0; r < reps; ++r) RDC_CUDA(cudaGraphLaunch(graph, stream));
+    }
+    const int64_t rest = n_steps - reps * per_graph;
+    if (rest > 0) step_sequence(handler, reactions, structural, (int)rest);
+    forces_live = true;
+    sync();
+    check_status();
+    if (rec) {
+        int c[C_COUNT];
+        read_counters(c);
+        const int nr = std::min(c[C_REC], d.counts_max);
+        std::vector<unsigned long long> h((size_t)nr * ctx.ntypes);
+        if (nr > 0)
+            RDC_CUDA(cudaMemcpyAsync(h.data(), d.counts_ring, sizeof(unsigned long long) * h.size(),
+                                     cudaMemcpyDeviceToHost, stream));
+        sync();
+        for (size_t i = 0; i < h.size(); ++i) counts[i] = (int64_t)h[i];
+        if (n_rec) *n_rec = nr;
+    } else if (n_rec) {
+        *n_rec = 0;
+    }
+    d.counts_stride = 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+const char *rdc_last_error(void) { return g_err.c_str(); }
+int rdc_version(void) { return 1000; }
+const char *rdc_kernel_name(void) { return "CUDA"; }
+
+int rdc_context_create(rdc_context **out, const double box[3], const int periodic[3], double kbt, int n_types,
+                       const double *diffusion) {
+    return guarded([&] {
+        require(out && box && periodic && diffusion, "null argument");
+        require(n_types > 0 && n_types <= MAX_TYPES, "n_types must be in [1, 32]");
+        require(kbt > 0, "kBT must be > 0");
+        for (int d = 0; d < 3; ++d) require(box[d] > 0, "box edges must be > 0");
+        auto c = std::make_unique<rdc_context>();
+        for (int d = 0; d < 3; ++d) {
+            c->d.box[d] = (double)(float)box[d];
+            c->d.pbc[d] = periodic[d] ? 1 : 0;
+        }
+        c->d.kbt = kbt;
+        c->d.ntypes = n_types;
+        c->d.D.assign(diffusion, diffusion + n_types);
+        for (double D : c->d.D) require(D >= 0, "diffusion constants must be >= 0");
+        *out = c.release();
+    });
+}
+int rdc_context_destroy(rdc_context *ctx) {
+    delete ctx;
+    return RDC_OK;
+}
+int rdc_context_max_cutoff(const rdc_context *ctx, double *cutoff) {
+    return guarded([&] {
+        require(ctx && cutoff, "null argument");
+        *cutoff = ctx->d.max_cutoff();
+    });
+}
+
+static void check_types(const rdc_context *ctx, std::initializer_list<int> ts) {
+    require(ctx != nullptr, "null context");
+    for (int t : ts) require(t >= 0 && t < ctx->d.ntypes, "particle type out of range");
+}
+
+int rdc_context_add_harmonic_repulsion(rdc_context *ctx, int t1, int t2, double k, double d) {
+    return guarded([&] {
+        check_types(ctx, {t1, t2});
+        require(d > 0, "interaction distance must be > 0");
+        HostPot h{t1, t2, {}, d};
+        h.pot.kind = POT_HARMONIC_REPULSION;
+        h.pot.p[0] = (float)k;
+        h.pot.p[1] = (float)d;
+        h.pot.cutoff2 = d * d;
+        h.pot.cutoff2f = (float)h.pot.cutoff2;
+        ctx->d.pots.push_back(h);
+    });
+}
+int rdc_context_add_weak_interaction_piecewise_harmonic(rdc_context *ctx, int t1, int t2, double k, double d0,
+                                                        double depth, double rc) {
+    return guarded([&] {
+        check_types(ctx, {t1, t2});
+        require(rc > d0 && d0 >= 0, "need 0 <= desired distance < no-interaction distance");
+        HostPot h{t1, t2, {}, rc};
+        h.pot.kind = POT_WEAK_PIECEWISE_HARMONIC;
+        h.pot.p[0] = (float)k; h.pot.p[1] = (float)d0; h.pot.p[2] = (float)depth; h.pot.p[3] = (float)rc;
+        h.pot.cutoff2 = rc * rc;
+        h.pot.cutoff2f = (float)h.pot.cutoff2;
+        ctx->d.pots.push_back(h);
+    });
+}
+int rdc_context_add_lennard_jones(rdc_context *ctx, int t1, int t2, unsigned m, unsigned n, double cutoff, int shift,
+                                  double epsilon, double sigma) {
+    return guarded([&] {
+        check_types(ctx, {t1, t2});
+        // Potentials.cpp:163-166
+        if (m <= n)
+            throw InvalidArgument("When constructing the LJ potential, the first exponent m=" + std::to_string(m) +
+                                  " was not greater than the second exponent n=" + std::to_string(n) + "!");
+        require(cutoff > 0 && sigma > 0, "LJ cutoff and sigma must be > 0");
+        require(m <= 64, "LJ exponent too large");
+        const double dm = m, dn = n;
+        const double rmin = sigma * std::pow(dn / dm, 1. / (dn - dm));  // Potentials.cpp:167-170
+        const double kk = -epsilon / (std::pow(sigma / rmin, dm) - std::pow(sigma / rmin, dn));
+        const double eshift = shift ? kk * (std::pow(sigma / cutoff, dm) - std::pow(sigma / cutoff, dn)) : 0.0;
+        HostPot h{t1, t2, {}, cutoff};
+        h.pot.kind = POT_LENNARD_JONES;
+        h.pot.p[0] = (float)m; h.pot.p[1] = (float)n; h.pot.p[2] = (float)cutoff; h.pot.p[3] = shift ? 1.f : 0.f;
+        h.pot.p[4] = (float)epsilon; h.pot.p[5] = (float)(sigma * sigma); h.pot.p[6] = (float)kk;
+        h.pot.p[7] = (float)eshift;
+        h.pot.cutoff2 = cutoff * cutoff;
+        h.pot.cutoff2f = (float)h.pot.cutoff2;
+        ctx->d.pots.push_back(h);
+    });
+}
+int rdc_context_add_screened_electrostatics(rdc_context *ctx, int t1, int t2, double C, double kappa, double D,
+                                            double sigma, unsigned exponent, double cutoff) {
+    return guarded([&] {
+        check_types(ctx, {t1, t2});
+        // Potentials.cpp:188-201
+        if (kappa < 0) throw InvalidArgument("inverse screening depth must be positive!");
+        if (D < 0) throw InvalidArgument("repulsion strength must be positive!");
+        if (sigma < 0) throw InvalidArgument("repulsion distance must be positive!");
+        if (cutoff < 0) throw InvalidArgument("cutoff must be positive!");
+        require(exponent <= 64, "exponent too large");
+        HostPot h{t1, t2, {}, cutoff};
+        h.pot.kind = POT_SCREENED_ELECTROSTATICS;
+        h.pot.p[0] = (float)C; h.pot.p[1] = (float)kappa; h.pot.p[2] = (float)D; h.pot.p[3] = (float)sigma;
+        h.pot.p[4] = (float)exponent;
+        h.pot.cutoff2 = cutoff * cutoff;
+        h.pot.cutoff2f = (float)h.pot.cutoff2;
+        ctx->d.pots.push_back(h);
+    });
+}
+
+static int add_reaction(rdc_context *ctx, HostReaction r, int *id) {
+    return guarded([&] {
+        require(ctx != nullptr, "null context");
+        require((int)ctx->d.reactions.size() < MAX_REACTIONS, "too many reactions");
+        require(r.rate >= 0, "reaction rate must be >= 0");
+        for (int k = 0; k < r.n_educts; ++k) check_types(ctx, {r.educt[k]});
+        for (int k = 0; k < r.n_products; ++k) check_types(ctx, {r.product[k]});
+        const double sum = r.w1 + r.w2;  // Fusion.h:62-68, Fission.h:64-70
+        if (sum != 1 && sum > 0) {
+            r.w1 /= sum;
+            r.w2 /= sum;
+        }
+        ctx->d.reactions.push_back(r);
+        if (id) *id = (int)ctx->d.reactions.size() - 1;
+    });
+}
+int rdc_context_add_conversion(rdc_context *ctx, int from, int to, double rate, int *id) {
+    return add_reaction(ctx, HostReaction{R_CONVERSION, 1, 1, {from, 0}, {to, 0}, rate, 0, 0, .5, .5}, id);
+}
+int rdc_context_add_decay(rdc_context *ctx, int from, double rate, int *id) {
+    return add_reaction(ctx, HostReaction{R_DECAY, 1, 0, {from, 0}, {0, 0}, rate, 0, 0, .5, .5}, id);
+}
+int rdc_context_add_fusion(rdc_context *ctx, int from1, int from2, int to, double rate, double ed, double w1, double w2,
+                           int *id) {
+    if (!(ed > 0)) {
+        g_err = "educt distance must be > 0";
+        return RDC_ERR_INVALID_ARGUMENT;
+    }
+    return add_reaction(ctx, HostReaction{R_FUSION, 2, 1, {from1, from2}, {to, 0}, rate, ed, 0, w1, w2}, id);
+}
+int rdc_context_add_fission(rdc_context *ctx, int from, int to1, int to2, double rate, double pd, double w1, double w2,
+                            int *id) {
+    return add_reaction(ctx, HostReaction{R_FISSION, 1, 2, {from, 0}, {to1, to2}, rate, 0, pd, w1, w2}, id);
+}
+int rdc_context_add_enzymatic(rdc_context *ctx, int catalyst, int from, int to, double rate, double ed, int *id) {
+    if (!(ed > 0)) {
+        g_err = "educt distance must be > 0";
+        return RDC_ERR_INVALID_ARGUMENT;
+    }
+    return add_reaction(ctx, HostReaction{R_ENZYMATIC, 2, 2, {from, catalyst}, {to, catalyst}, rate, ed, 0, .5, .5},
+                        id);
+}
+
+int rdc_context_configure_harmonic_bond(rdc_context *ctx, int t1, int t2, double k, double l0) {
+    return guarded([&] {
+        check_types(ctx, {t1, t2});
+        ctx->d.bonds.push_back(BondCfg{t1, t2, k, l0});
+    });
+}
+int rdc_context_configure_harmonic_angle(rdc_context *ctx, int t1, int t2, int t3, double k, double theta0) {
+    return guarded([&] {
+        check_types(ctx, {t1, t2, t3});
+        ctx->d.angles.push_back(AngleCfg{t1, t2, t3, k, theta0});
+    });
+}
+int rdc_context_configure_cosine_dihedral(rdc_context *ctx, int t1, int t2, int t3, int t4, double k, double mult,
+                                          double phi0) {
+    return guarded([&] {
+        check_types(ctx, {t1, t2, t3, t4});
+        // TorsionPotential.h:63-67
+        if (phi0 > M_PI || phi0 < -M_PI)
+            throw InvalidArgument("the equilibrium angle should be within [-pi, pi], but was " + std::to_string(phi0));
+        ctx->d.dihedrals.push_back(DihedralCfg{t1, t2, t3, t4, k, mult, phi0});
+    });
+}
+
+int rdc_system_create(rdc_system **out, const rdc_context *ctx, uint64_t seed) {
+    return guarded([&] {
+        require(out && ctx, "null argument");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            throw CudaError("no CUDA device available");
+        }
+        auto s = std::make_unique<rdc_system>();
+        s->init(ctx->d, seed);
+        *out = s.release();
+    });
+}
+int rdc_system_destroy(rdc_system *s) {
+    if (s) {
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        delete s;
+    }
+    return RDC_OK;
+}
+
+int rdc_add_particles(rdc_system *s, int64_t n, const double *pos, const int *types, uint64_t *ids_out) {
+    return guarded([&] {
+        require(s != nullptr && (n == 0 || (pos && types)), "null argument");
+        require(n >= 0, "n must be >= 0");
+        s->append(n, pos, types, nullptr, ids_out);
+        s->invalidate_graph();
+    });
+}
+int rdc_add_topology(rdc_system *s, int64_t n, const double *pos, const int *types, int64_t n_edges,
+                     const int64_t *edges, uint64_t *ids_out) {
+    return guarded([&] {
+        require(s && pos && types && (n_edges == 0 || edges), "null argument");
+        s->add_topology(n, pos, types, n_edges, edges, ids_out);
+    });
+}
+int rdc_get_n_particles(rdc_system *s, int64_t *n) {
+    return guarded([&] {
+        require(s && n, "null argument");
+        // active = storage minus the dead still awaiting a sort
+        launch_count_types(s->d, s->count_buf, s->stream);
+        std::vector<unsigned long long> h(s->ctx.ntypes);
+        RDC_CUDA(cudaMemcpyAsync(h.data(), s->count_buf, sizeof(unsigned long long) * h.size(),
+                                 cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        int64_t k = 0;
+        for (auto v : h) k += (int64_t)v;
+        *n = k;
+    });
+}
+
+static void fetch(rdc_system *s, std::vector<float4> &p, std::vector<uint32_t> &id, std::vector<float4> *f) {
+    int c[C_COUNT];
+    s->read_counters(c);
+    const int n = c[C_N_TOTAL];
+    p.resize(n);
+    id.resize(n);
+    if (n > 0) {
+        RDC_CUDA(cudaMemcpyAsync(p.data(), s->d.pos, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+        RDC_CUDA(cudaMemcpyAsync(id.data(), s->d.id, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s->stream));
+        if (f) {
+            f->resize(n);
+            RDC_CUDA(cudaMemcpyAsync(f->data(), s->d.force, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+        }
+    }
+    s->sync();
+}
+
+int rdc_get_particles(rdc_system *s, int64_t cap, double *pos, int *types, uint64_t *ids, int64_t *n_out) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        std::vector<float4> p;
+        std::vector<uint32_t> id;
+        fetch(s, p, id, nullptr);
+        int64_t k = 0;
+        for (size_t i = 0; i < p.size(); ++i) {
+            int t;
+            std::memcpy(&t, &p[i].w, 4);
+            if (t < 0) continue;
+            if (k < cap) {
+                if (pos) { pos[3 * k] = p[i].x; pos[3 * k + 1] = p[i].y; pos[3 * k + 2] = p[i].z; }
+                if (types) types[k] = t;
+                if (ids) ids[k] = id[i];
+            }
+            ++k;
+        }
+        if (n_out) *n_out = k;
+        if (k > cap) throw CapacityError("output capacity too small for the particles");
+    });
+}
+int rdc_get_forces(rdc_system *s, int64_t cap, double *forces, uint64_t *ids, int64_t *n_out) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        std::vector<float4> p, f;
+        std::vector<uint32_t> id;
+        fetch(s, p, id, &f);
+        int64_t k = 0;
+        for (size_t i = 0; i < p.size(); ++i) {
+            int t;
+            std::memcpy(&t, &p[i].w, 4);
+            if (t < 0) continue;
+            if (k < cap) {
+                if (forces) { forces[3 * k] = f[i].x; forces[3 * k + 1] = f[i].y; forces[3 * k + 2] = f[i].z; }
+                if (ids) ids[k] = id[i];
+            }
+            ++k;
+        }
+        if (n_out) *n_out = k;
+        if (k > cap) throw CapacityError("output capacity too small for the particles");
+    });
+}
+int rdc_get_energy(rdc_system *s, double *e) {
+    return guarded([&] {
+        require(s && e, "null argument");
+        RDC_CUDA(cudaMemcpyAsync(e, s->d.energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+    });
+}
+int rdc_count_types(rdc_system *s, int64_t *counts) {
+    return guarded([&] {
+        require(s && counts, "null argument");
+        launch_count_types(s->d, s->count_buf, s->stream);
+        std::vector<unsigned long long> h(s->ctx.ntypes);
+        RDC_CUDA(cudaMemcpyAsync(h.data(), s->count_buf, sizeof(unsigned long long) * h.size(),
+                                 cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        for (int t = 0; t < s->ctx.ntypes; ++t) counts[t] = (int64_t)h[t];
+    });
+}
+int rdc_get_reaction_counts(rdc_system *s, int n, int64_t *counts) {
+    return guarded([&] {
+        require(s && (n == 0 || counts), "null argument");
+        std::vector<unsigned long long> h(MAX_REACTIONS);
+        RDC_CUDA(cudaMemcpyAsync(h.data(), s->d.reaction_counts, sizeof(unsigned long long) * MAX_REACTIONS,
+                                 cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        for (int i = 0; i < n && i < MAX_REACTIONS; ++i) counts[i] = (int64_t)h[i];
+    });
+}
+int rdc_reserve(rdc_system *s, int64_t capacity) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        require(capacity > 0 && capacity < INT_MAX / 2, "capacity out of range");
+        s->reserve((int)capacity);
+    });
+}
+int rdc_set_cell_radius(rdc_system *s, int radius) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        require(radius >= 1 && radius <= 3, "cell radius must be 1, 2 or 3");
+        s->radius = radius;
+        s->d.radius = radius;
+        if (s->nl_ready && s->nl_cutoff > 0) s->nl_create(s->nl_cutoff);
+    });
+}
+
+int rdc_initialize(rdc_system *s) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        RDC_CUDA(cudaMemsetAsync(s->d.reaction_counts, 0, sizeof(unsigned long long) * MAX_REACTIONS, s->stream));
+    });
+}
+int rdc_nl_create(rdc_system *s, double cutoff) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->nl_create(cutoff);
+    });
+}
+int rdc_nl_update(rdc_system *s) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->nl_update();
+    });
+}
+int rdc_nl_clear(rdc_system *s) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->nl_clear();
+    });
+}
+int rdc_calculate_forces(rdc_system *s) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->calculate_forces();
+    });
+}
+int rdc_euler_bd_integrate(rdc_system *s, double dt) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        require(dt > 0, "time step must be > 0");
+        s->integrate(dt);
+    });
+}
+int rdc_uncontrolled_approximation(rdc_system *s, double dt) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->react(dt, H_UNCONTROLLED_APPROXIMATION);
+    });
+}
+int rdc_gillespie(rdc_system *s, double dt) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->react(dt, H_GILLESPIE);
+    });
+}
+int rdc_run(rdc_system *s, int64_t n_steps, double dt, int handler, int64_t stride, int64_t *counts, int64_t max_rec,
+            int64_t *n_rec) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->run(n_steps, dt, handler, stride, counts, max_rec, n_rec);
+    });
+}
+int rdc_nl_pairs(rdc_system *s, double cutoff, int64_t cap, uint64_t *pairs, int64_t *n_pairs) {
+    return guarded([&] {
+        require(s && n_pairs, "null argument");
+        if (!s->nl_ready || s->nl_cutoff <= 0) throw LogicError("neighbor list not set up");
+        require(cutoff > 0 && cutoff <= s->nl_cutoff * (1 + 1e-12), "pair cutoff exceeds the neighbor-list cutoff");
+        int c[C_COUNT];
+        s->read_counters(c);
+        int dcap = (int)std::min<int64_t>(std::max<int64_t>(cap, 1), 1 << 28);
+        uint64_t *buf = dalloc<uint64_t>(dcap);
+        RDC_CUDA(cudaMemsetAsync(s->pairs_n, 0, sizeof(int), s->stream));
+        const double c2 = cutoff * cutoff;
+        const float L[3] = {s->d.geo.L[0], s->d.geo.L[1], s->d.geo.L[2]};
+        launch_pairs(s->d, (float)c2, band_for(cutoff, L), c2, buf, dcap, s->pairs_n, s->stream);
+        int n = 0;
+        RDC_CUDA(cudaMemcpyAsync(&n, s->pairs_n, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        *n_pairs = n;
+        if (n > cap) {
+            dfree(buf);
+            throw CapacityError("pair output capacity too small");
+        }
+        std::vector<uint64_t> h(n);
+        if (n > 0) RDC_CUDA(cudaMemcpyAsync(h.data(), buf, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        dfree(buf);
+        std::sort(h.begin(), h.end());
+        for (int i = 0; i < n; ++i) {
+            pairs[2 * i] = h[i] >> 32;
+            pairs[2 * i + 1] = h[i] & 0xffffffffull;
+        }
+    });
+}
+int rdc_synchronize(rdc_system *s) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->sync();
+        RDC_CUDA(cudaGetLastError());
+        s->check_status();
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,421 @@
+// Device-side building blocks shared by the per-system kernels and the batched replica kernel.
+//
+// Semantics follow ReaDDy's CPU kernel (paths relative to the readdy/readdy project root):
+//   minimum image / wrap ........ include/readdy/common/boundary_condition_operations.h:53-80
+//   pair potentials .............. include/readdy/model/potentials/PotentialsOrder2.h:54-305
+//   harmonic bond ................ include/readdy/model/topologies/potentials/BondedPotential.h:105-113
+//   harmonic angle ............... readdy/main/model/topologies/potentials/AnglePotential.cpp:58-104
+//   cosine dihedral .............. readdy/main/model/topologies/potentials/TorsionPotential.cpp:53-153
+//   reaction coin ................ include/readdy/kernel/cpu/actions/reactions/ReactionUtils.h:64-76
+// Arithmetic is FP32 except the pair-membership predicate: pairs whose FP32 squared distance lies
+// within a rounding band of the cutoff are re-decided in FP64 exactly as the reference does, so the
+// neighbour pair set is bit-identical to the FP64 CPU kernel on the same (FP32) positions.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rdc_types.h"
+
+namespace rdc {
+
+// ------------------------------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, "Parallel random numbers:
+// as easy as 1, 2, 3", SC'11).  Constants are the published round multipliers and Weyl increments.
+// ------------------------------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+__host__ __device__ inline void mulhilo32(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
+    uint64_t p = (uint64_t)a * (uint64_t)b;
+    hi = (uint32_t)(p >> 32);
+    lo = (uint32_t)p;
+}
+
+__host__ __device__ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo32(0xD2511F53u, c.x, hi0, lo0);
+        mulhilo32(0xCD9E8D57u, c.z, hi1, lo1);
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// purposes (the 4th counter word) keep the streams of different uses disjoint
+enum : uint32_t { RNG_BD = 1u, RNG_COIN1 = 2u, RNG_COIN2 = 3u, RNG_PRIO1 = 4u, RNG_PRIO2 = 5u, RNG_FISSION = 6u };
+
+__host__ __device__ inline U4 rng_draw(uint64_t seed, uint32_t a, uint32_t b, uint64_t step, uint32_t purpose,
+                                       uint32_t reaction) {
+    U4 c{a, b, (uint32_t)step, purpose | ((uint32_t)(step >> 32) << 8) | (reaction << 16)};
+    return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// uniform in (0,1), 24-bit resolution, never 0
+__device__ inline float u01(uint32_t r) { return ((float)(r >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+
+// four standard normals by the Box-Muller transform of two uniform pairs
+__device__ inline void normal4(U4 r, float &n0, float &n1, float &n2, float &n3) {
+    float u1 = u01(r.x), u2 = u01(r.y), u3 = u01(r.z), u4 = u01(r.w);
+    float r1 = sqrtf(-2.0f * logf(u1)), r2 = sqrtf(-2.0f * logf(u3));
+    float s1, c1, s2, c2;
+    sincospif(2.0f * u2, &s1, &c1);
+    sincospif(2.0f * u4, &s2, &c2);
+    n0 = r1 * c1; n1 = r1 * s1; n2 = r2 * c2; n3 = r2 * s2;
+}
+
+// ------------------------------------------------------------------------------------------------
+// geometry
+// ------------------------------------------------------------------------------------------------
+__device__ inline float type_of(float4 p) { return p.w; }
+__device__ inline int itype(float4 p) { return __float_as_int(p.w); }
+
+// bcs::fixPosition in FP32 with a bounded number of wraps (the box is FP32-exact, so the
+// comparisons against +-L/2 are exact)
+__device__ inline float wrap1(float x, float L, float hL, int pbc) {
+    if (pbc) {
+#pragma unroll 1
+        for (int k = 0; k < 4 && x >= hL; ++k) x -= L;
+#pragma unroll 1
+        for (int k = 0; k < 4 && x < -hL; ++k) x += L;
+    }
+    return x;
+}
+
+// bcs::shortestDifference(lhs, rhs) component, FP32
+__device__ inline float mi1(float dv, float L, float hL, int pbc) {
+    if (pbc) {
+        if (dv > hL) dv -= L;
+        else if (dv <= -hL) dv += L;
+    }
+    return dv;
+}
+
+// bcs::shortestDifference + inner product in FP64 with the reference's rounding order
+// ((0 + x*x) + y*y) + z*z and no fused multiply-add
+__device__ inline double dist2_exact(float4 lhs, float4 rhs, const Geo &g, double &dx, double &dy, double &dz) {
+    double d[3] = {__dsub_rn((double)rhs.x, (double)lhs.x), __dsub_rn((double)rhs.y, (double)lhs.y),
+                   __dsub_rn((double)rhs.z, (double)lhs.z)};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (g.pbc[i]) {
+            const double h = g.Ld[i] * 0.5;
+            if (d[i] > h) d[i] = __dsub_rn(d[i], g.Ld[i]);
+            else if (d[i] <= -h) d[i] = __dadd_rn(d[i], g.Ld[i]);
+        }
+    }
+    double s = __dmul_rn(d[0], d[0]);
+    s = __dadd_rn(s, __dmul_rn(d[1], d[1]));
+    s = __dadd_rn(s, __dmul_rn(d[2], d[2]));
+    dx = d[0]; dy = d[1]; dz = d[2];
+    return s;
+}
+
+// Minimum-image difference rhs - lhs in FP32 and its squared norm.
+struct PairGeom {
+    float dx, dy, dz, d2;
+};
+
+__device__ inline PairGeom pair_geom(float4 lhs, float4 rhs, const Geo &g) {
+    PairGeom r;
+    r.dx = mi1(rhs.x - lhs.x, g.L[0], g.hL[0], g.pbc[0]);
+    r.dy = mi1(rhs.y - lhs.y, g.L[1], g.hL[1], g.pbc[1]);
+    r.dz = mi1(rhs.z - lhs.z, g.L[2], g.hL[2], g.pbc[2]);
+    r.d2 = fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, r.dz * r.dz));
+    return r;
+}
+
+// d^2 < c^2 decided exactly as the FP64 reference: FP32 outside the rounding band, FP64 inside it.
+// On an FP64 decision the FP32 difference is replaced by the rounded FP64 one.
+__device__ inline bool within(const PairGeom &pg0, PairGeom &pg, float4 lhs, float4 rhs, const Geo &g, float c2f,
+                              float band, double c2) {
+    if (!g.exact_always) {
+        if (pg0.d2 < c2f - band) return true;
+        if (pg0.d2 > c2f + band) return false;
+    }
+    double dx, dy, dz;
+    double d2 = dist2_exact(lhs, rhs, g, dx, dy, dz);
+    pg.dx = (float)dx; pg.dy = (float)dy; pg.dz = (float)dz;
+    pg.d2 = (float)d2;
+    return d2 < c2;
+}
+
+// in-box test of the cell list (CellLinkedList.cpp:188-192), exact because the box is FP32-exact
+__device__ inline bool in_box(float4 p, const Geo &g) {
+    return -g.hL[0] <= p.x && g.hL[0] > p.x && -g.hL[1] <= p.y && g.hL[1] > p.y && -g.hL[2] <= p.z &&
+           g.hL[2] > p.z;
+}
+
+__device__ inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// cell of a particle; the grid is row-major with z fastest (include/readdy/common/Index.h:130-141)
+__device__ inline void cell_coords(float4 p, const Geo &g, int &cx, int &cy, int &cz) {
+    cx = clampi(__float2int_rd((p.x + g.hL[0]) * g.invW[0]), 0, g.dims[0] - 1);
+    cy = clampi(__float2int_rd((p.y + g.hL[1]) * g.invW[1]), 0, g.dims[1] - 1);
+    cz = clampi(__float2int_rd((p.z + g.hL[2]) * g.invW[2]), 0, g.dims[2] - 1);
+}
+__device__ inline int cell_index(int cx, int cy, int cz, const Geo &g) {
+    return cz + g.dims[2] * (cy + g.dims[1] * cx);
+}
+
+// bin of a particle: its cell, OUT (outside the box on a non-periodic axis) or DEAD
+__device__ inline int bin_of(float4 p, const Geo &g) {
+    if (itype(p) < 0) return g.ncells + 1;  // DEAD
+    if (!in_box(p, g)) return g.ncells;     // OUT
+    int cx, cy, cz;
+    cell_coords(p, g, cx, cy, cz);
+    return cell_index(cx, cy, cz, g);
+}
+
+// neighbour-cell offsets along one axis without duplicates: dims 1 -> {0}, 2 -> {0,+1} (periodic)
+__device__ inline int axis_offsets(int c, int dim, int pbc, int *out) {
+    int n = 0;
+    if (dim == 1) { out[n++] = 0; return n; }
+    for (int o = -1; o <= 1; ++o) {
+        int v = c + o;
+        if (pbc) {
+            v = (v + dim) % dim;
+            bool dup = false;
+            for (int k = 0; k < n; ++k) dup |= (out[k] == v);
+            if (dup) continue;
+        } else if (v < 0 || v >= dim) {
+            continue;
+        }
+        out[n++] = v;
+    }
+    return n;
+}
+
+// ------------------------------------------------------------------------------------------------
+// pair potentials (force on the particle at lhs, x = rhs - lhs, half the pair energy added to e)
+// ------------------------------------------------------------------------------------------------
+__device__ inline float ipow(float x, int n) {
+    float r = 1.0f;
+#pragma unroll 1
+    while (n > 0) {
+        if (n & 1) r *= x;
+        x *= x;
+        n >>= 1;
+    }
+    return r;
+}
+
+__device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float &fx, float &fy, float &fz, float &e) {
+    const float d2 = g.d2;
+    switch (pp.kind) {
+        case POT_HARMONIC_REPULSION: {  // PotentialsOrder2.h:73-91
+            const float k = pp.p[0], d = pp.p[1];
+            if (d2 > 0.0f) {
+                const float r = sqrtf(d2);
+                const float s = k * (r - d) / r;
+                fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
+                e += 0.25f * k * (r - d) * (r - d);  // half of 0.5 k (r-d)^2
+            } else {
+                e += 0.25f * k * d * d;
+            }
+            break;
+        }
+        case POT_WEAK_PIECEWISE_HARMONIC: {  // PotentialsOrder2.h:131-183
+            const float k = pp.p[0], d0 = pp.p[1], depth = pp.p[2], rc = pp.p[3];
+            const float dist = sqrtf(d2);
+            const float half = 0.5f * (rc - d0);
+            const float c = depth / (half * half);
+            float en, factor;
+            if (dist < d0) {
+                en = 0.5f * k * (dist - d0) * (dist - d0) - depth;
+                factor = -k * (d0 - dist);
+            } else if (dist < d0 + half) {
+                en = 0.5f * c * (dist - d0) * (dist - d0) - depth;
+                factor = -c * (d0 - dist);
+            } else if (dist < rc) {
+                en = -0.5f * c * (dist - rc) * (dist - rc);
+                factor = c * (rc - dist);
+            } else {
+                en = 0.0f;
+                factor = 0.0f;
+            }
+            e += 0.5f * en;
+            if (dist > 0.0f && factor != 0.0f) {
+                const float s = factor / dist;
+                fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
+            }
+            break;
+        }
+        case POT_LENNARD_JONES: {  // PotentialsOrder2.h:240-264, integer powers by multiplication
+            const int m = (int)pp.p[0], n = (int)pp.p[1];
+            const float sigma2 = pp.p[5], kk = pp.p[6], eshift = pp.p[7];
+            const float s2 = sigma2 / d2;  // (sigma/r)^2
+            float sm, sn;
+            if ((m & 1) == 0 && (n & 1) == 0) {
+                sm = ipow(s2, m >> 1);
+                sn = ipow(s2, n >> 1);
+            } else {
+                const float s1 = sqrtf(s2);
+                sm = ipow(s1, m);
+                sn = ipow(s1, n);
+            }
+            // F = -k/sigma^2 (m (s/r)^(m+2) - n (s/r)^(n+2)) x
+            const float s = -kk / sigma2 * (m * sm - n * sn) * s2;
+            fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
+            e += 0.5f * (kk * (sm - sn) - eshift);
+            break;
+        }
+        case POT_SCREENED_ELECTROSTATICS: {  // PotentialsOrder2.h:291-305
+            const float C = pp.p[0], kappa = pp.p[1], D = pp.p[2], sigma = pp.p[3];
+            const int ex = (int)pp.p[4];
+            const float r = sqrtf(d2);
+            const float ir = 1.0f / r;
+            const float ekr = C * expf(-kappa * r);
+            const float sr = sigma * ir;
+            const float srn = ipow(sr, ex);
+            e += 0.5f * (ekr * ir + D * srn);
+            float ff = ekr * (kappa * ir + ir * ir);
+            ff += D * (float)ex / sigma * srn * sr;
+            const float s = -ff * ir;
+            fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
+            break;
+        }
+        default:
+            break;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// bonded terms.  Each participant evaluates the whole term and keeps only its own force
+// (no atomics, deterministic); 'role' selects the participant.
+// ------------------------------------------------------------------------------------------------
+struct F3 { float x, y, z; };
+__device__ inline F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ inline F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ inline F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ inline F3 operator*(float s, F3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ inline float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ inline F3 cross(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+
+__device__ inline F3 shortest3(float4 lhs, float4 rhs, const Geo &g) {
+    return F3{mi1(rhs.x - lhs.x, g.L[0], g.hL[0], g.pbc[0]), mi1(rhs.y - lhs.y, g.L[1], g.hL[1], g.pbc[1]),
+              mi1(rhs.z - lhs.z, g.L[2], g.hL[2], g.pbc[2])};
+}
+
+// harmonic bond: E = k (r - l0)^2, force on i = 2k (r-l0)/r x_ij, on j its negative
+__device__ inline F3 bond_force(float4 pi, float4 pj, float k, float l0, const Geo &g, int role, float &e) {
+    const F3 x = shortest3(pi, pj, g);
+    const float r = sqrtf(dot(x, x));
+    const float s = 2.0f * k * (r - l0) / r;
+    e = k * (r - l0) * (r - l0);
+    return role == 0 ? s * x : (-s) * x;
+}
+
+// harmonic angle with the reference's clamps (AnglePotential.cpp:67-102)
+__device__ inline F3 angle_force(float4 pi, float4 pj, float4 pk, float kf, float theta0, const Geo &g, int role,
+                                 float &e) {
+    const float SMALL = 1e-10f;
+    const F3 xji = shortest3(pj, pi, g);
+    const F3 xjk = shortest3(pj, pk, g);
+    const float sp = dot(xji, xjk);
+    float nji2 = fmaxf(dot(xji, xji), SMALL);
+    float njk2 = fmaxf(dot(xjk, xjk), SMALL);
+    const float nji = sqrtf(nji2), njk = sqrtf(njk2);
+    const float np = fmaxf(nji * njk, SMALL);
+    const float inp = 1.0f / np;
+    float c = fminf(1.0f, fmaxf(-1.0f, inp * sp));
+    const float theta = acosf(c);
+    e = kf * (theta - theta0) * (theta - theta0);
+    float sinv = fmaxf(sqrtf(fmaxf(0.0f, 1.0f - c * c)), SMALL);
+    sinv = 1.0f / sinv;
+    const float cc = 2.0f * kf * (theta - theta0) * sinv;
+    const F3 fi = (cc * c / nji2) * xji - (cc * inp) * xjk;
+    const F3 fk = (-cc * inp) * xji + (cc * c / njk2) * xjk;
+    if (role == 0) return (-1.0f) * fi;
+    if (role == 1) return fi + fk;
+    return (-1.0f) * fk;
+}
+
+// cosine dihedral, the analytic gradient of TorsionPotential.cpp:70-153 written with explicit
+// cross products; same clamps (1e-4) and the same zero-force rule for |cos phi| < 1e-4
+__device__ inline F3 dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl, float kf, float mult, float phi0,
+                                    const Geo &g, int role, float &e) {
+    const float SMALL = 1e-4f;
+    const F3 xji = shortest3(pj, pi, g);
+    const F3 xkj = shortest3(pk, pj, g);
+    const F3 xkl = shortest3(pk, pl, g);
+    const F3 xjk = (-1.0f) * xkj;
+    // energy (TorsionPotential.cpp:53-68) uses clamped norms of |x_jk| and |m||n|
+    const F3 m = cross(xji, xkj);
+    const F3 n = cross(xkl, xjk);
+    const float mm_raw = dot(m, m), nn_raw = dot(n, n), jk2_raw = dot(xjk, xjk);
+    {
+        const float xjkn_e = fmaxf(sqrtf(jk2_raw), SMALL);
+        const float mnn_e = fmaxf(sqrtf(mm_raw) * sqrtf(nn_raw), SMALL);
+        const float sinT = dot(cross(m, n), xjk) / (mnn_e * xjkn_e);
+        const float cosT = dot(m, n) / mnn_e;
+        const float dih = -atan2f(sinT, cosT);
+        e = kf * (1.0f + cosf(mult * dih - phi0));
+    }
+    const float xjkn2 = fmaxf(jk2_raw, SMALL);
+    const float xjkn = sqrtf(xjkn2);
+    const float mn2 = fmaxf(mm_raw, SMALL), nn2 = fmaxf(nn_raw, SMALL);
+    const float mn = sqrtf(mn2), nn = sqrtf(nn2);
+    const float nmn = fmaxf(mn * nn, SMALL);
+    const F3 mxn = cross(m, n);
+    const float cphi = dot(n, m) / nmn;
+    if (fabsf(cphi) < SMALL) return f3(0.f, 0.f, 0.f);
+    const float sphi = dot(mxn, xjk) / (nmn * xjkn);
+    const float phi = -atan2f(sphi, cphi);
+    const float dVdphi = -kf * mult * sinf(mult * phi - phi0);
+    const float sbc = sphi / cphi;
+    const float ppre = -1.0f / (cphi * (1.0f + sbc * sbc));
+    const float cpre = 1.0f / nmn;
+    const float spre = 1.0f / (nmn * xjkn);
+    // gradients of |m| and |n| (TorsionPotential.cpp:95-106)
+    const float jikj = dot(xji, xkj), kljk = dot(xkl, xjk);
+    const F3 dmn2_dxi = (2.0f * xjkn2) * xji - (2.0f * jikj) * xkj;
+    const F3 dmn2_dxk = (-2.0f * dot(xji, xji)) * xkj + (2.0f * jikj) * xji;
+    const F3 dnn2_dxl = (2.0f * xjkn2) * xkl - (2.0f * kljk) * xjk;
+    const F3 dnn2_dxj = (-2.0f * dot(xkl, xkl)) * xjk + (2.0f * kljk) * xkl;
+    const float i2m = 1.0f / (2.0f * mn), i2n = 1.0f / (2.0f * nn);
+    // the participant's derivatives.  With the skew tensors of the reference:
+    //   v * dm_dxi = x_kj x v, v * dm_dxk = x_ji x v, v * dn_dxj = x_kl x v, v * dn_dxl = -(x_kj x v)
+    //   x_jk * dmxn_dx = d(m x n) contracted with x_jk
+    F3 dc, ds;
+    if (role == 0) {  // x_i: m depends on x_ji, n does not
+        const F3 dmn = i2m * dmn2_dxi;
+        const F3 n_dm = cross(xkj, n);
+        dc = cpre * (n_dm - (cphi * nn) * dmn);
+        // x_jk . (dm/dxi_c x n) = (n x x_jk) . dm/dxi_c = (x_kj x (n x x_jk))_c
+        const F3 v = cross(xkj, cross(n, xjk));
+        ds = spre * (v - (sphi * nn * xjkn) * dmn);
+    } else if (role == 3) {  // x_l: only n depends on x_kl
+        const F3 dnn = i2n * dnn2_dxl;
+        const F3 m_dn = (-1.0f) * cross(xkj, m);
+        dc = cpre * (m_dn - (cphi * mn) * dnn);
+        // x_jk . (m x dn/dxl_c) = (x_jk x m) . dn/dxl_c ; dn/dxl_c = -(skew(x_kj) col c)
+        const F3 v = (-1.0f) * cross(xkj, cross(xjk, m));
+        ds = spre * (v - (sphi * mn * xjkn) * dnn);
+    } else if (role == 1) {  // x_j
+        const F3 dmn = i2m * ((-1.0f) * (dmn2_dxi + dmn2_dxk));
+        const F3 dnn = i2n * dnn2_dxj;
+        // dm_dxj = -(dm_dxk + dm_dxi), dn_dxj = skew(x_kl)
+        const F3 n_dm = (-1.0f) * (cross(xji, n) + cross(xkj, n));
+        const F3 m_dn = cross(xkl, m);
+        dc = cpre * (n_dm + m_dn - (cphi * nn) * dmn - (cphi * mn) * dnn);
+        const F3 nxj = cross(n, xjk), jxm = cross(xjk, m);
+        const F3 v = (-1.0f) * (cross(xji, nxj) + cross(xkj, nxj)) + cross(xkl, jxm);
+        ds = spre * (v - mxn - (sphi * nn * xjkn) * dmn - (sphi * mn * xjkn) * dnn + (sphi * nmn / xjkn) * xjk);
+    } else {  // role 2, x_k
+        const F3 dmn = i2m * dmn2_dxk;
+        const F3 dnn = i2n * ((-1.0f) * (dnn2_dxl + dnn2_dxj));
+        // dm_dxk = skew(x_ji), dn_dxk = -(dn_dxj + dn_dxl) = -(skew(x_kl) - skew(x_kj))
+        const F3 n_dm = cross(xji, n);
+        const F3 m_dn = (-1.0f) * (cross(xkl, m) - cross(xkj, m));
+        dc = cpre * (n_dm + m_dn - (cphi * nn) * dmn - (cphi * mn) * dnn);
+        const F3 nxj = cross(n, xjk), jxm = cross(xjk, m);
+        const F3 v = cross(xji, nxj) - (cross(xkl, jxm) - cross(xkj, jxm));
+        ds = spre * (v + mxn - (sphi * nn * xjkn) * dmn - (sphi * mn * xjkn) * dnn - (sphi * nmn / xjkn) * xjk);
+    }
+    const F3 dphi = ppre * (ds - sbc * dc);
+    return (-dVdphi) * dphi;
+}
+
+}  // namespace rdc

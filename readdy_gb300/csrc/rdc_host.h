@@ -1,0 +1,165 @@
+// Host-side structures of the CUDA core: the context registries, the device tables built from
+// them, and the per-system device state.  Internal to libreaddy_cuda_core.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "rdc_types.h"
+
+namespace rdc {
+
+// ---- errors -----------------------------------------------------------------------------------
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct CapacityError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define RDC_CUDA(call)                                                                                 \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            throw ::rdc::CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+// ---- context (model::Context) -------------------------------------------------------------------
+struct HostPot {
+    int t1, t2;
+    PairPot pot;
+    double cutoff;
+};
+struct HostReaction {
+    int kind, n_educts, n_products;
+    int educt[2], product[2];
+    double rate, educt_distance, product_distance, w1, w2;
+};
+struct BondCfg { int t1, t2; double k, l0; };
+struct AngleCfg { int t1, t2, t3; double k, theta0; };
+struct DihedralCfg { int t1, t2, t3, t4; double k, mult, phi0; };
+
+struct ContextData {
+    double box[3];
+    int pbc[3];
+    double kbt;
+    int ntypes;
+    std::vector<double> D;
+    std::vector<HostPot> pots;
+    std::vector<HostReaction> reactions;
+    std::vector<BondCfg> bonds;
+    std::vector<AngleCfg> angles;
+    std::vector<DihedralCfg> dihedrals;
+
+    double max_cutoff() const;
+    bool structural_reactions() const;  // fusion, fission or decay present (particles appear/vanish/move)
+};
+
+// device-resident tables: potentials by type pair, reactions by educt types, per-type integration
+struct Tables {
+    int ntypes, npots, nreactions;
+    int has_o2_any;
+    float bd_drift[MAX_TYPES];  // D dt / kBT
+    float bd_scale[MAX_TYPES];  // sqrt(2 D dt)
+    int pair_tab[MAX_TYPES * MAX_TYPES];  // (first << 8) | count into pots, 0 = none
+    PairPot pots[MAX_PAIR_POTENTIALS];
+    ReactionDev reactions[MAX_REACTIONS];
+    int o1_tab[MAX_TYPES];                 // (first << 8) | count into o1_list
+    int o1_list[MAX_REACTIONS];
+    int o2_tab[MAX_TYPES * MAX_TYPES];     // (first << 8) | count into o2_list
+    int o2_list[MAX_REACTIONS * 2];
+    int o2_any[MAX_TYPES];                 // type has any order-2 reaction
+};
+
+// builds the tables from a context for a box (band widths depend on the GPU machine) and time step
+void build_tables(const ContextData &c, const double box[3], double dt, Tables &t);
+void set_time_step(const ContextData &c, double dt, Tables &t);
+// FP32-rounded box, cell grid for cutoff/radius
+Geo make_geo(const double box[3], const int pbc[3], double cutoff, int radius);
+
+// ---- per-system device state -------------------------------------------------------------------
+enum Counter : int {
+    C_N = 0,         // particles in storage (cells + OUT), sorted
+    C_N_TOTAL = 1,   // including particles appended by reactions since the last sort
+    C_N_INCELLS = 2, // particles inside cells (storage [0, C_N_INCELLS))
+    C_STATUS = 3,    // Status bits
+    C_N_EVENTS = 4,
+    C_NEXT_ID = 5,
+    C_REC = 6,       // observable records written
+    C_N_BIRTHS = 7,  // births of the last reaction step (host statistics)
+    C_COUNT = 8
+};
+
+struct SysDev {
+    Geo geo;
+    int radius;
+    const Tables *tab;
+    float4 *pos;
+    uint32_t *id;
+    int *tslot;
+    float4 *force;
+    float4 *pos_alt;
+    uint32_t *id_alt;
+    int *tslot_alt;
+    float4 *force_alt;
+    int *bin, *rank, *src;
+    int *cnt, *start;
+    int *scan_blocks;
+    int *tloc;
+    int *counters;
+    uint64_t *step;
+    int capacity;
+    uint64_t seed;
+    // reactions
+    EventRec *events;
+    int event_capacity;
+    int *claim;
+    int *taken;
+    unsigned long long *reaction_counts;
+    // energy
+    double *epart;     // per-block partial energies (pair kernel blocks, then bonded blocks)
+    double *energy;
+    // bonded (topology slots)
+    int n_top;
+    const int *top_off;    // CSR offsets per topology slot
+    const int *top_terms;  // (kind << 28) | (role << 24) | term index
+    const int4 *bond_idx;  // slots (i, j, -, -)
+    const float2 *bond_par;
+    const int4 *angle_idx;
+    const float2 *angle_par;
+    const int4 *dih_idx;
+    const float4 *dih_par;
+    // observables
+    unsigned long long *counts_ring;
+    int counts_stride;
+    int counts_max;
+    uint64_t rec_base;  // BD step at which the current recording started
+};
+
+constexpr int FORCE_BLOCKS = 4 * 152;
+constexpr int FORCE_THREADS = 256;
+constexpr int BONDED_BLOCKS = 152;
+constexpr int GRID_BLOCKS = 8 * 152;
+constexpr int GRID_THREADS = 256;
+
+// ---- launchers (rdc_kernels.cu) -----------------------------------------------------------------
+void launch_integrate_bin(const SysDev &s, bool integrate, cudaStream_t st);
+void launch_bin(const SysDev &s, cudaStream_t st);
+void launch_sort(const SysDev &s, bool permute_force, cudaStream_t st);  // scan, scatter, per-cell order, gather
+void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st);
+void launch_events(const SysDev &s, int handler, cudaStream_t st);
+void launch_resolve_apply(const SysDev &s, int handler, cudaStream_t st);
+void launch_count_types(const SysDev &s, unsigned long long *out, cudaStream_t st);
+void launch_record_counts(const SysDev &s, cudaStream_t st);
+void launch_step_advance(const SysDev &s, cudaStream_t st);
+void launch_pairs(const SysDev &s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out,
+                  cudaStream_t st);
+void launch_fill_ids(uint32_t *id, uint32_t first, int n, cudaStream_t st);
+int scan_block_count(int n);
+size_t resolve_smem_bytes();
+void init_kernel_attributes();
+
+}  // namespace rdc

@@ -1,0 +1,421 @@
+// Kernels of the per-system ("plain") path: one simulation, every stage a grid-wide launch.
+//
+//   K1  cell list as a deterministic counting sort            (CellLinkedList.cpp:52-247)
+//   K3  pair forces over the 27-cell stencil                  (CPUCalculateForces.cpp:214-268)
+//   K4  bonded bond/angle/dihedral terms per topology particle (CPUTopologyActions.cpp:55-123)
+//   K5  Euler Brownian dynamics fused with binning            (CPUEulerBDIntegrator.cpp:51-103)
+//   K6  reaction events (order 1 per particle, order 2 per pair)   (CPUUncontrolledApproximation.cpp:70-133,
+//                                                                    ReactionUtils.h:83-144)
+//   K7  conflict resolution by seeded priority + application   (CPUUncontrolledApproximation.cpp:197-253,
+//                                                                algorithm.h:62-136, ReactionUtils.h:146-227)
+// Storage is structure-of-arrays in cell order; a sort writes the alternate buffers.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "rdc_phases.cuh"
+#include "rdc_host.h"
+
+namespace rdc {
+
+#define GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+// ------------------------------------------------------------------------------------------------
+// K5 (+ bin): Euler-Maruyama step, then the bin of the new position and its rank inside the bin
+// ------------------------------------------------------------------------------------------------
+__global__ void k_integrate_bin(SysDev s, int integrate, int bin) {
+    const int n = s.counters[C_N_TOTAL];
+    const uint64_t step = s.step[0];
+    GRID_STRIDE(i, n) {
+        float4 p = s.pos[i];
+        if (integrate && itype(p) >= 0) {
+            const float4 f = s.force[i];
+            p = euler_bd(p, f.x, f.y, f.z, s.id[i], s.seed, step, s.tab, s.geo);
+            s.pos[i] = p;
+        }
+        if (bin) {
+            const int b = bin_of(p, s.geo);
+            s.bin[i] = b;
+            s.rank[i] = atomicAdd(&s.cnt[b], 1);
+        }
+    }
+}
+
+__global__ void k_bd_step_advance(SysDev s) { s.step[0] += 1; }
+
+// ------------------------------------------------------------------------------------------------
+// exclusive scan of the bin counts (tiles of 2048, one pass over tile sums, one add pass)
+// ------------------------------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void k_scan_tiles(const int *__restrict__ in, int *__restrict__ out, int *__restrict__ tile_sums, int n) {
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        sum += v[k];
+    }
+    int total;
+    int run = block_exclusive_scan(sum, total);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// single block: exclusive scan of the tile sums in place; out[n] = grand total
+__global__ void k_scan_top(int *tile_sums, int ntiles, int *out, int n) {
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ntiles; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int v = i < ntiles ? tile_sums[i] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, total);
+        if (i < ntiles) tile_sums[i] = ex + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void k_scan_add(int *out, const int *tile_sums, int n) {
+    const int add = tile_sums[blockIdx.x];
+    const int base = blockIdx.x * SCAN_TILE;
+    for (int k = threadIdx.x; k < SCAN_TILE; k += blockDim.x)
+        if (base + k < n) out[base + k] += add;
+}
+
+int scan_block_count(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+
+static void launch_scan(const int *in, int *out, int *tiles, int n, cudaStream_t st) {
+    const int nt = scan_block_count(n);
+    k_scan_tiles<<<nt, SCAN_THREADS, 0, st>>>(in, out, tiles, n);
+    k_scan_top<<<1, 1024, 0, st>>>(tiles, nt, out, n);
+    k_scan_add<<<nt, SCAN_THREADS, 0, st>>>(out, tiles, n);
+}
+
+// ------------------------------------------------------------------------------------------------
+// K1 counting sort: scatter source indices, order each cell by source index (deterministic),
+// gather the particle arrays into the alternate buffers
+// ------------------------------------------------------------------------------------------------
+__global__ void k_scatter(SysDev s) {
+    const int n = s.counters[C_N_TOTAL];
+    const int nc = s.geo.ncells;
+    GRID_STRIDE(i, n) {
+        const int b = s.bin[i];
+        if (b <= nc) s.src[s.start[b] + s.rank[i]] = i;
+    }
+}
+
+__global__ void k_cell_order(SysDev s) {
+    GRID_STRIDE(c, s.geo.ncells) {
+        const int b = s.start[c], e = s.start[c + 1];
+        for (int j = b + 1; j < e; ++j) {
+            const int v = s.src[j];
+            int k = j - 1;
+            while (k >= b && s.src[k] > v) {
+                s.src[k + 1] = s.src[k];
+                --k;
+            }
+            s.src[k + 1] = v;
+        }
+    }
+}
+
+__global__ void k_gather(SysDev s, int permute_force) {
+    const int nc = s.geo.ncells;
+    const int n_new = s.start[nc + 1];  // cells + OUT, without the dead
+    GRID_STRIDE(j, n_new) {
+        const int k = s.src[j];
+        s.pos_alt[j] = s.pos[k];
+        s.id_alt[j] = s.id[k];
+        const int ts = s.tslot[k];
+        s.tslot_alt[j] = ts;
+        if (ts >= 0) s.tloc[ts] = j;
+        if (permute_force) s.force_alt[j] = s.force[k];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        s.counters[C_N] = n_new;
+        s.counters[C_N_TOTAL] = n_new;
+        s.counters[C_N_INCELLS] = s.start[nc];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// K3 pair forces: one thread per particle, full (both-direction) stencil, force and half the pair
+// energies accumulated in registers; per-block FP64 energy partials in a fixed order
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(FORCE_THREADS) k_pair_forces(SysDev s) {
+    __shared__ int sh_tab[MAX_TYPES * MAX_TYPES];
+    __shared__ PairPot sh_pots[MAX_PAIR_POTENTIALS];
+    const Tables *tab = s.tab;
+    const int T = tab->ntypes, NP = tab->npots;
+    for (int k = threadIdx.x; k < T * T; k += blockDim.x) sh_tab[k] = tab->pair_tab[k];
+    for (int k = threadIdx.x; k < NP; k += blockDim.x) sh_pots[k] = tab->pots[k];
+    __syncthreads();
+    const int n = s.counters[C_N], n_in = s.counters[C_N_INCELLS];
+    double esum = 0.0;
+    GRID_STRIDE(i, n) {
+        float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+        if (i < n_in && NP > 0)
+            pair_force_at(i, s.pos[i], s.pos, s.start, s.geo, s.radius, sh_tab, sh_pots, T, fx, fy, fz, e);
+        s.force[i] = make_float4(fx, fy, fz, e);
+        esum += (double)e;
+    }
+    const double b = block_sum_double(esum);
+    if (threadIdx.x == 0) s.epart[blockIdx.x] = b;
+}
+
+// ------------------------------------------------------------------------------------------------
+// K4 bonded terms, one thread per topology particle gathering every term it takes part in
+// ------------------------------------------------------------------------------------------------
+__global__ void k_bonded(SysDev s) {
+    const Geo &g = s.geo;
+    double esum = 0.0;
+    GRID_STRIDE(t, s.n_top) {
+        const int j = s.tloc[t];
+        float fx = 0.f, fy = 0.f, fz = 0.f, eown = 0.f;
+        for (int q = s.top_off[t]; q < s.top_off[t + 1]; ++q) {
+            const int ref = s.top_terms[q];
+            const int kind = ref >> 28, role = (ref >> 24) & 0xf, idx = ref & 0xffffff;
+            float e = 0.f;
+            F3 f;
+            if (kind == 0) {
+                const int4 I = s.bond_idx[idx];
+                const float2 P = s.bond_par[idx];
+                if (P.x == 0.0f) continue;  // terms with k = 0 are skipped (CPUTopologyActions.cpp:62)
+                f = bond_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], P.x, P.y, g, role, e);
+            } else if (kind == 1) {
+                const int4 I = s.angle_idx[idx];
+                const float2 P = s.angle_par[idx];
+                f = angle_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], P.x, P.y, g, role, e);
+            } else {
+                const int4 I = s.dih_idx[idx];
+                const float4 P = s.dih_par[idx];
+                f = dihedral_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], s.pos[s.tloc[I.w]],
+                                   P.x, P.y, P.z, g, role, e);
+            }
+            fx += f.x; fy += f.y; fz += f.z;
+            if (role == 0) eown += e;  // each term's energy counted once
+        }
+        float4 cur = s.force[j];
+        cur.x += fx; cur.y += fy; cur.z += fz; cur.w += eown;
+        s.force[j] = cur;
+        esum += (double)eown;
+    }
+    const double b = block_sum_double(esum);
+    if (threadIdx.x == 0) s.epart[FORCE_BLOCKS + blockIdx.x] = b;
+}
+
+__global__ void k_energy_final(SysDev s, int pair, int bonded) {
+    double v = 0.0;
+    if (pair)
+        for (int k = threadIdx.x; k < FORCE_BLOCKS; k += blockDim.x) v += s.epart[k];
+    if (bonded)
+        for (int k = threadIdx.x; k < BONDED_BLOCKS; k += blockDim.x) v += s.epart[FORCE_BLOCKS + k];
+    const double b = block_sum_double(v);
+    if (threadIdx.x == 0) *s.energy = b;
+}
+
+// ------------------------------------------------------------------------------------------------
+// K6 reaction events that pass their acceptance coin
+// ------------------------------------------------------------------------------------------------
+__global__ void k_events(SysDev s, int handler) {
+    const int n = s.counters[C_N], n_in = s.counters[C_N_INCELLS];
+    const uint64_t step = s.step[1];
+    auto emit = [&](uint64_t key, int p1, int p2, int r) {
+        const int k = atomicAdd(&s.counters[C_N_EVENTS], 1);
+        if (k < s.event_capacity) {
+            EventRec ev;
+            ev.key = key; ev.p1 = p1; ev.p2 = p2; ev.reaction = r; ev.pad = 0;
+            s.events[k] = ev;
+        } else {
+            atomicOr(&s.counters[C_STATUS], ST_EVENTS);
+        }
+    };
+    GRID_STRIDE(i, n) {
+        events_at(i, i < n_in, s.pos, s.id, s.start, s.geo, s.radius, s.tab, s.seed, step, handler, emit);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// K7 one block: priority order, greedy maximal independent set, application of the winners
+// ------------------------------------------------------------------------------------------------
+constexpr int RESOLVE_THREADS = 1024;
+
+size_t resolve_smem_bytes() {
+    return (size_t)RESOLVE_MAX_EVENTS * (sizeof(uint64_t) + sizeof(int) + sizeof(int)) + 64;
+}
+
+__global__ void __launch_bounds__(RESOLVE_THREADS) k_resolve_apply(SysDev s, int handler) {
+    extern __shared__ unsigned char smem[];
+    uint64_t *key = reinterpret_cast<uint64_t *>(smem);
+    int *idx = reinterpret_cast<int *>(key + RESOLVE_MAX_EVENTS);
+    int *state = idx + RESOLVE_MAX_EVENTS;
+    int E = s.counters[C_N_EVENTS];
+    if (E > s.event_capacity) E = s.event_capacity;
+    ApplyTarget t;
+    t.pos = s.pos; t.id = s.id; t.tslot = s.tslot; t.force = s.force;
+    t.claim = s.claim; t.taken = s.taken; t.reaction_counts = s.reaction_counts;
+    t.n_total = s.counters[C_N_TOTAL];
+    t.capacity = s.capacity;
+    t.next_id = (uint32_t)s.counters[C_NEXT_ID];
+    ApplyResult res;
+    block_resolve_apply(s.events, E, RESOLVE_MAX_EVENTS, key, idx, state, s.tab, s.geo, s.seed, s.step[1], t, res);
+    if (threadIdx.x == 0) {
+        s.counters[C_N_TOTAL] = t.n_total + res.births;
+        s.counters[C_NEXT_ID] = (int)(t.next_id + (uint32_t)res.ids);
+        s.counters[C_N_BIRTHS] = res.births;
+        s.counters[C_N_EVENTS] = 0;
+        if (res.status) atomicOr(&s.counters[C_STATUS], res.status);
+        s.step[1] += 1;
+    }
+    (void)handler;
+}
+
+// ------------------------------------------------------------------------------------------------
+// observables and the parity pair list
+// ------------------------------------------------------------------------------------------------
+__global__ void k_count_types(SysDev s, unsigned long long *out) {
+    __shared__ unsigned int hist[MAX_TYPES];
+    const int T = s.tab->ntypes;
+    for (int k = threadIdx.x; k < T; k += blockDim.x) hist[k] = 0;
+    __syncthreads();
+    const int n = s.counters[C_N_TOTAL];
+    GRID_STRIDE(i, n) {
+        const int t = itype(s.pos[i]);
+        if (t >= 0 && t < T) atomicAdd(&hist[t], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < T; k += blockDim.x)
+        if (hist[k]) atomicAdd(&out[k], (unsigned long long)hist[k]);
+}
+
+// counts into the record ring when the step is a multiple of the stride
+__global__ void k_record_counts(SysDev s) {
+    const uint64_t t = s.step[0] - s.rec_base;
+    if (s.counts_stride <= 0 || t % (uint64_t)s.counts_stride != 0) return;
+    const int rec = s.counters[C_REC];
+    if (rec >= s.counts_max) return;
+    __shared__ unsigned int hist[MAX_TYPES];
+    const int T = s.tab->ntypes;
+    for (int k = threadIdx.x; k < T; k += blockDim.x) hist[k] = 0;
+    __syncthreads();
+    const int n = s.counters[C_N_TOTAL];
+    GRID_STRIDE(i, n) {
+        const int ty = itype(s.pos[i]);
+        if (ty >= 0 && ty < T) atomicAdd(&hist[ty], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < T; k += blockDim.x)
+        if (hist[k]) atomicAdd(&s.counts_ring[(size_t)rec * T + k], (unsigned long long)hist[k]);
+}
+
+__global__ void k_record_advance(SysDev s) {
+    const uint64_t t = s.step[0] - s.rec_base;
+    if (s.counts_stride > 0 && t % (uint64_t)s.counts_stride == 0 && s.counters[C_REC] < s.counts_max)
+        s.counters[C_REC] += 1;
+}
+
+__global__ void k_pairs(SysDev s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out) {
+    const int n_in = s.counters[C_N_INCELLS];
+    const Geo &g = s.geo;
+    GRID_STRIDE(i, n_in) {
+        const float4 p = s.pos[i];
+        int cx, cy, cz;
+        cell_coords(p, g, cx, cy, cz);
+        int ax[7], ay[7], az[7];
+        const int nx = axis_cells(cx, g.dims[0], g.pbc[0], s.radius, ax);
+        const int ny = axis_cells(cy, g.dims[1], g.pbc[1], s.radius, ay);
+        const int nz = axis_cells(cz, g.dims[2], g.pbc[2], s.radius, az);
+        const uint32_t idi = s.id[i];
+        for (int a = 0; a < nx; ++a)
+            for (int b = 0; b < ny; ++b)
+                for (int c = 0; c < nz; ++c) {
+                    const int cell = cell_index(ax[a], ay[b], az[c], g);
+                    const int jb = max(s.start[cell], i + 1), je = s.start[cell + 1];
+                    for (int j = jb; j < je; ++j) {
+                        const float4 q = s.pos[j];
+                        const PairGeom g0 = pair_geom(p, q, g);
+                        PairGeom gg = g0;
+                        if (!within(g0, gg, p, q, g, c2f, band, c2)) continue;
+                        const uint32_t idj = s.id[j];
+                        const int k = atomicAdd(n_out, 1);
+                        if (k < cap) out[k] = ((uint64_t)min(idi, idj) << 32) | max(idi, idj);
+                    }
+                }
+    }
+}
+
+__global__ void k_fill_ids(uint32_t *id, uint32_t first, int n) {
+    GRID_STRIDE(i, n) id[i] = first + (uint32_t)i;
+}
+
+// ------------------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------------------
+void init_kernel_attributes() {
+    RDC_CUDA(cudaFuncSetAttribute(k_resolve_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)resolve_smem_bytes()));
+}
+
+void launch_integrate_bin(const SysDev &s, bool integrate, cudaStream_t st) {
+    RDC_CUDA(cudaMemsetAsync(s.cnt, 0, sizeof(int) * (s.geo.ncells + 2), st));
+    k_integrate_bin<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, integrate ? 1 : 0, 1);
+    if (integrate) k_bd_step_advance<<<1, 1, 0, st>>>(s);
+}
+
+void launch_bin(const SysDev &s, cudaStream_t st) { launch_integrate_bin(s, false, st); }
+
+void launch_sort(const SysDev &s, bool permute_force, cudaStream_t st) {
+    const int nb = s.geo.ncells + 2;
+    launch_scan(s.cnt, s.start, s.scan_blocks, nb, st);
+    k_scatter<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
+    k_cell_order<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
+    k_gather<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, permute_force ? 1 : 0);
+}
+
+void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st) {
+    k_pair_forces<<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
+    if (bonded && s.n_top > 0) k_bonded<<<BONDED_BLOCKS, 256, 0, st>>>(s);
+    k_energy_final<<<1, 256, 0, st>>>(s, 1, (bonded && s.n_top > 0) ? 1 : 0);
+    (void)pair;
+}
+
+void launch_events(const SysDev &s, int handler, cudaStream_t st) {
+    k_events<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, handler);
+}
+
+void launch_resolve_apply(const SysDev &s, int handler, cudaStream_t st) {
+    k_resolve_apply<<<1, RESOLVE_THREADS, resolve_smem_bytes(), st>>>(s, handler);
+}
+
+void launch_count_types(const SysDev &s, unsigned long long *out, cudaStream_t st) {
+    RDC_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long) * MAX_TYPES, st));
+    k_count_types<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, out);
+}
+
+void launch_record_counts(const SysDev &s, cudaStream_t st) {
+    k_record_counts<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
+    k_record_advance<<<1, 1, 0, st>>>(s);
+}
+
+void launch_pairs(const SysDev &s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out,
+                  cudaStream_t st) {
+    k_pairs<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, c2f, band, c2, out, cap, n_out);
+}
+
+void launch_fill_ids(uint32_t *id, uint32_t first, int n, cudaStream_t st) {
+    if (n > 0) k_fill_ids<<<(n + 255) / 256, 256, 0, st>>>(id, first, n);
+}
+
+}  // namespace rdc

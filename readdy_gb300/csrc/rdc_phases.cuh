@@ -1,0 +1,409 @@
+// Per-particle and per-block phases shared by the grid-wide per-system kernels and the fused
+// batched-replica kernel.  Both paths call the same functions, so one replica advanced alone or
+// inside a batch performs the same arithmetic in the same order.
+#pragma once
+#include <climits>
+#include <cstdint>
+
+#include "rdc_device.cuh"
+#include "rdc_host.h"
+
+namespace rdc {
+
+// cells along one axis of the (2r+1)-stencil around c, each cell once
+__device__ inline int axis_cells(int c, int dim, int pbc, int r, int *out) {
+    int n = 0;
+    if (pbc && dim <= 2 * r + 1) {
+        for (int v = 0; v < dim; ++v) out[n++] = v;
+        return n;
+    }
+    for (int o = -r; o <= r; ++o) {
+        int v = c + o;
+        if (pbc) v = (v + dim) % dim;
+        else if (v < 0 || v >= dim) continue;
+        out[n++] = v;
+    }
+    return n;
+}
+
+// calls f(cell) for every cell of the stencil around the particle's cell, in a fixed order
+template <typename F>
+__device__ inline void for_each_stencil_cell(float4 p, const Geo &g, int radius, F f) {
+    int cx, cy, cz;
+    cell_coords(p, g, cx, cy, cz);
+    int ax[7], ay[7], az[7];
+    const int nx = axis_cells(cx, g.dims[0], g.pbc[0], radius, ax);
+    const int ny = axis_cells(cy, g.dims[1], g.pbc[1], radius, ay);
+    const int nz = axis_cells(cz, g.dims[2], g.pbc[2], radius, az);
+    for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b)
+            for (int c = 0; c < nz; ++c) f(cell_index(ax[a], ay[b], az[c], g));
+}
+
+// exclusive scan of one value per thread across the block; total receives the block sum
+__device__ inline int block_exclusive_scan(int v, int &total) {
+    __shared__ int warp_sums[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int before = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
+    total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before;
+}
+
+__device__ inline double block_sum_double(double v) {
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double r = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += red[w];
+    __syncthreads();
+    return r;
+}
+
+// Pair force and half pair energy on particle i (storage index inside the cells) from every
+// neighbour of the stencil; the full both-direction iteration of CPUCalculateForces.cpp:214-268.
+__device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const int *__restrict__ start,
+                                     const Geo &g, int radius, const int *tab, const PairPot *pots, int T, float &fx,
+                                     float &fy, float &fz, float &e) {
+    const int ti = itype(p);
+    for_each_stencil_cell(p, g, radius, [&](int cell) {
+        const int jb = start[cell], je = start[cell + 1];
+        for (int j = jb; j < je; ++j) {
+            if (j == i) continue;
+            const float4 q = pos[j];
+            const int tj = itype(q);
+            if (tj < 0) continue;
+            const int pt = tab[ti * T + tj];
+            if (pt == 0) continue;
+            const PairGeom g0 = pair_geom(p, q, g);
+            const int first = pt >> 8, cnt = pt & 0xff;
+            for (int k = first; k < first + cnt; ++k) {
+                const PairPot &pp = pots[k];
+                PairGeom gg = g0;
+                if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, fx, fy, fz, e);
+            }
+        }
+    });
+}
+
+// Euler-Maruyama update of one particle (CPUEulerBDIntegrator.cpp:66-73), FP32, Philox noise
+// keyed by (seed, particle id, integrator step)
+__device__ inline float4 euler_bd(float4 p, float fx, float fy, float fz, uint32_t id, uint64_t seed, uint64_t step,
+                                  const Tables *tab, const Geo &g) {
+    const int t = itype(p);
+    const float drift = tab->bd_drift[t], sc = tab->bd_scale[t];
+    float n0, n1, n2, n3;
+    normal4(rng_draw(seed, id, 0u, step, RNG_BD, 0u), n0, n1, n2, n3);
+    p.x = wrap1(p.x + (sc * n0 + fx * drift), g.L[0], g.hL[0], g.pbc[0]);
+    p.y = wrap1(p.y + (sc * n1 + fy * drift), g.L[1], g.hL[1], g.pbc[1]);
+    p.z = wrap1(p.z + (sc * n2 + fz * drift), g.L[2], g.hL[2], g.pbc[2]);
+    return p;
+}
+
+// ------------------------------------------------------------------------------------------------
+// reaction events that pass the acceptance coin u < 1 - exp(-k dt) (ReactionUtils.h:64-71)
+// ------------------------------------------------------------------------------------------------
+__device__ inline uint64_t coin_bits(U4 r) { return ((uint64_t)r.x << 32) | r.y; }
+
+__device__ inline uint64_t priority_key(U4 r, const ReactionDev &R, int handler) {
+    if (handler == H_GILLESPIE) {
+        // exponential clock E / k with E ~ Exp(1): the order of proportional-to-rate selection
+        // without replacement (algorithm.h:80-88)
+        const double u = ((double)r.z + 0.5) * (1.0 / 4294967296.0);
+        const double clock = -log(u) / R.rate;
+        return (uint64_t)__double_as_longlong(clock);  // positive doubles order like their bits
+    }
+    return ((uint64_t)r.z << 32) | r.w;  // uniformly random order (the shuffle, :198)
+}
+
+// order-1 events of particle i and order-2 events of the pairs (i, j > i); emit(key, p1, p2, r)
+// with p1 the particle of smaller id
+template <typename Emit>
+__device__ inline void events_at(int i, bool in_cells, const float4 *__restrict__ pos, const uint32_t *__restrict__ id,
+                                 const int *__restrict__ start, const Geo &g, int radius, const Tables *tab,
+                                 uint64_t seed, uint64_t step, int handler, Emit emit) {
+    const float4 p = pos[i];
+    const int ti = itype(p);
+    if (ti < 0) return;
+    const int T = tab->ntypes;
+    const uint32_t idi = id[i];
+    const int o1 = tab->o1_tab[ti];
+    for (int k = (o1 >> 8); k < (o1 >> 8) + (o1 & 0xff); ++k) {
+        const int r = tab->o1_list[k];
+        const ReactionDev &R = tab->reactions[r];
+        if (!(R.rate > 0)) continue;
+        const U4 u = rng_draw(seed, idi, 0u, step, RNG_COIN1, (uint32_t)r);
+        if (coin_bits(u) < R.coin_threshold) emit(priority_key(u, R, handler), i, i, r);
+    }
+    if (!in_cells || !tab->o2_any[ti]) return;
+    for_each_stencil_cell(p, g, radius, [&](int cell) {
+        const int jb = max(start[cell], i + 1), je = start[cell + 1];
+        for (int j = jb; j < je; ++j) {
+            const float4 q = pos[j];
+            const int tj = itype(q);
+            if (tj < 0) continue;
+            const int o2 = tab->o2_tab[ti * T + tj];
+            if (o2 == 0) continue;
+            const PairGeom g0 = pair_geom(p, q, g);
+            const uint32_t idj = id[j];
+            const uint32_t lo = min(idi, idj), hi = max(idi, idj);
+            for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
+                const int r = tab->o2_list[k];
+                const ReactionDev &R = tab->reactions[r];
+                if (!(R.rate > 0)) continue;
+                PairGeom gg = g0;
+                if (!within(g0, gg, p, q, g, R.educt_distance2f, R.band, R.educt_distance2)) continue;
+                const U4 u = rng_draw(seed, lo, hi, step, RNG_COIN2, (uint32_t)r);
+                if (coin_bits(u) < R.coin_threshold) {
+                    if (idi < idj) emit(priority_key(u, R, handler), i, j, r);
+                    else emit(priority_key(u, R, handler), j, i, r);
+                }
+            }
+        }
+    });
+}
+
+// ------------------------------------------------------------------------------------------------
+// block-level conflict resolution and application of accepted events
+// ------------------------------------------------------------------------------------------------
+struct ApplyTarget {
+    float4 *pos;
+    uint32_t *id;
+    int *tslot;    // may be null (replicas carry no topologies)
+    float4 *force; // may be null
+    int *claim, *taken;
+    unsigned long long *reaction_counts;
+    int n_total;   // storage size before the births
+    int capacity;
+    uint32_t next_id;
+};
+
+struct ApplyResult {
+    int births, ids, status, winners;
+};
+
+__device__ inline F3 fission_direction(uint64_t seed, uint32_t id1, uint64_t step, int r) {
+    float n0, n1, n2, n3;
+    normal4(rng_draw(seed, id1, 0u, step, RNG_FISSION, (uint32_t)r), n0, n1, n2, n3);
+    const float inv = rsqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+    return f3(n0 * inv, n1 * inv, n2 * inv);
+}
+
+// All threads of the block call this.  key/idx/state are shared-memory arrays of max_events
+// entries.  An event wins iff no earlier winner (by priority) shares a particle: the greedy scan of
+// CPUUncontrolledApproximation.cpp:206-253 and algorithm.h:62-136, computed in parallel rounds
+// (each round the undecided events that are minimal among the undecided events of both their
+// particles win, and the events touching a winner lose).
+__device__ inline void block_resolve_apply(const EventRec *events, int E, int max_events, uint64_t *key, int *idx,
+                                           int *state, const Tables *tab, const Geo &g, uint64_t seed,
+                                           uint64_t step, ApplyTarget t, ApplyResult &res) {
+    __shared__ int sh_any, sh_births, sh_ids, sh_status, sh_win;
+    if (threadIdx.x == 0) sh_status = 0;
+    if (E > max_events) {
+        if (threadIdx.x == 0) sh_status |= ST_EVENTS;
+        E = max_events;
+    }
+    int P = 1;
+    while (P < E) P <<= 1;
+    for (int k = threadIdx.x; k < P; k += blockDim.x) {
+        key[k] = k < E ? events[k].key : ~0ull;
+        idx[k] = k < E ? k : INT_MAX;
+    }
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int k = threadIdx.x; k < P; k += blockDim.x) {
+                const int l = k ^ stride;
+                if (l > k) {
+                    const bool up = (k & size) == 0;
+                    const bool gt = key[k] > key[l] || (key[k] == key[l] && idx[k] > idx[l]);
+                    if (gt == up) {
+                        const uint64_t tk = key[k]; key[k] = key[l]; key[l] = tk;
+                        const int ti = idx[k]; idx[k] = idx[l]; idx[l] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int k = threadIdx.x; k < E; k += blockDim.x) state[k] = 0;
+    __syncthreads();
+    for (int round = 0;; ++round) {
+        for (int k = threadIdx.x; k < E; k += blockDim.x)
+            if (state[k] == 0) {
+                const EventRec ev = events[idx[k]];
+                atomicMin(&t.claim[ev.p1], k);
+                if (ev.p2 != ev.p1) atomicMin(&t.claim[ev.p2], k);
+            }
+        __syncthreads();
+        for (int k = threadIdx.x; k < E; k += blockDim.x)
+            if (state[k] == 0) {
+                const EventRec ev = events[idx[k]];
+                if (t.claim[ev.p1] == k && t.claim[ev.p2] == k) {
+                    state[k] = 1;
+                    t.taken[ev.p1] = 1;
+                    t.taken[ev.p2] = 1;
+                }
+            }
+        if (threadIdx.x == 0) sh_any = 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < E; k += blockDim.x) {
+            const EventRec ev = events[idx[k]];
+            if (state[k] == 0) {
+                if (t.taken[ev.p1] || t.taken[ev.p2]) state[k] = 2;
+                else sh_any = 1;
+            }
+            t.claim[ev.p1] = INT_MAX;
+            t.claim[ev.p2] = INT_MAX;
+        }
+        __syncthreads();
+        if (!sh_any) break;
+        if (round >= 255) {
+            if (threadIdx.x == 0) sh_status |= ST_RESOLVE_ROUNDS;
+            break;
+        }
+        __syncthreads();
+    }
+    // births and new ids of the winners in priority order; offsets reuse the key storage
+    int *boff = reinterpret_cast<int *>(key);
+    int *ioff = boff + max_events;
+    if (threadIdx.x == 0) {
+        int nb = 0, ni = 0, nw = 0;
+        for (int k = 0; k < E; ++k) {
+            boff[k] = nb;
+            ioff[k] = ni;
+            if (state[k] != 1) continue;
+            ++nw;
+            switch (tab->reactions[events[idx[k]].reaction].kind) {
+                case R_CONVERSION: ni += 1; break;
+                case R_ENZYMATIC: ni += 1; break;
+                case R_FISSION: nb += 1; ni += 2; break;
+                case R_FUSION: nb += 1; ni += 1; break;
+                default: break;
+            }
+        }
+        sh_births = nb;
+        sh_ids = ni;
+        sh_win = nw;
+    }
+    __syncthreads();
+    const bool room = t.n_total + sh_births <= t.capacity;
+    for (int k = threadIdx.x; k < E; k += blockDim.x) {
+        const EventRec ev = events[idx[k]];
+        t.taken[ev.p1] = 0;
+        t.taken[ev.p2] = 0;
+        if (state[k] != 1) continue;
+        const ReactionDev &R = tab->reactions[ev.reaction];
+        const int bslot = t.n_total + boff[k];
+        const uint32_t nid = t.next_id + (uint32_t)ioff[k];
+        float4 p1 = t.pos[ev.p1];
+        switch (R.kind) {
+            case R_DECAY:  // ReactionUtils.h:164-167
+                p1.w = __int_as_float(-1);
+                t.pos[ev.p1] = p1;
+                break;
+            case R_CONVERSION:  // :168-173
+                p1.w = __int_as_float(R.product[0]);
+                t.pos[ev.p1] = p1;
+                t.id[ev.p1] = nid;
+                break;
+            case R_ENZYMATIC: {  // :174-189, the non-catalyst converts
+                if (itype(p1) == R.educt[1]) {
+                    float4 p2 = t.pos[ev.p2];
+                    p2.w = __int_as_float(R.product[0]);
+                    t.pos[ev.p2] = p2;
+                    t.id[ev.p2] = nid;
+                } else {
+                    p1.w = __int_as_float(R.product[0]);
+                    t.pos[ev.p1] = p1;
+                    t.id[ev.p1] = nid;
+                }
+                break;
+            }
+            case R_FISSION: {  // :190-207
+                if (!room) break;
+                const F3 dir = fission_direction(seed, t.id[ev.p1], step, ev.reaction);
+                const float a = R.w2 * R.product_distance, b = R.w1 * R.product_distance;
+                float4 q;
+                q.x = wrap1(p1.x - a * dir.x, g.L[0], g.hL[0], g.pbc[0]);
+                q.y = wrap1(p1.y - a * dir.y, g.L[1], g.hL[1], g.pbc[1]);
+                q.z = wrap1(p1.z - a * dir.z, g.L[2], g.hL[2], g.pbc[2]);
+                q.w = __int_as_float(R.product[1]);
+                t.pos[bslot] = q;
+                t.id[bslot] = nid;
+                if (t.tslot) t.tslot[bslot] = -1;
+                if (t.force) t.force[bslot] = make_float4(0.f, 0.f, 0.f, 0.f);
+                p1.x = wrap1(p1.x + b * dir.x, g.L[0], g.hL[0], g.pbc[0]);
+                p1.y = wrap1(p1.y + b * dir.y, g.L[1], g.hL[1], g.pbc[1]);
+                p1.z = wrap1(p1.z + b * dir.z, g.L[2], g.hL[2], g.pbc[2]);
+                p1.w = __int_as_float(R.product[0]);
+                t.pos[ev.p1] = p1;
+                t.id[ev.p1] = nid + 1u;
+                break;
+            }
+            case R_FUSION: {  // :208-225
+                if (!room) break;
+                const float4 p2 = t.pos[ev.p2];
+                const float w = (R.educt[0] == itype(p1)) ? R.w1 : R.w2;
+                const float dx = mi1(p2.x - p1.x, g.L[0], g.hL[0], g.pbc[0]);
+                const float dy = mi1(p2.y - p1.y, g.L[1], g.hL[1], g.pbc[1]);
+                const float dz = mi1(p2.z - p1.z, g.L[2], g.hL[2], g.pbc[2]);
+                float4 q;
+                q.x = wrap1(p1.x + w * dx, g.L[0], g.hL[0], g.pbc[0]);
+                q.y = wrap1(p1.y + w * dy, g.L[1], g.hL[1], g.pbc[1]);
+                q.z = wrap1(p1.z + w * dz, g.L[2], g.hL[2], g.pbc[2]);
+                q.w = __int_as_float(R.product[0]);
+                t.pos[bslot] = q;
+                t.id[bslot] = nid;
+                if (t.tslot) t.tslot[bslot] = -1;
+                if (t.force) t.force[bslot] = make_float4(0.f, 0.f, 0.f, 0.f);
+                p1.w = __int_as_float(-1);
+                t.pos[ev.p1] = p1;
+                float4 d2 = p2;
+                d2.w = __int_as_float(-1);
+                t.pos[ev.p2] = d2;
+                break;
+            }
+            default:
+                break;
+        }
+        if (t.reaction_counts) atomicAdd(&t.reaction_counts[R.id], 1ull);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int st = sh_status;
+        if (!room && sh_births > 0) st |= ST_CAPACITY;
+        if ((uint64_t)t.next_id + (uint64_t)sh_ids > 0xFFFFFF00ull) st |= ST_ID_OVERFLOW;
+        sh_status = st;
+    }
+    __syncthreads();
+    res.births = room ? sh_births : 0;
+    res.ids = sh_ids;
+    res.status = sh_status;
+    res.winners = sh_win;
+    __syncthreads();
+}
+
+}  // namespace rdc

@@ -1,0 +1,248 @@
+"""The "CUDA" kernel: a ReaDDy model::Kernel over the C ABI.
+
+``Context`` mirrors model::Context (box, periodicity, kBT, species, potential, reaction and topology
+registries) and ``CUDAKernel`` mirrors a kernel instance with its state model and action factory
+(include/readdy/model/Kernel.h:71-235, StateModel.h:53-118, actions/ActionFactory.h:56-129).
+Every method is one call into libreaddy_cuda_core.so; nothing runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+KERNEL_NAME = "CUDA"
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Context:
+    """Physical description of a system (include/readdy/model/Context.h)."""
+
+    def __init__(self, box_size, periodic_boundary_conditions=(True, True, True), kbt=1.0,
+                 diffusion_constants=(1.0,)):
+        self._lib = N.load()
+        box = np.ascontiguousarray(box_size, dtype=np.float64)
+        pbc = np.ascontiguousarray([int(bool(x)) for x in periodic_boundary_conditions], dtype=np.int32)
+        D = np.ascontiguousarray(diffusion_constants, dtype=np.float64)
+        h = C.c_void_p()
+        N.check(self._lib.rdc_context_create(C.byref(h), _p(box, C.c_double), _p(pbc, C.c_int), float(kbt),
+                                             len(D), _p(D, C.c_double)))
+        self._h = h
+        self.box_size = tuple(float(np.float32(x)) for x in box)
+        self.periodic_boundary_conditions = tuple(bool(x) for x in pbc)
+        self.kbt = float(kbt)
+        self.diffusion_constants = tuple(float(x) for x in D)
+        self.n_types = len(D)
+        self.n_reactions = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.rdc_context_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def calculate_max_cutoff(self) -> float:
+        c = C.c_double()
+        N.check(self._lib.rdc_context_max_cutoff(self._h, C.byref(c)))
+        return c.value
+
+    # PotentialRegistry
+    def add_harmonic_repulsion(self, t1, t2, force_constant, interaction_distance):
+        N.check(self._lib.rdc_context_add_harmonic_repulsion(self._h, t1, t2, force_constant, interaction_distance))
+
+    def add_weak_interaction_piecewise_harmonic(self, t1, t2, force_constant, desired_distance, depth,
+                                                no_interaction_distance):
+        N.check(self._lib.rdc_context_add_weak_interaction_piecewise_harmonic(
+            self._h, t1, t2, force_constant, desired_distance, depth, no_interaction_distance))
+
+    def add_lennard_jones(self, t1, t2, m, n, cutoff, shift, epsilon, sigma):
+        N.check(self._lib.rdc_context_add_lennard_jones(self._h, t1, t2, m, n, cutoff, int(bool(shift)),
+                                                        epsilon, sigma))
+
+    def add_screened_electrostatics(self, t1, t2, electrostatic_strength, inverse_screening_depth,
+                                    repulsion_strength, repulsion_distance, exponent, cutoff):
+        N.check(self._lib.rdc_context_add_screened_electrostatics(
+            self._h, t1, t2, electrostatic_strength, inverse_screening_depth, repulsion_strength,
+            repulsion_distance, exponent, cutoff))
+
+    # ReactionRegistry
+    def _rid(self, rc, rid):
+        N.check(rc)
+        self.n_reactions = max(self.n_reactions, rid.value + 1)
+        return rid.value
+
+    def add_conversion(self, type_from, type_to, rate):
+        rid = C.c_int()
+        return self._rid(self._lib.rdc_context_add_conversion(self._h, type_from, type_to, rate, C.byref(rid)), rid)
+
+    def add_decay(self, type_from, rate):
+        rid = C.c_int()
+        return self._rid(self._lib.rdc_context_add_decay(self._h, type_from, rate, C.byref(rid)), rid)
+
+    def add_fusion(self, type_from1, type_from2, type_to, rate, educt_distance, weight1=0.5, weight2=0.5):
+        rid = C.c_int()
+        return self._rid(self._lib.rdc_context_add_fusion(self._h, type_from1, type_from2, type_to, rate,
+                                                          educt_distance, weight1, weight2, C.byref(rid)), rid)
+
+    def add_fission(self, type_from, type_to1, type_to2, rate, product_distance, weight1=0.5, weight2=0.5):
+        rid = C.c_int()
+        return self._rid(self._lib.rdc_context_add_fission(self._h, type_from, type_to1, type_to2, rate,
+                                                           product_distance, weight1, weight2, C.byref(rid)), rid)
+
+    def add_enzymatic(self, type_catalyst, type_from, type_to, rate, educt_distance):
+        rid = C.c_int()
+        return self._rid(self._lib.rdc_context_add_enzymatic(self._h, type_catalyst, type_from, type_to, rate,
+                                                             educt_distance, C.byref(rid)), rid)
+
+    # TopologyRegistry potential configuration
+    def configure_harmonic_bond(self, t1, t2, force_constant=1.0, length=1.0):
+        N.check(self._lib.rdc_context_configure_harmonic_bond(self._h, t1, t2, force_constant, length))
+
+    def configure_harmonic_angle(self, t1, t2, t3, force_constant=1.0, equilibrium_angle=0.0):
+        N.check(self._lib.rdc_context_configure_harmonic_angle(self._h, t1, t2, t3, force_constant,
+                                                               equilibrium_angle))
+
+    def configure_cosine_dihedral(self, t1, t2, t3, t4, force_constant=1.0, multiplicity=1, phi0=0.0):
+        N.check(self._lib.rdc_context_configure_cosine_dihedral(self._h, t1, t2, t3, t4, force_constant,
+                                                                float(multiplicity), phi0))
+
+
+class CUDAKernel:
+    """One simulation on the GPU: state model plus the ActionFactory's actions."""
+
+    name = KERNEL_NAME
+
+    def __init__(self, context: Context, seed: int = 0):
+        self._lib = N.load()
+        self.context = context
+        h = C.c_void_p()
+        N.check(self._lib.rdc_system_create(C.byref(h), context.handle, int(seed) & (2 ** 64 - 1)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.rdc_system_destroy(h)
+            self._h = None
+
+    # ---- StateModel ----
+    def add_particles(self, positions, types):
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(types, dtype=np.int32), (len(pos),)))
+        ids = np.zeros(len(pos), np.uint64)
+        N.check(self._lib.rdc_add_particles(self._h, len(pos), _p(pos, C.c_double), _p(t, C.c_int),
+                                            _p(ids, C.c_uint64)))
+        return ids
+
+    def add_topology(self, positions, types, edges):
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(types, dtype=np.int32), (len(pos),)))
+        e = np.ascontiguousarray(np.asarray(edges, dtype=np.int64).reshape(-1, 2))
+        ids = np.zeros(len(pos), np.uint64)
+        N.check(self._lib.rdc_add_topology(self._h, len(pos), _p(pos, C.c_double), _p(t, C.c_int), len(e),
+                                           _p(e, C.c_int64), _p(ids, C.c_uint64)))
+        return ids
+
+    @property
+    def n_particles(self) -> int:
+        n = C.c_int64()
+        N.check(self._lib.rdc_get_n_particles(self._h, C.byref(n)))
+        return n.value
+
+    def get_particles(self):
+        """(positions[n,3] float64, types[n] int32, ids[n] uint64) in device storage order."""
+        n = self.n_particles
+        pos = np.zeros((n, 3)); t = np.zeros(n, np.int32); ids = np.zeros(n, np.uint64)
+        got = C.c_int64()
+        N.check(self._lib.rdc_get_particles(self._h, n, _p(pos, C.c_double), _p(t, C.c_int),
+                                            _p(ids, C.c_uint64), C.byref(got)))
+        return pos[:got.value], t[:got.value], ids[:got.value]
+
+    def get_forces(self):
+        n = self.n_particles
+        f = np.zeros((n, 3)); ids = np.zeros(n, np.uint64)
+        got = C.c_int64()
+        N.check(self._lib.rdc_get_forces(self._h, n, _p(f, C.c_double), _p(ids, C.c_uint64), C.byref(got)))
+        return f[:got.value], ids[:got.value]
+
+    @property
+    def energy(self) -> float:
+        e = C.c_double()
+        N.check(self._lib.rdc_get_energy(self._h, C.byref(e)))
+        return e.value
+
+    def count_types(self):
+        out = np.zeros(self.context.n_types, np.int64)
+        N.check(self._lib.rdc_count_types(self._h, _p(out, C.c_int64)))
+        return out
+
+    def reaction_counts(self):
+        n = max(self.context.n_reactions, 1)
+        out = np.zeros(n, np.int64)
+        N.check(self._lib.rdc_get_reaction_counts(self._h, n, _p(out, C.c_int64)))
+        return out[:self.context.n_reactions]
+
+    def reserve(self, capacity):
+        N.check(self._lib.rdc_reserve(self._h, int(capacity)))
+
+    def set_cell_radius(self, radius):
+        N.check(self._lib.rdc_set_cell_radius(self._h, int(radius)))
+
+    # ---- actions ----
+    def initialize(self):
+        N.check(self._lib.rdc_initialize(self._h))
+
+    def create_neighbor_list(self, cutoff):
+        N.check(self._lib.rdc_nl_create(self._h, float(cutoff)))
+
+    def update_neighbor_list(self):
+        N.check(self._lib.rdc_nl_update(self._h))
+
+    def clear_neighbor_list(self):
+        N.check(self._lib.rdc_nl_clear(self._h))
+
+    def calculate_forces(self):
+        N.check(self._lib.rdc_calculate_forces(self._h))
+
+    def euler_bd_integrator(self, dt):
+        N.check(self._lib.rdc_euler_bd_integrate(self._h, float(dt)))
+
+    def uncontrolled_approximation(self, dt):
+        N.check(self._lib.rdc_uncontrolled_approximation(self._h, float(dt)))
+
+    def gillespie(self, dt):
+        N.check(self._lib.rdc_gillespie(self._h, float(dt)))
+
+    def run(self, n_steps, dt, handler=N.UNCONTROLLED_APPROXIMATION, count_stride=0):
+        """SimulationLoop::run on the device; returns per-type counts every count_stride steps."""
+        nrec = (n_steps // count_stride + 1) if count_stride > 0 else 0
+        counts = np.zeros((max(nrec, 1), self.context.n_types), np.int64)
+        got = C.c_int64()
+        N.check(self._lib.rdc_run(self._h, int(n_steps), float(dt), int(handler), int(count_stride),
+                                  _p(counts, C.c_int64) if nrec else None, nrec, C.byref(got)))
+        return counts[:got.value]
+
+    def neighbor_pairs(self, cutoff):
+        """Sorted (min id, max id) pairs with d^2 < cutoff^2 from the current cell list."""
+        cap = max(1024, 64 * self.n_particles)
+        while True:
+            out = np.zeros((cap, 2), np.uint64)
+            n = C.c_int64()
+            rc = self._lib.rdc_nl_pairs(self._h, float(cutoff), cap, _p(out, C.c_uint64), C.byref(n))
+            if rc == N.RDC_ERR_CAPACITY and n.value > cap:
+                cap = int(n.value) + 16
+                continue
+            N.check(rc)
+            return out[:n.value].copy()
+
+    def synchronize(self):
+        N.check(self._lib.rdc_synchronize(self._h))

@@ -1,0 +1,99 @@
+"""Builds the same system on the CUDA kernel and on the FP64 oracle from one description."""
+import numpy as np
+
+import oracle
+
+
+def _pot_args(kind, p):
+    if kind == "harmonic_repulsion":
+        return (p["k"], p["d"])
+    if kind == "weak_interaction_piecewise_harmonic":
+        return (p["k"], p["desired"], p["depth"], p["cutoff"])
+    if kind == "lennard_jones":
+        return (p["m"], p["n"], p["cutoff"], p["shift"], p["epsilon"], p["sigma"])
+    if kind == "screened_electrostatics":
+        return (p["C"], p["kappa"], p["D"], p["sigma"], p["exponent"], p["cutoff"])
+    raise KeyError(kind)
+
+
+def make_context(spec):
+    import readdy_gb300 as rg
+    ctx = rg.Context(spec["box"], spec.get("periodic", (True, True, True)), spec.get("kbt", 1.0),
+                     spec["diffusion"])
+    for kind, t1, t2, p in spec.get("potentials", []):
+        getattr(ctx, "add_" + kind)(t1, t2, *_pot_args(kind, p))
+    for kind, p in spec.get("reactions", []):
+        if kind == "fusion":
+            ctx.add_fusion(p["a"], p["b"], p["c"], p["rate"], p["educt_distance"], p.get("w1", .5), p.get("w2", .5))
+        elif kind == "fission":
+            ctx.add_fission(p["a"], p["b"], p["c"], p["rate"], p["product_distance"], p.get("w1", .5),
+                            p.get("w2", .5))
+        elif kind == "conversion":
+            ctx.add_conversion(p["a"], p["b"], p["rate"])
+        elif kind == "decay":
+            ctx.add_decay(p["a"], p["rate"])
+        elif kind == "enzymatic":
+            ctx.add_enzymatic(p["catalyst"], p["a"], p["b"], p["rate"], p["educt_distance"])
+    return ctx
+
+
+def make_oracle(spec, seed=1, n_threads=1, cll_radius=1):
+    box = [float(np.float32(b)) for b in spec["box"]]
+    s = oracle.OracleSystem(box, spec.get("periodic", (True, True, True)), spec.get("kbt", 1.0),
+                            spec["diffusion"], seed=seed, n_threads=n_threads, cll_radius=cll_radius)
+    for kind, t1, t2, p in spec.get("potentials", []):
+        getattr(s, "add_" + kind)(t1, t2, *_pot_args(kind, p))
+    for kind, p in spec.get("reactions", []):
+        if kind == "fusion":
+            s.add_fusion(p["a"], p["b"], p["c"], p["rate"], p["educt_distance"], p.get("w1", .5), p.get("w2", .5))
+        elif kind == "fission":
+            s.add_fission(p["a"], p["b"], p["c"], p["rate"], p["product_distance"], p.get("w1", .5), p.get("w2", .5))
+        elif kind == "conversion":
+            s.add_conversion(p["a"], p["b"], p["rate"])
+        elif kind == "decay":
+            s.add_decay(p["a"], p["rate"])
+        elif kind == "enzymatic":
+            s.add_enzymatic(p["catalyst"], p["a"], p["b"], p["rate"], p["educt_distance"])
+    return s
+
+
+def f32(a):
+    """Values as the device holds them (FP32), widened back to FP64."""
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def by_id(ids, *arrays):
+    o = np.argsort(ids)
+    return [np.asarray(a)[o] for a in arrays]
+
+
+def crowded_spec(n=20000, density=0.2, seed=0):
+    """The three-species crowded chemistry of the 200k-particle benchmark at a smaller size."""
+    L = float(np.float32((n / density) ** (1 / 3)))
+    rng = np.random.default_rng(seed)
+    pos = (rng.random((n, 3)) - 0.5) * L
+    types = rng.choice(3, size=n, p=[0.5, 0.3, 0.2])
+    spec = dict(
+        box=(L, L, L), periodic=(True, True, True), diffusion=(1.0, 0.5, 0.2),
+        potentials=[("lennard_jones", 0, 0, dict(m=12, n=6, cutoff=2.5, shift=True, epsilon=1.0, sigma=1.0)),
+                    ("weak_interaction_piecewise_harmonic", 1, 1, dict(k=10.0, desired=1.0, depth=0.5,
+                                                                       cutoff=1.5)),
+                    ("harmonic_repulsion", 0, 1, dict(k=10.0, d=1.0)),
+                    ("harmonic_repulsion", 0, 2, dict(k=10.0, d=1.0)),
+                    ("harmonic_repulsion", 1, 2, dict(k=10.0, d=1.0)),
+                    ("harmonic_repulsion", 2, 2, dict(k=10.0, d=1.0))],
+        reactions=[("conversion", dict(a=0, b=1, rate=0.01))],
+    )
+    return spec, pos, types
+
+
+def abc_spec(n=2000, box=20.0, seed=0):
+    """A + B <-> C with harmonic repulsion between all species (the 1000 A + 1000 B workload)."""
+    rng = np.random.default_rng(seed)
+    pos = (rng.random((n, 3)) - 0.5) * box
+    types = np.array([0] * (n // 2) + [1] * (n - n // 2))
+    pots = [("harmonic_repulsion", a, b, dict(k=10.0, d=1.0)) for a in range(3) for b in range(a, 3)]
+    spec = dict(box=(box, box, box), periodic=(True, True, True), diffusion=(1.0, 1.0, 0.5), potentials=pots,
+                reactions=[("fusion", dict(a=0, b=1, c=2, rate=1.0, educt_distance=1.0)),
+                           ("fission", dict(a=2, b=0, c=1, rate=0.1, product_distance=1.0))])
+    return spec, pos, types

@@ -1,0 +1,60 @@
+"""The C ABI library builds, loads and exports every entry point include/*.h declares.
+
+No compute call is made here: these run on machines without a GPU.
+"""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(rdc_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "rdc_system_create" in names and "rdc_batch_step" in names
+    assert len(names) >= 40
+
+
+def test_library_exports_every_declared_symbol():
+    from readdy_gb300 import _native
+    lib = _native.load()
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_kernel_name_and_version_without_gpu():
+    from readdy_gb300 import _native
+    lib = _native.load()
+    assert lib.rdc_kernel_name().decode() == "CUDA"
+    assert lib.rdc_version() >= 1000
+
+
+def test_context_registries_validate_like_the_reference():
+    """Argument checks of the registries need no device (Potentials.cpp:163-201, TorsionPotential.h:63-67)."""
+    import readdy_gb300 as rg
+    ctx = rg.Context((10, 10, 10), diffusion_constants=(1.0, 0.5))
+    with pytest.raises(ValueError, match="not greater than the second exponent"):
+        ctx.add_lennard_jones(0, 0, 6, 12, 2.5, True, 1.0, 1.0)
+    with pytest.raises(ValueError, match="inverse screening depth"):
+        ctx.add_screened_electrostatics(0, 0, -1.0, -1.0, 1.0, 1.0, 6, 8.0)
+    with pytest.raises(ValueError, match="equilibrium angle"):
+        ctx.configure_cosine_dihedral(0, 0, 0, 0, 1.0, 3, 4.0)
+    with pytest.raises(ValueError, match="type out of range"):
+        ctx.add_harmonic_repulsion(0, 5, 1.0, 1.0)
+    ctx.add_harmonic_repulsion(0, 1, 10.0, 1.0)
+    ctx.add_fusion(0, 1, 1, 1.0, 1.5)
+    assert ctx.calculate_max_cutoff() == pytest.approx(1.5)
+    assert ctx.add_fission(1, 0, 1, 0.1, 1.0) == 1

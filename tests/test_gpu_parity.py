@@ -1,0 +1,307 @@
+"""Parity of the CUDA kernel with the FP64 oracle and with the reference's known answers.
+
+Tolerances (FP32 device arithmetic against FP64):
+  * neighbour pair sets: bit-exact;
+  * forces: |F_gpu - F_ref| <= 1e-5 * max(|F_ref|, 1e-2 * F_rms) per particle, where F_rms is the
+    root-mean-square force of the system (the absolute floor guards particles whose net force
+    cancels to near zero); energies: relative 1e-5;
+  * known-answer vectors: the reference test's own tolerance or 1e-5 relative, whichever is looser.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests.golden import known_answers as ka
+from tests.helpers import abc_spec, by_id, crowded_spec, f32, make_context, make_oracle
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-5
+ENERGY_RTOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def rg():
+    import readdy_gb300
+    readdy_gb300.load()
+    return readdy_gb300
+
+
+def gpu_system(rg, spec, pos, types, seed=1):
+    ctx = make_context(spec)
+    k = rg.CUDAKernel(ctx, seed=seed)
+    k.add_particles(pos, types)
+    return ctx, k
+
+
+def force_error(f_gpu, f_ref):
+    rms = np.sqrt(np.mean(np.sum(f_ref ** 2, axis=1))) if len(f_ref) else 0.0
+    denom = np.maximum(np.linalg.norm(f_ref, axis=1), 1e-2 * rms)
+    denom = np.where(denom > 0, denom, 1.0)
+    return np.linalg.norm(f_gpu - f_ref, axis=1) / denom
+
+
+@pytest.mark.parametrize("case", ka.PAIR_CASES, ids=lambda c: c["name"])
+def test_pair_potential_known_answers(rg, case):
+    spec = dict(box=case["box"], periodic=case["periodic"], diffusion=case["diffusion"],
+                potentials=[(k, a, b, p) for k, a, b, p in case["potentials"]])
+    ctx, k = gpu_system(rg, spec, np.array(case["positions"], float), np.array(case["types"]))
+    k.create_neighbor_list(ctx.calculate_max_cutoff())
+    k.calculate_forces()
+    k.calculate_forces()  # must not accumulate (TestStateModel.cpp:80-81)
+    e = k.energy
+    assert e == pytest.approx(case["energy"], rel=max(case.get("energy_rtol", 0), ENERGY_RTOL))
+    f, ids = k.get_forces()
+    (f,) = by_id(ids, f)
+    exp = np.array(ka.per_particle_forces(case))
+    scale = max(np.abs(exp).max(), 1e-12)
+    np.testing.assert_allclose(f, exp, rtol=0, atol=max(case["force_atol"], FORCE_RTOL * scale))
+
+
+@pytest.mark.parametrize("case", ka.BONDED_CASES, ids=lambda c: c["name"])
+def test_bonded_known_answers(rg, case):
+    ctx = rg.Context(case["box"], case["periodic"], 1.0, (1.0,))
+    for idx, kf, l0 in case["bonds"]:
+        ctx.configure_harmonic_bond(0, 0, kf, l0)
+    for idx, kf, th in case["angles"]:
+        ctx.configure_harmonic_angle(0, 0, 0, kf, th)
+    for idx, kf, mult, phi0 in case["dihedrals"]:
+        ctx.configure_cosine_dihedral(0, 0, 0, 0, kf, mult, phi0)
+    n = len(case["positions"])
+    edges = [(i, i + 1) for i in range(n - 1)]
+    if not case["bonds"]:
+        # every edge needs a bond configuration (GraphTopology.cpp:89-99); k = 0 bonds are skipped
+        ctx.configure_harmonic_bond(0, 0, 0.0, 1.0)
+    k = rg.CUDAKernel(ctx)
+    k.add_topology(np.array(case["positions"], float), np.zeros(n, np.int32), edges)
+    k.calculate_forces()
+    e = k.energy
+    assert e == pytest.approx(case["energy"], rel=max(case["energy_rtol"], ENERGY_RTOL), abs=1e-6)
+    f, ids = k.get_forces()
+    (f,) = by_id(ids, f)
+    exp = np.array(case["forces"], float)
+    np.testing.assert_allclose(f, exp, rtol=0, atol=max(case["force_atol"], 2e-5 * np.abs(exp).max()))
+
+
+NL_BOXES = [((10, 10, 10), (1, 1, 1)), ((10, 10, 10), (0, 0, 0)), ((5, 12, 7), (1, 0, 1)),
+            ((3.3, 3.3, 3.3), (1, 1, 1)), ((2.5, 8, 2.5), (1, 1, 0)), ((20, 4, 4), (1, 1, 1)),
+            ((6, 6, 30), (0, 1, 1))]
+
+
+@pytest.mark.parametrize("box,pbc", NL_BOXES)
+@pytest.mark.parametrize("radius", [1, 2])
+def test_neighbor_pairs_bit_exact(rg, box, pbc, radius):
+    """kernels/cpu/test/TestNeighborList.cpp:267-362 on the device: the pair set equals the oracle's."""
+    rng = np.random.default_rng(17)
+    spec = dict(box=box, periodic=pbc, diffusion=(1.0, 1.0),
+                potentials=[("harmonic_repulsion", 0, 1, dict(k=1.0, d=1.2)),
+                            ("harmonic_repulsion", 0, 0, dict(k=1.0, d=0.9))])
+    n = 600
+    pos = (rng.random((n, 3)) - 0.5) * np.array(box, float)
+    types = rng.integers(0, 2, n)
+    ctx, k = gpu_system(rg, spec, pos, types)
+    k.set_cell_radius(radius)
+    k.create_neighbor_list(1.2)
+    for step in range(3):
+        p, t, ids = k.get_particles()
+        o = make_oracle(spec)
+        (p, t, ids) = by_id(ids, p, t, ids)
+        o.add_particles(p, t)  # oracle ids 0..n-1 follow the id order of the device
+        ref = o.brute_force_pairs(1.2)
+        got = k.neighbor_pairs(1.2)
+        id_of = ids.astype(np.uint64)
+        ref_ids = np.sort(np.stack([id_of[ref[:, 0].astype(int)], id_of[ref[:, 1].astype(int)]], 1), axis=1)
+        ref_ids = ref_ids[np.lexsort((ref_ids[:, 1], ref_ids[:, 0]))]
+        assert len(got) > 0
+        np.testing.assert_array_equal(got, ref_ids)
+        k.euler_bd_integrator(0.01)
+        k.update_neighbor_list()
+
+
+def test_neighbor_pairs_at_the_cutoff(rg):
+    """Pairs placed within a few ulp of the cutoff are decided exactly like the FP64 reference."""
+    L = 50.0
+    rc = 1.0
+    pts, types = [], []
+    rng = np.random.default_rng(3)
+    for i in range(400):
+        a = (rng.random(3) - 0.5) * (L - 4)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        r = np.float64(rc) * (1 + rng.integers(-4, 5) * 2.0 ** -24)
+        b = a + r * d
+        pts += [a, b]
+        types += [0, 0]
+    # pairs straddling the periodic boundary
+    for i in range(100):
+        a = np.array([L / 2 - 0.3, (rng.random() - 0.5) * L, (rng.random() - 0.5) * L])
+        b = a + np.array([rc * (1 + rng.integers(-4, 5) * 2.0 ** -24), 0, 0])
+        b[0] -= L
+        pts += [a, b]
+        types += [0, 0]
+    pos = f32(np.array(pts))
+    spec = dict(box=(L, L, L), periodic=(1, 1, 1), diffusion=(1.0,),
+                potentials=[("harmonic_repulsion", 0, 0, dict(k=1.0, d=rc))])
+    ctx, k = gpu_system(rg, spec, pos, np.array(types))
+    k.create_neighbor_list(rc)
+    p, t, ids = k.get_particles()
+    (p, t, ids) = by_id(ids, p, t, ids)
+    o = make_oracle(spec)
+    o.add_particles(p, t)
+    ref = o.brute_force_pairs(rc)
+    got = k.neighbor_pairs(rc)
+    np.testing.assert_array_equal(got, ref)
+
+
+def _compare_forces(rg, spec, pos, types, label):
+    ctx, k = gpu_system(rg, spec, pos, types)
+    k.create_neighbor_list(ctx.calculate_max_cutoff())
+    k.calculate_forces()
+    e_gpu = k.energy
+    f_gpu, ids = k.get_forces()
+    p, t, ids2 = k.get_particles()
+    (f_gpu,) = by_id(ids, f_gpu)
+    (p, t) = by_id(ids2, p, t)
+    o = make_oracle(spec, n_threads=4)
+    o.add_particles(p, t)
+    o.nl_setup(o.calculate_max_cutoff())
+    e_ref = o.calculate_forces()
+    _, _, oid, f_ref, _ = o.particles()
+    (f_ref,) = by_id(oid, f_ref)
+    err = force_error(f_gpu, f_ref)
+    print(f"{label}: n={len(p)} max rel force err {err.max():.3e} (p99.9 {np.quantile(err, .999):.3e}), "
+          f"energy {e_gpu:.9g} vs {e_ref:.9g} rel {abs(e_gpu - e_ref) / max(abs(e_ref), 1e-30):.3e}")
+    return err, e_gpu, e_ref
+
+
+@pytest.mark.parametrize("which", ["lennard_jones", "weak_interaction_piecewise_harmonic", "harmonic_repulsion",
+                                   "all"])
+def test_forces_match_oracle_crowded(rg, which):
+    """The crowded three-species chemistry at 20k particles, per potential type and combined."""
+    spec, pos, types = crowded_spec(n=20000, density=0.2, seed=4)
+    if which != "all":
+        spec["potentials"] = [p for p in spec["potentials"] if p[0] == which]
+    spec["reactions"] = []
+    err, e_gpu, e_ref = _compare_forces(rg, spec, f32(pos), types, which)
+    assert err.max() <= FORCE_RTOL
+    assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
+
+
+def test_forces_match_oracle_screened_electrostatics(rg):
+    rng = np.random.default_rng(8)
+    n, L = 3000, 20.0
+    pos = f32((rng.random((n, 3)) - 0.5) * L)
+    spec = dict(box=(L, L, L), periodic=(1, 1, 1), diffusion=(1.0,),
+                potentials=[("screened_electrostatics", 0, 0,
+                             dict(C=-1.0, kappa=1.0, D=1.0, sigma=1.0, exponent=6, cutoff=3.0))])
+    err, e_gpu, e_ref = _compare_forces(rg, spec, pos, np.zeros(n, int), "screened_electrostatics")
+    assert err.max() <= FORCE_RTOL
+    assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
+
+
+def _reaction_case_system(rg, case, seed):
+    spec = dict(box=case["box"], periodic=case["periodic"], diffusion=case["diffusion"],
+                reactions=[(kind, dict(p)) for kind, p in case["reactions"]])
+    return gpu_system(rg, spec, np.array(case["positions"], float),
+                      np.array(case.get("types", [0] * len(case["positions"]))), seed=seed)
+
+
+@pytest.mark.parametrize("handler", ["uncontrolled_approximation", "gillespie"])
+@pytest.mark.parametrize("case", ka.REACTION_CASES, ids=lambda c: c["name"])
+def test_reaction_known_answers(rg, case, handler):
+    for seed in range(5):
+        ctx, k = _reaction_case_system(rg, case, seed)
+        k.create_neighbor_list(ctx.calculate_max_cutoff())
+        getattr(k, handler)(1.0)
+        pos, types, _ = k.get_particles()
+        assert len(pos) == case["expect_n"]
+        if "expect_positions" in case:
+            np.testing.assert_allclose(pos, np.array(case["expect_positions"]), rtol=case["pos_rtol"])
+        else:
+            got = sorted((int(t), tuple(np.round(p, 5))) for t, p in zip(types, pos))
+            exp = sorted((t, tuple(np.round(np.array(p, float), 5))) for t, p in case["expect_particles"])
+            assert [g[0] for g in got] == [e[0] for e in exp]
+            np.testing.assert_allclose(np.array([g[1] for g in got]), np.array([e[1] for e in exp]),
+                                       atol=case["pos_atol"])
+
+
+@pytest.mark.parametrize("handler", ["uncontrolled_approximation", "gillespie"])
+def test_fission_near_boundary(rg, handler):
+    """readdy/test/TestReactions.cpp:191-213."""
+    for seed in range(10):
+        ctx = rg.Context((10., 10., 10.), (1, 1, 1), 1.0, (0.,))
+        ctx.add_fission(0, 0, 0, 1e16, 2.0)
+        k = rg.CUDAKernel(ctx, seed=seed)
+        k.add_particles([(-4.9999999, 0, 0)], [0])
+        k.create_neighbor_list(1.0)
+        getattr(k, handler)(1.0)
+        pos, _, _ = k.get_particles()
+        assert len(pos) == 2
+        assert (pos[0, 0] <= 0) != (pos[1, 0] <= 0)
+        assert np.all(pos >= -5.0) and np.all(pos < 5.0)
+
+
+def test_brownian_msd_matches_6Dt(rg):
+    """Free diffusion: <|dx|^2> within 1 % of 6 D t with 60k displacement samples."""
+    rng = np.random.default_rng(5)
+    n, steps, dt, D = 60000, 30, 1e-3, 1.0
+    ctx = rg.Context((1000., 1000., 1000.), (1, 1, 1), 1.0, (D,))
+    k = rg.CUDAKernel(ctx, seed=11)
+    p0 = f32((rng.random((n, 3)) - 0.5) * 100.0)
+    ids = k.add_particles(p0, np.zeros(n, np.int32))
+    for _ in range(steps):
+        k.euler_bd_integrator(dt)
+    p1, _, ids1 = k.get_particles()
+    (p1,) = by_id(ids1, p1)
+    msd = np.mean(np.sum((p1 - p0) ** 2, axis=1))
+    assert abs(msd / (6 * D * dt * steps) - 1) < 0.01
+
+
+def test_run_conserves_a_plus_b_c(rg):
+    """A + B <-> C: A + C and B + C are conserved over a run (counts every 10 steps)."""
+    spec, pos, types = abc_spec(n=2000, box=20.0, seed=2)
+    ctx, k = gpu_system(rg, spec, pos, types, seed=3)
+    counts = k.run(200, 1e-3, handler=rg.UNCONTROLLED_APPROXIMATION, count_stride=10)
+    assert counts.shape == (21, 3)
+    assert np.all(counts[:, 0] + counts[:, 2] == 1000)
+    assert np.all(counts[:, 1] + counts[:, 2] == 1000)
+    assert counts[-1, 2] > 0
+    k.synchronize()
+
+
+@pytest.mark.parametrize("handler", [0, 1])
+def test_batch_replica_equals_plain_run(rg, handler):
+    """A replica advanced inside a batch follows the same trajectory as the same system run alone
+    through the per-system path with the replica's seed."""
+    from readdy_gb300.batch import ReplicaBatch, replica_seed
+    rng = np.random.default_rng(9)
+    sizes = [200, 900, 2000, 450]
+    specs = []
+    poss, typess, boxes = [], [], []
+    for n in sizes:
+        L = float(np.float32((n / 0.25) ** (1 / 3)))
+        spec, pos, types = abc_spec(n=n, box=L, seed=int(rng.integers(1 << 30)))
+        specs.append(spec)
+        poss.append(f32(pos))
+        typess.append(types)
+        boxes.append((L, L, L))
+    ctx = make_context(specs[0])
+    b = ReplicaBatch(ctx, boxes, [2 * n for n in sizes], seed=77)
+    b.set_particles(poss, typess)
+    b.configure(handler=handler, dt=1e-3, cell_radius=1, threads_per_block=256)
+    steps = 100
+    b.step(steps)
+    b.synchronize()
+    for r, n in enumerate(sizes):
+        ctx_r = make_context(specs[r])
+        k = rg.CUDAKernel(ctx_r, seed=replica_seed(77, r))
+        k.add_particles(poss[r], typess[r])
+        k.run(steps, 1e-3, handler=handler)
+        pa, ta, ia = k.get_particles()
+        pb, tb, ib = b.get_particles(r)
+        (pa, ta, ia) = by_id(ia, pa, ta, ia)
+        (pb, tb, ib) = by_id(ib, pb, tb, ib)
+        assert len(pa) == len(pb)
+        np.testing.assert_array_equal(ia, ib)
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_allclose(pa, pb, rtol=0, atol=1e-5)
