@@ -570,7 +570,12 @@ void rdc_system::add_topology(int64_t n, const double *pos, const int *types, in
     }
     std::vector<int> slots(n);
     for (int64_t i = 0; i < n; ++i) slots[i] = base + (int)i;
+    // the slot -> storage map must cover the new slots before any sort gathers them
     n_top += (int)n;
+    dfree(d.tloc);
+    d.tloc = dalloc<int>(n_top);
+    d.tloc_size = n_top;
+    d.n_top = 0;  // bonded terms are uploaded below; until then the force kernel skips them
     append(n, pos, types, slots.data(), ids_out);
     upload_topology();
 }
@@ -615,8 +620,6 @@ void rdc_system::upload_topology() {
     up(angle_par_dev, top.angle_par);
     up(dih_idx_dev, top.dihedrals);
     up(dih_par_dev, top.dih_par);
-    dfree(d.tloc);
-    d.tloc = dalloc<int>(n_top);
     d.n_top = n_top;
     d.top_off = top_off_dev;
     d.top_terms = top_terms_dev;

@@ -123,7 +123,8 @@ struct SysDev {
     double *epart;     // per-block partial energies (pair kernel blocks, then bonded blocks)
     double *energy;
     // bonded (topology slots)
-    int n_top;
+    int n_top;             // topology slots whose bonded terms are live
+    int tloc_size;         // slots covered by tloc
     const int *top_off;    // CSR offsets per topology slot
     const int *top_terms;  // (kind << 28) | (role << 24) | term index
     const int4 *bond_idx;  // slots (i, j, -, -)

@@ -140,7 +140,7 @@ __global__ void k_gather(SysDev s, int permute_force) {
         s.id_alt[j] = s.id[k];
         const int ts = s.tslot[k];
         s.tslot_alt[j] = ts;
-        if (ts >= 0) s.tloc[ts] = j;
+        if (ts >= 0 && ts < s.tloc_size) s.tloc[ts] = j;
         if (permute_force) s.force_alt[j] = s.force[k];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
