@@ -160,8 +160,9 @@ int rdc_batch_create(rdc_batch **out, const rdc_context *ctx, int n_replicas, co
 int rdc_batch_destroy(rdc_batch *b);
 /* initial particles of every replica: offsets (n_replicas+1) into positions3/types */
 int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *positions3, const int *types);
-/* handler, time step and the cell-list knobs (cells per cutoff, threads per block) */
-int rdc_batch_configure(rdc_batch *b, int handler, double dt, int cell_radius, int threads_per_block);
+/* handler, time step and the launch knobs: cell width as a multiple (>= 1) of the largest cutoff, and
+ * threads per block (one block advances one replica at a time) */
+int rdc_batch_configure(rdc_batch *b, int handler, double dt, double cell_width_scale, int threads_per_block);
 /* advance every replica n_steps; each step is one fused launch replayed from a CUDA graph */
 int rdc_batch_step(rdc_batch *b, int64_t n_steps);
 /* per-replica, per-type counts (n_replicas * n_types) */

@@ -61,6 +61,7 @@ def _load():
             "orc_n_entries": (i, [vp]),
             "orc_get_particles": (i, [vp, P(d), P(i), P(u64), P(d), P(i)]),
             "orc_calculate_max_cutoff": (d, [vp]),
+            "orc_get_force_scales": (i, [vp, P(d)]),
             "orc_nl_setup": (i, [vp, d]),
             "orc_nl_update": (i, [vp]),
             "orc_nl_pairs": (i64, [vp, d, i64, P(u64)]),
@@ -189,6 +190,12 @@ class OracleSystem:
         self._lib.orc_get_particles(self._h, _ptr(pos, C.c_double), _ptr(t, C.c_int), _ptr(ids, C.c_uint64),
                                     _ptr(f, C.c_double), _ptr(si, C.c_int))
         return pos, t, ids, f, si
+
+    def force_scales(self):
+        """Per active particle: sum of the magnitudes of its force terms (same order as particles())."""
+        out = np.zeros(self.n_particles)
+        self._lib.orc_get_force_scales(self._h, _ptr(out, C.c_double))
+        return out
 
     def calculate_max_cutoff(self):
         return self._lib.orc_calculate_max_cutoff(self._h)

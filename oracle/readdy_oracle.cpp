@@ -188,6 +188,7 @@ struct Reaction {
 
 struct Entry {
     V3 pos, force;
+    double fscale = 0;  // sum of the magnitudes of the force terms acting on the particle
     uint64_t id = 0;
     int type = 0;
     bool deactivated = false;
@@ -437,7 +438,7 @@ struct orc_system {
     double calculateForces() {
         energy = 0;
         if (pot2.empty() && bonds.empty() && angles.empty() && dihedrals.empty()) return 0;
-        for (auto &e : entries) e.force = {0, 0, 0};
+        for (auto &e : entries) { e.force = {0, 0, 0}; e.fscale = 0; }
         int nt = pool.size();
         std::vector<double> part(nt, 0.);
         if (!bonds.empty() || !angles.empty() || !dihedrals.empty()) energy += bondedForces();
@@ -473,6 +474,7 @@ struct orc_system {
                                 myE += pot.energy(xij);
                                 pot.force(upd, xij);
                                 entry.force += upd;
+                                entry.fscale += norm(upd);
                             }
                         }
                     }
@@ -494,6 +496,8 @@ struct orc_system {
             V3 upd = (2. * b.k * (nrm - b.l0) / nrm) * xij;
             e1.force += upd;
             e2.force -= upd;
+            e1.fscale += norm(upd);
+            e2.fscale += norm(upd);
             const double n2 = std::sqrt(dot(xij, xij));
             e += b.k * (n2 - b.l0) * (n2 - b.l0);
         }
@@ -502,7 +506,10 @@ struct orc_system {
             V3 xji = box.shortest(e2.pos, e1.pos);
             V3 xjk = box.shortest(e2.pos, e3.pos);
             e += angleEnergy(xji, xjk, a);
-            angleForce(e1.force, e2.force, e3.force, xji, xjk, a);
+            V3 f1{0, 0, 0}, f2{0, 0, 0}, f3{0, 0, 0};
+            angleForce(f1, f2, f3, xji, xjk, a);
+            e1.force += f1; e2.force += f2; e3.force += f3;
+            e1.fscale += norm(f1); e2.fscale += norm(f2); e3.fscale += norm(f3);
         }
         for (const auto &d : dihedrals) {  // :106-123, TorsionPotential.cpp:53-159
             Entry &ei = entries.at(d.i), &ej = entries.at(d.j), &ek = entries.at(d.k), &el = entries.at(d.l);
@@ -510,7 +517,10 @@ struct orc_system {
             V3 xkj = box.shortest(ek.pos, ej.pos);
             V3 xkl = box.shortest(ek.pos, el.pos);
             e += dihedralEnergy(xji, xkj, xkl, d);
-            dihedralForce(ei.force, ej.force, ek.force, el.force, xji, xkj, xkl, d);
+            V3 f1{0, 0, 0}, f2{0, 0, 0}, f3{0, 0, 0}, f4{0, 0, 0};
+            dihedralForce(f1, f2, f3, f4, xji, xkj, xkl, d);
+            ei.force += f1; ej.force += f2; ek.force += f3; el.force += f4;
+            ei.fscale += norm(f1); ej.fscale += norm(f2); ek.fscale += norm(f3); el.fscale += norm(f4);
         }
         return e;
     }
@@ -994,6 +1004,12 @@ int orc_n_particles(const orc_system *s) {
     return n;
 }
 int orc_n_entries(const orc_system *s) { return (int)s->entries.size(); }
+int orc_get_force_scales(const orc_system *s, double *out) {
+    int k = 0;
+    for (const auto &e : s->entries)
+        if (!e.deactivated) out[k++] = e.fscale;
+    return k;
+}
 int orc_get_particles(const orc_system *s, double *pos, int *types, uint64_t *ids, double *force, int *sidx) {
     int k = 0;
     for (size_t i = 0; i < s->entries.size(); ++i) {

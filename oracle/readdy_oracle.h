@@ -58,6 +58,9 @@ int orc_n_entries(const orc_system *s);         /* storage size incl. blanks */
 int orc_get_particles(const orc_system *s, double *pos3, int *types, uint64_t *ids, double *force3,
                       int *storage_index);
 double orc_calculate_max_cutoff(const orc_system *s);
+/* per active particle (storage order): sum over the force terms of the last CalculateForces of their
+ * magnitudes -- the scale of the rounding error of an FP32 evaluation of the same sum */
+int orc_get_force_scales(const orc_system *s, double *out);
 
 /* neighbour list (CellLinkedList.cpp) */
 int orc_nl_setup(orc_system *s, double cutoff);

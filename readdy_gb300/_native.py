@@ -81,7 +81,7 @@ def _sig(lib):
         "rdc_batch_create": (i, [vpp, vp, i, P(d), P(i64), u64]),
         "rdc_batch_destroy": (i, [vp]),
         "rdc_batch_set_particles": (i, [vp, P(i64), P(d), P(i)]),
-        "rdc_batch_configure": (i, [vp, i, d, i, i]),
+        "rdc_batch_configure": (i, [vp, i, d, d, i]),
         "rdc_batch_step": (i, [vp, i64]),
         "rdc_batch_count_types": (i, [vp, P(i64)]),
         "rdc_batch_n_particles": (i, [vp, P(i64)]),

@@ -62,10 +62,11 @@ class ReplicaBatch:
         N.check(self._lib.rdc_batch_set_particles(self._h, _p(offs, C.c_int64), _p(pos, C.c_double),
                                                   _p(types, C.c_int)))
 
-    def configure(self, handler=N.GILLESPIE, dt=1e-3, cell_radius=1, threads_per_block=256):
-        N.check(self._lib.rdc_batch_configure(self._h, int(handler), float(dt), int(cell_radius),
+    def configure(self, handler=N.GILLESPIE, dt=1e-3, cell_width_scale=1.0, threads_per_block=256):
+        N.check(self._lib.rdc_batch_configure(self._h, int(handler), float(dt), float(cell_width_scale),
                                               int(threads_per_block)))
-        self.handler, self.dt, self.cell_radius, self.threads_per_block = handler, dt, cell_radius, threads_per_block
+        self.handler, self.dt = handler, dt
+        self.cell_width_scale, self.threads_per_block = cell_width_scale, threads_per_block
 
     def step(self, n_steps=1):
         N.check(self._lib.rdc_batch_step(self._h, int(n_steps)))
@@ -92,14 +93,14 @@ class ReplicaBatch:
         return pos[:got.value], t[:got.value], ids[:got.value]
 
 
-def autotune(make_batch, steps=20, radii=(1, 2), threads=(128, 256, 512), handler=N.GILLESPIE, dt=1e-3):
-    """Times short runs of freshly made batches over cell radius x threads per block and returns the
-    fastest setting as a dict.  `make_batch()` must return a batch with its particles set."""
+def autotune(make_batch, steps=20, scales=(1.0, 1.5, 2.0), threads=(256, 512), handler=N.GILLESPIE, dt=1e-3):
+    """Times short runs of freshly made batches over cell width scale x threads per block and returns
+    the fastest setting as a dict.  `make_batch()` must return a batch with its particles set."""
     best = None
-    for r in radii:
+    for r in scales:
         for t in threads:
             b = make_batch()
-            b.configure(handler=handler, dt=dt, cell_radius=r, threads_per_block=t)
+            b.configure(handler=handler, dt=dt, cell_width_scale=r, threads_per_block=t)
             b.step(2)
             b.synchronize()
             t0 = time.perf_counter()
@@ -107,6 +108,6 @@ def autotune(make_batch, steps=20, radii=(1, 2), threads=(128, 256, 512), handle
             b.synchronize()
             dtm = (time.perf_counter() - t0) / steps
             if best is None or dtm < best["s_per_step"]:
-                best = dict(cell_radius=r, threads_per_block=t, s_per_step=dtm)
+                best = dict(cell_width_scale=r, threads_per_block=t, s_per_step=dtm)
             del b
     return best

@@ -78,6 +78,22 @@ uint64_t coin_threshold(double rate, double dt) {
     return (uint64_t)x;
 }
 
+// x as an unevaluated float sum hi + lo
+void split_ff(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+float4 bond_params(double k, double l0) {
+    float hi, lo;
+    split_ff(l0 * l0, hi, lo);
+    return make_float4((float)k, (float)l0, hi, lo);
+}
+
+float4 angle_params(double k, double theta0) {
+    return make_float4((float)k, (float)theta0, (float)(M_PI - theta0), 0.f);
+}
+
 float band_for(double cutoff, const float L[3]) {
     const double Lmax = std::max(L[0], std::max(L[1], L[2]));
     const double c2 = cutoff * cutoff;
@@ -104,7 +120,7 @@ bool ContextData::structural_reactions() const {
     return false;
 }
 
-Geo make_geo(const double box[3], const int pbc[3], double cutoff, int radius) {
+Geo make_geo(const double box[3], const int pbc[3], double cutoff, int radius, double min_width) {
     Geo g{};
     double Lmax = 0;
     for (int d = 0; d < 3; ++d) {
@@ -120,7 +136,7 @@ Geo make_geo(const double box[3], const int pbc[3], double cutoff, int radius) {
         if (cutoff > 0) {
             // cell width >= cutoff/radius with a margin covering FP32 binning error
             const double w = cutoff / radius + std::ldexp(g.Ld[d], -19) / radius + 1e-6 * cutoff;
-            dims = (int)std::max(1.0, std::floor(g.Ld[d] / w));
+            dims = (int)std::max(1.0, std::floor(g.Ld[d] / std::max(w, min_width)));
         }
         g.dims[d] = dims;
         g.invW[d] = (float)((double)dims / g.Ld[d]);
@@ -226,9 +242,9 @@ void set_last_error(const std::string &m) { g_err = m; }
 struct Topology {
     // terms refer to topology slots
     std::vector<int4> bonds;
-    std::vector<float2> bond_par;
+    std::vector<float4> bond_par;
     std::vector<int4> angles;
-    std::vector<float2> angle_par;
+    std::vector<float4> angle_par;
     std::vector<int4> dihedrals;
     std::vector<float4> dih_par;
 };
@@ -249,7 +265,7 @@ struct rdc_system {
     Topology top;
     int *top_off_dev = nullptr, *top_terms_dev = nullptr;
     int4 *bond_idx_dev = nullptr, *angle_idx_dev = nullptr, *dih_idx_dev = nullptr;
-    float2 *bond_par_dev = nullptr, *angle_par_dev = nullptr;
+    float4 *bond_par_dev = nullptr, *angle_par_dev = nullptr;
     float4 *dih_par_dev = nullptr;
     int top_capacity = 0;
     int ncells_alloc = -1;
@@ -530,7 +546,7 @@ void rdc_system::add_topology(int64_t n, const double *pos, const int *types, in
                 for (auto &c : ctx.bonds) {
                     if ((c.t1 == ty(v1) && c.t2 == ty(nb)) || (c.t1 == ty(nb) && c.t2 == ty(v1))) {
                         top.bonds.push_back(make_int4(base + v1, base + nb, 0, 0));
-                        top.bond_par.push_back(make_float2((float)c.k, (float)c.l0));
+                        top.bond_par.push_back(bond_params(c.k, c.l0));
                         found = true;
                     }
                 }
@@ -561,7 +577,7 @@ void rdc_system::add_topology(int64_t n, const double *pos, const int *types, in
                         const bool bwd = c.t1 == tt[2] && c.t2 == tt[1] && c.t3 == tt[0];
                         if (fwd || bwd) {
                             top.angles.push_back(make_int4(base + nb2, base + v1, base + nb, 0));
-                            top.angle_par.push_back(make_float2((float)c.k, (float)c.theta0));
+                            top.angle_par.push_back(angle_params(c.k, c.theta0));
                         }
                     }
                 }
@@ -784,6 +800,7 @@ int rdc_context_add_harmonic_repulsion(rdc_context *ctx, int t1, int t2, double 
         h.pot.kind = POT_HARMONIC_REPULSION;
         h.pot.p[0] = (float)k;
         h.pot.p[1] = (float)d;
+        split_ff(d * d, h.pot.p[2], h.pot.p[3]);
         h.pot.cutoff2 = d * d;
         h.pot.cutoff2f = (float)h.pot.cutoff2;
         ctx->d.pots.push_back(h);
@@ -797,6 +814,10 @@ int rdc_context_add_weak_interaction_piecewise_harmonic(rdc_context *ctx, int t1
         HostPot h{t1, t2, {}, rc};
         h.pot.kind = POT_WEAK_PIECEWISE_HARMONIC;
         h.pot.p[0] = (float)k; h.pot.p[1] = (float)d0; h.pot.p[2] = (float)depth; h.pot.p[3] = (float)rc;
+        split_ff(d0 * d0, h.pot.p[4], h.pot.p[5]);
+        split_ff(rc * rc, h.pot.p[6], h.pot.p[7]);
+        const double mid = d0 + 0.5 * (rc - d0);
+        h.pot.p[8] = (float)(mid * mid);
         h.pot.cutoff2 = rc * rc;
         h.pot.cutoff2f = (float)h.pot.cutoff2;
         ctx->d.pots.push_back(h);
@@ -821,6 +842,8 @@ int rdc_context_add_lennard_jones(rdc_context *ctx, int t1, int t2, unsigned m, 
         h.pot.p[0] = (float)m; h.pot.p[1] = (float)n; h.pot.p[2] = (float)cutoff; h.pot.p[3] = shift ? 1.f : 0.f;
         h.pot.p[4] = (float)epsilon; h.pot.p[5] = (float)(sigma * sigma); h.pot.p[6] = (float)kk;
         h.pot.p[7] = (float)eshift;
+        h.pot.p[8] = (m == 12 && n == 6) ? 1.f : 0.f;
+        split_ff(std::pow(sigma, 6.0), h.pot.p[9], h.pot.p[10]);
         h.pot.cutoff2 = cutoff * cutoff;
         h.pot.cutoff2f = (float)h.pot.cutoff2;
         ctx->d.pots.push_back(h);

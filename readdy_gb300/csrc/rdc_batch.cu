@@ -27,12 +27,16 @@ using namespace rdc;
 
 namespace rdc {
 
+// cell starts of a replica whose grid has at most SMEM_CELLS - 3 cells live in shared memory
+constexpr int SMEM_CELLS = 16384;
+
 struct RepDesc {
     Geo geo;
     int poff, cap;     // particle slots [poff, poff + cap) in every per-particle array
-    int coff;          // cell counts at cnt[coff .. coff + ncells + 2)
-    int soff;          // cell starts at start[soff .. soff + ncells + 3)
+    int soff;          // cell starts at start[soff .. soff + ncells + 3) between steps
     int eoff, ecap;    // event buffer
+    int smem_cells;    // 1: cell array in shared memory during the step
+    int pad;
     uint64_t seed;
 };
 
@@ -49,10 +53,9 @@ struct BatchDev {
     float4 *posA, *posB;
     uint32_t *idA, *idB;
     int *bin, *rank, *src, *claim, *taken;
-    int *cnt, *start;
+    int *start;
     EventRec *events;
     const Tables *tab;
-    int radius;
     uint64_t *step;  // [0] integrator step, [1] reaction step (shared by all replicas)
     int handler, reactions;
     unsigned long long *counts;  // replica-major per-type counts, refreshed every count_stride steps
@@ -61,9 +64,18 @@ struct BatchDev {
     unsigned long long *reaction_counts;
 };
 
-// exclusive scan of n ints in global memory by one block; the input is zeroed on the way (the
-// counts are reused by the next sort) and out[n] receives the total
-__device__ inline void block_scan_zero(int *in, int *out, int n) {
+__device__ inline void block_zero(int *a, int n) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) a[k] = 0;
+    __syncthreads();
+}
+
+__device__ inline void block_copy(int *dst, const int *src, int n) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+    __syncthreads();
+}
+
+// in-place exclusive scan of a[0..n) by one block (shared or global memory); a[n] = total
+__device__ inline void block_scan_inplace(int *a, int n) {
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -75,39 +87,50 @@ __device__ inline void block_scan_zero(int *in, int *out, int n) {
         int sum = 0;
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            v[k] = (b + k < n) ? in[b + k] : 0;
-            if (b + k < n) in[b + k] = 0;
+            v[k] = (b + k < n) ? a[b + k] : 0;
             sum += v[k];
         }
         int total;
         int run = block_exclusive_scan(sum, total) + carry;
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            if (b + k < n) out[b + k] = run;
+            if (b + k < n) a[b + k] = run;
             run += v[k];
         }
         __syncthreads();
         if (threadIdx.x == 0) carry += total;
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[n] = carry;
+    if (threadIdx.x == 0) a[n] = carry;
     __syncthreads();
 }
 
-// counting sort of one replica by bins already in bin/rank/cnt: scatter, order each cell by source
-// index, gather into the destination arrays
+// ranks of the particles inside their bins (bin[] already set); cells receives the counts
+__device__ inline void block_rank(int n, const int *bin, int *rank, int *cells, int nbins) {
+    block_zero(cells, nbins);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) rank[i] = atomicAdd(&cells[bin[i]], 1);
+    __syncthreads();
+}
+
+__device__ inline void block_bin(const float4 *pos, int n, int *bin, const Geo &g) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) bin[i] = bin_of(pos[i], g);
+    __syncthreads();
+}
+
+// counting sort of one replica from counts in cells: scan to cell starts, scatter, order each cell
+// by source index (deterministic), gather into the destination arrays
 __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n, float4 *dpos, uint32_t *did,
-                                  const int *bin, const int *rank, int *src, int *cnt, int *start, const Geo &g,
-                                  int &n_new, int &n_in) {
+                                  const int *bin, const int *rank, int *src, int *cells, const Geo &g, int &n_new,
+                                  int &n_in) {
     const int nc = g.ncells;
-    block_scan_zero(cnt, start, nc + 2);
+    block_scan_inplace(cells, nc + 2);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int b = bin[i];
-        if (b <= nc) src[start[b] + rank[i]] = i;
+        if (b <= nc) src[cells[b] + rank[i]] = i;
     }
     __syncthreads();
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-        const int b = start[c], e = start[c + 1];
+        const int b = cells[c], e = cells[c + 1];
         for (int j = b + 1; j < e; ++j) {
             const int v = src[j];
             int k = j - 1;
@@ -119,21 +142,12 @@ __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n
         }
     }
     __syncthreads();
-    n_new = start[nc + 1];
-    n_in = start[nc];
+    n_new = cells[nc + 1];
+    n_in = cells[nc];
     for (int j = threadIdx.x; j < n_new; j += blockDim.x) {
         const int k = src[j];
         dpos[j] = spos[k];
         did[j] = sid[k];
-    }
-    __syncthreads();
-}
-
-__device__ inline void block_bin(const float4 *pos, int n, int *bin, int *rank, int *cnt, const Geo &g) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int b = bin_of(pos[i], g);
-        bin[i] = b;
-        rank[i] = atomicAdd(&cnt[b], 1);
     }
     __syncthreads();
 }
@@ -156,6 +170,7 @@ struct SmemLayout {
     PairPot *pots;
     uint64_t *key;
     int *idx, *state;
+    int *cells;
 };
 
 __device__ inline SmemLayout carve(unsigned char *smem, int T, int NP, int max_events) {
@@ -170,12 +185,14 @@ __device__ inline SmemLayout carve(unsigned char *smem, int T, int NP, int max_e
     L.idx = reinterpret_cast<int *>(smem + off);
     off += sizeof(int) * max_events;
     L.state = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * max_events;
+    L.cells = reinterpret_cast<int *>(smem + off);
     return L;
 }
 
 size_t batch_smem_bytes(int T, int NP, int max_events) {
     return sizeof(uint64_t) * max_events + sizeof(PairPot) * (NP > 0 ? NP : 1) + sizeof(int) * T * T +
-           2 * sizeof(int) * max_events + 16;
+           2 * sizeof(int) * max_events + sizeof(int) * (SMEM_CELLS + 4) + 16;
 }
 
 // one step of one replica by the whole block
@@ -193,30 +210,32 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
     const Tables *tab = B.tab;
     const int T = tab->ntypes, NP = tab->npots;
     const Geo &g = D.geo;
+    const int nc = g.ncells;
     float4 *posX = (st.cur ? B.posB : B.posA) + D.poff;
     uint32_t *idX = (st.cur ? B.idB : B.idA) + D.poff;
     float4 *posY = (st.cur ? B.posA : B.posB) + D.poff;
     uint32_t *idY = (st.cur ? B.idA : B.idB) + D.poff;
     int *bin = B.bin + D.poff, *rank = B.rank + D.poff, *src = B.src + D.poff;
-    int *cnt = B.cnt + D.coff, *start = B.start + D.soff;
+    int *gstart = B.start + D.soff;
+    int *cells = D.smem_cells ? S.cells : gstart;
+    if (D.smem_cells) block_copy(cells, gstart, nc + 3);
     const int n = st.n, n_in = st.n_in;
 
     // forces on the current state, Euler step into Y, bins of the new positions
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 p = posX[i];
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-        if (i < n_in && NP > 0) pair_force_at(i, p, posX, start, g, B.radius, S.tab, S.pots, T, fx, fy, fz, e);
+        if (i < n_in && NP > 0) pair_force_at(i, p, posX, cells, g, 1, S.tab, S.pots, T, fx, fy, fz, e);
         const uint32_t id = idX[i];
         const float4 q = euler_bd(p, fx, fy, fz, id, D.seed, bd_step, tab, g);
         posY[i] = q;
         idY[i] = id;
-        const int b = bin_of(q, g);
-        bin[i] = b;
-        rank[i] = atomicAdd(&cnt[b], 1);
+        bin[i] = bin_of(q, g);
     }
     __syncthreads();
+    block_rank(n, bin, rank, cells, nc + 2);
     int n1, nin1;
-    block_sort(posY, idY, n, posX, idX, bin, rank, src, cnt, start, g, n1, nin1);
+    block_sort(posY, idY, n, posX, idX, bin, rank, src, cells, g, n1, nin1);
 
     int n_final = n1, nin_final = nin1, cur = st.cur, next_id = st.next_id;
     if (B.reactions) {
@@ -233,7 +252,7 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
             }
         };
         for (int i = threadIdx.x; i < n1; i += blockDim.x)
-            events_at(i, i < nin1, posX, idX, start, g, B.radius, tab, D.seed, rx_step, B.handler, emit);
+            events_at(i, i < nin1, posX, idX, cells, g, 1, tab, D.seed, rx_step, B.handler, emit);
         __syncthreads();
         const int E = min(sh_nev, ecap);
         if (E > 0) {
@@ -251,15 +270,17 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
             if (res.winners > 0) {
                 // particles changed cells, appeared or vanished: sort again, into Y
                 const int n_total = n1 + res.births;
-                block_bin(posX, n_total, bin, rank, cnt, g);
+                block_bin(posX, n_total, bin, g);
+                block_rank(n_total, bin, rank, cells, nc + 2);
                 int n2, nin2;
-                block_sort(posX, idX, n_total, posY, idY, bin, rank, src, cnt, start, g, n2, nin2);
+                block_sort(posX, idX, n_total, posY, idY, bin, rank, src, cells, g, n2, nin2);
                 n_final = n2;
                 nin_final = nin2;
                 cur ^= 1;
             }
         }
     }
+    if (D.smem_cells) block_copy(gstart, cells, nc + 3);
     if (B.count_stride > 0 && (bd_step + 1) % (uint64_t)B.count_stride == 0) {
         const float4 *pf = (cur ? B.posB : B.posA) + D.poff;
         block_count_types(pf, n_final, T, B.counts + (size_t)r * T);
@@ -303,7 +324,8 @@ __global__ void k_batch_advance(BatchDev B) {
     *B.work = 0;
 }
 
-// initial binning and sort of every replica (state.cur selects the source)
+// initial binning and sort of every replica (state.cur selects the source); the cell starts are
+// sorted in the global start array
 __global__ void k_batch_sort(BatchDev B) {
     __shared__ int sh_r;
     for (;;) {
@@ -319,10 +341,11 @@ __global__ void k_batch_sort(BatchDev B) {
         float4 *posY = (st.cur ? B.posA : B.posB) + D.poff;
         uint32_t *idY = (st.cur ? B.idA : B.idB) + D.poff;
         int *bin = B.bin + D.poff, *rank = B.rank + D.poff, *src = B.src + D.poff;
-        int *cnt = B.cnt + D.coff, *start = B.start + D.soff;
-        block_bin(posX, st.n, bin, rank, cnt, D.geo);
+        int *cells = B.start + D.soff;
+        block_bin(posX, st.n, bin, D.geo);
+        block_rank(st.n, bin, rank, cells, D.geo.ncells + 2);
         int n2, nin2;
-        block_sort(posX, idX, st.n, posY, idY, bin, rank, src, cnt, start, D.geo, n2, nin2);
+        block_sort(posX, idX, st.n, posY, idY, bin, rank, src, cells, D.geo, n2, nin2);
         if (threadIdx.x == 0) {
             st.n = n2;
             st.n_in = nin2;
@@ -402,7 +425,7 @@ struct rdc_batch {
     Tables *tab_dev = nullptr;
     double dt = 0;
     int handler = H_GILLESPIE;
-    int radius = 1;
+    double cell_scale = 1.0;  // cell width = cutoff * cell_scale (at least)
     int threads = 256;
     int blocks = 0;
     size_t smem = 0;
@@ -417,7 +440,7 @@ struct rdc_batch {
         bfree(desc_dev); bfree(state_dev); bfree(order_dev); bfree(tab_dev); bfree(count_dev);
         bfree(d.posA); bfree(d.posB); bfree(d.idA); bfree(d.idB);
         bfree(d.bin); bfree(d.rank); bfree(d.src); bfree(d.claim); bfree(d.taken);
-        bfree(d.cnt); bfree(d.start); bfree(d.events); bfree(d.work); bfree(d.step); bfree(d.counts);
+        bfree(d.start); bfree(d.events); bfree(d.work); bfree(d.step); bfree(d.counts);
         bfree(d.reaction_counts);
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
@@ -430,38 +453,42 @@ struct rdc_batch {
         graph = nullptr;
     }
 
-    // cell grids and offsets for the current cell radius
+    // cell grids and offsets: cells at least cutoff * cell_scale wide, widened for a replica whose
+    // grid would not fit the shared-memory cell array
     void layout() {
         const double cutoff = ctx.max_cutoff();
-        int64_t poff = 0, coff = 0, soff = 0, eoff = 0;
+        int64_t poff = 0, soff = 0, eoff = 0;
         desc.resize(R);
         for (int r = 0; r < R; ++r) {
             RepDesc &D = desc[r];
-            D.geo = make_geo(&boxes[3 * r], ctx.pbc, cutoff, radius);
+            double w = cutoff * cell_scale;
+            D.geo = make_geo(&boxes[3 * r], ctx.pbc, cutoff, 1, w);
+            for (int k = 0; k < 64 && D.geo.ncells + 3 > SMEM_CELLS && cutoff > 0; ++k) {
+                w *= 1.05;
+                D.geo = make_geo(&boxes[3 * r], ctx.pbc, cutoff, 1, w);
+            }
+            D.smem_cells = D.geo.ncells + 3 <= SMEM_CELLS ? 1 : 0;
+            D.pad = 0;
             D.poff = (int)poff;
             D.cap = (int)caps[r];
-            D.coff = (int)coff;
             D.soff = (int)soff;
             D.ecap = 64 + D.cap / 32;
             D.eoff = (int)eoff;
             D.seed = replica_seed(seed, r);
             poff += D.cap;
-            coff += D.geo.ncells + 2;
             soff += D.geo.ncells + 3;
             eoff += D.ecap;
-            if (poff > INT_MAX / 2 || coff > INT_MAX / 2 || eoff > INT_MAX / 2)
+            if (poff > INT_MAX / 2 || soff > INT_MAX / 2 || eoff > INT_MAX / 2)
                 throw std::invalid_argument("batch too large for 32-bit offsets");
         }
-        bfree(d.cnt); bfree(d.start); bfree(d.events);
-        d.cnt = balloc<int>(coff);
+        bfree(d.start); bfree(d.events);
         d.start = balloc<int>(soff);
         d.events = balloc<EventRec>(eoff);
-        RDC_CUDA(cudaMemsetAsync(d.cnt, 0, sizeof(int) * coff, stream));
+        RDC_CUDA(cudaMemsetAsync(d.start, 0, sizeof(int) * soff, stream));
         bfree(desc_dev);
         desc_dev = balloc<RepDesc>(R);
         RDC_CUDA(cudaMemcpyAsync(desc_dev, desc.data(), sizeof(RepDesc) * R, cudaMemcpyHostToDevice, stream));
         d.desc = desc_dev;
-        d.radius = radius;
         invalidate_graph();
     }
 
@@ -673,13 +700,14 @@ int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *
     });
 }
 
-int rdc_batch_configure(rdc_batch *b, int handler, double dt, int cell_radius, int threads_per_block) {
+int rdc_batch_configure(rdc_batch *b, int handler, double dt, double cell_width_scale, int threads_per_block) {
     BATCH_CALL({
         if (!b) throw std::invalid_argument("null argument");
         if (handler != H_UNCONTROLLED_APPROXIMATION && handler != H_GILLESPIE)
             throw std::invalid_argument("unknown reaction handler");
         if (!(dt > 0)) throw std::invalid_argument("time step must be > 0");
-        if (cell_radius < 1 || cell_radius > 3) throw std::invalid_argument("cell radius must be 1, 2 or 3");
+        if (!(cell_width_scale >= 1.0 && cell_width_scale <= 8.0))
+            throw std::invalid_argument("cell width scale must be in [1, 8]");
         if (threads_per_block < 64 || threads_per_block > 1024 || threads_per_block % 32)
             throw std::invalid_argument("threads per block must be a multiple of 32 in [64, 1024]");
         b->handler = handler;
@@ -688,8 +716,8 @@ int rdc_batch_configure(rdc_batch *b, int handler, double dt, int cell_radius, i
         set_time_step(b->ctx, dt, b->tab);
         RDC_CUDA(cudaMemcpyAsync(b->tab_dev, &b->tab, sizeof(Tables), cudaMemcpyHostToDevice, b->stream));
         b->threads = threads_per_block;
-        if (cell_radius != b->radius) {
-            b->radius = cell_radius;
+        if (cell_width_scale != b->cell_scale) {
+            b->cell_scale = cell_width_scale;
             b->layout();
             b->sort_all();
         }

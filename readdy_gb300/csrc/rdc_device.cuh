@@ -83,11 +83,14 @@ __device__ inline float wrap1(float x, float L, float hL, int pbc) {
     return x;
 }
 
-// bcs::shortestDifference(lhs, rhs) component, FP32
-__device__ inline float mi1(float dv, float L, float hL, int pbc) {
+// bcs::shortestDifference(lhs, rhs) component rhs - lhs, FP32.  A wrapped difference is formed
+// as (rhs -+ L) - lhs rather than (rhs - lhs) -+ L: shifting first is exact for coordinates inside
+// the box, so the result carries one rounding instead of an error of order ulp(L).
+__device__ inline float mi_diff(float rhs, float lhs, float L, float hL, int pbc) {
+    float dv = rhs - lhs;
     if (pbc) {
-        if (dv > hL) dv -= L;
-        else if (dv <= -hL) dv += L;
+        if (dv > hL) dv = (rhs - L) - lhs;
+        else if (dv <= -hL) dv = (rhs + L) - lhs;
     }
     return dv;
 }
@@ -112,6 +115,77 @@ __device__ inline double dist2_exact(float4 lhs, float4 rhs, const Geo &g, doubl
     return s;
 }
 
+// ------------------------------------------------------------------------------------------------
+// compensated FP32 (error-free transformations) for the terms that cancel near a cutoff, a rest
+// length or a potential minimum: the difference of two positions is carried exactly as hi + lo and
+// the squared distance as a float-float pair, so r - d, d0 - r, 2 sigma^6 - r^6 ... keep ~24 bits.
+// Intrinsics keep the compiler from contracting the products whose rounding errors are captured.
+// ------------------------------------------------------------------------------------------------
+// rounding error of s = fl(a + b) (Knuth's TwoSum)
+__device__ inline float two_sum_err(float a, float b, float s) {
+    const float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// minimum-image rhs - lhs as an unevaluated sum hi + lo; hi equals mi_diff()
+__device__ inline void mi_diff2(float rhs, float lhs, float L, float hL, int pbc, float &hi, float &lo) {
+    float a = rhs, ea = 0.f;
+    const float dv = __fsub_rn(rhs, lhs);
+    if (pbc) {
+        if (dv > hL) {
+            a = __fsub_rn(rhs, L);
+            ea = two_sum_err(rhs, -L, a);
+        } else if (dv <= -hL) {
+            a = __fadd_rn(rhs, L);
+            ea = two_sum_err(rhs, L, a);
+        }
+    }
+    hi = __fsub_rn(a, lhs);
+    lo = __fadd_rn(two_sum_err(a, -lhs, hi), ea);
+}
+
+struct FF { float hi, lo; };
+
+// exact differences and their squared norm as float-float
+struct PairExact {
+    float dx, dy, dz;  // hi parts (the FP32 minimum-image difference)
+    FF d2;
+};
+
+__device__ inline float sq_err(float h, float l, float p) {  // (h + l)^2 - p, to first order in l
+    return __fadd_rn(__fmaf_rn(h, h, -p), 2.0f * h * l);
+}
+
+__device__ inline PairExact pair_exact(float4 lhs, float4 rhs, const float L[3], const float hL[3], const int pbc[3]) {
+    PairExact r;
+    float lx, ly, lz;
+    mi_diff2(rhs.x, lhs.x, L[0], hL[0], pbc[0], r.dx, lx);
+    mi_diff2(rhs.y, lhs.y, L[1], hL[1], pbc[1], r.dy, ly);
+    mi_diff2(rhs.z, lhs.z, L[2], hL[2], pbc[2], r.dz, lz);
+    const float px = __fmul_rn(r.dx, r.dx), py = __fmul_rn(r.dy, r.dy), pz = __fmul_rn(r.dz, r.dz);
+    const float s1 = __fadd_rn(px, py);
+    const float t1 = two_sum_err(px, py, s1);
+    const float h = __fadd_rn(s1, pz);
+    const float t2 = two_sum_err(s1, pz, h);
+    const float e = sq_err(r.dx, lx, px) + sq_err(r.dy, ly, py) + sq_err(r.dz, lz, pz);
+    r.d2.hi = h;
+    r.d2.lo = __fadd_rn(__fadd_rn(t1, t2), e);
+    return r;
+}
+
+// (d2 - c) for a float-float d2 and a constant c = chi + clo; accurate when d2 is close to c
+__device__ inline float ff_sub(FF d2, float chi, float clo) {
+    return __fadd_rn(__fsub_rn(d2.hi, chi), __fsub_rn(d2.lo, clo));
+}
+
+// a*b - c*d with one rounding error (Kahan's difference of products)
+__device__ inline float diff_prod(float a, float b, float c, float d) {
+    const float w = __fmul_rn(c, d);
+    const float e = __fmaf_rn(c, d, -w);
+    const float f = __fmaf_rn(a, b, -w);
+    return __fsub_rn(f, e);
+}
+
 // Minimum-image difference rhs - lhs in FP32 and its squared norm.
 struct PairGeom {
     float dx, dy, dz, d2;
@@ -119,9 +193,9 @@ struct PairGeom {
 
 __device__ inline PairGeom pair_geom(float4 lhs, float4 rhs, const Geo &g) {
     PairGeom r;
-    r.dx = mi1(rhs.x - lhs.x, g.L[0], g.hL[0], g.pbc[0]);
-    r.dy = mi1(rhs.y - lhs.y, g.L[1], g.hL[1], g.pbc[1]);
-    r.dz = mi1(rhs.z - lhs.z, g.L[2], g.hL[2], g.pbc[2]);
+    r.dx = mi_diff(rhs.x, lhs.x, g.L[0], g.hL[0], g.pbc[0]);
+    r.dy = mi_diff(rhs.y, lhs.y, g.L[1], g.hL[1], g.pbc[1]);
+    r.dz = mi_diff(rhs.z, lhs.z, g.L[2], g.hL[2], g.pbc[2]);
     r.d2 = fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, r.dz * r.dz));
     return r;
 }
@@ -201,70 +275,100 @@ __device__ inline float ipow(float x, int n) {
     return r;
 }
 
-__device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float &fx, float &fy, float &fz, float &e) {
-    const float d2 = g.d2;
+// Parameter layout of PairPot::p (set by the context registry):
+//   harmonic repulsion: k, d, d^2 hi, d^2 lo
+//   weak piecewise harmonic: k, d0, depth, rc, d0^2 hi, d0^2 lo, rc^2 hi, rc^2 lo, mid^2 (mid = (d0 + rc) / 2)
+//   Lennard-Jones: m, n, rc, shift, epsilon, sigma^2, k, E(rc) shift, is-12-6, sigma^6 hi, sigma^6 lo
+//   screened electrostatics: C, kappa, D, sigma, exponent
+__device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float4 lhs, float4 rhs, const Geo &geo,
+                                  float &fx, float &fy, float &fz, float &e) {
     switch (pp.kind) {
-        case POT_HARMONIC_REPULSION: {  // PotentialsOrder2.h:73-91
+        case POT_HARMONIC_REPULSION: {  // PotentialsOrder2.h:73-91; r - d = (d2 - d^2) / (r + d)
             const float k = pp.p[0], d = pp.p[1];
+            const PairExact x = pair_exact(lhs, rhs, geo.L, geo.hL, geo.pbc);
+            const float d2 = __fadd_rn(x.d2.hi, x.d2.lo);
+            const float r = sqrtf(d2);
+            const float rd = ff_sub(x.d2, pp.p[2], pp.p[3]) / (r + d);
             if (d2 > 0.0f) {
-                const float r = sqrtf(d2);
-                const float s = k * (r - d) / r;
-                fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
-                e += 0.25f * k * (r - d) * (r - d);  // half of 0.5 k (r-d)^2
-            } else {
-                e += 0.25f * k * d * d;
+                const float s = k * rd / r;
+                fx += s * x.dx; fy += s * x.dy; fz += s * x.dz;
             }
+            e += 0.25f * k * rd * rd;  // half of 0.5 k (r - d)^2
             break;
         }
         case POT_WEAK_PIECEWISE_HARMONIC: {  // PotentialsOrder2.h:131-183
             const float k = pp.p[0], d0 = pp.p[1], depth = pp.p[2], rc = pp.p[3];
+            const PairExact x = pair_exact(lhs, rhs, geo.L, geo.hL, geo.pbc);
+            const float d2 = __fadd_rn(x.d2.hi, x.d2.lo);
             const float dist = sqrtf(d2);
             const float half = 0.5f * (rc - d0);
             const float c = depth / (half * half);
+            const float diff0 = ff_sub(x.d2, pp.p[4], pp.p[5]);  // d2 - d0^2
             float en, factor;
-            if (dist < d0) {
-                en = 0.5f * k * (dist - d0) * (dist - d0) - depth;
-                factor = -k * (d0 - dist);
-            } else if (dist < d0 + half) {
-                en = 0.5f * c * (dist - d0) * (dist - d0) - depth;
-                factor = -c * (d0 - dist);
-            } else if (dist < rc) {
-                en = -0.5f * c * (dist - rc) * (dist - rc);
-                factor = c * (rc - dist);
-            } else {
-                en = 0.0f;
-                factor = 0.0f;
+            if (diff0 < 0.0f) {  // dist < d0
+                const float t = -diff0 / (d0 + dist);  // d0 - dist
+                en = 0.5f * k * t * t - depth;
+                factor = -k * t;
+            } else if (d2 < pp.p[8]) {  // dist < d0 + half
+                const float t = -diff0 / (d0 + dist);  // d0 - dist (<= 0)
+                en = 0.5f * c * t * t - depth;
+                factor = -c * t;
+            } else {  // dist < rc (pre-filtered)
+                const float u = -ff_sub(x.d2, pp.p[6], pp.p[7]) / (rc + dist);  // rc - dist
+                en = -0.5f * c * u * u;
+                factor = c * u;
             }
             e += 0.5f * en;
             if (dist > 0.0f && factor != 0.0f) {
                 const float s = factor / dist;
-                fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
+                fx += s * x.dx; fy += s * x.dy; fz += s * x.dz;
             }
             break;
         }
-        case POT_LENNARD_JONES: {  // PotentialsOrder2.h:240-264, integer powers by multiplication
-            const int m = (int)pp.p[0], n = (int)pp.p[1];
-            const float sigma2 = pp.p[5], kk = pp.p[6], eshift = pp.p[7];
-            const float s2 = sigma2 / d2;  // (sigma/r)^2
-            float sm, sn;
-            if ((m & 1) == 0 && (n & 1) == 0) {
-                sm = ipow(s2, m >> 1);
-                sn = ipow(s2, n >> 1);
+        case POT_LENNARD_JONES: {  // PotentialsOrder2.h:240-264
+            const float kk = pp.p[6], eshift = pp.p[7];
+            if (pp.p[8] != 0.0f) {
+                // 12-6: F = -6k s^6 (2 s^6 - 1) / r^2 x and E = k s^6 (s^6 - 1), s^6 = sigma^6 / r^6, with
+                // 2 sigma^6 - r^6 and sigma^6 - r^6 from a float-float r^6 (they cancel at the minimum and at sigma)
+                const PairExact x = pair_exact(lhs, rhs, geo.L, geo.hL, geo.pbc);
+                const float h = x.d2.hi, l = x.d2.lo;
+                const float q = __fmul_rn(h, h);
+                const float eq = __fmaf_rn(h, h, -q);
+                const float c = __fmul_rn(q, h);
+                const float ec = __fmaf_rn(q, h, -c);
+                const float cerr = ec + eq * h + 3.0f * q * l;  // r^6 = c + cerr
+                const float s6h = pp.p[9], s6l = pp.p[10];
+                const float numF = __fadd_rn(__fsub_rn(2.0f * s6h, c), __fsub_rn(2.0f * s6l, cerr));
+                const float numE = __fadd_rn(__fsub_rn(s6h, c), __fsub_rn(s6l, cerr));
+                const float t = s6h / c;
+                const float s = -6.0f * kk * t * (numF / c) / h;
+                fx += s * x.dx; fy += s * x.dy; fz += s * x.dz;
+                e += 0.5f * (kk * t * (numE / c) - eshift);
             } else {
-                const float s1 = sqrtf(s2);
-                sm = ipow(s1, m);
-                sn = ipow(s1, n);
+                // general exponents: integer powers by multiplication
+                const int m = (int)pp.p[0], n = (int)pp.p[1];
+                const float sigma2 = pp.p[5];
+                const float s2 = sigma2 / g.d2;  // (sigma/r)^2
+                float sm, sn;
+                if ((m & 1) == 0 && (n & 1) == 0) {
+                    sm = ipow(s2, m >> 1);
+                    sn = ipow(s2, n >> 1);
+                } else {
+                    const float s1 = sqrtf(s2);
+                    sm = ipow(s1, m);
+                    sn = ipow(s1, n);
+                }
+                // F = -k/sigma^2 (m (s/r)^(m+2) - n (s/r)^(n+2)) x
+                const float s = -kk / sigma2 * (m * sm - n * sn) * s2;
+                fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
+                e += 0.5f * (kk * (sm - sn) - eshift);
             }
-            // F = -k/sigma^2 (m (s/r)^(m+2) - n (s/r)^(n+2)) x
-            const float s = -kk / sigma2 * (m * sm - n * sn) * s2;
-            fx += s * g.dx; fy += s * g.dy; fz += s * g.dz;
-            e += 0.5f * (kk * (sm - sn) - eshift);
             break;
         }
         case POT_SCREENED_ELECTROSTATICS: {  // PotentialsOrder2.h:291-305
             const float C = pp.p[0], kappa = pp.p[1], D = pp.p[2], sigma = pp.p[3];
             const int ex = (int)pp.p[4];
-            const float r = sqrtf(d2);
+            const float r = sqrtf(g.d2);
             const float ir = 1.0f / r;
             const float ekr = C * expf(-kappa * r);
             const float sr = sigma * ir;
@@ -294,39 +398,48 @@ __device__ inline float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b
 __device__ inline F3 cross(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 
 __device__ inline F3 shortest3(float4 lhs, float4 rhs, const Geo &g) {
-    return F3{mi1(rhs.x - lhs.x, g.L[0], g.hL[0], g.pbc[0]), mi1(rhs.y - lhs.y, g.L[1], g.hL[1], g.pbc[1]),
-              mi1(rhs.z - lhs.z, g.L[2], g.hL[2], g.pbc[2])};
+    return F3{mi_diff(rhs.x, lhs.x, g.L[0], g.hL[0], g.pbc[0]), mi_diff(rhs.y, lhs.y, g.L[1], g.hL[1], g.pbc[1]),
+              mi_diff(rhs.z, lhs.z, g.L[2], g.hL[2], g.pbc[2])};
 }
 
 // harmonic bond: E = k (r - l0)^2, force on i = 2k (r-l0)/r x_ij, on j its negative
-__device__ inline F3 bond_force(float4 pi, float4 pj, float k, float l0, const Geo &g, int role, float &e) {
-    const F3 x = shortest3(pi, pj, g);
-    const float r = sqrtf(dot(x, x));
-    const float s = 2.0f * k * (r - l0) / r;
-    e = k * (r - l0) * (r - l0);
-    return role == 0 ? s * x : (-s) * x;
+// (BondedPotential.h:105-113, CPUTopologyActions.cpp:61-74); r - l0 = (d2 - l0^2) / (r + l0)
+// from the float-float d2.  P = (k, l0, l0^2 hi, l0^2 lo)
+__device__ inline F3 bond_force(float4 pi, float4 pj, float4 P, const Geo &g, int role, float &e) {
+    const PairExact x = pair_exact(pi, pj, g.L, g.hL, g.pbc);
+    const float r = sqrtf(__fadd_rn(x.d2.hi, x.d2.lo));
+    const float rd = ff_sub(x.d2, P.z, P.w) / (r + P.y);
+    e = P.x * rd * rd;
+    const float s = 2.0f * P.x * rd / r;
+    const F3 v = f3(x.dx, x.dy, x.dz);
+    return role == 0 ? s * v : (-s) * v;
 }
 
-// harmonic angle with the reference's clamps (AnglePotential.cpp:67-102)
-__device__ inline F3 angle_force(float4 pi, float4 pj, float4 pk, float kf, float theta0, const Geo &g, int role,
-                                 float &e) {
+// harmonic angle, E = k (theta - theta0)^2 (AnglePotential.cpp:58-104) with the reference's clamps
+// (|x|^2, |x_ji||x_jk|, sin theta >= 1e-10).  theta comes from atan2(|x_ji x x_jk|, x_ji . x_jk)
+// (cross product by Kahan's difference of products); for obtuse angles theta - theta0 is formed as
+// (pi - theta0) - atan2(|cross|, -dot), which stays exact at the straight-chain minimum theta0 = pi.
+// P = (k, theta0, pi - theta0, -)
+__device__ inline F3 angle_force(float4 pi, float4 pj, float4 pk, float4 P, const Geo &g, int role, float &e) {
     const float SMALL = 1e-10f;
-    const F3 xji = shortest3(pj, pi, g);
-    const F3 xjk = shortest3(pj, pk, g);
-    const float sp = dot(xji, xjk);
-    float nji2 = fmaxf(dot(xji, xji), SMALL);
-    float njk2 = fmaxf(dot(xjk, xjk), SMALL);
-    const float nji = sqrtf(nji2), njk = sqrtf(njk2);
-    const float np = fmaxf(nji * njk, SMALL);
+    const float kf = P.x;
+    const F3 a = shortest3(pj, pi, g);  // x_ji
+    const F3 b = shortest3(pj, pk, g);  // x_jk
+    const F3 cr = f3(diff_prod(a.y, b.z, a.z, b.y), diff_prod(a.z, b.x, a.x, b.z), diff_prod(a.x, b.y, a.y, b.x));
+    const float cn = sqrtf(dot(cr, cr));
+    const float sp = dot(a, b);
+    const float na2 = fmaxf(dot(a, a), SMALL), nb2 = fmaxf(dot(b, b), SMALL);
+    const float np = fmaxf(sqrtf(na2) * sqrtf(nb2), SMALL);
     const float inp = 1.0f / np;
-    float c = fminf(1.0f, fmaxf(-1.0f, inp * sp));
-    const float theta = acosf(c);
-    e = kf * (theta - theta0) * (theta - theta0);
-    float sinv = fmaxf(sqrtf(fmaxf(0.0f, 1.0f - c * c)), SMALL);
-    sinv = 1.0f / sinv;
-    const float cc = 2.0f * kf * (theta - theta0) * sinv;
-    const F3 fi = (cc * c / nji2) * xji - (cc * inp) * xjk;
-    const F3 fk = (-cc * inp) * xji + (cc * c / njk2) * xjk;
+    const float c = fminf(1.0f, fmaxf(-1.0f, sp * inp));
+    float dth;
+    if (sp < 0.0f) dth = P.z - atan2f(cn, -sp);
+    else dth = atan2f(cn, sp) - P.y;
+    e = kf * dth * dth;
+    const float sinv = 1.0f / fmaxf(cn * inp, SMALL);
+    const float cc = 2.0f * kf * dth * sinv;
+    const F3 fi = (cc * c / na2) * a - (cc * inp) * b;
+    const F3 fk = (-cc * inp) * a + (cc * c / nb2) * b;
     if (role == 0) return (-1.0f) * fi;
     if (role == 1) return fi + fk;
     return (-1.0f) * fk;

@@ -77,8 +77,8 @@ struct Tables {
 // builds the tables from a context for a box (band widths depend on the GPU machine) and time step
 void build_tables(const ContextData &c, const double box[3], double dt, Tables &t);
 void set_time_step(const ContextData &c, double dt, Tables &t);
-// FP32-rounded box, cell grid for cutoff/radius
-Geo make_geo(const double box[3], const int pbc[3], double cutoff, int radius);
+// FP32-rounded box, cell grid for cutoff/radius with cells at least min_width wide
+Geo make_geo(const double box[3], const int pbc[3], double cutoff, int radius, double min_width = 0.0);
 
 // ---- per-system device state -------------------------------------------------------------------
 enum Counter : int {
@@ -128,9 +128,9 @@ struct SysDev {
     const int *top_off;    // CSR offsets per topology slot
     const int *top_terms;  // (kind << 28) | (role << 24) | term index
     const int4 *bond_idx;  // slots (i, j, -, -)
-    const float2 *bond_par;
+    const float4 *bond_par;  // (k, l0, l0^2 hi, l0^2 lo)
     const int4 *angle_idx;
-    const float2 *angle_par;
+    const float4 *angle_par; // (k, theta0, pi - theta0, -)
     const int4 *dih_idx;
     const float4 *dih_par;
     // observables

@@ -191,13 +191,13 @@ __global__ void k_bonded(SysDev s) {
             F3 f;
             if (kind == 0) {
                 const int4 I = s.bond_idx[idx];
-                const float2 P = s.bond_par[idx];
+                const float4 P = s.bond_par[idx];
                 if (P.x == 0.0f) continue;  // terms with k = 0 are skipped (CPUTopologyActions.cpp:62)
-                f = bond_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], P.x, P.y, g, role, e);
+                f = bond_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], P, g, role, e);
             } else if (kind == 1) {
                 const int4 I = s.angle_idx[idx];
-                const float2 P = s.angle_par[idx];
-                f = angle_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], P.x, P.y, g, role, e);
+                const float4 P = s.angle_par[idx];
+                f = angle_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], P, g, role, e);
             } else {
                 const int4 I = s.dih_idx[idx];
                 const float4 P = s.dih_par[idx];

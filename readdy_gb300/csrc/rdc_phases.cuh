@@ -103,7 +103,7 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
             for (int k = first; k < first + cnt; ++k) {
                 const PairPot &pp = pots[k];
                 PairGeom gg = g0;
-                if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, fx, fy, fz, e);
+                if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, p, q, g, fx, fy, fz, e);
             }
         }
     });
@@ -367,9 +367,9 @@ __device__ inline void block_resolve_apply(const EventRec *events, int E, int ma
                 if (!room) break;
                 const float4 p2 = t.pos[ev.p2];
                 const float w = (R.educt[0] == itype(p1)) ? R.w1 : R.w2;
-                const float dx = mi1(p2.x - p1.x, g.L[0], g.hL[0], g.pbc[0]);
-                const float dy = mi1(p2.y - p1.y, g.L[1], g.hL[1], g.pbc[1]);
-                const float dz = mi1(p2.z - p1.z, g.L[2], g.hL[2], g.pbc[2]);
+                const float dx = mi_diff(p2.x, p1.x, g.L[0], g.hL[0], g.pbc[0]);
+                const float dy = mi_diff(p2.y, p1.y, g.L[1], g.hL[1], g.pbc[1]);
+                const float dz = mi_diff(p2.z, p1.z, g.L[2], g.hL[2], g.pbc[2]);
                 float4 q;
                 q.x = wrap1(p1.x + w * dx, g.L[0], g.hL[0], g.pbc[0]);
                 q.y = wrap1(p1.y + w * dy, g.L[1], g.hL[1], g.pbc[1]);

@@ -41,7 +41,7 @@ struct Geo {
 struct PairPot {
     int kind;
     int pad;
-    float p[8];
+    float p[12];
     double cutoff2;   // FP64 squared cutoff, computed as the reference does
     float cutoff2f;
     float band;       // half-width of the FP32 rounding band around cutoff2f

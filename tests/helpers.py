@@ -97,3 +97,23 @@ def abc_spec(n=2000, box=20.0, seed=0):
                 reactions=[("fusion", dict(a=0, b=1, c=2, rate=1.0, educt_distance=1.0)),
                            ("fission", dict(a=2, b=0, c=1, rate=0.1, product_distance=1.0))])
     return spec, pos, types
+
+
+def polymer_spec(n_chains=200, chain_len=50, n_solvent=10000, box=30.0, seed=0):
+    """Linear chains as random walks of step 1.0 in solvent with harmonic repulsion between all pairs
+    (the polymer-in-solvent chemistry at a smaller size).  Type 0 = bead, 1 = solvent."""
+    rng = np.random.default_rng(seed)
+    chains = []
+    for c in range(n_chains):
+        start = (rng.random(3) - 0.5) * box
+        steps = rng.normal(size=(chain_len - 1, 3))
+        steps /= np.linalg.norm(steps, axis=1)[:, None]
+        p = np.vstack([start, start + np.cumsum(steps, axis=0)])
+        p = (p + box / 2) % box - box / 2
+        chains.append(p)
+    solvent = (rng.random((n_solvent, 3)) - 0.5) * box
+    spec = dict(box=(box, box, box), periodic=(True, True, True), diffusion=(0.1, 1.0),
+                potentials=[("harmonic_repulsion", a, b, dict(k=10.0, d=1.0)) for a, b in [(0, 0), (0, 1), (1, 1)]],
+                bond=dict(k=100.0, l0=1.0), angle=dict(k=10.0, theta0=np.pi),
+                dihedral=dict(k=1.0, n=3, phi0=0.0))
+    return spec, chains, solvent

@@ -2,9 +2,10 @@
 
 Tolerances (FP32 device arithmetic against FP64):
   * neighbour pair sets: bit-exact;
-  * forces: |F_gpu - F_ref| <= 1e-5 * max(|F_ref|, 1e-2 * F_rms) per particle, where F_rms is the
-    root-mean-square force of the system (the absolute floor guards particles whose net force
-    cancels to near zero); energies: relative 1e-5;
+  * forces: |F_gpu - F_ref| <= 1e-5 * max(|F_ref|, 0.1 * S) per particle, where S is the sum of the
+    magnitudes of the force terms acting on the particle (from the oracle).  The floor covers
+    particles whose net force cancels: FP32 rounds every term at ~6e-8 of its own size, so the error
+    of a cancelling sum scales with S, not with the net force; energies: relative 1e-5;
   * known-answer vectors: the reference test's own tolerance or 1e-5 relative, whichever is looser.
 """
 import numpy as np
@@ -34,11 +35,18 @@ def gpu_system(rg, spec, pos, types, seed=1):
     return ctx, k
 
 
-def force_error(f_gpu, f_ref):
-    rms = np.sqrt(np.mean(np.sum(f_ref ** 2, axis=1))) if len(f_ref) else 0.0
-    denom = np.maximum(np.linalg.norm(f_ref, axis=1), 1e-2 * rms)
+FLOOR = 0.1
+
+
+def force_error(f_gpu, f_ref, scale):
+    """Per-particle |dF| / max(|F|, FLOOR * S) and the plain relative error of the well-conditioned
+    particles (|F| >= FLOOR * S)."""
+    fn = np.linalg.norm(f_ref, axis=1)
+    denom = np.maximum(fn, FLOOR * scale)
     denom = np.where(denom > 0, denom, 1.0)
-    return np.linalg.norm(f_gpu - f_ref, axis=1) / denom
+    d = np.linalg.norm(f_gpu - f_ref, axis=1)
+    good = (fn >= FLOOR * scale) & (fn > 0)
+    return d / denom, (d[good] / fn[good]) if good.any() else np.zeros(1)
 
 
 @pytest.mark.parametrize("case", ka.PAIR_CASES, ids=lambda c: c["name"])
@@ -167,9 +175,11 @@ def _compare_forces(rg, spec, pos, types, label):
     o.nl_setup(o.calculate_max_cutoff())
     e_ref = o.calculate_forces()
     _, _, oid, f_ref, _ = o.particles()
-    (f_ref,) = by_id(oid, f_ref)
-    err = force_error(f_gpu, f_ref)
-    print(f"{label}: n={len(p)} max rel force err {err.max():.3e} (p99.9 {np.quantile(err, .999):.3e}), "
+    sc = o.force_scales()
+    (f_ref, sc) = by_id(oid, f_ref, sc)
+    err, rel_good = force_error(f_gpu, f_ref, sc)
+    print(f"{label}: n={len(p)} max err (floored) {err.max():.3e} (p99.9 {np.quantile(err, .999):.3e}); "
+          f"max rel err of well-conditioned {rel_good.max():.3e} ({len(rel_good)} particles); "
           f"energy {e_gpu:.9g} vs {e_ref:.9g} rel {abs(e_gpu - e_ref) / max(abs(e_ref), 1e-30):.3e}")
     return err, e_gpu, e_ref
 
@@ -288,7 +298,7 @@ def test_batch_replica_equals_plain_run(rg, handler):
     ctx = make_context(specs[0])
     b = ReplicaBatch(ctx, boxes, [2 * n for n in sizes], seed=77)
     b.set_particles(poss, typess)
-    b.configure(handler=handler, dt=1e-3, cell_radius=1, threads_per_block=256)
+    b.configure(handler=handler, dt=1e-3, cell_width_scale=1.0, threads_per_block=256)
     steps = 100
     b.step(steps)
     b.synchronize()
@@ -305,3 +315,57 @@ def test_batch_replica_equals_plain_run(rg, handler):
         np.testing.assert_array_equal(ia, ib)
         np.testing.assert_array_equal(ta, tb)
         np.testing.assert_allclose(pa, pb, rtol=0, atol=1e-5)
+
+
+@pytest.mark.parametrize("terms", ["bond", "angle", "dihedral", "all"])
+def test_polymer_forces_match_oracle(rg, terms):
+    """Random-walk chains (step 1.0) with bond/angle/dihedral terms in solvent, per term type."""
+    from tests.helpers import polymer_spec
+    spec, chains, solvent = polymer_spec(n_chains=200, chain_len=50, n_solvent=10000, box=30.0, seed=6)
+    use = {"bond", "angle", "dihedral"} if terms == "all" else {terms}
+    ctx = make_context(dict(spec, potentials=spec["potentials"] if terms == "all" else []))
+    ctx.configure_harmonic_bond(0, 0, spec["bond"]["k"] if "bond" in use else 0.0, spec["bond"]["l0"])
+    if "angle" in use:
+        ctx.configure_harmonic_angle(0, 0, 0, spec["angle"]["k"], spec["angle"]["theta0"])
+    if "dihedral" in use:
+        d = spec["dihedral"]
+        ctx.configure_cosine_dihedral(0, 0, 0, 0, d["k"], d["n"], d["phi0"])
+    k = rg.CUDAKernel(ctx, seed=1)
+    L = len(chains[0])
+    for c in chains:
+        k.add_topology(f32(c), np.zeros(L, np.int32), [(i, i + 1) for i in range(L - 1)])
+    k.add_particles(f32(solvent), np.ones(len(solvent), np.int32))
+    k.create_neighbor_list(1.0)
+    k.calculate_forces()
+    f_gpu, ids = k.get_forces()
+    p, t, ids2 = k.get_particles()
+    (f_gpu,) = by_id(ids, f_gpu)
+    (p, t) = by_id(ids2, p, t)
+    o = make_oracle(dict(spec, potentials=spec["potentials"] if terms == "all" else []), n_threads=4)
+    o.add_particles(p, t)
+    nb = len(chains) * L
+    idx = np.arange(nb).reshape(len(chains), L)
+    if "bond" in use:
+        o.add_harmonic_bonds(np.stack([idx[:, :-1].ravel(), idx[:, 1:].ravel()], 1), spec["bond"]["k"],
+                             spec["bond"]["l0"])
+    if "angle" in use:
+        o.add_harmonic_angles(np.stack([idx[:, :-2].ravel(), idx[:, 1:-1].ravel(), idx[:, 2:].ravel()], 1),
+                              spec["angle"]["k"], spec["angle"]["theta0"])
+    if "dihedral" in use:
+        d = spec["dihedral"]
+        o.add_cosine_dihedrals(np.stack([idx[:, :-3].ravel(), idx[:, 1:-2].ravel(), idx[:, 2:-1].ravel(),
+                                         idx[:, 3:].ravel()], 1), d["k"], d["n"], d["phi0"])
+    o.nl_setup(1.0)
+    e_ref = o.calculate_forces()
+    _, _, oid, f_ref, _ = o.particles()
+    sc = o.force_scales()
+    (f_ref, sc) = by_id(oid, f_ref, sc)
+    err, rel_good = force_error(f_gpu, f_ref, sc)
+    e_gpu = k.energy
+    print(f"polymer {terms}: max err (floored) {err.max():.3e} p99.9 {np.quantile(err, .999):.3e} "
+          f"well-conditioned max {rel_good.max():.3e}; energy {e_gpu:.9g} vs {e_ref:.9g}")
+    # dihedral terms within FP32 noise of the |cos phi| < 1e-4 zero-force threshold
+    # (TorsionPotential.cpp:91-93) are reported, not hidden: at most a handful of particles
+    bad = err > FORCE_RTOL
+    assert bad.sum() <= (3 if "dihedral" in use else 0), np.sort(err)[-8:]
+    assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
