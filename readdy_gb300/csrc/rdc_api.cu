@@ -199,6 +199,7 @@ void build_tables(const ContextData &c, const double box[3], double dt, Tables &
         d.band = band_for(h.educt_distance, L);
         d.rate = h.rate;
         d.inv_rate = h.rate > 0 ? (float)(1.0 / h.rate) : 0.f;
+        d.active = (h.rate > 0 && std::isfinite(d.inv_rate)) ? 1 : 0;
     }
     std::vector<std::vector<int>> o1(T);
     std::map<std::pair<int, int>, std::vector<int>> o2;
@@ -282,7 +283,7 @@ struct rdc_system {
         dfree(d.pos); dfree(d.id); dfree(d.tslot); dfree(d.force);
         dfree(d.pos_alt); dfree(d.id_alt); dfree(d.tslot_alt); dfree(d.force_alt);
         dfree(d.bin); dfree(d.rank); dfree(d.src);
-        dfree(d.cnt); dfree(d.start); dfree(d.scan_blocks);
+        dfree(d.cnt); dfree(d.start); dfree(d.scan_blocks); dfree(d.big_cells);
         dfree(d.tloc); dfree(d.counters); dfree(d.step);
         dfree(d.events); dfree(d.claim); dfree(d.taken); dfree(d.reaction_counts);
         dfree(d.epart); dfree(d.energy); dfree(d.counts_ring);
@@ -364,7 +365,8 @@ struct rdc_system {
 
     void alloc_cells(int ncells) {
         if (ncells == ncells_alloc) return;
-        dfree(d.cnt); dfree(d.start); dfree(d.scan_blocks);
+        dfree(d.cnt); dfree(d.start); dfree(d.scan_blocks); dfree(d.big_cells);
+        d.big_cells = dalloc<int>(ncells + 2);
         d.cnt = dalloc<int>(ncells + 2);
         d.start = dalloc<int>(ncells + 3);
         d.scan_blocks = dalloc<int>(scan_block_count(ncells + 2) + 1);
@@ -446,13 +448,19 @@ struct rdc_system {
         if (ids_out)
             for (int64_t i = 0; i < n; ++i) ids_out[i] = (uint64_t)(c[C_NEXT_ID] + i);
         sync();
-        // without a neighbour list the storage is one bin; keep the new particles reachable
+        // without a neighbour list the storage is kept unsorted: every particle is storage, none is in a
+        // cell; topology slots map to their insertion index
         if (!nl_ready) {
-            d.geo = make_geo(ctx.box, ctx.pbc, 0.0, radius);
-            alloc_cells(d.geo.ncells);
-            launch_bin(d, stream);
-            launch_sort(d, true, stream);
-            swap_buffers();
+            int upd2[2] = {(int)need, 0};
+            RDC_CUDA(cudaMemcpyAsync(d.counters + C_N, &upd2[0], sizeof(int), cudaMemcpyHostToDevice, stream));
+            RDC_CUDA(cudaMemcpyAsync(d.counters + C_N_INCELLS, &upd2[1], sizeof(int), cudaMemcpyHostToDevice,
+                                     stream));
+            if (tslots) {
+                std::vector<int> loc(n);
+                for (int64_t i = 0; i < n; ++i) loc[i] = base + (int)i;
+                RDC_CUDA(cudaMemcpyAsync(d.tloc + tslots[0], loc.data(), sizeof(int) * n, cudaMemcpyHostToDevice,
+                                         stream));
+            }
             sync();
         }
     }
@@ -642,10 +650,12 @@ void rdc_system::upload_topology() {
     d.bond_idx = bond_idx_dev; d.bond_par = bond_par_dev;
     d.angle_idx = angle_idx_dev; d.angle_par = angle_par_dev;
     d.dih_idx = dih_idx_dev; d.dih_par = dih_par_dev;
-    // tloc is rebuilt by a sort
-    launch_bin(d, stream);
-    launch_sort(d, forces_live, stream);
-    swap_buffers();
+    // with a neighbour list the new particles join the cells and tloc is rebuilt by a sort
+    if (nl_ready) {
+        launch_bin(d, stream);
+        launch_sort(d, forces_live, stream);
+        swap_buffers();
+    }
     sync();
     invalidate_graph();
 }

@@ -129,19 +129,27 @@ __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n
         if (b <= nc) src[cells[b] + rank[i]] = i;
     }
     __syncthreads();
+    __shared__ int big[64];
+    __shared__ int nbig;
+    if (threadIdx.x == 0) nbig = 0;
+    __syncthreads();
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         const int b = cells[c], e = cells[c + 1];
-        for (int j = b + 1; j < e; ++j) {
-            const int v = src[j];
-            int k = j - 1;
-            while (k >= b && src[k] > v) {
-                src[k + 1] = src[k];
-                --k;
-            }
-            src[k + 1] = v;
+        if (e - b > CELL_SORT_SMALL) {
+            const int q = atomicAdd(&nbig, 1);
+            if (q < 64) big[q] = c;
+            continue;
         }
+        insertion_sort(src, b, e);
     }
     __syncthreads();
+    // crowded cells: ordered by the whole block (rank[] is free scratch after the scatter)
+    if (nbig <= 64) {
+        for (int q = 0; q < nbig; ++q) block_rank_sort(src, const_cast<int *>(rank), cells[big[q]], cells[big[q] + 1]);
+    } else {
+        for (int c = 0; c < nc; ++c)
+            if (cells[c + 1] - cells[c] > CELL_SORT_SMALL) block_rank_sort(src, const_cast<int *>(rank), cells[c], cells[c + 1]);
+    }
     n_new = cells[nc + 1];
     n_in = cells[nc];
     for (int j = threadIdx.x; j < n_new; j += blockDim.x) {
@@ -167,6 +175,7 @@ __device__ inline void block_count_types(const float4 *pos, int n, int T, unsign
 
 struct SmemLayout {
     int *tab;
+    float *drift, *scale;
     PairPot *pots;
     uint64_t *key;
     int *idx, *state;
@@ -196,7 +205,8 @@ size_t batch_smem_bytes(int T, int NP, int max_events) {
 }
 
 // one step of one replica by the whole block
-__device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint64_t bd_step, uint64_t rx_step) {
+__device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, const RxnTables &rt, uint64_t bd_step,
+                             uint64_t rx_step) {
     __shared__ RepDesc D;
     __shared__ RepState st;
     __shared__ int sh_nev, sh_status;
@@ -209,8 +219,9 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
     __syncthreads();
     const Tables *tab = B.tab;
     const int T = tab->ntypes, NP = tab->npots;
-    const Geo &g = D.geo;
-    const int nc = g.ncells;
+    const Geo &gs = D.geo;
+    const GeoR g = geo_r(gs);
+    const int nc = gs.ncells;
     float4 *posX = (st.cur ? B.posB : B.posA) + D.poff;
     uint32_t *idX = (st.cur ? B.idB : B.idA) + D.poff;
     float4 *posY = (st.cur ? B.posA : B.posB) + D.poff;
@@ -227,15 +238,16 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
         if (i < n_in && NP > 0) pair_force_at(i, p, posX, cells, g, 1, S.tab, S.pots, T, fx, fy, fz, e);
         const uint32_t id = idX[i];
-        const float4 q = euler_bd(p, fx, fy, fz, id, D.seed, bd_step, tab, g);
+        const int t = itype(p);
+        const float4 q = euler_bd(p, fx, fy, fz, id, D.seed, bd_step, S.drift[t], S.scale[t], g);
         posY[i] = q;
         idY[i] = id;
-        bin[i] = bin_of(q, g);
+        bin[i] = bin_of(q, gs);
     }
     __syncthreads();
     block_rank(n, bin, rank, cells, nc + 2);
     int n1, nin1;
-    block_sort(posY, idY, n, posX, idX, bin, rank, src, cells, g, n1, nin1);
+    block_sort(posY, idY, n, posX, idX, bin, rank, src, cells, gs, n1, nin1);
 
     int n_final = n1, nin_final = nin1, cur = st.cur, next_id = st.next_id;
     if (B.reactions) {
@@ -252,7 +264,7 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
             }
         };
         for (int i = threadIdx.x; i < n1; i += blockDim.x)
-            events_at(i, i < nin1, posX, idX, cells, g, 1, tab, D.seed, rx_step, B.handler, emit);
+            events_at(i, i < nin1, posX, idX, cells, g, 1, rt, D.seed, rx_step, B.handler, emit);
         __syncthreads();
         const int E = min(sh_nev, ecap);
         if (E > 0) {
@@ -264,16 +276,16 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
             t.capacity = D.cap;
             t.next_id = (uint32_t)st.next_id;
             ApplyResult res;
-            block_resolve_apply(ev, E, B.max_events_sm, S.key, S.idx, S.state, tab, g, D.seed, rx_step, t, res);
+            block_resolve_apply(ev, E, B.max_events_sm, S.key, S.idx, S.state, tab, gs, D.seed, rx_step, t, res);
             next_id = st.next_id + res.ids;
             if (threadIdx.x == 0) sh_status |= res.status;
             if (res.winners > 0) {
                 // particles changed cells, appeared or vanished: sort again, into Y
                 const int n_total = n1 + res.births;
-                block_bin(posX, n_total, bin, g);
+                block_bin(posX, n_total, bin, gs);
                 block_rank(n_total, bin, rank, cells, nc + 2);
                 int n2, nin2;
-                block_sort(posX, idX, n_total, posY, idY, bin, rank, src, cells, g, n2, nin2);
+                block_sort(posX, idX, n_total, posY, idY, bin, rank, src, cells, gs, n2, nin2);
                 n_final = n2;
                 nin_final = nin2;
                 cur ^= 1;
@@ -298,14 +310,24 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, uint
     __syncthreads();
 }
 
-__global__ void k_batch_step(BatchDev B) {
+__global__ void __launch_bounds__(512, 1) k_batch_step(BatchDev B) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int sh_r;
+    __shared__ int sh_rt_ints[MAX_TYPES + MAX_REACTIONS * 3 + MAX_TYPES * MAX_TYPES + MAX_TYPES];
+    __shared__ ReactionDev sh_rx[MAX_REACTIONS];
+    __shared__ float sh_drift[MAX_TYPES], sh_scale[MAX_TYPES];
     const Tables *tab = B.tab;
     const int T = tab->ntypes, NP = tab->npots;
     SmemLayout S = carve(smem, T, NP, B.max_events_sm);
+    S.drift = sh_drift;
+    S.scale = sh_scale;
     for (int k = threadIdx.x; k < T * T; k += blockDim.x) S.tab[k] = tab->pair_tab[k];
     for (int k = threadIdx.x; k < NP; k += blockDim.x) S.pots[k] = tab->pots[k];
+    for (int k = threadIdx.x; k < T; k += blockDim.x) {
+        sh_drift[k] = tab->bd_drift[k];
+        sh_scale[k] = tab->bd_scale[k];
+    }
+    const RxnTables rt = stage_rxn_tables(tab, sh_rt_ints, sh_rx);
     const uint64_t bd_step = B.step[0], rx_step = B.step[1];
     __syncthreads();
     for (;;) {
@@ -314,7 +336,7 @@ __global__ void k_batch_step(BatchDev B) {
         const int w = sh_r;
         __syncthreads();
         if (w >= B.R) break;
-        replica_step(B, B.order[w], S, bd_step, rx_step);
+        replica_step(B, B.order[w], S, rt, bd_step, rx_step);
     }
 }
 
@@ -560,6 +582,7 @@ struct rdc_batch {
     void configure_launch() {
         smem = batch_smem_bytes(tab.ntypes, tab.npots, d.max_events_sm);
         RDC_CUDA(cudaFuncSetAttribute(k_batch_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        RDC_CUDA(cudaFuncSetAttribute(k_batch_step, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         int per_sm = 0;
         RDC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_step, threads, smem));
         int dev = 0, sms = 0;

@@ -95,24 +95,59 @@ __device__ inline float mi_diff(float rhs, float lhs, float L, float hL, int pbc
     return dv;
 }
 
+// geometry held in registers by the hot loops (same member names as Geo; the box edges are FP32-exact,
+// so (double)L is the FP64 box of the reference)
+struct GeoR {
+    float L[3], hL[3], invW[3];
+    int dims[3];
+    int pbc[3];
+    int exact_always;
+};
+
+__device__ inline GeoR geo_r(const Geo &g) {
+    GeoR r;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        r.L[d] = g.L[d];
+        r.hL[d] = g.hL[d];
+        r.invW[d] = g.invW[d];
+        r.dims[d] = g.dims[d];
+        r.pbc[d] = g.pbc[d];
+    }
+    r.exact_always = g.exact_always;
+    return r;
+}
+
+// result of the FP64 pair predicate: the rounded FP64 difference and whether d^2 < c^2
+struct ExactPair {
+    float dx, dy, dz, d2;
+    int inside;
+};
+
 // bcs::shortestDifference + inner product in FP64 with the reference's rounding order
-// ((0 + x*x) + y*y) + z*z and no fused multiply-add
-__device__ inline double dist2_exact(float4 lhs, float4 rhs, const Geo &g, double &dx, double &dy, double &dz) {
+// ((0 + x*x) + y*y) + z*z and no fused multiply-add.  Out of line: it runs only for the rare pairs
+// within the FP32 rounding band of a cutoff and keeps the hot loops small.
+static __device__ __noinline__ ExactPair pair_exact_fp64(float4 lhs, float4 rhs, float L0, float L1, float L2, int pbcmask,
+                                                  double c2) {
     double d[3] = {__dsub_rn((double)rhs.x, (double)lhs.x), __dsub_rn((double)rhs.y, (double)lhs.y),
                    __dsub_rn((double)rhs.z, (double)lhs.z)};
+    const double L[3] = {(double)L0, (double)L1, (double)L2};
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        if (g.pbc[i]) {
-            const double h = g.Ld[i] * 0.5;
-            if (d[i] > h) d[i] = __dsub_rn(d[i], g.Ld[i]);
-            else if (d[i] <= -h) d[i] = __dadd_rn(d[i], g.Ld[i]);
+        if (pbcmask & (1 << i)) {
+            const double h = L[i] * 0.5;
+            if (d[i] > h) d[i] = __dsub_rn(d[i], L[i]);
+            else if (d[i] <= -h) d[i] = __dadd_rn(d[i], L[i]);
         }
     }
     double s = __dmul_rn(d[0], d[0]);
     s = __dadd_rn(s, __dmul_rn(d[1], d[1]));
     s = __dadd_rn(s, __dmul_rn(d[2], d[2]));
-    dx = d[0]; dy = d[1]; dz = d[2];
-    return s;
+    ExactPair r;
+    r.dx = (float)d[0]; r.dy = (float)d[1]; r.dz = (float)d[2];
+    r.d2 = (float)s;
+    r.inside = s < c2;
+    return r;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -156,12 +191,13 @@ __device__ inline float sq_err(float h, float l, float p) {  // (h + l)^2 - p, t
     return __fadd_rn(__fmaf_rn(h, h, -p), 2.0f * h * l);
 }
 
-__device__ inline PairExact pair_exact(float4 lhs, float4 rhs, const float L[3], const float hL[3], const int pbc[3]) {
+template <typename G>
+__device__ inline PairExact pair_exact(float4 lhs, float4 rhs, const G &g) {
     PairExact r;
     float lx, ly, lz;
-    mi_diff2(rhs.x, lhs.x, L[0], hL[0], pbc[0], r.dx, lx);
-    mi_diff2(rhs.y, lhs.y, L[1], hL[1], pbc[1], r.dy, ly);
-    mi_diff2(rhs.z, lhs.z, L[2], hL[2], pbc[2], r.dz, lz);
+    mi_diff2(rhs.x, lhs.x, g.L[0], g.hL[0], g.pbc[0], r.dx, lx);
+    mi_diff2(rhs.y, lhs.y, g.L[1], g.hL[1], g.pbc[1], r.dy, ly);
+    mi_diff2(rhs.z, lhs.z, g.L[2], g.hL[2], g.pbc[2], r.dz, lz);
     const float px = __fmul_rn(r.dx, r.dx), py = __fmul_rn(r.dy, r.dy), pz = __fmul_rn(r.dz, r.dz);
     const float s1 = __fadd_rn(px, py);
     const float t1 = two_sum_err(px, py, s1);
@@ -191,7 +227,8 @@ struct PairGeom {
     float dx, dy, dz, d2;
 };
 
-__device__ inline PairGeom pair_geom(float4 lhs, float4 rhs, const Geo &g) {
+template <typename G>
+__device__ inline PairGeom pair_geom(float4 lhs, float4 rhs, const G &g) {
     PairGeom r;
     r.dx = mi_diff(rhs.x, lhs.x, g.L[0], g.hL[0], g.pbc[0]);
     r.dy = mi_diff(rhs.y, lhs.y, g.L[1], g.hL[1], g.pbc[1]);
@@ -202,17 +239,18 @@ __device__ inline PairGeom pair_geom(float4 lhs, float4 rhs, const Geo &g) {
 
 // d^2 < c^2 decided exactly as the FP64 reference: FP32 outside the rounding band, FP64 inside it.
 // On an FP64 decision the FP32 difference is replaced by the rounded FP64 one.
-__device__ inline bool within(const PairGeom &pg0, PairGeom &pg, float4 lhs, float4 rhs, const Geo &g, float c2f,
+template <typename G>
+__device__ inline bool within(const PairGeom &pg0, PairGeom &pg, float4 lhs, float4 rhs, const G &g, float c2f,
                               float band, double c2) {
     if (!g.exact_always) {
         if (pg0.d2 < c2f - band) return true;
         if (pg0.d2 > c2f + band) return false;
     }
-    double dx, dy, dz;
-    double d2 = dist2_exact(lhs, rhs, g, dx, dy, dz);
-    pg.dx = (float)dx; pg.dy = (float)dy; pg.dz = (float)dz;
-    pg.d2 = (float)d2;
-    return d2 < c2;
+    const ExactPair e = pair_exact_fp64(lhs, rhs, g.L[0], g.L[1], g.L[2],
+                                        (g.pbc[0] ? 1 : 0) | (g.pbc[1] ? 2 : 0) | (g.pbc[2] ? 4 : 0), c2);
+    pg.dx = e.dx; pg.dy = e.dy; pg.dz = e.dz;
+    pg.d2 = e.d2;
+    return e.inside != 0;
 }
 
 // in-box test of the cell list (CellLinkedList.cpp:188-192), exact because the box is FP32-exact
@@ -224,7 +262,8 @@ __device__ inline bool in_box(float4 p, const Geo &g) {
 __device__ inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // cell of a particle; the grid is row-major with z fastest (include/readdy/common/Index.h:130-141)
-__device__ inline void cell_coords(float4 p, const Geo &g, int &cx, int &cy, int &cz) {
+template <typename G>
+__device__ inline void cell_coords(float4 p, const G &g, int &cx, int &cy, int &cz) {
     cx = clampi(__float2int_rd((p.x + g.hL[0]) * g.invW[0]), 0, g.dims[0] - 1);
     cy = clampi(__float2int_rd((p.y + g.hL[1]) * g.invW[1]), 0, g.dims[1] - 1);
     cz = clampi(__float2int_rd((p.z + g.hL[2]) * g.invW[2]), 0, g.dims[2] - 1);
@@ -280,12 +319,13 @@ __device__ inline float ipow(float x, int n) {
 //   weak piecewise harmonic: k, d0, depth, rc, d0^2 hi, d0^2 lo, rc^2 hi, rc^2 lo, mid^2 (mid = (d0 + rc) / 2)
 //   Lennard-Jones: m, n, rc, shift, epsilon, sigma^2, k, E(rc) shift, is-12-6, sigma^6 hi, sigma^6 lo
 //   screened electrostatics: C, kappa, D, sigma, exponent
-__device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float4 lhs, float4 rhs, const Geo &geo,
+template <typename G>
+__device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float4 lhs, float4 rhs, const G &geo,
                                   float &fx, float &fy, float &fz, float &e) {
     switch (pp.kind) {
         case POT_HARMONIC_REPULSION: {  // PotentialsOrder2.h:73-91; r - d = (d2 - d^2) / (r + d)
             const float k = pp.p[0], d = pp.p[1];
-            const PairExact x = pair_exact(lhs, rhs, geo.L, geo.hL, geo.pbc);
+            const PairExact x = pair_exact(lhs, rhs, geo);
             const float d2 = __fadd_rn(x.d2.hi, x.d2.lo);
             const float r = sqrtf(d2);
             const float rd = ff_sub(x.d2, pp.p[2], pp.p[3]) / (r + d);
@@ -298,7 +338,7 @@ __device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float4 l
         }
         case POT_WEAK_PIECEWISE_HARMONIC: {  // PotentialsOrder2.h:131-183
             const float k = pp.p[0], d0 = pp.p[1], depth = pp.p[2], rc = pp.p[3];
-            const PairExact x = pair_exact(lhs, rhs, geo.L, geo.hL, geo.pbc);
+            const PairExact x = pair_exact(lhs, rhs, geo);
             const float d2 = __fadd_rn(x.d2.hi, x.d2.lo);
             const float dist = sqrtf(d2);
             const float half = 0.5f * (rc - d0);
@@ -330,7 +370,7 @@ __device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float4 l
             if (pp.p[8] != 0.0f) {
                 // 12-6: F = -6k s^6 (2 s^6 - 1) / r^2 x and E = k s^6 (s^6 - 1), s^6 = sigma^6 / r^6, with
                 // 2 sigma^6 - r^6 and sigma^6 - r^6 from a float-float r^6 (they cancel at the minimum and at sigma)
-                const PairExact x = pair_exact(lhs, rhs, geo.L, geo.hL, geo.pbc);
+                const PairExact x = pair_exact(lhs, rhs, geo);
                 const float h = x.d2.hi, l = x.d2.lo;
                 const float q = __fmul_rn(h, h);
                 const float eq = __fmaf_rn(h, h, -q);
@@ -406,7 +446,7 @@ __device__ inline F3 shortest3(float4 lhs, float4 rhs, const Geo &g) {
 // (BondedPotential.h:105-113, CPUTopologyActions.cpp:61-74); r - l0 = (d2 - l0^2) / (r + l0)
 // from the float-float d2.  P = (k, l0, l0^2 hi, l0^2 lo)
 __device__ inline F3 bond_force(float4 pi, float4 pj, float4 P, const Geo &g, int role, float &e) {
-    const PairExact x = pair_exact(pi, pj, g.L, g.hL, g.pbc);
+    const PairExact x = pair_exact(pi, pj, g);
     const float r = sqrtf(__fadd_rn(x.d2.hi, x.d2.lo));
     const float rd = ff_sub(x.d2, P.z, P.w) / (r + P.y);
     e = P.x * rd * rd;

@@ -90,7 +90,8 @@ enum Counter : int {
     C_NEXT_ID = 5,
     C_REC = 6,       // observable records written
     C_N_BIRTHS = 7,  // births of the last reaction step (host statistics)
-    C_COUNT = 8
+    C_BIG = 8,       // cells with more than CELL_SORT_SMALL entries found by the last sort
+    C_COUNT = 9
 };
 
 struct SysDev {
@@ -106,6 +107,7 @@ struct SysDev {
     int *tslot_alt;
     float4 *force_alt;
     int *bin, *rank, *src;
+    int *big_cells;  // cells too full for the per-thread insertion sort (capacity ncells)
     int *cnt, *start;
     int *scan_blocks;
     int *tloc;

@@ -28,11 +28,13 @@ namespace rdc {
 __global__ void k_integrate_bin(SysDev s, int integrate, int bin) {
     const int n = s.counters[C_N_TOTAL];
     const uint64_t step = s.step[0];
+    const GeoR g = geo_r(s.geo);
     GRID_STRIDE(i, n) {
         float4 p = s.pos[i];
-        if (integrate && itype(p) >= 0) {
+        const int t = itype(p);
+        if (integrate && t >= 0) {
             const float4 f = s.force[i];
-            p = euler_bd(p, f.x, f.y, f.z, s.id[i], s.seed, step, s.tab, s.geo);
+            p = euler_bd(p, f.x, f.y, f.z, s.id[i], s.seed, step, s.tab->bd_drift[t], s.tab->bd_scale[t], g);
             s.pos[i] = p;
         }
         if (bin) {
@@ -119,16 +121,24 @@ __global__ void k_scatter(SysDev s) {
 __global__ void k_cell_order(SysDev s) {
     GRID_STRIDE(c, s.geo.ncells) {
         const int b = s.start[c], e = s.start[c + 1];
-        for (int j = b + 1; j < e; ++j) {
-            const int v = s.src[j];
-            int k = j - 1;
-            while (k >= b && s.src[k] > v) {
-                s.src[k + 1] = s.src[k];
-                --k;
-            }
-            s.src[k + 1] = v;
+        if (e - b > CELL_SORT_SMALL) {
+            s.big_cells[atomicAdd(&s.counters[C_BIG], 1)] = c;
+            continue;
         }
+        insertion_sort(s.src, b, e);
     }
+}
+
+// cells with many entries: one block per cell, every entry's rank is the number of smaller entries
+// (the source indices of a cell are distinct); rank[] is free scratch once the scatter is done
+__global__ void k_big_cell_order(SysDev s) {
+    const int nbig = s.counters[C_BIG];
+    for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
+        const int c = s.big_cells[q];
+        block_rank_sort(s.src, s.rank, s.start[c], s.start[c + 1]);
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.counters[C_BIG] = 0;
 }
 
 __global__ void k_gather(SysDev s, int permute_force) {
@@ -154,7 +164,7 @@ __global__ void k_gather(SysDev s, int permute_force) {
 // K3 pair forces: one thread per particle, full (both-direction) stencil, force and half the pair
 // energies accumulated in registers; per-block FP64 energy partials in a fixed order
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(FORCE_THREADS) k_pair_forces(SysDev s) {
+__global__ void __launch_bounds__(FORCE_THREADS, 2) k_pair_forces(SysDev s) {
     __shared__ int sh_tab[MAX_TYPES * MAX_TYPES];
     __shared__ PairPot sh_pots[MAX_PAIR_POTENTIALS];
     const Tables *tab = s.tab;
@@ -163,11 +173,12 @@ __global__ void __launch_bounds__(FORCE_THREADS) k_pair_forces(SysDev s) {
     for (int k = threadIdx.x; k < NP; k += blockDim.x) sh_pots[k] = tab->pots[k];
     __syncthreads();
     const int n = s.counters[C_N], n_in = s.counters[C_N_INCELLS];
+    const GeoR g = geo_r(s.geo);
     double esum = 0.0;
     GRID_STRIDE(i, n) {
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
         if (i < n_in && NP > 0)
-            pair_force_at(i, s.pos[i], s.pos, s.start, s.geo, s.radius, sh_tab, sh_pots, T, fx, fy, fz, e);
+            pair_force_at(i, s.pos[i], s.pos, s.start, g, s.radius, sh_tab, sh_pots, T, fx, fy, fz, e);
         s.force[i] = make_float4(fx, fy, fz, e);
         esum += (double)e;
     }
@@ -230,6 +241,11 @@ __global__ void k_energy_final(SysDev s, int pair, int bonded) {
 // K6 reaction events that pass their acceptance coin
 // ------------------------------------------------------------------------------------------------
 __global__ void k_events(SysDev s, int handler) {
+    __shared__ int sh_rt_ints[MAX_TYPES + MAX_REACTIONS * 3 + MAX_TYPES * MAX_TYPES + MAX_TYPES];
+    __shared__ ReactionDev sh_rx[MAX_REACTIONS];
+    const RxnTables rt = stage_rxn_tables(s.tab, sh_rt_ints, sh_rx);
+    __syncthreads();
+    const GeoR g = geo_r(s.geo);
     const int n = s.counters[C_N], n_in = s.counters[C_N_INCELLS];
     const uint64_t step = s.step[1];
     auto emit = [&](uint64_t key, int p1, int p2, int r) {
@@ -243,7 +259,7 @@ __global__ void k_events(SysDev s, int handler) {
         }
     };
     GRID_STRIDE(i, n) {
-        events_at(i, i < n_in, s.pos, s.id, s.start, s.geo, s.radius, s.tab, s.seed, step, handler, emit);
+        events_at(i, i < n_in, s.pos, s.id, s.start, g, s.radius, rt, s.seed, step, handler, emit);
     }
 }
 
@@ -328,31 +344,21 @@ __global__ void k_record_advance(SysDev s) {
 
 __global__ void k_pairs(SysDev s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out) {
     const int n_in = s.counters[C_N_INCELLS];
-    const Geo &g = s.geo;
+    const GeoR g = geo_r(s.geo);
     GRID_STRIDE(i, n_in) {
         const float4 p = s.pos[i];
-        int cx, cy, cz;
-        cell_coords(p, g, cx, cy, cz);
-        int ax[7], ay[7], az[7];
-        const int nx = axis_cells(cx, g.dims[0], g.pbc[0], s.radius, ax);
-        const int ny = axis_cells(cy, g.dims[1], g.pbc[1], s.radius, ay);
-        const int nz = axis_cells(cz, g.dims[2], g.pbc[2], s.radius, az);
         const uint32_t idi = s.id[i];
-        for (int a = 0; a < nx; ++a)
-            for (int b = 0; b < ny; ++b)
-                for (int c = 0; c < nz; ++c) {
-                    const int cell = cell_index(ax[a], ay[b], az[c], g);
-                    const int jb = max(s.start[cell], i + 1), je = s.start[cell + 1];
-                    for (int j = jb; j < je; ++j) {
-                        const float4 q = s.pos[j];
-                        const PairGeom g0 = pair_geom(p, q, g);
-                        PairGeom gg = g0;
-                        if (!within(g0, gg, p, q, g, c2f, band, c2)) continue;
-                        const uint32_t idj = s.id[j];
-                        const int k = atomicAdd(n_out, 1);
-                        if (k < cap) out[k] = ((uint64_t)min(idi, idj) << 32) | max(idi, idj);
-                    }
-                }
+        for_each_neighbor_range(p, g, s.start, s.radius, [&](int jb0, int je) {
+            for (int j = max(jb0, i + 1); j < je; ++j) {
+                const float4 q = s.pos[j];
+                const PairGeom g0 = pair_geom(p, q, g);
+                PairGeom gg = g0;
+                if (!within(g0, gg, p, q, g, c2f, band, c2)) continue;
+                const uint32_t idj = s.id[j];
+                const int k = atomicAdd(n_out, 1);
+                if (k < cap) out[k] = ((uint64_t)min(idi, idj) << 32) | max(idi, idj);
+            }
+        });
     }
 }
 
@@ -381,6 +387,7 @@ void launch_sort(const SysDev &s, bool permute_force, cudaStream_t st) {
     launch_scan(s.cnt, s.start, s.scan_blocks, nb, st);
     k_scatter<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
     k_cell_order<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
+    k_big_cell_order<<<152, 512, 0, st>>>(s);
     k_gather<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, permute_force ? 1 : 0);
 }
 

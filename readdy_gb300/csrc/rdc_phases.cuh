@@ -26,18 +26,95 @@ __device__ inline int axis_cells(int c, int dim, int pbc, int r, int *out) {
     return n;
 }
 
-// calls f(cell) for every cell of the stencil around the particle's cell, in a fixed order
-template <typename F>
-__device__ inline void for_each_stencil_cell(float4 p, const Geo &g, int radius, F f) {
+// cells up to this many entries are ordered by one thread (insertion sort)
+constexpr int CELL_SORT_SMALL = 32;
+
+__device__ inline void insertion_sort(int *a, int b, int e) {
+    for (int j = b + 1; j < e; ++j) {
+        const int v = a[j];
+        int k = j - 1;
+        while (k >= b && a[k] > v) {
+            a[k + 1] = a[k];
+            --k;
+        }
+        a[k + 1] = v;
+    }
+}
+
+// orders the distinct values a[b..e) by the whole block: each value's rank is the count of smaller
+// values; tmp[b..e) is scratch
+__device__ inline void block_rank_sort(int *a, int *tmp, int b, int e) {
+    const int k = e - b;
+    for (int t = threadIdx.x; t < k; t += blockDim.x) {
+        const int v = a[b + t];
+        int r = 0;
+        for (int u = 0; u < k; ++u) r += a[b + u] < v;
+        tmp[b + r] = v;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < k; t += blockDim.x) a[b + t] = tmp[b + t];
+    __syncthreads();
+}
+
+// Calls f(jb, je) for the storage ranges of every cell of the (2r+1)^3 stencil around the particle's
+// cell, cells in x-major, z-fastest order.  For r = 1 on grids of at least 3 cells along each periodic
+// axis the three z-cells of a column are contiguous in storage and are visited as one range (two if
+// the column wraps); other grids take the general per-cell path.
+template <typename G, typename F>
+__device__ inline void for_each_neighbor_range(float4 p, const G &g, const int *__restrict__ start, int radius,
+                                               F f) {
     int cx, cy, cz;
     cell_coords(p, g, cx, cy, cz);
+    const int dx0 = g.dims[0], dy0 = g.dims[1], dz0 = g.dims[2];
+    const bool fast = radius == 1 && (!g.pbc[0] || dx0 >= 3) && (!g.pbc[1] || dy0 >= 3) && (!g.pbc[2] || dz0 >= 3);
+    if (fast) {
+#pragma unroll 1
+        for (int ox = -1; ox <= 1; ++ox) {
+            int x = cx + ox;
+            if (x < 0) {
+                if (!g.pbc[0]) continue;
+                x += dx0;
+            } else if (x >= dx0) {
+                if (!g.pbc[0]) continue;
+                x -= dx0;
+            }
+#pragma unroll 1
+            for (int oy = -1; oy <= 1; ++oy) {
+                int y = cy + oy;
+                if (y < 0) {
+                    if (!g.pbc[1]) continue;
+                    y += dy0;
+                } else if (y >= dy0) {
+                    if (!g.pbc[1]) continue;
+                    y -= dy0;
+                }
+                const int base = (x * dy0 + y) * dz0;
+                int z0 = cz - 1, z1 = cz + 1;
+                if (z0 < 0) {
+                    if (g.pbc[2]) f(start[base + dz0 - 1], start[base + dz0]);
+                    z0 = 0;
+                }
+                bool wrap_hi = false;
+                if (z1 >= dz0) {
+                    wrap_hi = g.pbc[2] != 0;
+                    z1 = dz0 - 1;
+                }
+                f(start[base + z0], start[base + z1 + 1]);
+                if (wrap_hi) f(start[base], start[base + 1]);
+            }
+        }
+        return;
+    }
     int ax[7], ay[7], az[7];
-    const int nx = axis_cells(cx, g.dims[0], g.pbc[0], radius, ax);
-    const int ny = axis_cells(cy, g.dims[1], g.pbc[1], radius, ay);
-    const int nz = axis_cells(cz, g.dims[2], g.pbc[2], radius, az);
+    const int nx = axis_cells(cx, dx0, g.pbc[0], radius, ax);
+    const int ny = axis_cells(cy, dy0, g.pbc[1], radius, ay);
+    const int nz = axis_cells(cz, dz0, g.pbc[2], radius, az);
     for (int a = 0; a < nx; ++a)
         for (int b = 0; b < ny; ++b)
-            for (int c = 0; c < nz; ++c) f(cell_index(ax[a], ay[b], az[c], g));
+            for (int c = 0; c < nz; ++c) {
+                const int cell = az[c] + dz0 * (ay[b] + dy0 * ax[a]);
+                f(start[cell], start[cell + 1]);
+            }
 }
 
 // exclusive scan of one value per thread across the block; total receives the block sum
@@ -85,18 +162,19 @@ __device__ inline double block_sum_double(double v) {
 
 // Pair force and half pair energy on particle i (storage index inside the cells) from every
 // neighbour of the stencil; the full both-direction iteration of CPUCalculateForces.cpp:214-268.
+template <typename G>
 __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const int *__restrict__ start,
-                                     const Geo &g, int radius, const int *tab, const PairPot *pots, int T, float &fx,
+                                     const G &g, int radius, const int *tab, const PairPot *pots, int T, float &fx,
                                      float &fy, float &fz, float &e) {
     const int ti = itype(p);
-    for_each_stencil_cell(p, g, radius, [&](int cell) {
-        const int jb = start[cell], je = start[cell + 1];
+    const int *trow = tab + ti * T;
+    for_each_neighbor_range(p, g, start, radius, [&](int jb, int je) {
         for (int j = jb; j < je; ++j) {
             if (j == i) continue;
             const float4 q = pos[j];
             const int tj = itype(q);
             if (tj < 0) continue;
-            const int pt = tab[ti * T + tj];
+            const int pt = trow[tj];
             if (pt == 0) continue;
             const PairGeom g0 = pair_geom(p, q, g);
             const int first = pt >> 8, cnt = pt & 0xff;
@@ -109,12 +187,14 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
     });
 }
 
+// pairs near enough to react are collected during the event scan and their coins drawn afterwards
+constexpr int PAIR_BATCH = 8;
+
 // Euler-Maruyama update of one particle (CPUEulerBDIntegrator.cpp:66-73), FP32, Philox noise
 // keyed by (seed, particle id, integrator step)
+template <typename G>
 __device__ inline float4 euler_bd(float4 p, float fx, float fy, float fz, uint32_t id, uint64_t seed, uint64_t step,
-                                  const Tables *tab, const Geo &g) {
-    const int t = itype(p);
-    const float drift = tab->bd_drift[t], sc = tab->bd_scale[t];
+                                  float drift, float sc, const G &g) {
     float n0, n1, n2, n3;
     normal4(rng_draw(seed, id, 0u, step, RNG_BD, 0u), n0, n1, n2, n3);
     p.x = wrap1(p.x + (sc * n0 + fx * drift), g.L[0], g.hL[0], g.pbc[0]);
@@ -128,62 +208,99 @@ __device__ inline float4 euler_bd(float4 p, float fx, float fy, float fz, uint32
 // ------------------------------------------------------------------------------------------------
 __device__ inline uint64_t coin_bits(U4 r) { return ((uint64_t)r.x << 32) | r.y; }
 
+// Priority of an accepted event (smaller resolves first).  Uncontrolled approximation: a uniformly
+// random order (the shuffle of CPUUncontrolledApproximation.cpp:198).  Gillespie: the exponential
+// clock E / k with E ~ Exp(1), whose order is proportional-to-rate selection without replacement
+// (algorithm.h:80-88).  The clock is an FP32 value in the high word (positive floats order like their
+// bits) and a random word breaks ties; everything stays off the FP64 pipe.
 __device__ inline uint64_t priority_key(U4 r, const ReactionDev &R, int handler) {
     if (handler == H_GILLESPIE) {
-        // exponential clock E / k with E ~ Exp(1): the order of proportional-to-rate selection
-        // without replacement (algorithm.h:80-88)
-        const double u = ((double)r.z + 0.5) * (1.0 / 4294967296.0);
-        const double clock = -log(u) / R.rate;
-        return (uint64_t)__double_as_longlong(clock);  // positive doubles order like their bits
+        const float clock = -logf(u01(r.z)) * R.inv_rate;
+        return ((uint64_t)__float_as_uint(clock) << 32) | r.w;
     }
-    return ((uint64_t)r.z << 32) | r.w;  // uniformly random order (the shuffle, :198)
+    return ((uint64_t)r.z << 32) | r.w;
+}
+
+// the reaction lookup tables of Tables, staged in shared memory by the kernels that generate events
+struct RxnTables {
+    const int *o1_tab, *o1_list, *o2_tab, *o2_list, *o2_any;
+    const ReactionDev *rx;
+    int T;
+};
+
+__device__ inline int rxn_tables_words(int T, int NR) { return T + NR + T * T + 2 * NR + T; }
+
+// all threads of the block copy the reaction tables into smem (words ints, then NR ReactionDev)
+__device__ inline RxnTables stage_rxn_tables(const Tables *tab, int *smem_ints, ReactionDev *smem_rx) {
+    const int T = tab->ntypes, NR = tab->nreactions;
+    int *o1t = smem_ints, *o1l = o1t + T, *o2t = o1l + NR, *o2l = o2t + T * T, *o2a = o2l + 2 * NR;
+    for (int k = threadIdx.x; k < T; k += blockDim.x) { o1t[k] = tab->o1_tab[k]; o2a[k] = tab->o2_any[k]; }
+    for (int k = threadIdx.x; k < NR; k += blockDim.x) { o1l[k] = tab->o1_list[k]; smem_rx[k] = tab->reactions[k]; }
+    for (int k = threadIdx.x; k < 2 * NR; k += blockDim.x) o2l[k] = tab->o2_list[k];
+    for (int k = threadIdx.x; k < T * T; k += blockDim.x) o2t[k] = tab->o2_tab[k];
+    return RxnTables{o1t, o1l, o2t, o2l, o2a, smem_rx, T};
 }
 
 // order-1 events of particle i and order-2 events of the pairs (i, j > i); emit(key, p1, p2, r)
-// with p1 the particle of smaller id
-template <typename Emit>
+// with p1 the particle of smaller id.  As for the forces, pairs near enough to react are collected
+// during the scan and their acceptance coins drawn afterwards.
+template <typename G, typename Emit>
 __device__ inline void events_at(int i, bool in_cells, const float4 *__restrict__ pos, const uint32_t *__restrict__ id,
-                                 const int *__restrict__ start, const Geo &g, int radius, const Tables *tab,
+                                 const int *__restrict__ start, const G &g, int radius, const RxnTables &rt,
                                  uint64_t seed, uint64_t step, int handler, Emit emit) {
     const float4 p = pos[i];
     const int ti = itype(p);
     if (ti < 0) return;
-    const int T = tab->ntypes;
     const uint32_t idi = id[i];
-    const int o1 = tab->o1_tab[ti];
+    const int o1 = rt.o1_tab[ti];
     for (int k = (o1 >> 8); k < (o1 >> 8) + (o1 & 0xff); ++k) {
-        const int r = tab->o1_list[k];
-        const ReactionDev &R = tab->reactions[r];
-        if (!(R.rate > 0)) continue;
+        const int r = rt.o1_list[k];
+        const ReactionDev &R = rt.rx[r];
+        if (!R.active) continue;
         const U4 u = rng_draw(seed, idi, 0u, step, RNG_COIN1, (uint32_t)r);
         if (coin_bits(u) < R.coin_threshold) emit(priority_key(u, R, handler), i, i, r);
     }
-    if (!in_cells || !tab->o2_any[ti]) return;
-    for_each_stencil_cell(p, g, radius, [&](int cell) {
-        const int jb = max(start[cell], i + 1), je = start[cell + 1];
-        for (int j = jb; j < je; ++j) {
+    if (!in_cells || !rt.o2_any[ti]) return;
+    const int *trow = rt.o2_tab + ti * rt.T;
+    int pj[PAIR_BATCH], pr[PAIR_BATCH];
+    int cnt = 0;
+    auto flush = [&]() {
+        for (int s = 0; s < cnt; ++s) {
+            const int j = pj[s], r = pr[s];
+            const ReactionDev &R = rt.rx[r];
+            const float4 q = pos[j];
+            const PairGeom g0 = pair_geom(p, q, g);
+            PairGeom gg = g0;
+            if (!within(g0, gg, p, q, g, R.educt_distance2f, R.band, R.educt_distance2)) continue;
+            const uint32_t idj = id[j];
+            const uint32_t lo = min(idi, idj), hi = max(idi, idj);
+            const U4 u = rng_draw(seed, lo, hi, step, RNG_COIN2, (uint32_t)r);
+            if (coin_bits(u) < R.coin_threshold) {
+                if (idi < idj) emit(priority_key(u, R, handler), i, j, r);
+                else emit(priority_key(u, R, handler), j, i, r);
+            }
+        }
+        cnt = 0;
+    };
+    for_each_neighbor_range(p, g, start, radius, [&](int jb0, int je) {
+        for (int j = max(jb0, i + 1); j < je; ++j) {
             const float4 q = pos[j];
             const int tj = itype(q);
             if (tj < 0) continue;
-            const int o2 = tab->o2_tab[ti * T + tj];
+            const int o2 = trow[tj];
             if (o2 == 0) continue;
             const PairGeom g0 = pair_geom(p, q, g);
-            const uint32_t idj = id[j];
-            const uint32_t lo = min(idi, idj), hi = max(idi, idj);
             for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
-                const int r = tab->o2_list[k];
-                const ReactionDev &R = tab->reactions[r];
-                if (!(R.rate > 0)) continue;
-                PairGeom gg = g0;
-                if (!within(g0, gg, p, q, g, R.educt_distance2f, R.band, R.educt_distance2)) continue;
-                const U4 u = rng_draw(seed, lo, hi, step, RNG_COIN2, (uint32_t)r);
-                if (coin_bits(u) < R.coin_threshold) {
-                    if (idi < idj) emit(priority_key(u, R, handler), i, j, r);
-                    else emit(priority_key(u, R, handler), j, i, r);
-                }
+                const int r = rt.o2_list[k];
+                const ReactionDev &R = rt.rx[r];
+                if (!R.active || g0.d2 > R.educt_distance2f + R.band) continue;
+                pj[cnt] = j;
+                pr[cnt] = r;
+                if (++cnt == PAIR_BATCH) flush();
             }
         }
     });
+    flush();
 }
 
 // ------------------------------------------------------------------------------------------------

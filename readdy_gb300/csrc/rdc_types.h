@@ -56,7 +56,8 @@ struct ReactionDev {
     float educt_distance2f, band;
     double educt_distance2;
     double rate;
-    float inv_rate;
+    float inv_rate;      // 1 / rate (0 when the rate is 0)
+    int active;          // rate > 0: the reaction takes part in event generation
     uint64_t coin_threshold;  // floor((1 - exp(-rate dt)) * 2^64), refreshed when dt changes
 };
 
