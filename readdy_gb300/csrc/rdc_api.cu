@@ -176,8 +176,12 @@ void build_tables(const ContextData &c, const double box[3], double dt, Tables &
         const int cnt = np - first;
         if (cnt > 255) throw InvalidArgument("too many potentials for one type pair");
         const int v = (first << 8) | cnt;
+        float scr = 0.f;
+        for (int k = first; k < np; ++k) scr = std::max(scr, t.pots[k].cutoff2f + 2.0f * t.pots[k].band);
         t.pair_tab[kv.first.first * T + kv.first.second] = v;
         t.pair_tab[kv.first.second * T + kv.first.first] = v;
+        t.pair_screen[kv.first.first * T + kv.first.second] = scr;
+        t.pair_screen[kv.first.second * T + kv.first.first] = scr;
     }
     t.npots = np;
     // reactions
@@ -216,6 +220,10 @@ void build_tables(const ContextData &c, const double box[3], double dt, Tables &
     k = 0;
     for (auto &kv : o2) {
         const int v = (k << 8) | (int)kv.second.size();
+        float scr = 0.f;
+        for (int r : kv.second) scr = std::max(scr, t.reactions[r].educt_distance2f + 2.0f * t.reactions[r].band);
+        t.rx_screen[kv.first.first * T + kv.first.second] = scr;
+        t.rx_screen[kv.first.second * T + kv.first.first] = scr;
         t.o2_tab[kv.first.first * T + kv.first.second] = v;
         t.o2_tab[kv.first.second * T + kv.first.first] = v;
         t.o2_any[kv.first.first] = 1;

@@ -175,6 +175,7 @@ __device__ inline void block_count_types(const float4 *pos, int n, int T, unsign
 
 struct SmemLayout {
     int *tab;
+    float *screen;
     float *drift, *scale;
     PairPot *pots;
     uint64_t *key;
@@ -236,7 +237,7 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, cons
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 p = posX[i];
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-        if (i < n_in && NP > 0) pair_force_at(i, p, posX, cells, g, 1, S.tab, S.pots, T, fx, fy, fz, e);
+        if (i < n_in && NP > 0) pair_force_at(i, p, posX, cells, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e);
         const uint32_t id = idX[i];
         const int t = itype(p);
         const float4 q = euler_bd(p, fx, fy, fz, id, D.seed, bd_step, S.drift[t], S.scale[t], g);
@@ -314,6 +315,8 @@ __global__ void __launch_bounds__(512, 1) k_batch_step(BatchDev B) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int sh_r;
     __shared__ int sh_rt_ints[MAX_TYPES + MAX_REACTIONS * 3 + MAX_TYPES * MAX_TYPES + MAX_TYPES];
+    __shared__ float sh_rt_scr[MAX_TYPES * MAX_TYPES];
+    __shared__ float sh_pair_scr[MAX_TYPES * MAX_TYPES];
     __shared__ ReactionDev sh_rx[MAX_REACTIONS];
     __shared__ float sh_drift[MAX_TYPES], sh_scale[MAX_TYPES];
     const Tables *tab = B.tab;
@@ -321,13 +324,17 @@ __global__ void __launch_bounds__(512, 1) k_batch_step(BatchDev B) {
     SmemLayout S = carve(smem, T, NP, B.max_events_sm);
     S.drift = sh_drift;
     S.scale = sh_scale;
-    for (int k = threadIdx.x; k < T * T; k += blockDim.x) S.tab[k] = tab->pair_tab[k];
+    S.screen = sh_pair_scr;
+    for (int k = threadIdx.x; k < T * T; k += blockDim.x) {
+        S.tab[k] = tab->pair_tab[k];
+        sh_pair_scr[k] = tab->pair_screen[k];
+    }
     for (int k = threadIdx.x; k < NP; k += blockDim.x) S.pots[k] = tab->pots[k];
     for (int k = threadIdx.x; k < T; k += blockDim.x) {
         sh_drift[k] = tab->bd_drift[k];
         sh_scale[k] = tab->bd_scale[k];
     }
-    const RxnTables rt = stage_rxn_tables(tab, sh_rt_ints, sh_rx);
+    const RxnTables rt = stage_rxn_tables(tab, sh_rt_ints, sh_rt_scr, sh_rx);
     const uint64_t bd_step = B.step[0], rx_step = B.step[1];
     __syncthreads();
     for (;;) {

@@ -98,7 +98,7 @@ __device__ inline float mi_diff(float rhs, float lhs, float L, float hL, int pbc
 // geometry held in registers by the hot loops (same member names as Geo; the box edges are FP32-exact,
 // so (double)L is the FP64 box of the reference)
 struct GeoR {
-    float L[3], hL[3], invW[3];
+    float L[3], hL[3], invW[3], invL[3];
     int dims[3];
     int pbc[3];
     int exact_always;
@@ -111,6 +111,7 @@ __device__ inline GeoR geo_r(const Geo &g) {
         r.L[d] = g.L[d];
         r.hL[d] = g.hL[d];
         r.invW[d] = g.invW[d];
+        r.invL[d] = 1.0f / g.L[d];
         r.dims[d] = g.dims[d];
         r.pbc[d] = g.pbc[d];
     }
@@ -220,6 +221,18 @@ __device__ inline float diff_prod(float a, float b, float c, float d) {
     const float e = __fmaf_rn(c, d, -w);
     const float f = __fmaf_rn(a, b, -w);
     return __fsub_rn(f, e);
+}
+
+// Screening distance: a branch-free minimum image (d - L rint(d / L) on periodic axes) and its squared
+// norm.  It differs from the reference-order difference by a few ulp of the box, which the screening
+// radius covers; a candidate that passes is re-evaluated exactly.
+template <typename G>
+__device__ inline float screen_d2(float4 lhs, float4 rhs, const G &g) {
+    float dx = rhs.x - lhs.x, dy = rhs.y - lhs.y, dz = rhs.z - lhs.z;
+    if (g.pbc[0]) dx = fmaf(-g.L[0], rintf(dx * g.invL[0]), dx);
+    if (g.pbc[1]) dy = fmaf(-g.L[1], rintf(dy * g.invL[1]), dy);
+    if (g.pbc[2]) dz = fmaf(-g.L[2], rintf(dz * g.invL[2]), dz);
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
 // Minimum-image difference rhs - lhs in FP32 and its squared norm.

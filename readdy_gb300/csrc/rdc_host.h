@@ -65,6 +65,8 @@ struct Tables {
     float bd_drift[MAX_TYPES];  // D dt / kBT
     float bd_scale[MAX_TYPES];  // sqrt(2 D dt)
     int pair_tab[MAX_TYPES * MAX_TYPES];  // (first << 8) | count into pots, 0 = none
+    float pair_screen[MAX_TYPES * MAX_TYPES];  // largest cutoff^2 + band of the pair's potentials (screening)
+    float rx_screen[MAX_TYPES * MAX_TYPES];    // largest educt distance^2 + band of the pair's reactions
     PairPot pots[MAX_PAIR_POTENTIALS];
     ReactionDev reactions[MAX_REACTIONS];
     int o1_tab[MAX_TYPES];                 // (first << 8) | count into o1_list

@@ -166,10 +166,14 @@ __global__ void k_gather(SysDev s, int permute_force) {
 // ------------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(FORCE_THREADS, 2) k_pair_forces(SysDev s) {
     __shared__ int sh_tab[MAX_TYPES * MAX_TYPES];
+    __shared__ float sh_scr[MAX_TYPES * MAX_TYPES];
     __shared__ PairPot sh_pots[MAX_PAIR_POTENTIALS];
     const Tables *tab = s.tab;
     const int T = tab->ntypes, NP = tab->npots;
-    for (int k = threadIdx.x; k < T * T; k += blockDim.x) sh_tab[k] = tab->pair_tab[k];
+    for (int k = threadIdx.x; k < T * T; k += blockDim.x) {
+        sh_tab[k] = tab->pair_tab[k];
+        sh_scr[k] = tab->pair_screen[k];
+    }
     for (int k = threadIdx.x; k < NP; k += blockDim.x) sh_pots[k] = tab->pots[k];
     __syncthreads();
     const int n = s.counters[C_N], n_in = s.counters[C_N_INCELLS];
@@ -178,7 +182,7 @@ __global__ void __launch_bounds__(FORCE_THREADS, 2) k_pair_forces(SysDev s) {
     GRID_STRIDE(i, n) {
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
         if (i < n_in && NP > 0)
-            pair_force_at(i, s.pos[i], s.pos, s.start, g, s.radius, sh_tab, sh_pots, T, fx, fy, fz, e);
+            pair_force_at(i, s.pos[i], s.pos, s.start, g, s.radius, sh_tab, sh_scr, sh_pots, T, fx, fy, fz, e);
         s.force[i] = make_float4(fx, fy, fz, e);
         esum += (double)e;
     }
@@ -242,8 +246,9 @@ __global__ void k_energy_final(SysDev s, int pair, int bonded) {
 // ------------------------------------------------------------------------------------------------
 __global__ void k_events(SysDev s, int handler) {
     __shared__ int sh_rt_ints[MAX_TYPES + MAX_REACTIONS * 3 + MAX_TYPES * MAX_TYPES + MAX_TYPES];
+    __shared__ float sh_rt_scr[MAX_TYPES * MAX_TYPES];
     __shared__ ReactionDev sh_rx[MAX_REACTIONS];
-    const RxnTables rt = stage_rxn_tables(s.tab, sh_rt_ints, sh_rx);
+    const RxnTables rt = stage_rxn_tables(s.tab, sh_rt_ints, sh_rt_scr, sh_rx);
     __syncthreads();
     const GeoR g = geo_r(s.geo);
     const int n = s.counters[C_N], n_in = s.counters[C_N_INCELLS];
@@ -348,16 +353,14 @@ __global__ void k_pairs(SysDev s, float c2f, float band, double c2, uint64_t *ou
     GRID_STRIDE(i, n_in) {
         const float4 p = s.pos[i];
         const uint32_t idi = s.id[i];
-        for_each_neighbor_range(p, g, s.start, s.radius, [&](int jb0, int je) {
-            for (int j = max(jb0, i + 1); j < je; ++j) {
-                const float4 q = s.pos[j];
-                const PairGeom g0 = pair_geom(p, q, g);
-                PairGeom gg = g0;
-                if (!within(g0, gg, p, q, g, c2f, band, c2)) continue;
-                const uint32_t idj = s.id[j];
-                const int k = atomicAdd(n_out, 1);
-                if (k < cap) out[k] = ((uint64_t)min(idi, idj) << 32) | max(idi, idj);
-            }
+        for_each_candidate(p, g, s.start, s.radius, i + 1, [&](int j) {
+            const float4 q = s.pos[j];
+            const PairGeom g0 = pair_geom(p, q, g);
+            PairGeom gg = g0;
+            if (!within(g0, gg, p, q, g, c2f, band, c2)) return;
+            const uint32_t idj = s.id[j];
+            const int k = atomicAdd(n_out, 1);
+            if (k < cap) out[k] = ((uint64_t)min(idi, idj) << 32) | max(idi, idj);
         });
     }
 }

@@ -60,14 +60,19 @@ __device__ inline void block_rank_sort(int *a, int *tmp, int b, int e) {
 // cell, cells in x-major, z-fastest order.  For r = 1 on grids of at least 3 cells along each periodic
 // axis the three z-cells of a column are contiguous in storage and are visited as one range (two if
 // the column wraps); other grids take the general per-cell path.
+template <typename G>
+__device__ inline bool stencil_fast(const G &g, int radius) {
+    return radius == 1 && (!g.pbc[0] || g.dims[0] >= 3) && (!g.pbc[1] || g.dims[1] >= 3) &&
+           (!g.pbc[2] || g.dims[2] >= 3);
+}
+
 template <typename G, typename F>
 __device__ inline void for_each_neighbor_range(float4 p, const G &g, const int *__restrict__ start, int radius,
                                                F f) {
     int cx, cy, cz;
     cell_coords(p, g, cx, cy, cz);
     const int dx0 = g.dims[0], dy0 = g.dims[1], dz0 = g.dims[2];
-    const bool fast = radius == 1 && (!g.pbc[0] || dx0 >= 3) && (!g.pbc[1] || dy0 >= 3) && (!g.pbc[2] || dz0 >= 3);
-    if (fast) {
+    if (stencil_fast(g, radius)) {
 #pragma unroll 1
         for (int ox = -1; ox <= 1; ++ox) {
             int x = cx + ox;
@@ -117,6 +122,42 @@ __device__ inline void for_each_neighbor_range(float4 p, const G &g, const int *
             }
 }
 
+// Calls f(j) for every candidate j >= jmin of the stencil, in the order of for_each_neighbor_range.
+// The ranges are gathered first and then walked as one flat sequence, so the lanes of a warp run the
+// candidate body together until each has exhausted its own candidates (short per-cell loops would cost
+// every range the longest lane's length).
+constexpr int MAX_RANGES = 18;
+
+template <typename G, typename F>
+__device__ inline void for_each_candidate(float4 p, const G &g, const int *__restrict__ start, int radius, int jmin,
+                                          F f) {
+    if (!stencil_fast(g, radius)) {
+        for_each_neighbor_range(p, g, start, radius, [&](int jb, int je) {
+            for (int j = max(jb, jmin); j < je; ++j) f(j);
+        });
+        return;
+    }
+    int rb[MAX_RANGES], re[MAX_RANGES];
+    int nr = 0;
+    for_each_neighbor_range(p, g, start, radius, [&](int jb, int je) {
+        jb = max(jb, jmin);
+        if (jb < je) {
+            rb[nr] = jb;
+            re[nr] = je;
+            ++nr;
+        }
+    });
+    int r = 0;
+    int j = nr > 0 ? rb[0] : 0, je = nr > 0 ? re[0] : 0;
+    while (r < nr) {
+        f(j);
+        if (++j == je && ++r < nr) {
+            j = rb[r];
+            je = re[r];
+        }
+    }
+}
+
 // exclusive scan of one value per thread across the block; total receives the block sum
 __device__ inline int block_exclusive_scan(int v, int &total) {
     __shared__ int warp_sums[32];
@@ -164,31 +205,28 @@ __device__ inline double block_sum_double(double v) {
 // neighbour of the stencil; the full both-direction iteration of CPUCalculateForces.cpp:214-268.
 template <typename G>
 __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const int *__restrict__ start,
-                                     const G &g, int radius, const int *tab, const PairPot *pots, int T, float &fx,
-                                     float &fy, float &fz, float &e) {
+                                     const G &g, int radius, const int *tab, const float *screen, const PairPot *pots,
+                                     int T, float &fx, float &fy, float &fz, float &e) {
     const int ti = itype(p);
     const int *trow = tab + ti * T;
-    for_each_neighbor_range(p, g, start, radius, [&](int jb, int je) {
-        for (int j = jb; j < je; ++j) {
-            if (j == i) continue;
-            const float4 q = pos[j];
-            const int tj = itype(q);
-            if (tj < 0) continue;
-            const int pt = trow[tj];
-            if (pt == 0) continue;
-            const PairGeom g0 = pair_geom(p, q, g);
-            const int first = pt >> 8, cnt = pt & 0xff;
-            for (int k = first; k < first + cnt; ++k) {
-                const PairPot &pp = pots[k];
-                PairGeom gg = g0;
-                if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, p, q, g, fx, fy, fz, e);
-            }
+    const float *srow = screen + ti * T;
+    for_each_candidate(p, g, start, radius, 0, [&](int j) {
+        if (j == i) return;
+        const float4 q = pos[j];
+        const int tj = itype(q);
+        if (tj < 0) return;
+        const int pt = trow[tj];
+        if (pt == 0) return;
+        if (screen_d2(p, q, g) > srow[tj]) return;
+        const PairGeom g0 = pair_geom(p, q, g);
+        const int first = pt >> 8, cnt = pt & 0xff;
+        for (int k = first; k < first + cnt; ++k) {
+            const PairPot &pp = pots[k];
+            PairGeom gg = g0;
+            if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, p, q, g, fx, fy, fz, e);
         }
     });
 }
-
-// pairs near enough to react are collected during the event scan and their coins drawn afterwards
-constexpr int PAIR_BATCH = 8;
 
 // Euler-Maruyama update of one particle (CPUEulerBDIntegrator.cpp:66-73), FP32, Philox noise
 // keyed by (seed, particle id, integrator step)
@@ -224,26 +262,28 @@ __device__ inline uint64_t priority_key(U4 r, const ReactionDev &R, int handler)
 // the reaction lookup tables of Tables, staged in shared memory by the kernels that generate events
 struct RxnTables {
     const int *o1_tab, *o1_list, *o2_tab, *o2_list, *o2_any;
+    const float *screen;
     const ReactionDev *rx;
     int T;
 };
 
-__device__ inline int rxn_tables_words(int T, int NR) { return T + NR + T * T + 2 * NR + T; }
-
-// all threads of the block copy the reaction tables into smem (words ints, then NR ReactionDev)
-__device__ inline RxnTables stage_rxn_tables(const Tables *tab, int *smem_ints, ReactionDev *smem_rx) {
+// all threads of the block copy the reaction tables into smem (ints, T*T screening floats, reactions)
+__device__ inline RxnTables stage_rxn_tables(const Tables *tab, int *smem_ints, float *smem_screen,
+                                             ReactionDev *smem_rx) {
     const int T = tab->ntypes, NR = tab->nreactions;
     int *o1t = smem_ints, *o1l = o1t + T, *o2t = o1l + NR, *o2l = o2t + T * T, *o2a = o2l + 2 * NR;
     for (int k = threadIdx.x; k < T; k += blockDim.x) { o1t[k] = tab->o1_tab[k]; o2a[k] = tab->o2_any[k]; }
     for (int k = threadIdx.x; k < NR; k += blockDim.x) { o1l[k] = tab->o1_list[k]; smem_rx[k] = tab->reactions[k]; }
     for (int k = threadIdx.x; k < 2 * NR; k += blockDim.x) o2l[k] = tab->o2_list[k];
-    for (int k = threadIdx.x; k < T * T; k += blockDim.x) o2t[k] = tab->o2_tab[k];
-    return RxnTables{o1t, o1l, o2t, o2l, o2a, smem_rx, T};
+    for (int k = threadIdx.x; k < T * T; k += blockDim.x) {
+        o2t[k] = tab->o2_tab[k];
+        smem_screen[k] = tab->rx_screen[k];
+    }
+    return RxnTables{o1t, o1l, o2t, o2l, o2a, smem_screen, smem_rx, T};
 }
 
 // order-1 events of particle i and order-2 events of the pairs (i, j > i); emit(key, p1, p2, r)
-// with p1 the particle of smaller id.  As for the forces, pairs near enough to react are collected
-// during the scan and their acceptance coins drawn afterwards.
+// with p1 the particle of smaller id
 template <typename G, typename Emit>
 __device__ inline void events_at(int i, bool in_cells, const float4 *__restrict__ pos, const uint32_t *__restrict__ id,
                                  const int *__restrict__ start, const G &g, int radius, const RxnTables &rt,
@@ -262,14 +302,17 @@ __device__ inline void events_at(int i, bool in_cells, const float4 *__restrict_
     }
     if (!in_cells || !rt.o2_any[ti]) return;
     const int *trow = rt.o2_tab + ti * rt.T;
-    int pj[PAIR_BATCH], pr[PAIR_BATCH];
-    int cnt = 0;
-    auto flush = [&]() {
-        for (int s = 0; s < cnt; ++s) {
-            const int j = pj[s], r = pr[s];
+    for_each_candidate(p, g, start, radius, i + 1, [&](int j) {
+        const float4 q = pos[j];
+        const int tj = itype(q);
+        if (tj < 0) return;
+        const int o2 = trow[tj];
+        if (o2 == 0) return;
+        const PairGeom g0 = pair_geom(p, q, g);
+        for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
+            const int r = rt.o2_list[k];
             const ReactionDev &R = rt.rx[r];
-            const float4 q = pos[j];
-            const PairGeom g0 = pair_geom(p, q, g);
+            if (!R.active) continue;
             PairGeom gg = g0;
             if (!within(g0, gg, p, q, g, R.educt_distance2f, R.band, R.educt_distance2)) continue;
             const uint32_t idj = id[j];
@@ -280,27 +323,7 @@ __device__ inline void events_at(int i, bool in_cells, const float4 *__restrict_
                 else emit(priority_key(u, R, handler), j, i, r);
             }
         }
-        cnt = 0;
-    };
-    for_each_neighbor_range(p, g, start, radius, [&](int jb0, int je) {
-        for (int j = max(jb0, i + 1); j < je; ++j) {
-            const float4 q = pos[j];
-            const int tj = itype(q);
-            if (tj < 0) continue;
-            const int o2 = trow[tj];
-            if (o2 == 0) continue;
-            const PairGeom g0 = pair_geom(p, q, g);
-            for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
-                const int r = rt.o2_list[k];
-                const ReactionDev &R = rt.rx[r];
-                if (!R.active || g0.d2 > R.educt_distance2f + R.band) continue;
-                pj[cnt] = j;
-                pr[cnt] = r;
-                if (++cnt == PAIR_BATCH) flush();
-            }
-        }
     });
-    flush();
 }
 
 // ------------------------------------------------------------------------------------------------
