@@ -1,0 +1,390 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched uneven ensemble on one GB300.
+
+Workload (the batched-replica configuration of the ReaDDy hot path): 4096 independent replicas of the
+A + B <-> C chemistry (fusion A + B -> C, rate 1, educt distance 1; fission C -> A + B, rate 0.1,
+product distance 1; harmonic repulsion k = 10, distance 1 between all species; D = 1, 1, 0.5;
+kBT = 1).  Replica particle counts are log-uniform in [200, 20000] from a seed, half A and half B,
+placed uniformly in a periodic cubic box whose edge holds the number density at 0.25.  Gillespie
+handler, dt = 1e-3.  Inputs are synthetic and seeded.
+
+Metric: particle-steps/s (particles advanced per step, summed over replicas and steps, over the device
+time of the timed steps).  Every step is one persistent fused launch over all replicas replayed from
+a CUDA graph.  The same replicas advanced one at a time through the per-system GPU path are timed on
+a random sample and reported beside it, as is the FP64 CPU restatement of the reference kernel on the
+host cores (a bounded sample).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s batched vs one-at-a-time on GB300; p50/p99 solve latency"
+UNIT = "particle-steps/s"
+DENSITY = 0.25
+N_MIN, N_MAX = 200, 20000
+# DRAM bytes per particle of one fused step (dram__bytes_read.sum + dram__bytes_write.sum of one ncu
+# capture of k_batch_step on a smaller ensemble, divided by its particles); None until captured.
+DRAM_BYTES_PER_PARTICLE = None
+# algorithmic bytes of one fused step per particle: the particle state (float4 position with the type,
+# uint32 id) read once and written once
+ALG_BYTES_PER_PARTICLE = 2 * (16 + 4)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--replicas", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def ensemble(seed: int, n_replicas: int):
+    """Particle counts, boxes, positions and types of the uneven ensemble."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(N_MIN), np.log(N_MAX), n_replicas)).astype(np.int64)
+    boxes, pos, types = [], [], []
+    for n in ns:
+        L = float(np.float32((n / DENSITY) ** (1.0 / 3.0)))
+        boxes.append((L, L, L))
+        pos.append((rng.random((n, 3)) - 0.5) * L)
+        t = np.zeros(n, np.int32)
+        t[n // 2:] = 1
+        types.append(t)
+    return ns, np.array(boxes), pos, types
+
+
+def chemistry(box=(10.0, 10.0, 10.0)):
+    import readdy_gb300 as rg
+    ctx = rg.Context(box, (True, True, True), 1.0, (1.0, 1.0, 0.5))
+    for a in range(3):
+        for b in range(a, 3):
+            ctx.add_harmonic_repulsion(a, b, 10.0, 1.0)
+    ctx.add_fusion(0, 1, 2, 1.0, 1.0)
+    ctx.add_fission(2, 0, 1, 0.1, 1.0)
+    return ctx
+
+
+def oracle_system(box, pos, types, seed, n_threads):
+    import oracle
+    o = oracle.OracleSystem(box, (True, True, True), 1.0, (1.0, 1.0, 0.5), seed=seed, n_threads=n_threads)
+    for a in range(3):
+        for b in range(a, 3):
+            o.add_harmonic_repulsion(a, b, 10.0, 1.0)
+    o.add_fusion(0, 1, 2, 1.0, 1.0)
+    o.add_fission(2, 0, 1, 0.1, 1.0)
+    o.add_particles(pos, types)
+    return o
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.path = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(ns, boxes, pos, types, seed, budget_s, rng_pick):
+    """FP64 restatement of the reference CPU kernel (Gillespie, SimulationLoop step order) timed on a
+    random sample of replicas with all host threads, until the time budget is spent."""
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    order = rng_pick.permutation(len(ns))
+    done_ps, spent, reps, steps = 0, 0.0, 0, 5
+    for r in order:
+        o = oracle_system(tuple(boxes[r]), pos[r], types[r], seed + int(r), cores)
+        t0 = time.perf_counter()
+        o.run(steps, 1e-3, handler=oracle.GILLESPIE)
+        spent += time.perf_counter() - t0
+        done_ps += int(ns[r]) * steps
+        reps += 1
+        if spent > budget_s:
+            break
+    return {"value": done_ps / spent, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{reps} random replicas of the ensemble x {steps} steps each (FP64 oracle, Gillespie), "
+                      f"{done_ps} particle-steps in {spent:.1f} s"}
+
+
+def one_at_a_time(ns, boxes, pos, types, seed, n_sample, steps, rng_pick):
+    """The same replicas through the per-system GPU path (rdc_run, graph-replayed), one after another,
+    on a random sample of the ensemble."""
+    import readdy_gb300 as rg
+    from readdy_gb300.batch import replica_seed
+    pick = rng_pick.choice(len(ns), size=min(n_sample, len(ns)), replace=False)
+    total_ps, total_t = 0, 0.0
+    for r in pick:
+        ctx = chemistry(tuple(boxes[r]))
+        k = rg.CUDAKernel(ctx, seed=replica_seed(seed, int(r)))
+        k.add_particles(pos[r], types[r])
+        k.run(2, 1e-3, handler=rg.GILLESPIE)
+        t0 = time.perf_counter()
+        k.run(steps, 1e-3, handler=rg.GILLESPIE)
+        total_t += time.perf_counter() - t0
+        total_ps += int(ns[r]) * steps
+    return {"value": total_ps / total_t, "unit": UNIT, "sample": f"{len(pick)} random replicas x {steps} steps, "
+            "each through the per-system path (CUDA-graph replay of the SimulationLoop step), run sequentially"}
+
+
+def run_gb300(args, rank, world):
+    import readdy_gb300 as rg
+    from readdy_gb300.batch import ReplicaBatch
+    rg.load()
+    seed = args.seed + 1000003 * rank
+    ns, boxes, pos, types = ensemble(seed, args.replicas)
+    caps = ns + 64
+    ctx = chemistry()
+    b = ReplicaBatch(ctx, boxes, caps, seed=seed)
+    b.set_particles(pos, types)
+    b.configure(handler=rg.GILLESPIE, dt=1e-3, cell_width_scale=1.0, threads_per_block=512)
+    b.step(args.warmup)
+    b.synchronize()
+    barrier(world)
+    ps0 = b.particle_steps()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        ms = b.step_timed(args.steps)
+    b.synchronize()
+    ps1 = b.particle_steps()
+    ms_max = allreduce_max(ms, world)
+    ps_sum = allreduce_sum(ps1 - ps0, world)
+    value = ps_sum / (ms_max / 1e3)
+
+    # end to end through the public API: host arrays in, counts out
+    t0 = time.perf_counter()
+    e = ReplicaBatch(ctx, boxes, caps, seed=seed + 7)
+    e.set_particles(pos, types)
+    e.configure(handler=rg.GILLESPIE, dt=1e-3, cell_width_scale=1.0, threads_per_block=512)
+    e.step(args.steps)
+    counts = e.count_types()
+    e2e_t = time.perf_counter() - t0
+    e2e_ps = e.particle_steps()
+    del e
+    # float4 particles, replica descriptors (136 B) and states (24 B), LPT order (4 B)
+    h2d = int(sum(len(p) for p in pos) * 16 + len(ns) * (136 + 24 + 4))
+    d2h = int(counts.nbytes)
+
+    result = None
+    if rank == 0:
+        pick = np.random.default_rng(args.seed + 99)
+        oat = one_at_a_time(ns, boxes, pos, types, seed, 64, 50, pick)
+        cpu = cpu_baseline(ns, boxes, pos, types, seed, args.cpu_seconds, np.random.default_rng(args.seed + 5))
+        peak, peak_kind = measured_peaks()
+        n_avg = (ps1 - ps0) / args.steps
+        launch_ms = ms / args.steps
+        achieved = ALG_BYTES_PER_PARTICLE * n_avg / (launch_ms / 1e3) / 1e9
+        result = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded uneven ensemble)",
+            "config": {
+                "workload": "batched uneven ensemble: 4096 replicas of A+B<->C, N log-uniform in [200, 20000], "
+                            "density 0.25, HR k=10 d=1, Gillespie, dt=1e-3",
+                "replicas": int(args.replicas), "particles": int(ns.sum()),
+                "launch": "one persistent fused launch per step (k_batch_step), CUDA graph",
+                "cell_width_scale": 1.0, "threads_per_block": 512,
+                "l2": "inputs larger than L2 (particle state %.0f MB > 129 MB)" % (ns.sum() * 40 / 1e6),
+                "parallelism": f"replicas only, {world} rank(s), one ensemble per GPU",
+            },
+            "one_at_a_time": oat,
+            "batched_over_one_at_a_time": value / world / oat["value"],
+            "e2e": {"value": e2e_ps / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d // max(args.steps, 1),
+                    "d2h_bytes_per_step": d2h // max(args.steps, 1),
+                    "timed": "ReplicaBatch create + set_particles (host arrays) + configure + steps + count_types"},
+            "roofline": {"bound": "hbm", "kernel": "k_batch_step", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": ALG_BYTES_PER_PARTICLE * n_avg,
+                         "traffic": DRAM_BYTES_PER_PARTICLE * n_avg if DRAM_BYTES_PER_PARTICLE else None,
+                         "traffic_source": "ncu capture of a smaller ensemble scaled by particles"},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": 2 * args.steps,
+        }
+    return result
+
+
+def run_reference(args):
+    """The reference path on the host cores: the FP64 CPU restatement (no compiled reference build
+    travels with the benchmark), all host threads, each step a bounded sample of the ensemble."""
+    import oracle
+    oracle.build()
+    ns, boxes, pos, types = ensemble(args.seed, args.replicas)
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(args.seed + 5)
+    sample = rng.choice(len(ns), size=min(8, len(ns)), replace=False)
+    systems = [oracle_system(tuple(boxes[r]), pos[r], types[r], args.seed + int(r), cores) for r in sample]
+    for o in systems:
+        o.nl_setup(o.calculate_max_cutoff())
+        o.calculate_forces()
+
+    def one_step(o):
+        o.euler_bd(1e-3)
+        o.nl_update()
+        o.gillespie(1e-3)
+        o.nl_update()
+        o.calculate_forces()
+
+    for _ in range(args.warmup):
+        for o in systems:
+            one_step(o)
+    t0 = time.perf_counter()
+    ps = 0
+    for _ in range(args.steps):
+        for o in systems:
+            ps += o.n_particles
+            one_step(o)
+    t = time.perf_counter() - t0
+    v = ps / t
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded uneven ensemble)", "impl": "reference",
+            "config": {"workload": "batched uneven ensemble: 4096 replicas of A+B<->C, N log-uniform in [200, 20000], "
+                                   "density 0.25, HR k=10 d=1, Gillespie, dt=1e-3",
+                       "sample": f"{len(sample)} random replicas per step"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{len(sample)} random replicas of the ensemble per step, FP64 restatement of "
+                                       "the reference CPU kernel (SimulationLoop order, Gillespie)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---- minimal distributed helpers (torch.distributed only when launched with several ranks) ----
+_dist = None
+
+
+def init_dist():
+    global _dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+        _dist = dist
+    return rank, world
+
+
+def barrier(world):
+    if world > 1 and _dist is not None:
+        _dist.barrier()
+
+
+def _allreduce(v, world, op):
+    if world <= 1 or _dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], device="cuda")
+    _dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+def allreduce_max(v, world):
+    return _allreduce(v, world, _dist.ReduceOp.MAX if _dist else None)
+
+
+def allreduce_sum(v, world):
+    return _allreduce(v, world, _dist.ReduceOp.SUM if _dist else None)
+
+
+def main():
+    args = parse()
+    rank, world = init_dist()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
+    res = run_gb300(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1 and _dist is not None:
+        _dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -165,6 +165,10 @@ int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *
 int rdc_batch_configure(rdc_batch *b, int handler, double dt, double cell_width_scale, int threads_per_block);
 /* advance every replica n_steps; each step is one fused launch replayed from a CUDA graph */
 int rdc_batch_step(rdc_batch *b, int64_t n_steps);
+/* rdc_batch_step bracketed by CUDA events on the batch's stream; *device_ms receives the device time */
+int rdc_batch_step_timed(rdc_batch *b, int64_t n_steps, double *device_ms);
+/* particles advanced so far, summed over replicas and steps (the particle-steps of the throughput metric) */
+int rdc_batch_particle_steps(rdc_batch *b, uint64_t *particle_steps);
 /* per-replica, per-type counts (n_replicas * n_types) */
 int rdc_batch_count_types(rdc_batch *b, int64_t *counts);
 /* active particles per replica */

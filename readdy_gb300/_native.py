@@ -83,6 +83,8 @@ def _sig(lib):
         "rdc_batch_set_particles": (i, [vp, P(i64), P(d), P(i)]),
         "rdc_batch_configure": (i, [vp, i, d, d, i]),
         "rdc_batch_step": (i, [vp, i64]),
+        "rdc_batch_step_timed": (i, [vp, i64, P(d)]),
+        "rdc_batch_particle_steps": (i, [vp, P(u64)]),
         "rdc_batch_count_types": (i, [vp, P(i64)]),
         "rdc_batch_n_particles": (i, [vp, P(i64)]),
         "rdc_batch_get_particles": (i, [vp, i, i64, P(d), P(i), P(u64), P(i64)]),

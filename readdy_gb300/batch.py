@@ -71,6 +71,17 @@ class ReplicaBatch:
     def step(self, n_steps=1):
         N.check(self._lib.rdc_batch_step(self._h, int(n_steps)))
 
+    def step_timed(self, n_steps=1):
+        """Advances n_steps and returns the device time in ms (CUDA events on the batch's stream)."""
+        ms = C.c_double()
+        N.check(self._lib.rdc_batch_step_timed(self._h, int(n_steps), C.byref(ms)))
+        return ms.value
+
+    def particle_steps(self):
+        v = C.c_uint64()
+        N.check(self._lib.rdc_batch_particle_steps(self._h, C.byref(v)))
+        return int(v.value)
+
     def synchronize(self):
         N.check(self._lib.rdc_batch_synchronize(self._h))
 

@@ -62,6 +62,7 @@ struct BatchDev {
     int count_stride;
     int max_events_sm;
     unsigned long long *reaction_counts;
+    unsigned long long *particle_steps;  // sum over replicas and steps of the particles advanced
 };
 
 __device__ inline void block_zero(int *a, int n) {
@@ -299,6 +300,7 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, cons
         block_count_types(pf, n_final, T, B.counts + (size_t)r * T);
     }
     if (threadIdx.x == 0) {
+        atomicAdd(B.particle_steps, (unsigned long long)n);
         RepState o;
         o.n = n_final;
         o.n_in = nin_final;
@@ -460,6 +462,7 @@ struct rdc_batch {
     size_t smem = 0;
     cudaGraphExec_t graph = nullptr;
     unsigned long long *count_dev = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
     ~rdc_batch() { release(); }
 
@@ -470,7 +473,9 @@ struct rdc_batch {
         bfree(d.posA); bfree(d.posB); bfree(d.idA); bfree(d.idB);
         bfree(d.bin); bfree(d.rank); bfree(d.src); bfree(d.claim); bfree(d.taken);
         bfree(d.start); bfree(d.events); bfree(d.work); bfree(d.step); bfree(d.counts);
-        bfree(d.reaction_counts);
+        bfree(d.reaction_counts); bfree(d.particle_steps);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -551,6 +556,10 @@ struct rdc_batch {
         count_dev = balloc<unsigned long long>((size_t)R * ctx.ntypes);
         d.reaction_counts = balloc<unsigned long long>(MAX_REACTIONS);
         RDC_CUDA(cudaMemsetAsync(d.reaction_counts, 0, sizeof(unsigned long long) * MAX_REACTIONS, stream));
+        d.particle_steps = balloc<unsigned long long>(1);
+        RDC_CUDA(cudaMemsetAsync(d.particle_steps, 0, sizeof(unsigned long long), stream));
+        RDC_CUDA(cudaEventCreate(&ev0));
+        RDC_CUDA(cudaEventCreate(&ev1));
         state_dev = balloc<RepState>(R);
         RDC_CUDA(cudaMemsetAsync(state_dev, 0, sizeof(RepState) * R, stream));
         d.state = state_dev;
@@ -761,6 +770,30 @@ int rdc_batch_step(rdc_batch *b, int64_t n_steps) {
         if (!b) throw std::invalid_argument("null argument");
         if (n_steps < 0) throw std::invalid_argument("n_steps must be >= 0");
         b->step(n_steps);
+    });
+}
+
+int rdc_batch_step_timed(rdc_batch *b, int64_t n_steps, double *device_ms) {
+    BATCH_CALL({
+        if (!b || !device_ms) throw std::invalid_argument("null argument");
+        if (n_steps < 0) throw std::invalid_argument("n_steps must be >= 0");
+        RDC_CUDA(cudaEventRecord(b->ev0, b->stream));
+        b->step(n_steps);
+        RDC_CUDA(cudaEventRecord(b->ev1, b->stream));
+        RDC_CUDA(cudaEventSynchronize(b->ev1));
+        float ms = 0.f;
+        RDC_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        *device_ms = ms;
+    });
+}
+
+int rdc_batch_particle_steps(rdc_batch *b, uint64_t *particle_steps) {
+    BATCH_CALL({
+        if (!b || !particle_steps) throw std::invalid_argument("null argument");
+        unsigned long long v = 0;
+        RDC_CUDA(cudaMemcpyAsync(&v, b->d.particle_steps, sizeof(v), cudaMemcpyDeviceToHost, b->stream));
+        b->sync();
+        *particle_steps = v;
     });
 }
 
