@@ -178,6 +178,29 @@ int rdc_batch_get_particles(rdc_batch *b, int replica, int64_t capacity, double 
                             uint64_t *ids, int64_t *n_out);
 int rdc_batch_synchronize(rdc_batch *b);
 
+/* ---- forces without device allocation (no counterpart in the reference) ----------------------
+ * For callers that cannot let the library allocate device memory where they need forces: code that
+ * records its step by CUDA stream capture (no cudaMalloc while a stream captures) and embeddings
+ * whose own pool owns all of the GPU's memory.  Pair forces and the pair energy of n particles held
+ * in the caller's device arrays -- positions3 (n*3 floats), types (n ints in [0, n_types)) -- are
+ * written to the caller's device arrays forces3 (n*3 floats) and *energy (one double), on `stream`
+ * (a cudaStream_t; NULL is the legacy default stream), asynchronously.  Same potentials, exact cutoff
+ * test and FP32 terms as rdc_calculate_forces; the neighbour summation order may differ.
+ *
+ * Working space is one static device array of RDC_NOALLOC_SCRATCH_BYTES per device, so at most
+ * RDC_NOALLOC_MAX_PARTICLES particles are accepted (more returns RDC_ERR_INVALID_ARGUMENT) and the
+ * cell grid is widened to at most RDC_NOALLOC_MAX_CELLS cells.  The first call on a device, and the
+ * first call after the context's potentials changed, finds the array and copies the potential tables
+ * into it, synchronising the stream; make that call before any stream capture (during capture it
+ * returns RDC_ERR_LOGIC).  All calls on one device share the array: calls that overlap (different
+ * streams or threads without ordering) race and give wrong results.  A type outside [0, n_types) gives that particle no force and makes
+ * *energy NaN. */
+#define RDC_NOALLOC_MAX_PARTICLES 65536
+#define RDC_NOALLOC_MAX_CELLS 131072
+#define RDC_NOALLOC_SCRATCH_BYTES 3181312
+int rdc_forces_noalloc(const rdc_context *ctx, int64_t n, const float *positions3, const int *types,
+                       float *forces3, double *energy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

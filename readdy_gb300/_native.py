@@ -89,6 +89,7 @@ def _sig(lib):
         "rdc_batch_n_particles": (i, [vp, P(i64)]),
         "rdc_batch_get_particles": (i, [vp, i, i64, P(d), P(i), P(u64), P(i64)]),
         "rdc_batch_synchronize": (i, [vp]),
+        "rdc_forces_noalloc": (i, [vp, i64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in table.items():
         f = getattr(lib, name)
