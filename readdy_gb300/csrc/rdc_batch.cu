@@ -27,15 +27,18 @@ using namespace rdc;
 
 namespace rdc {
 
-// cell starts of a replica whose grid has at most SMEM_CELLS - 3 cells live in shared memory
-constexpr int SMEM_CELLS = 16384;
+// Cell counts and starts of a replica of fewer than 65536 particles live in shared memory during its
+// step as uint16_t, SMEM_CELLS entries (96 KB): at cells of the cutoff's width and density 0.25 that
+// holds replicas of up to ~12k particles, and larger ones get proportionally wider cells.  Replicas of
+// more particles keep int starts in global memory at the natural cell width.
+constexpr int SMEM_CELLS = 49152;
 
 struct RepDesc {
     Geo geo;
     int poff, cap;     // particle slots [poff, poff + cap) in every per-particle array
     int soff;          // cell starts at start[soff .. soff + ncells + 3) between steps
     int eoff, ecap;    // event buffer
-    int smem_cells;    // 1: cell array in shared memory during the step
+    int smem_cells;    // 1: uint16_t cell array in shared memory during the step, 0: int in global
     int pad;
     uint64_t seed;
 };
@@ -65,18 +68,21 @@ struct BatchDev {
     unsigned long long *particle_steps;  // sum over replicas and steps of the particles advanced
 };
 
-__device__ inline void block_zero(int *a, int n) {
+template <typename T>
+__device__ inline void block_zero(T *a, int n) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) a[k] = 0;
     __syncthreads();
 }
 
-__device__ inline void block_copy(int *dst, const int *src, int n) {
-    for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+template <typename D, typename T>
+__device__ inline void block_copy(D *dst, const T *src, int n) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = (D)src[k];
     __syncthreads();
 }
 
 // in-place exclusive scan of a[0..n) by one block (shared or global memory); a[n] = total
-__device__ inline void block_scan_inplace(int *a, int n) {
+template <typename T>
+__device__ inline void block_scan_inplace(T *a, int n) {
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -95,14 +101,14 @@ __device__ inline void block_scan_inplace(int *a, int n) {
         int run = block_exclusive_scan(sum, total) + carry;
 #pragma unroll
         for (int k = 0; k < ITEMS; ++k) {
-            if (b + k < n) a[b + k] = run;
+            if (b + k < n) a[b + k] = (T)run;
             run += v[k];
         }
         __syncthreads();
         if (threadIdx.x == 0) carry += total;
         __syncthreads();
     }
-    if (threadIdx.x == 0) a[n] = carry;
+    if (threadIdx.x == 0) a[n] = (T)carry;
     __syncthreads();
 }
 
@@ -113,6 +119,19 @@ __device__ inline void block_rank(int n, const int *bin, int *rank, int *cells, 
     __syncthreads();
 }
 
+// 16-bit counters, two per 32-bit word (4-byte aligned array); a count never exceeds the replica's
+// particles (< 65536), so an increment never carries into the neighbouring counter
+__device__ inline void block_rank(int n, const int *bin, int *rank, uint16_t *cells, int nbins) {
+    block_zero(cells, nbins);
+    unsigned *w = reinterpret_cast<unsigned *>(cells);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int b = bin[i];
+        const unsigned sh = (unsigned)(b & 1) * 16u;
+        rank[i] = (int)((atomicAdd(&w[b >> 1], 1u << sh) >> sh) & 0xffffu);
+    }
+    __syncthreads();
+}
+
 __device__ inline void block_bin(const float4 *pos, int n, int *bin, const Geo &g) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) bin[i] = bin_of(pos[i], g);
     __syncthreads();
@@ -120,8 +139,9 @@ __device__ inline void block_bin(const float4 *pos, int n, int *bin, const Geo &
 
 // counting sort of one replica from counts in cells: scan to cell starts, scatter, order each cell
 // by source index (deterministic), gather into the destination arrays
+template <typename C>
 __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n, float4 *dpos, uint32_t *did,
-                                  const int *bin, const int *rank, int *src, int *cells, const Geo &g, int &n_new,
+                                  const int *bin, const int *rank, int *src, C *cells, const Geo &g, int &n_new,
                                   int &n_in) {
     const int nc = g.ncells;
     block_scan_inplace(cells, nc + 2);
@@ -181,7 +201,8 @@ struct SmemLayout {
     PairPot *pots;
     uint64_t *key;
     int *idx, *state;
-    int *cells;
+    TupleQueue queue;
+    uint16_t *cells;
 };
 
 __device__ inline SmemLayout carve(unsigned char *smem, int T, int NP, int max_events) {
@@ -197,28 +218,30 @@ __device__ inline SmemLayout carve(unsigned char *smem, int T, int NP, int max_e
     off += sizeof(int) * max_events;
     L.state = reinterpret_cast<int *>(smem + off);
     off += sizeof(int) * max_events;
-    L.cells = reinterpret_cast<int *>(smem + off);
+    L.queue.p1 = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * EVENT_QUEUE;
+    L.queue.p2 = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * EVENT_QUEUE;
+    L.queue.count = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * 4;
+    L.queue.r = smem + off;
+    off += EVENT_QUEUE;
+    L.cells = reinterpret_cast<uint16_t *>(smem + off);
     return L;
 }
 
 size_t batch_smem_bytes(int T, int NP, int max_events) {
     return sizeof(uint64_t) * max_events + sizeof(PairPot) * (NP > 0 ? NP : 1) + sizeof(int) * T * T +
-           2 * sizeof(int) * max_events + sizeof(int) * (SMEM_CELLS + 4) + 16;
+           2 * sizeof(int) * max_events + (2 * sizeof(int) + 1) * EVENT_QUEUE + 4 * sizeof(int) +
+           sizeof(uint16_t) * (SMEM_CELLS + 4) + 16;
 }
 
-// one step of one replica by the whole block
-__device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, const RxnTables &rt, uint64_t bd_step,
-                             uint64_t rx_step) {
-    __shared__ RepDesc D;
-    __shared__ RepState st;
-    __shared__ int sh_nev, sh_status;
-    if (threadIdx.x == 0) {
-        D = B.desc[r];
-        st = B.state[r];
-        sh_nev = 0;
-        sh_status = 0;
-    }
-    __syncthreads();
+// one step of one replica by the whole block; C is the cell array's type (uint16_t in shared memory
+// or int in global memory)
+template <typename C>
+__device__ void replica_body(const BatchDev &B, int r, const SmemLayout &S, const RxnTables &rt, uint64_t bd_step,
+                             uint64_t rx_step, const RepDesc &D, const RepState &st, int &sh_nev, int &sh_status,
+                             C *cells) {
     const Tables *tab = B.tab;
     const int T = tab->ntypes, NP = tab->npots;
     const Geo &gs = D.geo;
@@ -230,8 +253,8 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, cons
     uint32_t *idY = (st.cur ? B.idA : B.idB) + D.poff;
     int *bin = B.bin + D.poff, *rank = B.rank + D.poff, *src = B.src + D.poff;
     int *gstart = B.start + D.soff;
-    int *cells = D.smem_cells ? S.cells : gstart;
-    if (D.smem_cells) block_copy(cells, gstart, nc + 3);
+    constexpr bool in_smem = sizeof(C) == sizeof(uint16_t);
+    if (in_smem) block_copy(cells, gstart, nc + 3);
     const int n = st.n, n_in = st.n_in;
 
     // forces on the current state, Euler step into Y, bins of the new positions
@@ -265,9 +288,7 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, cons
                 atomicOr(&sh_status, ST_EVENTS);
             }
         };
-        for (int i = threadIdx.x; i < n1; i += blockDim.x)
-            events_at(i, i < nin1, posX, idX, cells, g, 1, rt, D.seed, rx_step, B.handler, emit);
-        __syncthreads();
+        block_events(0, blockDim.x, n1, nin1, posX, idX, cells, g, 1, rt, D.seed, rx_step, B.handler, S.queue, emit);
         const int E = min(sh_nev, ecap);
         if (E > 0) {
             ApplyTarget t;
@@ -294,7 +315,7 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, cons
             }
         }
     }
-    if (D.smem_cells) block_copy(gstart, cells, nc + 3);
+    if (in_smem) block_copy(gstart, cells, nc + 3);
     if (B.count_stride > 0 && (bd_step + 1) % (uint64_t)B.count_stride == 0) {
         const float4 *pf = (cur ? B.posB : B.posA) + D.poff;
         block_count_types(pf, n_final, T, B.counts + (size_t)r * T);
@@ -311,6 +332,22 @@ __device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, cons
         B.state[r] = o;
     }
     __syncthreads();
+}
+
+__device__ void replica_step(const BatchDev &B, int r, const SmemLayout &S, const RxnTables &rt, uint64_t bd_step,
+                             uint64_t rx_step) {
+    __shared__ RepDesc D;
+    __shared__ RepState st;
+    __shared__ int sh_nev, sh_status;
+    if (threadIdx.x == 0) {
+        D = B.desc[r];
+        st = B.state[r];
+        sh_nev = 0;
+        sh_status = 0;
+    }
+    __syncthreads();
+    if (D.smem_cells) replica_body(B, r, S, rt, bd_step, rx_step, D, st, sh_nev, sh_status, S.cells);
+    else replica_body(B, r, S, rt, bd_step, rx_step, D, st, sh_nev, sh_status, B.start + D.soff);
 }
 
 __global__ void __launch_bounds__(512, 1) k_batch_step(BatchDev B) {
@@ -497,11 +534,14 @@ struct rdc_batch {
             RepDesc &D = desc[r];
             double w = cutoff * cell_scale;
             D.geo = make_geo(&boxes[3 * r], ctx.pbc, cutoff, 1, w);
-            for (int k = 0; k < 64 && D.geo.ncells + 3 > SMEM_CELLS && cutoff > 0; ++k) {
-                w *= 1.05;
-                D.geo = make_geo(&boxes[3 * r], ctx.pbc, cutoff, 1, w);
-            }
-            D.smem_cells = D.geo.ncells + 3 <= SMEM_CELLS ? 1 : 0;
+            const bool small = caps[r] < 65536;  // cell starts fit 16 bits
+            if (small)
+                for (int k = 0; k < 64 && D.geo.ncells + 3 > SMEM_CELLS && cutoff > 0; ++k) {
+                    w *= 1.05;
+                    D.geo = make_geo(&boxes[3 * r], ctx.pbc, cutoff, 1, w);
+                }
+            D.smem_cells = (small && D.geo.ncells + 3 <= SMEM_CELLS) ? 1 : 0;
+            if (!D.smem_cells) D.geo = make_geo(&boxes[3 * r], ctx.pbc, cutoff, 1, cutoff * cell_scale);
             D.pad = 0;
             D.poff = (int)poff;
             D.cap = (int)caps[r];

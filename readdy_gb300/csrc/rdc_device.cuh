@@ -449,10 +449,27 @@ __device__ inline F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z -
 __device__ inline F3 operator*(float s, F3 a) { return {s * a.x, s * a.y, s * a.z}; }
 __device__ inline float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ inline F3 cross(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+// cross product with each component as a Kahan difference of products (error ~1 ulp of the result)
+__device__ inline F3 cross_k(F3 a, F3 b) {
+    return {diff_prod(a.y, b.z, a.z, b.y), diff_prod(a.z, b.x, a.x, b.z), diff_prod(a.x, b.y, a.y, b.x)};
+}
 
 __device__ inline F3 shortest3(float4 lhs, float4 rhs, const Geo &g) {
     return F3{mi_diff(rhs.x, lhs.x, g.L[0], g.hL[0], g.pbc[0]), mi_diff(rhs.y, lhs.y, g.L[1], g.hL[1], g.pbc[1]),
               mi_diff(rhs.z, lhs.z, g.L[2], g.hL[2], g.pbc[2])};
+}
+
+// the same difference as an unevaluated sum hi + lo (hi equals shortest3)
+__device__ inline void shortest3_ff(float4 lhs, float4 rhs, const Geo &g, F3 &hi, F3 &lo) {
+    mi_diff2(rhs.x, lhs.x, g.L[0], g.hL[0], g.pbc[0], hi.x, lo.x);
+    mi_diff2(rhs.y, lhs.y, g.L[1], g.hL[1], g.pbc[1], hi.y, lo.y);
+    mi_diff2(rhs.z, lhs.z, g.L[2], g.hL[2], g.pbc[2], hi.z, lo.z);
+}
+
+// (ah + al) x (bh + bl) to first order in the low parts: accurate to a few ulp of the result even
+// when the two vectors are nearly parallel and the result is much shorter than |a||b|
+__device__ inline F3 cross_ff(F3 ah, F3 al, F3 bh, F3 bl) {
+    return cross_k(ah, bh) + (cross(ah, bl) + cross(al, bh));
 }
 
 // harmonic bond: E = k (r - l0)^2, force on i = 2k (r-l0)/r x_ij, on j its negative
@@ -476,23 +493,26 @@ __device__ inline F3 bond_force(float4 pi, float4 pj, float4 P, const Geo &g, in
 __device__ inline F3 angle_force(float4 pi, float4 pj, float4 pk, float4 P, const Geo &g, int role, float &e) {
     const float SMALL = 1e-10f;
     const float kf = P.x;
-    const F3 a = shortest3(pj, pi, g);  // x_ji
-    const F3 b = shortest3(pj, pk, g);  // x_jk
-    const F3 cr = f3(diff_prod(a.y, b.z, a.z, b.y), diff_prod(a.z, b.x, a.x, b.z), diff_prod(a.x, b.y, a.y, b.x));
+    F3 a, la, b, lb;
+    shortest3_ff(pj, pi, g, a, la);  // x_ji
+    shortest3_ff(pj, pk, g, b, lb);  // x_jk
+    const F3 cr = cross_ff(a, la, b, lb);  // short near theta = 0 and pi: formed from the exact differences
     const float cn = sqrtf(dot(cr, cr));
     const float sp = dot(a, b);
     const float na2 = fmaxf(dot(a, a), SMALL), nb2 = fmaxf(dot(b, b), SMALL);
     const float np = fmaxf(sqrtf(na2) * sqrtf(nb2), SMALL);
-    const float inp = 1.0f / np;
-    const float c = fminf(1.0f, fmaxf(-1.0f, sp * inp));
     float dth;
     if (sp < 0.0f) dth = P.z - atan2f(cn, -sp);
     else dth = atan2f(cn, sp) - P.y;
     e = kf * dth * dth;
-    const float sinv = 1.0f / fmaxf(cn * inp, SMALL);
-    const float cc = 2.0f * kf * dth * sinv;
-    const F3 fi = (cc * c / na2) * a - (cc * inp) * b;
-    const F3 fk = (-cc * inp) * a + (cc * c / nb2) * b;
+    // The reference's force_i = c cos(theta)/|a|^2 a - c/(|a||b|) b with c = 2k dth / sin(theta) is
+    // -(c/(|a||b|)) times the part of b perpendicular to a, ((a x b) x a)/|a|^2; force_k likewise
+    // with (b x (a x b))/|b|^2.  Formed from the cross product, that part keeps its relative accuracy
+    // near theta = 0 and pi, where the two terms of the reference's expression cancel.  The
+    // reference's clamp sin(theta) >= SMALL becomes |a x b| >= SMALL |a||b|.
+    const float q = 2.0f * kf * dth / fmaxf(cn, SMALL * np);
+    const F3 fi = (-q / na2) * cross_k(cr, a);
+    const F3 fk = (-q / nb2) * cross_k(b, cr);
     if (role == 0) return (-1.0f) * fi;
     if (role == 1) return fi + fk;
     return (-1.0f) * fk;
@@ -503,13 +523,16 @@ __device__ inline F3 angle_force(float4 pi, float4 pj, float4 pk, float4 P, cons
 __device__ inline F3 dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl, float kf, float mult, float phi0,
                                     const Geo &g, int role, float &e) {
     const float SMALL = 1e-4f;
-    const F3 xji = shortest3(pj, pi, g);
-    const F3 xkj = shortest3(pk, pj, g);
-    const F3 xkl = shortest3(pk, pl, g);
+    F3 xji, lji, xkj, lkj, xkl, lkl;
+    shortest3_ff(pj, pi, g, xji, lji);  // x_i - x_j
+    shortest3_ff(pk, pj, g, xkj, lkj);  // x_j - x_k
+    shortest3_ff(pk, pl, g, xkl, lkl);  // x_l - x_k
     const F3 xjk = (-1.0f) * xkj;
+    // m = x_ji x x_kj and n = x_kl x x_jk from the exact differences: near a straight bond angle m or n
+    // is short, and rounded differences would cost it most of its digits (and phi with them)
+    const F3 m = cross_ff(xji, lji, xkj, lkj);
+    const F3 n = (-1.0f) * cross_ff(xkl, lkl, xkj, lkj);
     // energy (TorsionPotential.cpp:53-68) uses clamped norms of |x_jk| and |m||n|
-    const F3 m = cross(xji, xkj);
-    const F3 n = cross(xkl, xjk);
     const float mm_raw = dot(m, m), nn_raw = dot(n, n), jk2_raw = dot(xjk, xjk);
     {
         const float xjkn_e = fmaxf(sqrtf(jk2_raw), SMALL);
@@ -530,6 +553,22 @@ __device__ inline F3 dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl, 
     const float sphi = dot(mxn, xjk) / (nmn * xjkn);
     const float phi = -atan2f(sphi, cphi);
     const float dVdphi = -kf * mult * sinf(mult * phi - phi0);
+    if (jk2_raw >= SMALL && mm_raw >= SMALL && nn_raw >= SMALL && mn * nn >= SMALL) {
+        // No clamp of the reference is active, so its gradient equals the analytic one.  Taken in the
+        // form of Blondel & Karplus (J. Comput. Chem. 17, 1132 (1996)) with F = x_ji, G = x_kj,
+        // H = x_kl, A = F x G (= m), B = H x G (= -n): no term cancels unless A or B vanishes.  The
+        // reference's phi is -(phi_BK +- pi), so its force -dV/dphi dphi/dx = dV/dphi dphi_BK/dx.
+        const F3 A = m, B = (-1.0f) * n;
+        const float A2 = dot(A, A), B2 = dot(B, B);
+        const float Gn = sqrtf(dot(xkj, xkj));
+        const float fg = dot(xji, xkj) / (A2 * Gn), hg = dot(xkl, xkj) / (B2 * Gn);
+        F3 gr;
+        if (role == 0) gr = (-Gn / A2) * A;
+        else if (role == 3) gr = (Gn / B2) * B;
+        else if (role == 1) gr = (Gn / A2 + fg) * A - hg * B;
+        else gr = (hg - Gn / B2) * B - fg * A;
+        return dVdphi * gr;
+    }
     const float sbc = sphi / cphi;
     const float ppre = -1.0f / (cphi * (1.0f + sbc * sbc));
     const float cpre = 1.0f / nmn;

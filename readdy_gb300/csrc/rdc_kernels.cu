@@ -263,9 +263,11 @@ __global__ void k_events(SysDev s, int handler) {
             atomicOr(&s.counters[C_STATUS], ST_EVENTS);
         }
     };
-    GRID_STRIDE(i, n) {
-        events_at(i, i < n_in, s.pos, s.id, s.start, g, s.radius, rt, s.seed, step, handler, emit);
-    }
+    __shared__ int q1[EVENT_QUEUE], q2[EVENT_QUEUE], qn;
+    __shared__ unsigned char qr[EVENT_QUEUE];
+    const TupleQueue Q{q1, q2, qr, &qn};
+    block_events(blockIdx.x * blockDim.x, gridDim.x * blockDim.x, n, n_in, s.pos, s.id, s.start, g, s.radius, rt,
+                 s.seed, step, handler, Q, emit);
 }
 
 // ------------------------------------------------------------------------------------------------
