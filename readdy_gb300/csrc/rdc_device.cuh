@@ -472,6 +472,27 @@ __device__ inline F3 cross_ff(F3 ah, F3 al, F3 bh, F3 bl) {
     return cross_k(ah, bh) + (cross(ah, bl) + cross(al, bh));
 }
 
+// (ah + al) + s (bh + bl) rounded once per component (s = +-1), from the exact sum of the high parts
+__device__ inline F3 ff_sum3(F3 ah, F3 al, F3 bh, F3 bl, float sgn) {
+    auto one = [&](float a, float la, float b, float lb) {
+        const float bb = sgn * b;
+        const float h = __fadd_rn(a, bb);
+        return __fadd_rn(h, __fadd_rn(two_sum_err(a, bb, h), __fadd_rn(la, sgn * lb)));
+    };
+    return F3{one(ah.x, al.x, bh.x, bl.x), one(ah.y, al.y, bh.y, bl.y), one(ah.z, al.z, bh.z, bl.z)};
+}
+
+// FP64 vectors for the few quantities that need more than FP32 (the dihedral angle)
+struct D3 { double x, y, z; };
+__device__ inline D3 d3(F3 hi, F3 lo) {
+    return D3{(double)hi.x + (double)lo.x, (double)hi.y + (double)lo.y, (double)hi.z + (double)lo.z};
+}
+__device__ inline D3 dcross(D3 a, D3 b) {
+    return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ inline D3 dneg(D3 a) { return D3{-a.x, -a.y, -a.z}; }
+__device__ inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
 // harmonic bond: E = k (r - l0)^2, force on i = 2k (r-l0)/r x_ij, on j its negative
 // (BondedPotential.h:105-113, CPUTopologyActions.cpp:61-74); r - l0 = (d2 - l0^2) / (r + l0)
 // from the float-float d2.  P = (k, l0, l0^2 hi, l0^2 lo)
@@ -528,47 +549,64 @@ __device__ inline F3 dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl, 
     shortest3_ff(pk, pj, g, xkj, lkj);  // x_j - x_k
     shortest3_ff(pk, pl, g, xkl, lkl);  // x_l - x_k
     const F3 xjk = (-1.0f) * xkj;
-    // m = x_ji x x_kj and n = x_kl x x_jk from the exact differences: near a straight bond angle m or n
-    // is short, and rounded differences would cost it most of its digits (and phi with them)
+    // m = x_ji x x_kj and n = x_kl x x_jk are formed from the exact differences: near a straight bond
+    // angle m or n is short, and rounded differences would cost it most of its digits.
+    // The dihedral angle is taken in FP64 from the exact differences.  Its force is dV/dphi times a
+    // gradient of length ~1/(|x_ji| sin theta); near n phi - phi0 = 0 mod pi, dV/dphi is small and an
+    // FP32 phi (error ~1e-7 rad) would leave it with few correct digits.
+    const D3 Fd = d3(xji, lji), Gd = d3(xkj, lkj), Hd = d3(xkl, lkl);
+    const D3 md = dcross(Fd, Gd), nd = dneg(dcross(Hd, Gd)), jkd = dneg(Gd);  // m, n, x_jk of the reference
+    const double mm_d = ddot(md, md), nn_d = ddot(nd, nd), jk2_d = ddot(jkd, jkd);
+    const double mxn_jk = ddot(dcross(md, nd), jkd), m_n = ddot(md, nd);
+    {   // energy (TorsionPotential.cpp:53-68): clamps on |x_jk| and |m||n|
+        const double xjkn_e = fmax(sqrt(jk2_d), (double)SMALL);
+        const double mnn_e = fmax(sqrt(mm_d) * sqrt(nn_d), (double)SMALL);
+        const double dih = -atan2(mxn_jk / (mnn_e * xjkn_e), m_n / mnn_e);
+        e = (float)((double)kf * (1.0 + cos((double)mult * dih - (double)phi0)));
+    }
+    // force (TorsionPotential.cpp:70-159): clamps on |x_jk|^2, |m|^2, |n|^2 and |m||n|
+    const double nmn_d = fmax(sqrt(fmax(mm_d, (double)SMALL)) * sqrt(fmax(nn_d, (double)SMALL)), (double)SMALL);
+    const double cphi_d = m_n / nmn_d;
+    if (fabs(cphi_d) < (double)SMALL) return f3(0.f, 0.f, 0.f);
+    const double sphi_d = mxn_jk / (nmn_d * sqrt(fmax(jk2_d, (double)SMALL)));
+    const double phi_d = -atan2(sphi_d, cphi_d);
+    const float dVdphi = (float)(-(double)kf * (double)mult * sin((double)mult * phi_d - (double)phi0));
+    if (jk2_d >= SMALL && mm_d >= SMALL && nn_d >= SMALL && sqrt(mm_d) * sqrt(nn_d) >= SMALL) {
+        // No clamp of the reference is active, so its gradient equals the analytic one.  Taken in the
+        // form of Blondel & Karplus (J. Comput. Chem. 17, 1132 (1996)) with F = x_ji, G = x_kj,
+        // H = x_kl, A = F x G (= m), B = H x G (= -n), in FP32: no term cancels unless A or B
+        // vanishes.  The coefficients of the middle atoms, |G|/|A|^2 + F.G/(|A|^2 |G|) and
+        // H.G/(|B|^2 |G|) - |G|/|B|^2, are G.(x_i - x_k)/(|A|^2 |G|) and G.(x_l - x_j)/(|B|^2 |G|),
+        // formed from exact sums so that they keep their digits when the two parts cancel.  The
+        // reference's phi is -(phi_BK +- pi), so its force -dV/dphi dphi/dx = dV/dphi dphi_BK/dx.
+        const F3 A = cross_ff(xji, lji, xkj, lkj), B = cross_ff(xkl, lkl, xkj, lkj);
+        const float A2 = dot(A, A), B2 = dot(B, B);
+        const float Gn = sqrtf(dot(xkj, xkj));
+        F3 gr;
+        if (role == 0) {
+            gr = (-Gn / A2) * A;
+        } else if (role == 3) {
+            gr = (Gn / B2) * B;
+        } else if (role == 1) {
+            const F3 xik = ff_sum3(xji, lji, xkj, lkj, 1.0f);  // x_i - x_k
+            gr = (dot(xkj, xik) / (A2 * Gn)) * A - (dot(xkl, xkj) / (B2 * Gn)) * B;
+        } else {
+            const F3 xlj = ff_sum3(xkl, lkl, xkj, lkj, -1.0f);  // x_l - x_j
+            gr = (dot(xkj, xlj) / (B2 * Gn)) * B - (dot(xji, xkj) / (A2 * Gn)) * A;
+        }
+        return dVdphi * gr;
+    }
+    // a clamp is active: the reference's own gradient expression, in FP32 (m and n of the reference)
     const F3 m = cross_ff(xji, lji, xkj, lkj);
     const F3 n = (-1.0f) * cross_ff(xkl, lkl, xkj, lkj);
-    // energy (TorsionPotential.cpp:53-68) uses clamped norms of |x_jk| and |m||n|
     const float mm_raw = dot(m, m), nn_raw = dot(n, n), jk2_raw = dot(xjk, xjk);
-    {
-        const float xjkn_e = fmaxf(sqrtf(jk2_raw), SMALL);
-        const float mnn_e = fmaxf(sqrtf(mm_raw) * sqrtf(nn_raw), SMALL);
-        const float sinT = dot(cross(m, n), xjk) / (mnn_e * xjkn_e);
-        const float cosT = dot(m, n) / mnn_e;
-        const float dih = -atan2f(sinT, cosT);
-        e = kf * (1.0f + cosf(mult * dih - phi0));
-    }
     const float xjkn2 = fmaxf(jk2_raw, SMALL);
     const float xjkn = sqrtf(xjkn2);
     const float mn2 = fmaxf(mm_raw, SMALL), nn2 = fmaxf(nn_raw, SMALL);
     const float mn = sqrtf(mn2), nn = sqrtf(nn2);
     const float nmn = fmaxf(mn * nn, SMALL);
     const F3 mxn = cross(m, n);
-    const float cphi = dot(n, m) / nmn;
-    if (fabsf(cphi) < SMALL) return f3(0.f, 0.f, 0.f);
-    const float sphi = dot(mxn, xjk) / (nmn * xjkn);
-    const float phi = -atan2f(sphi, cphi);
-    const float dVdphi = -kf * mult * sinf(mult * phi - phi0);
-    if (jk2_raw >= SMALL && mm_raw >= SMALL && nn_raw >= SMALL && mn * nn >= SMALL) {
-        // No clamp of the reference is active, so its gradient equals the analytic one.  Taken in the
-        // form of Blondel & Karplus (J. Comput. Chem. 17, 1132 (1996)) with F = x_ji, G = x_kj,
-        // H = x_kl, A = F x G (= m), B = H x G (= -n): no term cancels unless A or B vanishes.  The
-        // reference's phi is -(phi_BK +- pi), so its force -dV/dphi dphi/dx = dV/dphi dphi_BK/dx.
-        const F3 A = m, B = (-1.0f) * n;
-        const float A2 = dot(A, A), B2 = dot(B, B);
-        const float Gn = sqrtf(dot(xkj, xkj));
-        const float fg = dot(xji, xkj) / (A2 * Gn), hg = dot(xkl, xkj) / (B2 * Gn);
-        F3 gr;
-        if (role == 0) gr = (-Gn / A2) * A;
-        else if (role == 3) gr = (Gn / B2) * B;
-        else if (role == 1) gr = (Gn / A2 + fg) * A - hg * B;
-        else gr = (hg - Gn / B2) * B - fg * A;
-        return dVdphi * gr;
-    }
+    const float cphi = (float)cphi_d, sphi = (float)sphi_d;
     const float sbc = sphi / cphi;
     const float ppre = -1.0f / (cphi * (1.0f + sbc * sbc));
     const float cpre = 1.0f / nmn;

@@ -206,6 +206,12 @@ __device__ inline double block_sum_double(double v) {
 
 // Pair force and half pair energy on particle i (storage index inside the cells) from every
 // neighbour of the stencil; the full both-direction iteration of CPUCalculateForces.cpp:214-268.
+// The walk only screens candidates (cheap FP32 distance test) and keeps up to PAIR_BUFFER survivors in
+// registers; their forces are evaluated afterwards, with the lanes of a warp evaluating their k-th
+// survivors together.  Evaluated inside the walk, the force body ran for the one lane in six or so
+// that had met a neighbour.  Survivors keep the walk order, so the summation order is unchanged.
+constexpr int PAIR_BUFFER = 4;
+
 template <typename G, typename S>
 __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const S *__restrict__ start,
                                      const G &g, int radius, const int *tab, const float *screen, const PairPot *pots,
@@ -213,14 +219,9 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
     const int ti = itype(p);
     const int *trow = tab + ti * T;
     const float *srow = screen + ti * T;
-    for_each_candidate(p, g, start, radius, 0, [&](int j) {
-        if (j == i) return;
+    auto body = [&](int j) {
         const float4 q = pos[j];
-        const int tj = itype(q);
-        if (tj < 0) return;
-        const int pt = trow[tj];
-        if (pt == 0) return;
-        if (screen_d2(p, q, g) > srow[tj]) return;
+        const int pt = trow[itype(q)];
         const PairGeom g0 = pair_geom(p, q, g);
         const int first = pt >> 8, cnt = pt & 0xff;
         for (int k = first; k < first + cnt; ++k) {
@@ -228,7 +229,30 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
             PairGeom gg = g0;
             if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, p, q, g, fx, fy, fz, e);
         }
+    };
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0, nb = 0;
+    for_each_candidate(p, g, start, radius, 0, [&](int j) {
+        if (j == i) return;
+        const float4 q = pos[j];
+        const int tj = itype(q);
+        if (tj < 0) return;
+        if (trow[tj] == 0) return;
+        if (screen_d2(p, q, g) > srow[tj]) return;
+        if (nb == PAIR_BUFFER) {  // full: evaluate the oldest survivor now and shift
+            body(b0);
+            b0 = b1; b1 = b2; b2 = b3;
+            --nb;
+        }
+        if (nb == 0) b0 = j;
+        else if (nb == 1) b1 = j;
+        else if (nb == 2) b2 = j;
+        else b3 = j;
+        ++nb;
     });
+    for (int k = 0; k < nb; ++k) {
+        body(b0);
+        b0 = b1; b1 = b2; b2 = b3;
+    }
 }
 
 // Euler-Maruyama update of one particle (CPUEulerBDIntegrator.cpp:66-73), FP32, Philox noise
