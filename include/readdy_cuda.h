@@ -178,6 +178,41 @@ int rdc_batch_get_particles(rdc_batch *b, int replica, int64_t capacity, double 
                             uint64_t *ids, int64_t *n_out);
 int rdc_batch_synchronize(rdc_batch *b);
 
+/* ---- served form (no reference counterpart: a request loop over independent simulations) --------
+ * Requests of different sizes and chemistries arrive with their own context, particles, step count,
+ * time step, count stride (per-type counts at t = 0 and every count_stride steps, like the NParticles
+ * observable, CPUObservables.cpp:153-171) and seed.  They are admitted first come, first served, while
+ * the device bytes of the admitted requests stay within budget_bytes; each keeps its particle state in
+ * device memory until it finishes.  Requests of up to plain_threshold particles (0: all) run together
+ * in the fused replica engine, one launch per step; larger ones run as per-system simulations on their
+ * own stream.  A request's result depends only on the request, not on the others in the mix. */
+typedef struct rdc_server rdc_server;
+int rdc_server_create(rdc_server **out, uint64_t budget_bytes, int max_active, int handler, int64_t plain_threshold);
+int rdc_server_destroy(rdc_server *s);
+/* device bytes a request would hold while active, and whether it would take the per-system leg
+ * (host arithmetic only, no device needed) */
+int rdc_server_request_bytes(const rdc_context *ctx, int64_t n, int64_t n_steps, int64_t count_stride,
+                             int64_t plain_threshold, uint64_t *bytes, int *plain);
+/* queue a request (the context is copied); *request_id identifies it from now on.  A request larger than
+ * the whole budget returns RDC_ERR_INVALID_ARGUMENT. */
+int rdc_server_submit(rdc_server *s, const rdc_context *ctx, int64_t n, const double *positions3, const int *types,
+                      int64_t n_steps, double dt, int64_t count_stride, uint64_t seed, int64_t *request_id);
+/* admit what fits, advance the engine requests by up to max_steps (fewer when one of them finishes
+ * first), retire finished requests of both legs */
+int rdc_server_progress(rdc_server *s, int64_t max_steps, int64_t *n_finished);
+/* ids of requests finished since the last poll */
+int rdc_server_poll(rdc_server *s, int64_t capacity, int64_t *ids, int64_t *n_out);
+/* count records (n_records x n_types of the request's context), status (-1 while unfinished) and the
+ * submit, admit and finish times in seconds since the server was created */
+int rdc_server_result(rdc_server *s, int64_t id, int64_t capacity, int64_t *counts, int64_t *n_records, int *status,
+                      double *times3);
+/* forget a finished request */
+int rdc_server_release(rdc_server *s, int64_t id);
+/* particles advanced so far (summed over requests and steps), device bytes held by admitted requests,
+ * requests running and waiting */
+int rdc_server_stats(rdc_server *s, uint64_t *particle_steps, uint64_t *bytes_in_use, int64_t *n_active,
+                     int64_t *n_pending);
+
 /* ---- forces without device allocation (no counterpart in the reference) ----------------------
  * For callers that cannot let the library allocate device memory where they need forces: code that
  * records its step by CUDA stream capture (no cudaMalloc while a stream captures) and embeddings

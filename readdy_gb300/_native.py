@@ -89,6 +89,15 @@ def _sig(lib):
         "rdc_batch_n_particles": (i, [vp, P(i64)]),
         "rdc_batch_get_particles": (i, [vp, i, i64, P(d), P(i), P(u64), P(i64)]),
         "rdc_batch_synchronize": (i, [vp]),
+        "rdc_server_create": (i, [vpp, u64, i, i, i64]),
+        "rdc_server_destroy": (i, [vp]),
+        "rdc_server_request_bytes": (i, [vp, i64, i64, i64, i64, P(u64), P(i)]),
+        "rdc_server_submit": (i, [vp, vp, i64, P(d), P(i), i64, d, i64, u64, P(i64)]),
+        "rdc_server_progress": (i, [vp, i64, P(i64)]),
+        "rdc_server_poll": (i, [vp, i64, P(i64), P(i64)]),
+        "rdc_server_result": (i, [vp, i64, i64, P(i64), P(i64), P(i), P(d)]),
+        "rdc_server_release": (i, [vp, i64]),
+        "rdc_server_stats": (i, [vp, P(u64), P(u64), P(i64), P(i64)]),
         "rdc_forces_noalloc": (i, [vp, i64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in table.items():

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libreaddy_cuda_core.so")
-SOURCES = ["rdc_kernels.cu", "rdc_api.cu", "rdc_batch.cu", "rdc_noalloc.cu"]
+SOURCES = ["rdc_kernels.cu", "rdc_api.cu", "rdc_engine.cu", "rdc_batch.cu", "rdc_serve.cu", "rdc_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]

@@ -242,6 +242,7 @@ struct rdc_context {
 
 namespace rdc {
 const ContextData &context_data(const rdc_context *ctx) { return ctx->d; }
+rdc_context *context_clone(const ContextData &d) { return new rdc_context{d}; }
 void set_last_error(const std::string &m) { g_err = m; }
 }  // namespace rdc
 

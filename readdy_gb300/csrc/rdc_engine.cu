@@ -1,0 +1,423 @@
+// Device side of the fused replica engine (declarations and overview in rdc_engine.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "rdc_engine.h"
+#include "rdc_phases.cuh"
+
+namespace rdc {
+
+template <typename T>
+__device__ inline void block_zero(T *a, int n) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) a[k] = 0;
+    __syncthreads();
+}
+
+template <typename D, typename T>
+__device__ inline void block_copy(D *dst, const T *src, int n) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = (D)src[k];
+    __syncthreads();
+}
+
+// in-place exclusive scan of a[0..n) by one block (shared or global memory); a[n] = total
+template <typename T>
+__device__ inline void block_scan_inplace(T *a, int n) {
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    constexpr int ITEMS = 4;
+    const int tile = blockDim.x * ITEMS;
+    for (int base = 0; base < n; base += tile) {
+        const int b = base + threadIdx.x * ITEMS;
+        int v[ITEMS];
+        int sum = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            v[k] = (b + k < n) ? a[b + k] : 0;
+            sum += v[k];
+        }
+        int total;
+        int run = block_exclusive_scan(sum, total) + carry;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (b + k < n) a[b + k] = (T)run;
+            run += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a[n] = (T)carry;
+    __syncthreads();
+}
+
+// ranks of the particles inside their bins (bin[] already set); cells receives the counts
+__device__ inline void block_rank(int n, const int *bin, int *rank, int *cells, int nbins) {
+    block_zero(cells, nbins);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) rank[i] = atomicAdd(&cells[bin[i]], 1);
+    __syncthreads();
+}
+
+// 16-bit counters, two per 32-bit word (4-byte aligned array); a count never exceeds the replica's
+// particles (< 65536), so an increment never carries into the neighbouring counter
+__device__ inline void block_rank(int n, const int *bin, int *rank, uint16_t *cells, int nbins) {
+    block_zero(cells, nbins);
+    unsigned *w = reinterpret_cast<unsigned *>(cells);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int b = bin[i];
+        const unsigned sh = (unsigned)(b & 1) * 16u;
+        rank[i] = (int)((atomicAdd(&w[b >> 1], 1u << sh) >> sh) & 0xffffu);
+    }
+    __syncthreads();
+}
+
+__device__ inline void block_bin(const float4 *pos, int n, int *bin, const Geo &g) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) bin[i] = bin_of(pos[i], g);
+    __syncthreads();
+}
+
+// counting sort of one replica from counts in cells: scan to cell starts, scatter, order each cell
+// by source index (deterministic), gather into the destination arrays
+template <typename C>
+__device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n, float4 *dpos, uint32_t *did,
+                                  const int *bin, const int *rank, int *src, C *cells, const Geo &g, int &n_new,
+                                  int &n_in) {
+    const int nc = g.ncells;
+    block_scan_inplace(cells, nc + 2);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int b = bin[i];
+        if (b <= nc) src[cells[b] + rank[i]] = i;
+    }
+    __syncthreads();
+    __shared__ int big[64];
+    __shared__ int nbig;
+    if (threadIdx.x == 0) nbig = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int b = cells[c], e = cells[c + 1];
+        if (e - b > CELL_SORT_SMALL) {
+            const int q = atomicAdd(&nbig, 1);
+            if (q < 64) big[q] = c;
+            continue;
+        }
+        insertion_sort(src, b, e);
+    }
+    __syncthreads();
+    // crowded cells: ordered by the whole block (rank[] is free scratch after the scatter)
+    if (nbig <= 64) {
+        for (int q = 0; q < nbig; ++q) block_rank_sort(src, const_cast<int *>(rank), cells[big[q]], cells[big[q] + 1]);
+    } else {
+        for (int c = 0; c < nc; ++c)
+            if (cells[c + 1] - cells[c] > CELL_SORT_SMALL) block_rank_sort(src, const_cast<int *>(rank), cells[c], cells[c + 1]);
+    }
+    n_new = cells[nc + 1];
+    n_in = cells[nc];
+    for (int j = threadIdx.x; j < n_new; j += blockDim.x) {
+        const int k = src[j];
+        dpos[j] = spos[k];
+        did[j] = sid[k];
+    }
+    __syncthreads();
+}
+
+__device__ inline void block_count_types(const float4 *pos, int n, int T, unsigned long long *out) {
+    __shared__ unsigned int hist[MAX_TYPES];
+    for (int k = threadIdx.x; k < T; k += blockDim.x) hist[k] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int t = itype(pos[i]);
+        if (t >= 0 && t < T) atomicAdd(&hist[t], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < T; k += blockDim.x) out[k] = hist[k];
+    __syncthreads();
+}
+
+struct SmemLayout {
+    int *tab;
+    float *screen;
+    float *drift, *scale;
+    PairPot *pots;
+    uint64_t *key;
+    int *idx, *state;
+    TupleQueue queue;
+    uint16_t *cells;
+};
+
+// dynamic shared memory: event keys, potentials and the type-pair table of the largest context,
+// resolution scratch, the event tuple queue, then the 16-bit cell array
+__device__ inline SmemLayout carve(unsigned char *smem, int max_events) {
+    SmemLayout L;
+    size_t off = 0;
+    L.key = reinterpret_cast<uint64_t *>(smem + off);
+    off += sizeof(uint64_t) * max_events;
+    L.pots = reinterpret_cast<PairPot *>(smem + off);
+    off += sizeof(PairPot) * MAX_PAIR_POTENTIALS;
+    L.tab = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * MAX_TYPES * MAX_TYPES;
+    L.idx = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * max_events;
+    L.state = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * max_events;
+    L.queue.p1 = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * EVENT_QUEUE;
+    L.queue.p2 = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * EVENT_QUEUE;
+    L.queue.count = reinterpret_cast<int *>(smem + off);
+    off += sizeof(int) * 4;
+    L.queue.r = smem + off;
+    off += EVENT_QUEUE;
+    L.cells = reinterpret_cast<uint16_t *>(smem + off);
+    return L;
+}
+
+size_t engine_smem_bytes(int max_events) {
+    return sizeof(uint64_t) * max_events + sizeof(PairPot) * MAX_PAIR_POTENTIALS + sizeof(int) * MAX_TYPES * MAX_TYPES +
+           2 * sizeof(int) * max_events + (2 * sizeof(int) + 1) * EVENT_QUEUE + 4 * sizeof(int) +
+           sizeof(uint16_t) * (SMEM_CELLS + 4) + 16;
+}
+
+// one step of one replica by the whole block; C is the cell array's type (uint16_t in shared memory
+// or int in global memory)
+template <typename C>
+__device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, const RxnTables &rt, const Tables *tab,
+                             const RepDesc &D, const RepState &st, int &sh_nev, int &sh_status, C *cells) {
+    const int T = tab->ntypes, NP = tab->npots;
+    const uint64_t step = (uint64_t)st.step;
+    const Geo &gs = D.geo;
+    const GeoR g = geo_r(gs);
+    const int nc = gs.ncells;
+    float4 *posX = D.pos[st.cur];
+    uint32_t *idX = D.id[st.cur];
+    float4 *posY = D.pos[st.cur ^ 1];
+    uint32_t *idY = D.id[st.cur ^ 1];
+    int *bin = D.bin, *rank = D.rank, *src = D.src;
+    int *gstart = D.start;
+    constexpr bool in_smem = sizeof(C) == sizeof(uint16_t);
+    if (in_smem) block_copy(cells, gstart, nc + 3);
+    const int n = st.n, n_in = st.n_in;
+
+    // forces on the current state, Euler step into Y, bins of the new positions
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float4 p = posX[i];
+        float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+        if (i < n_in && NP > 0) pair_force_at(i, p, posX, cells, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e);
+        const uint32_t id = idX[i];
+        const int t = itype(p);
+        const float4 q = euler_bd(p, fx, fy, fz, id, D.seed, step, S.drift[t], S.scale[t], g);
+        posY[i] = q;
+        idY[i] = id;
+        bin[i] = bin_of(q, gs);
+    }
+    __syncthreads();
+    block_rank(n, bin, rank, cells, nc + 2);
+    int n1, nin1;
+    block_sort(posY, idY, n, posX, idX, bin, rank, src, cells, gs, n1, nin1);
+
+    int n_final = n1, nin_final = nin1, cur = st.cur, next_id = st.next_id;
+    if (tab->nreactions > 0) {
+        EventRec *ev = D.events;
+        const int ecap = D.ecap;
+        auto emit = [&](uint64_t key, int p1, int p2, int rr) {
+            const int k = atomicAdd(&sh_nev, 1);
+            if (k < ecap) {
+                EventRec e;
+                e.key = key; e.p1 = p1; e.p2 = p2; e.reaction = rr; e.pad = 0;
+                ev[k] = e;
+            } else {
+                atomicOr(&sh_status, ST_EVENTS);
+            }
+        };
+        block_events(0, blockDim.x, n1, nin1, posX, idX, cells, g, 1, rt, D.seed, step, E.handler, S.queue, emit);
+        const int Ev = min(sh_nev, ecap);
+        if (Ev > 0) {
+            ApplyTarget t;
+            t.pos = posX; t.id = idX; t.tslot = nullptr; t.force = nullptr;
+            t.claim = D.claim; t.taken = D.taken;
+            t.reaction_counts = D.rx_counts;
+            t.n_total = n1;
+            t.capacity = D.cap;
+            t.next_id = (uint32_t)st.next_id;
+            ApplyResult res;
+            block_resolve_apply(ev, Ev, E.max_events_sm, S.key, S.idx, S.state, tab, gs, D.seed, step, t, res);
+            next_id = st.next_id + res.ids;
+            if (threadIdx.x == 0) sh_status |= res.status;
+            if (res.winners > 0) {
+                // particles changed cells, appeared or vanished: sort again, into Y
+                const int n_total = n1 + res.births;
+                block_bin(posX, n_total, bin, gs);
+                block_rank(n_total, bin, rank, cells, nc + 2);
+                int n2, nin2;
+                block_sort(posX, idX, n_total, posY, idY, bin, rank, src, cells, gs, n2, nin2);
+                n_final = n2;
+                nin_final = nin2;
+                cur ^= 1;
+            }
+        }
+    }
+    if (in_smem) block_copy(gstart, cells, nc + 3);
+    int rec = st.rec;
+    if (D.records && D.count_stride > 0 && (step + 1) % (uint64_t)D.count_stride == 0 && rec < D.max_records) {
+        block_count_types(D.pos[cur], n_final, T, D.records + (size_t)rec * T);
+        ++rec;
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(E.particle_steps, (unsigned long long)n);
+        RepState o;
+        o.n = n_final;
+        o.n_in = nin_final;
+        o.cur = cur;
+        o.next_id = next_id;
+        o.status = st.status | sh_status;
+        o.rec = rec;
+        o.step = st.step + 1;
+        E.state[r] = o;
+    }
+    __syncthreads();
+}
+
+// Stages the potential and reaction tables of a context into shared memory (whole block).
+__device__ inline RxnTables stage_tables(const Tables *tab, const SmemLayout &S, int *rt_ints, float *rt_screen,
+                                         ReactionDev *rt_rx) {
+    const int T = tab->ntypes, NP = tab->npots;
+    for (int k = threadIdx.x; k < T * T; k += blockDim.x) {
+        S.tab[k] = tab->pair_tab[k];
+        S.screen[k] = tab->pair_screen[k];
+    }
+    for (int k = threadIdx.x; k < NP; k += blockDim.x) S.pots[k] = tab->pots[k];
+    for (int k = threadIdx.x; k < T; k += blockDim.x) {
+        S.drift[k] = tab->bd_drift[k];
+        S.scale[k] = tab->bd_scale[k];
+    }
+    return stage_rxn_tables(tab, rt_ints, rt_screen, rt_rx);
+}
+
+__global__ void __launch_bounds__(ENGINE_THREADS_MAX, 1) k_engine_step(EngineDev E) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int sh_r, sh_table, sh_nev, sh_status;
+    __shared__ RepDesc D;
+    __shared__ RepState st;
+    __shared__ int sh_rt_ints[MAX_TYPES + MAX_REACTIONS * 3 + MAX_TYPES * MAX_TYPES + MAX_TYPES];
+    __shared__ float sh_rt_scr[MAX_TYPES * MAX_TYPES];
+    __shared__ float sh_pair_scr[MAX_TYPES * MAX_TYPES];
+    __shared__ ReactionDev sh_rx[MAX_REACTIONS];
+    __shared__ float sh_drift[MAX_TYPES], sh_scale[MAX_TYPES];
+    SmemLayout S = carve(smem, E.max_events_sm);
+    S.drift = sh_drift;
+    S.scale = sh_scale;
+    S.screen = sh_pair_scr;
+    RxnTables rt{};
+    const int n_work = *E.n_work;
+    if (threadIdx.x == 0) sh_table = -1;
+    __syncthreads();
+    for (;;) {
+        if (threadIdx.x == 0) sh_r = atomicAdd(E.work, 1);
+        __syncthreads();
+        const int w = sh_r;
+        if (w >= n_work) break;
+        const int r = E.order[w];
+        if (threadIdx.x == 0) {
+            D = E.desc[r];
+            st = E.state[r];
+            sh_nev = 0;
+            sh_status = 0;
+        }
+        __syncthreads();
+        // a replica that has run its steps, or whose state is in error, idles
+        if (st.step >= D.n_steps || st.status != 0) continue;
+        const Tables *tab = E.tabs + D.table;
+        if (D.table != sh_table) {
+            rt = stage_tables(tab, S, sh_rt_ints, sh_rt_scr, sh_rx);
+            __syncthreads();
+            if (threadIdx.x == 0) sh_table = D.table;
+        }
+        __syncthreads();
+        if (D.smem_cells) replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, S.cells);
+        else replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, D.start);
+    }
+}
+
+__global__ void k_engine_reset(EngineDev E) { *E.work = 0; }
+
+// ids 0..n-1 (fill_ids), binning and sort of each listed replica (state.cur selects the source; the cell starts
+// are sorted in the replica's global start array), and its t = 0 count record
+__global__ void k_engine_admit(EngineDev E, const int *list, int count, int fill_ids) {
+    for (int w = blockIdx.x; w < count; w += gridDim.x) {
+        const int r = list[w];
+        const RepDesc D = E.desc[r];
+        RepState st = E.state[r];
+        float4 *posX = D.pos[st.cur];
+        uint32_t *idX = D.id[st.cur];
+        if (fill_ids) {
+            for (int i = threadIdx.x; i < st.n; i += blockDim.x) idX[i] = (uint32_t)i;
+            __syncthreads();
+        }
+        block_bin(posX, st.n, D.bin, D.geo);
+        block_rank(st.n, D.bin, D.rank, D.start, D.geo.ncells + 2);
+        int n2, nin2;
+        block_sort(posX, idX, st.n, D.pos[st.cur ^ 1], D.id[st.cur ^ 1], D.bin, D.rank, D.src, D.start, D.geo, n2,
+                   nin2);
+        st.n = n2;
+        st.n_in = nin2;
+        st.cur ^= 1;
+        if (D.records && D.count_stride > 0 && st.rec == 0 && D.max_records > 0) {
+            block_count_types(D.pos[st.cur], st.n, E.tabs[D.table].ntypes, D.records);
+            st.rec = 1;
+        }
+        if (threadIdx.x == 0) E.state[r] = st;
+        __syncthreads();
+    }
+}
+
+__global__ void k_engine_count(EngineDev E, int R, int T, unsigned long long *out) {
+    for (int r = blockIdx.x; r < R; r += gridDim.x) {
+        const RepDesc &D = E.desc[r];
+        const RepState st = E.state[r];
+        block_count_types(D.pos[st.cur], st.n, T, out + (size_t)r * T);
+    }
+}
+
+// ---- host side ----------------------------------------------------------------------------------
+
+Geo replica_geo(const double box[3], const int pbc[3], double cutoff, double cell_scale, int64_t capacity,
+                int &smem_cells) {
+    double w = cutoff * cell_scale;
+    Geo g = make_geo(box, pbc, cutoff, 1, w);
+    const bool small = capacity < 65536;  // cell starts fit 16 bits
+    if (small)
+        for (int k = 0; k < 64 && g.ncells + 3 > SMEM_CELLS && cutoff > 0; ++k) {
+            w *= 1.05;
+            g = make_geo(box, pbc, cutoff, 1, w);
+        }
+    smem_cells = (small && g.ncells + 3 <= SMEM_CELLS) ? 1 : 0;
+    if (!smem_cells) g = make_geo(box, pbc, cutoff, 1, cutoff * cell_scale);
+    return g;
+}
+
+int engine_grid(int threads, size_t smem) {
+    RDC_CUDA(cudaFuncSetAttribute(k_engine_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RDC_CUDA(cudaFuncSetAttribute(k_engine_step, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 0;
+    RDC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_step, threads, smem));
+    int dev = 0, sms = 0;
+    RDC_CUDA(cudaGetDevice(&dev));
+    RDC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return std::max(1, per_sm) * sms;
+}
+
+void launch_engine_step(const EngineDev &E, int blocks, int threads, size_t smem, cudaStream_t st) {
+    k_engine_step<<<blocks, threads, smem, st>>>(E);
+    k_engine_reset<<<1, 1, 0, st>>>(E);
+}
+
+void launch_engine_admit(const EngineDev &E, const int *list, int count, bool fill_ids, cudaStream_t st) {
+    if (count > 0) k_engine_admit<<<std::min(count, 4 * 152), 256, 0, st>>>(E, list, count, fill_ids ? 1 : 0);
+}
+
+void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long long *out, cudaStream_t st) {
+    if (R > 0) k_engine_count<<<std::min(R, 4 * 152), 256, 0, st>>>(E, R, ntypes, out);
+}
+
+}  // namespace rdc

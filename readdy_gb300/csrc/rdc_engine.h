@@ -1,0 +1,81 @@
+// The fused replica engine shared by the batched form (rdc_batch.cu) and the served form
+// (rdc_serve.cu).  A replica is one independent system: its own box, particles, seed, step counter
+// and reaction/potential tables.  Every step is ONE persistent launch over the replicas of a work
+// list: each CTA takes replicas from a work counter (largest first) and runs the whole step of one
+// replica in block-level phases
+//
+//   forces (pair stencil) -> Euler BD -> bin -> counting sort -> reaction events -> conflict
+//   resolution + application -> (re-sort if particles appeared or vanished) -> observables
+//
+// The arithmetic is the per-system path's (rdc_phases.cuh), so a replica gives the same trajectory
+// alone, inside any batch or request mix, or through rdc_run with the replica's seed.  Forces are
+// computed at the start of a step from the state left by the previous step's reactions, which is where
+// SimulationLoop::run computes them (SimulationLoop.h:283-289).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rdc_host.h"
+
+namespace rdc {
+
+// Cell counts and starts of a replica of fewer than 65536 particles live in shared memory during its
+// step as uint16_t, SMEM_CELLS entries (96 KB): at cells of the cutoff's width and density 0.25 that
+// holds replicas of up to ~12k particles, and larger ones get proportionally wider cells.  Replicas of
+// more particles keep int starts in global memory at the natural cell width.
+constexpr int SMEM_CELLS = 49152;
+constexpr int ENGINE_THREADS_MAX = 512;
+
+struct RepDesc {
+    Geo geo;
+    float4 *pos[2];              // double buffer; state.cur selects the current one
+    uint32_t *id[2];
+    int *bin, *rank, *src, *claim, *taken;   // capacity entries each
+    int *start;                  // cell starts between steps, ncells + 3 entries
+    EventRec *events;            // ecap entries
+    unsigned long long *records; // per-type counts, max_records x ntypes (null: none)
+    unsigned long long *rx_counts;  // performed events per reaction (null: none)
+    uint64_t seed;
+    int64_t n_steps;             // the replica idles once it has run this many steps
+    int cap, ecap;
+    int smem_cells;              // 1: uint16_t cell array in shared memory during the step
+    int table;                   // index into EngineDev::tabs
+    int count_stride;            // record counts at t = 0 and after every count_stride steps (0: never)
+    int max_records;
+};
+
+struct RepState {
+    int n, n_in, cur, next_id, status, rec;  // rec: count records written
+    int64_t step;                            // steps run (keys the random streams)
+};
+
+struct EngineDev {
+    const RepDesc *desc;
+    RepState *state;
+    const int *order;   // work item -> replica
+    const int *n_work;  // work items of a step; on the device, so one captured graph serves any list
+    int *work;          // work counter, reset after each step
+    const Tables *tabs;
+    int handler;
+    int max_events_sm;  // events one replica step resolves in shared memory
+    unsigned long long *particle_steps;  // particles advanced, summed over replicas and steps
+};
+
+// decides the cell grid of a replica: cells at least cutoff * cell_scale wide, widened until the
+// grid fits the shared-memory cell array when the replica is small enough for 16-bit starts
+Geo replica_geo(const double box[3], const int pbc[3], double cutoff, double cell_scale, int64_t capacity,
+                int &smem_cells);
+
+size_t engine_smem_bytes(int max_events_sm);
+// kernel attributes for the dynamic shared memory; returns the persistent grid (CTAs resident at once)
+int engine_grid(int threads, size_t smem);
+// one step of every listed replica, then the work counter reset (both captured in the step graph)
+void launch_engine_step(const EngineDev &E, int blocks, int threads, size_t smem, cudaStream_t st);
+// binning and sort of the listed replicas (list: device array of replica indices), after setting the
+// ids to 0..n-1 when fill_ids; replicas with records and none written yet get their t = 0 record
+void launch_engine_admit(const EngineDev &E, const int *list, int count, bool fill_ids, cudaStream_t st);
+// current per-type counts of replicas [0, R) into out (R x ntypes)
+void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long long *out, cudaStream_t st);
+
+}  // namespace rdc

@@ -1,0 +1,77 @@
+"""Served form on the GPU: a request's result is the same alone, in a mix of requests and through the
+per-system path; admission respects the device-memory budget and the submit order."""
+import numpy as np
+import pytest
+
+from readdy_gb300.serve import serving_workload
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rg():
+    import readdy_gb300
+    readdy_gb300.load()
+    return readdy_gb300
+
+
+def small_stream(n_requests=6, seed=11):
+    """Requests of the serving workload at test size: N in [300, 3000], 100-400 steps, counts every 50."""
+    specs = serving_workload(seed=seed, n_requests=n_requests, n_range=(300, 3000), steps=(100, 400))
+    for s in specs:
+        s.count_stride = 50
+    return specs
+
+
+def run_all(specs, budget=1 << 30, plain_threshold=1 << 30, max_steps=64, **kw):
+    from readdy_gb300.serve import Server
+    srv = Server(budget, plain_threshold=plain_threshold, **kw)
+    ids = {srv.submit(s.context(), s.positions, s.types, s.n_steps, s.dt, s.count_stride, s.seed): k
+           for k, s in enumerate(specs)}
+    out, trace = {}, []
+    while len(out) < len(specs):
+        srv.progress(max_steps)
+        trace.append(srv.stats())
+        for rid in srv.poll():
+            out[ids[rid]] = srv.result(rid)
+    return out, trace
+
+
+def test_engine_request_equals_per_system_run(rg):
+    s = small_stream(1, seed=5)[0]
+    res, _ = run_all([s])
+    k = rg.CUDAKernel(s.context(), seed=s.seed)
+    k.add_particles(s.positions, s.types)
+    ref = k.run(s.n_steps, s.dt, handler=rg.GILLESPIE, count_stride=s.count_stride)
+    assert res[0]["status"] == 0
+    np.testing.assert_array_equal(res[0]["counts"], ref)
+
+
+def test_results_are_the_same_alone_and_in_the_mix(rg):
+    specs = small_stream(6, seed=11)
+    # the largest request takes the per-system leg, the others share the fused engine
+    thr = sorted(len(s.positions) for s in specs)[-2]
+    mix, _ = run_all(specs, plain_threshold=thr)
+    for k, s in enumerate(specs):
+        alone, _ = run_all([s], plain_threshold=thr)
+        assert mix[k]["status"] == 0 and alone[0]["status"] == 0
+        np.testing.assert_array_equal(mix[k]["counts"], alone[0]["counts"], err_msg=f"request {k}")
+        assert len(mix[k]["counts"]) == s.n_steps // s.count_stride + 1
+
+
+def test_admission_respects_the_budget_and_the_submit_order(rg):
+    from readdy_gb300.serve import Server
+    specs = small_stream(6, seed=23)
+    sizes = [Server.request_bytes(s.context(), len(s.positions), s.n_steps, s.count_stride)[0] for s in specs]
+    budget = int(2.2 * max(sizes))  # room for two of the largest at a time
+    res, trace = run_all(specs, budget=budget)
+    assert all(t["bytes_in_use"] <= budget for t in trace)
+    assert max(t["active"] for t in trace) <= budget // min(sizes)
+    admits = [res[k]["admit"] for k in range(len(specs))]
+    assert admits == sorted(admits)  # first come, first served
+    for k, s in enumerate(specs):
+        c = res[k]["counts"]
+        assert res[k]["status"] == 0
+        mass = c @ np.asarray(s.mass)
+        assert np.all(mass == len(s.positions))  # the network conserves mass units
+        assert res[k]["finish"] >= res[k]["admit"] >= res[k]["submit"]
