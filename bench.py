@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--replicas", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--serve-requests", type=int, default=32, help="requests of the served-stream sample (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=150.0, help="wall-time limit of the served-stream sample")
+    ap.add_argument("--plain-threshold", type=int, default=4096,
+                    help="requests above this many particles take the per-system leg of the server")
     return ap.parse_args()
 
 
@@ -202,6 +206,25 @@ def one_at_a_time(ns, boxes, pos, types, seed, n_sample, steps, rng_pick):
             "each through the per-system path (CUDA-graph replay of the SimulationLoop step), run sequentially"}
 
 
+def serving(n_requests, time_limit, plain_threshold, seed=7):
+    """The served form on the first n_requests of the seeded serving stream (Poisson arrivals at 20/s;
+    2-6 species; N log-uniform in [500, 200000] at density 0.1-0.5; 1k-100k steps; counts every 100
+    steps), replayed in wall-clock time against a 150 GB device-memory budget."""
+    from readdy_gb300.serve import Server, run_stream, serving_workload
+    specs = serving_workload(seed=seed, n_requests=n_requests)
+    srv = Server(150 << 30, plain_threshold=plain_threshold)
+    res, wall, ps = run_stream(srv, specs, max_steps=100, time_limit=time_limit)
+    lat = np.array(sorted(r["finish"] - r["submit"] for r in res.values()))
+    return {"p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "particle_steps_per_s": ps / wall, "completed": len(res), "requests": n_requests,
+            "wall_s": wall, "offered_particle_steps": float(sum(len(s.positions) * s.n_steps for s in specs)),
+            "failed": int(sum(r["status"] != 0 for r in res.values())),
+            "plain_threshold": plain_threshold,
+            "sample": f"first {n_requests} requests of the seeded 2000-request stream (seed {seed}), arrivals at "
+                      "20/s replayed in wall-clock time, 150 GB budget; latency = finish - submit"}
+
+
 def run_gb300(args, rank, world):
     import readdy_gb300 as rg
     from readdy_gb300.batch import ReplicaBatch
@@ -244,6 +267,7 @@ def run_gb300(args, rank, world):
         pick = np.random.default_rng(args.seed + 99)
         oat = one_at_a_time(ns, boxes, pos, types, seed, 64, 50, pick)
         cpu = cpu_baseline(ns, boxes, pos, types, seed, args.cpu_seconds, np.random.default_rng(args.seed + 5))
+        served = serving(args.serve_requests, args.serve_seconds, args.plain_threshold) if args.serve_requests else None
         peak, peak_kind = measured_peaks()
         n_avg = (ps1 - ps0) / args.steps
         launch_ms = ms / args.steps
@@ -283,6 +307,7 @@ def run_gb300(args, rank, world):
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": 2 * args.steps,
+            "serving": served,
         }
     return result
 
