@@ -38,8 +38,8 @@ UNIT = "particle-steps/s"
 DENSITY = 0.25
 N_MIN, N_MAX = 200, 20000
 # DRAM bytes per particle of one fused step (dram__bytes_read.sum + dram__bytes_write.sum of one ncu
-# capture of k_batch_step on the first 512 replicas of the ensemble, divided by its particles).
-DRAM_BYTES_PER_PARTICLE = (78.10e6 + 121.95e6) / 2097522
+# capture of k_engine_step on the first 512 replicas of the ensemble, divided by its particles).
+DRAM_BYTES_PER_PARTICLE = (90.13e6 + 126.86e6) / 2097522
 # algorithmic bytes of one fused step per particle: the particle state (float4 position with the type,
 # uint32 id) read once and written once
 ALG_BYTES_PER_PARTICLE = 2 * (16 + 4)
@@ -289,7 +289,7 @@ def run_gb300(args, rank, world):
                 "workload": "batched uneven ensemble: 4096 replicas of A+B<->C, N log-uniform in [200, 20000], "
                             "density 0.25, HR k=10 d=1, Gillespie, dt=1e-3",
                 "replicas": int(args.replicas), "particles": int(ns.sum()),
-                "launch": "one persistent fused launch per step (k_batch_step), CUDA graph",
+                "launch": "one persistent fused launch per step (k_engine_step), CUDA graph",
                 "cell_width_scale": 1.0, "threads_per_block": 512,
                 "l2": "inputs larger than L2 (particle state %.0f MB > 129 MB)" % (ns.sum() * 40 / 1e6),
                 "parallelism": f"replicas only, {world} rank(s), one ensemble per GPU",
@@ -299,7 +299,7 @@ def run_gb300(args, rank, world):
             "e2e": {"value": e2e_ps / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d // max(args.steps, 1),
                     "d2h_bytes_per_step": d2h // max(args.steps, 1),
                     "timed": "ReplicaBatch create + set_particles (host arrays) + configure + steps + count_types"},
-            "roofline": {"bound": "hbm", "kernel": "k_batch_step", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": "k_engine_step", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": ALG_BYTES_PER_PARTICLE * n_avg,
                          "traffic": DRAM_BYTES_PER_PARTICLE * n_avg if DRAM_BYTES_PER_PARTICLE else None,

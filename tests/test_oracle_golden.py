@@ -159,3 +159,23 @@ def test_brownian_msd_matches_6Dt():
     p1 = s.particles()[0]
     msd = np.mean(np.sum((p1 - p0) ** 2, axis=1))
     assert abs(msd / (6 * D * dt * steps) - 1) < 0.01
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("handler", [oracle.UNCONTROLLED_APPROXIMATION, oracle.GILLESPIE])
+def test_michaelis_menten_time_averaged_substrate(handler):
+    """readdy/test/IntegrationTests.cpp:30-106: the substrate count averaged over 37501 observations
+    lies within 3 % of 665.2 for both reaction handlers."""
+    mm = ka.MICHAELIS_MENTEN
+    rng = np.random.default_rng(2024)
+    L = mm["box"][0]
+    n = mm["n_e"] + mm["n_s"]
+    pos = (rng.random((n, 3)) - 0.5) * L
+    types = np.array([0] * mm["n_e"] + [1] * mm["n_s"])
+    o = oracle.OracleSystem(mm["box"], mm["periodic"], 1.0, mm["diffusion"], seed=7, n_threads=4)
+    o.add_fusion(0, 1, 2, mm["k_fwd"], mm["educt_distance"])
+    o.add_fission(2, 0, 1, mm["k_back"], mm["product_distance"])
+    o.add_fission(2, 0, 3, mm["k_prod"], mm["product_distance"])
+    o.add_particles(pos, types)
+    c = o.run(mm["n_steps"], mm["dt"], handler=handler, count_stride=1)
+    assert abs(c[:, 1].mean() - mm["mean_s"]) < mm["rel_band"] * mm["mean_s"]
