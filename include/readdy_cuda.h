@@ -68,6 +68,24 @@ int rdc_context_add_screened_electrostatics(rdc_context *ctx, int type1, int typ
                                             double inverse_screening_depth, double repulsion_strength,
                                             double repulsion_distance, unsigned exponent, double cutoff);
 
+/* order-1 (external) potentials of one particle type, PotentialRegistry (PotentialRegistry.h:99-345) with
+ * the classes of include/readdy/model/potentials/PotentialsOrder1.h and the geometries of
+ * include/readdy/model/geometry.h.  Box and capsule also take the exclusion form of
+ * addHarmonicGeometry (PotentialRegistry.h:335-345); addBox itself is inclusion. */
+/* harmonic box: the box spans origin .. origin + extent */
+int rdc_context_add_box(rdc_context *ctx, int type, double force_constant, const double origin[3],
+                        const double extent[3], int inclusion);
+int rdc_context_add_sphere(rdc_context *ctx, int type, double force_constant, const double origin[3], double radius,
+                           int inclusion);
+int rdc_context_add_capsule(rdc_context *ctx, int type, double force_constant, const double center[3],
+                            const double direction[3], double length, double radius, int inclusion);
+/* SphericalBarrier (PotentialsOrder1.h:97-152); width must not exceed radius (Potentials.cpp:86-92) */
+int rdc_context_add_spherical_barrier(rdc_context *ctx, int type, double height, double width,
+                                      const double origin[3], double radius);
+/* Cylinder (PotentialsOrder1.h:154-209); the normal is normalised */
+int rdc_context_add_cylinder(rdc_context *ctx, int type, double force_constant, const double origin[3],
+                             const double normal[3], double radius, int inclusion);
+
 /* ReactionRegistry::addConversion / addDecay / addFusion / addFission / addEnzymatic
  * (include/readdy/model/reactions/{Conversion,Decay,Fusion,Fission,Enzymatic}.h); *reaction_id is the
  * reaction's index in registration order (Reaction.h:93-96) */
@@ -219,8 +237,9 @@ int rdc_server_stats(rdc_server *s, uint64_t *particle_steps, uint64_t *bytes_in
  * whose own pool owns all of the GPU's memory.  Pair forces and the pair energy of n particles held
  * in the caller's device arrays -- positions3 (n*3 floats), types (n ints in [0, n_types)) -- are
  * written to the caller's device arrays forces3 (n*3 floats) and *energy (one double), on `stream`
- * (a cudaStream_t; NULL is the legacy default stream), asynchronously.  Same potentials, exact cutoff
- * test and FP32 terms as rdc_calculate_forces; the neighbour summation order may differ.
+ * (a cudaStream_t; NULL is the legacy default stream), asynchronously.  Same pair potentials, exact
+ * cutoff test and FP32 terms as rdc_calculate_forces; the neighbour summation order may differ.  The
+ * context's order-1 (external) potentials are not applied here. 
  *
  * Working space is one static device array of RDC_NOALLOC_SCRATCH_BYTES per device, so at most
  * RDC_NOALLOC_MAX_PARTICLES particles are accepted (more returns RDC_ERR_INVALID_ARGUMENT) and the
@@ -232,7 +251,7 @@ int rdc_server_stats(rdc_server *s, uint64_t *particle_steps, uint64_t *bytes_in
  * *energy NaN. */
 #define RDC_NOALLOC_MAX_PARTICLES 65536
 #define RDC_NOALLOC_MAX_CELLS 131072
-#define RDC_NOALLOC_SCRATCH_BYTES 3181312
+#define RDC_NOALLOC_SCRATCH_BYTES 3185408
 int rdc_forces_noalloc(const rdc_context *ctx, int64_t n, const float *positions3, const int *types,
                        float *forces3, double *energy, void *stream);
 

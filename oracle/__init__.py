@@ -44,6 +44,11 @@ def _load():
             "orc_create": (vp, [P(d), P(i), d, i, P(d), u64, i, i]),
             "orc_destroy": (None, [vp]),
             "orc_last_error": (C.c_char_p, []),
+            "orc_add_box": (i, [vp, i, d, P(d), P(d), i]),
+            "orc_add_sphere": (i, [vp, i, d, P(d), d, i]),
+            "orc_add_capsule": (i, [vp, i, d, P(d), P(d), d, d, i]),
+            "orc_add_spherical_barrier": (i, [vp, i, d, d, P(d), d]),
+            "orc_add_cylinder": (i, [vp, i, d, P(d), P(d), d, i]),
             "orc_add_harmonic_repulsion": (i, [vp, i, i, d, d]),
             "orc_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
             "orc_add_lennard_jones": (i, [vp, i, i, C.c_uint, C.c_uint, d, i, d, d]),
@@ -112,6 +117,36 @@ class OracleSystem:
         if rc < 0:
             raise RuntimeError(self._lib.orc_last_error().decode())
         return rc
+
+    # order-1 (external) potentials
+    @staticmethod
+    def _v3(v):
+        return np.ascontiguousarray(v, dtype=np.float64).reshape(3)
+
+    def add_box(self, t, force_constant, origin, extent, inclusion=True):
+        o, e = self._v3(origin), self._v3(extent)
+        return self._check(self._lib.orc_add_box(self._h, t, force_constant, _ptr(o, C.c_double),
+                                                 _ptr(e, C.c_double), int(bool(inclusion))))
+
+    def add_sphere(self, t, force_constant, origin, radius, inclusion):
+        o = self._v3(origin)
+        return self._check(self._lib.orc_add_sphere(self._h, t, force_constant, _ptr(o, C.c_double), radius,
+                                                    int(bool(inclusion))))
+
+    def add_capsule(self, t, force_constant, center, direction, length, radius, inclusion=True):
+        c, v = self._v3(center), self._v3(direction)
+        return self._check(self._lib.orc_add_capsule(self._h, t, force_constant, _ptr(c, C.c_double),
+                                                     _ptr(v, C.c_double), length, radius, int(bool(inclusion))))
+
+    def add_spherical_barrier(self, t, height, width, origin, radius):
+        o = self._v3(origin)
+        return self._check(self._lib.orc_add_spherical_barrier(self._h, t, height, width, _ptr(o, C.c_double),
+                                                               radius))
+
+    def add_cylinder(self, t, force_constant, origin, normal, radius, inclusion):
+        o, n = self._v3(origin), self._v3(normal)
+        return self._check(self._lib.orc_add_cylinder(self._h, t, force_constant, _ptr(o, C.c_double),
+                                                      _ptr(n, C.c_double), radius, int(bool(inclusion))))
 
     # potentials
     def add_harmonic_repulsion(self, t1, t2, k, d):

@@ -79,6 +79,100 @@ struct Box {
     double dist2(V3 lhs, V3 rhs) const { V3 d = shortest(lhs, rhs); return dot(d, d); }
 };
 
+enum Pot1Kind { P1_BOX = 0, P1_SPHERE = 1, P1_CAPSULE = 2, P1_SPHERICAL_BARRIER = 3, P1_CYLINDER = 4 };
+
+/* order-1 (external) potentials, include/readdy/model/potentials/PotentialsOrder1.h:60-225 with the
+ * geometries of include/readdy/model/geometry.h */
+struct Pot1 {
+    int kind;
+    bool inclusion;
+    double k = 0;
+    V3 a, b;            // box v0/v1; sphere/capsule/barrier/cylinder centre or origin in a; direction/normal in b
+    double radius = 0, length = 0, height = 0, width = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0, keff = 0;
+
+    /* geometry::Sphere::smallestDifference, geometry.h:25-49 */
+    static V3 sphereDiff(V3 center, double radius, V3 position, bool inclusion) {
+        V3 delta = position - center;
+        double d2 = dot(delta, delta);
+        if (inclusion) {
+            if (d2 < radius * radius) return {0, 0, 0};
+            double d = std::sqrt(d2);
+            return delta * (d - radius) / d;
+        }
+        if (d2 > radius * radius) return {0, 0, 0};
+        double nrm = std::sqrt(d2);
+        if (nrm < 1e-5) return {-radius, 0, 0};
+        return (nrm - radius) * delta / norm(delta);
+    }
+    /* geometry::Box::smallestDifference, geometry.h:77-116 */
+    V3 boxDiff(V3 x) const {
+        V3 diff{0, 0, 0};
+        if (inclusion) {
+            for (int d = 0; d < 3; ++d) {
+                if (x[d] < a[d]) diff[d] = x[d] - a[d];
+                else if (x[d] > b[d]) diff[d] = x[d] - b[d];
+            }
+            return diff;
+        }
+        bool inside = true;
+        for (int d = 0; d < 3; ++d) inside = inside && x[d] > a[d] && x[d] < b[d];
+        if (!inside) return diff;
+        double diffs[6];
+        for (int d = 0; d < 3; ++d) { diffs[2 * d] = std::abs(x[d] - a[d]); diffs[2 * d + 1] = std::abs(x[d] - b[d]); }
+        int ix = (int)(std::min_element(diffs, diffs + 6) - diffs);
+        diff[ix / 2] = (ix % 2 == 0) ? x[ix / 2] - a[ix / 2] : x[ix / 2] - b[ix / 2];
+        return diff;
+    }
+    /* geometry::Capsule::closestCircleCenter, geometry.h:132-150 */
+    V3 capsuleCenter(V3 x) const {
+        V3 nd = b / norm(b);
+        V3 v = dot(x - a, nd) * nd;
+        double lambda = norm(v);
+        auto differ = [](double t1, double t2) { return (t1 >= 0 && t2 < 0) || (t1 < 0 && t2 >= 0); };
+        if (differ(v.x, nd.x) || differ(v.y, nd.y) || differ(v.z, nd.z)) lambda = -lambda;
+        lambda = std::clamp(lambda, -length / 2, length / 2);
+        return a + lambda * nd;
+    }
+    V3 geometryDiff(V3 x) const {
+        if (kind == P1_BOX) return boxDiff(x);
+        if (kind == P1_SPHERE) return sphereDiff(a, radius, x, inclusion);
+        return sphereDiff(capsuleCenter(x), radius, x, inclusion);
+    }
+    /* calculateForceAndEnergy of each class: force += F, energy += E */
+    void forceEnergy(V3 x, V3 &force, double &energy) const {
+        if (kind == P1_BOX || kind == P1_SPHERE || kind == P1_CAPSULE) {  // HarmonicGeometryPotential, :66-74
+            V3 d = geometryDiff(x);
+            energy += 0.5 * k * dot(d, d);
+            force += -1 * k * d;
+            return;
+        }
+        if (kind == P1_SPHERICAL_BARRIER) {  // SphericalBarrier, :103-146
+            V3 diff = x - a;
+            double dist = norm(diff);
+            if (dist < r1 || r4 <= dist) return;
+            if (dist < r2) {
+                energy += 0.5 * keff * std::pow(dist - radius + width, 2.);
+                force += -keff * (dist - radius + width) * diff / dist;
+            } else if (dist < r3) {
+                energy += height - 0.5 * keff * std::pow(dist - radius, 2.);
+                force += keff * (dist - radius) * diff / dist;
+            } else {
+                energy += 0.5 * keff * std::pow(dist - radius - width, 2.);
+                force += -keff * (dist - radius - width) * diff / dist;
+            }
+            return;
+        }
+        // Cylinder, :168-209
+        V3 pos = x - a;
+        V3 perp = pos - dot(pos, b) * b;
+        double dist = norm(perp);
+        if ((inclusion && dist > radius) || (!inclusion && dist < radius)) {
+            energy += 0.5 * k * std::pow(dist - radius, 2.);
+            force += -k * (dist - radius) * perp / dist;
+        }
+    }
+};
+
 enum PotKind { HARMONIC_REPULSION = 0, WEAK_PIECEWISE_HARMONIC = 1, LENNARD_JONES = 2, SCREENED_ELECTROSTATICS = 3 };
 
 struct Pot2 {
@@ -281,6 +375,7 @@ struct orc_system {
     std::vector<double> D;
     int nTypes;
     std::map<std::pair<int, int>, std::vector<Pot2>> pot2;          // symmetric key (min,max)
+    std::vector<std::vector<Pot1>> pot1;                           // by type
     std::vector<std::vector<const Reaction *>> o1;                 // by type
     std::map<std::pair<int, int>, std::vector<const Reaction *>> o2;  // symmetric key
     std::vector<Reaction *> reactions;
@@ -312,6 +407,7 @@ struct orc_system {
         for (int d = 0; d < 3; ++d) { box.L[d] = b[d]; box.pbc[d] = p[d] != 0; }
         D.assign(diff, diff + nt);
         o1.resize(nt);
+        pot1.resize(nt);
         std::seed_seq ss{(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32), 0x5eedu};
         std::vector<uint32_t> seeds(pool.size());
         ss.generate(seeds.begin(), seeds.end());
@@ -437,8 +533,11 @@ struct orc_system {
     /* CPUCalculateForces::perform, kernels/cpu/src/actions/CPUCalculateForces.cpp:46-212 */
     double calculateForces() {
         energy = 0;
-        if (pot2.empty() && bonds.empty() && angles.empty() && dihedrals.empty()) return 0;
+        bool any1 = false;
+        for (auto &v : pot1) any1 = any1 || !v.empty();
+        if (!any1 && pot2.empty() && bonds.empty() && angles.empty() && dihedrals.empty()) return 0;
         for (auto &e : entries) { e.force = {0, 0, 0}; e.fscale = 0; }
+        if (any1) energy += order1();
         int nt = pool.size();
         std::vector<double> part(nt, 0.);
         if (!bonds.empty() || !angles.empty() || !dihedrals.empty()) energy += bondedForces();
@@ -452,6 +551,20 @@ struct orc_system {
             for (double p : part) energy += p;
         }
         return energy;
+    }
+    /* calculateOrder1, CPUCalculateForces.cpp:295-314 */
+    double order1() {
+        double eUpd = 0;
+        for (auto &e : entries) {
+            if (e.deactivated) continue;
+            for (const auto &p : pot1[e.type]) {
+                V3 upd{0, 0, 0};
+                p.forceEnergy(e.pos, upd, eUpd);
+                e.force += upd;
+                e.fscale += norm(upd);
+            }
+        }
+        return eUpd;
     }
     /* calculateOrder2<false>, CPUCalculateForces.cpp:214-268 */
     double order2(size_t cb, size_t ce) {
@@ -911,6 +1024,50 @@ static int addPot(orc_system *s, int t1, int t2, Pot2 p) {
     s->pot2[orc_system::key(t1, t2)].push_back(p);
     return 0;
 }
+static int addPot1(orc_system *s, int t, const Pot1 &p) {
+    if (t < 0 || t >= s->nTypes) { g_err = "type out of range"; return -1; }
+    s->pot1[t].push_back(p);
+    return 0;
+}
+static V3 v3(const double *a) { return V3{a[0], a[1], a[2]}; }
+/* PotentialRegistry::addBox / addHarmonicGeometry(Box) (PotentialRegistry.h:99-112, 335-345): v1 = origin + extent */
+int orc_add_box(orc_system *s, int t, double k, const double *origin, const double *extent, int inclusion) {
+    Pot1 p{P1_BOX, inclusion != 0};
+    p.k = k; p.a = v3(origin); p.b = v3(origin) + v3(extent);
+    return addPot1(s, t, p);
+}
+/* PotentialRegistry::addSphere (:253-270) */
+int orc_add_sphere(orc_system *s, int t, double k, const double *origin, double radius, int inclusion) {
+    Pot1 p{P1_SPHERE, inclusion != 0};
+    p.k = k; p.a = v3(origin); p.radius = radius;
+    return addPot1(s, t, p);
+}
+/* PotentialRegistry::addCapsule / addHarmonicGeometry(Capsule) (:274-293) */
+int orc_add_capsule(orc_system *s, int t, double k, const double *center, const double *direction, double length,
+                    double radius, int inclusion) {
+    Pot1 p{P1_CAPSULE, inclusion != 0};
+    p.k = k; p.a = v3(center); p.b = v3(direction); p.length = length; p.radius = radius;
+    return addPot1(s, t, p);
+}
+/* PotentialRegistry::addSphericalBarrier (:305-317), SphericalBarrier ctor (Potentials.cpp:86-92) */
+int orc_add_spherical_barrier(orc_system *s, int t, double height, double width, const double *origin,
+                              double radius) {
+    if (width > radius) { g_err = "SphericalBarrier must have a radius larger than its width"; return -1; }
+    Pot1 p{P1_SPHERICAL_BARRIER, true};
+    p.a = v3(origin); p.radius = radius; p.height = height; p.width = width;
+    p.r1 = radius - width; p.r2 = radius - width / 2.; p.r3 = radius + width / 2.; p.r4 = radius + width;
+    p.keff = 4. * height / width / width;
+    return addPot1(s, t, p);
+}
+/* PotentialRegistry::addCylinder (:330-...), Cylinder ctor normalises the normal (PotentialsOrder1.h:160-163) */
+int orc_add_cylinder(orc_system *s, int t, double k, const double *origin, const double *normal, double radius,
+                     int inclusion) {
+    Pot1 p{P1_CYLINDER, inclusion != 0};
+    V3 n = v3(normal);
+    p.k = k; p.a = v3(origin); p.b = n / norm(n); p.radius = radius;
+    return addPot1(s, t, p);
+}
+
 int orc_add_harmonic_repulsion(orc_system *s, int t1, int t2, double k, double d) {
     Pot2 p{HARMONIC_REPULSION, {k, d, d * d}, d * d};
     return addPot(s, t1, t2, p);

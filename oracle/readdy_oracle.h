@@ -26,6 +26,15 @@ void orc_destroy(orc_system *s);
 const char *orc_last_error(void);
 
 /* pair potentials (PotentialsOrder2.h); return 0 on success */
+/* order-1 (external) potentials (include/readdy/model/potentials/PotentialsOrder1.h) */
+int orc_add_box(orc_system *s, int type, double k, const double *origin3, const double *extent3, int inclusion);
+int orc_add_sphere(orc_system *s, int type, double k, const double *origin3, double radius, int inclusion);
+int orc_add_capsule(orc_system *s, int type, double k, const double *center3, const double *direction3, double length,
+                    double radius, int inclusion);
+int orc_add_spherical_barrier(orc_system *s, int type, double height, double width, const double *origin3,
+                              double radius);
+int orc_add_cylinder(orc_system *s, int type, double k, const double *origin3, const double *normal3, double radius,
+                     int inclusion);
 int orc_add_harmonic_repulsion(orc_system *s, int t1, int t2, double k, double interaction_distance);
 int orc_add_weak_interaction_piecewise_harmonic(orc_system *s, int t1, int t2, double k, double desired_distance,
                                                 double depth, double no_interaction_distance);

@@ -47,6 +47,11 @@ def _sig(lib):
         "rdc_context_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
         "rdc_context_add_lennard_jones": (i, [vp, i, i, C.c_uint, C.c_uint, d, i, d, d]),
         "rdc_context_add_screened_electrostatics": (i, [vp, i, i, d, d, d, d, C.c_uint, d]),
+        "rdc_context_add_box": (i, [vp, i, d, P(d), P(d), i]),
+        "rdc_context_add_sphere": (i, [vp, i, d, P(d), d, i]),
+        "rdc_context_add_capsule": (i, [vp, i, d, P(d), P(d), d, d, i]),
+        "rdc_context_add_spherical_barrier": (i, [vp, i, d, d, P(d), d]),
+        "rdc_context_add_cylinder": (i, [vp, i, d, P(d), P(d), d, i]),
         "rdc_context_add_conversion": (i, [vp, i, i, d, P(i)]),
         "rdc_context_add_decay": (i, [vp, i, d, P(i)]),
         "rdc_context_add_fusion": (i, [vp, i, i, i, d, d, d, d, P(i)]),

@@ -231,6 +231,61 @@ void build_tables(const ContextData &c, const double box[3], double dt, Tables &
         t.has_o2_any = 1;
         for (int r : kv.second) t.o2_list[k++] = r;
     }
+    // order-1 potentials grouped by type, registration order kept within a type
+    int q = 0;
+    for (int ty = 0; ty < T; ++ty) {
+        const int first = q;
+        for (const auto &h : c.o1pots) {
+            if (h.type != ty) continue;
+            if (q >= MAX_O1_POTENTIALS) throw InvalidArgument("too many order-1 potentials");
+            O1Pot &o = t.o1pots[q++];
+            o.kind = h.kind;
+            o.inclusion = h.inclusion;
+            float *p = o.p;
+            switch (h.kind) {
+                case O1_BOX:
+                    p[0] = (float)h.k;
+                    for (int d = 0; d < 3; ++d) { p[1 + d] = (float)h.a[d]; p[4 + d] = (float)(h.a[d] + h.b[d]); }
+                    break;
+                case O1_SPHERE:
+                    p[0] = (float)h.k;
+                    for (int d = 0; d < 3; ++d) p[1 + d] = (float)h.a[d];
+                    p[4] = (float)h.radius;
+                    split_ff(h.radius * h.radius, p[5], p[6]);
+                    break;
+                case O1_CAPSULE: {
+                    const double nn = std::sqrt(h.b[0] * h.b[0] + h.b[1] * h.b[1] + h.b[2] * h.b[2]);
+                    p[0] = (float)h.k;
+                    for (int d = 0; d < 3; ++d) { p[1 + d] = (float)h.a[d]; split_ff(h.b[d] / nn, p[4 + d], p[11 + d]); }
+                    p[7] = (float)(h.length / 2);
+                    p[8] = (float)h.radius;
+                    split_ff(h.radius * h.radius, p[9], p[10]);
+                    break;
+                }
+                case O1_SPHERICAL_BARRIER:
+                    for (int d = 0; d < 3; ++d) p[d] = (float)h.a[d];
+                    p[3] = (float)h.radius;
+                    split_ff(h.radius * h.radius, p[11], p[12]);
+                    p[4] = (float)h.width;
+                    p[5] = (float)h.height;
+                    p[6] = (float)(4.0 * h.height / h.width / h.width);
+                    p[7] = (float)(h.radius - h.width);
+                    p[8] = (float)(h.radius - h.width / 2.0);
+                    p[9] = (float)(h.radius + h.width / 2.0);
+                    p[10] = (float)(h.radius + h.width);
+                    break;
+                case O1_CYLINDER: {
+                    const double nn = std::sqrt(h.b[0] * h.b[0] + h.b[1] * h.b[1] + h.b[2] * h.b[2]);
+                    p[0] = (float)h.k;
+                    for (int d = 0; d < 3; ++d) { p[1 + d] = (float)h.a[d]; split_ff(h.b[d] / nn, p[4 + d], p[10 + d]); }
+                    p[7] = (float)h.radius;
+                    split_ff(h.radius * h.radius, p[8], p[9]);
+                    break;
+                }
+            }
+        }
+        t.o1pot_tab[ty] = q > first ? ((first << 8) | (q - first)) : 0;
+    }
     set_time_step(c, dt, t);
 }
 
@@ -809,6 +864,59 @@ int rdc_context_max_cutoff(const rdc_context *ctx, double *cutoff) {
 static void check_types(const rdc_context *ctx, std::initializer_list<int> ts) {
     require(ctx != nullptr, "null context");
     for (int t : ts) require(t >= 0 && t < ctx->d.ntypes, "particle type out of range");
+}
+
+static void add_o1(rdc_context *ctx, int type, int kind, int inclusion, double k, const double *a, const double *b,
+                   double radius, double length, double height, double width) {
+    HostO1 h{type, kind, inclusion ? 1 : 0, k, {0, 0, 0}, {0, 0, 0}, radius, length, height, width};
+    for (int d = 0; d < 3; ++d) {
+        h.a[d] = a[d];
+        if (b) h.b[d] = b[d];
+    }
+    ctx->d.o1pots.push_back(h);
+}
+int rdc_context_add_box(rdc_context *ctx, int type, double k, const double origin[3], const double extent[3],
+                        int inclusion) {
+    return guarded([&] {
+        check_types(ctx, {type});
+        require(origin && extent, "null argument");
+        add_o1(ctx, type, O1_BOX, inclusion, k, origin, extent, 0, 0, 0, 0);
+    });
+}
+int rdc_context_add_sphere(rdc_context *ctx, int type, double k, const double origin[3], double radius, int inclusion) {
+    return guarded([&] {
+        check_types(ctx, {type});
+        require(origin != nullptr, "null argument");
+        add_o1(ctx, type, O1_SPHERE, inclusion, k, origin, nullptr, radius, 0, 0, 0);
+    });
+}
+int rdc_context_add_capsule(rdc_context *ctx, int type, double k, const double center[3], const double direction[3],
+                            double length, double radius, int inclusion) {
+    return guarded([&] {
+        check_types(ctx, {type});
+        require(center && direction, "null argument");
+        require(direction[0] != 0 || direction[1] != 0 || direction[2] != 0, "capsule direction must be nonzero");
+        add_o1(ctx, type, O1_CAPSULE, inclusion, k, center, direction, radius, length, 0, 0);
+    });
+}
+int rdc_context_add_spherical_barrier(rdc_context *ctx, int type, double height, double width, const double origin[3],
+                                      double radius) {
+    return guarded([&] {
+        check_types(ctx, {type});
+        require(origin != nullptr, "null argument");
+        require(width > 0, "spherical barrier width must be > 0");
+        require(!(width > radius), "SphericalBarrier must have a radius larger than its width");  // Potentials.cpp:89-91
+        add_o1(ctx, type, O1_SPHERICAL_BARRIER, 1, 0, origin, nullptr, radius, 0, height, width);
+    });
+}
+int rdc_context_add_cylinder(rdc_context *ctx, int type, double k, const double origin[3], const double normal[3],
+                             double radius, int inclusion) {
+    return guarded([&] {
+        check_types(ctx, {type});
+        require(origin && normal, "null argument");
+        require(normal[0] != 0 || normal[1] != 0 || normal[2] != 0, "cylinder normal must be nonzero");
+        add_o1(ctx, type, O1_CYLINDER, inclusion, k, origin, normal, radius, 0, 0, 0);
+    });
 }
 
 int rdc_context_add_harmonic_repulsion(rdc_context *ctx, int t1, int t2, double k, double d) {

@@ -496,6 +496,163 @@ __device__ inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z *
 // harmonic bond: E = k (r - l0)^2, force on i = 2k (r-l0)/r x_ij, on j its negative
 // (BondedPotential.h:105-113, CPUTopologyActions.cpp:61-74); r - l0 = (d2 - l0^2) / (r + l0)
 // from the float-float d2.  P = (k, l0, l0^2 hi, l0^2 lo)
+// ------------------------------------------------------------------------------------------------
+// order-1 (external) potentials (include/readdy/model/potentials/PotentialsOrder1.h:60-225, geometries of
+// include/readdy/model/geometry.h).  Differences to the geometry come from TwoSum, and every (d - r)
+// near a surface is formed as (d^2 - r^2)/(d + r) from a float-float d^2, so forces keep their digits
+// where they vanish.
+// ------------------------------------------------------------------------------------------------
+struct FF3 { F3 hi, lo; };
+__device__ inline FF3 diff_ff(float4 x, const float *c) {  // x - c, exactly
+    FF3 r;
+    r.hi.x = __fsub_rn(x.x, c[0]); r.lo.x = two_sum_err(x.x, -c[0], r.hi.x);
+    r.hi.y = __fsub_rn(x.y, c[1]); r.lo.y = two_sum_err(x.y, -c[1], r.hi.y);
+    r.hi.z = __fsub_rn(x.z, c[2]); r.lo.z = two_sum_err(x.z, -c[2], r.hi.z);
+    return r;
+}
+__device__ inline FF norm2_ff(const FF3 &v) {  // |hi + lo|^2 as float-float, to first order in lo
+    const float px = __fmul_rn(v.hi.x, v.hi.x), py = __fmul_rn(v.hi.y, v.hi.y), pz = __fmul_rn(v.hi.z, v.hi.z);
+    const float s1 = __fadd_rn(px, py);
+    const float t1 = two_sum_err(px, py, s1);
+    const float h = __fadd_rn(s1, pz);
+    const float t2 = two_sum_err(s1, pz, h);
+    const float e = sq_err(v.hi.x, v.lo.x, px) + sq_err(v.hi.y, v.lo.y, py) + sq_err(v.hi.z, v.lo.z, pz);
+    return FF{h, __fadd_rn(__fadd_rn(t1, t2), e)};
+}
+__device__ inline F3 ff_value(const FF3 &v) { return v.hi + v.lo; }
+
+// v + s * u as float-float (v float-float, s and u FP32): the products' rounding errors are kept
+__device__ inline FF3 axpy_ff(const FF3 &v, float s, F3 u) {
+    auto one = [&](float vh, float vl, float uu) {
+        const float ph = __fmul_rn(s, uu), pe = __fmaf_rn(s, uu, -ph);
+        const float h = __fadd_rn(vh, ph);
+        return FF{h, __fadd_rn(__fadd_rn(two_sum_err(vh, ph, h), vl), pe)};
+    };
+    const FF x = one(v.hi.x, v.lo.x, u.x), y = one(v.hi.y, v.lo.y, u.y), z = one(v.hi.z, v.lo.z, u.z);
+    return FF3{f3(x.hi, y.hi, z.hi), f3(x.lo, y.lo, z.lo)};
+}
+
+// (ah + al) x (bh + bl) as float-float: a1 b2 - a2 b1 per component with both products' rounding
+// errors and the first-order low-part terms kept
+__device__ inline FF3 cross_ff3(const FF3 &a, const FF3 &b) {
+    auto one = [](float a1h, float a1l, float b2h, float b2l, float a2h, float a2l, float b1h, float b1l) {
+        const float p1 = __fmul_rn(a1h, b2h), e1 = __fmaf_rn(a1h, b2h, -p1);
+        const float p2 = __fmul_rn(a2h, b1h), e2 = __fmaf_rn(a2h, b1h, -p2);
+        const float h = __fsub_rn(p1, p2);
+        const float l = two_sum_err(p1, -p2, h) + (e1 - e2) + (a1l * b2h - a2l * b1h) + (a1h * b2l - a2h * b1l);
+        return FF{h, l};
+    };
+    const FF x = one(a.hi.y, a.lo.y, b.hi.z, b.lo.z, a.hi.z, a.lo.z, b.hi.y, b.lo.y);
+    const FF y = one(a.hi.z, a.lo.z, b.hi.x, b.lo.x, a.hi.x, a.lo.x, b.hi.z, b.lo.z);
+    const FF z = one(a.hi.x, a.lo.x, b.hi.y, b.lo.y, a.hi.y, a.lo.y, b.hi.x, b.lo.x);
+    return FF3{f3(x.hi, y.hi, z.hi), f3(x.lo, y.lo, z.lo)};
+}
+
+// geometry::Sphere::smallestDifference (geometry.h:25-49) for a difference `delta` from the centre
+__device__ inline F3 sphere_diff(const FF3 &delta, float radius, float r2hi, float r2lo, int inclusion) {
+    const FF d2 = norm2_ff(delta);
+    const float d2f = __fadd_rn(d2.hi, d2.lo);
+    if (inclusion ? d2f < r2hi : d2f > r2hi) return f3(0.f, 0.f, 0.f);
+    const float d = sqrtf(d2f);
+    if (!inclusion && d < 1e-5f) return f3(-radius, 0.f, 0.f);
+    const float dr = ff_sub(d2, r2hi, r2lo) / (d + radius);  // d - r
+    return (dr / d) * ff_value(delta);
+}
+
+// adds the force and energy of the order-1 potentials first..first+cnt-1 on a particle at p
+__device__ inline void order1_force(float4 p, const O1Pot *pots, int first, int cnt, float &fx, float &fy, float &fz,
+                                    float &e) {
+    for (int q = first; q < first + cnt; ++q) {
+        const O1Pot &o = pots[q];
+        const float *P = o.p;
+        F3 f = f3(0.f, 0.f, 0.f);
+        switch (o.kind) {
+            case O1_BOX: {  // HarmonicGeometryPotential<Box>, geometry.h:77-116
+                const float x[3] = {p.x, p.y, p.z};
+                float dv[3] = {0.f, 0.f, 0.f};
+                if (o.inclusion) {
+                    for (int d = 0; d < 3; ++d) {
+                        if (x[d] < P[1 + d]) dv[d] = x[d] - P[1 + d];
+                        else if (x[d] > P[4 + d]) dv[d] = x[d] - P[4 + d];
+                    }
+                } else {
+                    bool inside = true;
+                    for (int d = 0; d < 3; ++d) inside = inside && x[d] > P[1 + d] && x[d] < P[4 + d];
+                    if (inside) {  // nearest face; the first minimum wins, like std::min_element
+                        int best = 0;
+                        float bd = fabsf(x[0] - P[1]);
+                        for (int k = 1; k < 6; ++k) {
+                            const float v = fabsf(x[k / 2] - P[(k % 2 == 0 ? 1 : 4) + k / 2]);
+                            if (v < bd) { bd = v; best = k; }
+                        }
+                        dv[best / 2] = x[best / 2] - P[(best % 2 == 0 ? 1 : 4) + best / 2];
+                    }
+                }
+                e += 0.5f * P[0] * (dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+                f = f3(-P[0] * dv[0], -P[0] * dv[1], -P[0] * dv[2]);
+                break;
+            }
+            case O1_SPHERE: {  // HarmonicGeometryPotential<Sphere>
+                const F3 dv = sphere_diff(diff_ff(p, P + 1), P[4], P[5], P[6], o.inclusion);
+                e += 0.5f * P[0] * dot(dv, dv);
+                f = (-P[0]) * dv;
+                break;
+            }
+            case O1_CAPSULE: {  // HarmonicGeometryPotential<Capsule>, closest circle centre geometry.h:132-150
+                const FF3 xc = diff_ff(p, P + 1);
+                const F3 n = f3(P[4], P[5], P[6]);
+                const float lambda = fminf(P[7], fmaxf(-P[7], dot(ff_value(xc), n)));
+                FF3 delta = axpy_ff(xc, -lambda, n);  // x - (c + lambda n) as float-float, n = hi + lo
+                delta.lo = delta.lo + (-lambda) * f3(P[11], P[12], P[13]);
+                const F3 dv = sphere_diff(delta, P[8], P[9], P[10], o.inclusion);
+                e += 0.5f * P[0] * dot(dv, dv);
+                f = (-P[0]) * dv;
+                break;
+            }
+            case O1_SPHERICAL_BARRIER: {  // SphericalBarrier, PotentialsOrder1.h:103-146
+                const FF3 df = diff_ff(p, P);
+                const FF d2 = norm2_ff(df);
+                const float dist = sqrtf(__fadd_rn(d2.hi, d2.lo));
+                const float radius = P[3], width = P[4], height = P[5], keff = P[6];
+                if (dist < P[7] || P[10] <= dist) break;
+                const float dr = ff_sub(d2, P[11], P[12]) / (dist + radius);  // dist - radius
+                const F3 u = (1.0f / dist) * ff_value(df);
+                if (dist < P[8]) {
+                    const float s = dr + width;
+                    e += 0.5f * keff * s * s;
+                    f = (-keff * s) * u;
+                } else if (dist < P[9]) {
+                    e += height - 0.5f * keff * dr * dr;
+                    f = (keff * dr) * u;
+                } else {
+                    const float s = dr - width;
+                    e += 0.5f * keff * s * s;
+                    f = (-keff * s) * u;
+                }
+                break;
+            }
+            case O1_CYLINDER: {  // Cylinder, PotentialsOrder1.h:168-209; perp = n x (pos x n)
+                const FF3 pos = diff_ff(p, P + 1);
+                const F3 n = f3(P[4], P[5], P[6]);
+                const FF3 pxn = cross_ff3(pos, FF3{n, f3(P[10], P[11], P[12])});
+                const FF d2 = norm2_ff(pxn);
+                const float dist = sqrtf(__fadd_rn(d2.hi, d2.lo));
+                const float radius = P[7];
+                if (o.inclusion ? dist > radius : dist < radius) {
+                    const F3 perp = cross_k(n, ff_value(pxn));
+                    const float dr = ff_sub(d2, P[8], P[9]) / (dist + radius);
+                    e += 0.5f * P[0] * dr * dr;
+                    f = (-P[0] * dr / dist) * perp;
+                }
+                break;
+            }
+        }
+        fx += f.x;
+        fy += f.y;
+        fz += f.z;
+    }
+}
+
 __device__ inline F3 bond_force(float4 pi, float4 pj, float4 P, const Geo &g, int role, float &e) {
     const PairExact x = pair_exact(pi, pj, g);
     const float r = sqrtf(__fadd_rn(x.d2.hi, x.d2.lo));

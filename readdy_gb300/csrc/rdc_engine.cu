@@ -206,6 +206,10 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
         if (i < n_in && NP > 0) pair_force_at(i, p, posX, cells, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e);
         const uint32_t id = idX[i];
         const int t = itype(p);
+        if (t >= 0) {  // order-1 potentials
+            const int o1 = tab->o1pot_tab[t];
+            if (o1) order1_force(p, tab->o1pots, o1 >> 8, o1 & 0xff, fx, fy, fz, e);
+        }
         const float4 q = euler_bd(p, fx, fy, fz, id, D.seed, step, S.drift[t], S.scale[t], g);
         posY[i] = q;
         idY[i] = id;

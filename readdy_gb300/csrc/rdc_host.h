@@ -38,6 +38,11 @@ struct HostReaction {
     int educt[2], product[2];
     double rate, educt_distance, product_distance, w1, w2;
 };
+struct HostO1 {
+    int type;
+    int kind, inclusion;
+    double k, a[3], b[3], radius, length, height, width;
+};
 struct BondCfg { int t1, t2; double k, l0; };
 struct AngleCfg { int t1, t2, t3; double k, theta0; };
 struct DihedralCfg { int t1, t2, t3, t4; double k, mult, phi0; };
@@ -49,6 +54,7 @@ struct ContextData {
     int ntypes;
     std::vector<double> D;
     std::vector<HostPot> pots;
+    std::vector<HostO1> o1pots;
     std::vector<HostReaction> reactions;
     std::vector<BondCfg> bonds;
     std::vector<AngleCfg> angles;
@@ -74,6 +80,8 @@ struct Tables {
     int o2_tab[MAX_TYPES * MAX_TYPES];     // (first << 8) | count into o2_list
     int o2_list[MAX_REACTIONS * 2];
     int o2_any[MAX_TYPES];                 // type has any order-2 reaction
+    int o1pot_tab[MAX_TYPES];              // (first << 8) | count into o1pots
+    O1Pot o1pots[MAX_O1_POTENTIALS];
 };
 
 // builds the tables from a context for a box (band widths depend on the GPU machine) and time step

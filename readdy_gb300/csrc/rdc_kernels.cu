@@ -181,8 +181,13 @@ __global__ void __launch_bounds__(FORCE_THREADS, 2) k_pair_forces(SysDev s) {
     double esum = 0.0;
     GRID_STRIDE(i, n) {
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-        if (i < n_in && NP > 0)
-            pair_force_at(i, s.pos[i], s.pos, s.start, g, s.radius, sh_tab, sh_scr, sh_pots, T, fx, fy, fz, e);
+        const float4 p = s.pos[i];
+        if (i < n_in && NP > 0) pair_force_at(i, p, s.pos, s.start, g, s.radius, sh_tab, sh_scr, sh_pots, T, fx, fy, fz, e);
+        const int ti = itype(p);
+        if (ti >= 0) {  // order-1 potentials act on every active particle, in the box or not (CPUCalculateForces.cpp:295-314)
+            const int o1 = tab->o1pot_tab[ti];
+            if (o1) order1_force(p, tab->o1pots, o1 >> 8, o1 & 0xff, fx, fy, fz, e);
+        }
         s.force[i] = make_float4(fx, fy, fz, e);
         esum += (double)e;
     }

@@ -7,6 +7,7 @@ namespace rdc {
 constexpr int MAX_TYPES = 32;          // particle species per system
 constexpr int MAX_PAIR_POTENTIALS = 128;
 constexpr int MAX_REACTIONS = 64;
+constexpr int MAX_O1_POTENTIALS = 64;  // order-1 (external) potentials per system
 constexpr int RESOLVE_MAX_EVENTS = 8192;  // accepted events one step may resolve (device-checked)
 
 enum PotKind : int {
@@ -14,6 +15,21 @@ enum PotKind : int {
     POT_WEAK_PIECEWISE_HARMONIC = 1,
     POT_LENNARD_JONES = 2,
     POT_SCREENED_ELECTROSTATICS = 3,
+};
+
+// order-1 (external) potentials, include/readdy/model/potentials/PotentialsOrder1.h
+enum O1Kind : int { O1_BOX = 0, O1_SPHERE = 1, O1_CAPSULE = 2, O1_SPHERICAL_BARRIER = 3, O1_CYLINDER = 4 };
+
+// Parameters in FP32 (positions are FP32 on the device).  Layouts of p[]:
+//   box:      k, v0[3], v1[3]
+//   sphere:   k, centre[3], radius, radius^2 (hi, lo)
+//   capsule:  k, centre[3], unit direction[3] (hi), length/2, radius, radius^2 (hi, lo), direction (lo)
+//   barrier:  centre[3], radius, width, height, keff, r1, r2, r3, r4, radius^2 (hi, lo)
+//   cylinder: k, origin[3], unit normal[3] (hi), radius, radius^2 (hi, lo), normal (lo)
+struct O1Pot {
+    int kind;
+    int inclusion;
+    float p[14];
 };
 
 enum ReactionKind : int { R_CONVERSION = 0, R_FUSION = 1, R_FISSION = 2, R_ENZYMATIC = 3, R_DECAY = 4 };

@@ -74,6 +74,31 @@ class Context:
             self._h, t1, t2, electrostatic_strength, inverse_screening_depth, repulsion_strength,
             repulsion_distance, exponent, cutoff))
 
+    # order-1 (external) potentials, names and argument order of api/registry/potentials.py
+    @staticmethod
+    def _v3(v):
+        return (C.c_double * 3)(*[float(x) for x in v])
+
+    def add_box(self, particle_type, force_constant, origin, extent, inclusion=True):
+        N.check(self._lib.rdc_context_add_box(self._h, particle_type, force_constant, self._v3(origin),
+                                              self._v3(extent), int(bool(inclusion))))
+
+    def add_sphere(self, particle_type, force_constant, origin, radius, inclusion):
+        N.check(self._lib.rdc_context_add_sphere(self._h, particle_type, force_constant, self._v3(origin), radius,
+                                                 int(bool(inclusion))))
+
+    def add_capsule(self, particle_type, force_constant, center, direction, length, radius, inclusion=True):
+        N.check(self._lib.rdc_context_add_capsule(self._h, particle_type, force_constant, self._v3(center),
+                                                  self._v3(direction), length, radius, int(bool(inclusion))))
+
+    def add_spherical_barrier(self, particle_type, height, width, origin, radius):
+        N.check(self._lib.rdc_context_add_spherical_barrier(self._h, particle_type, height, width,
+                                                            self._v3(origin), radius))
+
+    def add_cylinder(self, particle_type, force_constant, origin, normal, radius, inclusion):
+        N.check(self._lib.rdc_context_add_cylinder(self._h, particle_type, force_constant, self._v3(origin),
+                                                   self._v3(normal), radius, int(bool(inclusion))))
+
     # ReactionRegistry
     def _rid(self, rc, rid):
         N.check(rc)

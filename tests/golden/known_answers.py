@@ -150,6 +150,47 @@ REACTION_CASES = [
 
 # Michaelis-Menten integration test, readdy/test/IntegrationTests.cpp:30-106:
 # <S> over 37,500 steps must lie within 3 % of 665.2.
+# order-1 (external) potentials: (kind, type, args in Context.add_<kind> order after the type)
+EXTERNAL_CASES = [
+    dict(name="spherical_membrane", source="readdy/test/TestPotentials.cpp:168-214",
+         box=(10., 10., 10.), periodic=(True, True, True),
+         potentials=[("sphere", 0, (1.0, (1., 0., 0.), 3.0, False)), ("sphere", 0, (1.0, (1., 0., 0.), 3.0, True))],
+         positions=[(2., 1., 1.), (4., 3., -3.)], types=[0, 0],
+         energy=0.803847577293 + 2.41154273188,
+         forces=[(0.73205081, 0.73205081, 0.73205081), (-1.26794919, -1.26794919, 1.26794919)], force_atol=1e-6),
+    dict(name="spherical_barrier", source="readdy/test/TestPotentials.cpp:216-259",
+         box=(10., 10., 10.), periodic=(True, True, True),
+         potentials=[("spherical_barrier", 0, (2.0, 0.3, (1.0, 0.9, 1.0), 1.0))],
+         positions=[(2.1, 1., 1.), (1.1, 1., 1.)], types=[0, 0],
+         energy=1.51432015278, forces=[(9.2539372, 0.84126702, 0.), (0., 0., 0.)], force_atol=1e-5),
+    dict(name="cylinder_inclusion", source="readdy/test/TestPotentials.cpp:261-317",
+         box=(20., 20., 20.), periodic=(True, True, True),
+         potentials=[("cylinder", 0, (4.0, (1., -2., 3.), (0., 0., 1.), 2.0, True))],
+         positions=[(-1., -4., 1.), (0., -3., 3.), (1.5, -1., 5.), (4., -2., 8.)], types=[0, 0, 0, 0],
+         energy=3.37258300203048,
+         forces=[(2.3431457505076203, 2.3431457505076203, 0.), (0., 0., 0.), (0., 0., 0.), (-4., 0., 0.)],
+         force_atol=1e-5),
+    dict(name="cylinder_exclusion", source="readdy/test/TestPotentials.cpp:319-375",
+         box=(20., 20., 20.), periodic=(True, True, True),
+         potentials=[("cylinder", 0, (4.0, (1., -2., 3.), (0., 0., 1.), 2.0, False))],
+         positions=[(-1., -4., 1.), (0., -3., 3.), (1.5, -1., 5.), (4., -2., 8.)], types=[0, 0, 0, 0],
+         energy=2.2420195910160805,
+         forces=[(0., 0., 0.), (-1.6568542494923801, -1.6568542494923801, 0.),
+                 (0.5 * 3.155417527999327, 3.155417527999327, 0.), (0., 0., 0.)], force_atol=1e-5),
+    # worked by hand from geometry::Box / geometry::Capsule (include/readdy/model/geometry.h:77-162)
+    dict(name="box_inclusion_and_exclusion", source="geometry.h:77-116 (hand-worked)",
+         box=(10., 10., 10.), periodic=(True, True, True),
+         potentials=[("box", 0, (10.0, (-1., -1., -1.), (2., 2., 2.), True)),
+                     ("box", 1, (10.0, (-1., -1., -1.), (2., 2., 2.), False))],
+         positions=[(1.5, 0., -2.), (0.75, 0.125, 0.)], types=[0, 1],
+         energy=6.25 + 0.3125, forces=[(-5., 0., 10.), (2.5, 0., 0.)], force_atol=1e-6),
+    dict(name="capsule_inclusion", source="geometry.h:118-162 (hand-worked)",
+         box=(10., 10., 10.), periodic=(True, True, True),
+         potentials=[("capsule", 0, (2.0, (0., 0., 0.), (0., 0., 2.), 4.0, 1.0, True))],
+         positions=[(0., 2., 1.), (0., 0., 3.5), (0., 0.5, -1.5)], types=[0, 0, 0],
+         energy=1.0 + 0.25, forces=[(0., -2., 0.), (0., 0., -1.), (0., 0., 0.)], force_atol=1e-6),
+]
+
 MICHAELIS_MENTEN = dict(
     source="readdy/test/IntegrationTests.cpp:30-106",
     box=(10., 10., 10.), periodic=(True, True, True),

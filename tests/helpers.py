@@ -22,6 +22,8 @@ def make_context(spec):
                      spec["diffusion"])
     for kind, t1, t2, p in spec.get("potentials", []):
         getattr(ctx, "add_" + kind)(t1, t2, *_pot_args(kind, p))
+    for kind, t, args in spec.get("externals", []):
+        getattr(ctx, "add_" + kind)(t, *args)
     for kind, p in spec.get("reactions", []):
         if kind == "fusion":
             ctx.add_fusion(p["a"], p["b"], p["c"], p["rate"], p["educt_distance"], p.get("w1", .5), p.get("w2", .5))
@@ -43,6 +45,8 @@ def make_oracle(spec, seed=1, n_threads=1, cll_radius=1):
                             spec["diffusion"], seed=seed, n_threads=n_threads, cll_radius=cll_radius)
     for kind, t1, t2, p in spec.get("potentials", []):
         getattr(s, "add_" + kind)(t1, t2, *_pot_args(kind, p))
+    for kind, t, args in spec.get("externals", []):
+        getattr(s, "add_" + kind)(t, *args)
     for kind, p in spec.get("reactions", []):
         if kind == "fusion":
             s.add_fusion(p["a"], p["b"], p["c"], p["rate"], p["educt_distance"], p.get("w1", .5), p.get("w2", .5))
@@ -117,3 +121,24 @@ def polymer_spec(n_chains=200, chain_len=50, n_solvent=10000, box=30.0, seed=0):
                 bond=dict(k=100.0, l0=1.0), angle=dict(k=10.0, theta0=np.pi),
                 dihedral=dict(k=1.0, n=3, phi0=0.0))
     return spec, chains, solvent
+
+
+def externals_spec(n=4000, box=20.0, seed=0, pair=False):
+    """Eight species, each under one order-1 potential (box in/out, sphere in/out, capsule in/out,
+    spherical barrier, cylinder in/out), particles uniform in a periodic box."""
+    rng = np.random.default_rng(seed)
+    pos = (rng.random((n, 3)) - 0.5) * box
+    types = rng.integers(0, 9, n)
+    ext = [("box", 0, (10.0, (-3., -4., -5.), (6., 8., 7.), True)),
+           ("box", 1, (10.0, (-3., -4., -5.), (6., 8., 7.), False)),
+           ("sphere", 2, (5.0, (1., -1., 0.5), 4.0, True)),
+           ("sphere", 3, (5.0, (1., -1., 0.5), 4.0, False)),
+           ("capsule", 4, (3.0, (0.5, 0., 0.), (1., 2., -1.), 6.0, 2.5, True)),
+           ("capsule", 5, (3.0, (0.5, 0., 0.), (1., 2., -1.), 6.0, 2.5, False)),
+           ("spherical_barrier", 6, (3.0, 2.0, (-1., 2., 0.), 6.0)),
+           ("cylinder", 7, (4.0, (1., -2., 3.), (0.3, 0.1, 1.), 3.5, True)),
+           ("cylinder", 8, (4.0, (1., -2., 3.), (0.3, 0.1, 1.), 3.5, False))]
+    pots = [("harmonic_repulsion", a, b, dict(k=10.0, d=1.0)) for a in range(9) for b in range(a, 9)] if pair else []
+    spec = dict(box=(box, box, box), periodic=(True, True, True), diffusion=(1.0,) * 9, potentials=pots,
+                externals=ext)
+    return spec, pos, types

@@ -54,6 +54,11 @@ def test_context_registries_validate_like_the_reference():
         ctx.configure_cosine_dihedral(0, 0, 0, 0, 1.0, 3, 4.0)
     with pytest.raises(ValueError, match="type out of range"):
         ctx.add_harmonic_repulsion(0, 5, 1.0, 1.0)
+    with pytest.raises(ValueError, match="radius larger than its width"):
+        ctx.add_spherical_barrier(0, 2.0, 3.0, (0, 0, 0), 1.0)
+    with pytest.raises(ValueError, match="normal must be nonzero"):
+        ctx.add_cylinder(0, 1.0, (0, 0, 0), (0, 0, 0), 1.0, True)
+    ctx.add_box(1, 10.0, (-1, -1, -1), (2, 2, 2))
     ctx.add_harmonic_repulsion(0, 1, 10.0, 1.0)
     ctx.add_fusion(0, 1, 1, 1.0, 1.5)
     assert ctx.calculate_max_cutoff() == pytest.approx(1.5)

@@ -161,6 +161,54 @@ def test_neighbor_pairs_at_the_cutoff(rg):
     np.testing.assert_array_equal(got, ref)
 
 
+@pytest.mark.parametrize("case", ka.EXTERNAL_CASES, ids=lambda c: c["name"])
+def test_external_potential_known_answers(rg, case):
+    n_types = max(case["types"]) + 1
+    ctx = rg.Context(case["box"], case["periodic"], 1.0, (1.0,) * n_types)
+    for kind, t, args in case["potentials"]:
+        getattr(ctx, "add_" + kind)(t, *args)
+    k = rg.CUDAKernel(ctx, seed=1)
+    k.add_particles(np.array(case["positions"], float), np.array(case["types"]))
+    k.calculate_forces()
+    k.calculate_forces()  # must not accumulate
+    assert k.energy == pytest.approx(case["energy"], rel=ENERGY_RTOL)
+    f, ids = k.get_forces()
+    (f,) = by_id(ids, f)
+    exp = np.array(case["forces"])
+    scale = max(np.abs(exp).max(), 1e-12)
+    np.testing.assert_allclose(f, exp, rtol=0, atol=max(case["force_atol"], FORCE_RTOL * scale))
+
+
+@pytest.mark.parametrize("pair", [False, True], ids=["external_only", "with_pairs"])
+def test_external_potentials_match_oracle(rg, pair):
+    """All eight order-1 forms on random positions, alone (each particle's force is one term, so the
+    1e-5 bound is plain relative error, also next to the surfaces) and together with pair repulsion."""
+    from tests.helpers import externals_spec
+    spec, pos, types = externals_spec(n=4000, seed=3, pair=pair)
+    pos = f32(pos)
+    ctx, k = gpu_system(rg, spec, pos, types)
+    if pair:
+        k.create_neighbor_list(ctx.calculate_max_cutoff())
+    k.calculate_forces()
+    e_gpu = k.energy
+    f_gpu, ids = k.get_forces()
+    (f_gpu,) = by_id(ids, f_gpu)
+    o = make_oracle(spec, n_threads=4)
+    o.add_particles(pos, types)
+    if pair:
+        o.nl_setup(o.calculate_max_cutoff())
+    e_ref = o.calculate_forces()
+    _, _, oid, f_ref, _ = o.particles()
+    sc = o.force_scales()
+    (f_ref, sc) = by_id(oid, f_ref, sc)
+    err, _ = force_error(f_gpu, f_ref, sc)
+    for t in range(9):
+        m = types == t
+        print(f"type {t} ({spec['externals'][t][0]}): max err {err[m].max():.3e}")
+    assert err.max() <= FORCE_RTOL
+    assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
+
+
 def _compare_forces(rg, spec, pos, types, label):
     ctx, k = gpu_system(rg, spec, pos, types)
     k.create_neighbor_list(ctx.calculate_max_cutoff())
@@ -279,10 +327,11 @@ def test_run_conserves_a_plus_b_c(rg):
     k.synchronize()
 
 
+@pytest.mark.parametrize("external", [False, True], ids=["pairs", "pairs_and_external"])
 @pytest.mark.parametrize("handler", [0, 1])
-def test_batch_replica_equals_plain_run(rg, handler):
+def test_batch_replica_equals_plain_run(rg, handler, external):
     """A replica advanced inside a batch follows the same trajectory as the same system run alone
-    through the per-system path with the replica's seed."""
+    through the per-system path with the replica's seed (also under order-1 potentials)."""
     from readdy_gb300.batch import ReplicaBatch, replica_seed
     rng = np.random.default_rng(9)
     sizes = [200, 900, 2000, 450]
@@ -291,6 +340,9 @@ def test_batch_replica_equals_plain_run(rg, handler):
     for n in sizes:
         L = float(np.float32((n / 0.25) ** (1 / 3)))
         spec, pos, types = abc_spec(n=n, box=L, seed=int(rng.integers(1 << 30)))
+        if external:
+            spec["externals"] = [("sphere", 0, (2.0, (0., 0., 0.), 3.0, True)),
+                                 ("cylinder", 2, (1.0, (0.5, 0., 0.), (0., 1., 1.), 2.0, False))]
         specs.append(spec)
         poss.append(f32(pos))
         typess.append(types)

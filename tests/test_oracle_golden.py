@@ -43,6 +43,25 @@ def test_pair_potential_known_answers(case):
     np.testing.assert_allclose(f[order], exp, rtol=0, atol=case["force_atol"] + 1e-12)
 
 
+@pytest.mark.parametrize("case", ka.EXTERNAL_CASES, ids=lambda c: c["name"])
+def test_external_potential_known_answers(case):
+    n_types = max(case["types"]) + 1
+    s = oracle.OracleSystem(case["box"], case["periodic"], 1.0, (1.0,) * n_types)
+    for kind, t, args in case["potentials"]:
+        getattr(s, "add_" + kind)(t, *args)
+    s.add_particles(np.array(case["positions"], float), np.array(case["types"]))
+    e = s.calculate_forces()
+    assert e == pytest.approx(case["energy"], rel=1e-9)
+    _, _, ids, f, _ = s.particles()
+    np.testing.assert_allclose(f[np.argsort(ids)], np.array(case["forces"]), rtol=0, atol=case["force_atol"])
+
+
+def test_spherical_barrier_rejects_a_width_above_its_radius():
+    s = oracle.OracleSystem((10., 10., 10.), (1, 1, 1), 1.0, (1.0,))
+    with pytest.raises(RuntimeError, match="radius larger than its width"):
+        s.add_spherical_barrier(0, 1.0, 2.0, (0., 0., 0.), 1.0)
+
+
 @pytest.mark.parametrize("case", ka.BONDED_CASES, ids=lambda c: c["name"])
 def test_bonded_known_answers(case):
     s = oracle.OracleSystem(case["box"], case["periodic"], 1.0, (1.0,), seed=1)
