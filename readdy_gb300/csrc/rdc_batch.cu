@@ -197,7 +197,7 @@ struct rdc_batch {
         e.work = work_dev;
         e.tabs = tab_dev;
         e.handler = handler;
-        e.max_events_sm = 1024;
+        e.max_events_sm = ENGINE_MAX_EVENTS_SM;
         e.particle_steps = particle_steps;
         layout();
         sync();

@@ -24,8 +24,16 @@ namespace rdc {
 // step as uint16_t, SMEM_CELLS entries (96 KB): at cells of the cutoff's width and density 0.25 that
 // holds replicas of up to ~12k particles, and larger ones get proportionally wider cells.  Replicas of
 // more particles keep int starts in global memory at the natural cell width.
-constexpr int SMEM_CELLS = 49152;
+#ifndef RDC_ENGINE_SMEM_CELLS
+#define RDC_ENGINE_SMEM_CELLS 49152
+#endif
+#ifndef RDC_ENGINE_MAX_EVENTS_SM
+#define RDC_ENGINE_MAX_EVENTS_SM 1024
+#endif
+constexpr int SMEM_CELLS = RDC_ENGINE_SMEM_CELLS;
 constexpr int ENGINE_THREADS_MAX = 512;
+// accepted events one replica step resolves in shared memory (more raise ST_EVENTS)
+constexpr int ENGINE_MAX_EVENTS_SM = RDC_ENGINE_MAX_EVENTS_SM;
 
 struct RepDesc {
     Geo geo;

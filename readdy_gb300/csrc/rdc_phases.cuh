@@ -161,6 +161,53 @@ __device__ inline void for_each_candidate(float4 p, const G &g, const S *__restr
     }
 }
 
+// for_each_candidate that also hands f the candidate's position: f(j, pos[j]).  On the fast stencil the
+// position of the next candidate is loaded before f runs on the current one, so each thread keeps a
+// load in flight while it screens; the walk is latency bound on these loads.
+template <typename G, typename S, typename F>
+__device__ inline void for_each_candidate_q(float4 p, const G &g, const S *__restrict__ start,
+                                            const float4 *__restrict__ pos, int radius, int jmin, F f) {
+    if (!stencil_fast(g, radius)) {
+        for_each_neighbor_range(p, g, start, radius, [&](int jb, int je) {
+            for (int j = max(jb, jmin); j < je; ++j) f(j, pos[j]);
+        });
+        return;
+    }
+    int rb[MAX_RANGES], re[MAX_RANGES];
+    int nr = 0;
+    for_each_neighbor_range(p, g, start, radius, [&](int jb, int je) {
+        jb = max(jb, jmin);
+        if (jb < je) {
+            rb[nr] = jb;
+            re[nr] = je;
+            ++nr;
+        }
+    });
+    if (nr == 0) return;
+    int r = 0, j = rb[0], je = re[0];
+    float4 q = pos[j];
+    for (;;) {
+        int jn = j + 1, rn = r, jen = je;
+        bool more = true;
+        if (jn == jen) {
+            if (++rn < nr) {
+                jn = rb[rn];
+                jen = re[rn];
+            } else {
+                more = false;
+            }
+        }
+        float4 qn = q;
+        if (more) qn = pos[jn];
+        f(j, q);
+        if (!more) break;
+        j = jn;
+        r = rn;
+        je = jen;
+        q = qn;
+    }
+}
+
 // exclusive scan of one value per thread across the block; total receives the block sum
 __device__ inline int block_exclusive_scan(int v, int &total) {
     __shared__ int warp_sums[32];
@@ -231,9 +278,8 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
         }
     };
     int b0 = 0, b1 = 0, b2 = 0, b3 = 0, nb = 0;
-    for_each_candidate(p, g, start, radius, 0, [&](int j) {
+    for_each_candidate_q(p, g, start, pos, radius, 0, [&](int j, float4 q) {
         if (j == i) return;
-        const float4 q = pos[j];
         const int tj = itype(q);
         if (tj < 0) return;
         if (trow[tj] == 0) return;
@@ -331,12 +377,13 @@ __device__ inline void event_tuples_at(int i, bool in_cells, const float4 *__res
     }
     if (!in_cells || !rt.o2_any[ti]) return;
     const int *trow = rt.o2_tab + ti * rt.T;
-    for_each_candidate(p, g, start, radius, i + 1, [&](int j) {
-        const float4 q = pos[j];
+    const float *srow = rt.screen + ti * rt.T;
+    for_each_candidate_q(p, g, start, pos, radius, i + 1, [&](int j, float4 q) {
         const int tj = itype(q);
         if (tj < 0) return;
         const int o2 = trow[tj];
         if (o2 == 0) return;
+        if (screen_d2(p, q, g) > srow[tj]) return;  // cheap FP32 reject before the exact geometry
         const PairGeom g0 = pair_geom(p, q, g);
         for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
             const int r = rt.o2_list[k];

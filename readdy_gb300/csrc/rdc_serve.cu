@@ -194,7 +194,7 @@ struct rdc_server {
         e.work = work_dev;
         e.tabs = tabs_dev;
         e.handler = handler;
-        e.max_events_sm = 1024;
+        e.max_events_sm = ENGINE_MAX_EVENTS_SM;
         e.particle_steps = particle_steps_dev;
         smem = engine_smem_bytes(e.max_events_sm);
         blocks = engine_grid(threads, smem);
