@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests of the served-stream sample (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=150.0, help="wall-time limit of the served-stream sample")
+    ap.add_argument("--single-systems", type=int, default=1, help="time the three single-system workloads (0: skip)")
     ap.add_argument("--plain-threshold", type=int, default=4096,
                     help="requests above this many particles take the per-system leg of the server")
     return ap.parse_args()
@@ -206,6 +207,128 @@ def one_at_a_time(ns, boxes, pos, types, seed, n_sample, steps, rng_pick):
             "each through the per-system path (CUDA-graph replay of the SimulationLoop step), run sequentially"}
 
 
+# ---- single systems through the per-system path (the drop-in for one ReaDDy simulation) ----------
+
+def single_system(name, seed=11):
+    """(context arguments, particles, topologies, run settings) of the three single-system workloads:
+    A+B<->C with 2000 particles in a 20^3 box; 200k crowded particles of three species (LJ, weak
+    piecewise harmonic, harmonic repulsion) in 100^3 on a jittered lattice; 2000 chains of 50 beads
+    with bonds, angles and dihedrals in 100k solvent in 120^3."""
+    rng = np.random.default_rng(seed)
+    if name == "abc_2k":
+        L = 20.0
+        pos = (rng.random((2000, 3)) - 0.5) * L
+        types = np.array([0] * 1000 + [1] * 1000, np.int32)
+        pots = [("harmonic_repulsion", a, b, (10.0, 1.0)) for a in range(3) for b in range(a, 3)]
+        rx = [("fusion", (0, 1, 2, 1.0, 1.0)), ("fission", (2, 0, 1, 0.1, 1.0))]
+        return dict(box=(L, L, L), D=(1.0, 1.0, 0.5), pots=pots, rx=rx, pos=pos, types=types, chains=None,
+                    dt=1e-3, handler="ua")
+    if name == "crowded_200k":
+        L = 100.0
+        n = 200000
+        # jittered cubic lattice: uniformly random positions overlap at this density, and the
+        # Lennard-Jones forces of overlapping pairs (~1e12 at r = 0.1) blow the Euler step up
+        side = int(np.ceil(n ** (1.0 / 3.0)))
+        a = L / side
+        sites = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)
+        sites = sites[rng.permutation(len(sites))[:n]]
+        pos = (sites + 0.5 + rng.uniform(-0.25, 0.25, (n, 3))) * a - L / 2
+        types = rng.choice(3, size=n, p=[0.5, 0.3, 0.2]).astype(np.int32)
+        pots = [("lennard_jones", 0, 0, (12, 6, 2.5, True, 1.0, 1.0)),
+                ("weak_interaction_piecewise_harmonic", 1, 1, (10.0, 1.0, 0.5, 1.5)),
+                ("harmonic_repulsion", 0, 1, (10.0, 1.0)), ("harmonic_repulsion", 0, 2, (10.0, 1.0)),
+                ("harmonic_repulsion", 1, 2, (10.0, 1.0)), ("harmonic_repulsion", 2, 2, (10.0, 1.0))]
+        rx = [("conversion", (0, 1, 0.01))]
+        # uncontrolled approximation: the reference's Gillespie selection is serial and quadratic in the
+        # event count, and every species-0 particle carries a conversion event here
+        return dict(box=(L, L, L), D=(1.0, 0.5, 0.2), pots=pots, rx=rx, pos=pos, types=types, chains=None,
+                    dt=1e-4, handler="ua")
+    if name == "polymer_200k":
+        L = 120.0
+        chains = []
+        for c in range(2000):
+            start = (rng.random(3) - 0.5) * L
+            steps = rng.normal(size=(49, 3))
+            steps /= np.linalg.norm(steps, axis=1)[:, None]
+            p = np.vstack([start, start + np.cumsum(steps, axis=0)])
+            chains.append((p + L / 2) % L - L / 2)
+        pos = (rng.random((100000, 3)) - 0.5) * L
+        pots = [("harmonic_repulsion", a, b, (10.0, 1.0)) for a, b in [(0, 0), (0, 1), (1, 1)]]
+        return dict(box=(L, L, L), D=(0.1, 1.0), pots=pots, rx=[], pos=pos, types=np.ones(100000, np.int32),
+                    chains=chains, dt=1e-4, handler="gillespie")
+    raise KeyError(name)
+
+
+def _gpu_system(w, seed):
+    import readdy_gb300 as rg
+    ctx = rg.Context(w["box"], (True, True, True), 1.0, w["D"])
+    for kind, a, b, args in w["pots"]:
+        getattr(ctx, "add_" + kind)(a, b, *args)
+    for kind, args in w["rx"]:
+        getattr(ctx, "add_" + kind)(*args)
+    if w["chains"] is not None:
+        ctx.configure_harmonic_bond(0, 0, 100.0, 1.0)
+        ctx.configure_harmonic_angle(0, 0, 0, 10.0, np.pi)
+        ctx.configure_cosine_dihedral(0, 0, 0, 0, 1.0, 3, 0.0)
+    k = rg.CUDAKernel(ctx, seed=seed)
+    if w["chains"] is not None:
+        for c in w["chains"]:
+            k.add_topology(c, np.zeros(len(c), np.int32), [(i, i + 1) for i in range(len(c) - 1)])
+    k.add_particles(w["pos"], w["types"])
+    return k
+
+
+def _oracle_system(w, seed, threads):
+    import oracle
+    o = oracle.OracleSystem(w["box"], (True, True, True), 1.0, w["D"], seed=seed, n_threads=threads)
+    for kind, a, b, args in w["pots"]:
+        getattr(o, "add_" + kind)(a, b, *args)
+    for kind, args in w["rx"]:
+        getattr(o, "add_" + kind)(*args)
+    if w["chains"] is not None:
+        nb = sum(len(c) for c in w["chains"])
+        o.add_particles(np.vstack(w["chains"]), np.zeros(nb, np.int32))
+        idx = np.arange(nb).reshape(len(w["chains"]), -1)
+        o.add_harmonic_bonds(np.stack([idx[:, :-1].ravel(), idx[:, 1:].ravel()], 1), 100.0, 1.0)
+        o.add_harmonic_angles(np.stack([idx[:, :-2].ravel(), idx[:, 1:-1].ravel(), idx[:, 2:].ravel()], 1),
+                              10.0, np.pi)
+        o.add_cosine_dihedrals(np.stack([idx[:, :-3].ravel(), idx[:, 1:-2].ravel(), idx[:, 2:-1].ravel(),
+                                         idx[:, 3:].ravel()], 1), 1.0, 3, 0.0)
+    o.add_particles(w["pos"], w["types"])
+    return o
+
+
+def single_systems(gpu_steps=200, cpu_steps=3):
+    """Time per step of each single-system workload through rdc_run (per-system kernels replayed from
+    a CUDA graph) and through the FP64 oracle on all host cores."""
+    import oracle
+    import readdy_gb300 as rg
+    oracle.build()
+    cores = os.cpu_count() or 1
+    out = {}
+    for name in ("abc_2k", "crowded_200k", "polymer_200k"):
+        w = single_system(name)
+        n = len(w["pos"]) + (sum(len(c) for c in w["chains"]) if w["chains"] is not None else 0)
+        h_gpu = rg.GILLESPIE if w["handler"] == "gillespie" else rg.UNCONTROLLED_APPROXIMATION
+        k = _gpu_system(w, seed=3)
+        k.run(5, w["dt"], handler=h_gpu)
+        k.synchronize()
+        t0 = time.perf_counter()
+        k.run(gpu_steps, w["dt"], handler=h_gpu)
+        k.synchronize()
+        g = (time.perf_counter() - t0) / gpu_steps
+        o = _oracle_system(w, seed=3, threads=cores)
+        h_orc = oracle.GILLESPIE if w["handler"] == "gillespie" else oracle.UNCONTROLLED_APPROXIMATION
+        t0 = time.perf_counter()
+        o.run(cpu_steps, w["dt"], handler=h_orc)
+        c = (time.perf_counter() - t0) / cpu_steps
+        out[name] = {"particles": int(n), "gpu_ms_per_step": g * 1e3, "cpu_ms_per_step": c * 1e3,
+                     "gpu_particle_steps_per_s": n / g, "cpu_particle_steps_per_s": n / c, "cpu_cores": cores,
+                     "gpu_steps": gpu_steps, "cpu_steps": cpu_steps,
+                     "timing": "wall clock around rdc_run (graph replays, one sync) / oracle run, same inputs"}
+    return out
+
+
 def serving(n_requests, time_limit, plain_threshold, seed=7):
     """The served form on the first n_requests of the seeded serving stream (Poisson arrivals at 20/s;
     2-6 species; N log-uniform in [500, 200000] at density 0.1-0.5; 1k-100k steps; counts every 100
@@ -268,6 +391,7 @@ def run_gb300(args, rank, world):
         oat = one_at_a_time(ns, boxes, pos, types, seed, 64, 50, pick)
         cpu = cpu_baseline(ns, boxes, pos, types, seed, args.cpu_seconds, np.random.default_rng(args.seed + 5))
         served = serving(args.serve_requests, args.serve_seconds, args.plain_threshold) if args.serve_requests else None
+        singles = single_systems() if args.single_systems else None
         peak, peak_kind = measured_peaks()
         n_avg = (ps1 - ps0) / args.steps
         launch_ms = ms / args.steps
@@ -308,6 +432,7 @@ def run_gb300(args, rank, world):
             "clocks": clocks.summary(),
             "gpu_launches": 2 * args.steps,
             "serving": served,
+            "single_systems": singles,
         }
     return result
 
