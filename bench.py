@@ -358,7 +358,9 @@ def run_gb300(args, rank, world):
     ctx = chemistry()
     b = ReplicaBatch(ctx, boxes, caps, seed=seed)
     b.set_particles(pos, types)
-    b.configure(handler=rg.GILLESPIE, dt=1e-3, cell_width_scale=1.0, threads_per_block=512)
+    from readdy_gb300.batch import autotune_inplace
+    tuned, tune_table = autotune_inplace(b)  # cell width x threads per block, on these replicas
+    cws, tpb = tuned["cell_width_scale"], tuned["threads_per_block"]
     b.step(args.warmup)
     b.synchronize()
     barrier(world)
@@ -375,7 +377,7 @@ def run_gb300(args, rank, world):
     t0 = time.perf_counter()
     e = ReplicaBatch(ctx, boxes, caps, seed=seed + 7)
     e.set_particles(pos, types)
-    e.configure(handler=rg.GILLESPIE, dt=1e-3, cell_width_scale=1.0, threads_per_block=512)
+    e.configure(handler=rg.GILLESPIE, dt=1e-3, cell_width_scale=cws, threads_per_block=tpb)
     e.step(args.steps)
     counts = e.count_types()
     e2e_t = time.perf_counter() - t0
@@ -414,7 +416,8 @@ def run_gb300(args, rank, world):
                             "density 0.25, HR k=10 d=1, Gillespie, dt=1e-3",
                 "replicas": int(args.replicas), "particles": int(ns.sum()),
                 "launch": "one persistent fused launch per step (k_engine_step), CUDA graph",
-                "cell_width_scale": 1.0, "threads_per_block": 512,
+                "cell_width_scale": cws, "threads_per_block": tpb,
+                "autotune": {"chosen": tuned, "table": tune_table},
                 "l2": "inputs larger than L2 (particle state %.0f MB > 129 MB)" % (ns.sum() * 40 / 1e6),
                 "parallelism": f"replicas only, {world} rank(s), one ensemble per GPU",
             },

@@ -50,6 +50,9 @@ const char *rdc_kernel_name(void);
 int rdc_context_create(rdc_context **out, const double box[3], const int periodic[3], double kbt, int n_types,
                        const double *diffusion);
 int rdc_context_destroy(rdc_context *ctx);
+/* Context::recordVirial (include/readdy/model/Context.h:168-174): systems created from ctx afterwards
+ * accumulate the pair virial in CalculateForces */
+int rdc_context_set_record_virial(rdc_context *ctx, int record);
 /* Context::calculateMaxCutoff, readdy/main/model/Context.cpp:126-144 */
 int rdc_context_max_cutoff(const rdc_context *ctx, double *cutoff);
 
@@ -127,6 +130,9 @@ int rdc_get_particles(rdc_system *s, int64_t capacity, double *positions3, int *
                       int64_t *n_out);
 /* Forces observable (CPUObservables.cpp): per-particle forces, same order as rdc_get_particles */
 int rdc_get_forces(rdc_system *s, int64_t capacity, double *forces3, uint64_t *ids, int64_t *n_out);
+/* StateModel::virial() after the last CalculateForces (row-major 3x3): the sum over pairs of
+ * outer(-x_ij, f_i) (CPUCalculateForces.cpp:247-249); zero unless the context records the virial */
+int rdc_get_virial(rdc_system *s, double *virial9);
 /* StateModel::energy() after the last CalculateForces */
 int rdc_get_energy(rdc_system *s, double *energy);
 /* NParticles observable per type (kernels/cpu/src/observables/CPUObservables.cpp:153-171) */

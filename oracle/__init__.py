@@ -44,6 +44,8 @@ def _load():
             "orc_create": (vp, [P(d), P(i), d, i, P(d), u64, i, i]),
             "orc_destroy": (None, [vp]),
             "orc_last_error": (C.c_char_p, []),
+            "orc_set_record_virial": (i, [vp, i]),
+            "orc_get_virial": (i, [vp, P(d)]),
             "orc_add_box": (i, [vp, i, d, P(d), P(d), i]),
             "orc_add_sphere": (i, [vp, i, d, P(d), d, i]),
             "orc_add_capsule": (i, [vp, i, d, P(d), P(d), d, d, i]),
@@ -117,6 +119,14 @@ class OracleSystem:
         if rc < 0:
             raise RuntimeError(self._lib.orc_last_error().decode())
         return rc
+
+    def set_record_virial(self, record=True):
+        self._lib.orc_set_record_virial(self._h, int(bool(record)))
+
+    def virial(self):
+        out = np.zeros(9)
+        self._lib.orc_get_virial(self._h, _ptr(out, C.c_double))
+        return out.reshape(3, 3)
 
     # order-1 (external) potentials
     @staticmethod

@@ -18,6 +18,7 @@
 #include "readdy_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <condition_variable>
@@ -376,6 +377,8 @@ struct orc_system {
     int nTypes;
     std::map<std::pair<int, int>, std::vector<Pot2>> pot2;          // symmetric key (min,max)
     std::vector<std::vector<Pot1>> pot1;                           // by type
+    bool recordVirial = false;                                      // Context::recordVirial (Context.h:168-174)
+    double virial[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};                 // StateModel::virial(), row-major
     std::vector<std::vector<const Reaction *>> o1;                 // by type
     std::map<std::pair<int, int>, std::vector<const Reaction *>> o2;  // symmetric key
     std::vector<Reaction *> reactions;
@@ -544,11 +547,18 @@ struct orc_system {
         if (!pot2.empty()) {
             if (!nlSetUp) throw std::logic_error("neighbor list not set up");
             size_t nCells = adjacency.size();
+            std::vector<std::array<double, 9>> vpart(nt);
             pool.run([&](int tid) {
                 auto [cb, ce] = chunk(nCells, nt, tid);
-                part[tid] = order2(cb, ce);
+                vpart[tid].fill(0.);
+                part[tid] = order2(cb, ce, vpart[tid].data());
             });
             for (double p : part) energy += p;
+            for (int k = 0; k < 9; ++k) {
+                virial[k] = 0;
+                if (recordVirial)
+                    for (auto &v : vpart) virial[k] += v[k];
+            }
         }
         return energy;
     }
@@ -567,7 +577,7 @@ struct orc_system {
         return eUpd;
     }
     /* calculateOrder2<false>, CPUCalculateForces.cpp:214-268 */
-    double order2(size_t cb, size_t ce) {
+    double order2(size_t cb, size_t ce, double *vir) {
         double eUpd = 0;
         for (size_t cell = cb; cell < ce; ++cell) {
             forEachInCell(cell, [&](size_t pi) {
@@ -588,6 +598,10 @@ struct orc_system {
                                 pot.force(upd, xij);
                                 entry.force += upd;
                                 entry.fscale += norm(upd);
+                                // calculateOrder2<true>: each pair once, outer(-x_ij, f_i) (CPUCalculateForces.cpp:247-249)
+                                if (recordVirial && pi < ni)
+                                    for (int a = 0; a < 3; ++a)
+                                        for (int b = 0; b < 3; ++b) vir[3 * a + b] += -xij[a] * upd[b];
                             }
                         }
                     }
@@ -1236,6 +1250,11 @@ int64_t orc_brute_force_pairs(const orc_system *s, double cutoff, int64_t cap, u
     return finishPairs(v, cap, out);
 }
 
+int orc_set_record_virial(orc_system *s, int record) { s->recordVirial = record != 0; return 0; }
+int orc_get_virial(const orc_system *s, double *out9) {
+    for (int k = 0; k < 9; ++k) out9[k] = s->virial[k];
+    return 0;
+}
 double orc_calculate_forces(orc_system *s) {
     try { return s->calculateForces(); } catch (const std::exception &e) { g_err = e.what(); return NAN; }
 }

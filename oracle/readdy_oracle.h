@@ -35,6 +35,9 @@ int orc_add_spherical_barrier(orc_system *s, int type, double height, double wid
                               double radius);
 int orc_add_cylinder(orc_system *s, int type, double k, const double *origin3, const double *normal3, double radius,
                      int inclusion);
+/* Context::recordVirial and StateModel::virial() (row-major 3x3) of the last force calculation */
+int orc_set_record_virial(orc_system *s, int record);
+int orc_get_virial(const orc_system *s, double *out9);
 int orc_add_harmonic_repulsion(orc_system *s, int t1, int t2, double k, double interaction_distance);
 int orc_add_weak_interaction_piecewise_harmonic(orc_system *s, int t1, int t2, double k, double desired_distance,
                                                 double depth, double no_interaction_distance);

@@ -43,6 +43,8 @@ def _sig(lib):
         "rdc_context_create": (i, [vpp, P(d), P(i), d, i, P(d)]),
         "rdc_context_destroy": (i, [vp]),
         "rdc_context_max_cutoff": (i, [vp, P(d)]),
+        "rdc_context_set_record_virial": (i, [vp, i]),
+        "rdc_get_virial": (i, [vp, P(d)]),
         "rdc_context_add_harmonic_repulsion": (i, [vp, i, i, d, d]),
         "rdc_context_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
         "rdc_context_add_lennard_jones": (i, [vp, i, i, C.c_uint, C.c_uint, d, i, d, d]),

@@ -122,3 +122,21 @@ def autotune(make_batch, steps=20, scales=(1.0, 1.5, 2.0), threads=(256, 512), h
                 best = dict(cell_width_scale=r, threads_per_block=t, s_per_step=dtm)
             del b
     return best
+
+
+def autotune_inplace(batch: ReplicaBatch, scales=(1.0, 1.15, 1.3), threads=(256, 384, 512), steps=5,
+                     handler=N.GILLESPIE, dt=1e-3):
+    """Autotunes a batch on its own replicas: for every cell width scale x threads per block it
+    reconfigures the batch, runs two untimed steps and `steps` steps timed with CUDA events on the
+    batch's stream, then leaves the batch configured with the fastest setting.  The replicas advance
+    by all these steps.  Returns the fastest setting and the table of timings (ms per step)."""
+    table = []
+    for r in scales:
+        for t in threads:
+            batch.configure(handler=handler, dt=dt, cell_width_scale=r, threads_per_block=t)
+            batch.step(2)
+            table.append(dict(cell_width_scale=r, threads_per_block=t, ms_per_step=batch.step_timed(steps) / steps))
+    best = min(table, key=lambda x: x["ms_per_step"])
+    batch.configure(handler=handler, dt=dt, cell_width_scale=best["cell_width_scale"],
+                    threads_per_block=best["threads_per_block"])
+    return best, table

@@ -350,7 +350,7 @@ struct rdc_system {
         dfree(d.cnt); dfree(d.start); dfree(d.scan_blocks); dfree(d.big_cells);
         dfree(d.tloc); dfree(d.counters); dfree(d.step);
         dfree(d.events); dfree(d.claim); dfree(d.taken); dfree(d.reaction_counts);
-        dfree(d.epart); dfree(d.energy); dfree(d.counts_ring);
+        dfree(d.epart); dfree(d.energy); dfree(d.counts_ring); dfree(d.vpart); dfree(d.virial);
         dfree(tab_dev); dfree(count_buf); dfree(pairs_n);
         dfree(top_off_dev); dfree(top_terms_dev);
         dfree(bond_idx_dev); dfree(angle_idx_dev); dfree(dih_idx_dev);
@@ -405,6 +405,11 @@ struct rdc_system {
         RDC_CUDA(cudaMemsetAsync(d.epart, 0, sizeof(double) * (FORCE_BLOCKS + BONDED_BLOCKS), stream));
         d.energy = dalloc<double>(1);
         RDC_CUDA(cudaMemsetAsync(d.energy, 0, sizeof(double), stream));
+        if (ctx.record_virial) {
+            d.vpart = dalloc<double>(9 * FORCE_BLOCKS);
+            d.virial = dalloc<double>(9);
+            RDC_CUDA(cudaMemsetAsync(d.virial, 0, sizeof(double) * 9, stream));
+        }
         d.event_capacity = 1 << 16;
         d.events = dalloc<EventRec>(d.event_capacity);
         count_buf = dalloc<unsigned long long>(MAX_TYPES);
@@ -854,6 +859,12 @@ int rdc_context_destroy(rdc_context *ctx) {
     delete ctx;
     return RDC_OK;
 }
+int rdc_context_set_record_virial(rdc_context *ctx, int record) {
+    return guarded([&] {
+        require(ctx != nullptr, "null context");
+        ctx->d.record_virial = record != 0;
+    });
+}
 int rdc_context_max_cutoff(const rdc_context *ctx, double *cutoff) {
     return guarded([&] {
         require(ctx && cutoff, "null argument");
@@ -1171,6 +1182,15 @@ int rdc_get_forces(rdc_system *s, int64_t cap, double *forces, uint64_t *ids, in
         }
         if (n_out) *n_out = k;
         if (k > cap) throw CapacityError("output capacity too small for the particles");
+    });
+}
+int rdc_get_virial(rdc_system *s, double *virial9) {
+    return guarded([&] {
+        require(s && virial9, "null argument");
+        for (int k = 0; k < 9; ++k) virial9[k] = 0.0;
+        if (s->d.virial)
+            RDC_CUDA(cudaMemcpyAsync(virial9, s->d.virial, sizeof(double) * 9, cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
     });
 }
 int rdc_get_energy(rdc_system *s, double *e) {

@@ -52,6 +52,7 @@ struct ContextData {
     int pbc[3];
     double kbt;
     int ntypes;
+    bool record_virial = false;  // Context::recordVirial (include/readdy/model/Context.h:168-174)
     std::vector<double> D;
     std::vector<HostPot> pots;
     std::vector<HostO1> o1pots;
@@ -134,6 +135,8 @@ struct SysDev {
     // energy
     double *epart;     // per-block partial energies (pair kernel blocks, then bonded blocks)
     double *energy;
+    double *vpart;     // per-block partial virials (9 per pair kernel block); null: virial not recorded
+    double *virial;    // row-major 3x3 pair virial of the last force calculation
     // bonded (topology slots)
     int n_top;             // topology slots whose bonded terms are live
     int tloc_size;         // slots covered by tloc

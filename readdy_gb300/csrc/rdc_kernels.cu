@@ -164,6 +164,7 @@ __global__ void k_gather(SysDev s, int permute_force) {
 // K3 pair forces: one thread per particle, full (both-direction) stencil, force and half the pair
 // energies accumulated in registers; per-block FP64 energy partials in a fixed order
 // ------------------------------------------------------------------------------------------------
+template <bool VIRIAL>
 __global__ void __launch_bounds__(FORCE_THREADS, 2) k_pair_forces(SysDev s) {
     __shared__ int sh_tab[MAX_TYPES * MAX_TYPES];
     __shared__ float sh_scr[MAX_TYPES * MAX_TYPES];
@@ -179,10 +180,21 @@ __global__ void __launch_bounds__(FORCE_THREADS, 2) k_pair_forces(SysDev s) {
     const int n = s.counters[C_N], n_in = s.counters[C_N_INCELLS];
     const GeoR g = geo_r(s.geo);
     double esum = 0.0;
+    float vir[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double vsum[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     GRID_STRIDE(i, n) {
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
         const float4 p = s.pos[i];
-        if (i < n_in && NP > 0) pair_force_at(i, p, s.pos, s.start, g, s.radius, sh_tab, sh_scr, sh_pots, T, fx, fy, fz, e);
+        if (i < n_in && NP > 0)
+            pair_force_at(i, p, s.pos, s.start, g, s.radius, sh_tab, sh_scr, sh_pots, T, fx, fy, fz, e,
+                          VIRIAL ? vir : nullptr);
+        if (VIRIAL) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                vsum[k] += (double)vir[k];
+                vir[k] = 0.f;
+            }
+        }
         const int ti = itype(p);
         if (ti >= 0) {  // order-1 potentials act on every active particle, in the box or not (CPUCalculateForces.cpp:295-314)
             const int o1 = tab->o1pot_tab[ti];
@@ -193,6 +205,22 @@ __global__ void __launch_bounds__(FORCE_THREADS, 2) k_pair_forces(SysDev s) {
     }
     const double b = block_sum_double(esum);
     if (threadIdx.x == 0) s.epart[blockIdx.x] = b;
+    if (VIRIAL) {
+        for (int k = 0; k < 9; ++k) {
+            const double v = block_sum_double(vsum[k]);
+            if (threadIdx.x == 0) s.vpart[9 * blockIdx.x + k] = v;
+        }
+    }
+}
+
+// virial of the last force calculation: block partials summed in a fixed order
+__global__ void k_virial_final(SysDev s) {
+    for (int k = 0; k < 9; ++k) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < FORCE_BLOCKS; b += blockDim.x) v += s.vpart[9 * b + k];
+        const double t = block_sum_double(v);
+        if (threadIdx.x == 0) s.virial[k] = t;
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -402,7 +430,12 @@ void launch_sort(const SysDev &s, bool permute_force, cudaStream_t st) {
 }
 
 void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st) {
-    k_pair_forces<<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
+    if (s.virial) {
+        k_pair_forces<true><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
+        k_virial_final<<<1, 256, 0, st>>>(s);
+    } else {
+        k_pair_forces<false><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
+    }
     if (bonded && s.n_top > 0) k_bonded<<<BONDED_BLOCKS, 256, 0, st>>>(s);
     k_energy_final<<<1, 256, 0, st>>>(s, 1, (bonded && s.n_top > 0) ? 1 : 0);
     (void)pair;

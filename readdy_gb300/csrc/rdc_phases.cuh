@@ -259,10 +259,13 @@ __device__ inline double block_sum_double(double v) {
 // that had met a neighbour.  Survivors keep the walk order, so the summation order is unchanged.
 constexpr int PAIR_BUFFER = 4;
 
+// With vir non-null, vir[3a+b] also receives half of -x_ij[a] f_i[b] per pair: the virial
+// sum over pairs of outer(-x_ij, f_i) of calculateOrder2<true> (CPUCalculateForces.cpp:247-249), seen
+// here once from each side.
 template <typename G, typename S>
 __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const S *__restrict__ start,
                                      const G &g, int radius, const int *tab, const float *screen, const PairPot *pots,
-                                     int T, float &fx, float &fy, float &fz, float &e) {
+                                     int T, float &fx, float &fy, float &fz, float &e, float *vir = nullptr) {
     const int ti = itype(p);
     const int *trow = tab + ti * T;
     const float *srow = screen + ti * T;
@@ -274,7 +277,20 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
         for (int k = first; k < first + cnt; ++k) {
             const PairPot &pp = pots[k];
             PairGeom gg = g0;
-            if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, p, q, g, fx, fy, fz, e);
+            if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) {
+                if (vir) {
+                    float tx = 0.f, ty = 0.f, tz = 0.f;
+                    pair_force(pp, gg, p, q, g, tx, ty, tz, e);
+                    fx += tx; fy += ty; fz += tz;
+                    const float d[3] = {-0.5f * gg.dx, -0.5f * gg.dy, -0.5f * gg.dz}, f[3] = {tx, ty, tz};
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+#pragma unroll
+                        for (int b = 0; b < 3; ++b) vir[3 * a + b] += d[a] * f[b];
+                } else {
+                    pair_force(pp, gg, p, q, g, fx, fy, fz, e);
+                }
+            }
         }
     };
     int b0 = 0, b1 = 0, b2 = 0, b3 = 0, nb = 0;

@@ -55,6 +55,15 @@ class Context:
         N.check(self._lib.rdc_context_max_cutoff(self._h, C.byref(c)))
         return c.value
 
+    @property
+    def record_virial(self) -> bool:
+        return getattr(self, "_record_virial", False)
+
+    @record_virial.setter
+    def record_virial(self, value: bool):
+        N.check(self._lib.rdc_context_set_record_virial(self._h, int(bool(value))))
+        self._record_virial = bool(value)
+
     # PotentialRegistry
     def add_harmonic_repulsion(self, t1, t2, force_constant, interaction_distance):
         N.check(self._lib.rdc_context_add_harmonic_repulsion(self._h, t1, t2, force_constant, interaction_distance))
@@ -204,6 +213,12 @@ class CUDAKernel:
         e = C.c_double()
         N.check(self._lib.rdc_get_energy(self._h, C.byref(e)))
         return e.value
+
+    def virial(self):
+        """StateModel::virial() of the last force calculation, 3x3."""
+        out = np.zeros(9)
+        N.check(self._lib.rdc_get_virial(self._h, _p(out, C.c_double)))
+        return out.reshape(3, 3)
 
     def count_types(self):
         out = np.zeros(self.context.n_types, np.int64)

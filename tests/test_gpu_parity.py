@@ -209,6 +209,36 @@ def test_external_potentials_match_oracle(rg, pair):
     assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
 
 
+def test_virial_matches_oracle(rg):
+    """Pair virial of the crowded three-species chemistry (LJ, WIPH, HR) against the FP64 oracle: each
+    entry within 1e-5 of the largest entry."""
+    spec, pos, types = crowded_spec(n=20000, density=0.2, seed=5)
+    pos = f32(pos)
+    ctx = make_context(spec)
+    ctx.record_virial = True
+    k = rg.CUDAKernel(ctx, seed=1)
+    k.add_particles(pos, types)
+    k.create_neighbor_list(ctx.calculate_max_cutoff())
+    k.calculate_forces()
+    v_gpu = k.virial()
+    p, t, ids = k.get_particles()
+    (p, t) = by_id(ids, p, t)
+    o = make_oracle(spec, n_threads=4)
+    o.set_record_virial(True)
+    o.add_particles(p, t)
+    o.nl_setup(o.calculate_max_cutoff())
+    o.calculate_forces()
+    v_ref = o.virial()
+    print("virial gpu", v_gpu.ravel(), "ref", v_ref.ravel())
+    np.testing.assert_allclose(v_gpu, v_ref, rtol=0, atol=1e-5 * np.abs(v_ref).max())
+    # without the flag the virial stays zero and forces are unchanged
+    k2 = rg.CUDAKernel(make_context(spec), seed=1)
+    k2.add_particles(pos, types)
+    k2.create_neighbor_list(ctx.calculate_max_cutoff())
+    k2.calculate_forces()
+    assert np.all(k2.virial() == 0)
+
+
 def _compare_forces(rg, spec, pos, types, label):
     ctx, k = gpu_system(rg, spec, pos, types)
     k.create_neighbor_list(ctx.calculate_max_cutoff())

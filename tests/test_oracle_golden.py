@@ -198,3 +198,17 @@ def test_michaelis_menten_time_averaged_substrate(handler):
     o.add_particles(pos, types)
     c = o.run(mm["n_steps"], mm["dt"], handler=handler, count_stride=1)
     assert abs(c[:, 1].mean() - mm["mean_s"]) < mm["rel_band"] * mm["mean_s"]
+
+
+def test_virial_of_one_pair():
+    """HR k=1, d=2, particles 1.8 apart along z (the pair of TestStateModel.cpp:57-99): the force on the
+    first is -0.2 z, x_01 = 1.8 z, so the virial outer(-x_01, f_0) has zz = 0.36 and nothing else."""
+    s = oracle.OracleSystem((10., 10., 10.), (1, 1, 1), 1.0, (1.0,))
+    s.set_record_virial(True)
+    s.add_harmonic_repulsion(0, 0, 1.0, 2.0)
+    s.add_particles(np.array([[0., 0., 0.], [0., 0., 1.8]]), np.array([0, 0]))
+    s.nl_setup(2.0)
+    s.calculate_forces()
+    expect = np.zeros((3, 3))
+    expect[2, 2] = 0.36
+    np.testing.assert_allclose(s.virial(), expect, atol=1e-12)
