@@ -402,12 +402,19 @@ Geo replica_geo(const double box[3], const int pbc[3], double cutoff, double cel
 
 int engine_grid(int threads, size_t smem) {
     RDC_CUDA(cudaFuncSetAttribute(k_engine_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    RDC_CUDA(cudaFuncSetAttribute(k_engine_step, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    int per_sm = 0;
-    RDC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_step, threads, smem));
-    int dev = 0, sms = 0;
+    int dev = 0, sms = 0, smem_sm = 0;
     RDC_CUDA(cudaGetDevice(&dev));
     RDC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    RDC_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    // Ask for just the shared memory one CTA needs: the rest of the SM's unified L1/shared array stays
+    // L1, which caches the neighbour positions of the candidate walks (a 100 % carveout leaves 28 KB).
+    cudaFuncAttributes fa{};
+    RDC_CUDA(cudaFuncGetAttributes(&fa, k_engine_step));
+    const size_t need = smem + fa.sharedSizeBytes + 1024;  // + the per-CTA reservation
+    const int carveout = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / std::max(smem_sm, 1));
+    RDC_CUDA(cudaFuncSetAttribute(k_engine_step, cudaFuncAttributePreferredSharedMemoryCarveout, carveout));
+    int per_sm = 0;
+    RDC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_step, threads, smem));
     return std::max(1, per_sm) * sms;
 }
 
