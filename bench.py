@@ -39,7 +39,7 @@ DENSITY = 0.25
 N_MIN, N_MAX = 200, 20000
 # DRAM bytes per particle of one fused step (dram__bytes_read.sum + dram__bytes_write.sum of one ncu
 # capture of k_engine_step on the first 512 replicas of the ensemble, divided by its particles).
-DRAM_BYTES_PER_PARTICLE = (90.13e6 + 126.86e6) / 2097522
+DRAM_BYTES_PER_PARTICLE = (75.89e6 + 115.51e6) / 2097522
 # algorithmic bytes of one fused step per particle: the particle state (float4 position with the type,
 # uint32 id) read once and written once
 ALG_BYTES_PER_PARTICLE = 2 * (16 + 4)
