@@ -120,7 +120,7 @@ struct rdc_batch {
             D.records = nullptr;
             so[r] = soff;
             eo[r] = eoff;
-            soff += D.geo.ncells + 3;
+            soff += (D.geo.ncells + 3 + 3) / 4 * 4;  // 16-byte aligned slices (vector copies of 16-bit starts)
             eoff += D.ecap;
             if (soff > INT_MAX / 2 || eoff > INT_MAX / 2) throw std::invalid_argument("batch too large");
         }

@@ -21,6 +21,29 @@ __device__ inline void block_copy(D *dst, const T *src, int n) {
     __syncthreads();
 }
 
+// 16-bit cell starts between global and shared memory, 8 entries per 16-byte access; both arrays are
+// 16-byte aligned and padded to a multiple of 8 entries
+__device__ inline void copy_starts16(uint16_t *dst, const uint16_t *src, int n) {
+    const int nv = (n + 7) >> 3;
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) d4[k] = s4[k];
+    __syncthreads();
+}
+
+// int cell starts narrowed to 16 bits in place (values < 65536): chunk by chunk every thread reads its
+// int before any thread writes, and the 16-bit writes of a chunk only cover ints already read
+__device__ inline void narrow_starts_inplace(int *a, int n) {
+    uint16_t *b = reinterpret_cast<uint16_t *>(a);
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int k = base + (int)threadIdx.x;
+        const int v = k < n ? a[k] : 0;
+        __syncthreads();
+        if (k < n) b[k] = (uint16_t)v;
+        __syncthreads();
+    }
+}
+
 // in-place exclusive scan of a[0..n) by one block (shared or global memory); a[n] = total
 template <typename T>
 __device__ inline void block_scan_inplace(T *a, int n) {
@@ -196,7 +219,8 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
     int *bin = D.bin, *rank = D.rank, *src = D.src;
     int *gstart = D.start;
     constexpr bool in_smem = sizeof(C) == sizeof(uint16_t);
-    if (in_smem) block_copy(cells, gstart, nc + 3);
+    // between steps a shared-memory replica keeps its starts as 16-bit entries in its start array
+    if (in_smem) copy_starts16(reinterpret_cast<uint16_t *>(cells), reinterpret_cast<const uint16_t *>(gstart), nc + 3);
     const int n = st.n, n_in = st.n_in;
 
     // forces on the current state, Euler step into Y, bins of the new positions
@@ -261,7 +285,7 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
             }
         }
     }
-    if (in_smem) block_copy(gstart, cells, nc + 3);
+    if (in_smem) copy_starts16(reinterpret_cast<uint16_t *>(gstart), reinterpret_cast<const uint16_t *>(cells), nc + 3);
     int rec = st.rec;
     if (D.records && D.count_stride > 0 && (step + 1) % (uint64_t)D.count_stride == 0 && rec < D.max_records) {
         block_count_types(D.pos[cur], n_final, T, D.records + (size_t)rec * T);
@@ -366,6 +390,7 @@ __global__ void k_engine_admit(EngineDev E, const int *list, int count, int fill
         st.n = n2;
         st.n_in = nin2;
         st.cur ^= 1;
+        if (D.smem_cells) narrow_starts_inplace(D.start, D.geo.ncells + 3);
         if (D.records && D.count_stride > 0 && st.rec == 0 && D.max_records > 0) {
             block_count_types(D.pos[st.cur], st.n, E.tabs[D.table].ntypes, D.records);
             st.rec = 1;
