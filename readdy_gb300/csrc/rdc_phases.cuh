@@ -69,11 +69,14 @@ __device__ inline bool stencil_fast(const G &g, int radius) {
 
 template <typename G, typename S, typename F>
 __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__restrict__ start, int radius,
-                                               F f) {
+                                               F f, bool skip_lower_columns = false) {
     int cx, cy, cz;
     cell_coords(p, g, cx, cy, cz);
     const int dx0 = g.dims[0], dy0 = g.dims[1], dz0 = g.dims[2];
     if (stencil_fast(g, radius)) {
+        // a column stored wholly before the particle's own column holds only smaller storage indices;
+        // walks that want partners j > i (skip_lower_columns) need not read its starts
+        const int own_base = (cx * dy0 + cy) * dz0;
 #pragma unroll 1
         for (int ox = -1; ox <= 1; ++ox) {
             int x = cx + ox;
@@ -95,6 +98,7 @@ __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__
                     y -= dy0;
                 }
                 const int base = (x * dy0 + y) * dz0;
+                if (skip_lower_columns && base < own_base) continue;
                 int z0 = cz - 1, z1 = cz + 1;
                 if (z0 < 0) {
                     if (g.pbc[2]) f(start[base + dz0 - 1], start[base + dz0]);
@@ -182,7 +186,7 @@ __device__ inline void for_each_candidate_q(float4 p, const G &g, const S *__res
             re[nr] = je;
             ++nr;
         }
-    });
+    }, jmin > 0);
     if (nr == 0) return;
     int r = 0, j = rb[0], je = re[0];
     float4 q = pos[j];
