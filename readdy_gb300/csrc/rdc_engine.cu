@@ -50,7 +50,7 @@ __device__ inline void block_scan_inplace(T *a, int n) {
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    constexpr int ITEMS = 4;
+    constexpr int ITEMS = 8;
     const int tile = blockDim.x * ITEMS;
     for (int base = 0; base < n; base += tile) {
         const int b = base + threadIdx.x * ITEMS;
@@ -86,7 +86,11 @@ __device__ inline void block_rank(int n, const int *bin, int *rank, int *cells, 
 // 16-bit counters, two per 32-bit word (4-byte aligned array); a count never exceeds the replica's
 // particles (< 65536), so an increment never carries into the neighbouring counter
 __device__ inline void block_rank(int n, const int *bin, int *rank, uint16_t *cells, int nbins) {
-    block_zero(cells, nbins);
+    {   // zero 8 counters per 16-byte store (the shared array is 16-byte aligned and padded)
+        uint4 *c4 = reinterpret_cast<uint4 *>(cells);
+        for (int k = threadIdx.x; k < (nbins + 7) >> 3; k += blockDim.x) c4[k] = make_uint4(0u, 0u, 0u, 0u);
+        __syncthreads();
+    }
     unsigned *w = reinterpret_cast<unsigned *>(cells);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int b = bin[i];
@@ -118,8 +122,13 @@ __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n
     __shared__ int nbig;
     if (threadIdx.x == 0) nbig = 0;
     __syncthreads();
-    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    // order every bin (cells and the out-of-box bin) holding two or more particles by source index;
+    // the particle of rank 0 in a bin does it, so the loop runs over particles, not over the 4x more cells
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = bin[i];
+        if (c > nc || rank[i] != 0) continue;
         const int b = cells[c], e = cells[c + 1];
+        if (e - b < 2) continue;
         if (e - b > CELL_SORT_SMALL) {
             const int q = atomicAdd(&nbig, 1);
             if (q < 64) big[q] = c;
@@ -128,11 +137,11 @@ __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n
         insertion_sort(src, b, e);
     }
     __syncthreads();
-    // crowded cells: ordered by the whole block (rank[] is free scratch after the scatter)
+    // crowded cells: ordered by the whole block (rank[] is free scratch now)
     if (nbig <= 64) {
         for (int q = 0; q < nbig; ++q) block_rank_sort(src, const_cast<int *>(rank), cells[big[q]], cells[big[q] + 1]);
     } else {
-        for (int c = 0; c < nc; ++c)
+        for (int c = 0; c <= nc; ++c)
             if (cells[c + 1] - cells[c] > CELL_SORT_SMALL) block_rank_sort(src, const_cast<int *>(rank), cells[c], cells[c + 1]);
     }
     n_new = cells[nc + 1];
