@@ -179,6 +179,54 @@ def test_external_potential_known_answers(rg, case):
     np.testing.assert_allclose(f, exp, rtol=0, atol=max(case["force_atol"], FORCE_RTOL * scale))
 
 
+def _run_reference_loop(k, ctx, dt, n_steps, check):
+    """run() of readdy/test/TestPotentials.cpp:56-73: forces, Euler BD and neighbour-list update for
+    200 steps, with the positions checked after every step."""
+    cutoff = ctx.calculate_max_cutoff()
+    if cutoff > 0:
+        k.create_neighbor_list(cutoff)
+    for _ in range(n_steps):
+        k.calculate_forces()
+        k.euler_bd_integrator(dt)
+        if cutoff > 0:
+            k.update_neighbor_list()
+        p, _, _ = k.get_particles()
+        check(p)
+
+
+def test_box_potential_confines_particles(rg):
+    """TestPotentials.cpp:80-125: 10 A (D = 1) and 10 B (D = 0.1) near the origin of a non-periodic
+    1^3 box, each under a harmonic box of k = 10 spanning [-1, 1]^3, A-B repulsion k = 0.01 d = 0.11:
+    over 200 steps of 0.005 every particle stays within [-2.5, 2.5]^3 (most of them outside the
+    simulation box, where only the external potential acts on them)."""
+    rng = np.random.default_rng(12)
+    ctx = rg.Context((1., 1., 1.), (False, False, False), 1.0, (1.0, 0.1))
+    ctx.add_harmonic_repulsion(0, 1, 0.01, 0.11)
+    for t in (0, 1):
+        ctx.add_box(t, 10.0, (-1., -1., -1.), (2., 2., 2.))
+    k = rg.CUDAKernel(ctx, seed=3)
+    k.add_particles(rng.normal(size=(20, 3)), [0] * 10 + [1] * 10)
+
+    def check(p):
+        assert np.all(np.abs(p) <= 2.5), np.abs(p).max()
+    _run_reference_loop(k, ctx, 0.005, 200, check)
+
+
+def test_spherical_inclusion_confines_particles(rg):
+    """TestPotentials.cpp:126-166: spherical inclusion of radius 3 (k = 20) in a non-periodic 10^3 box:
+    every particle stays within distance 4 of the origin for 200 steps of 0.005."""
+    rng = np.random.default_rng(13)
+    ctx = rg.Context((10., 10., 10.), (False, False, False), 1.0, (1.0, 0.1))
+    for t in (0, 1):
+        ctx.add_sphere(t, 20.0, (0., 0., 0.), 3.0, True)
+    k = rg.CUDAKernel(ctx, seed=4)
+    k.add_particles(rng.normal(size=(20, 3)), [0] * 10 + [1] * 10)
+
+    def check(p):
+        assert np.all((p * p).sum(1) < 16.0)
+    _run_reference_loop(k, ctx, 0.005, 200, check)
+
+
 @pytest.mark.parametrize("pair", [False, True], ids=["external_only", "with_pairs"])
 def test_external_potentials_match_oracle(rg, pair):
     """All eight order-1 forms on random positions, alone (each particle's force is one term, so the
