@@ -352,7 +352,7 @@ def run_gb300(args, rank, world):
     import readdy_gb300 as rg
     from readdy_gb300.batch import ReplicaBatch
     rg.load()
-    seed = args.seed + 1000003 * rank
+    seed = rank_seed(args.seed, rank)
     ns, boxes, pos, types = ensemble(seed, args.replicas)
     caps = ns + 64
     ctx = chemistry()
@@ -488,15 +488,31 @@ def run_reference(args):
 _dist = None
 
 
+_dist_device = "cpu"
+
+
+def rank_seed(seed: int, rank: int) -> int:
+    """Seed of a rank's ensemble: every rank advances its own, disjoint set of replicas."""
+    return seed + 1000003 * rank
+
+
 def init_dist():
-    global _dist
+    """One process per GPU under torchrun (NCCL); gloo on machines without CUDA.  The only collectives
+    are the barrier around the timed region and the reductions of its time (max) and particle-steps
+    (sum): replicas are independent, so the data path has no exchange."""
+    global _dist, _dist_device
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            dist.init_process_group("nccl")
+            _dist_device = "cuda"
+        else:
+            dist.init_process_group("gloo")
+            _dist_device = "cpu"
         _dist = dist
     return rank, world
 
@@ -510,7 +526,7 @@ def _allreduce(v, world, op):
     if world <= 1 or _dist is None:
         return v
     import torch
-    t = torch.tensor([float(v)], device="cuda")
+    t = torch.tensor([float(v)], dtype=torch.float64, device=_dist_device)
     _dist.all_reduce(t, op=op)
     return float(t.item())
 
