@@ -187,6 +187,11 @@ int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *
 /* handler, time step and the launch knobs: cell width as a multiple (>= 1) of the largest cutoff, and
  * threads per block (one block advances one replica at a time) */
 int rdc_batch_configure(rdc_batch *b, int handler, double dt, double cell_width_scale, int threads_per_block);
+/* on (the default): a replica with reactions and shared-memory cells sums its pair forces in the
+ * stencil walk of its event search and carries them to the next step's Euler update (two float4
+ * per particle slot); off: the forces are summed at the start of every step.  Trajectories are
+ * bitwise the same either way. */
+int rdc_batch_set_carry_forces(rdc_batch *b, int on);
 /* advance every replica n_steps; each step is one fused launch replayed from a CUDA graph */
 int rdc_batch_step(rdc_batch *b, int64_t n_steps);
 /* rdc_batch_step bracketed by CUDA events on the batch's stream; *device_ms receives the device time */

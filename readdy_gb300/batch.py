@@ -68,6 +68,11 @@ class ReplicaBatch:
         self.handler, self.dt = handler, dt
         self.cell_width_scale, self.threads_per_block = cell_width_scale, threads_per_block
 
+    def set_carry_forces(self, on=True):
+        """Pair forces carried from each step's event walk to the next step (default) or summed at
+        the start of every step; the trajectories are bitwise the same."""
+        N.check(self._lib.rdc_batch_set_carry_forces(self._h, 1 if on else 0))
+
     def step(self, n_steps=1):
         N.check(self._lib.rdc_batch_step(self._h, int(n_steps)))
 

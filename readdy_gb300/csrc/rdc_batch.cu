@@ -58,6 +58,7 @@ struct rdc_batch {
     std::vector<double> boxes;
     // flat per-particle arrays; replica r owns slots [poff[r], poff[r] + caps[r])
     float4 *posA = nullptr, *posB = nullptr;
+    float4 *forceA = nullptr, *forceB = nullptr;  // pair forces carried between steps
     uint32_t *idA = nullptr, *idB = nullptr;
     int *bin = nullptr, *rank = nullptr, *src = nullptr, *claim = nullptr, *taken = nullptr;
     int *start = nullptr;
@@ -86,7 +87,7 @@ struct rdc_batch {
         graph = nullptr;
         bfree(desc_dev); bfree(state_dev); bfree(order_dev); bfree(n_work_dev); bfree(work_dev); bfree(all_dev);
         bfree(tab_dev); bfree(count_dev); bfree(reaction_counts); bfree(particle_steps);
-        bfree(posA); bfree(posB); bfree(idA); bfree(idB);
+        bfree(posA); bfree(posB); bfree(forceA); bfree(forceB); bfree(idA); bfree(idB);
         bfree(bin); bfree(rank); bfree(src); bfree(claim); bfree(taken); bfree(start); bfree(events);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -132,6 +133,8 @@ struct rdc_batch {
             RepDesc &D = desc[r];
             const int64_t p = poff[r];
             D.pos[0] = posA + p; D.pos[1] = posB + p;
+            D.force[0] = forceA ? forceA + p : nullptr;
+            D.force[1] = forceB ? forceB + p : nullptr;
             D.id[0] = idA + p; D.id[1] = idB + p;
             D.bin = bin + p; D.rank = rank + p; D.src = src + p; D.claim = claim + p; D.taken = taken + p;
             D.start = start + so[r];
@@ -159,6 +162,7 @@ struct rdc_batch {
         }
         if (total > INT_MAX / 2) throw std::invalid_argument("batch capacity too large");
         posA = balloc<float4>(total); posB = balloc<float4>(total);
+        forceA = balloc<float4>(total); forceB = balloc<float4>(total);
         idA = balloc<uint32_t>(total); idB = balloc<uint32_t>(total);
         bin = balloc<int>(total); rank = balloc<int>(total); src = balloc<int>(total);
         claim = balloc<int>(total); taken = balloc<int>(total);
@@ -235,6 +239,29 @@ struct rdc_batch {
         RDC_CUDA(cudaMemcpyAsync(h.data(), state_dev, sizeof(RepState) * R, cudaMemcpyDeviceToHost, stream));
         sync();
         return h;
+    }
+
+    // pair forces carried between steps (allocated) or summed at the start of every step (freed)
+    void set_carry_forces(bool on) {
+        int64_t total = 0;
+        for (int64_t c : caps) total += c;
+        if (on && !forceA) {
+            forceA = balloc<float4>(total);
+            forceB = balloc<float4>(total);
+        } else if (!on && forceA) {
+            sync();
+            bfree(forceA); bfree(forceB);
+            forceA = forceB = nullptr;
+        }
+        for (int r = 0; r < R; ++r) {
+            desc[r].force[0] = forceA ? forceA + poff[r] : nullptr;
+            desc[r].force[1] = forceB ? forceB + poff[r] : nullptr;
+        }
+        RDC_CUDA(cudaMemcpyAsync(desc_dev, desc.data(), sizeof(RepDesc) * R, cudaMemcpyHostToDevice, stream));
+        auto st = states();
+        for (auto &x : st) x.fvalid = 0;
+        RDC_CUDA(cudaMemcpyAsync(state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, stream));
+        sync();
     }
 
     void check_status() {
@@ -332,7 +359,7 @@ int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *
                 std::memcpy(&p.w, &t, 4);
                 hp[b->poff[r] + i] = p;
             }
-            st[r] = RepState{(int)n[r], 0, 0, (int)n[r], 0, 0, 0};
+            st[r] = RepState{(int)n[r], 0, 0, (int)n[r], 0, 0, 0, 0};
         }
         RDC_CUDA(cudaMemcpyAsync(b->posA, hp.data(), sizeof(float4) * total, cudaMemcpyHostToDevice, b->stream));
         RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, b->stream));
@@ -365,6 +392,13 @@ int rdc_batch_configure(rdc_batch *b, int handler, double dt, double cell_width_
         }
         b->invalidate_graph();
         b->sync();
+    });
+}
+
+int rdc_batch_set_carry_forces(rdc_batch *b, int on) {
+    BATCH_CALL({
+        if (!b) throw std::invalid_argument("null argument");
+        b->set_carry_forces(on != 0);
     });
 }
 

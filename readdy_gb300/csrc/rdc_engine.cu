@@ -211,10 +211,112 @@ size_t engine_smem_bytes(int max_events) {
            sizeof(uint16_t) * (SMEM_CELLS + 4) + 16;
 }
 
+// The candidate pass of block_events and the pair forces of the same sorted state in one stencil walk
+// per particle: the walk that sums particle i's pair forces also finds its reaction partners j > i,
+// and force[i] receives the sum (zero outside the cells).  The walk runs without block barriers, like
+// the plain force walk.  It keeps up to two partner tuples in registers and lists them after the
+// walk (measured: an atomic list append inside the divergent candidate loop made the walk 8x slower);
+// a particle with more partners lists its tuples by its own event walk.  The list holds up to `room`
+// tuples in global scratch (tp1, tp2, tr) and the coins are drawn after it with all lanes converged;
+// a list that overflows is dropped and block_events generates the tuples again.  Tuples, coins and
+// forces are those of block_events and pair_force_at on their own.
+template <typename G, typename Emit>
+__device__ __forceinline__ void block_events_forces(int n, int n_in, const float4 *__restrict__ pos,
+                                                    const uint32_t *__restrict__ id,
+                                                    const uint16_t *__restrict__ start, const G &g,
+                                                    const SmemLayout &S, int T, bool pair_pots, const RxnTables &rt,
+                                                    uint64_t seed, uint64_t step, int handler,
+                                                    float4 *__restrict__ force, int *tp1, int *tp2, int *tr, int room,
+                                                    Emit emit) {
+    int *count = S.queue.count;
+    auto push = [&](int a, int b, int r) {
+        const int k = atomicAdd(count, 1);
+        if (k < room) {
+            tp1[k] = a;
+            tp2[k] = b;
+            tr[k] = r;
+        }
+    };
+    if (threadIdx.x == 0) *count = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float4 p = pos[i];
+        const int ti = itype(p);
+        float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+        if (ti >= 0) {
+            const bool pairs = i < n_in && rt.o2_any[ti];
+            int t0 = 0, t1 = 0, nt = 0;  // partner tuples j | r << 16 (j < 65536 in shared-memory replicas)
+            if (i < n_in && (pairs || pair_pots)) {
+                const int *rrow = rt.o2_tab + ti * rt.T;
+                const float *rsrow = rt.screen + ti * rt.T;
+                auto partner = [&](int j, float4 q, int tj, float d2s) {
+                    if (!pairs || j < i) return;
+                    const int o2 = rrow[tj];
+                    if (o2 == 0 || d2s > rsrow[tj]) return;
+                    const PairGeom g0 = pair_geom(p, q, g);
+                    for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
+                        const int r = rt.o2_list[k];
+                        const ReactionDev &R = rt.rx[r];
+                        if (!R.active) continue;
+                        PairGeom gg = g0;
+                        if (within(g0, gg, p, q, g, R.educt_distance2f, R.band, R.educt_distance2)) {
+                            if (nt == 0) t0 = j | (r << 16);
+                            else if (nt == 1) t1 = j | (r << 16);
+                            ++nt;
+                        }
+                    }
+                };
+                pair_force_at(i, p, pos, start, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e, nullptr, partner);
+            }
+            if (nt > 2) {
+                event_tuples_at(i, true, pos, start, g, 1, rt, push);
+            } else {
+                const int o1 = rt.o1_tab[ti];
+                for (int k = (o1 >> 8); k < (o1 >> 8) + (o1 & 0xff); ++k) {
+                    const int r = rt.o1_list[k];
+                    if (rt.rx[r].active) push(i, i, r);
+                }
+                if (nt > 0) push(i, t0 & 0xffff, t0 >> 16);
+                if (nt > 1) push(i, t1 & 0xffff, t1 >> 16);
+            }
+        }
+        force[i] = make_float4(fx, fy, fz, 0.f);
+    }
+    __syncthreads();
+    const int nq = *count;
+    __syncthreads();
+    if (nq > room) {
+        block_events(0, blockDim.x, n, n_in, pos, id, start, g, 1, rt, seed, step, handler, S.queue, emit);
+        return;
+    }
+    for (int k = threadIdx.x; k < nq; k += blockDim.x)
+        event_coin(tp1[k], tp2[k], tr[k], id, rt, seed, step, handler, emit);
+    __syncthreads();
+}
+
+// sets the bits of the cells of the 3x3x3 stencil around cell c: the cells whose particles see c
+// (the stencil relation is symmetric)
+__device__ inline void mark_stencil(uint32_t *mark, int c, const Geo &g) {
+    const int dy = g.dims[1], dz = g.dims[2];
+    int ax[3], ay[3], az[3];
+    const int nx = axis_cells(c / (dy * dz), g.dims[0], g.pbc[0], 1, ax);
+    const int ny = axis_cells((c / dz) % dy, dy, g.pbc[1], 1, ay);
+    const int nz = axis_cells(c % dz, dz, g.pbc[2], 1, az);
+    for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b)
+            for (int k = 0; k < nz; ++k) {
+                const int m = az[k] + dz * (ay[b] + dy * ax[a]);
+                atomicOr(&mark[m >> 5], 1u << (m & 31));
+            }
+}
+
+__device__ inline bool marked(const uint32_t *mark, int c) { return (mark[c >> 5] >> (c & 31)) & 1u; }
+
 // one step of one replica by the whole block; C is the cell array's type (uint16_t in shared memory
-// or int in global memory)
+// or int in global memory).  Inlined into the kernel: as a call, the geometry and tables it passes
+// down by reference live in local memory and the candidate walks reload them per candidate.
 template <typename C>
-__device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, const RxnTables &rt, const Tables *tab,
+__device__ __forceinline__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, const RxnTables &rt, const Tables *tab,
                              const RepDesc &D, const RepState &st, int &sh_nev, int &sh_status, C *cells) {
     const int T = tab->ntypes, NP = tab->npots;
     const uint64_t step = (uint64_t)st.step;
@@ -231,12 +333,20 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
     // between steps a shared-memory replica keeps its starts as 16-bit entries in its start array
     if (in_smem) copy_starts16(reinterpret_cast<uint16_t *>(cells), reinterpret_cast<const uint16_t *>(gstart), nc + 3);
     const int n = st.n, n_in = st.n_in;
+    // forces stored by the previous step's event walk (replicas with reactions and shared-memory cells)
+    const bool fuse = in_smem && tab->nreactions > 0 && D.force[0] != nullptr;
+    const float4 *fX = (fuse && st.fvalid) ? D.force[st.cur] : nullptr;
 
     // forces on the current state, Euler step into Y, bins of the new positions
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 p = posX[i];
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-        if (i < n_in && NP > 0) pair_force_at(i, p, posX, cells, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e);
+        if (fX) {
+            const float4 f = fX[i];
+            fx = f.x; fy = f.y; fz = f.z;
+        } else if (i < n_in && NP > 0) {
+            pair_force_at(i, p, posX, cells, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e);
+        }
         const uint32_t id = idX[i];
         const int t = itype(p);
         if (t >= 0) {  // order-1 potentials
@@ -253,8 +363,11 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
     int n1, nin1;
     block_sort(posY, idY, n, posX, idX, bin, rank, src, cells, gs, n1, nin1);
 
-    int n_final = n1, nin_final = nin1, cur = st.cur, next_id = st.next_id;
+    int n_final = n1, nin_final = nin1, cur = st.cur, next_id = st.next_id, fvalid = 0;
     if (tab->nreactions > 0) {
+        // the next step's forces come from this step's event walk unless this is the replica's last step
+        const bool keep = fuse && st.step + 1 < D.n_steps;
+        uint32_t *mark = reinterpret_cast<uint32_t *>(S.queue.p1);  // cell bitmap, free after the coins
         EventRec *ev = D.events;
         const int ecap = D.ecap;
         auto emit = [&](uint64_t key, int p1, int p2, int rr) {
@@ -267,8 +380,25 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
                 atomicOr(&sh_status, ST_EVENTS);
             }
         };
-        block_events(0, blockDim.x, n1, nin1, posX, idX, cells, g, 1, rt, D.seed, step, E.handler, S.queue, emit);
+        if (keep)
+            // the sort scratch (bin, rank, src) is free until the re-sort: it holds the tuple list
+            block_events_forces(n1, nin1, posX, idX, reinterpret_cast<const uint16_t *>(cells), g, S, T, NP > 0, rt,
+                                D.seed, step, E.handler, D.force[st.cur], bin, rank, src, D.cap, emit);
+        else
+            block_events(0, blockDim.x, n1, nin1, posX, idX, cells, g, 1, rt, D.seed, step, E.handler, S.queue, emit);
+        fvalid = keep ? 1 : 0;
         const int Ev = min(sh_nev, ecap);
+        if (Ev > 0 && keep) {
+            // cells around the educts, before the reactions move or remove them
+            for (int k = threadIdx.x; k < (nc + 31) / 32; k += blockDim.x) mark[k] = 0u;
+            __syncthreads();
+            for (int k = threadIdx.x; k < 2 * Ev; k += blockDim.x) {
+                const EventRec e = ev[k >> 1];
+                const int c = bin_of(posX[(k & 1) ? e.p2 : e.p1], gs);
+                if (c < nc) mark_stencil(mark, c, gs);
+            }
+            __syncthreads();
+        }
         if (Ev > 0) {
             ApplyTarget t;
             t.pos = posX; t.id = idX; t.tslot = nullptr; t.force = nullptr;
@@ -285,9 +415,42 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
                 // particles changed cells, appeared or vanished: sort again, into Y
                 const int n_total = n1 + res.births;
                 block_bin(posX, n_total, bin, gs);
+                if (keep) {
+                    // cells around the products and the births
+                    for (int k = threadIdx.x; k < 2 * Ev + res.births; k += blockDim.x) {
+                        int c;
+                        if (k < 2 * Ev) {
+                            const EventRec e = ev[k >> 1];
+                            c = bin[(k & 1) ? e.p2 : e.p1];
+                        } else {
+                            c = bin[n1 + k - 2 * Ev];
+                        }
+                        if (c < nc) mark_stencil(mark, c, gs);
+                    }
+                }
                 block_rank(n_total, bin, rank, cells, nc + 2);
                 int n2, nin2;
                 block_sort(posX, idX, n_total, posY, idY, bin, rank, src, cells, gs, n2, nin2);
+                if (keep) {
+                    // forces follow their particles; a particle whose stencil saw a reaction walks again
+                    const float4 *fi = D.force[st.cur];
+                    float4 *fo = D.force[st.cur ^ 1];
+                    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                        const int k = src[i];
+                        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (i < nin2) {
+                            if (!marked(mark, bin[k])) {
+                                f = fi[k];
+                            } else if (NP > 0) {
+                                float e = 0.f;
+                                pair_force_at(i, posY[i], posY, cells, g, 1, S.tab, S.screen, S.pots, T, f.x, f.y,
+                                              f.z, e);
+                            }
+                        }
+                        fo[i] = f;
+                    }
+                    __syncthreads();
+                }
                 n_final = n2;
                 nin_final = nin2;
                 cur ^= 1;
@@ -309,6 +472,7 @@ __device__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, con
         o.next_id = next_id;
         o.status = st.status | sh_status;
         o.rec = rec;
+        o.fvalid = fvalid;
         o.step = st.step + 1;
         E.state[r] = o;
     }
@@ -399,6 +563,7 @@ __global__ void k_engine_admit(EngineDev E, const int *list, int count, int fill
         st.n = n2;
         st.n_in = nin2;
         st.cur ^= 1;
+        st.fvalid = 0;
         if (D.smem_cells) narrow_starts_inplace(D.start, D.geo.ncells + 3);
         if (D.records && D.count_stride > 0 && st.rec == 0 && D.max_records > 0) {
             block_count_types(D.pos[st.cur], st.n, E.tabs[D.table].ntypes, D.records);

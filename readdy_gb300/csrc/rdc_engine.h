@@ -8,9 +8,13 @@
 //   resolution + application -> (re-sort if particles appeared or vanished) -> observables
 //
 // The arithmetic is the per-system path's (rdc_phases.cuh), so a replica gives the same trajectory
-// alone, inside any batch or request mix, or through rdc_run with the replica's seed.  Forces are
-// computed at the start of a step from the state left by the previous step's reactions, which is where
-// SimulationLoop::run computes them (SimulationLoop.h:283-289).
+// alone, inside any batch or request mix, or through rdc_run with the replica's seed.  Forces act on
+// the state left by the previous step's reactions, which is where SimulationLoop::run computes them
+// (SimulationLoop.h:283-289).  A replica with reactions and shared-memory cells computes them one
+// walk earlier: the stencil walk that looks for reaction partners after the sort also sums every
+// particle's pair force and stores it; after the reactions, only particles whose 27-cell stencil
+// held a reacting particle walk again.  The stored forces are the ones a walk over the final state
+// gives, bit for bit: an untouched stencil holds the same particles in the same storage order.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -42,6 +46,7 @@ struct RepDesc {
     Geo geo;
     float4 *pos[2];              // double buffer; state.cur selects the current one
     uint32_t *id[2];
+    float4 *force[2];            // pair forces on pos[k] between steps (null: summed at the step start)
     int *bin, *rank, *src, *claim, *taken;   // capacity entries each
     int *start;                  // cell starts between steps, ncells + 3 entries
     EventRec *events;            // ecap entries
@@ -58,6 +63,7 @@ struct RepDesc {
 
 struct RepState {
     int n, n_in, cur, next_id, status, rec;  // rec: count records written
+    int fvalid;                              // force[cur] holds the pair forces on pos[cur]
     int64_t step;                            // steps run (keys the random streams)
 };
 

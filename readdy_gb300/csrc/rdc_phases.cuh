@@ -4,6 +4,7 @@
 #pragma once
 #include <climits>
 #include <cstdint>
+#include <type_traits>
 
 #include "rdc_device.cuh"
 #include "rdc_host.h"
@@ -266,10 +267,19 @@ constexpr int PAIR_BUFFER = 4;
 // With vir non-null, vir[3a+b] also receives half of -x_ij[a] f_i[b] per pair: the virial
 // sum over pairs of outer(-x_ij, f_i) of calculateOrder2<true> (CPUCalculateForces.cpp:247-249), seen
 // here once from each side.
-template <typename G, typename S>
+// With an `extra` callable, extra(j, q, tj, d2) also sees every live candidate j != i of the walk with
+// its FP32 screening distance, before the force filters: the replica engine finds its reaction
+// pairs in the same walk.  The force arithmetic and its order do not depend on it.
+struct NoExtra {
+    __device__ void operator()(int, float4, int, float) const {}
+};
+
+template <typename G, typename S, typename Extra = NoExtra>
 __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const S *__restrict__ start,
                                      const G &g, int radius, const int *tab, const float *screen, const PairPot *pots,
-                                     int T, float &fx, float &fy, float &fz, float &e, float *vir = nullptr) {
+                                     int T, float &fx, float &fy, float &fz, float &e, float *vir = nullptr,
+                                     Extra extra = Extra()) {
+    constexpr bool has_extra = !std::is_same<Extra, NoExtra>::value;
     const int ti = itype(p);
     const int *trow = tab + ti * T;
     const float *srow = screen + ti * T;
@@ -302,8 +312,14 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
         if (j == i) return;
         const int tj = itype(q);
         if (tj < 0) return;
-        if (trow[tj] == 0) return;
-        if (screen_d2(p, q, g) > srow[tj]) return;
+        if constexpr (has_extra) {
+            const float d2s = screen_d2(p, q, g);
+            extra(j, q, tj, d2s);
+            if (trow[tj] == 0 || d2s > srow[tj]) return;
+        } else {
+            if (trow[tj] == 0) return;
+            if (screen_d2(p, q, g) > srow[tj]) return;
+        }
         if (nb == PAIR_BUFFER) {  // full: evaluate the oldest survivor now and shift
             body(b0);
             b0 = b1; b1 = b2; b2 = b3;

@@ -55,7 +55,7 @@ struct EngineLayout {
 EngineLayout engine_layout(int64_t cap, int ncells, int ecap, int max_records, int ntypes) {
     EngineLayout L{};
     size_t off = 0;
-    L.pos = off; off += up(2 * sizeof(float4) * cap);
+    L.pos = off; off += up(4 * sizeof(float4) * cap);  // two position and two force buffers
     L.id = off; off += up(2 * sizeof(uint32_t) * cap);
     L.ints = off; off += up(5 * sizeof(int) * cap);
     L.start = off; off += up(sizeof(int) * (ncells + 3));
@@ -271,6 +271,8 @@ struct rdc_server {
             D.geo = q.geo;
             D.pos[0] = reinterpret_cast<float4 *>(b + q.L.pos);
             D.pos[1] = D.pos[0] + q.cap;
+            D.force[0] = D.pos[1] + q.cap;
+            D.force[1] = D.force[0] + q.cap;
             D.id[0] = reinterpret_cast<uint32_t *>(b + q.L.id);
             D.id[1] = D.id[0] + q.cap;
             int *ints = reinterpret_cast<int *>(b + q.L.ints);
@@ -290,7 +292,7 @@ struct rdc_server {
             D.max_records = q.max_records;
             Tables tab;
             build_tables(q.ctx, q.ctx.box, q.dt, tab);
-            RepState S{(int)q.n, 0, 0, (int)q.n, 0, 0, 0};
+            RepState S{(int)q.n, 0, 0, (int)q.n, 0, 0, 0, 0};
             RDC_CUDA(cudaMemcpyAsync(D.pos[0], q.pos.data(), sizeof(float4) * q.n, cudaMemcpyHostToDevice, stream));
             RDC_CUDA(cudaMemsetAsync(D.claim, 0x7f, sizeof(int) * q.cap, stream));
             RDC_CUDA(cudaMemsetAsync(D.taken, 0, sizeof(int) * q.cap, stream));

@@ -447,6 +447,62 @@ def test_batch_replica_equals_plain_run(rg, handler, external):
         np.testing.assert_allclose(pa, pb, rtol=0, atol=1e-5)
 
 
+def _reactive_batch(rg, periodic, dense, carry):
+    """Six replicas of four species under harmonic repulsion with fast fusion, fission, conversion,
+    decay and enzymatic reactions (capacity twice the initial count)."""
+    from readdy_gb300.batch import ReplicaBatch
+    rng = np.random.default_rng(31)
+    density, reach = (1.0, 2.0) if dense else (0.25, 1.0)
+    sizes = [200, 700, 1500, 3000, 450, 5000]
+    boxes, poss, typess = [], [], []
+    for n in sizes:
+        L = float(np.float32((n / density) ** (1 / 3)))
+        boxes.append((L, L, L))
+        poss.append(f32((rng.random((n, 3)) - 0.5) * L))
+        typess.append(rng.integers(0, 4, n).astype(np.int32))
+    ctx = rg.Context(boxes[0], (periodic,) * 3, 1.0, (1.0, 1.0, 0.5, 0.8))
+    for a in range(4):
+        for b in range(a, 4):
+            ctx.add_harmonic_repulsion(a, b, 10.0, 1.0)
+    ctx.add_fusion(0, 1, 2, 5.0, reach)
+    ctx.add_fission(2, 0, 1, 2.0, 1.0)
+    ctx.add_conversion(0, 3, 0.5)
+    ctx.add_decay(3, 0.5)
+    ctx.add_enzymatic(2, 1, 0, 1.0, reach)
+    b = ReplicaBatch(ctx, boxes, [2 * n for n in sizes], seed=5)
+    b.set_particles(poss, typess)
+    b.configure(handler=rg.UNCONTROLLED_APPROXIMATION, dt=1e-3, cell_width_scale=1.0, threads_per_block=256)
+    b.set_carry_forces(carry)
+    return b, sizes
+
+
+@pytest.mark.parametrize("dense", [False, True], ids=["sparse", "dense"])
+@pytest.mark.parametrize("periodic", [True, False], ids=["periodic", "walls"])
+def test_batch_carried_forces_bitwise(rg, periodic, dense):
+    """Pair forces carried from each step's event walk to the next step, with the particles near a
+    reaction walking again, give the trajectory of forces summed at the start of every step bit for
+    bit.  Dense replicas have particles with more reaction partners than the walk keeps in registers
+    and more tuples than the tuple list holds; without walls particles leave the box."""
+    a, sizes = _reactive_batch(rg, periodic, dense, carry=True)
+    b, _ = _reactive_batch(rg, periodic, dense, carry=False)
+    c0 = a.count_types()
+    a.step(150)
+    b.step(150)
+    a.synchronize()
+    b.synchronize()
+    ca, cb = a.count_types(), b.count_types()
+    np.testing.assert_array_equal(ca, cb)
+    assert np.any(ca != c0)
+    for r in range(len(sizes)):
+        pa, ta, ia = a.get_particles(r)
+        pb, tb, ib = b.get_particles(r)
+        (pa, ta, ia) = by_id(ia, pa, ta, ia)
+        (pb, tb, ib) = by_id(ib, pb, tb, ib)
+        np.testing.assert_array_equal(ia, ib)
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_array_equal(pa, pb)
+
+
 @pytest.mark.parametrize("terms", ["bond", "angle", "dihedral", "all"])
 def test_polymer_forces_match_oracle(rg, terms):
     """Random-walk chains (step 1.0) with bond/angle/dihedral terms in solvent, per term type."""
