@@ -258,9 +258,8 @@ struct rdc_batch {
             desc[r].force[1] = forceB ? forceB + poff[r] : nullptr;
         }
         RDC_CUDA(cudaMemcpyAsync(desc_dev, desc.data(), sizeof(RepDesc) * R, cudaMemcpyHostToDevice, stream));
-        auto st = states();
-        for (auto &x : st) x.fvalid = 0;
-        RDC_CUDA(cudaMemcpyAsync(state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, stream));
+        // sorted again, cell starts in place, no forces carried
+        sort_all(false);
         sync();
     }
 
@@ -274,6 +273,7 @@ struct rdc_batch {
             sync();
             if (any & ST_CAPACITY) throw rdc::CapacityError("replica particle capacity exceeded by reaction products");
             if (any & ST_EVENTS) throw rdc::CapacityError("replica reaction event buffer overflow");
+            if (any & ST_INDEX) throw std::runtime_error("replica step met a storage index out of range");
             throw std::runtime_error("replica device status " + std::to_string(any));
         }
     }
@@ -449,8 +449,18 @@ int rdc_batch_count_types(rdc_batch *b, int64_t *counts) {
 int rdc_batch_n_particles(rdc_batch *b, int64_t *n) {
     BATCH_CALL({
         if (!b || !n) throw std::invalid_argument("null argument");
-        auto st = b->states();
-        for (int r = 0; r < b->R; ++r) n[r] = st[r].n;
+        // the per-type counts: a replica's storage may still hold the slots of removed particles
+        const int T = b->ctx.ntypes;
+        launch_engine_count(b->e, b->R, T, b->count_dev, b->stream);
+        std::vector<unsigned long long> h((size_t)b->R * T);
+        RDC_CUDA(cudaMemcpyAsync(h.data(), b->count_dev, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost,
+                                 b->stream));
+        b->sync();
+        for (int r = 0; r < b->R; ++r) {
+            int64_t sum = 0;
+            for (int t = 0; t < T; ++t) sum += (int64_t)h[(size_t)r * T + t];
+            n[r] = sum;
+        }
     });
 }
 

@@ -106,7 +106,8 @@ __device__ inline void block_bin(const float4 *pos, int n, int *bin, const Geo &
 }
 
 // counting sort of one replica from counts in cells: scan to cell starts, scatter, order each cell
-// by source index (deterministic), gather into the destination arrays
+// by particle id (deterministic, and independent of the order of the source arrays), gather into the
+// destination arrays
 template <typename C>
 __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n, float4 *dpos, uint32_t *did,
                                   const int *bin, const int *rank, int *src, C *cells, const Geo &g, int &n_new,
@@ -122,7 +123,7 @@ __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n
     __shared__ int nbig;
     if (threadIdx.x == 0) nbig = 0;
     __syncthreads();
-    // order every bin (cells and the out-of-box bin) holding two or more particles by source index;
+    // order every bin (cells and the out-of-box bin) holding two or more particles by id;
     // the particle of rank 0 in a bin does it, so the loop runs over particles, not over the 4x more cells
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int c = bin[i];
@@ -134,15 +135,17 @@ __device__ inline void block_sort(const float4 *spos, const uint32_t *sid, int n
             if (q < 64) big[q] = c;
             continue;
         }
-        insertion_sort(src, b, e);
+        insertion_sort_by(src, b, e, sid);
     }
     __syncthreads();
     // crowded cells: ordered by the whole block (rank[] is free scratch now)
     if (nbig <= 64) {
-        for (int q = 0; q < nbig; ++q) block_rank_sort(src, const_cast<int *>(rank), cells[big[q]], cells[big[q] + 1]);
+        for (int q = 0; q < nbig; ++q)
+            block_rank_sort_by(src, const_cast<int *>(rank), cells[big[q]], cells[big[q] + 1], sid);
     } else {
         for (int c = 0; c <= nc; ++c)
-            if (cells[c + 1] - cells[c] > CELL_SORT_SMALL) block_rank_sort(src, const_cast<int *>(rank), cells[c], cells[c + 1]);
+            if (cells[c + 1] - cells[c] > CELL_SORT_SMALL)
+                block_rank_sort_by(src, const_cast<int *>(rank), cells[c], cells[c + 1], sid);
     }
     n_new = cells[nc + 1];
     n_in = cells[nc];
@@ -227,7 +230,7 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
                                                     const SmemLayout &S, int T, bool pair_pots, const RxnTables &rt,
                                                     uint64_t seed, uint64_t step, int handler,
                                                     float4 *__restrict__ force, int *tp1, int *tp2, int *tr, int room,
-                                                    Emit emit) {
+                                                    int *status, Emit emit) {
     int *count = S.queue.count;
     auto push = [&](int a, int b, int r) {
         const int k = atomicAdd(count, 1);
@@ -289,8 +292,13 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
         block_events(0, blockDim.x, n, n_in, pos, id, start, g, 1, rt, seed, step, handler, S.queue, emit);
         return;
     }
-    for (int k = threadIdx.x; k < nq; k += blockDim.x)
-        event_coin(tp1[k], tp2[k], tr[k], id, rt, seed, step, handler, emit);
+    for (int k = threadIdx.x; k < nq; k += blockDim.x) {
+        const int a = tp1[k], b = tp2[k], r = tr[k];
+        if ((unsigned)a < (unsigned)n && (unsigned)b < (unsigned)n && (unsigned)r < (unsigned)MAX_REACTIONS)
+            event_coin(a, b, r, id, rt, seed, step, handler, emit);
+        else
+            atomicOr(status, ST_INDEX);
+    }
     __syncthreads();
 }
 
@@ -312,6 +320,188 @@ __device__ inline void mark_stencil(uint32_t *mark, int c, const Geo &g) {
 
 __device__ inline bool marked(const uint32_t *mark, int c) { return (mark[c >> 5] >> (c & 31)) & 1u; }
 
+// first entry of the ascending keys[0, n) that is >= v
+__device__ inline int lower_bound_u64(const uint64_t *keys, int n, uint64_t v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (keys[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Particles a step's reactions changed, in a state they left unsorted: the sorted storage of the step
+// (cell starts `start`, cells in particle-id order) with removed particles (type < 0), particles that
+// took part in a performed reaction (flagged in `taken`: they may have moved and have new ids) and the
+// births appended.  `mkey` lists the changed particles inside the box as cell << 32 | id, ascending,
+// with their storage indices in `midx`.
+struct Changed {
+    const uint64_t *mkey;
+    const int *midx;
+    int n;
+    const int *taken;
+    int nstore;   // storage slots of the state; an index outside raises ST_INDEX
+    int *status;
+};
+
+// Pair force on particle i of such a state, with the candidates in the order of the sorted state: per
+// stencil cell, the cell's unchanged storage range merged by id with the changed particles now in the
+// cell -- the order in which block_sort would store them.  The arithmetic is pair_force_at's.
+template <typename G>
+__device__ inline void pair_force_unsorted(int i, float4 p, const float4 *__restrict__ pos,
+                                           const uint32_t *__restrict__ id, const uint16_t *__restrict__ start,
+                                           const Geo &gs, const G &g, const Changed &X, const int *tab,
+                                           const float *screen, const PairPot *pots, int T, float &fx, float &fy,
+                                           float &fz) {
+    const int ti = itype(p);
+    const int *trow = tab + ti * T;
+    const float *srow = screen + ti * T;
+    float e = 0.f;
+    auto visit = [&](int j) {
+        if (j == i) return;
+        if ((unsigned)j >= (unsigned)X.nstore) {
+            atomicOr(X.status, ST_INDEX);
+            return;
+        }
+        const float4 q = pos[j];
+        const int tj = itype(q);
+        if (tj < 0 || trow[tj] == 0) return;
+        if (screen_d2(p, q, g) > srow[tj]) return;
+        pair_force_body(p, q, g, trow[tj], pots, fx, fy, fz, e);
+    };
+    for_each_neighbor_cell(p, g, [&](int c) {
+        const int je = start[c + 1];
+        // the next member of the cell's storage range that is still there, unchanged
+        auto member = [&](int j) {
+            while (j < je && (X.taken[j] || bin_of(pos[j], gs) != c)) ++j;
+            return j;
+        };
+        int j = member(start[c]);
+        int x = lower_bound_u64(X.mkey, X.n, (uint64_t)c << 32);
+        const int xe = lower_bound_u64(X.mkey, X.n, (uint64_t)(c + 1) << 32);
+        while (j < je || x < xe) {
+            if (x < xe && (j >= je || (uint32_t)X.mkey[x] < id[j])) {
+                visit(X.midx[x]);
+                ++x;
+            } else {
+                visit(j);
+                j = member(j + 1);
+            }
+        }
+    });
+}
+
+// After the reactions of a replica that carries its forces, without sorting again: the particles of
+// the marked cells get their pair forces again (in force[], by storage index), walked over the state
+// as the reactions left it.  The performed events are events[idx[k]] for state[k] == 1, k < n_events
+// (block_resolve_apply's scratch); births are storage slots [n1, n1 + births).  Scratch: mkey and midx
+// (cap entries), tmp and list (one entry per storage slot), cnt (2 ints).  Returns false when the
+// changed particles do not fit mkey; only zero forces of changed particles outside the box are
+// written then.  Every storage index is checked against the n1 + births slots; one outside raises
+// ST_INDEX in *status and its access is skipped.
+template <typename G>
+__device__ inline bool refresh_in_place(const float4 *__restrict__ pos, const uint32_t *__restrict__ id, int n1,
+                                        int births, const EventRec *events, const int *idx, const int *state,
+                                        int n_events, const uint32_t *mark, const uint16_t *start, const Geo &gs,
+                                        const G &g, int *taken, uint64_t *mkey, int *midx, int cap, int *tmp,
+                                        int *list, int *cnt, const SmemLayout &S, int T, bool pair_pots,
+                                        float4 *force, int *status) {
+    const int nc = gs.ncells;
+    const int nstore = n1 + births;
+    auto inside = [&](int q) {
+        if ((unsigned)q < (unsigned)nstore) return true;
+        atomicOr(status, ST_INDEX);
+        return false;
+    };
+    // every particle of a performed event and every birth: flagged, listed when inside the box
+    auto each_changed = [&](auto f) {
+        for (int k = threadIdx.x; k < n_events + births; k += blockDim.x) {
+            if (k < n_events) {
+                if (state[k] != 1) continue;
+                const EventRec e = events[idx[k]];
+                f(e.p1);
+                if (e.p2 != e.p1) f(e.p2);
+            } else {
+                f(n1 + k - n_events);
+            }
+        }
+    };
+    if (threadIdx.x == 0) { cnt[0] = 0; cnt[1] = 0; }
+    __syncthreads();
+    each_changed([&](int q) {
+        if (!inside(q)) return;
+        const float4 p = pos[q];
+        if (itype(p) < 0) return;  // removed
+        taken[q] = 1;
+        const int c = bin_of(p, gs);
+        if (c == nc) {  // outside the box: no pair forces
+            force[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+            return;
+        }
+        const int x = atomicAdd(&cnt[0], 1);
+        if (x < cap) {
+            mkey[x] = ((uint64_t)c << 32) | id[q];
+            midx[x] = q;
+        }
+    });
+    __syncthreads();
+    const int nm = cnt[0];
+    const bool fits = nm <= cap;
+    if (fits) {
+        // ascending keys (distinct: ids are): ranks place the indices, the keys follow
+        for (int x = threadIdx.x; x < nm; x += blockDim.x) {
+            const uint64_t v = mkey[x];
+            int r = 0;
+            for (int y = 0; y < nm; ++y) r += mkey[y] < v;
+            tmp[r] = midx[x];
+        }
+        __syncthreads();
+        for (int x = threadIdx.x; x < nm; x += blockDim.x) {
+            const int q = tmp[x];
+            if (!inside(q)) continue;
+            midx[x] = q;
+            mkey[x] = ((uint64_t)bin_of(pos[q], gs) << 32) | id[q];
+        }
+        __syncthreads();
+        // the particles now in marked cells: unchanged storage-range members, then the changed ones
+        for (int w = threadIdx.x; w < (nc + 31) / 32; w += blockDim.x) {
+            uint32_t bits = mark[w];
+            while (bits) {
+                const int c = w * 32 + __ffs(bits) - 1;
+                bits &= bits - 1;
+                for (int j = start[c]; j < start[c + 1]; ++j)
+                    if (!taken[j] && bin_of(pos[j], gs) == c) {
+                        const int l = atomicAdd(&cnt[1], 1);
+                        if (inside(l)) list[l] = j;
+                    }
+            }
+        }
+        for (int x = threadIdx.x; x < nm; x += blockDim.x) {
+            const int l = atomicAdd(&cnt[1], 1);
+            if (inside(l)) list[l] = midx[x];
+        }
+        __syncthreads();
+        // each particle is listed once (a storage-range member of its own cell, or changed)
+        const int nl = min(cnt[1], nstore);
+        const Changed X{mkey, midx, nm, taken, nstore, status};
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+            const int k = list[l];
+            if (!inside(k)) continue;
+            float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (pair_pots)
+                pair_force_unsorted(k, pos[k], pos, id, start, gs, g, X, S.tab, S.screen, S.pots, T, f.x, f.y, f.z);
+            force[k] = f;
+        }
+    }
+    __syncthreads();
+    each_changed([&](int q) {
+        if ((unsigned)q < (unsigned)nstore) taken[q] = 0;
+    });
+    __syncthreads();
+    return fits;
+}
+
 // one step of one replica by the whole block; C is the cell array's type (uint16_t in shared memory
 // or int in global memory).  Inlined into the kernel: as a call, the geometry and tables it passes
 // down by reference live in local memory and the candidate walks reload them per candidate.
@@ -330,12 +520,15 @@ __device__ __forceinline__ void replica_body(const EngineDev &E, int r, const Sm
     int *bin = D.bin, *rank = D.rank, *src = D.src;
     int *gstart = D.start;
     constexpr bool in_smem = sizeof(C) == sizeof(uint16_t);
-    // between steps a shared-memory replica keeps its starts as 16-bit entries in its start array
-    if (in_smem) copy_starts16(reinterpret_cast<uint16_t *>(cells), reinterpret_cast<const uint16_t *>(gstart), nc + 3);
     const int n = st.n, n_in = st.n_in;
-    // forces stored by the previous step's event walk (replicas with reactions and shared-memory cells)
+    // forces stored by the previous step's event walk (replicas with reactions and shared-memory cells);
+    // the state is then the one the reactions left, unsorted, with removed particles in place
     const bool fuse = in_smem && tab->nreactions > 0 && D.force[0] != nullptr;
     const float4 *fX = (fuse && st.fvalid) ? D.force[st.cur] : nullptr;
+    // otherwise the state is sorted and a shared-memory replica keeps its starts as 16-bit entries in
+    // its start array between steps
+    if (in_smem && !fX)
+        copy_starts16(reinterpret_cast<uint16_t *>(cells), reinterpret_cast<const uint16_t *>(gstart), nc + 3);
 
     // forces on the current state, Euler step into Y, bins of the new positions
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -353,7 +546,7 @@ __device__ __forceinline__ void replica_body(const EngineDev &E, int r, const Sm
             const int o1 = tab->o1pot_tab[t];
             if (o1) order1_force(p, tab->o1pots, o1 >> 8, o1 & 0xff, fx, fy, fz, e);
         }
-        const float4 q = euler_bd(p, fx, fy, fz, id, D.seed, step, S.drift[t], S.scale[t], g);
+        const float4 q = t >= 0 ? euler_bd(p, fx, fy, fz, id, D.seed, step, S.drift[t], S.scale[t], g) : p;
         posY[i] = q;
         idY[i] = id;
         bin[i] = bin_of(q, gs);
@@ -383,7 +576,7 @@ __device__ __forceinline__ void replica_body(const EngineDev &E, int r, const Sm
         if (keep)
             // the sort scratch (bin, rank, src) is free until the re-sort: it holds the tuple list
             block_events_forces(n1, nin1, posX, idX, reinterpret_cast<const uint16_t *>(cells), g, S, T, NP > 0, rt,
-                                D.seed, step, E.handler, D.force[st.cur], bin, rank, src, D.cap, emit);
+                                D.seed, step, E.handler, D.force[st.cur], bin, rank, src, D.cap, &sh_status, emit);
         else
             block_events(0, blockDim.x, n1, nin1, posX, idX, cells, g, 1, rt, D.seed, step, E.handler, S.queue, emit);
         fvalid = keep ? 1 : 0;
@@ -411,23 +604,35 @@ __device__ __forceinline__ void replica_body(const EngineDev &E, int r, const Sm
             block_resolve_apply(ev, Ev, E.max_events_sm, S.key, S.idx, S.state, tab, gs, D.seed, step, t, res);
             next_id = st.next_id + res.ids;
             if (threadIdx.x == 0) sh_status |= res.status;
-            if (res.winners > 0) {
-                // particles changed cells, appeared or vanished: sort again, into Y
-                const int n_total = n1 + res.births;
-                block_bin(posX, n_total, bin, gs);
-                if (keep) {
-                    // cells around the products and the births
-                    for (int k = threadIdx.x; k < 2 * Ev + res.births; k += blockDim.x) {
-                        int c;
-                        if (k < 2 * Ev) {
-                            const EventRec e = ev[k >> 1];
-                            c = bin[(k & 1) ? e.p2 : e.p1];
-                        } else {
-                            c = bin[n1 + k - 2 * Ev];
-                        }
-                        if (c < nc) mark_stencil(mark, c, gs);
+            const int n_total = n1 + res.births;
+            bool sort_again = res.winners > 0;
+            if (sort_again && keep) {
+                // cells around the products and the births
+                for (int k = threadIdx.x; k < 2 * Ev + res.births; k += blockDim.x) {
+                    int q;
+                    if (k < 2 * Ev) {
+                        const EventRec e = ev[k >> 1];
+                        q = (k & 1) ? e.p2 : e.p1;
+                    } else {
+                        q = n1 + k - 2 * Ev;
                     }
+                    const int c = bin_of(posX[q], gs);
+                    if (c < nc) mark_stencil(mark, c, gs);
                 }
+                __syncthreads();
+                // the particles around them walk again over the state as it is; it stays unsorted (the
+                // next step sorts after its Euler update anyway)
+                if (refresh_in_place(posX, idX, n1, res.births, ev, S.idx, S.state, min(Ev, E.max_events_sm), mark,
+                                     reinterpret_cast<const uint16_t *>(cells), gs, g, D.taken, S.key,
+                                     S.queue.p2, E.max_events_sm, src, rank, S.queue.count + 1, S, T, NP > 0,
+                                     D.force[st.cur], &sh_status)) {
+                    n_final = n_total;
+                    sort_again = false;
+                }
+            }
+            if (sort_again) {
+                // particles changed cells, appeared or vanished: sort again, into Y
+                block_bin(posX, n_total, bin, gs);
                 block_rank(n_total, bin, rank, cells, nc + 2);
                 int n2, nin2;
                 block_sort(posX, idX, n_total, posY, idY, bin, rank, src, cells, gs, n2, nin2);
@@ -457,14 +662,16 @@ __device__ __forceinline__ void replica_body(const EngineDev &E, int r, const Sm
             }
         }
     }
-    if (in_smem) copy_starts16(reinterpret_cast<uint16_t *>(gstart), reinterpret_cast<const uint16_t *>(cells), nc + 3);
+    // a replica that carries its forces does not read its starts at the next step
+    if (in_smem && !fvalid)
+        copy_starts16(reinterpret_cast<uint16_t *>(gstart), reinterpret_cast<const uint16_t *>(cells), nc + 3);
     int rec = st.rec;
     if (D.records && D.count_stride > 0 && (step + 1) % (uint64_t)D.count_stride == 0 && rec < D.max_records) {
         block_count_types(D.pos[cur], n_final, T, D.records + (size_t)rec * T);
         ++rec;
     }
     if (threadIdx.x == 0) {
-        atomicAdd(E.particle_steps, (unsigned long long)n);
+        atomicAdd(E.particle_steps, (unsigned long long)n1);
         RepState o;
         o.n = n_final;
         o.n_in = nin_final;

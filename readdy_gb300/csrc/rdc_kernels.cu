@@ -106,8 +106,8 @@ static void launch_scan(const int *in, int *out, int *tiles, int n, cudaStream_t
 }
 
 // ------------------------------------------------------------------------------------------------
-// K1 counting sort: scatter source indices, order each cell by source index (deterministic),
-// gather the particle arrays into the alternate buffers
+// K1 counting sort: scatter source indices, order each cell by particle id (deterministic, and
+// independent of the order of the source arrays), gather the particle arrays into the alternate buffers
 // ------------------------------------------------------------------------------------------------
 __global__ void k_scatter(SysDev s) {
     const int n = s.counters[C_N_TOTAL];
@@ -125,17 +125,17 @@ __global__ void k_cell_order(SysDev s) {
             s.big_cells[atomicAdd(&s.counters[C_BIG], 1)] = c;
             continue;
         }
-        insertion_sort(s.src, b, e);
+        insertion_sort_by(s.src, b, e, s.id);
     }
 }
 
-// cells with many entries: one block per cell, every entry's rank is the number of smaller entries
-// (the source indices of a cell are distinct); rank[] is free scratch once the scatter is done
+// cells with many entries: one block per cell, every entry's rank is the number of entries with a
+// smaller id (ids are distinct); rank[] is free scratch once the scatter is done
 __global__ void k_big_cell_order(SysDev s) {
     const int nbig = s.counters[C_BIG];
     for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
         const int c = s.big_cells[q];
-        block_rank_sort(s.src, s.rank, s.start[c], s.start[c + 1]);
+        block_rank_sort_by(s.src, s.rank, s.start[c], s.start[c + 1], s.id);
     }
     __syncthreads();
     if (blockIdx.x == 0 && threadIdx.x == 0) s.counters[C_BIG] = 0;

@@ -30,11 +30,14 @@ __device__ inline int axis_cells(int c, int dim, int pbc, int r, int *out) {
 // cells up to this many entries are ordered by one thread (insertion sort)
 constexpr int CELL_SORT_SMALL = 32;
 
-__device__ inline void insertion_sort(int *a, int b, int e) {
+// orders the source indices a[b..e) by their particles' ids key[a[.]] (distinct within a system), so
+// that a cell's storage order does not depend on the order of the source arrays
+__device__ inline void insertion_sort_by(int *a, int b, int e, const uint32_t *__restrict__ key) {
     for (int j = b + 1; j < e; ++j) {
         const int v = a[j];
+        const uint32_t kv = key[v];
         int k = j - 1;
-        while (k >= b && a[k] > v) {
+        while (k >= b && key[a[k]] > kv) {
             a[k + 1] = a[k];
             --k;
         }
@@ -42,14 +45,15 @@ __device__ inline void insertion_sort(int *a, int b, int e) {
     }
 }
 
-// orders the distinct values a[b..e) by the whole block: each value's rank is the count of smaller
-// values; tmp[b..e) is scratch
-__device__ inline void block_rank_sort(int *a, int *tmp, int b, int e) {
+// insertion_sort_by for crowded cells, by the whole block: each index's rank is the count of smaller
+// keys; tmp[b..e) is scratch
+__device__ inline void block_rank_sort_by(int *a, int *tmp, int b, int e, const uint32_t *__restrict__ key) {
     const int k = e - b;
     for (int t = threadIdx.x; t < k; t += blockDim.x) {
         const int v = a[b + t];
+        const uint32_t kv = key[v];
         int r = 0;
-        for (int u = 0; u < k; ++u) r += a[b + u] < v;
+        for (int u = 0; u < k; ++u) r += key[a[b + u]] < kv;
         tmp[b + r] = v;
     }
     __syncthreads();
@@ -126,6 +130,58 @@ __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__
                 const int cell = az[c] + dz0 * (ay[b] + dy0 * ax[a]);
                 f(start[cell], start[cell + 1]);
             }
+}
+
+// Calls f(cell) for every cell of the radius-1 stencil around the particle's cell, in the order in
+// which for_each_neighbor_range visits their storage ranges.
+template <typename G, typename F>
+__device__ inline void for_each_neighbor_cell(float4 p, const G &g, F f) {
+    int cx, cy, cz;
+    cell_coords(p, g, cx, cy, cz);
+    const int dx0 = g.dims[0], dy0 = g.dims[1], dz0 = g.dims[2];
+    if (stencil_fast(g, 1)) {
+        for (int ox = -1; ox <= 1; ++ox) {
+            int x = cx + ox;
+            if (x < 0) {
+                if (!g.pbc[0]) continue;
+                x += dx0;
+            } else if (x >= dx0) {
+                if (!g.pbc[0]) continue;
+                x -= dx0;
+            }
+            for (int oy = -1; oy <= 1; ++oy) {
+                int y = cy + oy;
+                if (y < 0) {
+                    if (!g.pbc[1]) continue;
+                    y += dy0;
+                } else if (y >= dy0) {
+                    if (!g.pbc[1]) continue;
+                    y -= dy0;
+                }
+                const int base = (x * dy0 + y) * dz0;
+                int z0 = cz - 1, z1 = cz + 1;
+                if (z0 < 0) {
+                    if (g.pbc[2]) f(base + dz0 - 1);
+                    z0 = 0;
+                }
+                bool wrap_hi = false;
+                if (z1 >= dz0) {
+                    wrap_hi = g.pbc[2] != 0;
+                    z1 = dz0 - 1;
+                }
+                for (int z = z0; z <= z1; ++z) f(base + z);
+                if (wrap_hi) f(base);
+            }
+        }
+        return;
+    }
+    int ax[7], ay[7], az[7];
+    const int nx = axis_cells(cx, dx0, g.pbc[0], 1, ax);
+    const int ny = axis_cells(cy, dy0, g.pbc[1], 1, ay);
+    const int nz = axis_cells(cz, dz0, g.pbc[2], 1, az);
+    for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b)
+            for (int c = 0; c < nz; ++c) f(az[c] + dz0 * (ay[b] + dy0 * ax[a]));
 }
 
 // Calls f(j) for every candidate j >= jmin of the stencil, in the order of for_each_neighbor_range.
@@ -274,6 +330,19 @@ struct NoExtra {
     __device__ void operator()(int, float4, int, float) const {}
 };
 
+// the pair potentials of one surviving candidate q (pt: its entry of the type-pair table) on p
+template <typename G>
+__device__ inline void pair_force_body(float4 p, float4 q, const G &g, int pt, const PairPot *pots, float &fx,
+                                       float &fy, float &fz, float &e) {
+    const PairGeom g0 = pair_geom(p, q, g);
+    const int first = pt >> 8, cnt = pt & 0xff;
+    for (int k = first; k < first + cnt; ++k) {
+        const PairPot &pp = pots[k];
+        PairGeom gg = g0;
+        if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) pair_force(pp, gg, p, q, g, fx, fy, fz, e);
+    }
+}
+
 template <typename G, typename S, typename Extra = NoExtra>
 __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const S *__restrict__ start,
                                      const G &g, int radius, const int *tab, const float *screen, const PairPot *pots,
@@ -286,24 +355,24 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
     auto body = [&](int j) {
         const float4 q = pos[j];
         const int pt = trow[itype(q)];
+        if (!vir) {
+            pair_force_body(p, q, g, pt, pots, fx, fy, fz, e);
+            return;
+        }
         const PairGeom g0 = pair_geom(p, q, g);
         const int first = pt >> 8, cnt = pt & 0xff;
         for (int k = first; k < first + cnt; ++k) {
             const PairPot &pp = pots[k];
             PairGeom gg = g0;
             if (within(g0, gg, p, q, g, pp.cutoff2f, pp.band, pp.cutoff2)) {
-                if (vir) {
-                    float tx = 0.f, ty = 0.f, tz = 0.f;
-                    pair_force(pp, gg, p, q, g, tx, ty, tz, e);
-                    fx += tx; fy += ty; fz += tz;
-                    const float d[3] = {-0.5f * gg.dx, -0.5f * gg.dy, -0.5f * gg.dz}, f[3] = {tx, ty, tz};
+                float tx = 0.f, ty = 0.f, tz = 0.f;
+                pair_force(pp, gg, p, q, g, tx, ty, tz, e);
+                fx += tx; fy += ty; fz += tz;
+                const float d[3] = {-0.5f * gg.dx, -0.5f * gg.dy, -0.5f * gg.dz}, f[3] = {tx, ty, tz};
 #pragma unroll
-                    for (int a = 0; a < 3; ++a)
+                for (int a = 0; a < 3; ++a)
 #pragma unroll
-                        for (int b = 0; b < 3; ++b) vir[3 * a + b] += d[a] * f[b];
-                } else {
-                    pair_force(pp, gg, p, q, g, fx, fy, fz, e);
-                }
+                    for (int b = 0; b < 3; ++b) vir[3 * a + b] += d[a] * f[b];
             }
         }
     };

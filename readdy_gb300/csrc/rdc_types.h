@@ -43,6 +43,7 @@ enum Status : int {
     ST_ID_OVERFLOW = 4,    // 32-bit particle id counter exhausted
     ST_RESOLVE_ROUNDS = 8, // conflict resolution did not converge within its round limit
     ST_TYPE = 16,          // particle type out of range
+    ST_INDEX = 32,         // a replica step met a storage index outside its particles (access skipped)
 };
 
 struct Geo {
