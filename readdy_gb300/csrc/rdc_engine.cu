@@ -240,9 +240,22 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
             tr[k] = r;
         }
     };
-    if (threadIdx.x == 0) *count = 0;
+    // warps take 32-particle chunks from a counter: the walks differ in length, and a static split
+    // leaves warps waiting at the barrier after the walk
+    int *next = S.queue.count + 3;
+    if (threadIdx.x == 0) {
+        *count = 0;
+        *next = 0;
+    }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(next, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int i = base + lane;
+        if (i >= n) continue;
         const float4 p = pos[i];
         const int ti = itype(p);
         float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
@@ -341,72 +354,113 @@ struct Changed {
     const int *midx;
     int n;
     const int *taken;
-    int nstore;   // storage slots of the state; an index outside raises ST_INDEX
+    const uint32_t *bloom;  // CHANGED_BLOOM_BITS bits over the cells of mkey, then as many over changed indices
+    int nstore;             // storage slots of the state; an index outside raises ST_INDEX
     int *status;
 };
 
+// single-hash Bloom filters in shared memory that spare the walks a search or a global flag load for
+// the cells and particles no reaction touched (a hit is confirmed exactly)
+constexpr int CHANGED_BLOOM_BITS = 4096;
+static_assert(2 * CHANGED_BLOOM_BITS / 8 <= EVENT_QUEUE, "the filters live in the tuple queue's reaction bytes");
+__device__ inline bool bloom_has(const uint32_t *b, int v) {
+    const int h = v & (CHANGED_BLOOM_BITS - 1);
+    return (b[h >> 5] >> (h & 31)) & 1u;
+}
+__device__ inline void bloom_add(uint32_t *b, int v) {
+    const int h = v & (CHANGED_BLOOM_BITS - 1);
+    atomicOr(&b[h >> 5], 1u << (h & 31));
+}
+
 // Pair force on particle i of such a state, with the candidates in the order of the sorted state: per
 // stencil cell, the cell's unchanged storage range merged by id with the changed particles now in the
-// cell -- the order in which block_sort would store them.  The arithmetic is pair_force_at's.
+// cell -- the order in which block_sort would store them.  The candidates are listed first (shared
+// memory only, up to UNSORTED_CANDIDATES) and then walked with the next position loaded ahead, as in
+// for_each_candidate_q; a longer list is walked cell by cell.  The arithmetic is pair_force_at's.
+constexpr int UNSORTED_CANDIDATES = 48;
+
 template <typename G>
 __device__ inline void pair_force_unsorted(int i, float4 p, const float4 *__restrict__ pos,
                                            const uint32_t *__restrict__ id, const uint16_t *__restrict__ start,
-                                           const Geo &gs, const G &g, const Changed &X, const int *tab,
-                                           const float *screen, const PairPot *pots, int T, float &fx, float &fy,
-                                           float &fz) {
+                                           const G &g, const Changed &X, const int *tab, const float *screen,
+                                           const PairPot *pots, int T, float &fx, float &fy, float &fz) {
     const int ti = itype(p);
     const int *trow = tab + ti * T;
     const float *srow = screen + ti * T;
     float e = 0.f;
-    auto visit = [&](int j) {
+    auto visit = [&](int j, float4 q) {
         if (j == i) return;
-        if ((unsigned)j >= (unsigned)X.nstore) {
-            atomicOr(X.status, ST_INDEX);
-            return;
-        }
-        const float4 q = pos[j];
         const int tj = itype(q);
         if (tj < 0 || trow[tj] == 0) return;
         if (screen_d2(p, q, g) > srow[tj]) return;
         pair_force_body(p, q, g, trow[tj], pots, fx, fy, fz, e);
     };
-    for_each_neighbor_cell(p, g, [&](int c) {
-        const int je = start[c + 1];
-        // the next member of the cell's storage range that is still there, unchanged
-        auto member = [&](int j) {
-            while (j < je && (X.taken[j] || bin_of(pos[j], gs) != c)) ++j;
-            return j;
-        };
-        int j = member(start[c]);
-        int x = lower_bound_u64(X.mkey, X.n, (uint64_t)c << 32);
-        const int xe = lower_bound_u64(X.mkey, X.n, (uint64_t)(c + 1) << 32);
-        while (j < je || x < xe) {
-            if (x < xe && (j >= je || (uint32_t)X.mkey[x] < id[j])) {
-                visit(X.midx[x]);
-                ++x;
-            } else {
-                visit(j);
-                j = member(j + 1);
+    const uint32_t *bloom_idx = X.bloom + CHANGED_BLOOM_BITS / 32;
+    // f(j) for the candidates in order; an index outside the storage raises ST_INDEX and is skipped
+    auto candidates = [&](auto f) {
+        for_each_neighbor_cell(p, g, [&](int c) {
+            const int je = start[c + 1];
+            // the next member of the cell's storage range that is unchanged (a removed one is skipped
+            // by visit; one that reacted is flagged in taken)
+            auto member = [&](int j) {
+                while (j < je && bloom_has(bloom_idx, j) && X.taken[j]) ++j;
+                return j;
+            };
+            int j = member(start[c]);
+            // changed particles now in c: entries x with cell c, from the first key >= c << 32
+            int x = bloom_has(X.bloom, c) ? lower_bound_u64(X.mkey, X.n, (uint64_t)c << 32) : X.n;
+            auto in_c = [&](int x) { return x < X.n && (int)(X.mkey[x] >> 32) == c; };
+            while (j < je || in_c(x)) {
+                int k;
+                if (in_c(x) && (j >= je || (uint32_t)X.mkey[x] < id[j])) {
+                    k = X.midx[x];
+                    ++x;
+                } else {
+                    k = j;
+                    j = member(j + 1);
+                }
+                if ((unsigned)k < (unsigned)X.nstore) f(k);
+                else atomicOr(X.status, ST_INDEX);
             }
-        }
+        });
+    };
+    int cand[UNSORTED_CANDIDATES];
+    int nc = 0;
+    candidates([&](int k) {
+        if (nc < UNSORTED_CANDIDATES) cand[nc] = k;
+        ++nc;
     });
+    if (nc > UNSORTED_CANDIDATES) {
+        candidates([&](int k) { visit(k, pos[k]); });
+        return;
+    }
+    if (nc == 0) return;
+    float4 q = pos[cand[0]];
+    for (int k = 0; k < nc; ++k) {
+        float4 qn = q;
+        if (k + 1 < nc) qn = pos[cand[k + 1]];
+        visit(cand[k], q);
+        q = qn;
+    }
 }
 
 // After the reactions of a replica that carries its forces, without sorting again: the particles of
 // the marked cells get their pair forces again (in force[], by storage index), walked over the state
 // as the reactions left it.  The performed events are events[idx[k]] for state[k] == 1, k < n_events
 // (block_resolve_apply's scratch); births are storage slots [n1, n1 + births).  Scratch: mkey and midx
-// (cap entries), tmp and list (one entry per storage slot), cnt (2 ints).  Returns false when the
+// (cap entries), tmp and list (one entry per storage slot), cnt (2 ints), bloom (2 CHANGED_BLOOM_BITS
+// bits).  Returns false when the
 // changed particles do not fit mkey; only zero forces of changed particles outside the box are
 // written then.  Every storage index is checked against the n1 + births slots; one outside raises
 // ST_INDEX in *status and its access is skipped.
 template <typename G>
 __device__ inline bool refresh_in_place(const float4 *__restrict__ pos, const uint32_t *__restrict__ id, int n1,
                                         int births, const EventRec *events, const int *idx, const int *state,
-                                        int n_events, const uint32_t *mark, const uint16_t *start, const Geo &gs,
-                                        const G &g, int *taken, uint64_t *mkey, int *midx, int cap, int *tmp,
-                                        int *list, int *cnt, const SmemLayout &S, int T, bool pair_pots,
-                                        float4 *force, int *status) {
+                                        int n_events, const uint32_t *mark, const uint16_t *start,
+                                        const Geo &gs, const G &g, int *taken, uint64_t *mkey, int *midx, int cap,
+                                        int *tmp,
+                                        int *list, int *cnt, uint32_t *bloom, const SmemLayout &S, int T,
+                                        bool pair_pots, float4 *force, int *status) {
     const int nc = gs.ncells;
     const int nstore = n1 + births;
     auto inside = [&](int q) {
@@ -428,17 +482,20 @@ __device__ inline bool refresh_in_place(const float4 *__restrict__ pos, const ui
         }
     };
     if (threadIdx.x == 0) { cnt[0] = 0; cnt[1] = 0; }
+    for (int k = threadIdx.x; k < 2 * CHANGED_BLOOM_BITS / 32; k += blockDim.x) bloom[k] = 0u;
     __syncthreads();
     each_changed([&](int q) {
         if (!inside(q)) return;
         const float4 p = pos[q];
         if (itype(p) < 0) return;  // removed
         taken[q] = 1;
+        bloom_add(bloom + CHANGED_BLOOM_BITS / 32, q);
         const int c = bin_of(p, gs);
         if (c == nc) {  // outside the box: no pair forces
             force[q] = make_float4(0.f, 0.f, 0.f, 0.f);
             return;
         }
+        bloom_add(bloom, c);
         const int x = atomicAdd(&cnt[0], 1);
         if (x < cap) {
             mkey[x] = ((uint64_t)c << 32) | id[q];
@@ -471,7 +528,7 @@ __device__ inline bool refresh_in_place(const float4 *__restrict__ pos, const ui
                 const int c = w * 32 + __ffs(bits) - 1;
                 bits &= bits - 1;
                 for (int j = start[c]; j < start[c + 1]; ++j)
-                    if (!taken[j] && bin_of(pos[j], gs) == c) {
+                    if (!(bloom_has(bloom + CHANGED_BLOOM_BITS / 32, j) && taken[j]) && itype(pos[j]) >= 0) {
                         const int l = atomicAdd(&cnt[1], 1);
                         if (inside(l)) list[l] = j;
                     }
@@ -484,13 +541,13 @@ __device__ inline bool refresh_in_place(const float4 *__restrict__ pos, const ui
         __syncthreads();
         // each particle is listed once (a storage-range member of its own cell, or changed)
         const int nl = min(cnt[1], nstore);
-        const Changed X{mkey, midx, nm, taken, nstore, status};
+        const Changed X{mkey, midx, nm, taken, bloom, nstore, status};
         for (int l = threadIdx.x; l < nl; l += blockDim.x) {
             const int k = list[l];
             if (!inside(k)) continue;
             float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
             if (pair_pots)
-                pair_force_unsorted(k, pos[k], pos, id, start, gs, g, X, S.tab, S.screen, S.pots, T, f.x, f.y, f.z);
+                pair_force_unsorted(k, pos[k], pos, id, start, g, X, S.tab, S.screen, S.pots, T, f.x, f.y, f.z);
             force[k] = f;
         }
     }
@@ -624,8 +681,9 @@ __device__ __forceinline__ void replica_body(const EngineDev &E, int r, const Sm
                 // next step sorts after its Euler update anyway)
                 if (refresh_in_place(posX, idX, n1, res.births, ev, S.idx, S.state, min(Ev, E.max_events_sm), mark,
                                      reinterpret_cast<const uint16_t *>(cells), gs, g, D.taken, S.key,
-                                     S.queue.p2, E.max_events_sm, src, rank, S.queue.count + 1, S, T, NP > 0,
-                                     D.force[st.cur], &sh_status)) {
+                                     S.queue.p2, E.max_events_sm, src, rank, S.queue.count + 1,
+                                     reinterpret_cast<uint32_t *>(S.queue.r), S, T, NP > 0, D.force[st.cur],
+                                     &sh_status)) {
                     n_final = n_total;
                     sort_again = false;
                 }
