@@ -542,7 +542,12 @@ __device__ inline bool refresh_in_place(const float4 *__restrict__ pos, const ui
         // each particle is listed once (a storage-range member of its own cell, or changed)
         const int nl = min(cnt[1], nstore);
         const Changed X{mkey, midx, nm, taken, bloom, nstore, status};
-        for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+        // entry l goes to lane l / warps of warp l % warps: the few walks spread over the warps instead
+        // of diverging inside the first one
+        const int warps = blockDim.x >> 5;
+        for (int l0 = 0; l0 < nl; l0 += blockDim.x) {
+            const int l = l0 + (int)(threadIdx.x & 31) * warps + (int)(threadIdx.x >> 5);
+            if (l >= nl) continue;
             const int k = list[l];
             if (!inside(k)) continue;
             float4 f = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -31,8 +31,17 @@ __device__ inline int axis_cells(int c, int dim, int pbc, int r, int *out) {
 constexpr int CELL_SORT_SMALL = 32;
 
 // orders the source indices a[b..e) by their particles' ids key[a[.]] (distinct within a system), so
-// that a cell's storage order does not depend on the order of the source arrays
+// that a cell's storage order does not depend on the order of the source arrays.  A pair -- nearly
+// every cell to order at the densities of the workloads -- loads both keys at once.
 __device__ inline void insertion_sort_by(int *a, int b, int e, const uint32_t *__restrict__ key) {
+    if (e - b == 2) {
+        const int v0 = a[b], v1 = a[b + 1];
+        if (key[v0] > key[v1]) {
+            a[b] = v1;
+            a[b + 1] = v0;
+        }
+        return;
+    }
     for (int j = b + 1; j < e; ++j) {
         const int v = a[j];
         const uint32_t kv = key[v];
@@ -140,6 +149,8 @@ __device__ inline void for_each_neighbor_cell(float4 p, const G &g, F f) {
     cell_coords(p, g, cx, cy, cz);
     const int dx0 = g.dims[0], dy0 = g.dims[1], dz0 = g.dims[2];
     if (stencil_fast(g, 1)) {
+        // loops kept rolled: f is inlined once, not once per stencil cell
+#pragma unroll 1
         for (int ox = -1; ox <= 1; ++ox) {
             int x = cx + ox;
             if (x < 0) {
@@ -149,6 +160,7 @@ __device__ inline void for_each_neighbor_cell(float4 p, const G &g, F f) {
                 if (!g.pbc[0]) continue;
                 x -= dx0;
             }
+#pragma unroll 1
             for (int oy = -1; oy <= 1; ++oy) {
                 int y = cy + oy;
                 if (y < 0) {
@@ -160,17 +172,17 @@ __device__ inline void for_each_neighbor_cell(float4 p, const G &g, F f) {
                 }
                 const int base = (x * dy0 + y) * dz0;
                 int z0 = cz - 1, z1 = cz + 1;
-                if (z0 < 0) {
-                    if (g.pbc[2]) f(base + dz0 - 1);
-                    z0 = 0;
-                }
+                if (z0 < 0) z0 = 0;
                 bool wrap_hi = false;
                 if (z1 >= dz0) {
                     wrap_hi = g.pbc[2] != 0;
                     z1 = dz0 - 1;
                 }
-                for (int z = z0; z <= z1; ++z) f(base + z);
-                if (wrap_hi) f(base);
+                // the column's cells in storage order: the wrapped low cell, z0..z1, the wrapped high cell
+                const int zs = (cz - 1 < 0 && g.pbc[2]) ? -1 : z0;
+                const int ze = wrap_hi ? z1 + 1 : z1;
+#pragma unroll 1
+                for (int z = zs; z <= ze; ++z) f(base + (z < 0 ? dz0 - 1 : (z > z1 ? 0 : z)));
             }
         }
         return;
@@ -179,8 +191,11 @@ __device__ inline void for_each_neighbor_cell(float4 p, const G &g, F f) {
     const int nx = axis_cells(cx, dx0, g.pbc[0], 1, ax);
     const int ny = axis_cells(cy, dy0, g.pbc[1], 1, ay);
     const int nz = axis_cells(cz, dz0, g.pbc[2], 1, az);
+#pragma unroll 1
     for (int a = 0; a < nx; ++a)
+#pragma unroll 1
         for (int b = 0; b < ny; ++b)
+#pragma unroll 1
             for (int c = 0; c < nz; ++c) f(az[c] + dz0 * (ay[b] + dy0 * ax[a]));
 }
 
