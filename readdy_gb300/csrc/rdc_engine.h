@@ -12,9 +12,12 @@
 // the state left by the previous step's reactions, which is where SimulationLoop::run computes them
 // (SimulationLoop.h:283-289).  A replica with reactions and shared-memory cells computes them one
 // walk earlier: the stencil walk that looks for reaction partners after the sort also sums every
-// particle's pair force and stores it; after the reactions, only particles whose 27-cell stencil
-// held a reacting particle walk again.  The stored forces are the ones a walk over the final state
-// gives, bit for bit: an untouched stencil holds the same particles in the same storage order.
+// particle's pair force and stores it.  Its reactions then change the state in place (removed
+// particles keep their slots, births are appended) and no re-sort follows; only particles whose
+// 27-cell stencil held a reacting particle walk again, over that state, with the candidates in the
+// order of the sorted one.  Every sort orders a cell by particle id, so the sorted order does not
+// depend on the order of the source arrays, and the stored forces are the ones a walk over the
+// sorted final state gives, bit for bit.
 #pragma once
 #include <cuda_runtime.h>
 
