@@ -184,6 +184,10 @@ int rdc_batch_create(rdc_batch **out, const rdc_context *ctx, int n_replicas, co
 int rdc_batch_destroy(rdc_batch *b);
 /* initial particles of every replica: offsets (n_replicas+1) into positions3/types */
 int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *positions3, const int *types);
+/* the same from one host array per replica: counts[r] particles at positions3[r] (3 doubles each) and
+ * types[r], without concatenating them first */
+int rdc_batch_set_particles_list(rdc_batch *b, const int64_t *counts, const double *const *positions3,
+                                 const int *const *types);
 /* handler, time step and the launch knobs: cell width as a multiple (>= 1) of the largest cutoff, and
  * threads per block (one block advances one replica at a time) */
 int rdc_batch_configure(rdc_batch *b, int handler, double dt, double cell_width_scale, int threads_per_block);

@@ -90,6 +90,7 @@ def _sig(lib):
         "rdc_batch_set_particles": (i, [vp, P(i64), P(d), P(i)]),
         "rdc_batch_configure": (i, [vp, i, d, d, i]),
         "rdc_batch_set_carry_forces": (i, [vp, i]),
+        "rdc_batch_set_particles_list": (i, [vp, vp, vp, vp]),
         "rdc_batch_step": (i, [vp, i64]),
         "rdc_batch_step_timed": (i, [vp, i64, P(d)]),
         "rdc_batch_particle_steps": (i, [vp, P(u64)]),

@@ -54,13 +54,19 @@ class ReplicaBatch:
             self._h = None
 
     def set_particles(self, positions_per_replica, types_per_replica):
-        offs = np.zeros(self.n_replicas + 1, np.int64)
-        offs[1:] = np.cumsum([len(p) for p in positions_per_replica])
-        pos = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1, 3)
-                                                   for p in positions_per_replica]))
-        types = np.ascontiguousarray(np.concatenate([np.asarray(t, np.int32) for t in types_per_replica]))
-        N.check(self._lib.rdc_batch_set_particles(self._h, _p(offs, C.c_int64), _p(pos, C.c_double),
-                                                  _p(types, C.c_int)))
+        """Initial particles, one (n, 3) position array and one type array per replica; the arrays are
+        read where they lie (no concatenated copy)."""
+        if len(positions_per_replica) != self.n_replicas or len(types_per_replica) != self.n_replicas:
+            raise ValueError("one position and one type array per replica")
+        pos = [np.ascontiguousarray(np.asarray(p, np.float64).reshape(-1, 3)) for p in positions_per_replica]
+        types = [np.ascontiguousarray(np.asarray(t, np.int32).reshape(-1)) for t in types_per_replica]
+        counts = np.array([len(p) for p in pos], np.int64)
+        if any(len(t) != len(p) for p, t in zip(pos, types)):
+            raise ValueError("positions and types differ in length")
+        pp = (C.c_void_p * self.n_replicas)(*[p.ctypes.data for p in pos])
+        tp = (C.c_void_p * self.n_replicas)(*[t.ctypes.data for t in types])
+        N.check(self._lib.rdc_batch_set_particles_list(self._h, _p(counts, C.c_int64), C.cast(pp, C.c_void_p),
+                                                       C.cast(tp, C.c_void_p)))
 
     def configure(self, handler=N.GILLESPIE, dt=1e-3, cell_width_scale=1.0, threads_per_block=256):
         N.check(self._lib.rdc_batch_configure(self._h, int(handler), float(dt), float(cell_width_scale),

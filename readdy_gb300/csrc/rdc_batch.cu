@@ -11,6 +11,7 @@
 #include <memory>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/readdy_cuda.h"
@@ -39,6 +40,37 @@ uint64_t splitmix64(uint64_t x) {
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
     x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
     return x ^ (x >> 31);
+}
+
+// the packed particles of every replica (packed_off[r] .. packed_off[r + 1]) into the replica slices
+// (slice_off[r] ..): one block per replica
+__global__ void k_unpack_replicas(const float4 *__restrict__ packed, const int64_t *__restrict__ packed_off,
+                                  const int64_t *__restrict__ slice_off, float4 *__restrict__ dst, int R) {
+    for (int r = blockIdx.x; r < R; r += gridDim.x) {
+        const int64_t b = packed_off[r], n = packed_off[r + 1] - b, d = slice_off[r];
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) dst[d + i] = packed[b + i];
+    }
+}
+
+// float4 (x, y, z, type bits) of replicas [r0, r1) into packed[], from per-replica host arrays; false
+// when a type is outside [0, ntypes)
+bool pack_replicas(int r0, int r1, const int64_t *n, const int64_t *packed_off, const double *const *pos,
+                   const int *const *types, int ntypes, float4 *packed) {
+    for (int r = r0; r < r1; ++r) {
+        float4 *out = packed + packed_off[r];
+        const double *p = pos[r];
+        const int *t = types[r];
+        for (int64_t i = 0; i < n[r]; ++i) {
+            if (t[i] < 0 || t[i] >= ntypes) return false;
+            float4 q;
+            q.x = (float)p[3 * i];
+            q.y = (float)p[3 * i + 1];
+            q.z = (float)p[3 * i + 2];
+            std::memcpy(&q.w, &t[i], 4);
+            out[i] = q;
+        }
+    }
+    return true;
 }
 }  // namespace
 
@@ -337,35 +369,79 @@ int rdc_batch_destroy(rdc_batch *b) {
     return RDC_OK;
 }
 
+namespace {
+// Initial particles of every replica from per-replica host arrays: converted to float4 by host threads
+// into one packed buffer, copied once into the second position buffer (free until the first sort) and
+// unpacked into the replica slices on the device.
+void set_particles_impl(rdc_batch *b, const int64_t *n, const double *const *pos, const int *const *types) {
+    const int R = b->R;
+    std::vector<int64_t> packed_off(R + 1, 0);
+    for (int r = 0; r < R; ++r) {
+        if (n[r] < 0 || n[r] > b->caps[r]) throw std::invalid_argument("replica particle count exceeds capacity");
+        if (n[r] > 0 && (!pos[r] || !types[r])) throw std::invalid_argument("null argument");
+        packed_off[r + 1] = packed_off[r] + n[r];
+    }
+    const int64_t total = packed_off[R];
+    std::unique_ptr<float4[]> packed(new float4[std::max<int64_t>(total, 1)]);
+    // replicas split into contiguous runs of about equal particle counts, one per host thread
+    const int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::vector<int> cut(nt + 1, R);
+    cut[0] = 0;
+    for (int t = 1, r = 0; t < nt; ++t) {
+        while (r < R && packed_off[r] < total * t / nt) ++r;
+        cut[t] = r;
+    }
+    std::vector<char> ok(nt, 1);
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t)
+        pool.emplace_back([&, t] { ok[t] = pack_replicas(cut[t], cut[t + 1], n, packed_off.data(), pos, types,
+                                                         b->ctx.ntypes, packed.get()); });
+    ok[0] = pack_replicas(cut[0], cut[1], n, packed_off.data(), pos, types, b->ctx.ntypes, packed.get());
+    for (auto &th : pool) th.join();
+    for (char o : ok)
+        if (!o) throw std::invalid_argument("particle type out of range");
+    std::vector<RepState> st(R);
+    for (int r = 0; r < R; ++r) st[r] = RepState{(int)n[r], 0, 0, (int)n[r], 0, 0, 0, 0};
+    int64_t *offs_dev = balloc<int64_t>(2 * (size_t)R + 1);
+    struct Release {
+        int64_t *&p;
+        ~Release() { bfree(p); }
+    } release{offs_dev};
+    std::vector<int64_t> offs(packed_off);
+    offs.insert(offs.end(), b->poff.begin(), b->poff.end());
+    RDC_CUDA(cudaMemcpyAsync(offs_dev, offs.data(), sizeof(int64_t) * offs.size(), cudaMemcpyHostToDevice, b->stream));
+    if (total > 0)
+        RDC_CUDA(cudaMemcpyAsync(b->posB, packed.get(), sizeof(float4) * total, cudaMemcpyHostToDevice, b->stream));
+    k_unpack_replicas<<<std::min(R, 4 * 152), 256, 0, b->stream>>>(b->posB, offs_dev, offs_dev + R + 1, b->posA, R);
+    RDC_CUDA(cudaGetLastError());
+    RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, b->stream));
+    b->set_order(std::vector<int64_t>(n, n + R));
+    b->sort_all(true);
+    b->sync();
+}
+}  // namespace
+
 int rdc_batch_set_particles(rdc_batch *b, const int64_t *offsets, const double *pos, const int *types) {
     BATCH_CALL({
         if (!b || !offsets || !pos || !types) throw std::invalid_argument("null argument");
         const int R = b->R;
-        std::vector<float4> hp;
-        std::vector<RepState> st(R);
         std::vector<int64_t> n(R);
-        int64_t total = 0;
-        for (int r = 0; r < R; ++r) total += b->caps[r];
-        hp.assign(total, make_float4(0, 0, 0, 0));
+        std::vector<const double *> p(R);
+        std::vector<const int *> t(R);
         for (int r = 0; r < R; ++r) {
             n[r] = offsets[r + 1] - offsets[r];
-            if (n[r] < 0 || n[r] > b->caps[r]) throw std::invalid_argument("replica particle count exceeds capacity");
-            for (int64_t i = 0; i < n[r]; ++i) {
-                const int64_t k = offsets[r] + i;
-                const int t = types[k];
-                if (t < 0 || t >= b->ctx.ntypes) throw std::invalid_argument("particle type out of range");
-                float4 p;
-                p.x = (float)pos[3 * k]; p.y = (float)pos[3 * k + 1]; p.z = (float)pos[3 * k + 2];
-                std::memcpy(&p.w, &t, 4);
-                hp[b->poff[r] + i] = p;
-            }
-            st[r] = RepState{(int)n[r], 0, 0, (int)n[r], 0, 0, 0, 0};
+            p[r] = pos + 3 * offsets[r];
+            t[r] = types + offsets[r];
         }
-        RDC_CUDA(cudaMemcpyAsync(b->posA, hp.data(), sizeof(float4) * total, cudaMemcpyHostToDevice, b->stream));
-        RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, b->stream));
-        b->set_order(n);
-        b->sort_all(true);
-        b->sync();
+        set_particles_impl(b, n.data(), p.data(), t.data());
+    });
+}
+
+int rdc_batch_set_particles_list(rdc_batch *b, const int64_t *counts, const double *const *positions3,
+                                 const int *const *types) {
+    BATCH_CALL({
+        if (!b || !counts || !positions3 || !types) throw std::invalid_argument("null argument");
+        set_particles_impl(b, counts, positions3, types);
     });
 }
 

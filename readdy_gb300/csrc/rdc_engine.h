@@ -40,8 +40,11 @@ namespace rdc {
 #ifndef RDC_ENGINE_MAX_EVENTS_SM
 #define RDC_ENGINE_MAX_EVENTS_SM 1024
 #endif
+#ifndef RDC_ENGINE_THREADS_MAX
+#define RDC_ENGINE_THREADS_MAX 512
+#endif
 constexpr int SMEM_CELLS = RDC_ENGINE_SMEM_CELLS;
-constexpr int ENGINE_THREADS_MAX = 512;
+constexpr int ENGINE_THREADS_MAX = RDC_ENGINE_THREADS_MAX;
 // accepted events one replica step resolves in shared memory (more raise ST_EVENTS)
 constexpr int ENGINE_MAX_EVENTS_SM = RDC_ENGINE_MAX_EVENTS_SM;
 
