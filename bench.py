@@ -384,8 +384,9 @@ def run_gb300(args, rank, world):
     e2e_t = time.perf_counter() - t0
     e2e_ps = e.particle_steps()
     del e
-    # float4 particles, replica descriptors (136 B) and states (24 B), LPT order (4 B)
-    h2d = int(sum(len(p) for p in pos) * 16 + len(ns) * (136 + 24 + 4))
+    # float4 particles; per replica its descriptor (256 B), state (40 B), LPT order slot (4 B) and two
+    # unpacking offsets (16 B); one set of potential/reaction tables (36752 B)
+    h2d = int(sum(len(p) for p in pos) * 16 + len(ns) * (256 + 40 + 4 + 16) + 36752)
     d2h = int(counts.nbytes)
 
     result = None
