@@ -265,6 +265,12 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
             if (i < n_in && (pairs || pair_pots)) {
                 const int *rrow = rt.o2_tab + ti * rt.T;
                 const float *rsrow = rt.screen + ti * rt.T;
+                // the cells walked reach as far as the largest force or reaction screen of i's type
+                float reach2 = 0.f;
+                for (int t = 0; t < T; ++t) {
+                    if (S.tab[ti * T + t]) reach2 = fmaxf(reach2, S.screen[ti * T + t]);
+                    if (pairs && rrow[t]) reach2 = fmaxf(reach2, rsrow[t]);
+                }
                 auto partner = [&](int j, float4 q, int tj, float d2s) {
                     if (!pairs || j < i) return;
                     const int o2 = rrow[tj];
@@ -282,7 +288,8 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
                         }
                     }
                 };
-                pair_force_at(i, p, pos, start, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e, nullptr, partner);
+                pair_force_at(i, p, pos, start, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e, nullptr, partner,
+                              reach2);
             }
             if (nt > 2) {
                 event_tuples_at(i, true, pos, start, g, 1, rt, push);

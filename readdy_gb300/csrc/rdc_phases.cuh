@@ -83,7 +83,7 @@ __device__ inline bool stencil_fast(const G &g, int radius) {
 
 template <typename G, typename S, typename F>
 __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__restrict__ start, int radius,
-                                               F f, bool skip_lower_columns = false) {
+                                               F f, bool skip_lower_columns = false, float reach2 = INFINITY) {
     int cx, cy, cz;
     cell_coords(p, g, cx, cy, cz);
     const int dx0 = g.dims[0], dy0 = g.dims[1], dz0 = g.dims[2];
@@ -91,8 +91,27 @@ __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__
         // a column stored wholly before the particle's own column holds only smaller storage indices;
         // walks that want partners j > i (skip_lower_columns) need not read its starts
         const int own_base = (cx * dy0 + cy) * dz0;
+        // Lower bounds of the distance from p to the cell below (lo) and above (hi) along each axis: its
+        // offset inside its own cell, less a margin that covers the rounding of the offset.  A column or an
+        // end cell farther than sqrt(reach2) holds no candidate that can pass the caller's screen, so it is
+        // skipped; the candidates that remain keep their order.
+        float lo[3], hi[3];
+        {
+            const float pc[3] = {p.x, p.y, p.z};
+            const int cc[3] = {cx, cy, cz};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float w = g.L[d] / (float)g.dims[d];
+                const float u = (pc[d] + g.hL[d]) - (float)cc[d] * w;
+                const float m = w * (1e-4f + 4e-7f * (float)g.dims[d]);
+                lo[d] = fmaxf(u - m, 0.f);
+                hi[d] = fmaxf(w - u - m, 0.f);
+            }
+        }
 #pragma unroll 1
         for (int ox = -1; ox <= 1; ++ox) {
+            const float dx2 = ox < 0 ? lo[0] * lo[0] : (ox > 0 ? hi[0] * hi[0] : 0.f);
+            if (dx2 > reach2) continue;
             int x = cx + ox;
             if (x < 0) {
                 if (!g.pbc[0]) continue;
@@ -103,6 +122,8 @@ __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__
             }
 #pragma unroll 1
             for (int oy = -1; oy <= 1; ++oy) {
+                const float dxy2 = dx2 + (oy < 0 ? lo[1] * lo[1] : (oy > 0 ? hi[1] * hi[1] : 0.f));
+                if (dxy2 > reach2) continue;
                 int y = cy + oy;
                 if (y < 0) {
                     if (!g.pbc[1]) continue;
@@ -113,7 +134,8 @@ __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__
                 }
                 const int base = (x * dy0 + y) * dz0;
                 if (skip_lower_columns && base < own_base) continue;
-                int z0 = cz - 1, z1 = cz + 1;
+                int z0 = dxy2 + lo[2] * lo[2] > reach2 ? cz : cz - 1;
+                int z1 = dxy2 + hi[2] * hi[2] > reach2 ? cz : cz + 1;
                 if (z0 < 0) {
                     if (g.pbc[2]) f(start[base + dz0 - 1], start[base + dz0]);
                     z0 = 0;
@@ -242,7 +264,8 @@ __device__ inline void for_each_candidate(float4 p, const G &g, const S *__restr
 // load in flight while it screens; the walk is latency bound on these loads.
 template <typename G, typename S, typename F>
 __device__ inline void for_each_candidate_q(float4 p, const G &g, const S *__restrict__ start,
-                                            const float4 *__restrict__ pos, int radius, int jmin, F f) {
+                                            const float4 *__restrict__ pos, int radius, int jmin, F f,
+                                            float reach2 = INFINITY) {
     if (!stencil_fast(g, radius)) {
         for_each_neighbor_range(p, g, start, radius, [&](int jb, int je) {
             for (int j = max(jb, jmin); j < je; ++j) f(j, pos[j]);
@@ -258,7 +281,7 @@ __device__ inline void for_each_candidate_q(float4 p, const G &g, const S *__res
             re[nr] = je;
             ++nr;
         }
-    }, jmin > 0);
+    }, jmin > 0, reach2);
     if (nr == 0) return;
     int r = 0, j = rb[0], je = re[0];
     float4 q = pos[j];
@@ -340,7 +363,9 @@ constexpr int PAIR_BUFFER = 4;
 // here once from each side.
 // With an `extra` callable, extra(j, q, tj, d2) also sees every live candidate j != i of the walk with
 // its FP32 screening distance, before the force filters: the replica engine finds its reaction
-// pairs in the same walk.  The force arithmetic and its order do not depend on it.
+// pairs in the same walk.  The force arithmetic and its order do not depend on it.  reach2 bounds the
+// cells walked (default: the largest pair-potential screen of i's type); a caller with an `extra` passes
+// the largest screen that either needs.
 struct NoExtra {
     __device__ void operator()(int, float4, int, float) const {}
 };
@@ -362,11 +387,16 @@ template <typename G, typename S, typename Extra = NoExtra>
 __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__ pos, const S *__restrict__ start,
                                      const G &g, int radius, const int *tab, const float *screen, const PairPot *pots,
                                      int T, float &fx, float &fy, float &fz, float &e, float *vir = nullptr,
-                                     Extra extra = Extra()) {
+                                     Extra extra = Extra(), float reach2 = -1.f) {
     constexpr bool has_extra = !std::is_same<Extra, NoExtra>::value;
     const int ti = itype(p);
     const int *trow = tab + ti * T;
     const float *srow = screen + ti * T;
+    if (reach2 < 0.f) {  // the largest screen of the type's pair potentials: cells beyond it are not walked
+        reach2 = 0.f;
+        for (int t = 0; t < T; ++t)
+            if (trow[t]) reach2 = fmaxf(reach2, srow[t]);
+    }
     auto body = [&](int j) {
         const float4 q = pos[j];
         const int pt = trow[itype(q)];
@@ -414,7 +444,7 @@ __device__ inline void pair_force_at(int i, float4 p, const float4 *__restrict__
         else if (nb == 2) b2 = j;
         else b3 = j;
         ++nb;
-    });
+    }, reach2);
     for (int k = 0; k < nb; ++k) {
         body(b0);
         b0 = b1; b1 = b2; b2 = b3;
