@@ -39,7 +39,7 @@ DENSITY = 0.25
 N_MIN, N_MAX = 200, 20000
 # DRAM bytes per particle of one fused step (dram__bytes_read.sum + dram__bytes_write.sum of one ncu
 # capture of k_engine_step on the first 512 replicas of the ensemble, divided by its particles).
-DRAM_BYTES_PER_PARTICLE = (92.01e6 + 95.35e6) / 2097522
+DRAM_BYTES_PER_PARTICLE = (91.30e6 + 93.78e6) / 2097522
 # algorithmic bytes of one fused step per particle: the particle state (float4 position with the type,
 # uint32 id) read once and written once (the pair forces carried between steps, 2 x 16 bytes, are a
 # choice of the implementation and count as traffic, not as algorithmic bytes)
