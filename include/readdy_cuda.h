@@ -140,6 +140,19 @@ int rdc_count_types(rdc_system *s, int64_t *counts);
 /* ReactionCounts observable: performed events per reaction id since creation
  * (kernels/cpu/src/CPUStateModel.cpp:126-144) */
 int rdc_get_reaction_counts(rdc_system *s, int n, int64_t *counts);
+/* HistogramAlongAxis observable of the CPU kernel (kernels/cpu/src/observables/CPUObservables.cpp:85-146):
+ * counts (n_borders - 1 values) of the active particles of the listed types by their coordinate on axis
+ * 0..2 and std::upper_bound over the ascending borders; like the CPU kernel, the last bin is never counted */
+int rdc_histogram_along_axis(rdc_system *s, int n_borders, const double *borders, int n_types, const int *types,
+                             int axis, double *counts);
+/* RadialDistribution observable (readdy/main/model/observables/RadialDistribution.cpp:75-128): pair counts
+ * (n_borders - 1) over all ordered pairs of distinct active particles, the first of a from type and the
+ * second of a to type, by their FP64 minimum-image distance; distribution = count / (4/3 pi (r_hi^3 -
+ * r_lo^3) n_from particle_to_density).  A distance below the first border is not counted (the reference
+ * would write before its counts). */
+int rdc_radial_distribution(rdc_system *s, int n_borders, const double *borders, int n_from, const int *from_types,
+                            int n_to, const int *to_types, double particle_to_density, double *counts,
+                            double *distribution);
 /* particle capacity on the device (reaction products beyond it raise RDC_ERR_CAPACITY) */
 int rdc_reserve(rdc_system *s, int64_t capacity);
 /* cell-list tuning: cells per cutoff (the reference's cll_radius, KernelConfiguration.h:63) */

@@ -80,6 +80,8 @@ def _load():
             "orc_gillespie": (i, [vp, d]),
             "orc_run": (i, [vp, i64, d, i, i, P(i64), i64]),
             "orc_reaction_counts": (i, [vp, P(i64), i]),
+            "orc_histogram_along_axis": (i, [vp, i, P(d), i, P(i), i, P(d)]),
+            "orc_radial_distribution": (i, [vp, i, P(d), i, P(i), i, P(i), d, P(d), P(d)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -299,3 +301,26 @@ class OracleSystem:
         out = np.zeros(n, np.int64)
         k = self._lib.orc_reaction_counts(self._h, _ptr(out, C.c_int64), n)
         return out[:k]
+
+    def histogram_along_axis(self, borders, types, axis):
+        """HistogramAlongAxis of the CPU kernel (CPUObservables.cpp:85-146); n_borders - 1 counts."""
+        b = np.ascontiguousarray(borders, np.float64)
+        t = np.ascontiguousarray(types, np.int32)
+        out = np.zeros(max(len(b) - 1, 1), np.float64)
+        if self._lib.orc_histogram_along_axis(self._h, len(b), _ptr(b, C.c_double), len(t), _ptr(t, C.c_int),
+                                              int(axis), _ptr(out, C.c_double)) < 0:
+            raise ValueError("need at least two borders and an axis in 0..2")
+        return out
+
+    def radial_distribution(self, borders, from_types, to_types, particle_to_density):
+        """RadialDistribution (RadialDistribution.cpp:75-128): (counts, distribution)."""
+        b = np.ascontiguousarray(borders, np.float64)
+        f = np.ascontiguousarray(from_types, np.int32)
+        t = np.ascontiguousarray(to_types, np.int32)
+        counts = np.zeros(max(len(b) - 1, 1), np.float64)
+        dist = np.zeros_like(counts)
+        if self._lib.orc_radial_distribution(self._h, len(b), _ptr(b, C.c_double), len(f), _ptr(f, C.c_int), len(t),
+                                             _ptr(t, C.c_int), float(particle_to_density), _ptr(counts, C.c_double),
+                                             _ptr(dist, C.c_double)) < 0:
+            raise ValueError("need at least two borders")
+        return counts, dist

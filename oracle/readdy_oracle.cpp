@@ -1303,4 +1303,55 @@ int orc_reaction_counts(const orc_system *s, int64_t *counts, int cap) {
     return n;
 }
 
+/* kernels/cpu/src/observables/CPUObservables.cpp:85-146: for every active particle of a listed type, the
+ * index of std::upper_bound(borders, pos[axis]); index k counts into bin k - 1 when 1 <= k < n_borders - 1
+ * (the result has n_borders - 1 bins and the CPU kernel compares the index with that size, so the last
+ * bin is never counted) */
+int orc_histogram_along_axis(const orc_system *s, int n_borders, const double *borders, int n_types,
+                             const int *types, int axis, double *counts) {
+    if (n_borders < 2 || axis < 0 || axis > 2) return -1;
+    const int size = n_borders - 1;
+    std::fill(counts, counts + size, 0.0);
+    for (const Entry &e : s->entries) {
+        if (e.deactivated || std::find(types, types + n_types, e.type) == types + n_types) continue;
+        const double *ub = std::upper_bound(borders, borders + n_borders, e.pos[axis]);
+        if (ub == borders + n_borders) continue;
+        const long k = ub - borders;
+        if (k >= 1 && k < size) counts[k - 1] += 1.0;
+    }
+    return size;
+}
+
+/* readdy/main/model/observables/RadialDistribution.cpp:75-128: every ordered pair (from, to) of active
+ * particles with distinct ids, from of a from type and to of a to type, counts into bin k - 1 of
+ * k = index of std::upper_bound(borders, |shortestDifference|) when k < n_borders; the distribution
+ * divides each count by 4/3 pi (r_hi^3 - r_lo^3) n_from particle_to_density.  A distance below the first
+ * border would count into bin -1 there; it is not counted here. */
+int orc_radial_distribution(const orc_system *s, int n_borders, const double *borders, int n_from,
+                            const int *from_types, int n_to, const int *to_types, double particle_to_density,
+                            double *counts, double *distribution) {
+    if (n_borders < 2) return -1;
+    const int size = n_borders - 1;
+    std::fill(counts, counts + size, 0.0);
+    auto in = [](int t, const int *set, int n) { return std::find(set, set + n, t) != set + n; };
+    long n_from_particles = 0;
+    for (const Entry &e : s->entries)
+        if (!e.deactivated && in(e.type, from_types, n_from)) ++n_from_particles;
+    for (const Entry &a : s->entries) {
+        if (a.deactivated || !in(a.type, from_types, n_from)) continue;
+        for (const Entry &b : s->entries) {
+            if (b.deactivated || !in(b.type, to_types, n_to) || a.id == b.id) continue;
+            const double dist = std::sqrt(s->box.dist2(a.pos, b.pos));
+            const double *ub = std::upper_bound(borders, borders + n_borders, dist);
+            if (ub == borders + n_borders || ub == borders) continue;
+            counts[(ub - borders) - 1] += 1.0;
+        }
+    }
+    const double pi = 3.14159265358979323846;
+    for (int k = 0; k < size; ++k)
+        distribution[k] = counts[k] / (4. / 3. * pi * (std::pow(borders[k + 1], 3.) - std::pow(borders[k], 3.)) *
+                                       (double)n_from_particles * particle_to_density);
+    return size;
+}
+
 }  // extern "C"

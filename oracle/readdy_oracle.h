@@ -94,6 +94,15 @@ int orc_run(orc_system *s, int64_t n_steps, double dt, int handler, int count_st
             int64_t max_records);
 /* per-reaction count of performed events accumulated since creation */
 int orc_reaction_counts(const orc_system *s, int64_t *counts, int cap);
+/* HistogramAlongAxis observable of the CPU kernel: counts (n_borders - 1 values) of the active particles of
+ * the listed types along one axis */
+int orc_histogram_along_axis(const orc_system *s, int n_borders, const double *borders, int n_types,
+                             const int *types, int axis, double *counts);
+/* RadialDistribution observable: pair counts (n_borders - 1) over ordered pairs of distinct particles (from
+ * types x to types) and the distribution normalised by shell volume, from-particle count and density */
+int orc_radial_distribution(const orc_system *s, int n_borders, const double *borders, int n_from,
+                            const int *from_types, int n_to, const int *to_types, double particle_to_density,
+                            double *counts, double *distribution);
 
 #ifdef __cplusplus
 }

@@ -72,6 +72,8 @@ def _sig(lib):
         "rdc_get_energy": (i, [vp, P(d)]),
         "rdc_count_types": (i, [vp, P(i64)]),
         "rdc_get_reaction_counts": (i, [vp, i, P(i64)]),
+        "rdc_histogram_along_axis": (i, [vp, i, P(d), i, P(i), i, P(d)]),
+        "rdc_radial_distribution": (i, [vp, i, P(d), i, P(i), i, P(i), d, P(d), P(d)]),
         "rdc_reserve": (i, [vp, i64]),
         "rdc_set_cell_radius": (i, [vp, i]),
         "rdc_initialize": (i, [vp]),

@@ -1211,6 +1211,92 @@ int rdc_count_types(rdc_system *s, int64_t *counts) {
         for (int t = 0; t < s->ctx.ntypes; ++t) counts[t] = (int64_t)h[t];
     });
 }
+}  // extern "C"
+
+namespace {
+// bit mask of the listed particle types (each in range)
+uint32_t type_mask(const rdc_system *s, int n, const int *types) {
+    uint32_t m = 0;
+    for (int k = 0; k < n; ++k) {
+        require(types[k] >= 0 && types[k] < s->ctx.ntypes, "particle type out of range");
+        m |= 1u << types[k];
+    }
+    return m;
+}
+
+// bin counts of one observable: borders uploaded, counters zeroed, `launch` run, counts read back
+template <typename Launch>
+std::vector<unsigned long long> observe_bins(rdc_system *s, int n_borders, const double *borders, Launch launch) {
+    require(n_borders >= 2, "at least two bin borders");
+    require(std::is_sorted(borders, borders + n_borders), "bin borders must be ascending");
+    double *bd = dalloc<double>(n_borders);
+    unsigned long long *od = dalloc<unsigned long long>(n_borders - 1);
+    struct Release {
+        double *&b;
+        unsigned long long *&o;
+        ~Release() { dfree(b); dfree(o); }
+    } release{bd, od};
+    RDC_CUDA(cudaMemcpyAsync(bd, borders, sizeof(double) * n_borders, cudaMemcpyHostToDevice, s->stream));
+    RDC_CUDA(cudaMemsetAsync(od, 0, sizeof(unsigned long long) * (n_borders - 1), s->stream));
+    launch(bd, od);
+    RDC_CUDA(cudaGetLastError());
+    std::vector<unsigned long long> h(n_borders - 1);
+    RDC_CUDA(cudaMemcpyAsync(h.data(), od, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost, s->stream));
+    s->sync();
+    return h;
+}
+}  // namespace
+
+extern "C" {
+
+int rdc_histogram_along_axis(rdc_system *s, int n_borders, const double *borders, int n_types, const int *types,
+                             int axis, double *counts) {
+    return guarded([&] {
+        require(s && borders && counts && (n_types == 0 || types), "null argument");
+        require(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+        const uint32_t mask = type_mask(s, n_types, types);
+        const auto h = observe_bins(s, n_borders, borders, [&](const double *bd, unsigned long long *od) {
+            launch_histogram_axis(s->d, bd, n_borders, mask, axis, od, s->stream);
+        });
+        for (size_t k = 0; k < h.size(); ++k) counts[k] = (double)h[k];
+    });
+}
+
+int rdc_radial_distribution(rdc_system *s, int n_borders, const double *borders, int n_from, const int *from_types,
+                            int n_to, const int *to_types, double particle_to_density, double *counts,
+                            double *distribution) {
+    return guarded([&] {
+        require(s && borders && counts && distribution && (n_from == 0 || from_types) && (n_to == 0 || to_types),
+                "null argument");
+        const uint32_t from = type_mask(s, n_from, from_types), to = type_mask(s, n_to, to_types);
+        // FP32 screen: beyond the last border by more than the rounding of an FP32 squared distance
+        const double rmax = borders[n_borders - 1];
+        const float reach2 = rmax > 0 ? (float)(rmax * rmax * (1.0 + 1e-5)) : 0.f;
+        int n_store = 0;
+        RDC_CUDA(cudaMemcpyAsync(&n_store, s->d.counters + C_N_TOTAL, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        const auto h = observe_bins(s, n_borders, borders, [&](const double *bd, unsigned long long *od) {
+            launch_radial_distribution(s->d, n_store, bd, n_borders, from, to, reach2, od, s->stream);
+        });
+        // from-particle count (the reference's count_if over the active particles)
+        launch_count_types(s->d, s->count_buf, s->stream);
+        std::vector<unsigned long long> tc(s->ctx.ntypes);
+        RDC_CUDA(cudaMemcpyAsync(tc.data(), s->count_buf, sizeof(unsigned long long) * tc.size(), cudaMemcpyDeviceToHost,
+                                 s->stream));
+        s->sync();
+        double n_from_particles = 0;
+        for (int t = 0; t < s->ctx.ntypes; ++t)
+            if ((from >> t) & 1u) n_from_particles += (double)tc[t];
+        // RadialDistribution.cpp:108-118, in the same operation order
+        const double pi = 3.14159265358979323846;
+        for (size_t k = 0; k < h.size(); ++k) {
+            counts[k] = (double)h[k];
+            distribution[k] = counts[k] / (4. / 3. * pi * (std::pow(borders[k + 1], 3.) - std::pow(borders[k], 3.)) *
+                                           n_from_particles * particle_to_density);
+        }
+    });
+}
+
 int rdc_get_reaction_counts(rdc_system *s, int n, int64_t *counts) {
     return guarded([&] {
         require(s && (n == 0 || counts), "null argument");

@@ -169,6 +169,11 @@ void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st);
 void launch_events(const SysDev &s, int handler, cudaStream_t st);
 void launch_resolve_apply(const SysDev &s, int handler, cudaStream_t st);
 void launch_count_types(const SysDev &s, unsigned long long *out, cudaStream_t st);
+// HistogramAlongAxis / RadialDistribution bin counts into out (nb - 1 zeroed counters)
+void launch_histogram_axis(const SysDev &s, const double *borders, int nb, uint32_t types, int axis,
+                           unsigned long long *out, cudaStream_t st);
+void launch_radial_distribution(const SysDev &s, int n, const double *borders, int nb, uint32_t from, uint32_t to,
+                                float reach2, unsigned long long *out, cudaStream_t st);
 void launch_record_counts(const SysDev &s, cudaStream_t st);
 void launch_step_advance(const SysDev &s, cudaStream_t st);
 void launch_pairs(const SysDev &s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out,

@@ -449,6 +449,134 @@ void launch_resolve_apply(const SysDev &s, int handler, cudaStream_t st) {
     k_resolve_apply<<<1, RESOLVE_THREADS, resolve_smem_bytes(), st>>>(s, handler);
 }
 
+// ------------------------------------------------------------------------------------------------
+// observables of ReaDDy's CPU kernel that bin particles or pairs (readdy/main/model/observables)
+// ------------------------------------------------------------------------------------------------
+// bins counted in a shared-memory histogram per block (more go straight to global memory)
+constexpr int OBS_SMEM_BINS = 4096;
+constexpr int RDF_TILE = 256;
+
+// std::upper_bound over borders[0, n): the first border greater than x (FP64 comparisons)
+__device__ inline int upper_bound_d(const double *__restrict__ b, int n, double x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (!(x < b[mid])) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// HistogramAlongAxis of the CPU kernel (kernels/cpu/src/observables/CPUObservables.cpp:85-146): every
+// active particle of a type in `types` (bit mask) adds one to bin k - 1 of k = upper_bound(borders, x),
+// x its coordinate on `axis`, when 1 <= k < nb - 1 (the CPU kernel compares k with the nb - 1 bins of
+// its result, so the last bin stays empty).  The FP32 coordinate widened to FP64 compares exactly.
+__global__ void k_histogram_axis(SysDev s, const double *__restrict__ borders, int nb, uint32_t types, int axis,
+                                 unsigned long long *out) {
+    extern __shared__ unsigned int hist[];
+    const int size = nb - 1;
+    const bool in_smem = size <= OBS_SMEM_BINS;
+    if (in_smem)
+        for (int k = threadIdx.x; k < size; k += blockDim.x) hist[k] = 0u;
+    __syncthreads();
+    const int n = s.counters[C_N_TOTAL];
+    GRID_STRIDE(i, n) {
+        const float4 p = s.pos[i];
+        const int t = itype(p);
+        if (t < 0 || !((types >> t) & 1u)) continue;
+        const double x = (double)(axis == 0 ? p.x : (axis == 1 ? p.y : p.z));
+        const int k = upper_bound_d(borders, nb, x);
+        if (k < 1 || k >= size) continue;
+        if (in_smem) atomicAdd(&hist[k - 1], 1u);
+        else atomicAdd(&out[k - 1], 1ull);
+    }
+    __syncthreads();
+    if (in_smem)
+        for (int k = threadIdx.x; k < size; k += blockDim.x)
+            if (hist[k]) atomicAdd(&out[k], (unsigned long long)hist[k]);
+}
+
+// RadialDistribution (readdy/main/model/observables/RadialDistribution.cpp:75-128): every ordered pair of
+// active particles with distinct ids, the first of a `from` type and the second of a `to` type, adds one to
+// bin k - 1 of k = upper_bound(borders, |x_to - x_from|) when 1 <= k < nb.  All pairs, like the reference:
+// each block holds RDF_TILE `from` particles and streams every particle through shared memory in tiles.  A
+// pair whose FP32 distance is beyond the last border by more than FP32 rounding (reach2) is dropped; the
+// others get the reference's FP64 distance (minimum image, squares summed x, y, z, sqrt), on positions that
+// are exact in FP64.
+__global__ void __launch_bounds__(RDF_TILE) k_radial_distribution(SysDev s, const double *__restrict__ borders,
+                                                                   int nb, uint32_t from, uint32_t to, float reach2,
+                                                                   unsigned long long *out) {
+    extern __shared__ __align__(16) unsigned char rdf_smem[];
+    float4 *tp = reinterpret_cast<float4 *>(rdf_smem);
+    uint32_t *tid = reinterpret_cast<uint32_t *>(tp + RDF_TILE);
+    unsigned int *hist = tid + RDF_TILE;
+    const int size = nb - 1;
+    const bool in_smem = size <= OBS_SMEM_BINS;
+    if (in_smem)
+        for (int k = threadIdx.x; k < size; k += blockDim.x) hist[k] = 0u;
+    const int n = s.counters[C_N_TOTAL];
+    const GeoR g = geo_r(s.geo);
+    const double L[3] = {(double)s.geo.L[0], (double)s.geo.L[1], (double)s.geo.L[2]};
+    for (int base = blockIdx.x * RDF_TILE; base < n; base += gridDim.x * RDF_TILE) {
+        const int i = base + (int)threadIdx.x;
+        float4 p = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        uint32_t idi = 0;
+        if (i < n) {
+            p = s.pos[i];
+            idi = s.id[i];
+        }
+        const int ti = itype(p);
+        const bool counts_from = ti >= 0 && ((from >> ti) & 1u);
+        for (int j0 = 0; j0 < n; j0 += RDF_TILE) {
+            __syncthreads();
+            if (j0 + (int)threadIdx.x < n) {
+                tp[threadIdx.x] = s.pos[j0 + threadIdx.x];
+                tid[threadIdx.x] = s.id[j0 + threadIdx.x];
+            }
+            __syncthreads();
+            if (!counts_from) continue;
+            const int m = min(RDF_TILE, n - j0);
+            for (int k = 0; k < m; ++k) {
+                const float4 q = tp[k];
+                const int tj = itype(q);
+                if (tj < 0 || !((to >> tj) & 1u) || tid[k] == idi) continue;
+                if (screen_d2(p, q, g) > reach2) continue;
+                double dv[3] = {(double)q.x - (double)p.x, (double)q.y - (double)p.y, (double)q.z - (double)p.z};
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    if (s.geo.pbc[d]) {
+                        if (dv[d] > L[d] * .5) dv[d] -= L[d];
+                        else if (dv[d] <= -L[d] * .5) dv[d] += L[d];
+                    }
+                const double d2 =
+                    __dadd_rn(__dadd_rn(__dmul_rn(dv[0], dv[0]), __dmul_rn(dv[1], dv[1])), __dmul_rn(dv[2], dv[2]));
+                const int kb = upper_bound_d(borders, nb, __dsqrt_rn(d2));
+                if (kb < 1 || kb >= nb) continue;
+                if (in_smem) atomicAdd(&hist[kb - 1], 1u);
+                else atomicAdd(&out[kb - 1], 1ull);
+            }
+        }
+    }
+    __syncthreads();
+    if (in_smem)
+        for (int k = threadIdx.x; k < size; k += blockDim.x)
+            if (hist[k]) atomicAdd(&out[k], (unsigned long long)hist[k]);
+}
+
+void launch_histogram_axis(const SysDev &s, const double *borders, int nb, uint32_t types, int axis,
+                           unsigned long long *out, cudaStream_t st) {
+    const size_t smem = nb - 1 <= OBS_SMEM_BINS ? sizeof(unsigned int) * (nb - 1) : 0;
+    k_histogram_axis<<<GRID_BLOCKS, GRID_THREADS, smem, st>>>(s, borders, nb, types, axis, out);
+}
+
+void launch_radial_distribution(const SysDev &s, int n, const double *borders, int nb, uint32_t from, uint32_t to,
+                                float reach2, unsigned long long *out, cudaStream_t st) {
+    const size_t smem = (sizeof(float4) + sizeof(uint32_t)) * RDF_TILE +
+                        (nb - 1 <= OBS_SMEM_BINS ? sizeof(unsigned int) * (nb - 1) : 0);
+    const int blocks = std::max(1, std::min((n + RDF_TILE - 1) / RDF_TILE, 8 * 152));
+    k_radial_distribution<<<blocks, RDF_TILE, smem, st>>>(s, borders, nb, from, to, reach2, out);
+}
+
 void launch_count_types(const SysDev &s, unsigned long long *out, cudaStream_t st) {
     RDC_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long) * MAX_TYPES, st));
     k_count_types<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, out);

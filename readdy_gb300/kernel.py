@@ -231,6 +231,29 @@ class CUDAKernel:
         N.check(self._lib.rdc_get_reaction_counts(self._h, n, _p(out, C.c_int64)))
         return out[:self.context.n_reactions]
 
+    def histogram_along_axis(self, bin_borders, types, axis):
+        """HistogramAlongAxis observable (CPUObservables.cpp:85-146): counts of the listed types' particles
+        along `axis` in the bins between ascending borders (the CPU kernel never fills the last bin)."""
+        b = np.ascontiguousarray(bin_borders, np.float64)
+        t = np.ascontiguousarray(types, np.int32)
+        out = np.zeros(max(len(b) - 1, 1), np.float64)
+        N.check(self._lib.rdc_histogram_along_axis(self._h, len(b), _p(b, C.c_double), len(t), _p(t, C.c_int),
+                                                   int(axis), _p(out, C.c_double)))
+        return out[:len(b) - 1]
+
+    def radial_distribution(self, bin_borders, from_types, to_types, particle_to_density):
+        """RadialDistribution observable (RadialDistribution.cpp:75-128): (bin centers, distribution, counts)."""
+        b = np.ascontiguousarray(bin_borders, np.float64)
+        f = np.ascontiguousarray(from_types, np.int32)
+        t = np.ascontiguousarray(to_types, np.int32)
+        counts = np.zeros(max(len(b) - 1, 1), np.float64)
+        dist = np.zeros_like(counts)
+        N.check(self._lib.rdc_radial_distribution(self._h, len(b), _p(b, C.c_double), len(f), _p(f, C.c_int), len(t),
+                                                  _p(t, C.c_int), float(particle_to_density), _p(counts, C.c_double),
+                                                  _p(dist, C.c_double)))
+        centers = (b[:-1] + b[1:]) / 2
+        return centers, dist[:len(b) - 1], counts[:len(b) - 1]
+
     def reserve(self, capacity):
         N.check(self._lib.rdc_reserve(self._h, int(capacity)))
 

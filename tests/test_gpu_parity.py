@@ -555,3 +555,54 @@ def test_polymer_forces_match_oracle(rg, terms):
     bad = err > FORCE_RTOL
     assert bad.sum() <= (3 if "dihedral" in use else 0), np.sort(err)[-8:]
     assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
+
+
+def _observable_case(case):
+    """(box, periodic, positions, types, borders for the histogram and the RDF, steps to run first)."""
+    rng = np.random.default_rng(41)
+    if case == "lattice":  # pair distances and coordinates on the bin borders
+        g = np.arange(-4.0, 4.0)
+        pos = np.array([[x, y, z] for x in g for y in g for z in g])
+        types = rng.integers(0, 3, len(pos)).astype(np.int32)
+        return (8., 8., 8.), (1, 1, 1), pos, types, np.arange(-4.0, 4.01, 1.0), np.arange(0., 4.01, 0.5), 0
+    if case == "walls":  # particles on both sides of the walls of a closed box
+        pos = (rng.random((3000, 3)) - 0.5) * 12.0
+        types = rng.integers(0, 3, len(pos)).astype(np.int32)
+        return (10., 10., 10.), (0, 0, 0), pos, types, np.linspace(-6., 6., 97), np.linspace(0., 7., 141), 0
+    pos = (rng.random((4000, 3)) - 0.5) * 16.0
+    types = rng.integers(0, 3, len(pos)).astype(np.int32)
+    return (16., 16., 16.), (1, 1, 1), pos, types, np.linspace(-8., 8., 257), np.linspace(0., 7.5, 301), 20
+
+
+@pytest.mark.parametrize("case", ["random", "lattice", "walls"])
+def test_observables_match_oracle(rg, case):
+    """HistogramAlongAxis and RadialDistribution on the device equal the FP64 restatement of the reference's
+    observables bit for bit (counts and normalised distribution), on the state left by the GPU's dynamics:
+    exact ties of coordinates and distances with the borders, particles outside a closed box, and a
+    bin set too large for the per-block shared-memory histogram."""
+    box, pbc, pos, types, hb, rb = _observable_case(case)[:6]
+    steps = _observable_case(case)[6]
+    ctx = rg.Context(box, pbc, 1.0, (1.0, 0.5, 0.2))
+    for a in range(3):
+        for b in range(a, 3):
+            ctx.add_harmonic_repulsion(a, b, 10.0, 1.0)
+    k = rg.CUDAKernel(ctx, seed=3)
+    k.add_particles(f32(pos), types)
+    if steps:
+        k.run(steps, 1e-3)
+    p, t, _ = k.get_particles()
+    o = oracle.OracleSystem([float(np.float32(x)) for x in box], pbc, 1.0, (1.0, 0.5, 0.2))
+    o.add_particles(np.asarray(p, np.float64), np.asarray(t, np.int32))
+    for axis in range(3):
+        for sel in ([0], [1, 2], [0, 1, 2]):
+            np.testing.assert_array_equal(k.histogram_along_axis(hb, sel, axis), o.histogram_along_axis(hb, sel, axis))
+    for frm, to in (([0], [1]), ([1, 2], [0, 1, 2]), ([0, 1, 2], [0, 1, 2])):
+        _, dist, counts = k.radial_distribution(rb, frm, to, 0.25)
+        oc, od = o.radial_distribution(rb, frm, to, 0.25)
+        np.testing.assert_array_equal(counts, oc)
+        np.testing.assert_array_equal(dist, od)
+        assert counts.sum() > 0
+    # more bins than the shared-memory histogram holds: counts go straight to global memory
+    fine = np.linspace(0., 7.5, 5001)
+    np.testing.assert_array_equal(k.radial_distribution(fine, [0], [1, 2], 0.25)[2],
+                                  o.radial_distribution(fine, [0], [1, 2], 0.25)[0])

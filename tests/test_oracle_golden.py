@@ -212,3 +212,38 @@ def test_virial_of_one_pair():
     expect = np.zeros((3, 3))
     expect[2, 2] = 0.36
     np.testing.assert_allclose(s.virial(), expect, atol=1e-12)
+
+
+def test_radial_distribution_of_one_pair():
+    """The reference's radial-distribution scenario (readdy/tests/test_observables_io.py:201-239): A at
+    (-2.5, 0, 0) and B at the origin in a periodic 10^3 box, bins of 0.01 up to 5, from A to B at density
+    1/1000: one count, in the bin of 2.5, normalised by its shell volume."""
+    s = oracle.OracleSystem((10., 10., 10.), (1, 1, 1), 2.0, (0.2, 0.2))
+    s.add_harmonic_repulsion(0, 1, 10.0, 2.0)
+    s.add_particles(np.array([[-2.5, 0., 0.], [0., 0., 0.]]), np.array([0, 1], np.int32))
+    borders = np.arange(0, 5, .01)
+    counts, dist = s.radial_distribution(borders, [0], [1], 1. / 1000.)
+    k = np.searchsorted(borders, 2.5, side="right") - 1  # std::upper_bound - 1
+    expected = np.zeros(len(borders) - 1)
+    expected[k] = 1.0
+    np.testing.assert_array_equal(counts, expected)
+    shell = 4. / 3. * np.pi * (borders[k + 1] ** 3 - borders[k] ** 3)
+    assert dist[k] == pytest.approx(1.0 / (shell * 1 * 1e-3), rel=1e-12)
+    assert np.count_nonzero(dist) == 1
+    # from B to A and from both to both count the reverse pair as well
+    c2, _ = s.radial_distribution(borders, [0, 1], [0, 1], 1. / 1000.)
+    assert c2[k] == 2.0 and c2.sum() == 2.0
+
+
+def test_histogram_along_axis_counts_like_the_cpu_kernel():
+    """HistogramAlongAxis of the CPU kernel (CPUObservables.cpp:85-146): a coordinate equal to a border
+    counts into the bin above it (upper_bound), only listed types count, and the last bin is never filled."""
+    s = oracle.OracleSystem((10., 10., 10.), (1, 1, 1), 1.0, (1.0, 1.0))
+    xs = [-4.0, -3.5, -3.0, -1.0, 0.0, 0.5, 3.9, 4.5, 2.0]
+    ts = [0, 0, 0, 0, 0, 0, 0, 0, 1]
+    s.add_particles(np.array([[x, 0., 0.] for x in xs]), np.array(ts, np.int32))
+    borders = np.array([-4.0, -3.0, 0.0, 1.0, 4.0, 5.0])
+    h = s.histogram_along_axis(borders, [0], 0)
+    # bins [-4,-3): -4, -3.5; [-3,0): -3, -1; [0,1): 0, 0.5; [1,4): 3.9; [4,5): 4.5 -> never counted
+    np.testing.assert_array_equal(h, [2., 2., 2., 1., 0.])
+    np.testing.assert_array_equal(s.histogram_along_axis(borders, [1], 0), [0., 0., 0., 1., 0.])
