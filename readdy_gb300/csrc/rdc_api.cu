@@ -491,10 +491,12 @@ struct rdc_system {
         read_counters(c);
         const int64_t need = (int64_t)c[C_N_TOTAL] + n;
         if (need > INT_MAX / 2) throw InvalidArgument("too many particles");
-        if (need > d.capacity) {
-            int cap = std::max(d.capacity, 1024);
-            while (cap < need) cap *= 2;
-            reserve(cap);
+        // room for the products a reaction step appends before the next sort compacts the storage
+        const int64_t want = need + need / 4 + 64;
+        if (want > d.capacity) {
+            int64_t cap = std::max(d.capacity, 1024);
+            while (cap < want) cap *= 2;
+            reserve((int)std::min<int64_t>(cap, INT_MAX / 2));
         }
         std::vector<float4> hp(n);
         std::vector<int> ht(n);
@@ -744,7 +746,7 @@ void rdc_system::step_sequence(int handler, bool reactions, bool structural, int
                 swap_buffers();
             }
         }
-        launch_forces(d, true, n_top > 0, stream);
+        launch_forces(d, true, n_top > 0, stream, false);  // energy and virial: once, after the run
         launch_record_counts(d, stream);
     }
 }
@@ -807,6 +809,8 @@ void rdc_system::run(int64_t n_steps, double dt, int handler, int64_t stride, in
     }
     const int64_t rest = n_steps - reps * per_graph;
     if (rest > 0) step_sequence(handler, reactions, structural, (int)rest);
+    // the energy and virial of the last force calculation (its per-block partials are still in place)
+    if (n_steps > 0) launch_force_finals(d, n_top > 0, stream);
     forces_live = true;
     sync();
     check_status();

@@ -102,7 +102,8 @@ enum Counter : int {
     C_REC = 6,       // observable records written
     C_N_BIRTHS = 7,  // births of the last reaction step (host statistics)
     C_BIG = 8,       // cells with more than CELL_SORT_SMALL entries found by the last sort
-    C_COUNT = 9
+    C_DONE = 9,      // blocks finished in the current launch (the last one advances a step or record counter)
+    C_COUNT = 10
 };
 
 struct SysDev {
@@ -165,7 +166,10 @@ constexpr int GRID_THREADS = 256;
 void launch_integrate_bin(const SysDev &s, bool integrate, cudaStream_t st);
 void launch_bin(const SysDev &s, cudaStream_t st);
 void launch_sort(const SysDev &s, bool permute_force, cudaStream_t st);  // scan, scatter, per-cell order, gather
-void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st);
+// pair (and bonded) forces; with finals the energy and virial reductions follow (a run does them once
+// after its last step instead, see launch_force_finals)
+void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st, bool finals = true);
+void launch_force_finals(const SysDev &s, bool bonded, cudaStream_t st);
 void launch_events(const SysDev &s, int handler, cudaStream_t st);
 void launch_resolve_apply(const SysDev &s, int handler, cudaStream_t st);
 void launch_count_types(const SysDev &s, unsigned long long *out, cudaStream_t st);

@@ -25,6 +25,20 @@ namespace rdc {
 // ------------------------------------------------------------------------------------------------
 // K5 (+ bin): Euler-Maruyama step, then the bin of the new position and its rank inside the bin
 // ------------------------------------------------------------------------------------------------
+// true in one thread of the last block of the grid to finish (C_DONE counts the finished blocks and is
+// reset by that block): the place for a counter update that every block must see unchanged
+__device__ inline bool last_block_done(int *counters) {
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&counters[C_DONE], 1) == (int)(gridDim.x * gridDim.y) - 1;
+        if (last) counters[C_DONE] = 0;
+    }
+    __syncthreads();
+    return last && threadIdx.x == 0;
+}
+
 __global__ void k_integrate_bin(SysDev s, int integrate, int bin) {
     const int n = s.counters[C_N_TOTAL];
     const uint64_t step = s.step[0];
@@ -43,9 +57,9 @@ __global__ void k_integrate_bin(SysDev s, int integrate, int bin) {
             s.rank[i] = atomicAdd(&s.cnt[b], 1);
         }
     }
+    // the integrator step counter (Philox key) advances once every block has read it
+    if (integrate && last_block_done(s.counters)) s.step[0] = step + 1;
 }
-
-__global__ void k_bd_step_advance(SysDev s) { s.step[0] += 1; }
 
 // ------------------------------------------------------------------------------------------------
 // exclusive scan of the bin counts (tiles of 2048, one pass over tile sums, one add pass)
@@ -98,7 +112,43 @@ __global__ void k_scan_add(int *out, const int *tile_sums, int n) {
 
 int scan_block_count(int n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
 
+// the whole scan in one block, tile after tile with a running carry (one launch instead of three for
+// grids of up to SCAN_ONE_BLOCK cells, where the launches cost more than the work)
+constexpr int SCAN_ONE_BLOCK = 16384, SCAN_ONE_THREADS = 1024;
+__global__ void __launch_bounds__(SCAN_ONE_THREADS) k_scan_one_block(const int *__restrict__ in, int *__restrict__ out,
+                                                                     int n) {
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int tile = SCAN_ONE_THREADS * SCAN_ITEMS;
+    for (int base = 0; base < n; base += tile) {
+        const int b = base + (int)threadIdx.x * SCAN_ITEMS;
+        int v[SCAN_ITEMS];
+        int sum = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            v[k] = (b + k < n) ? in[b + k] : 0;
+            sum += v[k];
+        }
+        int total;
+        int run = block_exclusive_scan(sum, total) + carry;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            if (b + k < n) out[b + k] = run;
+            run += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
 static void launch_scan(const int *in, int *out, int *tiles, int n, cudaStream_t st) {
+    if (n <= SCAN_ONE_BLOCK) {
+        k_scan_one_block<<<1, SCAN_ONE_THREADS, 0, st>>>(in, out, n);
+        return;
+    }
     const int nt = scan_block_count(n);
     k_scan_tiles<<<nt, SCAN_THREADS, 0, st>>>(in, out, tiles, n);
     k_scan_top<<<1, 1024, 0, st>>>(tiles, nt, out, n);
@@ -356,7 +406,8 @@ __global__ void k_count_types(SysDev s, unsigned long long *out) {
         if (hist[k]) atomicAdd(&out[k], (unsigned long long)hist[k]);
 }
 
-// counts into the record ring when the step is a multiple of the stride
+// counts into the record ring when the step is a multiple of the stride; the record counter advances
+// once every block has added its counts
 __global__ void k_record_counts(SysDev s) {
     const uint64_t t = s.step[0] - s.rec_base;
     if (s.counts_stride <= 0 || t % (uint64_t)s.counts_stride != 0) return;
@@ -374,12 +425,7 @@ __global__ void k_record_counts(SysDev s) {
     __syncthreads();
     for (int k = threadIdx.x; k < T; k += blockDim.x)
         if (hist[k]) atomicAdd(&s.counts_ring[(size_t)rec * T + k], (unsigned long long)hist[k]);
-}
-
-__global__ void k_record_advance(SysDev s) {
-    const uint64_t t = s.step[0] - s.rec_base;
-    if (s.counts_stride > 0 && t % (uint64_t)s.counts_stride == 0 && s.counters[C_REC] < s.counts_max)
-        s.counters[C_REC] += 1;
+    if (last_block_done(s.counters)) s.counters[C_REC] = rec + 1;
 }
 
 __global__ void k_pairs(SysDev s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out) {
@@ -415,7 +461,6 @@ void init_kernel_attributes() {
 void launch_integrate_bin(const SysDev &s, bool integrate, cudaStream_t st) {
     RDC_CUDA(cudaMemsetAsync(s.cnt, 0, sizeof(int) * (s.geo.ncells + 2), st));
     k_integrate_bin<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, integrate ? 1 : 0, 1);
-    if (integrate) k_bd_step_advance<<<1, 1, 0, st>>>(s);
 }
 
 void launch_bin(const SysDev &s, cudaStream_t st) { launch_integrate_bin(s, false, st); }
@@ -429,15 +474,16 @@ void launch_sort(const SysDev &s, bool permute_force, cudaStream_t st) {
     k_gather<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, permute_force ? 1 : 0);
 }
 
-void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st) {
-    if (s.virial) {
-        k_pair_forces<true><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
-        k_virial_final<<<1, 256, 0, st>>>(s);
-    } else {
-        k_pair_forces<false><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
-    }
-    if (bonded && s.n_top > 0) k_bonded<<<BONDED_BLOCKS, 256, 0, st>>>(s);
+void launch_force_finals(const SysDev &s, bool bonded, cudaStream_t st) {
+    if (s.virial) k_virial_final<<<1, 256, 0, st>>>(s);
     k_energy_final<<<1, 256, 0, st>>>(s, 1, (bonded && s.n_top > 0) ? 1 : 0);
+}
+
+void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st, bool finals) {
+    if (s.virial) k_pair_forces<true><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
+    else k_pair_forces<false><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
+    if (bonded && s.n_top > 0) k_bonded<<<BONDED_BLOCKS, 256, 0, st>>>(s);
+    if (finals) launch_force_finals(s, bonded, st);
     (void)pair;
 }
 
@@ -584,7 +630,6 @@ void launch_count_types(const SysDev &s, unsigned long long *out, cudaStream_t s
 
 void launch_record_counts(const SysDev &s, cudaStream_t st) {
     k_record_counts<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
-    k_record_advance<<<1, 1, 0, st>>>(s);
 }
 
 void launch_pairs(const SysDev &s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out,
