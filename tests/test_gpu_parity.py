@@ -493,14 +493,54 @@ def test_batch_carried_forces_bitwise(rg, periodic, dense):
     ca, cb = a.count_types(), b.count_types()
     np.testing.assert_array_equal(ca, cb)
     assert np.any(ca != c0)
+    na = a.n_particles()
     for r in range(len(sizes)):
         pa, ta, ia = a.get_particles(r)
         pb, tb, ib = b.get_particles(r)
+        assert na[r] == len(pa) == ca[r].sum()  # live particles of a state with removed slots in place
         (pa, ta, ia) = by_id(ia, pa, ta, ia)
         (pb, tb, ib) = by_id(ib, pb, tb, ib)
         np.testing.assert_array_equal(ia, ib)
         np.testing.assert_array_equal(ta, tb)
         np.testing.assert_array_equal(pa, pb)
+
+
+def test_batch_flat_upload_equals_list_upload(rg):
+    """rdc_batch_set_particles (one flat array with offsets) and rdc_batch_set_particles_list (one array per
+    replica) give the same batch, and both reject a type out of range."""
+    import ctypes as C
+    from readdy_gb300 import _native as N
+    b1, sizes = _reactive_batch(rg, True, False, carry=True)
+    rng = np.random.default_rng(31)
+    boxes, poss, typess = [], [], []
+    for n in sizes:  # the draws of _reactive_batch
+        L = float(np.float32((n / 0.25) ** (1 / 3)))
+        boxes.append((L, L, L))
+        poss.append(f32((rng.random((n, 3)) - 0.5) * L))
+        typess.append(rng.integers(0, 4, n).astype(np.int32))
+    b2, _ = _reactive_batch(rg, True, False, carry=True)
+    offs = np.zeros(len(sizes) + 1, np.int64)
+    offs[1:] = np.cumsum(sizes)
+    flat = np.ascontiguousarray(np.concatenate(poss), np.float64)
+    ty = np.ascontiguousarray(np.concatenate(typess), np.int32)
+    lib = N.load()
+    lib.rdc_batch_set_particles.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    assert lib.rdc_batch_set_particles(b2._h, offs.ctypes.data, flat.ctypes.data, ty.ctypes.data) == 0
+    b2.configure(handler=rg.UNCONTROLLED_APPROXIMATION, dt=1e-3, cell_width_scale=1.0, threads_per_block=256)
+    b1.step(20)
+    b2.step(20)
+    b1.synchronize()
+    b2.synchronize()
+    for r in range(len(sizes)):
+        p1, t1, i1 = b1.get_particles(r)
+        p2, t2, i2 = b2.get_particles(r)
+        np.testing.assert_array_equal(i1, i2)
+        np.testing.assert_array_equal(t1, t2)
+        np.testing.assert_array_equal(p1, p2)
+    bad = [t.copy() for t in typess]
+    bad[2][5] = 7
+    with pytest.raises(ValueError):
+        b1.set_particles(poss, bad)
 
 
 @pytest.mark.parametrize("terms", ["bond", "angle", "dihedral", "all"])
