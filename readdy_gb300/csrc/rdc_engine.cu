@@ -572,11 +572,12 @@ __device__ inline bool refresh_in_place(const float4 *__restrict__ pos, const ui
 }
 
 // one step of one replica by the whole block; C is the cell array's type (uint16_t in shared memory
-// or int in global memory).  Inlined into the kernel: as a call, the geometry and tables it passes
-// down by reference live in local memory and the candidate walks reload them per candidate.
+// or int in global memory).  Inlined into the kernel: compiled as a call it took a 700-byte stack frame
+// per thread (the arguments it passes down by reference live in local memory), 232 bytes inlined.
 template <typename C>
-__device__ __forceinline__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, const RxnTables &rt, const Tables *tab,
-                             const RepDesc &D, const RepState &st, int &sh_nev, int &sh_status, C *cells) {
+__device__ __forceinline__ void replica_body(const EngineDev &E, int r, const SmemLayout &S, const RxnTables &rt,
+                                             const Tables *tab, const RepDesc &D, const RepState &st, int &sh_nev,
+                                             int &sh_status, C *cells) {
     const int T = tab->ntypes, NP = tab->npots;
     const uint64_t step = (uint64_t)st.step;
     const Geo &gs = D.geo;
