@@ -63,3 +63,29 @@ def test_context_registries_validate_like_the_reference():
     ctx.add_fusion(0, 1, 1, 1.0, 1.5)
     assert ctx.calculate_max_cutoff() == pytest.approx(1.5)
     assert ctx.add_fission(1, 0, 1, 0.1, 1.0) == 1
+
+
+def test_null_arguments_are_rejected_before_any_device_call():
+    """The entry points added for observables, uploads and the force switch check their pointers first, so a
+    caller's mistake is an RDC_ERR_INVALID_ARGUMENT (1) with a message, on any machine."""
+    from readdy_gb300 import _native
+    lib = _native.load()
+    v = ctypes.c_void_p
+    for name, nargs in (("rdc_histogram_along_axis", 7), ("rdc_radial_distribution", 10),
+                        ("rdc_batch_set_particles_list", 4), ("rdc_batch_set_carry_forces", 2)):
+        f = getattr(lib, name)
+        f.restype = ctypes.c_int
+        args = [None] * nargs
+        if name == "rdc_histogram_along_axis":
+            f.argtypes = [v, ctypes.c_int, v, ctypes.c_int, v, ctypes.c_int, v]
+            args = [None, 2, None, 0, None, 0, None]
+        elif name == "rdc_radial_distribution":
+            f.argtypes = [v, ctypes.c_int, v, ctypes.c_int, v, ctypes.c_int, v, ctypes.c_double, v, v]
+            args = [None, 2, None, 0, None, 0, None, 1.0, None, None]
+        elif name == "rdc_batch_set_carry_forces":
+            f.argtypes = [v, ctypes.c_int]
+            args = [None, 1]
+        else:
+            f.argtypes = [v] * nargs
+        assert f(*args) == 1, name
+        assert "null argument" in lib.rdc_last_error().decode()
