@@ -549,7 +549,9 @@ def main():
             print(json.dumps(run_reference(args)), flush=True)
         return
     if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
+        # the library creates its streams and buffers on the rank's own GPU
+        from readdy_gb300 import _native
+        _native.check(_native.load().rdc_set_device(int(os.environ.get("LOCAL_RANK", "0"))))
     res = run_gb300(args, rank, world)
     if rank == 0 and res is not None:
         print(json.dumps(res), flush=True)

@@ -4,7 +4,7 @@
  * libreaddy_cuda_core.so exports these symbols.  They take plain pointers, sizes and PODs, return an
  * int status (RDC_OK or an RDC_ERR_* code) and never throw; rdc_last_error() returns the message of
  * the calling thread's last failure.  A ReaDDy kernel plugin (model::Kernel, StateModel,
- * ActionFactory) binds one call per action; the binding is shown in INTEGRATION.md.
+ * ActionFactory) binds one call per action.
  *
  * Each entry point names the reference interface it replaces (paths inside readdy/readdy).
  * Positions, box sizes and parameters are passed in FP64 like the reference's `scalar`
@@ -43,6 +43,9 @@ const char *rdc_last_error(void);
 int rdc_version(void);
 /* KernelProvider plugin identity: name() of kernels/cpu .. CPUKernel.h:150-152; returns "CUDA" */
 const char *rdc_kernel_name(void);
+/* the GPU that the calling thread's later calls create their objects on (cudaSetDevice); objects stay
+ * on the device they were created on.  No reference counterpart: the CPU kernel has no device. */
+int rdc_set_device(int device);
 
 /* ---- model::Context (include/readdy/model/Context.h) ------------------------------------------ */
 /* box, periodicity, kBT (Context.h:76-108) and species with diffusion constants
@@ -222,6 +225,17 @@ int rdc_batch_n_particles(rdc_batch *b, int64_t *n_per_replica);
 /* particles of one replica, same layout as rdc_get_particles */
 int rdc_batch_get_particles(rdc_batch *b, int replica, int64_t capacity, double *positions3, int *types,
                             uint64_t *ids, int64_t *n_out);
+/* the Forces observable of one replica (kernels/cpu/src/observables/CPUObservables.cpp:177-197): the force its next Euler update applies to each particle, pair forces (carried from the
+ * last event walk, or summed over the sorted state) plus order-1 potentials, in the order and with
+ * the ids of rdc_batch_get_particles */
+int rdc_batch_get_forces(rdc_batch *b, int replica, int64_t capacity, double *forces3, uint64_t *ids,
+                         int64_t *n_out);
+/* performed events per replica and reaction since the batch was created (n_replicas * n, by reaction
+ * id; the ReactionCounts observable, CPUStateModel.cpp:126-144, of every replica) */
+int rdc_batch_reaction_counts(rdc_batch *b, int n, int64_t *counts);
+/* the cell grid a replica runs on (cells per axis) and whether its cell starts live in shared memory
+ * during a step (1) or in global memory (0) */
+int rdc_batch_replica_grid(rdc_batch *b, int replica, int *dims3, int *shared_cells);
 int rdc_batch_synchronize(rdc_batch *b);
 
 /* ---- served form (no reference counterpart: a request loop over independent simulations) --------
@@ -260,23 +274,29 @@ int rdc_server_stats(rdc_server *s, uint64_t *particle_steps, uint64_t *bytes_in
                      int64_t *n_pending);
 
 /* ---- forces without device allocation (no counterpart in the reference) ----------------------
- * For callers that cannot let the library allocate device memory where they need forces: code that
- * records its step by CUDA stream capture (no cudaMalloc while a stream captures) and embeddings
- * whose own pool owns all of the GPU's memory.  Pair forces and the pair energy of n particles held
- * in the caller's device arrays -- positions3 (n*3 floats), types (n ints in [0, n_types)) -- are
- * written to the caller's device arrays forces3 (n*3 floats) and *energy (one double), on `stream`
- * (a cudaStream_t; NULL is the legacy default stream), asynchronously.  Same pair potentials, exact
- * cutoff test and FP32 terms as rdc_calculate_forces; the neighbour summation order may differ.  The
- * context's order-1 (external) potentials are not applied here. 
+ * For callers that cannot let the library call cudaMalloc where they need forces: embeddings whose
+ * own pool owns all of the GPU's memory (an MD engine, a framework with its own caching allocator, a
+ * service that carves HBM into fixed pools) and step loops that must not stall on the allocator.
+ * Pair forces and the pair energy of n particles held in the caller's device arrays -- positions3
+ * (n*3 floats), types (n ints in [0, n_types)) -- are written to the caller's device arrays forces3
+ * (n*3 floats) and *energy (one double), on `stream` (a cudaStream_t; NULL is the legacy default
+ * stream), asynchronously.  Same pair potentials, exact cutoff test and FP32 terms as
+ * rdc_calculate_forces; the neighbour summation order may differ.  The context's order-1 (external)
+ * potentials are not applied here.  Positions on a periodic axis must lie in [-L/2, L/2), the range
+ * bcs::fixPosition keeps them in; on a closed axis a particle outside the box gets no force, as in the
+ * reference's cell list.
  *
  * Working space is one static device array of RDC_NOALLOC_SCRATCH_BYTES per device, so at most
  * RDC_NOALLOC_MAX_PARTICLES particles are accepted (more returns RDC_ERR_INVALID_ARGUMENT) and the
  * cell grid is widened to at most RDC_NOALLOC_MAX_CELLS cells.  The first call on a device, and the
- * first call after the context's potentials changed, finds the array and copies the potential tables
- * into it, synchronising the stream; make that call before any stream capture (during capture it
- * returns RDC_ERR_LOGIC).  All calls on one device share the array: calls that overlap (different
- * streams or threads without ordering) race and give wrong results.  A type outside [0, n_types) gives that particle no force and makes
- * *energy NaN. */
+ * first call after the context's potentials changed, finds the array (cudaGetSymbolAddress with that
+ * device current) and copies the potential tables into it, synchronising the stream; that call should
+ * come before any stream capture (during capture it returns RDC_ERR_LOGIC).  All calls on one device
+ * share the array and it keeps the last call's contents: calls that overlap on the GPU (different
+ * streams or threads without ordering) race and give wrong results; when such a call has replaced
+ * the tables with another context's, the forces and *energy come out NaN.  A type outside
+ * [0, n_types), a coordinate that is not a number, or one outside the box on a periodic axis gives
+ * that particle no force and makes *energy NaN. */
 #define RDC_NOALLOC_MAX_PARTICLES 65536
 #define RDC_NOALLOC_MAX_CELLS 131072
 #define RDC_NOALLOC_SCRATCH_BYTES 3185408

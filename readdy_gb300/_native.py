@@ -40,6 +40,7 @@ def _sig(lib):
         "rdc_last_error": (C.c_char_p, []),
         "rdc_version": (i, []),
         "rdc_kernel_name": (C.c_char_p, []),
+        "rdc_set_device": (i, [i]),
         "rdc_context_create": (i, [vpp, P(d), P(i), d, i, P(d)]),
         "rdc_context_destroy": (i, [vp]),
         "rdc_context_max_cutoff": (i, [vp, P(d)]),
@@ -99,6 +100,9 @@ def _sig(lib):
         "rdc_batch_count_types": (i, [vp, P(i64)]),
         "rdc_batch_n_particles": (i, [vp, P(i64)]),
         "rdc_batch_get_particles": (i, [vp, i, i64, P(d), P(i), P(u64), P(i64)]),
+        "rdc_batch_get_forces": (i, [vp, i, i64, P(d), P(u64), P(i64)]),
+        "rdc_batch_reaction_counts": (i, [vp, i, P(i64)]),
+        "rdc_batch_replica_grid": (i, [vp, i, P(i), P(i)]),
         "rdc_batch_synchronize": (i, [vp]),
         "rdc_server_create": (i, [vpp, u64, i, i, i64]),
         "rdc_server_destroy": (i, [vp]),

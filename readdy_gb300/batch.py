@@ -106,6 +106,30 @@ class ReplicaBatch:
         N.check(self._lib.rdc_batch_n_particles(self._h, _p(out, C.c_int64)))
         return out
 
+    def get_forces(self, replica):
+        """(forces (n, 3), ids) of one replica's live particles, in the order of get_particles: the force
+        its next step applies (pair forces carried or summed, plus order-1 potentials)."""
+        n = int(self.n_particles()[replica])
+        f = np.zeros((n, 3)); ids = np.zeros(n, np.uint64)
+        got = C.c_int64()
+        N.check(self._lib.rdc_batch_get_forces(self._h, int(replica), n, _p(f, C.c_double), _p(ids, C.c_uint64),
+                                               C.byref(got)))
+        return f[:got.value], ids[:got.value]
+
+    def reaction_counts(self):
+        """Performed events per replica and reaction id, (n_replicas, n_reactions)."""
+        n = self.context.n_reactions
+        out = np.zeros((self.n_replicas, max(n, 1)), np.int64)
+        N.check(self._lib.rdc_batch_reaction_counts(self._h, n, _p(out, C.c_int64)))
+        return out[:, :n]
+
+    def replica_grid(self, replica):
+        """(cells per axis, cell starts in shared memory during a step) of one replica."""
+        dims = np.zeros(3, np.int32)
+        sh = C.c_int()
+        N.check(self._lib.rdc_batch_replica_grid(self._h, int(replica), _p(dims, C.c_int), C.byref(sh)))
+        return tuple(int(x) for x in dims), bool(sh.value)
+
     def get_particles(self, replica):
         n = int(self.n_particles()[replica])
         pos = np.zeros((n, 3)); t = np.zeros(n, np.int32); ids = np.zeros(n, np.uint64)

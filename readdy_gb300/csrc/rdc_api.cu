@@ -840,6 +840,15 @@ const char *rdc_last_error(void) { return g_err.c_str(); }
 int rdc_version(void) { return 1000; }
 const char *rdc_kernel_name(void) { return "CUDA"; }
 
+int rdc_set_device(int device) {
+    return guarded([&] {
+        int n = 0;
+        RDC_CUDA(cudaGetDeviceCount(&n));
+        require(device >= 0 && device < n, "device index out of range");
+        RDC_CUDA(cudaSetDevice(device));
+    });
+}
+
 int rdc_context_create(rdc_context **out, const double box[3], const int periodic[3], double kbt, int n_types,
                        const double *diffusion) {
     return guarded([&] {
@@ -1219,6 +1228,7 @@ int rdc_count_types(rdc_system *s, int64_t *counts) {
 
 namespace {
 // bit mask of the listed particle types (each in range)
+static_assert(MAX_TYPES <= 32, "type selections are 32-bit masks");
 uint32_t type_mask(const rdc_system *s, int n, const int *types) {
     uint32_t m = 0;
     for (int k = 0; k < n; ++k) {

@@ -171,7 +171,7 @@ struct rdc_batch {
             D.bin = bin + p; D.rank = rank + p; D.src = src + p; D.claim = claim + p; D.taken = taken + p;
             D.start = start + so[r];
             D.events = events + eo[r];
-            D.rx_counts = reaction_counts;
+            D.rx_counts = reaction_counts + (size_t)r * MAX_REACTIONS;
         }
         RDC_CUDA(cudaMemcpyAsync(desc_dev, desc.data(), sizeof(RepDesc) * R, cudaMemcpyHostToDevice, stream));
         invalidate_graph();
@@ -200,8 +200,9 @@ struct rdc_batch {
         claim = balloc<int>(total); taken = balloc<int>(total);
         RDC_CUDA(cudaMemsetAsync(claim, 0x7f, sizeof(int) * total, stream));
         RDC_CUDA(cudaMemsetAsync(taken, 0, sizeof(int) * total, stream));
-        reaction_counts = balloc<unsigned long long>(MAX_REACTIONS);
-        RDC_CUDA(cudaMemsetAsync(reaction_counts, 0, sizeof(unsigned long long) * MAX_REACTIONS, stream));
+        // performed events per replica and reaction (MAX_REACTIONS counters per replica)
+        reaction_counts = balloc<unsigned long long>((size_t)R * MAX_REACTIONS);
+        RDC_CUDA(cudaMemsetAsync(reaction_counts, 0, sizeof(unsigned long long) * MAX_REACTIONS * R, stream));
         particle_steps = balloc<unsigned long long>(1);
         RDC_CUDA(cudaMemsetAsync(particle_steps, 0, sizeof(unsigned long long), stream));
         count_dev = balloc<unsigned long long>((size_t)R * ctx.ntypes);
@@ -295,8 +296,10 @@ struct rdc_batch {
         sync();
     }
 
-    void check_status() {
-        auto st = states();
+    void check_status() { check_status(states()); }
+
+    // a device status raised by any replica becomes an error (and is cleared)
+    void check_status(std::vector<RepState> st) {
         int any = 0;
         for (auto &s : st) any |= s.status;
         if (any) {
@@ -412,7 +415,7 @@ void set_particles_impl(rdc_batch *b, const int64_t *n, const double *const *pos
     RDC_CUDA(cudaMemcpyAsync(offs_dev, offs.data(), sizeof(int64_t) * offs.size(), cudaMemcpyHostToDevice, b->stream));
     if (total > 0)
         RDC_CUDA(cudaMemcpyAsync(b->posB, packed.get(), sizeof(float4) * total, cudaMemcpyHostToDevice, b->stream));
-    k_unpack_replicas<<<std::min(R, 4 * 152), 256, 0, b->stream>>>(b->posB, offs_dev, offs_dev + R + 1, b->posA, R);
+    k_unpack_replicas<<<std::min(R, 4 * sm_count()), 256, 0, b->stream>>>(b->posB, offs_dev, offs_dev + R + 1, b->posA, R);
     RDC_CUDA(cudaGetLastError());
     RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, b->stream));
     b->set_order(std::vector<int64_t>(n, n + R));
@@ -513,6 +516,7 @@ int rdc_batch_particle_steps(rdc_batch *b, uint64_t *particle_steps) {
 int rdc_batch_count_types(rdc_batch *b, int64_t *counts) {
     BATCH_CALL({
         if (!b || !counts) throw std::invalid_argument("null argument");
+        b->check_status();
         launch_engine_count(b->e, b->R, b->ctx.ntypes, b->count_dev, b->stream);
         std::vector<unsigned long long> h((size_t)b->R * b->ctx.ntypes);
         RDC_CUDA(cudaMemcpyAsync(h.data(), b->count_dev, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost,
@@ -525,6 +529,7 @@ int rdc_batch_count_types(rdc_batch *b, int64_t *counts) {
 int rdc_batch_n_particles(rdc_batch *b, int64_t *n) {
     BATCH_CALL({
         if (!b || !n) throw std::invalid_argument("null argument");
+        b->check_status();
         // the per-type counts: a replica's storage may still hold the slots of removed particles
         const int T = b->ctx.ntypes;
         launch_engine_count(b->e, b->R, T, b->count_dev, b->stream);
@@ -546,6 +551,7 @@ int rdc_batch_get_particles(rdc_batch *b, int replica, int64_t cap, double *pos,
         if (!b) throw std::invalid_argument("null argument");
         if (replica < 0 || replica >= b->R) throw std::invalid_argument("replica out of range");
         auto st = b->states();
+        b->check_status(st);
         const RepState s = st[replica];
         const RepDesc &D = b->desc[replica];
         std::vector<float4> hp(s.n);
@@ -570,6 +576,70 @@ int rdc_batch_get_particles(rdc_batch *b, int replica, int64_t cap, double *pos,
         }
         if (n_out) *n_out = k;
         if (k > cap) throw rdc::CapacityError("output capacity too small for the particles");
+    });
+}
+
+int rdc_batch_get_forces(rdc_batch *b, int replica, int64_t cap, double *forces, uint64_t *ids, int64_t *n_out) {
+    BATCH_CALL({
+        if (!b) throw std::invalid_argument("null argument");
+        if (replica < 0 || replica >= b->R) throw std::invalid_argument("replica out of range");
+        auto st = b->states();
+        b->check_status(st);
+        const RepState s = st[replica];
+        const RepDesc &D = b->desc[replica];
+        std::vector<float4> hp(s.n), hf(s.n);
+        std::vector<uint32_t> hid(s.n);
+        if (s.n > 0) {
+            float4 *f = balloc<float4>(s.n);
+            struct Release {
+                float4 *&p;
+                ~Release() { bfree(p); }
+            } release{f};
+            launch_engine_forces(b->e, replica, s.n, f, b->stream);
+            RDC_CUDA(cudaGetLastError());
+            RDC_CUDA(cudaMemcpyAsync(hf.data(), f, sizeof(float4) * s.n, cudaMemcpyDeviceToHost, b->stream));
+            RDC_CUDA(cudaMemcpyAsync(hp.data(), D.pos[s.cur], sizeof(float4) * s.n, cudaMemcpyDeviceToHost, b->stream));
+            RDC_CUDA(cudaMemcpyAsync(hid.data(), D.id[s.cur], sizeof(uint32_t) * s.n, cudaMemcpyDeviceToHost,
+                                     b->stream));
+            b->sync();
+        }
+        int64_t k = 0;
+        for (int i = 0; i < s.n; ++i) {
+            int t;
+            std::memcpy(&t, &hp[i].w, 4);
+            if (t < 0) continue;
+            if (k < cap) {
+                if (forces) { forces[3 * k] = hf[i].x; forces[3 * k + 1] = hf[i].y; forces[3 * k + 2] = hf[i].z; }
+                if (ids) ids[k] = hid[i];
+            }
+            ++k;
+        }
+        if (n_out) *n_out = k;
+        if (k > cap) throw rdc::CapacityError("output capacity too small for the particles");
+    });
+}
+
+int rdc_batch_reaction_counts(rdc_batch *b, int n, int64_t *counts) {
+    BATCH_CALL({
+        if (!b || !counts) throw std::invalid_argument("null argument");
+        if (n < 0 || n > MAX_REACTIONS) throw std::invalid_argument("reaction count out of range");
+        b->check_status();
+        std::vector<unsigned long long> h((size_t)b->R * MAX_REACTIONS);
+        RDC_CUDA(cudaMemcpyAsync(h.data(), b->reaction_counts, sizeof(unsigned long long) * h.size(),
+                                 cudaMemcpyDeviceToHost, b->stream));
+        b->sync();
+        for (int r = 0; r < b->R; ++r)
+            for (int k = 0; k < n; ++k) counts[(size_t)r * n + k] = (int64_t)h[(size_t)r * MAX_REACTIONS + k];
+    });
+}
+
+int rdc_batch_replica_grid(rdc_batch *b, int replica, int *dims3, int *shared_cells) {
+    BATCH_CALL({
+        if (!b || !dims3) throw std::invalid_argument("null argument");
+        if (replica < 0 || replica >= b->R) throw std::invalid_argument("replica out of range");
+        const RepDesc &D = b->desc[replica];
+        for (int k = 0; k < 3; ++k) dims3[k] = D.geo.dims[k];
+        if (shared_cells) *shared_cells = D.smem_cells;
     });
 }
 

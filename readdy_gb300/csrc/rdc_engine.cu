@@ -860,6 +860,43 @@ __global__ void k_engine_count(EngineDev E, int R, int T, unsigned long long *ou
     }
 }
 
+// The force the next Euler update of replica r applies to each particle of its current state, in
+// storage order (fx, fy, fz, 0): the pair forces it carries from its last event walk where it carries
+// them, otherwise a pair walk over its sorted state (16-bit or int starts, as the replica keeps them
+// between steps), plus the order-1 potentials.  Removed particles get zero.
+template <typename C>
+__device__ inline void engine_forces_of(const RepDesc &D, const RepState &st, const Tables *tab, const C *start,
+                                        float4 *out) {
+    const GeoR g = geo_r(D.geo);
+    const float4 *pos = D.pos[st.cur];
+    const float4 *carried = (st.fvalid && D.force[st.cur]) ? D.force[st.cur] : nullptr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < st.n; i += gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        const int t = itype(p);
+        float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+        if (t >= 0) {
+            if (carried) {
+                const float4 f = carried[i];
+                fx = f.x; fy = f.y; fz = f.z;
+            } else if (i < st.n_in && tab->npots > 0) {
+                pair_force_at(i, p, pos, start, g, 1, tab->pair_tab, tab->pair_screen, tab->pots, tab->ntypes, fx, fy,
+                              fz, e);
+            }
+            const int o1 = tab->o1pot_tab[t];
+            if (o1) order1_force(p, tab->o1pots, o1 >> 8, o1 & 0xff, fx, fy, fz, e);
+        }
+        out[i] = make_float4(fx, fy, fz, 0.f);
+    }
+}
+
+__global__ void k_engine_forces(EngineDev E, int r, float4 *out) {
+    const RepDesc D = E.desc[r];
+    const RepState st = E.state[r];
+    const Tables *tab = E.tabs + D.table;
+    if (D.smem_cells) engine_forces_of(D, st, tab, reinterpret_cast<const uint16_t *>(D.start), out);
+    else engine_forces_of(D, st, tab, D.start, out);
+}
+
 // ---- host side ----------------------------------------------------------------------------------
 
 Geo replica_geo(const double box[3], const int pbc[3], double cutoff, double cell_scale, int64_t capacity,
@@ -875,6 +912,13 @@ Geo replica_geo(const double box[3], const int pbc[3], double cutoff, double cel
     smem_cells = (small && g.ncells + 3 <= SMEM_CELLS) ? 1 : 0;
     if (!smem_cells) g = make_geo(box, pbc, cutoff, 1, cutoff * cell_scale);
     return g;
+}
+
+int sm_count() {
+    int dev = 0, sms = 0;
+    RDC_CUDA(cudaGetDevice(&dev));
+    RDC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return std::max(1, sms);
 }
 
 int engine_grid(int threads, size_t smem) {
@@ -901,11 +945,15 @@ void launch_engine_step(const EngineDev &E, int blocks, int threads, size_t smem
 }
 
 void launch_engine_admit(const EngineDev &E, const int *list, int count, bool fill_ids, cudaStream_t st) {
-    if (count > 0) k_engine_admit<<<std::min(count, 4 * 152), 256, 0, st>>>(E, list, count, fill_ids ? 1 : 0);
+    if (count > 0) k_engine_admit<<<std::min(count, 4 * sm_count()), 256, 0, st>>>(E, list, count, fill_ids ? 1 : 0);
 }
 
 void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long long *out, cudaStream_t st) {
-    if (R > 0) k_engine_count<<<std::min(R, 4 * 152), 256, 0, st>>>(E, R, ntypes, out);
+    if (R > 0) k_engine_count<<<std::min(R, 4 * sm_count()), 256, 0, st>>>(E, R, ntypes, out);
+}
+
+void launch_engine_forces(const EngineDev &E, int r, int n, float4 *out, cudaStream_t st) {
+    if (n > 0) k_engine_forces<<<std::min((n + 255) / 256, 4 * sm_count()), 256, 0, st>>>(E, r, out);
 }
 
 }  // namespace rdc

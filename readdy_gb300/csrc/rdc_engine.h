@@ -100,5 +100,10 @@ void launch_engine_step(const EngineDev &E, int blocks, int threads, size_t smem
 void launch_engine_admit(const EngineDev &E, const int *list, int count, bool fill_ids, cudaStream_t st);
 // current per-type counts of replicas [0, R) into out (R x ntypes)
 void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long long *out, cudaStream_t st);
+// the force the next step applies to each of the n storage slots of replica r's current state (pair
+// forces carried or walked, plus order-1 potentials) into out (float4 per slot, removed slots zero)
+void launch_engine_forces(const EngineDev &E, int r, int n, float4 *out, cudaStream_t st);
+// multiprocessors of the current device
+int sm_count();
 
 }  // namespace rdc

@@ -296,7 +296,7 @@ def _compare_forces(rg, spec, pos, types, label):
     p, t, ids2 = k.get_particles()
     (f_gpu,) = by_id(ids, f_gpu)
     (p, t) = by_id(ids2, p, t)
-    o = make_oracle(spec, n_threads=4)
+    o = make_oracle(spec, n_threads=8)
     o.add_particles(p, t)
     o.nl_setup(o.calculate_max_cutoff())
     e_ref = o.calculate_forces()
@@ -310,11 +310,13 @@ def _compare_forces(rg, spec, pos, types, label):
     return err, e_gpu, e_ref
 
 
+@pytest.mark.parametrize("n", [20000, 200000], ids=["20k", "200k"])
 @pytest.mark.parametrize("which", ["lennard_jones", "weak_interaction_piecewise_harmonic", "harmonic_repulsion",
                                    "all"])
-def test_forces_match_oracle_crowded(rg, which):
-    """The crowded three-species chemistry at 20k particles, per potential type and combined."""
-    spec, pos, types = crowded_spec(n=20000, density=0.2, seed=4)
+def test_forces_match_oracle_crowded(rg, which, n):
+    """The crowded three-species chemistry, per potential type and combined: at 20k particles and at the
+    full 200k-particle size (100^3 box, density 0.2)."""
+    spec, pos, types = crowded_spec(n=n, density=0.2, seed=4)
     if which != "all":
         spec["potentials"] = [p for p in spec["potentials"] if p[0] == which]
     spec["reactions"] = []
@@ -543,11 +545,45 @@ def test_batch_flat_upload_equals_list_upload(rg):
         b1.set_particles(poss, bad)
 
 
+POLYMER_SIZES = {
+    # 200 chains of 50 beads in 10k solvent, 30^3 box
+    "small": dict(n_chains=200, chain_len=50, n_solvent=10000, box=30.0),
+    # the full polymer workload: 2000 chains of 50 beads in 100k solvent, 120^3 box
+    "full": dict(n_chains=2000, chain_len=50, n_solvent=100000, box=120.0),
+}
+
+
+def dihedral_near_zero_force_switch(pos, quads, box, band=2e-6):
+    """Per particle: whether it belongs to a dihedral whose FP64 |cos phi| (the reference's m.n / (|m||n|),
+    TorsionPotential.cpp:80-93) lies within `band` of the 1e-4 below which the reference sets the force
+    to zero, so that FP32 rounding may put it on either side."""
+    L = np.asarray(box, float)
+
+    def d(a, b):  # minimum image b - a
+        v = pos[b] - pos[a]
+        return v - L * np.round(v / L)
+
+    x_ji = d(quads[:, 1], quads[:, 0])
+    x_kj = d(quads[:, 2], quads[:, 1])
+    x_kl = d(quads[:, 2], quads[:, 3])
+    m = np.cross(x_ji, x_kj)
+    n = np.cross(x_kl, -x_kj)
+    mm = np.maximum((m * m).sum(1), 1e-4)
+    nn = np.maximum((n * n).sum(1), 1e-4)
+    cos_phi = (m * n).sum(1) / np.maximum(np.sqrt(mm) * np.sqrt(nn), 1e-4)
+    near = np.abs(np.abs(cos_phi) - 1e-4) < band
+    flag = np.zeros(len(pos), bool)
+    flag[quads[near].ravel()] = True
+    return flag
+
+
+@pytest.mark.parametrize("size", list(POLYMER_SIZES))
 @pytest.mark.parametrize("terms", ["bond", "angle", "dihedral", "all"])
-def test_polymer_forces_match_oracle(rg, terms):
-    """Random-walk chains (step 1.0) with bond/angle/dihedral terms in solvent, per term type."""
+def test_polymer_forces_match_oracle(rg, terms, size):
+    """Random-walk chains (step 1.0) with bond/angle/dihedral terms in solvent, per term type, at a small
+    size and at the full polymer-in-solvent size."""
     from tests.helpers import polymer_spec
-    spec, chains, solvent = polymer_spec(n_chains=200, chain_len=50, n_solvent=10000, box=30.0, seed=6)
+    spec, chains, solvent = polymer_spec(**POLYMER_SIZES[size], seed=6)
     use = {"bond", "angle", "dihedral"} if terms == "all" else {terms}
     ctx = make_context(dict(spec, potentials=spec["potentials"] if terms == "all" else []))
     ctx.configure_harmonic_bond(0, 0, spec["bond"]["k"] if "bond" in use else 0.0, spec["bond"]["l0"])
@@ -567,7 +603,7 @@ def test_polymer_forces_match_oracle(rg, terms):
     p, t, ids2 = k.get_particles()
     (f_gpu,) = by_id(ids, f_gpu)
     (p, t) = by_id(ids2, p, t)
-    o = make_oracle(dict(spec, potentials=spec["potentials"] if terms == "all" else []), n_threads=4)
+    o = make_oracle(dict(spec, potentials=spec["potentials"] if terms == "all" else []), n_threads=8)
     o.add_particles(p, t)
     nb = len(chains) * L
     idx = np.arange(nb).reshape(len(chains), L)
@@ -577,10 +613,10 @@ def test_polymer_forces_match_oracle(rg, terms):
     if "angle" in use:
         o.add_harmonic_angles(np.stack([idx[:, :-2].ravel(), idx[:, 1:-1].ravel(), idx[:, 2:].ravel()], 1),
                               spec["angle"]["k"], spec["angle"]["theta0"])
+    quads = np.stack([idx[:, :-3].ravel(), idx[:, 1:-2].ravel(), idx[:, 2:-1].ravel(), idx[:, 3:].ravel()], 1)
     if "dihedral" in use:
         d = spec["dihedral"]
-        o.add_cosine_dihedrals(np.stack([idx[:, :-3].ravel(), idx[:, 1:-2].ravel(), idx[:, 2:-1].ravel(),
-                                         idx[:, 3:].ravel()], 1), d["k"], d["n"], d["phi0"])
+        o.add_cosine_dihedrals(quads, d["k"], d["n"], d["phi0"])
     o.nl_setup(1.0)
     e_ref = o.calculate_forces()
     _, _, oid, f_ref, _ = o.particles()
@@ -590,10 +626,15 @@ def test_polymer_forces_match_oracle(rg, terms):
     e_gpu = k.energy
     print(f"polymer {terms}: max err (floored) {err.max():.3e} p99.9 {np.quantile(err, .999):.3e} "
           f"well-conditioned max {rel_good.max():.3e}; energy {e_gpu:.9g} vs {e_ref:.9g}")
-    # dihedral terms within FP32 noise of the |cos phi| < 1e-4 zero-force threshold
-    # (TorsionPotential.cpp:91-93) are reported, not hidden: at most a handful of particles
+    # a particle above the tolerance must sit on a dihedral within FP32 rounding of the |cos phi| < 1e-4
+    # zero-force switch (TorsionPotential.cpp:91-93); any other is a failure
     bad = err > FORCE_RTOL
-    assert bad.sum() <= (3 if "dihedral" in use else 0), np.sort(err)[-8:]
+    if bad.any():
+        assert "dihedral" in use, np.sort(err)[-8:]
+        excused = dihedral_near_zero_force_switch(p[:nb], quads, spec["box"])
+        excused = np.concatenate([excused, np.zeros(len(err) - nb, bool)])
+        print(f"{bad.sum()} particles above tolerance, all on dihedrals at the zero-force switch")
+        assert np.all(excused[bad]), (np.flatnonzero(bad & ~excused), err[bad & ~excused])
     assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
 
 
