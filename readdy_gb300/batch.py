@@ -139,7 +139,7 @@ class ReplicaBatch:
         return pos[:got.value], t[:got.value], ids[:got.value]
 
 
-def autotune(make_batch, steps=20, scales=(1.0, 1.5, 2.0), threads=(256, 512), handler=N.GILLESPIE, dt=1e-3):
+def autotune(make_batch, steps=20, scales=(1.0, 1.5, 2.0), threads=(512, 768), handler=N.GILLESPIE, dt=1e-3):
     """Times short runs of freshly made batches over cell width scale x threads per block and returns
     the fastest setting as a dict.  `make_batch()` must return a batch with its particles set."""
     best = None
@@ -159,7 +159,7 @@ def autotune(make_batch, steps=20, scales=(1.0, 1.5, 2.0), threads=(256, 512), h
     return best
 
 
-def autotune_inplace(batch: ReplicaBatch, scales=(1.0, 1.15, 1.3), threads=(256, 384, 512), steps=5,
+def autotune_inplace(batch: ReplicaBatch, scales=(1.0, 1.15, 1.3), threads=(512, 640, 768), steps=5,
                      handler=N.GILLESPIE, dt=1e-3):
     """Autotunes a batch on its own replicas: for every cell width scale x threads per block it
     reconfigures the batch, runs two untimed steps and `steps` steps timed with CUDA events on the

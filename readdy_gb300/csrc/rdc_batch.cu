@@ -457,7 +457,8 @@ int rdc_batch_configure(rdc_batch *b, int handler, double dt, double cell_width_
         if (!(cell_width_scale >= 1.0 && cell_width_scale <= 8.0))
             throw std::invalid_argument("cell width scale must be in [1, 8]");
         if (threads_per_block < 64 || threads_per_block > ENGINE_THREADS_MAX || threads_per_block % 32)
-            throw std::invalid_argument("threads per block must be a multiple of 32 in [64, 512]");
+            throw std::invalid_argument("threads per block must be a multiple of 32 in [64, " +
+                                        std::to_string(ENGINE_THREADS_MAX) + "]");
         b->handler = handler;
         b->e.handler = handler;
         b->dt = dt;

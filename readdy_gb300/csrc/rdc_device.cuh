@@ -99,6 +99,7 @@ __device__ inline float mi_diff(float rhs, float lhs, float L, float hL, int pbc
 // so (double)L is the FP64 box of the reference)
 struct GeoR {
     float L[3], hL[3], invW[3], invL[3];
+    float W[3], M[3];  // cell widths, and the rounding margins of distance bounds to neighbour cells
     int dims[3];
     int pbc[3];
     int exact_always;
@@ -114,9 +115,22 @@ __device__ inline GeoR geo_r(const Geo &g) {
         r.invL[d] = 1.0f / g.L[d];
         r.dims[d] = g.dims[d];
         r.pbc[d] = g.pbc[d];
+        r.W[d] = g.L[d] / (float)g.dims[d];
+        r.M[d] = r.W[d] * (1e-4f + 4e-7f * (float)g.dims[d]);
     }
     r.exact_always = g.exact_always;
     return r;
+}
+
+// cell width along axis d and the margin that covers the rounding of a particle's offset inside its cell
+// (precomputed once per system in GeoR; computed on the spot from a Geo)
+__device__ inline void cell_width_margin(const GeoR &g, int d, float &w, float &m) {
+    w = g.W[d];
+    m = g.M[d];
+}
+__device__ inline void cell_width_margin(const Geo &g, int d, float &w, float &m) {
+    w = g.L[d] / (float)g.dims[d];
+    m = w * (1e-4f + 4e-7f * (float)g.dims[d]);
 }
 
 // result of the FP64 pair predicate: the rounded FP64 difference and whether d^2 < c^2

@@ -249,6 +249,17 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    // per type: the largest force or reaction screen, as far as the walk of a particle of that type reaches
+    __shared__ float sh_reach[MAX_TYPES];
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        float r2 = 0.f;
+        for (int u = 0; u < T; ++u) {
+            if (S.tab[t * T + u]) r2 = fmaxf(r2, S.screen[t * T + u]);
+            if (rt.o2_any[t] && rt.o2_tab[t * rt.T + u]) r2 = fmaxf(r2, rt.screen[t * rt.T + u]);
+        }
+        sh_reach[t] = r2;
+    }
+    __syncthreads();
     for (;;) {
         int base = 0;
         if (lane == 0) base = atomicAdd(next, 32);
@@ -265,12 +276,9 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
             if (i < n_in && (pairs || pair_pots)) {
                 const int *rrow = rt.o2_tab + ti * rt.T;
                 const float *rsrow = rt.screen + ti * rt.T;
-                // the cells walked reach as far as the largest force or reaction screen of i's type
-                float reach2 = 0.f;
-                for (int t = 0; t < T; ++t) {
-                    if (S.tab[ti * T + t]) reach2 = fmaxf(reach2, S.screen[ti * T + t]);
-                    if (pairs && rrow[t]) reach2 = fmaxf(reach2, rsrow[t]);
-                }
+                // the cells walked reach as far as the largest force or reaction screen of i's type (a walking
+                // particle is inside the cells, so its type's reaction screens count when it has any)
+                const float reach2 = sh_reach[ti];
                 auto partner = [&](int j, float4 q, int tj, float d2s) {
                     if (!pairs || j < i) return;
                     const int o2 = rrow[tj];

@@ -40,8 +40,13 @@ namespace rdc {
 #ifndef RDC_ENGINE_MAX_EVENTS_SM
 #define RDC_ENGINE_MAX_EVENTS_SM 1024
 #endif
+// The launch bound of the fused step, which also caps its registers (65536 / 768 -> 80 per thread).
+// Measured on the 4096-replica ensemble (one CTA per SM, the shared-memory cell array above): 4.88 ms
+// per step at 512 threads and 128 registers, 4.33 ms at 640 threads and 96 registers, 4.02 ms at 768
+// and 80 (84 bytes of spills), 4.03 ms at 896 and 72 (596 bytes of spills).  The walk phases are bound
+// by the latency of dependent loads and arithmetic; more warps per SM hide more of it.
 #ifndef RDC_ENGINE_THREADS_MAX
-#define RDC_ENGINE_THREADS_MAX 512
+#define RDC_ENGINE_THREADS_MAX 768
 #endif
 constexpr int SMEM_CELLS = RDC_ENGINE_SMEM_CELLS;
 constexpr int ENGINE_THREADS_MAX = RDC_ENGINE_THREADS_MAX;

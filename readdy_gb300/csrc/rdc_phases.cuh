@@ -101,9 +101,9 @@ __device__ inline void for_each_neighbor_range(float4 p, const G &g, const S *__
             const int cc[3] = {cx, cy, cz};
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const float w = g.L[d] / (float)g.dims[d];
+                float w, m;
+                cell_width_margin(g, d, w, m);
                 const float u = (pc[d] + g.hL[d]) - (float)cc[d] * w;
-                const float m = w * (1e-4f + 4e-7f * (float)g.dims[d]);
                 lo[d] = fmaxf(u - m, 0.f);
                 hi[d] = fmaxf(w - u - m, 0.f);
             }
