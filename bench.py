@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--single-systems", type=int, default=1, help="time the three single-system workloads (0: skip)")
     ap.add_argument("--plain-threshold", type=int, default=4096,
                     help="requests above this many particles take the per-system leg of the server")
+    ap.add_argument("--profile-system", choices=["abc_2k", "crowded_200k", "polymer_200k"], default=None,
+                    help="only run one single-system workload through the per-system path (--warmup then "
+                         "--steps steps; for profiler captures of its kernels)")
     return ap.parse_args()
 
 
@@ -330,6 +333,23 @@ def single_systems(gpu_steps=200, cpu_steps=3):
     return out
 
 
+def profile_system(name, warmup, steps):
+    """One single-system workload through rdc_run: `warmup` steps, then `steps` steps timed by wall
+    clock (the command that profiler captures of the per-system kernels run)."""
+    import readdy_gb300 as rg
+    w = single_system(name)
+    h = rg.GILLESPIE if w["handler"] == "gillespie" else rg.UNCONTROLLED_APPROXIMATION
+    k = _gpu_system(w, seed=3)
+    k.run(warmup, w["dt"], handler=h)
+    k.synchronize()
+    t0 = time.perf_counter()
+    k.run(steps, w["dt"], handler=h)
+    k.synchronize()
+    dt = (time.perf_counter() - t0) / max(steps, 1)
+    n = len(w["pos"]) + (sum(len(c) for c in w["chains"]) if w["chains"] is not None else 0)
+    return {"profile_system": name, "particles": int(n), "steps": steps, "ms_per_step": dt * 1e3}
+
+
 def serving(n_requests, time_limit, plain_threshold, seed=7):
     """The served form on the first n_requests of the seeded serving stream (Poisson arrivals at 20/s;
     2-6 species; N log-uniform in [500, 200000] at density 0.1-0.5; 1k-100k steps; counts every 100
@@ -547,6 +567,10 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)
+        return
+    if args.profile_system:
+        if rank == 0:
+            print(json.dumps(profile_system(args.profile_system, args.warmup, args.steps)), flush=True)
         return
     if world > 1:
         # the library creates its streams and buffers on the rank's own GPU

@@ -1,0 +1,692 @@
+// The "CUDA" kernel plugin: each ReaDDy interface method is one call into the C ABI of
+// libreaddy_cuda_core.so.  Declarations and the build/installation notes are in CUDAKernel.h.
+#include "CUDAKernel.h"
+
+#include <readdy/model/potentials/PotentialsOrder1.h>
+#include <readdy/model/potentials/PotentialsOrder2.h>
+#include <readdy/model/reactions/Reaction.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <random>
+#include <set>
+#include <stdexcept>
+#include <unordered_map>
+
+namespace readdy::kernel::cuda {
+
+void check(int rc) {
+    if (rc == RDC_OK) return;
+    const std::string m = rdc_last_error();
+    if (rc == RDC_ERR_INVALID_ARGUMENT) throw std::invalid_argument(m);
+    if (rc == RDC_ERR_LOGIC) throw std::logic_error(m);
+    throw std::runtime_error(m);
+}
+
+namespace {
+
+namespace pot = model::potentials;
+
+// Most of ReaDDy's pair and order-1 potential classes keep their parameters as protected members with no
+// getters (PotentialsOrder1.h:97-209, PotentialsOrder2.h:54-323).  A class derived from a potential may
+// name them, and the pointers-to-member it forms apply to any object of the potential's class, so the
+// plugin reads them without a change to ReaDDy's headers.
+struct HRAccess : pot::HarmonicRepulsion {
+    static constexpr auto forceConstant = &HRAccess::_forceConstant;
+    static constexpr auto distance = &HRAccess::_interactionDistance;
+};
+struct WIPHAccess : pot::WeakInteractionPiecewiseHarmonic {
+    static constexpr auto forceConstant = &WIPHAccess::forceConstant;
+};
+struct LJAccess : pot::LennardJones {
+    static constexpr auto m = &LJAccess::m;
+    static constexpr auto n = &LJAccess::n;
+    static constexpr auto cutoff = &LJAccess::cutoffDistance;
+    static constexpr auto shift = &LJAccess::shift;
+    static constexpr auto epsilon = &LJAccess::epsilon;
+    static constexpr auto sigma = &LJAccess::sigma;
+};
+struct SEAccess : pot::ScreenedElectrostatics {
+    static constexpr auto strength = &SEAccess::electrostaticStrength;
+    static constexpr auto inverseDepth = &SEAccess::inverseScreeningDepth;
+    static constexpr auto repulsion = &SEAccess::repulsionStrength;
+    static constexpr auto repulsionDistance = &SEAccess::repulsionDistance;
+    static constexpr auto exponent = &SEAccess::exponent;
+    static constexpr auto cutoff = &SEAccess::cutoff;
+};
+struct BarrierAccess : pot::SphericalBarrier {
+    static constexpr auto origin = &BarrierAccess::origin;
+    static constexpr auto radius = &BarrierAccess::radius;
+    static constexpr auto height = &BarrierAccess::height;
+    static constexpr auto width = &BarrierAccess::width;
+};
+template <bool inclusion>
+struct CylinderAccess : pot::Cylinder<inclusion> {
+    static constexpr auto origin = &CylinderAccess::origin;
+    static constexpr auto normal = &CylinderAccess::normal;
+    static constexpr auto forceConstant = &CylinderAccess::forceConstant;
+    static constexpr auto radius = &CylinderAccess::radius;
+};
+
+// The weak-interaction potential's distances live in a Configuration whose fields only the potential
+// itself may read.  Its describe() prints them with {fmt}'s shortest round-trip form, so parsing the
+// printed value gives back the exact double (readdy/main/model/potentials/Potentials.cpp:139-144).
+double describedValue(const std::string &text, const std::string &label) {
+    const auto at = text.find(label);
+    if (at == std::string::npos) throw std::invalid_argument("CUDA kernel: cannot read '" + label + "' of: " + text);
+    return std::strtod(text.c_str() + at + label.size(), nullptr);
+}
+
+void addPairPotential(rdc_context *c, const pot::PotentialOrder2 *p) {
+    const int t1 = (int)p->particleType1(), t2 = (int)p->particleType2();
+    if (auto *hr = dynamic_cast<const pot::HarmonicRepulsion *>(p)) {
+        check(rdc_context_add_harmonic_repulsion(c, t1, t2, hr->*HRAccess::forceConstant, hr->*HRAccess::distance));
+    } else if (auto *w = dynamic_cast<const pot::WeakInteractionPiecewiseHarmonic *>(p)) {
+        // classified by its class, not by type(), which returns "HarmonicRepulsion" (Potentials.cpp:146-148)
+        const std::string d = w->describe();
+        check(rdc_context_add_weak_interaction_piecewise_harmonic(c, t1, t2, w->*WIPHAccess::forceConstant,
+                                                                  describedValue(d, "desired distance="),
+                                                                  describedValue(d, "depth="),
+                                                                  describedValue(d, "cutoff=")));
+    } else if (auto *lj = dynamic_cast<const pot::LennardJones *>(p)) {
+        check(rdc_context_add_lennard_jones(c, t1, t2, (unsigned)(lj->*LJAccess::m), (unsigned)(lj->*LJAccess::n),
+                                            lj->*LJAccess::cutoff, lj->*LJAccess::shift ? 1 : 0,
+                                            lj->*LJAccess::epsilon, lj->*LJAccess::sigma));
+    } else if (auto *se = dynamic_cast<const pot::ScreenedElectrostatics *>(p)) {
+        check(rdc_context_add_screened_electrostatics(c, t1, t2, se->*SEAccess::strength, se->*SEAccess::inverseDepth,
+                                                      se->*SEAccess::repulsion, se->*SEAccess::repulsionDistance,
+                                                      (unsigned)(se->*SEAccess::exponent), se->*SEAccess::cutoff));
+    } else {
+        throw std::invalid_argument("CUDA kernel: unsupported order-2 potential: " + p->describe());
+    }
+}
+
+template <bool inclusion>
+bool addGeometryPotential(rdc_context *c, int t, const pot::PotentialOrder1 *p) {
+    using BoxG = model::geometry::Box<scalar>;
+    using SphereG = model::geometry::Sphere<scalar>;
+    using CapsuleG = model::geometry::Capsule<scalar>;
+    if (auto *b = dynamic_cast<const pot::HarmonicGeometryPotential<BoxG, inclusion> *>(p)) {
+        const auto &g = b->geometry();
+        const double origin[3] = {g.v0[0], g.v0[1], g.v0[2]};
+        const double extent[3] = {g.v1[0] - g.v0[0], g.v1[1] - g.v0[1], g.v1[2] - g.v0[2]};
+        check(rdc_context_add_box(c, t, b->forceConstant(), origin, extent, inclusion));
+        return true;
+    }
+    if (auto *s = dynamic_cast<const pot::HarmonicGeometryPotential<SphereG, inclusion> *>(p)) {
+        const auto &g = s->geometry();
+        const double centre[3] = {g.center[0], g.center[1], g.center[2]};
+        check(rdc_context_add_sphere(c, t, s->forceConstant(), centre, g.radius,
+                                     inclusion));
+        return true;
+    }
+    if (auto *k = dynamic_cast<const pot::HarmonicGeometryPotential<CapsuleG, inclusion> *>(p)) {
+        const auto &g = k->geometry();
+        const double centre[3] = {g.center[0], g.center[1], g.center[2]};
+        const double dir[3] = {g.direction[0], g.direction[1], g.direction[2]};
+        check(rdc_context_add_capsule(c, t, k->forceConstant(), centre, dir,
+                                      g.length, g.radius, inclusion));
+        return true;
+    }
+    if (auto *y = dynamic_cast<const pot::Cylinder<inclusion> *>(p)) {
+        const Vec3 &o = y->*CylinderAccess<inclusion>::origin, &nrm = y->*CylinderAccess<inclusion>::normal;
+        const double origin[3] = {o[0], o[1], o[2]}, normal[3] = {nrm[0], nrm[1], nrm[2]};
+        check(rdc_context_add_cylinder(c, t, y->*CylinderAccess<inclusion>::forceConstant, origin, normal,
+                                       y->*CylinderAccess<inclusion>::radius, inclusion));
+        return true;
+    }
+    return false;
+}
+
+void addExternalPotential(rdc_context *c, const pot::PotentialOrder1 *p) {
+    const int t = (int)p->particleType();
+    if (addGeometryPotential<true>(c, t, p) || addGeometryPotential<false>(c, t, p)) return;
+    if (auto *b = dynamic_cast<const pot::SphericalBarrier *>(p)) {
+        const Vec3 &o = b->*BarrierAccess::origin;
+        const double origin[3] = {o[0], o[1], o[2]};
+        check(rdc_context_add_spherical_barrier(c, t, b->*BarrierAccess::height, b->*BarrierAccess::width, origin,
+                                                b->*BarrierAccess::radius));
+        return;
+    }
+    throw std::invalid_argument("CUDA kernel: unsupported order-1 potential: " + p->describe());
+}
+
+void addReaction(rdc_context *c, const model::reactions::Reaction *r, std::vector<int> &rx) {
+    using RT = model::reactions::ReactionType;
+    const auto &e = r->educts();
+    const auto &p = r->products();
+    int id = -1;
+    switch (r->type()) {
+        case RT::Conversion: check(rdc_context_add_conversion(c, (int)e[0], (int)p[0], r->rate(), &id)); break;
+        case RT::Decay: check(rdc_context_add_decay(c, (int)e[0], r->rate(), &id)); break;
+        case RT::Fusion:
+            check(rdc_context_add_fusion(c, (int)e[0], (int)e[1], (int)p[0], r->rate(), r->eductDistance(),
+                                         r->weight1(), r->weight2(), &id));
+            break;
+        case RT::Fission:
+            check(rdc_context_add_fission(c, (int)e[0], (int)p[0], (int)p[1], r->rate(), r->productDistance(),
+                                          r->weight1(), r->weight2(), &id));
+            break;
+        case RT::Enzymatic:  // educts (from, catalyst), products (to, catalyst) (reactions/Enzymatic.h:53-65)
+            check(rdc_context_add_enzymatic(c, (int)e[1], (int)e[0], (int)p[0], r->rate(), r->eductDistance(), &id));
+            break;
+    }
+    if (rx.size() <= r->id()) rx.resize(r->id() + 1, -1);
+    rx[r->id()] = id;
+}
+
+// the seed of the device's random streams: READDY_CUDA_SEED when set, otherwise a random device draw
+uint64_t seedFromEnvironment() {
+    if (const char *s = std::getenv("READDY_CUDA_SEED")) return std::strtoull(s, nullptr, 10);
+    std::random_device rd;
+    return ((uint64_t)rd() << 32) ^ rd();
+}
+
+std::vector<ParticleTypeId> typeIds(const model::Context &ctx, const std::vector<std::string> &names) {
+    std::vector<ParticleTypeId> ids;
+    for (const auto &n : names) ids.push_back(ctx.particleTypes().idOf(n));
+    return ids;
+}
+
+}  // namespace
+
+rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx) {
+    const auto &types = ctx.particleTypes();
+    ParticleTypeId maxId = 0;
+    for (const auto &[name, id] : types.typeMapping()) maxId = std::max(maxId, id);
+    std::vector<double> D(types.nTypes() == 0 ? 1 : (std::size_t)maxId + 1, 0.0);
+    for (const auto &[name, id] : types.typeMapping()) D[id] = types.infoOf(id).diffusionConstant;  // ParticleTypeRegistry.h:128-133
+    const auto &box = ctx.boxSize();
+    const auto &pbc = ctx.periodicBoundaryConditions();
+    const double b[3] = {box[0], box[1], box[2]};
+    const int p[3] = {pbc[0] ? 1 : 0, pbc[1] ? 1 : 0, pbc[2] ? 1 : 0};
+    rdc_context *c = nullptr;
+    check(rdc_context_create(&c, b, p, ctx.kBT(), (int)D.size(), D.data()));
+    try {
+        // each unordered type pair once: the registry files a pair's potentials under both orders
+        std::set<const pot::PotentialOrder2 *> seen;
+        for (const auto &[key, pots] : ctx.potentials().potentialsOrder2())
+            for (const auto *q : pots)
+                if (seen.insert(q).second) addPairPotential(c, q);
+        for (const auto &[type, pots] : ctx.potentials().potentialsOrder1())
+            for (const auto *q : pots) addExternalPotential(c, q);
+        rx.clear();
+        for (const auto *r : ctx.reactions().order1Flat()) addReaction(c, r, rx);
+        for (const auto *r : ctx.reactions().order2Flat()) addReaction(c, r, rx);
+        // bonded terms of static topologies: TopologyRegistry::potentialConfiguration (PotentialConfiguration.h:136-161)
+        const auto &pc = ctx.topologyRegistry().potentialConfiguration();
+        for (const auto &[key, bonds] : pc.pairPotentials)
+            for (const auto &bd : bonds)
+                check(rdc_context_configure_harmonic_bond(c, (int)std::get<0>(key), (int)std::get<1>(key),
+                                                          bd.forceConstant, bd.length));
+        for (const auto &[key, angles] : pc.anglePotentials)
+            for (const auto &a : angles)
+                check(rdc_context_configure_harmonic_angle(c, (int)std::get<0>(key), (int)std::get<1>(key),
+                                                           (int)std::get<2>(key), a.forceConstant, a.equilibriumAngle));
+        for (const auto &[key, torsions] : pc.torsionPotentials)
+            for (const auto &d : torsions)
+                check(rdc_context_configure_cosine_dihedral(c, (int)std::get<0>(key), (int)std::get<1>(key),
+                                                            (int)std::get<2>(key), (int)std::get<3>(key),
+                                                            d.forceConstant, d.multiplicity, d.phi_0));
+        check(rdc_context_set_record_virial(c, ctx.recordVirial() ? 1 : 0));  // Context.h:168-174
+    } catch (...) {
+        rdc_context_destroy(c);
+        throw;
+    }
+    return c;
+}
+
+// ---- state model ------------------------------------------------------------------------------------
+
+namespace {
+struct HostParticles {
+    std::vector<double> pos;
+    std::vector<int> types;
+    std::vector<uint64_t> ids;
+};
+HostParticles fetch(rdc_system *s) {
+    HostParticles h;
+    if (!s) return h;
+    int64_t n = 0;
+    check(rdc_get_n_particles(s, &n));
+    h.pos.resize(3 * (std::size_t)n);
+    h.types.resize((std::size_t)n);
+    h.ids.resize((std::size_t)n);
+    int64_t got = 0;
+    check(rdc_get_particles(s, n, h.pos.data(), h.types.data(), h.ids.data(), &got));
+    h.pos.resize(3 * (std::size_t)got);
+    h.types.resize((std::size_t)got);
+    h.ids.resize((std::size_t)got);
+    return h;
+}
+}  // namespace
+
+std::vector<Vec3> CUDAStateModel::getParticlePositions() const {
+    const auto h = fetch(_kernel->sysIfCreated());
+    std::vector<Vec3> out;
+    for (std::size_t i = 0; i < h.types.size(); ++i) out.emplace_back(h.pos[3 * i], h.pos[3 * i + 1], h.pos[3 * i + 2]);
+    return out;
+}
+
+std::vector<model::Particle> CUDAStateModel::getParticles() const {
+    const auto h = fetch(_kernel->sysIfCreated());
+    std::vector<model::Particle> out;
+    for (std::size_t i = 0; i < h.types.size(); ++i)
+        out.emplace_back(Vec3(h.pos[3 * i], h.pos[3 * i + 1], h.pos[3 * i + 2]), (ParticleTypeId)h.types[i],
+                         (ParticleId)h.ids[i]);
+    return out;
+}
+
+// the particle whose device id is `index` (topology vertices hold device ids as their particle index)
+model::Particle CUDAStateModel::getParticleForIndex(std::size_t index) const {
+    for (const auto &p : getParticles())
+        if (p.id() == index) return p;
+    throw std::out_of_range("CUDA kernel: no particle with index " + std::to_string(index));
+}
+
+ParticleTypeId CUDAStateModel::getParticleType(std::size_t index) const { return getParticleForIndex(index).type(); }
+
+void CUDAStateModel::initializeNeighborList(scalar cutoff) { check(rdc_nl_create(_kernel->sys(), cutoff)); }
+void CUDAStateModel::updateNeighborList() { check(rdc_nl_update(_kernel->sys())); }
+void CUDAStateModel::clearNeighborList() { check(rdc_nl_clear(_kernel->sys())); }
+
+void CUDAStateModel::addParticles(const std::vector<model::Particle> &ps) {
+    std::vector<double> x(3 * ps.size());
+    std::vector<int> t(ps.size());
+    for (std::size_t i = 0; i < ps.size(); ++i) {
+        for (int d = 0; d < 3; ++d) x[3 * i + d] = ps[i].pos()[d];
+        t[i] = (int)ps[i].type();
+    }
+    check(rdc_add_particles(_kernel->sys(), (int64_t)ps.size(), x.data(), t.data(), nullptr));
+}
+
+model::top::GraphTopology *const CUDAStateModel::addTopology(TopologyTypeId type,
+                                                            const std::vector<model::Particle> &particles) {
+    model::top::Graph graph;
+    for (std::size_t i = 0; i < particles.size(); ++i) graph.addVertex(model::top::VertexData{i});
+    auto top = std::make_unique<model::top::GraphTopology>(type, std::move(graph), _kernel->context(), this);
+    auto *raw = top.get();
+    _pending.push_back(PendingTopology{std::move(top), particles});
+    return raw;
+}
+
+void CUDAStateModel::flushTopologies() {
+    if (_pending.empty()) return;
+    rdc_system *s = _kernel->sysIfCreated();
+    if (!s) return;
+    for (auto &pt : _pending) {
+        auto &g = pt.top->graph();
+        const auto n = pt.particles.size();
+        std::vector<double> x(3 * n);
+        std::vector<int> t(n);
+        for (std::size_t i = 0; i < n; ++i) {
+            for (int d = 0; d < 3; ++d) x[3 * i + d] = pt.particles[i].pos()[d];
+            t[i] = (int)pt.particles[i].type();
+        }
+        // edges by the vertices' local particle indices (the position in the list given to addTopology)
+        std::vector<int64_t> edges;
+        for (const auto &[v1, v2] : g.edges()) {
+            edges.push_back((int64_t)g.vertices().at(v1)->particleIndex);
+            edges.push_back((int64_t)g.vertices().at(v2)->particleIndex);
+        }
+        std::vector<uint64_t> ids(n);
+        check(rdc_add_topology(s, (int64_t)n, x.data(), t.data(), (int64_t)(edges.size() / 2), edges.data(), ids.data()));
+        // from now on a vertex refers to its particle by the device id
+        model::top::Graph relabelled;
+        std::unordered_map<std::size_t, std::size_t> local;
+        for (std::size_t i = 0; i < n; ++i) relabelled.addVertex(model::top::VertexData{(std::size_t)ids[i]});
+        for (const auto &[v1, v2] : g.edges())
+            relabelled.addEdge(relabelled.vertices().begin_persistent() + g.vertices().at(v1)->particleIndex,
+                               relabelled.vertices().begin_persistent() + g.vertices().at(v2)->particleIndex);
+        pt.top->setGraph(std::move(relabelled));
+        _topologies.push_back(std::move(pt.top));
+    }
+    _pending.clear();
+}
+
+std::vector<model::top::GraphTopology *> CUDAStateModel::getTopologies() {
+    std::vector<model::top::GraphTopology *> out;
+    for (auto &t : _topologies) out.push_back(t.get());
+    for (auto &p : _pending) out.push_back(p.top.get());
+    return out;
+}
+
+void CUDAStateModel::removeParticle(const model::Particle &) {
+    throw std::logic_error("CUDA kernel: removing single particles is not supported (decay reactions remove them)");
+}
+
+void CUDAStateModel::removeAllParticles() {
+    _pending.clear();
+    _topologies.clear();
+    _kernel->initialize();
+}
+
+scalar CUDAStateModel::energy() const {
+    double e = 0.0;
+    if (_kernel->sysIfCreated()) check(rdc_get_energy(_kernel->sysIfCreated(), &e));
+    _energy = e;
+    return _energy;
+}
+
+scalar &CUDAStateModel::energy() {
+    double e = 0.0;
+    if (_kernel->sysIfCreated()) check(rdc_get_energy(_kernel->sysIfCreated(), &e));
+    _energy = e;
+    return _energy;
+}
+
+void CUDAStateModel::toDenseParticleIndices(std::vector<std::size_t>::iterator begin,
+                                            std::vector<std::size_t>::iterator end) const {
+    // device ids -> positions in getParticles()'s order
+    const auto h = fetch(_kernel->sysIfCreated());
+    std::unordered_map<uint64_t, std::size_t> dense;
+    for (std::size_t i = 0; i < h.ids.size(); ++i) dense[h.ids[i]] = i;
+    for (auto it = begin; it != end; ++it) *it = dense.at(*it);
+}
+
+// ---- actions ----------------------------------------------------------------------------------------
+
+namespace act = model::actions;
+
+namespace {
+template <typename Base, typename... Args>
+struct CallAction : Base {
+    std::function<void()> fn;
+    CallAction(std::function<void()> f, Args... args) : Base(args...), fn(std::move(f)) {}
+    void perform() override { fn(); }
+};
+}  // namespace
+
+std::unique_ptr<act::AddParticles> CUDAActionFactory::addParticles(const std::vector<model::Particle> &particles) const {
+    return std::make_unique<act::AddParticles>(_kernel, particles);
+}
+std::unique_ptr<act::EulerBDIntegrator> CUDAActionFactory::eulerBDIntegrator(scalar dt) const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::EulerBDIntegrator, scalar>>([k, dt] { check(rdc_euler_bd_integrate(k->sys(), dt)); }, dt);
+}
+std::unique_ptr<act::CalculateForces> CUDAActionFactory::calculateForces() const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::CalculateForces>>([k] { check(rdc_calculate_forces(k->sys())); });
+}
+std::unique_ptr<act::CreateNeighborList> CUDAActionFactory::createNeighborList(scalar cutoff) const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::CreateNeighborList, scalar>>([k, cutoff] { check(rdc_nl_create(k->sys(), cutoff)); }, cutoff);
+}
+std::unique_ptr<act::UpdateNeighborList> CUDAActionFactory::updateNeighborList() const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::UpdateNeighborList>>([k] { check(rdc_nl_update(k->sys())); });
+}
+std::unique_ptr<act::ClearNeighborList> CUDAActionFactory::clearNeighborList() const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::ClearNeighborList>>([k] { check(rdc_nl_clear(k->sys())); });
+}
+std::unique_ptr<act::EvaluateCompartments> CUDAActionFactory::evaluateCompartments() const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::EvaluateCompartments>>([k] {
+        if (!k->context().compartments().get().empty())
+            throw std::logic_error("CUDA kernel: compartments are not supported");
+    });
+}
+std::unique_ptr<act::reactions::UncontrolledApproximation> CUDAActionFactory::uncontrolledApproximation(scalar dt) const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::reactions::UncontrolledApproximation, scalar>>(
+            [k, dt] { check(rdc_uncontrolled_approximation(k->sys(), dt)); }, dt);
+}
+std::unique_ptr<act::reactions::Gillespie> CUDAActionFactory::gillespie(scalar dt) const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::reactions::Gillespie, scalar>>([k, dt] { check(rdc_gillespie(k->sys(), dt)); }, dt);
+}
+std::unique_ptr<act::reactions::DetailedBalance> CUDAActionFactory::detailedBalance(scalar) const {
+    throw std::logic_error("CUDA kernel: the detailed-balance reaction handler is not supported");
+}
+std::unique_ptr<act::top::EvaluateTopologyReactions> CUDAActionFactory::evaluateTopologyReactions(scalar dt) const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::top::EvaluateTopologyReactions, scalar>>([k] {
+        if (k->context().topologyRegistry().nStructuralReactions() > 0 ||
+            !k->context().topologyRegistry().spatialReactionRegistry().empty())
+            throw std::logic_error("CUDA kernel: topology reactions are not supported");
+    }, dt);
+}
+std::unique_ptr<act::top::BreakBonds> CUDAActionFactory::breakBonds(scalar, act::top::BreakConfig) const {
+    throw std::logic_error("CUDA kernel: BreakBonds is not supported");
+}
+std::unique_ptr<act::EvaluateObservables> CUDAActionFactory::evaluateObservables() const {
+    struct Evaluate : act::EvaluateObservables {
+        CUDAKernel *k;
+        explicit Evaluate(CUDAKernel *k) : k(k) {}
+        void perform(TimeStep t) override { k->evaluateObservables(t); }
+    };
+    return std::make_unique<Evaluate>(_kernel);
+}
+std::unique_ptr<act::MakeCheckpoint> CUDAActionFactory::makeCheckpoint(std::string, std::size_t) const {
+    throw std::logic_error("CUDA kernel: checkpoints are not supported");
+}
+std::unique_ptr<act::InitializeKernel> CUDAActionFactory::initializeKernel() const {
+    auto *k = _kernel;
+    return std::make_unique<CallAction<act::InitializeKernel>>([k] { check(rdc_initialize(k->sys())); });
+}
+
+// ---- observables ------------------------------------------------------------------------------------
+
+namespace obs = model::observables;
+
+namespace {
+struct NParticlesCUDA : obs::NParticles {
+    CUDAKernel *k;
+    NParticlesCUDA(CUDAKernel *k, Stride s, std::vector<std::string> t) : obs::NParticles(k, s, std::move(t)), k(k) {}
+    void evaluate() override {  // CPUObservables.cpp:153-171
+        const auto nt = (std::size_t)k->context().particleTypes().nTypes();
+        std::vector<int64_t> c(std::max<std::size_t>(nt, 1) + 32);
+        check(rdc_count_types(k->sys(), c.data()));
+        result.clear();
+        if (typesToCount.empty()) {
+            unsigned long sum = 0;
+            for (std::size_t i = 0; i < nt; ++i) sum += (unsigned long)c[i];
+            result.push_back(sum);
+        } else {
+            for (auto t : typesToCount) result.push_back((unsigned long)c[t]);
+        }
+    }
+};
+
+struct ForcesCUDA : obs::Forces {
+    CUDAKernel *k;
+    ForcesCUDA(CUDAKernel *k, Stride s, std::vector<std::string> t) : obs::Forces(k, s, std::move(t)), k(k) {}
+    void evaluate() override {  // CPUObservables.cpp:177-197
+        int64_t n = 0;
+        check(rdc_get_n_particles(k->sys(), &n));
+        std::vector<double> f(3 * (std::size_t)n);
+        std::vector<uint64_t> ids((std::size_t)n);
+        int64_t got = 0;
+        check(rdc_get_forces(k->sys(), n, f.data(), ids.data(), &got));
+        std::vector<int> types((std::size_t)n);
+        check(rdc_get_particles(k->sys(), n, nullptr, types.data(), nullptr, &got));
+        result.clear();
+        for (int64_t i = 0; i < got; ++i)
+            if (typesToCount.empty() ||
+                std::find(typesToCount.begin(), typesToCount.end(), (ParticleTypeId)types[i]) != typesToCount.end())
+                result.emplace_back(f[3 * i], f[3 * i + 1], f[3 * i + 2]);
+    }
+};
+
+struct PositionsCUDA : obs::Positions {
+    CUDAKernel *k;
+    PositionsCUDA(CUDAKernel *k, Stride s, std::vector<std::string> t) : obs::Positions(k, s, std::move(t)), k(k) {}
+    void evaluate() override {
+        result.clear();
+        for (const auto &p : k->stateModel().getParticles())
+            if (typesToCount.empty() ||
+                std::find(typesToCount.begin(), typesToCount.end(), p.type()) != typesToCount.end())
+                result.push_back(p.pos());
+    }
+};
+
+struct ParticlesCUDA : obs::Particles {
+    CUDAKernel *k;
+    ParticlesCUDA(CUDAKernel *k, Stride s) : obs::Particles(k, s), k(k) {}
+    void evaluate() override {
+        auto &[types, ids, positions] = result;
+        types.clear(); ids.clear(); positions.clear();
+        for (const auto &p : k->stateModel().getParticles()) {
+            types.push_back(p.type());
+            ids.push_back(p.id());
+            positions.push_back(p.pos());
+        }
+    }
+};
+
+struct HistogramCUDA : obs::HistogramAlongAxis {
+    CUDAKernel *k;
+    unsigned axis_;
+    HistogramCUDA(CUDAKernel *k, Stride s, std::vector<scalar> b, std::vector<std::string> t, unsigned axis)
+        : obs::HistogramAlongAxis(k, s, std::move(b), std::move(t), axis), k(k), axis_(axis) {}
+    void evaluate() override {  // CPUObservables.cpp:85-146
+        std::vector<int> types(typesToCount.begin(), typesToCount.end());
+        result.assign(binBorders.size() - 1, 0);
+        check(rdc_histogram_along_axis(k->sys(), (int)binBorders.size(), binBorders.data(), (int)types.size(),
+                                       types.data(), (int)axis_, result.data()));
+    }
+};
+
+struct RadialDistributionCUDA : obs::RadialDistribution {
+    CUDAKernel *k;
+    RadialDistributionCUDA(CUDAKernel *k, Stride s, std::vector<scalar> b, std::vector<std::string> from,
+                           std::vector<std::string> to, scalar density)
+        : obs::RadialDistribution(k, s, b, from, to, density), k(k) {}
+    void evaluate() override {  // RadialDistribution.cpp:75-128, evaluated on the device
+        std::vector<int> from(typeCountFrom.begin(), typeCountFrom.end()), to(typeCountTo.begin(), typeCountTo.end());
+        auto &[centers, distribution] = result;
+        distribution.assign(binBorders.size() - 1, 0);
+        counts.assign(binBorders.size() - 1, 0);
+        check(rdc_radial_distribution(k->sys(), (int)binBorders.size(), binBorders.data(), (int)from.size(), from.data(),
+                                      (int)to.size(), to.data(), particleToDensity, counts.data(), distribution.data()));
+    }
+};
+
+struct ReactionCountsCUDA : obs::ReactionCounts {
+    CUDAKernel *k;
+    ReactionCountsCUDA(CUDAKernel *k, Stride s) : obs::ReactionCounts(k, s), k(k) {}
+    void evaluate() override {  // CPUStateModel.cpp:126-144
+        const auto &rx = k->reactionIds();
+        std::vector<int64_t> c(rx.size() + 1, 0);
+        check(rdc_get_reaction_counts(k->sys(), (int)c.size(), c.data()));
+        auto &counts = std::get<0>(result);
+        counts.clear();
+        for (std::size_t rid = 0; rid < rx.size(); ++rid)
+            if (rx[rid] >= 0) counts[(ReactionId)rid] = (std::size_t)c[(std::size_t)rx[rid]];
+    }
+};
+
+struct VirialCUDA : obs::Virial {
+    CUDAKernel *k;
+    VirialCUDA(CUDAKernel *k, Stride s) : obs::Virial(k, s), k(k) {}
+    void evaluate() override {
+        double v[9];
+        check(rdc_get_virial(k->sys(), v));
+        result = Matrix33{{{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8]}}};
+    }
+};
+}  // namespace
+
+CUDAObservableFactory::CUDAObservableFactory(CUDAKernel *kernel) : obs::ObservableFactory(kernel), _kernel(kernel) {}
+
+std::unique_ptr<obs::Energy> CUDAObservableFactory::energy(Stride s, ObsCallback<obs::Energy> cb) const {
+    auto o = std::make_unique<obs::Energy>(_kernel, s);  // evaluates StateModel::energy()
+    o->setCallback(cb);
+    return o;
+}
+std::unique_ptr<obs::Virial> CUDAObservableFactory::virial(Stride s, ObsCallback<obs::Virial> cb) const {
+    auto o = std::make_unique<VirialCUDA>(_kernel, s);
+    o->setCallback(cb);
+    _kernel->context().recordVirial() = true;
+    return o;
+}
+std::unique_ptr<obs::HistogramAlongAxis>
+CUDAObservableFactory::histogramAlongAxis(Stride s, std::vector<scalar> b, std::vector<std::string> t, unsigned int axis,
+                                          ObsCallback<obs::HistogramAlongAxis> cb) const {
+    auto o = std::make_unique<HistogramCUDA>(_kernel, s, std::move(b), std::move(t), axis);
+    o->setCallback(cb);
+    return o;
+}
+std::unique_ptr<obs::NParticles>
+CUDAObservableFactory::nParticles(Stride s, std::vector<std::string> t, ObsCallback<obs::NParticles> cb) const {
+    auto o = std::make_unique<NParticlesCUDA>(_kernel, s, std::move(t));
+    o->setCallback(cb);
+    return o;
+}
+std::unique_ptr<obs::Forces>
+CUDAObservableFactory::forces(Stride s, std::vector<std::string> t, ObsCallback<obs::Forces> cb) const {
+    auto o = std::make_unique<ForcesCUDA>(_kernel, s, std::move(t));
+    o->setCallback(cb);
+    return o;
+}
+std::unique_ptr<obs::Positions>
+CUDAObservableFactory::positions(Stride s, std::vector<std::string> t, ObsCallback<obs::Positions> cb) const {
+    auto o = std::make_unique<PositionsCUDA>(_kernel, s, std::move(t));
+    o->setCallback(cb);
+    return o;
+}
+std::unique_ptr<obs::RadialDistribution>
+CUDAObservableFactory::radialDistribution(Stride s, std::vector<scalar> b, std::vector<std::string> from,
+                                          std::vector<std::string> to, scalar density,
+                                          ObsCallback<obs::RadialDistribution> cb) const {
+    auto o = std::make_unique<RadialDistributionCUDA>(_kernel, s, std::move(b), std::move(from), std::move(to), density);
+    o->setCallback(cb);
+    return o;
+}
+std::unique_ptr<obs::Particles> CUDAObservableFactory::particles(Stride s, ObsCallback<obs::Particles> cb) const {
+    auto o = std::make_unique<ParticlesCUDA>(_kernel, s);
+    o->setCallback(cb);
+    return o;
+}
+std::unique_ptr<obs::Reactions> CUDAObservableFactory::reactions(Stride, ObsCallback<obs::Reactions>) const {
+    throw std::logic_error("CUDA kernel: the Reactions observable (records with positions) is not supported");
+}
+std::unique_ptr<obs::ReactionCounts> CUDAObservableFactory::reactionCounts(Stride s, ObsCallback<obs::ReactionCounts> cb) const {
+    auto o = std::make_unique<ReactionCountsCUDA>(_kernel, s);
+    o->setCallback(cb);
+    _kernel->context().recordReactionCounts() = true;
+    return o;
+}
+
+// ---- kernel -----------------------------------------------------------------------------------------
+
+CUDAKernel::CUDAKernel() : model::Kernel("CUDA"), _state(this), _actions(this), _observables(this) {}
+
+CUDAKernel::~CUDAKernel() {
+    if (_sys) rdc_system_destroy(_sys);
+    if (_ctx) rdc_context_destroy(_ctx);
+}
+
+// Kernel::initialize (CPUKernel.cpp:63-83): a device context from the current model::Context and a fresh
+// system; particles added before are kept (read back and added to the new system)
+void CUDAKernel::initialize() {
+    model::Kernel::initialize();
+    std::vector<model::Particle> keep;
+    if (_sys) keep = _state.getParticles();
+    rdc_context *c = toDevice(context(), _rx);
+    rdc_system *s = nullptr;
+    const int rc = rdc_system_create(&s, c, seedFromEnvironment());
+    if (rc != RDC_OK) {
+        rdc_context_destroy(c);
+        check(rc);
+    }
+    if (_sys) rdc_system_destroy(_sys);
+    if (_ctx) rdc_context_destroy(_ctx);
+    _ctx = c;
+    _sys = s;
+    if (!keep.empty()) _state.addParticles(keep);
+    check(rdc_initialize(_sys));
+}
+
+rdc_system *CUDAKernel::sys() {
+    if (!_sys) initialize();
+    _state.flushTopologies();
+    return _sys;
+}
+
+}  // namespace readdy::kernel::cuda
+
+extern "C" const char *name() { return rdc_kernel_name(); }  // "CUDA"; CPUKernel.cpp:89-91
+
+extern "C" readdy::model::Kernel *createKernel() { return new readdy::kernel::cuda::CUDAKernel(); }  // :93-95

@@ -1,0 +1,162 @@
+// The "CUDA" kernel plugin for ReaDDy: model::Kernel, StateModel, ActionFactory and ObservableFactory of
+// the reference's plugin interface (include/readdy/model/Kernel.h:71-235, StateModel.h:53-118,
+// actions/ActionFactory.h:56-129, observables/ObservableFactory.h:62-185), each method one call into the C
+// ABI of libreaddy_cuda_core.so (include/readdy_cuda.h).  Built against ReaDDy's headers like the CPU
+// kernel (kernels/cpu) and linked to libreaddy and libreaddy_cuda_core.so; install it as
+// libreaddy_kernel_cuda.so in READDY_PLUGIN_DIR, whose loader accepts file names that contain ".so" and
+// none of ".a", ".lib", ".obj", ... anywhere in the path (readdy/main/plugin/KernelProvider.cpp:123-133).
+#pragma once
+
+#include <readdy/model/Kernel.h>
+#include <readdy/model/actions/Actions.h>
+#include <readdy/model/observables/ObservableFactory.h>
+#include <readdy/model/topologies/GraphTopology.h>
+#include <readdy_cuda.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace readdy::kernel::cuda {
+
+// status code of the C ABI -> the exception type the CPU kernel throws for the same failure
+void check(int rc);
+
+class CUDAKernel;
+
+// StateModel over one rdc_system.  Particles added through addParticles go to the device at once.
+// Topology particles stay on the host until the first action after they were added: their graph's
+// edges are only complete then (the API adds edges after addTopology returns), and rdc_add_topology
+// takes particles and edges together.
+class CUDAStateModel : public model::StateModel {
+public:
+    explicit CUDAStateModel(CUDAKernel *kernel) : _kernel(kernel) {}
+
+    std::vector<Vec3> getParticlePositions() const override;
+    std::vector<model::Particle> getParticles() const override;
+    model::Particle getParticleForIndex(std::size_t index) const override;
+    ParticleTypeId getParticleType(std::size_t index) const override;
+    void initializeNeighborList(scalar interactionDistance) override;
+    void updateNeighborList() override;
+    void clearNeighborList() override;
+    void addParticle(const model::Particle &p) override { addParticles({p}); }
+    void addParticles(const std::vector<model::Particle> &p) override;
+    model::top::GraphTopology *const addTopology(TopologyTypeId type,
+                                                 const std::vector<model::Particle> &particles) override;
+    std::vector<model::top::GraphTopology *> getTopologies() override;
+    void removeParticle(const model::Particle &p) override;
+    void removeAllParticles() override;
+    scalar energy() const override;
+    scalar &energy() override;
+    scalar time() const override { return _time; }
+    void setTime(scalar t) override { _time = t; }
+    void toDenseParticleIndices(std::vector<std::size_t>::iterator begin,
+                                std::vector<std::size_t>::iterator end) const override;
+    void clear() override { removeAllParticles(); }
+
+    // uploads the pending topologies (particles and graph edges) to the device
+    void flushTopologies();
+
+private:
+    struct PendingTopology {
+        std::unique_ptr<model::top::GraphTopology> top;
+        std::vector<model::Particle> particles;
+    };
+    CUDAKernel *_kernel;
+    std::vector<PendingTopology> _pending;
+    std::vector<std::unique_ptr<model::top::GraphTopology>> _topologies;
+    mutable scalar _energy = 0;
+    scalar _time = 0;
+};
+
+class CUDAActionFactory : public model::actions::ActionFactory {
+public:
+    explicit CUDAActionFactory(CUDAKernel *kernel) : _kernel(kernel) {}
+
+    std::unique_ptr<model::actions::AddParticles> addParticles(const std::vector<model::Particle> &particles) const override;
+    std::unique_ptr<model::actions::EulerBDIntegrator> eulerBDIntegrator(scalar timeStep) const override;
+    std::unique_ptr<model::actions::CalculateForces> calculateForces() const override;
+    std::unique_ptr<model::actions::CreateNeighborList> createNeighborList(scalar interactionDistance) const override;
+    std::unique_ptr<model::actions::UpdateNeighborList> updateNeighborList() const override;
+    std::unique_ptr<model::actions::ClearNeighborList> clearNeighborList() const override;
+    std::unique_ptr<model::actions::EvaluateCompartments> evaluateCompartments() const override;
+    std::unique_ptr<model::actions::reactions::UncontrolledApproximation> uncontrolledApproximation(scalar timeStep) const override;
+    std::unique_ptr<model::actions::reactions::Gillespie> gillespie(scalar timeStep) const override;
+    std::unique_ptr<model::actions::reactions::DetailedBalance> detailedBalance(scalar timeStep) const override;
+    std::unique_ptr<model::actions::top::EvaluateTopologyReactions> evaluateTopologyReactions(scalar timeStep) const override;
+    std::unique_ptr<model::actions::top::BreakBonds> breakBonds(scalar timeStep, model::actions::top::BreakConfig config) const override;
+    std::unique_ptr<model::actions::EvaluateObservables> evaluateObservables() const override;
+    std::unique_ptr<model::actions::MakeCheckpoint> makeCheckpoint(std::string base, std::size_t maxNSaves) const override;
+    std::unique_ptr<model::actions::InitializeKernel> initializeKernel() const override;
+
+private:
+    CUDAKernel *_kernel;
+};
+
+class CUDAObservableFactory : public model::observables::ObservableFactory {
+public:
+    explicit CUDAObservableFactory(CUDAKernel *kernel);
+
+    std::unique_ptr<model::observables::Energy> energy(Stride stride, ObsCallback<model::observables::Energy> callback) const override;
+    std::unique_ptr<model::observables::Virial> virial(Stride stride, ObsCallback<model::observables::Virial> callback) const override;
+    std::unique_ptr<model::observables::HistogramAlongAxis>
+    histogramAlongAxis(Stride stride, std::vector<scalar> binBorders, std::vector<std::string> typesToCount,
+                       unsigned int axis, ObsCallback<model::observables::HistogramAlongAxis> callback) const override;
+    std::unique_ptr<model::observables::NParticles>
+    nParticles(Stride stride, std::vector<std::string> typesToCount, ObsCallback<model::observables::NParticles> callback) const override;
+    std::unique_ptr<model::observables::Forces>
+    forces(Stride stride, std::vector<std::string> typesToCount, ObsCallback<model::observables::Forces> callback) const override;
+    std::unique_ptr<model::observables::Positions>
+    positions(Stride stride, std::vector<std::string> typesToCount, ObsCallback<model::observables::Positions> callback) const override;
+    std::unique_ptr<model::observables::RadialDistribution>
+    radialDistribution(Stride stride, std::vector<scalar> binBorders, std::vector<std::string> typeCountFrom,
+                       std::vector<std::string> typeCountTo, scalar particleDensity,
+                       ObsCallback<model::observables::RadialDistribution> callback) const override;
+    std::unique_ptr<model::observables::Particles> particles(Stride stride, ObsCallback<model::observables::Particles> callback) const override;
+    std::unique_ptr<model::observables::Reactions> reactions(Stride stride, ObsCallback<model::observables::Reactions> callback) const override;
+    std::unique_ptr<model::observables::ReactionCounts> reactionCounts(Stride stride, ObsCallback<model::observables::ReactionCounts> callback) const override;
+
+private:
+    CUDAKernel *_kernel;
+};
+
+class CUDAKernel : public model::Kernel {
+public:
+    CUDAKernel();
+    ~CUDAKernel() override;
+
+    const model::StateModel &stateModel() const override { return _state; }
+    model::StateModel &stateModel() override { return _state; }
+    const model::actions::ActionFactory &actions() const override { return _actions; }
+    model::actions::ActionFactory &actions() override { return _actions; }
+    const model::observables::ObservableFactory &observe() const override { return _observables; }
+    model::observables::ObservableFactory &observe() override { return _observables; }
+    // topology reactions and BreakBonds are not provided; static topologies are (bonds, angles, dihedrals)
+    const model::top::TopologyActionFactory *const getTopologyActionFactory() const override { return nullptr; }
+    model::top::TopologyActionFactory *const getTopologyActionFactory() override { return nullptr; }
+    void initialize() override;
+    bool supportsGillespie() const override { return true; }
+
+    // the device system of the current context (created by initialize); pending topologies are uploaded
+    // first, so every action sees all particles
+    rdc_system *sys();
+    rdc_system *sysIfCreated() const { return _sys; }
+    // reference reaction id -> device reaction id (-1: not registered on the device)
+    const std::vector<int> &reactionIds() const { return _rx; }
+
+private:
+    rdc_context *_ctx = nullptr;
+    rdc_system *_sys = nullptr;
+    std::vector<int> _rx;
+    CUDAStateModel _state;
+    CUDAActionFactory _actions;
+    CUDAObservableFactory _observables;
+};
+
+// model::Context -> a device context; fills rx with the device id of each reference reaction id
+rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx);
+
+}  // namespace readdy::kernel::cuda
+
+extern "C" const char *name();
+extern "C" readdy::model::Kernel *createKernel();

@@ -687,3 +687,48 @@ def test_observables_match_oracle(rg, case):
     fine = np.linspace(0., 7.5, 5001)
     np.testing.assert_array_equal(k.radial_distribution(fine, [0], [1, 2], 0.25)[2],
                                   o.radial_distribution(fine, [0], [1, 2], 0.25)[0])
+
+
+@pytest.mark.parametrize("steps", [0, 20], ids=["initial", "after_20_steps"])
+@pytest.mark.parametrize("name", ["crowded_200k", "polymer_200k"])
+def test_forces_match_oracle_on_the_benchmarked_single_systems(rg, name, steps):
+    """The inputs that bench.py times through the per-system path (the 200k crowded system on its jittered
+    lattice; 2000 chains of 50 beads in 100k solvent), at the start and after 20 steps of their own
+    dynamics: forces and energy of the state the GPU holds against the oracle."""
+    import bench
+    w = bench.single_system(name)
+    k = bench._gpu_system(w, seed=3)
+    if steps:
+        k.run(steps, w["dt"], handler=rg.GILLESPIE if w["handler"] == "gillespie" else rg.UNCONTROLLED_APPROXIMATION)
+    cutoff = k.context.calculate_max_cutoff()
+    k.create_neighbor_list(cutoff)
+    k.calculate_forces()
+    f_gpu, ids = k.get_forces()
+    p, t, ids2 = k.get_particles()
+    (f_gpu,) = by_id(ids, f_gpu)
+    (p, t) = by_id(ids2, p, t)
+    nb = 0
+    w2 = dict(w, pos=p, types=t)
+    if w["chains"] is not None:
+        L = len(w["chains"][0])
+        nb = L * len(w["chains"])
+        w2 = dict(w, chains=list(p[:nb].reshape(-1, L, 3)), pos=p[nb:], types=t[nb:])
+    o = bench._oracle_system(w2, seed=3, threads=8)
+    o.nl_setup(cutoff)
+    e_ref = o.calculate_forces()
+    _, _, oid, f_ref, _ = o.particles()
+    sc = o.force_scales()
+    (f_ref, sc) = by_id(oid, f_ref, sc)
+    err, rel_good = force_error(f_gpu, f_ref, sc)
+    e_gpu = k.energy
+    print(f"{name} after {steps} steps: max err (floored) {err.max():.3e} p99.9 {np.quantile(err, .999):.3e}; "
+          f"energy {e_gpu:.9g} vs {e_ref:.9g}")
+    bad = err > FORCE_RTOL
+    if bad.any():
+        assert nb > 0, np.sort(err)[-8:]
+        idx = np.arange(nb).reshape(len(w["chains"]), -1)
+        quads = np.stack([idx[:, :-3].ravel(), idx[:, 1:-2].ravel(), idx[:, 2:-1].ravel(), idx[:, 3:].ravel()], 1)
+        excused = np.concatenate([dihedral_near_zero_force_switch(p[:nb], quads, w["box"]),
+                                  np.zeros(len(err) - nb, bool)])
+        assert np.all(excused[bad]), (np.flatnonzero(bad & ~excused), err[bad & ~excused])
+    assert abs(e_gpu - e_ref) <= ENERGY_RTOL * abs(e_ref)
