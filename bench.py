@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--replicas", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=60.0,
+                    help="time budget of the CPU legs: no further sampled replica starts once it is spent")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests of the served-stream sample (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=150.0, help="wall-time limit of the served-stream sample")
     ap.add_argument("--single-systems", type=int, default=1, help="time the three single-system workloads (0: skip)")
@@ -169,26 +170,60 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(ns, boxes, pos, types, seed, budget_s, rng_pick):
-    """FP64 restatement of the reference CPU kernel (Gillespie, SimulationLoop step order) timed on a
-    random sample of replicas with all host threads, until the time budget is spent."""
+CPU_SAMPLE = 16  # replicas of the ensemble that the CPU legs advance
+
+
+def reference_cpu(ns, boxes, pos, types, seed, steps, warmup, budget_s=60.0):
+    """The reference path on the host cores, on a fixed random sample of CPU_SAMPLE replicas of the ensemble:
+    the reference's own pthread CPU kernel (kernels/cpu built from the reference sources into
+    oracle/_ref; SimulationLoop::run with Gillespie) when it could be built, otherwise the FP64 oracle
+    restatement.  Every sampled replica runs `warmup` untimed steps, then `steps` timed steps with all host
+    threads; no further replica starts once budget_s is spent.  Returns (particle-steps/s, particles of the
+    replicas run, cpu_baseline description).  The in-run baseline of the GPU arm and the reference arm call
+    this with the same sample, step counts and budget."""
     import oracle
-    oracle.build()
+    from oracle import ref_build, reference_kernel
     cores = os.cpu_count() or 1
-    order = rng_pick.permutation(len(ns))
-    done_ps, spent, reps, steps = 0, 0.0, 0, 5
-    for r in order:
-        o = oracle_system(tuple(boxes[r]), pos[r], types[r], seed + int(r), cores)
-        t0 = time.perf_counter()
-        o.run(steps, 1e-3, handler=oracle.GILLESPIE)
-        spent += time.perf_counter() - t0
-        done_ps += int(ns[r]) * steps
-        reps += 1
-        if spent > budget_s:
+    sample = np.random.default_rng(seed + 5).choice(len(ns), size=min(CPU_SAMPLE, len(ns)), replace=False)
+    use_ref = reference_kernel.available()
+    spent, done, ran = 0.0, 0, []
+    for r in sample:
+        if ran and spent > budget_s:
             break
-    return {"value": done_ps / spent, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{reps} random replicas of the ensemble x {steps} steps each (FP64 oracle, Gillespie), "
-                      f"{done_ps} particle-steps in {spent:.1f} s"}
+        ran.append(int(r))
+        box = tuple(float(x) for x in boxes[r])
+        if use_ref:
+            k = reference_kernel.ReferenceKernel(box, (True, True, True), 1.0, (1.0, 1.0, 0.5), n_threads=cores)
+            for a in range(3):
+                for b in range(a, 3):
+                    k.add_harmonic_repulsion(a, b, 10.0, 1.0)
+            k.add_fusion(0, 1, 2, 1.0, 1.0)
+            k.add_fission(2, 0, 1, 0.1, 1.0)
+            k.add_particles(pos[r], types[r])
+            if warmup:
+                k.run(warmup, 1e-3, handler=reference_kernel.GILLESPIE)
+            _, sec = k.run(steps, 1e-3, handler=reference_kernel.GILLESPIE)
+        else:
+            oracle.build()
+            o = oracle_system(box, pos[r], types[r], seed + int(r), cores)
+            if warmup:
+                o.run(warmup, 1e-3, handler=oracle.GILLESPIE)
+            t0 = time.perf_counter()
+            o.run(steps, 1e-3, handler=oracle.GILLESPIE)
+            sec = time.perf_counter() - t0
+        spent += sec
+        done += int(ns[r]) * steps
+    what = ("the reference's pthread CPU kernel (kernels/cpu, compiled from the reference sources, "
+            "SimulationLoop::run, Gillespie)" if use_ref else
+            "the FP64 restatement of the reference CPU kernel (reference build unavailable: "
+            f"{ref_build.unavailable_reason()})")
+    v = done / spent
+    n_run = int(ns[ran].sum())
+    return v, n_run, {"value": v, "unit": UNIT, "cores": cores, "kind": "reference" if use_ref else "port",
+               "threads": cores, "reference_default_threads": 4 * cores,
+               "sample": f"{len(ran)} random replicas of the ensemble ({n_run} particles) x "
+                         f"{steps} steps after {warmup} warm-up steps, {what}, {cores} threads per replica; "
+                         f"{done} particle-steps in {spent:.1f} s"}
 
 
 def one_at_a_time(ns, boxes, pos, types, seed, n_sample, steps, rng_pick):
@@ -413,7 +448,7 @@ def run_gb300(args, rank, world):
     if rank == 0:
         pick = np.random.default_rng(args.seed + 99)
         oat = one_at_a_time(ns, boxes, pos, types, seed, 64, 50, pick)
-        cpu = cpu_baseline(ns, boxes, pos, types, seed, args.cpu_seconds, np.random.default_rng(args.seed + 5))
+        _, _, cpu = reference_cpu(ns, boxes, pos, types, args.seed, args.steps, args.warmup, args.cpu_seconds)
         served = serving(args.serve_requests, args.serve_seconds, args.plain_threshold) if args.serve_requests else None
         singles = single_systems() if args.single_systems else None
         peak, peak_kind = measured_peaks()
@@ -463,46 +498,18 @@ def run_gb300(args, rank, world):
 
 
 def run_reference(args):
-    """The reference path on the host cores: the FP64 CPU restatement (no compiled reference build
-    travels with the benchmark), all host threads, each step a bounded sample of the ensemble."""
-    import oracle
-    oracle.build()
+    """The reference arm: the reference path on the host cores (reference_cpu), on this arm's config,
+    metric and unit."""
     ns, boxes, pos, types = ensemble(args.seed, args.replicas)
-    cores = os.cpu_count() or 1
-    rng = np.random.default_rng(args.seed + 5)
-    sample = rng.choice(len(ns), size=min(8, len(ns)), replace=False)
-    systems = [oracle_system(tuple(boxes[r]), pos[r], types[r], args.seed + int(r), cores) for r in sample]
-    for o in systems:
-        o.nl_setup(o.calculate_max_cutoff())
-        o.calculate_forces()
-
-    def one_step(o):
-        o.euler_bd(1e-3)
-        o.nl_update()
-        o.gillespie(1e-3)
-        o.nl_update()
-        o.calculate_forces()
-
-    for _ in range(args.warmup):
-        for o in systems:
-            one_step(o)
-    t0 = time.perf_counter()
-    ps = 0
-    for _ in range(args.steps):
-        for o in systems:
-            ps += o.n_particles
-            one_step(o)
-    t = time.perf_counter() - t0
-    v = ps / t
+    v, n_run, cpu = reference_cpu(ns, boxes, pos, types, args.seed, args.steps, args.warmup, args.cpu_seconds)
+    ms = n_run / v * 1e3  # one step of every sampled replica
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded uneven ensemble)", "impl": "reference",
             "config": {"workload": "batched uneven ensemble: 4096 replicas of A+B<->C, N log-uniform in [200, 20000], "
                                    "density 0.25, HR k=10 d=1, Gillespie, dt=1e-3",
-                       "sample": f"{len(sample)} random replicas per step"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{len(sample)} random replicas of the ensemble per step, FP64 restatement of "
-                                       "the reference CPU kernel (SimulationLoop order, Gillespie)"},
+                       "sample": cpu["sample"]},
+            "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -7,6 +7,7 @@
 #pragma once
 #include <fmt/format.h>
 
+#include <cassert>  // spdlog's headers bring it in; ReaDDy's sources rely on that
 #include <cstdio>
 #include <map>
 #include <memory>
@@ -33,6 +34,7 @@ public:
     explicit logger(std::string name) : _name(std::move(name)) {}
     logger(std::string name, std::shared_ptr<sinks::sink>) : _name(std::move(name)) {}
     void set_level(level::level_enum l) { _level = l; }
+    void set_pattern(const std::string &) {}
     level::level_enum level() const { return _level; }
     const std::string &name() const { return _name; }
     template <typename... A> void trace(format_string_t<A...> f, A &&...a) { log(level::trace, f, std::forward<A>(a)...); }

@@ -158,7 +158,10 @@ struct SysDev {
 
 constexpr int FORCE_BLOCKS = 4 * 152;
 constexpr int FORCE_THREADS = 256;
-constexpr int BONDED_BLOCKS = 152;
+#ifndef RDC_BONDED_BLOCKS
+#define RDC_BONDED_BLOCKS 152
+#endif
+constexpr int BONDED_BLOCKS = RDC_BONDED_BLOCKS;
 constexpr int GRID_BLOCKS = 8 * 152;
 constexpr int GRID_THREADS = 256;
 
