@@ -38,8 +38,12 @@ UNIT = "particle-steps/s"
 DENSITY = 0.25
 N_MIN, N_MAX = 200, 20000
 # DRAM bytes per particle of one fused step (dram__bytes_read.sum + dram__bytes_write.sum of one ncu
-# capture of k_engine_step on the first 512 replicas of the ensemble, divided by its particles).
-DRAM_BYTES_PER_PARTICLE = (91.30e6 + 93.78e6) / 2097522
+# capture of k_engine_step on the first 512 replicas of the ensemble, divided by its particles), and the
+# same capture's warp instructions per particle-step and issue activity: the bound that applies to this
+# kernel is the instruction stream, not DRAM bandwidth.
+DRAM_BYTES_PER_PARTICLE = (95.71e6 + 99.75e6) / 2097522
+WARP_INST_PER_PARTICLE = 319.44e6 / 2097522
+ISSUE_ACTIVE_PCT = 54.0
 # algorithmic bytes of one fused step per particle: the particle state (float4 position with the type,
 # uint32 id) read once and written once (the pair forces carried between steps, 2 x 16 bytes, are a
 # choice of the implementation and count as traffic, not as algorithmic bytes)
@@ -487,7 +491,11 @@ def run_gb300(args, rank, world):
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": ALG_BYTES_PER_PARTICLE * n_avg,
                          "traffic": DRAM_BYTES_PER_PARTICLE * n_avg if DRAM_BYTES_PER_PARTICLE else None,
-                         "traffic_source": "ncu capture of a smaller ensemble scaled by particles"},
+                         "traffic_source": "ncu capture of a smaller ensemble scaled by particles",
+                         "issue": {"warp_instructions_per_particle_step": WARP_INST_PER_PARTICLE,
+                                   "warp_instructions_per_launch": WARP_INST_PER_PARTICLE * n_avg,
+                                   "issue_active_pct": ISSUE_ACTIVE_PCT,
+                                   "source": "ncu capture of the first 512 replicas (768 threads), scaled by particles"}},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": 2 * args.steps,
