@@ -138,6 +138,9 @@ int rdc_get_forces(rdc_system *s, int64_t capacity, double *forces3, uint64_t *i
 int rdc_get_virial(rdc_system *s, double *virial9);
 /* StateModel::energy() after the last CalculateForces */
 int rdc_get_energy(rdc_system *s, double *energy);
+/* particles advanced by the integrator since the system was created, summed over steps (the
+ * particle-steps of the throughput figures; no reference counterpart) */
+int rdc_get_particle_steps(rdc_system *s, uint64_t *particle_steps);
 /* NParticles observable per type (kernels/cpu/src/observables/CPUObservables.cpp:153-171) */
 int rdc_count_types(rdc_system *s, int64_t *counts);
 /* ReactionCounts observable: performed events per reaction id since creation
@@ -230,6 +233,21 @@ int rdc_batch_get_particles(rdc_batch *b, int replica, int64_t capacity, double 
  * the ids of rdc_batch_get_particles */
 int rdc_batch_get_forces(rdc_batch *b, int replica, int64_t capacity, double *forces3, uint64_t *ids,
                          int64_t *n_out);
+/* NParticles time series of every replica, streamed: from now on each replica records its per-type counts
+ * (record 0 now, then after every `stride` steps of its step count, at most max_records records; the
+ * NParticles observable with a stride, CPUObservables.cpp:153-171, written the way TimeSeriesWriter appends
+ * a time series, include/readdy/model/observables/io/TimeSeriesWriter.h:56-92).  The records stay on the
+ * device until polled. */
+int rdc_batch_record_counts(rdc_batch *b, int64_t stride, int64_t max_records);
+/* copies the records written since the last poll (at most capacity records): steps[k] is the time step of
+ * record k, counts holds n_replicas * n_types values per record (record-major).  The copy runs on a stream
+ * of its own after the steps already queued; the batch's own stream keeps going.  *n_out = records copied */
+int rdc_batch_poll_count_records(rdc_batch *b, int64_t capacity, int64_t *steps, int64_t *counts, int64_t *n_out);
+/* the Virial observable of every replica (Context::recordVirial, CPUCalculateForces.cpp:247-249): the pair
+ * virial of the forces its next Euler update applies, row-major 3x3 per replica (n_replicas * 9).  Taken
+ * from forces summed over the sorted state, so carried forces must be off (rdc_batch_set_carry_forces(b, 0);
+ * RDC_ERR_LOGIC otherwise) */
+int rdc_batch_get_virial(rdc_batch *b, double *virial9);
 /* performed events per replica and reaction since the batch was created (n_replicas * n, by reaction
  * id; the ReactionCounts observable, CPUStateModel.cpp:126-144, of every replica) */
 int rdc_batch_reaction_counts(rdc_batch *b, int n, int64_t *counts);

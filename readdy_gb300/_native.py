@@ -72,6 +72,7 @@ def _sig(lib):
         "rdc_get_forces": (i, [vp, i64, P(d), P(u64), P(i64)]),
         "rdc_get_energy": (i, [vp, P(d)]),
         "rdc_count_types": (i, [vp, P(i64)]),
+        "rdc_get_particle_steps": (i, [vp, P(u64)]),
         "rdc_get_reaction_counts": (i, [vp, i, P(i64)]),
         "rdc_histogram_along_axis": (i, [vp, i, P(d), i, P(i), i, P(d)]),
         "rdc_radial_distribution": (i, [vp, i, P(d), i, P(i), i, P(i), d, P(d), P(d)]),
@@ -102,6 +103,9 @@ def _sig(lib):
         "rdc_batch_get_particles": (i, [vp, i, i64, P(d), P(i), P(u64), P(i64)]),
         "rdc_batch_get_forces": (i, [vp, i, i64, P(d), P(u64), P(i64)]),
         "rdc_batch_reaction_counts": (i, [vp, i, P(i64)]),
+        "rdc_batch_get_virial": (i, [vp, P(d)]),
+        "rdc_batch_record_counts": (i, [vp, i64, i64]),
+        "rdc_batch_poll_count_records": (i, [vp, i64, P(i64), P(i64), P(i64)]),
         "rdc_batch_replica_grid": (i, [vp, i, P(i), P(i)]),
         "rdc_batch_synchronize": (i, [vp]),
         "rdc_server_create": (i, [vpp, u64, i, i, i64]),

@@ -116,6 +116,27 @@ class ReplicaBatch:
                                                C.byref(got)))
         return f[:got.value], ids[:got.value]
 
+    def record_counts(self, stride: int, max_records: int):
+        """From now on every replica records its per-type counts every `stride` steps (record 0 now)."""
+        N.check(self._lib.rdc_batch_record_counts(self._h, int(stride), int(max_records)))
+        self._max_records = int(max_records)
+
+    def poll_count_records(self):
+        """(steps (k,), counts (k, n_replicas, n_types)) of the records written since the last poll."""
+        cap = getattr(self, "_max_records", 0)
+        steps = np.zeros(max(cap, 1), np.int64)
+        counts = np.zeros((max(cap, 1), self.n_replicas, self.context.n_types), np.int64)
+        n = C.c_int64()
+        N.check(self._lib.rdc_batch_poll_count_records(self._h, cap, _p(steps, C.c_int64), _p(counts, C.c_int64),
+                                                       C.byref(n)))
+        return steps[:n.value], counts[:n.value]
+
+    def virial(self):
+        """Pair virial of every replica's current state, (n_replicas, 3, 3); needs carried forces off."""
+        out = np.zeros((self.n_replicas, 3, 3))
+        N.check(self._lib.rdc_batch_get_virial(self._h, _p(out, C.c_double)))
+        return out
+
     def reaction_counts(self):
         """Performed events per replica and reaction id, (n_replicas, n_reactions)."""
         n = self.context.n_reactions

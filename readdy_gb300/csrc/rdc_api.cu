@@ -397,8 +397,8 @@ struct rdc_system {
         d.radius = radius;
         d.counters = dalloc<int>(C_COUNT);
         RDC_CUDA(cudaMemsetAsync(d.counters, 0, sizeof(int) * C_COUNT, stream));
-        d.step = dalloc<uint64_t>(2);
-        RDC_CUDA(cudaMemsetAsync(d.step, 0, sizeof(uint64_t) * 2, stream));
+        d.step = dalloc<uint64_t>(3);  // integrator step, reaction step, particles advanced
+        RDC_CUDA(cudaMemsetAsync(d.step, 0, sizeof(uint64_t) * 3, stream));
         d.reaction_counts = dalloc<unsigned long long>(MAX_REACTIONS);
         RDC_CUDA(cudaMemsetAsync(d.reaction_counts, 0, sizeof(unsigned long long) * MAX_REACTIONS, stream));
         d.epart = dalloc<double>(FORCE_BLOCKS + BONDED_BLOCKS);
@@ -1211,6 +1211,15 @@ int rdc_get_energy(rdc_system *s, double *e) {
         require(s && e, "null argument");
         RDC_CUDA(cudaMemcpyAsync(e, s->d.energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         s->sync();
+    });
+}
+int rdc_get_particle_steps(rdc_system *s, uint64_t *particle_steps) {
+    return guarded([&] {
+        require(s && particle_steps, "null argument");
+        unsigned long long v = 0;
+        RDC_CUDA(cudaMemcpyAsync(&v, s->d.step + 2, sizeof(v), cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        *particle_steps = v;
     });
 }
 int rdc_count_types(rdc_system *s, int64_t *counts) {

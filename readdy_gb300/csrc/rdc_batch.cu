@@ -111,6 +111,12 @@ struct rdc_batch {
     size_t smem = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // per-type count records streamed to the host (NParticles time series): record k of every replica is one
+    // contiguous block of R x ntypes counters, so a poll copies new records with one copy on its own stream
+    unsigned long long *records = nullptr;
+    int64_t rec_stride = 0, rec_max = 0, rec_polled = 0, rec_start = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy = nullptr;
 
     ~rdc_batch() { release(); }
 
@@ -123,6 +129,10 @@ struct rdc_batch {
         bfree(bin); bfree(rank); bfree(src); bfree(claim); bfree(taken); bfree(start); bfree(events);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (ev_copy) cudaEventDestroy(ev_copy);
+        bfree(records);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
+        copy_stream = nullptr;
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -172,9 +182,19 @@ struct rdc_batch {
             D.start = start + so[r];
             D.events = events + eo[r];
             D.rx_counts = reaction_counts + (size_t)r * MAX_REACTIONS;
+            apply_records(r);
         }
         RDC_CUDA(cudaMemcpyAsync(desc_dev, desc.data(), sizeof(RepDesc) * R, cudaMemcpyHostToDevice, stream));
         invalidate_graph();
+    }
+
+    // count-record fields of replica r's descriptor (none until recording is switched on)
+    void apply_records(int r) {
+        RepDesc &D = desc[r];
+        D.records = records ? records + (size_t)r * ctx.ntypes : nullptr;
+        D.record_pitch = (int64_t)R * ctx.ntypes;
+        D.count_stride = records ? (int)rec_stride : 0;
+        D.max_records = records ? (int)rec_max : 0;
     }
 
     void init(const ContextData &c, int nrep, const double *bx, const int64_t *cp, uint64_t s) {
@@ -418,6 +438,8 @@ void set_particles_impl(rdc_batch *b, const int64_t *n, const double *const *pos
     k_unpack_replicas<<<std::min(R, 4 * sm_count()), 256, 0, b->stream>>>(b->posB, offs_dev, offs_dev + R + 1, b->posA, R);
     RDC_CUDA(cudaGetLastError());
     RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, b->stream));
+    b->rec_polled = 0;  // with records on, the admission below writes record 0 again (t = 0)
+    b->rec_start = 0;
     b->set_order(std::vector<int64_t>(n, n + R));
     b->sort_all(true);
     b->sync();
@@ -617,6 +639,95 @@ int rdc_batch_get_forces(rdc_batch *b, int replica, int64_t cap, double *forces,
         }
         if (n_out) *n_out = k;
         if (k > cap) throw rdc::CapacityError("output capacity too small for the particles");
+    });
+}
+
+int rdc_batch_record_counts(rdc_batch *b, int64_t stride, int64_t max_records) {
+    BATCH_CALL({
+        if (!b) throw std::invalid_argument("null argument");
+        if (stride < 1 || max_records < 1) throw std::invalid_argument("stride and max_records must be >= 1");
+        const size_t per_record = (size_t)b->R * b->ctx.ntypes;
+        if ((double)per_record * (double)max_records * 8.0 > 16e9)
+            throw std::invalid_argument("count records would take more than 16 GB of device memory");
+        if (max_records > INT_MAX / 2) throw std::invalid_argument("max_records too large");
+        auto st = b->states();
+        b->check_status(st);
+        bfree(b->records);
+        b->records = balloc<unsigned long long>(per_record * (size_t)max_records);
+        b->rec_stride = stride;
+        b->rec_max = max_records;
+        b->rec_polled = 0;
+        b->rec_start = st.empty() ? 0 : st[0].step;
+        if (!b->copy_stream) {
+            RDC_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+            RDC_CUDA(cudaEventCreateWithFlags(&b->ev_copy, cudaEventDisableTiming));
+        }
+        for (int r = 0; r < b->R; ++r) b->apply_records(r);
+        RDC_CUDA(cudaMemcpyAsync(b->desc_dev, b->desc.data(), sizeof(RepDesc) * b->R, cudaMemcpyHostToDevice,
+                                 b->stream));
+        // record 0: the counts now; later records follow every stride steps of the replicas' own step count
+        launch_engine_record_now(b->e, b->R, b->ctx.ntypes, 0, b->stream);
+        RDC_CUDA(cudaGetLastError());
+        for (auto &x : st) x.rec = 1;
+        RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * b->R, cudaMemcpyHostToDevice, b->stream));
+        b->sync();
+    });
+}
+
+int rdc_batch_poll_count_records(rdc_batch *b, int64_t capacity, int64_t *steps, int64_t *counts, int64_t *n_out) {
+    BATCH_CALL({
+        if (!b || !n_out || (capacity > 0 && !counts)) throw std::invalid_argument("null argument");
+        if (!b->records) throw std::logic_error("count records are off (rdc_batch_record_counts switches them on)");
+        // the copies run on their own stream after the steps queued so far; the batch's stream goes on
+        RDC_CUDA(cudaEventRecord(b->ev_copy, b->stream));
+        RDC_CUDA(cudaStreamWaitEvent(b->copy_stream, b->ev_copy, 0));
+        std::vector<RepState> st(b->R);
+        RDC_CUDA(cudaMemcpyAsync(st.data(), b->state_dev, sizeof(RepState) * b->R, cudaMemcpyDeviceToHost,
+                                 b->copy_stream));
+        RDC_CUDA(cudaStreamSynchronize(b->copy_stream));
+        int64_t written = b->rec_max;
+        for (const auto &x : st) {
+            if (x.status) throw std::runtime_error("replica device status " + std::to_string(x.status));
+            written = std::min<int64_t>(written, x.rec);
+        }
+        const int64_t n = std::max<int64_t>(0, std::min<int64_t>(written - b->rec_polled, capacity));
+        const size_t per_record = (size_t)b->R * b->ctx.ntypes;
+        if (n > 0) {
+            std::vector<unsigned long long> h(per_record * (size_t)n);
+            RDC_CUDA(cudaMemcpyAsync(h.data(), b->records + per_record * (size_t)b->rec_polled,
+                                     sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost, b->copy_stream));
+            RDC_CUDA(cudaStreamSynchronize(b->copy_stream));
+            for (size_t k = 0; k < h.size(); ++k) counts[k] = (int64_t)h[k];
+        }
+        if (steps) {
+            // record 0 at the step recording started, record k >= 1 after the k-th later multiple of stride
+            const int64_t first = (b->rec_start / b->rec_stride + 1) * b->rec_stride;
+            for (int64_t k = 0; k < n; ++k) {
+                const int64_t idx = b->rec_polled + k;
+                steps[k] = idx == 0 ? b->rec_start : first + (idx - 1) * b->rec_stride;
+            }
+        }
+        b->rec_polled += n;
+        *n_out = n;
+    });
+}
+
+int rdc_batch_get_virial(rdc_batch *b, double *virial9) {
+    BATCH_CALL({
+        if (!b || !virial9) throw std::invalid_argument("null argument");
+        if (b->forceA)
+            throw std::logic_error("the virial is taken from forces summed over the sorted state: switch carried "
+                                   "forces off first (rdc_batch_set_carry_forces(b, 0))");
+        b->check_status();
+        double *d = balloc<double>((size_t)b->R * 9);
+        struct Release {
+            double *&p;
+            ~Release() { bfree(p); }
+        } release{d};
+        launch_engine_virial(b->e, b->R, d, b->stream);
+        RDC_CUDA(cudaGetLastError());
+        RDC_CUDA(cudaMemcpyAsync(virial9, d, sizeof(double) * 9 * b->R, cudaMemcpyDeviceToHost, b->stream));
+        b->sync();
     });
 }
 

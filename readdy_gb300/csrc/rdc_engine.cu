@@ -746,7 +746,7 @@ __device__ __forceinline__ void replica_body(const EngineDev &E, int r, const Sm
         copy_starts16(reinterpret_cast<uint16_t *>(gstart), reinterpret_cast<const uint16_t *>(cells), nc + 3);
     int rec = st.rec;
     if (D.records && D.count_stride > 0 && (step + 1) % (uint64_t)D.count_stride == 0 && rec < D.max_records) {
-        block_count_types(D.pos[cur], n_final, T, D.records + (size_t)rec * T);
+        block_count_types(D.pos[cur], n_final, T, D.records + (size_t)rec * (D.record_pitch ? (size_t)D.record_pitch : (size_t)T));
         ++rec;
     }
     if (threadIdx.x == 0) {
@@ -860,6 +860,17 @@ __global__ void k_engine_admit(EngineDev E, const int *list, int count, int fill
     }
 }
 
+// current per-type counts of replicas [0, R) as count record `rec` of each (its records array and pitch)
+__global__ void k_engine_record_now(EngineDev E, int R, int T, int rec) {
+    for (int r = blockIdx.x; r < R; r += gridDim.x) {
+        const RepDesc &D = E.desc[r];
+        const RepState st = E.state[r];
+        if (!D.records) continue;
+        const size_t pitch = D.record_pitch ? (size_t)D.record_pitch : (size_t)T;
+        block_count_types(D.pos[st.cur], st.n, T, D.records + (size_t)rec * pitch);
+    }
+}
+
 __global__ void k_engine_count(EngineDev E, int R, int T, unsigned long long *out) {
     for (int r = blockIdx.x; r < R; r += gridDim.x) {
         const RepDesc &D = E.desc[r];
@@ -894,6 +905,52 @@ __device__ inline void engine_forces_of(const RepDesc &D, const RepState &st, co
             if (o1) order1_force(p, tab->o1pots, o1 >> 8, o1 & 0xff, fx, fy, fz, e);
         }
         out[i] = make_float4(fx, fy, fz, 0.f);
+    }
+}
+
+// The pair virial of every listed replica's current state (Context::recordVirial; the sum over pairs of
+// outer(-x_ij, f_i) that calculateOrder2<true> accumulates, CPUCalculateForces.cpp:247-249, seen here once
+// from each side with half the weight), one block per replica, FP32 per thread and FP64 per block, into
+// out (9 doubles per replica, row-major).  The state must be sorted (forces not carried), so that its
+// cell starts are valid; a replica that carries its forces gets NaN.
+template <typename C>
+__device__ inline void engine_virial_of(const RepDesc &D, const RepState &st, const Tables *tab, const C *start,
+                                        double *out) {
+    const GeoR g = geo_r(D.geo);
+    const float4 *pos = D.pos[st.cur];
+    float vir[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < st.n_in; i += blockDim.x) {
+        const float4 p = pos[i];
+        if (itype(p) < 0 || tab->npots == 0) continue;
+        float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+        pair_force_at(i, p, pos, start, g, 1, tab->pair_tab, tab->pair_screen, tab->pots, tab->ntypes, fx, fy, fz, e,
+                      vir);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            acc[k] += (double)vir[k];
+            vir[k] = 0.f;
+        }
+    }
+    for (int k = 0; k < 9; ++k) {
+        const double v = block_sum_double(acc[k]);
+        if (threadIdx.x == 0) out[k] = v;
+    }
+}
+
+__global__ void k_engine_virial(EngineDev E, int R, double *out) {
+    for (int r = blockIdx.x; r < R; r += gridDim.x) {
+        const RepDesc D = E.desc[r];
+        const RepState st = E.state[r];
+        if (st.fvalid) {
+            if (threadIdx.x < 9) out[(size_t)r * 9 + threadIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
+        const Tables *tab = E.tabs + D.table;
+        if (D.smem_cells) engine_virial_of(D, st, tab, reinterpret_cast<const uint16_t *>(D.start), out + (size_t)r * 9);
+        else engine_virial_of(D, st, tab, D.start, out + (size_t)r * 9);
+        __syncthreads();
     }
 }
 
@@ -958,6 +1015,14 @@ void launch_engine_admit(const EngineDev &E, const int *list, int count, bool fi
 
 void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long long *out, cudaStream_t st) {
     if (R > 0) k_engine_count<<<std::min(R, 4 * sm_count()), 256, 0, st>>>(E, R, ntypes, out);
+}
+
+void launch_engine_record_now(const EngineDev &E, int R, int ntypes, int rec, cudaStream_t st) {
+    if (R > 0) k_engine_record_now<<<std::min(R, 4 * sm_count()), 256, 0, st>>>(E, R, ntypes, rec);
+}
+
+void launch_engine_virial(const EngineDev &E, int R, double *out, cudaStream_t st) {
+    if (R > 0) k_engine_virial<<<std::min(R, 4 * sm_count()), 256, 0, st>>>(E, R, out);
 }
 
 void launch_engine_forces(const EngineDev &E, int r, int n, float4 *out, cudaStream_t st) {

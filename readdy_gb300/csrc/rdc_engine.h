@@ -70,6 +70,7 @@ struct RepDesc {
     int table;                   // index into EngineDev::tabs
     int count_stride;            // record counts at t = 0 and after every count_stride steps (0: never)
     int max_records;
+    int64_t record_pitch;        // entries between successive count records of this replica (0: ntypes)
 };
 
 struct RepState {
@@ -108,6 +109,11 @@ void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long lo
 // the force the next step applies to each of the n storage slots of replica r's current state (pair
 // forces carried or walked, plus order-1 potentials) into out (float4 per slot, removed slots zero)
 void launch_engine_forces(const EngineDev &E, int r, int n, float4 *out, cudaStream_t st);
+// current per-type counts of replicas [0, R) written as count record `rec` of each
+void launch_engine_record_now(const EngineDev &E, int R, int ntypes, int rec, cudaStream_t st);
+// pair virial (9 doubles, row-major) of replicas [0, R) on their current states into out (R x 9); NaN for a
+// replica that carries its forces (its state is not sorted)
+void launch_engine_virial(const EngineDev &E, int R, double *out, cudaStream_t st);
 // multiprocessors of the current device
 int sm_count();
 

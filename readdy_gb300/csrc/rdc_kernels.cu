@@ -43,6 +43,7 @@ __global__ void k_integrate_bin(SysDev s, int integrate, int bin) {
     const int n = s.counters[C_N_TOTAL];
     const uint64_t step = s.step[0];
     const GeoR g = geo_r(s.geo);
+    unsigned advanced = 0;
     GRID_STRIDE(i, n) {
         float4 p = s.pos[i];
         const int t = itype(p);
@@ -50,12 +51,19 @@ __global__ void k_integrate_bin(SysDev s, int integrate, int bin) {
             const float4 f = s.force[i];
             p = euler_bd(p, f.x, f.y, f.z, s.id[i], s.seed, step, s.tab->bd_drift[t], s.tab->bd_scale[t], g);
             s.pos[i] = p;
+            ++advanced;
         }
         if (bin) {
             const int b = bin_of(p, s.geo);
             s.bin[i] = b;
             s.rank[i] = atomicAdd(&s.cnt[b], 1);
         }
+    }
+    // particles advanced, summed over steps (the particle-steps of the throughput figures)
+    if (integrate) {
+        advanced = __reduce_add_sync(0xffffffffu, advanced);
+        if ((threadIdx.x & 31) == 0 && advanced) atomicAdd(reinterpret_cast<unsigned long long *>(&s.step[2]),
+                                                           (unsigned long long)advanced);
     }
     // the integrator step counter (Philox key) advances once every block has read it
     if (integrate && last_block_done(s.counters)) s.step[0] = step + 1;

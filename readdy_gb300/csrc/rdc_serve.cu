@@ -10,8 +10,8 @@
 //    every engine step is one persistent launch over all of them, replayed from one CUDA graph, and
 //    requests join and leave between chunks of steps (continuous batching);
 //  * larger requests run as plain per-system simulations (rdc_run: grid-wide kernels replayed from a
-//    CUDA graph) on their own stream and host worker thread, because one CTA per replica would make
-//    their steps the longest of every engine launch.
+//    CUDA graph), each on its own stream, taken by a fixed pool of host worker threads (at most that many
+//    run at once), because one CTA per replica would make their steps the longest of every engine launch.
 // A request's random streams are keyed by its own seed, particle ids and step counter, and its cell grid
 // by its own box, so its result does not depend on which other requests share the GPU.
 #include <cuda_runtime.h>
@@ -21,6 +21,7 @@
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -98,8 +99,7 @@ struct Request {
     void *block = nullptr;
     EngineLayout L{};
     int64_t steps_done = 0;
-    // plain leg
-    std::thread worker;
+    // plain leg (run by a worker of the pool)
     std::atomic<int> worker_done{0};
     int worker_rc = RDC_OK;
     std::string worker_err;
@@ -128,6 +128,13 @@ struct rdc_server {
     std::vector<int64_t> slot_owner;  // engine slot -> request id (0: free)
     std::vector<int64_t> plain_running;
     std::vector<int64_t> unpolled;
+    // worker pool of the per-system leg: admitted requests wait in plain_queue for a worker
+    int plain_workers = 8;
+    std::vector<std::thread> workers;
+    std::deque<Request *> plain_queue;
+    std::mutex plain_mutex;
+    std::condition_variable plain_cv;
+    bool stopping = false;
     // engine state
     EngineDev e{};
     RepDesc *desc_dev = nullptr;
@@ -141,8 +148,13 @@ struct rdc_server {
     cudaGraphExec_t graph = nullptr;
 
     ~rdc_server() {
-        for (auto &kv : requests)
-            if (kv.second->worker.joinable()) kv.second->worker.join();
+        {
+            std::lock_guard<std::mutex> lock(plain_mutex);
+            stopping = true;
+            plain_queue.clear();  // queued requests that no worker took are dropped with the server
+        }
+        plain_cv.notify_all();
+        for (auto &t : workers) t.join();
         if (stream) cudaStreamSynchronize(stream);
         for (auto &kv : requests)
             if (kv.second->block) cudaFreeAsync(kv.second->block, stream);
@@ -205,6 +217,22 @@ struct rdc_server {
         RDC_CUDA(cudaGraphInstantiate(&graph, g, 0));
         cudaGraphDestroy(g);
         RDC_CUDA(cudaStreamSynchronize(stream));
+        for (int k = 0; k < plain_workers; ++k) workers.emplace_back([this] { worker_loop(); });
+    }
+
+    // a pool worker: runs queued per-system requests one after another until the server stops
+    void worker_loop() {
+        for (;;) {
+            Request *q = nullptr;
+            {
+                std::unique_lock<std::mutex> lock(plain_mutex);
+                plain_cv.wait(lock, [this] { return stopping || !plain_queue.empty(); });
+                if (stopping) return;
+                q = plain_queue.front();
+                plain_queue.pop_front();
+            }
+            run_plain(q, device, handler);
+        }
     }
 
     int free_slot() const {
@@ -228,13 +256,16 @@ struct rdc_server {
         }
         std::vector<int64_t> counts((size_t)q->max_records * q->ctx.ntypes, 0);
         int64_t nrec = 0;
+        uint64_t advanced = 0;
         rc = rdc_system_create(&sys, ctx, q->seed);
         if (rc == RDC_OK) rc = rdc_reserve(sys, q->cap);
         if (rc == RDC_OK) rc = rdc_add_particles(sys, q->n, x.data(), t.data(), nullptr);
         if (rc == RDC_OK)
             rc = rdc_run(sys, q->n_steps, q->dt, handler, q->stride, q->max_records > 0 ? counts.data() : nullptr,
                          q->max_records, &nrec);
+        if (rc == RDC_OK) rc = rdc_get_particle_steps(sys, &advanced);  // counted on the device
         if (rc != RDC_OK) q->worker_err = rdc_last_error();
+        q->particle_steps = advanced;
         if (sys) rdc_system_destroy(sys);
         rdc_context_destroy(ctx);
         q->records = std::move(counts);
@@ -249,11 +280,18 @@ struct rdc_server {
             Request &q = *requests[pending.front()];
             if (in_use + q.bytes > budget) break;  // first come, first served: no overtaking
             if (q.plain) {
+                // at most plain_workers per-system requests admitted at once (first come, first served:
+                // the queue waits behind a per-system request until a worker is free)
+                if ((int)plain_running.size() >= plain_workers) break;
                 in_use += q.bytes;
                 q.t_admit = now_s(t0);
                 pending.pop_front();
                 plain_running.push_back(q.id);
-                q.worker = std::thread(run_plain, &q, device, handler);
+                {
+                    std::lock_guard<std::mutex> lock(plain_mutex);
+                    plain_queue.push_back(&q);
+                }
+                plain_cv.notify_one();
                 continue;
             }
             const int slot = free_slot();
@@ -385,20 +423,9 @@ struct rdc_server {
         for (auto it = plain_running.begin(); it != plain_running.end();) {
             Request &q = *requests[*it];
             if (q.worker_done.load()) {
-                q.worker.join();
                 q.status = q.worker_rc;
                 q.message = q.worker_err;
-                // particle-steps of the plain leg from its count records (trapezoid over each stride),
-                // or the initial count times the steps when it records nothing
-                if (q.n_records < 2) plain_particle_steps += (uint64_t)q.n * (uint64_t)q.n_steps;
-                for (int64_t r = 1; r < q.n_records; ++r) {
-                    int64_t a = 0, b = 0;
-                    for (int t = 0; t < q.ctx.ntypes; ++t) {
-                        a += q.records[(size_t)(r - 1) * q.ctx.ntypes + t];
-                        b += q.records[(size_t)r * q.ctx.ntypes + t];
-                    }
-                    plain_particle_steps += (uint64_t)((a + b) / 2) * (uint64_t)q.stride;
-                }
+                plain_particle_steps += q.particle_steps;  // counted on the device by the integrator
                 finish(q);
                 ++finished;
                 it = plain_running.erase(it);

@@ -225,6 +225,12 @@ class CUDAKernel:
         N.check(self._lib.rdc_count_types(self._h, _p(out, C.c_int64)))
         return out
 
+    def particle_steps(self) -> int:
+        """Particles advanced by the integrator since creation, summed over steps."""
+        v = C.c_uint64()
+        N.check(self._lib.rdc_get_particle_steps(self._h, C.byref(v)))
+        return int(v.value)
+
     def reaction_counts(self):
         n = max(self.context.n_reactions, 1)
         out = np.zeros(n, np.int64)

@@ -137,6 +137,80 @@ def test_carried_forces_of_widened_replicas_match_oracle(rg, handler):
         assert err.max() <= FORCE_RTOL
 
 
+def test_streamed_count_records_equal_the_per_system_records(rg):
+    """Count records streamed from a batch (switched on after 7 steps, polled twice while steps continue)
+    equal, record for record, the counts of the same replicas run alone through the per-system path, and
+    carry the time steps of ReaDDy's time series."""
+    from readdy_gb300.batch import ReplicaBatch, replica_seed
+    from readdy_gb300 import io
+    rng = np.random.default_rng(41)
+    sizes = [300, 1200, 2500]
+    specs, poss, typess, boxes = [], [], [], []
+    for n in sizes:
+        L = _box(n)
+        spec, pos, types = abc_spec(n=n, box=L, seed=int(rng.integers(1 << 30)))
+        specs.append(spec)
+        poss.append(f32(pos))
+        typess.append(types)
+        boxes.append((L, L, L))
+    b = ReplicaBatch(make_context(specs[0]), boxes, [2 * n for n in sizes], seed=55)
+    b.set_particles(poss, typess)
+    b.configure(handler=1, dt=1e-3, cell_width_scale=1.0, threads_per_block=256)
+    b.step(7)
+    b.record_counts(stride=10, max_records=16)
+    b.step(23)
+    s1, c1 = b.poll_count_records()
+    b.step(40)
+    s2, c2 = b.poll_count_records()
+    steps, counts = np.concatenate([s1, s2]), np.concatenate([c1, c2])
+    np.testing.assert_array_equal(steps, [7, 10, 20, 30, 40, 50, 60, 70])
+    np.testing.assert_array_equal(counts[-1], b.count_types())
+    lay = io.batch_n_particles_layout(steps, counts)
+    for r, n in enumerate(sizes):
+        k = rg.CUDAKernel(make_context(specs[r]), seed=replica_seed(55, r))
+        k.add_particles(poss[r], typess[r])
+        ref = k.run(70, 1e-3, handler=1, count_stride=10)  # t = 0, 10, ..., 70
+        np.testing.assert_array_equal(counts[1:, r, :], ref[1:])
+        np.testing.assert_array_equal(lay[f"readdy/observables/n_particles/replica_{r}/data"][1:], ref[1:])
+
+
+def test_batch_virial_matches_oracle(rg):
+    """The Virial observable of replicas of the batch (forces summed over the sorted state, carried forces
+    off), after a few steps of dynamics with reactions, against the oracle's virial of the same positions:
+    each entry within 1e-5 of the largest entry; a batch that carries its forces refuses."""
+    from readdy_gb300.batch import ReplicaBatch
+    rng = np.random.default_rng(29)
+    sizes = [3000, 800, 14000, 25000]
+    caps = [2 * n if n < 25000 else 70000 for n in sizes]
+    specs, poss, typess, boxes = [], [], [], []
+    for n in sizes:
+        L = _box(n)
+        spec, pos, types = abc_spec(n=n, box=L, seed=int(rng.integers(1 << 30)))
+        specs.append(spec)
+        poss.append(f32(pos))
+        typess.append(types)
+        boxes.append((L, L, L))
+    b = ReplicaBatch(make_context(specs[0]), boxes, caps, seed=3)
+    b.set_particles(poss, typess)
+    b.configure(handler=1, dt=1e-3, cell_width_scale=1.0, threads_per_block=512)
+    with pytest.raises(RuntimeError):
+        b.virial()
+    b.set_carry_forces(False)
+    b.step(10)
+    b.synchronize()
+    vir = b.virial()
+    for r in range(len(sizes)):
+        p, t, ids = b.get_particles(r)
+        (p, t) = by_id(ids, p, t)
+        o = make_oracle(dict(specs[r], box=boxes[r], reactions=[]), n_threads=8)
+        o.set_record_virial(True)
+        o.add_particles(p, t)
+        o.nl_setup(o.calculate_max_cutoff())
+        o.calculate_forces()
+        v_ref = o.virial()
+        np.testing.assert_allclose(vir[r], v_ref, rtol=0, atol=1e-5 * np.abs(v_ref).max())
+
+
 # ---- ensembles through the batch against ensembles of oracle runs ----------------------------------
 
 SYSTEMS = {

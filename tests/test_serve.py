@@ -75,3 +75,25 @@ def test_admission_respects_the_budget_and_the_submit_order(rg):
         mass = c @ np.asarray(s.mass)
         assert np.all(mass == len(s.positions))  # the network conserves mass units
         assert res[k]["finish"] >= res[k]["admit"] >= res[k]["submit"]
+
+
+def test_particle_steps_are_counted_on_the_device_in_both_legs(rg):
+    """Requests whose networks only convert species keep their particle count, so the particle-steps the
+    server reports (engine leg and per-system leg, both counted on the device) are the sum of N x steps."""
+    from readdy_gb300.serve import Server, RequestSpec
+    rng = np.random.default_rng(3)
+    specs = []
+    for n, steps in [(400, 120), (900, 80), (5000, 60), (6000, 50)]:
+        L = float(np.float32((n / 0.3) ** (1 / 3)))
+        specs.append(RequestSpec(arrival=0.0, n_types=2, diffusion=[1.0, 0.5], box=L,
+                                 reactions=[("conversion", (0, 1, 0.5)), ("conversion", (1, 0, 0.5))],
+                                 positions=(rng.random((n, 3)) - 0.5) * L, types=np.zeros(n, np.int32),
+                                 n_steps=steps, seed=int(rng.integers(1 << 40)), count_stride=10, mass=[1, 1]))
+    srv = Server(1 << 32, plain_threshold=4096)  # the two larger requests take the per-system leg
+    for s in specs:
+        srv.submit(s.context(), s.positions, s.types, s.n_steps, s.dt, s.count_stride, s.seed)
+    done = 0
+    while done < len(specs):
+        srv.progress(32)
+        done += len(srv.poll())
+    assert srv.stats()["particle_steps"] == sum(len(s.positions) * s.n_steps for s in specs)
