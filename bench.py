@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--single-systems", type=int, default=1, help="time the three single-system workloads (0: skip)")
     ap.add_argument("--plain-threshold", type=int, default=4096,
                     help="requests above this many particles take the per-system leg of the server")
+    ap.add_argument("--plain-workers", type=int, default=8,
+                    help="per-system requests the server runs at once, each on its own stream")
     ap.add_argument("--profile-system", choices=["abc_2k", "crowded_200k", "polymer_200k"], default=None,
                     help="only run one single-system workload through the per-system path (--warmup then "
                          "--steps steps; for profiler captures of its kernels)")
@@ -389,13 +391,13 @@ def profile_system(name, warmup, steps):
     return {"profile_system": name, "particles": int(n), "steps": steps, "ms_per_step": dt * 1e3}
 
 
-def serving(n_requests, time_limit, plain_threshold, seed=7):
+def serving(n_requests, time_limit, plain_threshold, seed=7, plain_workers=8):
     """The served form on the first n_requests of the seeded serving stream (Poisson arrivals at 20/s;
     2-6 species; N log-uniform in [500, 200000] at density 0.1-0.5; 1k-100k steps; counts every 100
     steps), replayed in wall-clock time against a 150 GB device-memory budget."""
     from readdy_gb300.serve import Server, run_stream, serving_workload
     specs = serving_workload(seed=seed, n_requests=n_requests)
-    srv = Server(150 << 30, plain_threshold=plain_threshold)
+    srv = Server(150 << 30, plain_threshold=plain_threshold, plain_workers=plain_workers)
     res, wall, ps = run_stream(srv, specs, max_steps=100, time_limit=time_limit)
     lat = np.array(sorted(r["finish"] - r["submit"] for r in res.values()))
     queue = np.array(sorted(r["admit"] - r["submit"] for r in res.values()))
@@ -408,7 +410,7 @@ def serving(n_requests, time_limit, plain_threshold, seed=7):
             "offered_particle_steps": float(sum(len(s.positions) * s.n_steps for s in specs)),
             "completed_particle_steps": done_ps,
             "failed": int(sum(r["status"] != 0 for r in res.values())),
-            "plain_threshold": plain_threshold,
+            "plain_threshold": plain_threshold, "plain_workers": plain_workers,
             "particle_steps": "counted on the device in both legs (engine counter, per-system integrator counter)",
             "sample": f"first {n_requests} requests of the seeded 2000-request stream (seed {seed}), arrivals at "
                       f"20/s replayed in wall-clock time, 150 GB budget, stopped after {time_limit:.0f} s; latency "
@@ -460,7 +462,8 @@ def run_gb300(args, rank, world):
         pick = np.random.default_rng(args.seed + 99)
         oat = one_at_a_time(ns, boxes, pos, types, seed, 64, 50, pick)
         _, _, cpu = reference_cpu(ns, boxes, pos, types, args.seed, args.steps, args.warmup, args.cpu_seconds)
-        served = serving(args.serve_requests, args.serve_seconds, args.plain_threshold) if args.serve_requests else None
+        served = (serving(args.serve_requests, args.serve_seconds, args.plain_threshold, plain_workers=args.plain_workers)
+                  if args.serve_requests else None)
         singles = single_systems() if args.single_systems else None
         peak, peak_kind = measured_peaks()
         n_avg = (ps1 - ps0) / args.steps

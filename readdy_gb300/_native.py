@@ -110,6 +110,7 @@ def _sig(lib):
         "rdc_batch_synchronize": (i, [vp]),
         "rdc_server_create": (i, [vpp, u64, i, i, i64]),
         "rdc_server_destroy": (i, [vp]),
+        "rdc_server_set_plain_workers": (i, [vp, i]),
         "rdc_server_request_bytes": (i, [vp, i64, i64, i64, i64, P(u64), P(i)]),
         "rdc_server_submit": (i, [vp, vp, i64, P(d), P(i), i64, d, i64, u64, P(i64)]),
         "rdc_server_progress": (i, [vp, i64, P(i64)]),

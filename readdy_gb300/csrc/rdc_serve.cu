@@ -503,6 +503,16 @@ int rdc_server_create(rdc_server **out, uint64_t budget_bytes, int max_active, i
     });
 }
 
+int rdc_server_set_plain_workers(rdc_server *s, int n) {
+    SERVE_CALL({
+        if (!s) throw std::invalid_argument("null argument");
+        if (n < 1 || n > 256) throw std::invalid_argument("plain workers must be in [1, 256]");
+        // the pool only grows; a smaller number lowers how many per-system requests are admitted at once
+        while ((int)s->workers.size() < n) s->workers.emplace_back([s] { s->worker_loop(); });
+        s->plain_workers = n;
+    });
+}
+
 int rdc_server_destroy(rdc_server *s) {
     delete s;
     return RDC_OK;

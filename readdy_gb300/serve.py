@@ -27,12 +27,14 @@ def _p(a, t):
 
 class Server:
     def __init__(self, budget_bytes: int, max_active: int = 1024, handler: int = N.GILLESPIE,
-                 plain_threshold: int = 4096):
+                 plain_threshold: int = 4096, plain_workers: int = 8):
         self._lib = N.load()
         h = C.c_void_p()
         N.check(self._lib.rdc_server_create(C.byref(h), int(budget_bytes), int(max_active), int(handler),
                                             int(plain_threshold)))
         self._h = h
+        N.check(self._lib.rdc_server_set_plain_workers(h, int(plain_workers)))
+        self.plain_workers = int(plain_workers)
         self.budget_bytes = int(budget_bytes)
         self.plain_threshold = int(plain_threshold)
         self.handler = handler
