@@ -217,9 +217,10 @@ size_t engine_smem_bytes(int max_events) {
 // The candidate pass of block_events and the pair forces of the same sorted state in one stencil walk
 // per particle: the walk that sums particle i's pair forces also finds its reaction partners j > i,
 // and force[i] receives the sum (zero outside the cells).  The walk runs without block barriers, like
-// the plain force walk.  It keeps up to two partner tuples in registers and lists them after the
-// walk (measured: an atomic list append inside the divergent candidate loop made the walk 8x slower);
-// a particle with more partners lists its tuples by its own event walk.  The list holds up to `room`
+// the plain force walk.  It keeps up to two partner candidates in registers, tries their reactions
+// after the walk and lists the tuples then (measured: an atomic list append inside the divergent
+// candidate loop made the walk 8x slower); a particle with more candidates lists its tuples by its
+// own event walk.  The list holds up to `room`
 // tuples in global scratch (tp1, tp2, tr) and the coins are drawn after it with all lanes converged;
 // a list that overflows is dropped and block_events generates the tuples again.  Tuples, coins and
 // forces are those of block_events and pair_force_at on their own.
@@ -249,15 +250,25 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    // per type: the largest force or reaction screen, as far as the walk of a particle of that type reaches
+    // per type: the largest force or reaction screen, as far as the walk of a particle of that type reaches,
+    // and the types it has a pair potential or a pair reaction with
     __shared__ float sh_reach[MAX_TYPES];
+    __shared__ uint32_t sh_mask[MAX_TYPES];
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
         float r2 = 0.f;
+        uint32_t m = 0u;
         for (int u = 0; u < T; ++u) {
-            if (S.tab[t * T + u]) r2 = fmaxf(r2, S.screen[t * T + u]);
-            if (rt.o2_any[t] && rt.o2_tab[t * rt.T + u]) r2 = fmaxf(r2, rt.screen[t * rt.T + u]);
+            if (S.tab[t * T + u]) {
+                r2 = fmaxf(r2, S.screen[t * T + u]);
+                m |= 1u << u;
+            }
+            if (rt.o2_any[t] && rt.o2_tab[t * rt.T + u]) {
+                r2 = fmaxf(r2, rt.screen[t * rt.T + u]);
+                m |= 1u << u;
+            }
         }
         sh_reach[t] = r2;
+        sh_mask[t] = m;
     }
     __syncthreads();
     for (;;) {
@@ -278,26 +289,40 @@ __device__ __forceinline__ void block_events_forces(int n, int n_in, const float
                 const float *rsrow = rt.screen + ti * rt.T;
                 // the cells walked reach as far as the largest force or reaction screen of i's type (a walking
                 // particle is inside the cells, so its type's reaction screens count when it has any)
-                const float reach2 = sh_reach[ti];
-                auto partner = [&](int j, float4 q, int tj, float d2s) {
+                // partner candidates j > i inside a reaction screen, in candidate order; their reactions are
+                // tried after the walk, with the lanes converged, instead of inside the divergent loop
+                int c0 = 0, c1 = 0, nc = 0;
+                auto partner = [&](int j, float4, int tj, float d2s) {
                     if (!pairs || j < i) return;
                     const int o2 = rrow[tj];
                     if (o2 == 0 || d2s > rsrow[tj]) return;
-                    const PairGeom g0 = pair_geom(p, q, g);
-                    for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
-                        const int r = rt.o2_list[k];
-                        const ReactionDev &R = rt.rx[r];
-                        if (!R.active) continue;
-                        PairGeom gg = g0;
-                        if (within(g0, gg, p, q, g, R.educt_distance2f, R.band, R.educt_distance2)) {
-                            if (nt == 0) t0 = j | (r << 16);
-                            else if (nt == 1) t1 = j | (r << 16);
-                            ++nt;
-                        }
-                    }
+                    if (nc == 0) c0 = j;
+                    else if (nc == 1) c1 = j;
+                    ++nc;
                 };
                 pair_force_at(i, p, pos, start, g, 1, S.tab, S.screen, S.pots, T, fx, fy, fz, e, nullptr, partner,
-                              reach2);
+                              sh_reach[ti], sh_mask[ti]);
+                if (nc > 2) {
+                    nt = 3;  // more candidates than registers: its own event walk lists the tuples
+                } else {
+                    for (int c = 0; c < nc; ++c) {
+                        const int j = c == 0 ? c0 : c1;
+                        const float4 q = pos[j];
+                        const int o2 = rrow[itype(q)];
+                        const PairGeom g0 = pair_geom(p, q, g);
+                        for (int k = (o2 >> 8); k < (o2 >> 8) + (o2 & 0xff); ++k) {
+                            const int r = rt.o2_list[k];
+                            const ReactionDev &R = rt.rx[r];
+                            if (!R.active) continue;
+                            PairGeom gg = g0;
+                            if (within(g0, gg, p, q, g, R.educt_distance2f, R.band, R.educt_distance2)) {
+                                if (nt == 0) t0 = j | (r << 16);
+                                else if (nt == 1) t1 = j | (r << 16);
+                                ++nt;
+                            }
+                        }
+                    }
+                }
             }
             if (nt > 2) {
                 event_tuples_at(i, true, pos, start, g, 1, rt, push);
