@@ -53,6 +53,9 @@ int rdc_set_device(int device);
 int rdc_context_create(rdc_context **out, const double box[3], const int periodic[3], double kbt, int n_types,
                        const double *diffusion);
 int rdc_context_destroy(rdc_context *ctx);
+/* ParticleTypeRegistry::add(name, D, flavor) (include/readdy/model/ParticleTypeRegistry.h:58-63,114):
+ * 0 NORMAL (the default), 1 TOPOLOGY, 2 MEMBRANE.  Read by rdc_break_bonds. */
+int rdc_context_set_particle_flavor(rdc_context *ctx, int type, int flavor);
 /* Context::recordVirial (include/readdy/model/Context.h:168-174): systems created from ctx afterwards
  * accumulate the pair virial in CalculateForces */
 int rdc_context_set_record_virial(rdc_context *ctx, int record);
@@ -125,6 +128,31 @@ int rdc_add_particles(rdc_system *s, int64_t n, const double *positions3, const 
  * (readdy/main/model/topologies/GraphTopology.cpp:59-143, include/graphs/bits/Graph_detail.h:39-76) */
 int rdc_add_topology(rdc_system *s, int64_t n, const double *positions3, const int *types, int64_t n_edges,
                      const int64_t *edges2, uint64_t *ids_out);
+/* StateModel::addTopology(type, particles) (StateModel.h:69-117): rdc_add_topology with a topology type
+ * id (>= 0; rdc_add_topology uses 0) that the topology and the pieces it breaks into keep */
+int rdc_add_topology_typed(rdc_system *s, int topology_type, int64_t n, const double *positions3, const int *types,
+                           int64_t n_edges, const int64_t *edges2, uint64_t *ids_out);
+/* ActionFactory::breakBonds(timeStep, BreakConfig) + perform (include/readdy/model/actions/Actions.h:190-290):
+ * BreakConfig::addBreakablePair(type1[k], type2[k], threshold_energy[k], rate[k]) for k < n_pairs (pairs
+ * are unordered).  Every graph edge whose harmonic bond energy exceeds its type pair's threshold breaks
+ * with probability 1 - exp(-rate time_step).  A topology that falls apart becomes its connected
+ * components, of the same topology type; a component of one particle whose type has NORMAL flavor leaves
+ * the topologies (include/readdy/model/actions/Utils.h:59-79).  Bonds, angles and dihedrals are derived
+ * again from the remaining edges.  Unlike the reference action, which also adds the evaluated bonds'
+ * forces to the particles' force accumulators (CPUTopologyActions.cpp:55-70), this leaves the forces as
+ * they were until the next rdc_calculate_forces.  n_broken (may be NULL) receives the edges removed. */
+int rdc_break_bonds(rdc_system *s, double time_step, int n_pairs, const int *type1, const int *type2,
+                    const double *threshold_energy, const double *rate, int64_t *n_broken);
+/* StateModel::getTopologies (StateModel.h:69-117): the active topologies as CSR, topology k has type
+ * topology_types[k] and the particles ids[offsets[k] .. offsets[k+1]) (offsets holds n_topologies + 1
+ * entries).  n_topologies and n_ids are written first; RDC_ERR_CAPACITY if either capacity is smaller.
+ * Any output array may be NULL. */
+int rdc_get_topologies(rdc_system *s, int64_t capacity_topologies, int *topology_types, int64_t *offsets,
+                       int64_t capacity_ids, uint64_t *ids, int64_t *n_topologies, int64_t *n_ids);
+/* GraphTopology::graph().edges() of every active topology, in the order of rdc_get_topologies: topology k
+ * has the edges edges2[2e], edges2[2e+1] (particle ids) for e in [offsets[k], offsets[k+1]) */
+int rdc_get_topology_edges(rdc_system *s, int64_t capacity_topologies, int64_t *offsets, int64_t capacity_edges,
+                           uint64_t *edges2, int64_t *n_topologies, int64_t *n_edges);
 /* active particle count (StateModel::getParticles().size()) */
 int rdc_get_n_particles(rdc_system *s, int64_t *n);
 /* StateModel::getParticles: positions, types and ids of active particles; order is the device's

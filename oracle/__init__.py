@@ -24,9 +24,8 @@ GILLESPIE = 1
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (g++, a few seconds)."""
-    if force or not os.path.exists(_LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle with its Makefile (g++, a few seconds; make skips an up-to-date library)."""
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB_PATH
 
 
@@ -63,6 +62,14 @@ def _load():
             "orc_add_harmonic_bonds": (i, [vp, i, P(i), P(d), P(d)]),
             "orc_add_harmonic_angles": (i, [vp, i, P(i), P(d), P(d)]),
             "orc_add_cosine_dihedrals": (i, [vp, i, P(i), P(d), P(d), P(d)]),
+            "orc_set_particle_flavor": (i, [vp, i, i]),
+            "orc_configure_harmonic_bond": (i, [vp, i, i, d, d]),
+            "orc_configure_harmonic_angle": (i, [vp, i, i, i, d, d]),
+            "orc_configure_cosine_dihedral": (i, [vp, i, i, i, i, d, d, d]),
+            "orc_add_topology": (i, [vp, i, i, P(d), P(i), i, P(i), P(u64)]),
+            "orc_break_bonds": (i, [vp, d, i, P(i), P(i), P(d), P(d), P(i64)]),
+            "orc_get_topologies": (i, [vp, P(i), P(i64), P(u64), P(i64), P(i64)]),
+            "orc_get_topology_edges": (i, [vp, P(i64), P(u64), P(i64)]),
             "orc_add_particles": (i, [vp, i, P(d), P(i)]),
             "orc_n_particles": (i, [vp]),
             "orc_n_entries": (i, [vp]),
@@ -217,6 +224,57 @@ class OracleSystem:
         p = np.ascontiguousarray(np.broadcast_to(phi0, (n,)), dtype=np.float64)
         return self._check(self._lib.orc_add_cosine_dihedrals(self._h, n, _ptr(idx, C.c_int), _ptr(k, C.c_double),
                                                               _ptr(m, C.c_double), _ptr(p, C.c_double)))
+
+    # topology registry, flavors, topologies, BreakBonds
+    def set_particle_flavor(self, t, flavor):
+        return self._check(self._lib.orc_set_particle_flavor(self._h, t, flavor))
+
+    def configure_harmonic_bond(self, t1, t2, k, l0):
+        return self._check(self._lib.orc_configure_harmonic_bond(self._h, t1, t2, k, l0))
+
+    def configure_harmonic_angle(self, t1, t2, t3, k, theta0):
+        return self._check(self._lib.orc_configure_harmonic_angle(self._h, t1, t2, t3, k, theta0))
+
+    def configure_cosine_dihedral(self, t1, t2, t3, t4, k, multiplicity, phi0):
+        return self._check(self._lib.orc_configure_cosine_dihedral(self._h, t1, t2, t3, t4, k, multiplicity, phi0))
+
+    def add_topology(self, positions, types, edges, topology_type=0):
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(np.broadcast_to(types, (len(pos),)), dtype=np.int32)
+        e = np.ascontiguousarray(np.asarray(edges, dtype=np.int32).reshape(-1, 2))
+        ids = np.zeros(len(pos), np.uint64)
+        self._check(self._lib.orc_add_topology(self._h, topology_type, len(pos), _ptr(pos, C.c_double),
+                                               _ptr(t, C.c_int), len(e), _ptr(e, C.c_int), _ptr(ids, C.c_uint64)))
+        return ids
+
+    def break_bonds(self, dt, breakable_pairs):
+        pairs = list(breakable_pairs)
+        t1 = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
+        t2 = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
+        thr = np.ascontiguousarray([p[2] for p in pairs], dtype=np.float64)
+        rate = np.ascontiguousarray([p[3] for p in pairs], dtype=np.float64)
+        nb = C.c_int64()
+        self._check(self._lib.orc_break_bonds(self._h, dt, len(pairs), _ptr(t1, C.c_int), _ptr(t2, C.c_int),
+                                              _ptr(thr, C.c_double), _ptr(rate, C.c_double), C.byref(nb)))
+        return nb.value
+
+    def topologies(self):
+        """[(topology type, particle ids[] uint64)]"""
+        nt, ni = C.c_int64(), C.c_int64()
+        self._lib.orc_get_topologies(self._h, None, None, None, C.byref(nt), C.byref(ni))
+        types = np.zeros(nt.value, np.int32); off = np.zeros(nt.value + 1, np.int64); ids = np.zeros(ni.value, np.uint64)
+        self._lib.orc_get_topologies(self._h, _ptr(types, C.c_int), _ptr(off, C.c_int64), _ptr(ids, C.c_uint64),
+                                     C.byref(nt), C.byref(ni))
+        return [(int(types[k]), ids[off[k]:off[k + 1]]) for k in range(nt.value)]
+
+    def topology_edges(self):
+        """[(m, 2) particle-id pairs] per topology, in the order of topologies()"""
+        ne = C.c_int64()
+        nt = len(self.topologies())
+        self._lib.orc_get_topology_edges(self._h, None, None, C.byref(ne))
+        off = np.zeros(nt + 1, np.int64); e = np.zeros((ne.value, 2), np.uint64)
+        self._lib.orc_get_topology_edges(self._h, _ptr(off, C.c_int64), _ptr(e, C.c_uint64), C.byref(ne))
+        return [e[off[k]:off[k + 1]] for k in range(nt)]
 
     # particles
     def add_particles(self, positions, types):

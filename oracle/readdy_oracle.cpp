@@ -30,6 +30,7 @@
 #include <stdexcept>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -386,6 +387,28 @@ struct orc_system {
     std::vector<Bond> bonds;
     std::vector<Angle> angles;
     std::vector<Dihedral> dihedrals;
+    // terms given explicitly (orc_add_harmonic_bonds and friends); configureTopologies keeps them
+    std::vector<Bond> fixedBonds;
+    std::vector<Angle> fixedAngles;
+    std::vector<Dihedral> fixedDihedrals;
+
+    // TopologyRegistry potential configuration (include/readdy/api/PotentialConfiguration.h:136-161) and
+    // particle flavors (ParticleTypeRegistry.h:58-63)
+    struct BondCfg { int t1, t2; double k, l0; };
+    struct AngleCfg { int t1, t2, t3; double k, theta0; };
+    struct DihedralCfg { int t1, t2, t3, t4; double k, mult, phi0; };
+    std::vector<BondCfg> bondCfg;
+    std::vector<AngleCfg> angleCfg;
+    std::vector<DihedralCfg> dihedralCfg;
+    std::vector<int> flavor;
+    // topologies: type, vertices (particle ids, in vertex order) and edges (vertex pairs)
+    struct Graph {
+        int type = 0;
+        std::vector<uint64_t> ids;
+        std::vector<std::pair<int, int>> edges;
+    };
+    std::vector<Graph> graphs;
+    uint64_t breakCalls = 0;
 
     std::vector<Entry> entries;
     std::vector<size_t> blanks;
@@ -409,6 +432,7 @@ struct orc_system {
         : kbt(kbt_), nTypes(nt), radius(r), pool(nthreads) {
         for (int d = 0; d < 3; ++d) { box.L[d] = b[d]; box.pbc[d] = p[d] != 0; }
         D.assign(diff, diff + nt);
+        flavor.assign(nt, 0);
         o1.resize(nt);
         pot1.resize(nt);
         std::seed_seq ss{(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32), 0x5eedu};
@@ -417,6 +441,150 @@ struct orc_system {
         for (int t = 0; t < pool.size(); ++t) rng.emplace_back(seeds[t] ^ (uint64_t(t) << 32));
     }
     ~orc_system() { for (auto r : reactions) delete r; }
+
+    using IdMap = std::unordered_map<uint64_t, size_t>;
+    IdMap idMap() const {
+        IdMap m;
+        for (size_t i = 0; i < entries.size(); ++i)
+            if (!entries[i].deactivated) m[entries[i].id] = i;
+        return m;
+    }
+    static size_t indexOf(const IdMap &m, uint64_t id) {
+        auto it = m.find(id);
+        if (it == m.end()) throw std::invalid_argument("no active particle with id " + std::to_string(id));
+        return it->second;
+    }
+
+    /* GraphTopology::configure (readdy/main/model/topologies/GraphTopology.cpp:59-143) over
+     * Graph::findNTuples (include/graphs/bits/Graph_detail.h:39-76); the configuration lookups are
+     * reversal-symmetric (PotentialConfiguration.h:136-161) */
+    void configureGraph(const Graph &g, const IdMap &ids) {
+        const size_t n = g.ids.size();
+        std::vector<std::vector<int>> nbrs(n);
+        for (auto &e : g.edges) {
+            nbrs[e.first].push_back(e.second);
+            nbrs[e.second].push_back(e.first);
+        }
+        std::vector<size_t> pidx(n);
+        std::vector<int> ty(n);
+        for (size_t v = 0; v < n; ++v) {
+            pidx[v] = indexOf(ids, g.ids[v]);
+            ty[v] = entries[pidx[v]].type;
+        }
+        auto pair_cb = [&](int a, int b) {
+            bool found = false;
+            for (auto &c : bondCfg)
+                if ((c.t1 == ty[a] && c.t2 == ty[b]) || (c.t1 == ty[b] && c.t2 == ty[a])) {
+                    bonds.push_back(Bond{pidx[a], pidx[b], c.k, c.l0});
+                    found = true;
+                }
+            if (!found) throw std::invalid_argument("an edge has no bond configured");
+        };
+        auto triple_cb = [&](int a, int b, int c3) {
+            for (auto &c : angleCfg)
+                if ((c.t1 == ty[a] && c.t2 == ty[b] && c.t3 == ty[c3]) || (c.t1 == ty[c3] && c.t2 == ty[b] && c.t3 == ty[a]))
+                    angles.push_back(Angle{pidx[a], pidx[b], pidx[c3], c.k, c.theta0});
+        };
+        auto quad_cb = [&](int a, int b, int c3, int d4) {
+            for (auto &c : dihedralCfg) {
+                const bool fwd = c.t1 == ty[a] && c.t2 == ty[b] && c.t3 == ty[c3] && c.t4 == ty[d4];
+                const bool bwd = c.t1 == ty[d4] && c.t2 == ty[c3] && c.t3 == ty[b] && c.t4 == ty[a];
+                if (fwd || bwd) dihedrals.push_back(Dihedral{pidx[a], pidx[b], pidx[c3], pidx[d4], c.k, c.mult, c.phi0});
+            }
+        };
+        std::vector<char> visited(n, 0);
+        for (size_t v1 = 0; v1 < n; ++v1) {
+            visited[v1] = 1;
+            for (int v2 : nbrs[v1]) {
+                if (!visited[v2]) {
+                    pair_cb((int)v1, v2);
+                    for (int v3 : nbrs[v1])
+                        if (v3 != v2)
+                            for (int v4 : nbrs[v2])
+                                if (v4 != (int)v1 && v4 != v3) quad_cb(v3, (int)v1, v2, v4);
+                }
+                for (int w : nbrs[v1])
+                    if (w != v2 && w < v2) triple_cb(w, (int)v1, v2);
+            }
+        }
+    }
+    void configureTopologies() {
+        bonds = fixedBonds;
+        angles = fixedAngles;
+        dihedrals = fixedDihedrals;
+        const IdMap ids = idMap();
+        for (auto &g : graphs) configureGraph(g, ids);
+    }
+
+    /* BreakBonds::genericPerform (include/readdy/model/actions/Actions.h:236-290): per topology and per
+     * edge, the energy of the edge's bond configurations (evaluateEdgeEnergy, :292-342; harmonic bond
+     * energy of BondedPotential.h) against the type pair's threshold, then a coin
+     * u < 1 - exp(-rate dt); the topology without the removed edges splits into its connected
+     * components (StructuralTopologyReaction.cpp:70-130), one-particle components of NORMAL flavor
+     * leave the topologies (include/readdy/model/actions/Utils.h:52-81, GraphTopology.cpp:161-173) */
+    int64_t breakBonds(double dt, int n, const int *t1, const int *t2, const double *thr, const double *rate) {
+        std::map<std::pair<int, int>, std::pair<double, double>> cfg;  // unordered pair -> (threshold, rate)
+        for (int k = 0; k < n; ++k) cfg[{std::min(t1[k], t2[k]), std::max(t1[k], t2[k])}] = {thr[k], rate[k]};
+        ++breakCalls;
+        int64_t removed = 0;
+        const IdMap idx = idMap();
+        std::vector<Graph> result;
+        for (auto &g : graphs) {
+            std::vector<char> gone(g.edges.size(), 0);
+            for (size_t e = 0; e < g.edges.size(); ++e) {
+                const Entry &a = entries[indexOf(idx, g.ids[g.edges[e].first])];
+                const Entry &b = entries[indexOf(idx, g.ids[g.edges[e].second])];
+                double energy = 0;
+                const double d = norm(box.shortest(a.pos, b.pos));
+                for (auto &c : bondCfg)
+                    if ((c.t1 == a.type && c.t2 == b.type) || (c.t1 == b.type && c.t2 == a.type))
+                        energy += c.k * (d - c.l0) * (d - c.l0);
+                auto it = cfg.find({std::min(a.type, b.type), std::max(a.type, b.type)});
+                if (it != cfg.end() && energy > it->second.first && uniform(0) < 1 - std::exp(-it->second.second * dt)) {
+                    gone[e] = 1;
+                    ++removed;
+                }
+            }
+            Graph kept;
+            kept.type = g.type;
+            kept.ids = g.ids;
+            for (size_t e = 0; e < g.edges.size(); ++e)
+                if (!gone[e]) kept.edges.push_back(g.edges[e]);
+            // connected components (Graph::connectedComponents), vertices in their graph order
+            const size_t nv = kept.ids.size();
+            std::vector<int> comp(nv, -1);
+            std::vector<std::vector<int>> nb(nv);
+            for (auto &e : kept.edges) { nb[e.first].push_back(e.second); nb[e.second].push_back(e.first); }
+            int nc = 0;
+            for (size_t v = 0; v < nv; ++v) {
+                if (comp[v] >= 0) continue;
+                std::vector<int> todo{(int)v};
+                comp[v] = nc;
+                while (!todo.empty()) {
+                    int u = todo.back();
+                    todo.pop_back();
+                    for (int w : nb[u]) if (comp[w] < 0) { comp[w] = nc; todo.push_back(w); }
+                }
+                ++nc;
+            }
+            if (nc == 1) { result.push_back(std::move(kept)); continue; }
+            std::vector<Graph> parts(nc);
+            std::vector<int> local(nv);
+            for (size_t v = 0; v < nv; ++v) {
+                local[v] = (int)parts[comp[v]].ids.size();
+                parts[comp[v]].ids.push_back(kept.ids[v]);
+                parts[comp[v]].type = kept.type;
+            }
+            for (auto &e : kept.edges) parts[comp[e.first]].edges.push_back({local[e.first], local[e.second]});
+            for (auto &part : parts) {
+                const bool normal = part.ids.size() == 1 && flavor[entries[indexOf(idx, part.ids[0])].type] == 0;
+                if (!normal) result.push_back(std::move(part));
+            }
+        }
+        graphs = std::move(result);
+        configureTopologies();
+        return removed;
+    }
 
     static std::pair<int, int> key(int a, int b) { return {std::min(a, b), std::max(a, b)}; }
 
@@ -1143,19 +1311,120 @@ int orc_add_enzymatic(orc_system *s, int catalyst, int from, int to, double rate
 }
 
 int orc_add_harmonic_bonds(orc_system *s, int n, const int *idx, const double *k, const double *l0) {
-    for (int i = 0; i < n; ++i) s->bonds.push_back(Bond{(size_t)idx[2 * i], (size_t)idx[2 * i + 1], k[i], l0[i]});
+    for (int i = 0; i < n; ++i) {
+        s->fixedBonds.push_back(Bond{(size_t)idx[2 * i], (size_t)idx[2 * i + 1], k[i], l0[i]});
+        s->bonds.push_back(s->fixedBonds.back());
+    }
     return 0;
 }
 int orc_add_harmonic_angles(orc_system *s, int n, const int *idx, const double *k, const double *th) {
-    for (int i = 0; i < n; ++i)
-        s->angles.push_back(Angle{(size_t)idx[3 * i], (size_t)idx[3 * i + 1], (size_t)idx[3 * i + 2], k[i], th[i]});
+    for (int i = 0; i < n; ++i) {
+        s->fixedAngles.push_back(Angle{(size_t)idx[3 * i], (size_t)idx[3 * i + 1], (size_t)idx[3 * i + 2], k[i], th[i]});
+        s->angles.push_back(s->fixedAngles.back());
+    }
     return 0;
 }
 int orc_add_cosine_dihedrals(orc_system *s, int n, const int *idx, const double *k, const double *mult,
                              const double *phi0) {
-    for (int i = 0; i < n; ++i)
-        s->dihedrals.push_back(Dihedral{(size_t)idx[4 * i], (size_t)idx[4 * i + 1], (size_t)idx[4 * i + 2],
-                                        (size_t)idx[4 * i + 3], k[i], mult[i], phi0[i]});
+    for (int i = 0; i < n; ++i) {
+        s->fixedDihedrals.push_back(Dihedral{(size_t)idx[4 * i], (size_t)idx[4 * i + 1], (size_t)idx[4 * i + 2],
+                                             (size_t)idx[4 * i + 3], k[i], mult[i], phi0[i]});
+        s->dihedrals.push_back(s->fixedDihedrals.back());
+    }
+    return 0;
+}
+
+/* topology registry, flavors, topologies and BreakBonds */
+int orc_set_particle_flavor(orc_system *s, int type, int flavor) {
+    if (type < 0 || type >= s->nTypes) { g_err = "particle type out of range"; return -1; }
+    s->flavor[type] = flavor;
+    return 0;
+}
+int orc_configure_harmonic_bond(orc_system *s, int t1, int t2, double k, double l0) {
+    s->bondCfg.push_back({t1, t2, k, l0});
+    return 0;
+}
+int orc_configure_harmonic_angle(orc_system *s, int t1, int t2, int t3, double k, double theta0) {
+    s->angleCfg.push_back({t1, t2, t3, k, theta0});
+    return 0;
+}
+int orc_configure_cosine_dihedral(orc_system *s, int t1, int t2, int t3, int t4, double k, double mult, double phi0) {
+    s->dihedralCfg.push_back({t1, t2, t3, t4, k, mult, phi0});
+    return 0;
+}
+/* StateModel::addTopology + the graph's edges + GraphTopology::configure; ids_out receives the ids */
+int orc_add_topology(orc_system *s, int type, int n, const double *pos, const int *types, int n_edges,
+                     const int *edges, uint64_t *ids_out) {
+    try {
+        orc_system::Graph g;
+        g.type = type;
+        orc_system::IdMap ids;
+        for (int i = 0; i < n; ++i) {
+            Entry e;
+            e.pos = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+            e.type = types[i];
+            e.id = s->nextId++;
+            ids[e.id] = s->addEntry(e);
+            g.ids.push_back(e.id);
+            if (ids_out) ids_out[i] = e.id;
+        }
+        for (int k = 0; k < n_edges; ++k) g.edges.push_back({edges[2 * k], edges[2 * k + 1]});
+        const size_t nb = s->bonds.size(), na = s->angles.size(), nd = s->dihedrals.size();
+        try {
+            s->configureGraph(g, ids);
+        } catch (...) {
+            s->bonds.resize(nb);
+            s->angles.resize(na);
+            s->dihedrals.resize(nd);
+            throw;
+        }
+        s->graphs.push_back(std::move(g));
+        return 0;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+int orc_break_bonds(orc_system *s, double dt, int n, const int *t1, const int *t2, const double *thr,
+                    const double *rate, int64_t *n_broken) {
+    try {
+        const int64_t r = s->breakBonds(dt, n, t1, t2, thr, rate);
+        if (n_broken) *n_broken = r;
+        return 0;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+/* topologies as CSR over particle ids (any output may be NULL; sizes first) */
+int orc_get_topologies(const orc_system *s, int *types, int64_t *offsets, uint64_t *ids, int64_t *n_top,
+                       int64_t *n_ids) {
+    int64_t at = 0;
+    for (size_t k = 0; k < s->graphs.size(); ++k) {
+        if (types) types[k] = s->graphs[k].type;
+        if (offsets) offsets[k] = at;
+        for (auto id : s->graphs[k].ids) {
+            if (ids) ids[at] = id;
+            ++at;
+        }
+    }
+    if (offsets) offsets[s->graphs.size()] = at;
+    if (n_top) *n_top = (int64_t)s->graphs.size();
+    if (n_ids) *n_ids = at;
+    return 0;
+}
+int orc_get_topology_edges(const orc_system *s, int64_t *offsets, uint64_t *edges2, int64_t *n_edges) {
+    int64_t at = 0;
+    for (size_t k = 0; k < s->graphs.size(); ++k) {
+        if (offsets) offsets[k] = at;
+        const auto &g = s->graphs[k];
+        for (auto &e : g.edges) {
+            if (edges2) { edges2[2 * at] = g.ids[e.first]; edges2[2 * at + 1] = g.ids[e.second]; }
+            ++at;
+        }
+    }
+    if (offsets) offsets[s->graphs.size()] = at;
+    if (n_edges) *n_edges = at;
     return 0;
 }
 

@@ -62,6 +62,21 @@ int orc_add_harmonic_angles(orc_system *s, int n, const int *idx3, const double 
 int orc_add_cosine_dihedrals(orc_system *s, int n, const int *idx4, const double *k, const double *multiplicity,
                              const double *phi0);
 
+/* topology registry (PotentialConfiguration.h:136-161), particle flavors, topologies with their graphs
+ * (bonded terms derived as GraphTopology::configure does; explicit terms above are kept beside them) and
+ * BreakBonds (Actions.h:236-290) */
+int orc_set_particle_flavor(orc_system *s, int type, int flavor);
+int orc_configure_harmonic_bond(orc_system *s, int t1, int t2, double k, double l0);
+int orc_configure_harmonic_angle(orc_system *s, int t1, int t2, int t3, double k, double theta0);
+int orc_configure_cosine_dihedral(orc_system *s, int t1, int t2, int t3, int t4, double k, double mult, double phi0);
+int orc_add_topology(orc_system *s, int type, int n, const double *pos3, const int *types, int n_edges,
+                     const int *edges2, uint64_t *ids_out);
+int orc_break_bonds(orc_system *s, double dt, int n, const int *t1, const int *t2, const double *threshold,
+                    const double *rate, int64_t *n_broken);
+int orc_get_topologies(const orc_system *s, int *types, int64_t *offsets, uint64_t *ids, int64_t *n_top,
+                       int64_t *n_ids);
+int orc_get_topology_edges(const orc_system *s, int64_t *offsets, uint64_t *edges2, int64_t *n_edges);
+
 /* particles */
 int orc_add_particles(orc_system *s, int n, const double *pos3, const int *types);
 int orc_n_particles(const orc_system *s);       /* active */

@@ -45,6 +45,7 @@ def _sig(lib):
         "rdc_context_destroy": (i, [vp]),
         "rdc_context_max_cutoff": (i, [vp, P(d)]),
         "rdc_context_set_record_virial": (i, [vp, i]),
+        "rdc_context_set_particle_flavor": (i, [vp, i, i]),
         "rdc_get_virial": (i, [vp, P(d)]),
         "rdc_context_add_harmonic_repulsion": (i, [vp, i, i, d, d]),
         "rdc_context_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
@@ -67,6 +68,10 @@ def _sig(lib):
         "rdc_system_destroy": (i, [vp]),
         "rdc_add_particles": (i, [vp, i64, P(d), P(i), P(u64)]),
         "rdc_add_topology": (i, [vp, i64, P(d), P(i), i64, P(i64), P(u64)]),
+        "rdc_add_topology_typed": (i, [vp, i, i64, P(d), P(i), i64, P(i64), P(u64)]),
+        "rdc_break_bonds": (i, [vp, d, i, P(i), P(i), P(d), P(d), P(i64)]),
+        "rdc_get_topologies": (i, [vp, i64, P(i), P(i64), i64, P(u64), P(i64), P(i64)]),
+        "rdc_get_topology_edges": (i, [vp, i64, P(i64), i64, P(u64), P(i64), P(i64)]),
         "rdc_get_n_particles": (i, [vp, P(i64)]),
         "rdc_get_particles": (i, [vp, i64, P(d), P(i), P(u64), P(i64)]),
         "rdc_get_forces": (i, [vp, i64, P(d), P(u64), P(i64)]),

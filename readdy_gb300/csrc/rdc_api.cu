@@ -7,6 +7,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <string>
@@ -312,6 +313,17 @@ struct Topology {
     std::vector<float4> angle_par;
     std::vector<int4> dihedrals;
     std::vector<float4> dih_par;
+    // graph edges: (slot1, slot2, first bond term, bond terms), and each bond term's (k, l0) in FP64
+    std::vector<int4> edges;
+    std::vector<double2> bond_kl;
+    std::vector<std::pair<int, int>> edge_owner;  // (graph, local edge) of each edge
+};
+
+// one topology: its type, its particles (vertex -> topology slot) and its graph's edges (local vertices)
+struct TopGraph {
+    int type = 0;
+    std::vector<int> slots;
+    std::vector<std::pair<int, int>> edges;
 };
 
 struct rdc_system {
@@ -328,6 +340,12 @@ struct rdc_system {
     bool forces_live = false;
     int n_top = 0;
     Topology top;
+    std::vector<TopGraph> graphs;     // the active topologies
+    std::vector<int> slot_type;       // particle type per topology slot
+    std::vector<uint32_t> slot_id;    // particle id per topology slot
+    uint64_t break_calls = 0;         // BreakBonds calls so far: keys their coins
+    int4 *edge_dev = nullptr;
+    double2 *bond_kl_dev = nullptr;
     int *top_off_dev = nullptr, *top_terms_dev = nullptr;
     int4 *bond_idx_dev = nullptr, *angle_idx_dev = nullptr, *dih_idx_dev = nullptr;
     float4 *bond_par_dev = nullptr, *angle_par_dev = nullptr;
@@ -355,6 +373,7 @@ struct rdc_system {
         dfree(top_off_dev); dfree(top_terms_dev);
         dfree(bond_idx_dev); dfree(angle_idx_dev); dfree(dih_idx_dev);
         dfree(bond_par_dev); dfree(angle_par_dev); dfree(dih_par_dev);
+        dfree(edge_dev); dfree(bond_kl_dev);
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -586,9 +605,12 @@ struct rdc_system {
     }
 
     // ---- topology ----
-    void add_topology(int64_t n, const double *pos, const int *types, int64_t n_edges, const int64_t *edges,
-                      uint64_t *ids_out);
-    void upload_topology();
+    void add_topology(int topology_type, int64_t n, const double *pos, const int *types, int64_t n_edges,
+                      const int64_t *edges, uint64_t *ids_out);
+    void configure(const TopGraph &g, int graph_index, Topology &out) const;
+    void upload_topology(bool sort_new_particles = true);
+    int64_t break_bonds(double dt, int n_pairs, const int *t1, const int *t2, const double *threshold,
+                        const double *rate);
 
     // ---- SimulationLoop::run ----
     void run(int64_t n_steps, double dt, int handler, int64_t stride, int64_t *counts, int64_t max_rec,
@@ -603,35 +625,41 @@ void rdc_system::integrate_only() {
 }
 
 // findNTuples over one topology graph (include/graphs/bits/Graph_detail.h:39-76) and the type-tuple
-// lookup of GraphTopology::configure (readdy/main/model/topologies/GraphTopology.cpp:59-143)
-void rdc_system::add_topology(int64_t n, const double *pos, const int *types, int64_t n_edges, const int64_t *edges,
-                              uint64_t *ids_out) {
-    require(n > 0, "topology needs particles");
+// lookup of GraphTopology::configure (readdy/main/model/topologies/GraphTopology.cpp:59-143): appends the
+// graph's bond, angle and dihedral terms and its edges to out; throws if an edge has no bond configured
+void rdc_system::configure(const TopGraph &gr, int graph_index, Topology &out) const {
+    const int n = (int)gr.slots.size();
     std::vector<std::vector<int>> adj(n);
-    for (int64_t e = 0; e < n_edges; ++e) {
-        const int64_t a = edges[2 * e], b = edges[2 * e + 1];
-        require(a >= 0 && b >= 0 && a < n && b < n && a != b, "bad topology edge");
-        adj[a].push_back((int)b);
-        adj[b].push_back((int)a);
+    std::vector<std::vector<int>> adj_edge(n);  // local edge index of each adjacency entry
+    for (size_t e = 0; e < gr.edges.size(); ++e) {
+        const int a = gr.edges[e].first, b = gr.edges[e].second;
+        adj[a].push_back(b);
+        adj_edge[a].push_back((int)e);
+        adj[b].push_back(a);
+        adj_edge[b].push_back((int)e);
     }
-    const int base = n_top;
-    auto ty = [&](int v) { return types[v]; };
+    auto ty = [&](int v) { return slot_type[gr.slots[v]]; };
+    auto sl = [&](int v) { return gr.slots[v]; };
     std::vector<char> visited(n, 0);
     for (int v1 = 0; v1 < n; ++v1) {
         visited[v1] = 1;
-        for (int nb : adj[v1]) {
+        for (size_t a = 0; a < adj[v1].size(); ++a) {
+            const int nb = adj[v1][a];
             if (!visited[nb]) {
-                bool found = false;
+                const int first = (int)out.bonds.size();
                 for (auto &c : ctx.bonds) {
                     if ((c.t1 == ty(v1) && c.t2 == ty(nb)) || (c.t1 == ty(nb) && c.t2 == ty(v1))) {
-                        top.bonds.push_back(make_int4(base + v1, base + nb, 0, 0));
-                        top.bond_par.push_back(bond_params(c.k, c.l0));
-                        found = true;
+                        out.bonds.push_back(make_int4(sl(v1), sl(nb), 0, 0));
+                        out.bond_par.push_back(bond_params(c.k, c.l0));
+                        out.bond_kl.push_back(make_double2(c.k, c.l0));
                     }
                 }
-                if (!found)
+                const int count = (int)out.bonds.size() - first;
+                if (count == 0)
                     throw InvalidArgument("The edge " + std::to_string(v1) + " -- " + std::to_string(nb) +
                                           " has no bond configured!");
+                out.edges.push_back(make_int4(sl(v1), sl(nb), first, count));
+                out.edge_owner.emplace_back(graph_index, adj_edge[v1][a]);
                 for (int q1 : adj[v1]) {
                     if (q1 == nb) continue;
                     for (int q2 : adj[nb]) {
@@ -641,8 +669,8 @@ void rdc_system::add_topology(int64_t n, const double *pos, const int *types, in
                             const bool fwd = c.t1 == tt[0] && c.t2 == tt[1] && c.t3 == tt[2] && c.t4 == tt[3];
                             const bool bwd = c.t1 == tt[3] && c.t2 == tt[2] && c.t3 == tt[1] && c.t4 == tt[0];
                             if (fwd || bwd) {
-                                top.dihedrals.push_back(make_int4(base + q1, base + v1, base + nb, base + q2));
-                                top.dih_par.push_back(make_float4((float)c.k, (float)c.mult, (float)c.phi0, 0.f));
+                                out.dihedrals.push_back(make_int4(sl(q1), sl(v1), sl(nb), sl(q2)));
+                                out.dih_par.push_back(make_float4((float)c.k, (float)c.mult, (float)c.phi0, 0.f));
                             }
                         }
                     }
@@ -655,27 +683,188 @@ void rdc_system::add_topology(int64_t n, const double *pos, const int *types, in
                         const bool fwd = c.t1 == tt[0] && c.t2 == tt[1] && c.t3 == tt[2];
                         const bool bwd = c.t1 == tt[2] && c.t2 == tt[1] && c.t3 == tt[0];
                         if (fwd || bwd) {
-                            top.angles.push_back(make_int4(base + nb2, base + v1, base + nb, 0));
-                            top.angle_par.push_back(angle_params(c.k, c.theta0));
+                            out.angles.push_back(make_int4(sl(nb2), sl(v1), sl(nb), 0));
+                            out.angle_par.push_back(angle_params(c.k, c.theta0));
                         }
                     }
                 }
             }
         }
     }
+}
+
+template <typename T>
+static void append_all(std::vector<T> &to, const std::vector<T> &from) {
+    to.insert(to.end(), from.begin(), from.end());
+}
+
+void rdc_system::add_topology(int topology_type, int64_t n, const double *pos, const int *types, int64_t n_edges,
+                              const int64_t *edges, uint64_t *ids_out) {
+    require(n > 0, "topology needs particles");
+    require(topology_type >= 0, "topology type must be >= 0");
+    for (int64_t i = 0; i < n; ++i) require(types[i] >= 0 && types[i] < ctx.ntypes, "particle type out of range");
+    const int base = n_top;
+    TopGraph g;
+    g.type = topology_type;
+    g.slots.resize(n);
+    for (int64_t i = 0; i < n; ++i) g.slots[i] = base + (int)i;
+    for (int64_t e = 0; e < n_edges; ++e) {
+        const int64_t a = edges[2 * e], b = edges[2 * e + 1];
+        require(a >= 0 && b >= 0 && a < n && b < n && a != b, "bad topology edge");
+        g.edges.emplace_back((int)a, (int)b);
+    }
+    // terms first, into a scratch list: an edge without a bond configuration leaves the system unchanged
+    const size_t old_slots = slot_type.size();
+    slot_type.insert(slot_type.end(), types, types + n);
+    Topology add;
+    try {
+        configure(g, (int)graphs.size(), add);
+    } catch (...) {
+        slot_type.resize(old_slots);
+        throw;
+    }
     std::vector<int> slots(n);
     for (int64_t i = 0; i < n; ++i) slots[i] = base + (int)i;
-    // the slot -> storage map must cover the new slots before any sort gathers them
-    n_top += (int)n;
+    // the slot -> storage map grows with its entries kept, and covers the new slots before any sort
+    // gathers them
+    int *tloc_new = dalloc<int>(n_top + n);
+    if (n_top > 0 && d.tloc)
+        RDC_CUDA(cudaMemcpyAsync(tloc_new, d.tloc, sizeof(int) * n_top, cudaMemcpyDeviceToDevice, stream));
+    sync();
     dfree(d.tloc);
-    d.tloc = dalloc<int>(n_top);
+    d.tloc = tloc_new;
+    n_top += (int)n;
     d.tloc_size = n_top;
     d.n_top = 0;  // bonded terms are uploaded below; until then the force kernel skips them
-    append(n, pos, types, slots.data(), ids_out);
+    std::vector<uint64_t> ids(n);
+    append(n, pos, types, slots.data(), ids.data());
+    if (ids_out) std::copy(ids.begin(), ids.end(), ids_out);
+    for (auto v : ids) slot_id.push_back((uint32_t)v);
+    graphs.push_back(std::move(g));
+    // shift the scratch list's bond term indices behind the existing ones
+    const int bond_base = (int)top.bonds.size();
+    for (auto &e : add.edges) e.z += bond_base;
+    append_all(top.bonds, add.bonds);
+    append_all(top.bond_par, add.bond_par);
+    append_all(top.bond_kl, add.bond_kl);
+    append_all(top.angles, add.angles);
+    append_all(top.angle_par, add.angle_par);
+    append_all(top.dihedrals, add.dihedrals);
+    append_all(top.dih_par, add.dih_par);
+    append_all(top.edges, add.edges);
+    append_all(top.edge_owner, add.edge_owner);
     upload_topology();
 }
 
-void rdc_system::upload_topology() {
+// BreakBonds (include/readdy/model/actions/Actions.h:236-290): the device draws which edges break; the
+// graphs lose those edges, a graph that falls apart becomes its connected components (same topology
+// type; a component of one particle of NORMAL flavor leaves the topologies,
+// include/readdy/model/actions/Utils.h:59-79, GraphTopology.cpp:161-173), and the bonded terms are
+// derived again from the remaining graphs (StructuralTopologyReaction.cpp:115-127).  The reference
+// action also adds the evaluated bonds' forces to the particles' force accumulators
+// (CPUTopologyActions.cpp:55-70); here forces stay as they were until the next CalculateForces.
+int64_t rdc_system::break_bonds(double dt, int n_pairs, const int *t1, const int *t2, const double *threshold,
+                                const double *rate) {
+    require(dt > 0, "time step must be > 0");
+    require(n_pairs >= 0, "n_pairs must be >= 0");
+    const int T = ctx.ntypes;
+    std::vector<double> thr(T * T, std::numeric_limits<double>::quiet_NaN());
+    std::vector<uint64_t> coin(T * T, 0);
+    for (int k = 0; k < n_pairs; ++k) {
+        require(t1[k] >= 0 && t1[k] < T && t2[k] >= 0 && t2[k] < T, "particle type out of range");
+        require(!std::isnan(threshold[k]), "threshold energy must be a number");
+        require(rate[k] >= 0, "break rate must be >= 0");
+        for (int o = 0; o < 2; ++o) {
+            const int a = o ? t2[k] : t1[k], b = o ? t1[k] : t2[k];
+            thr[a * T + b] = threshold[k];
+            coin[a * T + b] = coin_threshold(rate[k], dt);
+        }
+    }
+    const int ne = (int)top.edges.size();
+    const uint64_t call = break_calls++;
+    if (ne == 0 || n_pairs == 0) return 0;
+    double *thr_dev = dalloc<double>(T * T);
+    uint64_t *coin_dev = dalloc<uint64_t>(T * T);
+    int *out_dev = dalloc<int>(ne + 1);
+    RDC_CUDA(cudaMemcpyAsync(thr_dev, thr.data(), sizeof(double) * T * T, cudaMemcpyHostToDevice, stream));
+    RDC_CUDA(cudaMemcpyAsync(coin_dev, coin.data(), sizeof(uint64_t) * T * T, cudaMemcpyHostToDevice, stream));
+    launch_break_bonds(d, edge_dev, ne, bond_kl_dev, thr_dev, coin_dev, T, seed, call, out_dev + 1, out_dev, stream);
+    int nb = 0;
+    RDC_CUDA(cudaMemcpyAsync(&nb, out_dev, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    sync();
+    std::vector<int> broken(nb);
+    if (nb > 0) RDC_CUDA(cudaMemcpyAsync(broken.data(), out_dev + 1, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream));
+    sync();
+    dfree(thr_dev);
+    dfree(coin_dev);
+    dfree(out_dev);
+    if (nb == 0) return 0;
+    // remove the broken edges from their graphs
+    std::vector<std::vector<char>> gone(graphs.size());
+    for (int e : broken) {
+        require(e >= 0 && e < ne, "broken edge index out of range");
+        const auto [gi, le] = top.edge_owner[e];
+        if (gone[gi].empty()) gone[gi].assign(graphs[gi].edges.size(), 0);
+        gone[gi][le] = 1;
+    }
+    std::vector<TopGraph> next;
+    next.reserve(graphs.size());
+    for (size_t gi = 0; gi < graphs.size(); ++gi) {
+        TopGraph &g = graphs[gi];
+        if (gone[gi].empty()) {
+            next.push_back(std::move(g));
+            continue;
+        }
+        std::vector<std::pair<int, int>> kept;
+        for (size_t e = 0; e < g.edges.size(); ++e)
+            if (!gone[gi][e]) kept.push_back(g.edges[e]);
+        // connected components over the kept edges, each listing its vertices in their graph order
+        const int n = (int)g.slots.size();
+        std::vector<std::vector<int>> adj(n);
+        for (auto &e : kept) {
+            adj[e.first].push_back(e.second);
+            adj[e.second].push_back(e.first);
+        }
+        std::vector<int> comp(n, -1);
+        int nc = 0;
+        for (int v = 0; v < n; ++v) {
+            if (comp[v] >= 0) continue;
+            std::vector<int> stack{v};
+            comp[v] = nc;
+            while (!stack.empty()) {
+                const int u = stack.back();
+                stack.pop_back();
+                for (int w : adj[u])
+                    if (comp[w] < 0) {
+                        comp[w] = nc;
+                        stack.push_back(w);
+                    }
+            }
+            ++nc;
+        }
+        std::vector<TopGraph> parts(nc);
+        std::vector<int> local(n);
+        for (int v = 0; v < n; ++v) {
+            local[v] = (int)parts[comp[v]].slots.size();
+            parts[comp[v]].slots.push_back(g.slots[v]);
+            parts[comp[v]].type = g.type;
+        }
+        for (auto &e : kept) parts[comp[e.first]].edges.emplace_back(local[e.first], local[e.second]);
+        for (auto &part : parts) {
+            const bool single_normal = nc > 1 && part.slots.size() == 1 &&
+                                       ctx.flavor[slot_type[part.slots[0]]] == FLAVOR_NORMAL;
+            if (!single_normal) next.push_back(std::move(part));
+        }
+    }
+    graphs = std::move(next);
+    Topology fresh;
+    for (size_t gi = 0; gi < graphs.size(); ++gi) configure(graphs[gi], (int)gi, fresh);
+    top = std::move(fresh);
+    upload_topology(false);
+    return nb;
+}
+
+void rdc_system::upload_topology(bool sort_new_particles) {
     // CSR: per topology slot, every (kind, role, term) it takes part in
     std::vector<std::vector<int>> per(n_top);
     for (size_t i = 0; i < top.bonds.size(); ++i) {
@@ -715,6 +904,8 @@ void rdc_system::upload_topology() {
     up(angle_par_dev, top.angle_par);
     up(dih_idx_dev, top.dihedrals);
     up(dih_par_dev, top.dih_par);
+    up(edge_dev, top.edges);
+    up(bond_kl_dev, top.bond_kl);
     d.n_top = n_top;
     d.top_off = top_off_dev;
     d.top_terms = top_terms_dev;
@@ -722,7 +913,7 @@ void rdc_system::upload_topology() {
     d.angle_idx = angle_idx_dev; d.angle_par = angle_par_dev;
     d.dih_idx = dih_idx_dev; d.dih_par = dih_par_dev;
     // with a neighbour list the new particles join the cells and tloc is rebuilt by a sort
-    if (nl_ready) {
+    if (nl_ready && sort_new_particles) {
         launch_bin(d, stream);
         launch_sort(d, forces_live, stream);
         swap_buffers();
@@ -864,6 +1055,7 @@ int rdc_context_create(rdc_context **out, const double box[3], const int periodi
         c->d.kbt = kbt;
         c->d.ntypes = n_types;
         c->d.D.assign(diffusion, diffusion + n_types);
+        c->d.flavor.assign(n_types, FLAVOR_NORMAL);
         for (double D : c->d.D) require(D >= 0, "diffusion constants must be >= 0");
         *out = c.release();
     });
@@ -871,6 +1063,15 @@ int rdc_context_create(rdc_context **out, const double box[3], const int periodi
 int rdc_context_destroy(rdc_context *ctx) {
     delete ctx;
     return RDC_OK;
+}
+int rdc_context_set_particle_flavor(rdc_context *ctx, int type, int flavor) {
+    return guarded([&] {
+        require(ctx != nullptr, "null context");
+        require(type >= 0 && type < ctx->d.ntypes, "particle type out of range");
+        require(flavor == FLAVOR_NORMAL || flavor == FLAVOR_TOPOLOGY || flavor == FLAVOR_MEMBRANE,
+                "flavor must be NORMAL (0), TOPOLOGY (1) or MEMBRANE (2)");
+        ctx->d.flavor[type] = flavor;
+    });
 }
 int rdc_context_set_record_virial(rdc_context *ctx, int record) {
     return guarded([&] {
@@ -1117,9 +1318,71 @@ int rdc_add_particles(rdc_system *s, int64_t n, const double *pos, const int *ty
 }
 int rdc_add_topology(rdc_system *s, int64_t n, const double *pos, const int *types, int64_t n_edges,
                      const int64_t *edges, uint64_t *ids_out) {
+    return rdc_add_topology_typed(s, 0, n, pos, types, n_edges, edges, ids_out);
+}
+int rdc_add_topology_typed(rdc_system *s, int topology_type, int64_t n, const double *pos, const int *types,
+                           int64_t n_edges, const int64_t *edges, uint64_t *ids_out) {
     return guarded([&] {
         require(s && pos && types && (n_edges == 0 || edges), "null argument");
-        s->add_topology(n, pos, types, n_edges, edges, ids_out);
+        s->add_topology(topology_type, n, pos, types, n_edges, edges, ids_out);
+    });
+}
+int rdc_break_bonds(rdc_system *s, double time_step, int n_pairs, const int *type1, const int *type2,
+                    const double *threshold_energy, const double *rate, int64_t *n_broken) {
+    return guarded([&] {
+        require(s && (n_pairs == 0 || (type1 && type2 && threshold_energy && rate)), "null argument");
+        const int64_t nb = s->break_bonds(time_step, n_pairs, type1, type2, threshold_energy, rate);
+        if (n_broken) *n_broken = nb;
+    });
+}
+int rdc_get_topologies(rdc_system *s, int64_t capacity_topologies, int *topology_types, int64_t *offsets,
+                       int64_t capacity_ids, uint64_t *ids, int64_t *n_topologies, int64_t *n_ids) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        const int64_t nt = (int64_t)s->graphs.size();
+        int64_t total = 0;
+        for (const auto &g : s->graphs) total += (int64_t)g.slots.size();
+        if (n_topologies) *n_topologies = nt;
+        if (n_ids) *n_ids = total;
+        if (nt > capacity_topologies || total > capacity_ids)
+            throw CapacityError("output capacity too small for the topologies");
+        int64_t at = 0;
+        for (int64_t k = 0; k < nt; ++k) {
+            const auto &g = s->graphs[k];
+            if (topology_types) topology_types[k] = g.type;
+            if (offsets) offsets[k] = at;
+            for (int slot : g.slots) {
+                if (ids) ids[at] = s->slot_id[slot];
+                ++at;
+            }
+        }
+        if (offsets) offsets[nt] = at;
+    });
+}
+int rdc_get_topology_edges(rdc_system *s, int64_t capacity_topologies, int64_t *offsets, int64_t capacity_edges,
+                           uint64_t *edges2, int64_t *n_topologies, int64_t *n_edges) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        const int64_t nt = (int64_t)s->graphs.size();
+        int64_t total = 0;
+        for (const auto &g : s->graphs) total += (int64_t)g.edges.size();
+        if (n_topologies) *n_topologies = nt;
+        if (n_edges) *n_edges = total;
+        if (nt > capacity_topologies || total > capacity_edges)
+            throw CapacityError("output capacity too small for the topology edges");
+        int64_t at = 0;
+        for (int64_t k = 0; k < nt; ++k) {
+            const auto &g = s->graphs[k];
+            if (offsets) offsets[k] = at;
+            for (const auto &e : g.edges) {
+                if (edges2) {
+                    edges2[2 * at] = s->slot_id[g.slots[e.first]];
+                    edges2[2 * at + 1] = s->slot_id[g.slots[e.second]];
+                }
+                ++at;
+            }
+        }
+        if (offsets) offsets[nt] = at;
     });
 }
 int rdc_get_n_particles(rdc_system *s, int64_t *n) {

@@ -47,6 +47,9 @@ struct BondCfg { int t1, t2; double k, l0; };
 struct AngleCfg { int t1, t2, t3; double k, theta0; };
 struct DihedralCfg { int t1, t2, t3, t4; double k, mult, phi0; };
 
+// particle flavors (include/readdy/model/ParticleTypeRegistry.h:58-63)
+constexpr int FLAVOR_NORMAL = 0, FLAVOR_TOPOLOGY = 1, FLAVOR_MEMBRANE = 2;
+
 struct ContextData {
     double box[3];
     int pbc[3];
@@ -54,6 +57,7 @@ struct ContextData {
     int ntypes;
     bool record_virial = false;  // Context::recordVirial (include/readdy/model/Context.h:168-174)
     std::vector<double> D;
+    std::vector<int> flavor;  // per type: FLAVOR_NORMAL, FLAVOR_TOPOLOGY or FLAVOR_MEMBRANE
     std::vector<HostPot> pots;
     std::vector<HostO1> o1pots;
     std::vector<HostReaction> reactions;
@@ -186,6 +190,10 @@ void launch_step_advance(const SysDev &s, cudaStream_t st);
 void launch_pairs(const SysDev &s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out,
                   cudaStream_t st);
 void launch_fill_ids(uint32_t *id, uint32_t first, int n, cudaStream_t st);
+// edges: (slot1, slot2, first bond term, bond terms); thr and coin: T x T per type pair
+void launch_break_bonds(const SysDev &s, const int4 *edges, int n_edges, const double2 *bond_kl, const double *thr,
+                        const uint64_t *coin, int T, uint64_t seed, uint64_t counter, int *out, int *out_n,
+                        cudaStream_t st);
 int scan_block_count(int n);
 size_t resolve_smem_bytes();
 void init_kernel_attributes();

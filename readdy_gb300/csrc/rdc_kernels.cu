@@ -324,6 +324,58 @@ __global__ void k_bonded(SysDev s) {
     if (threadIdx.x == 0) s.epart[FORCE_BLOCKS + blockIdx.x] = b;
 }
 
+// ------------------------------------------------------------------------------------------------
+// BreakBonds (include/readdy/model/actions/Actions.h:236-290): one thread per graph edge of the
+// topologies.  The edge's energy is the sum of its harmonic bonds, k (|x_ij| - l0)^2 over the bond
+// configurations of its type pair (BondedPotential.h harmonic bond energy), taken in FP64 from the FP32
+// positions with bcs::shortestDifference (boundary_condition_operations.h:71-80).  An edge above its
+// type pair's threshold energy breaks when its coin, keyed by the ordered ids of its particles and the
+// call counter, falls below 1 - exp(-rate dt); the indices of the broken edges are appended to out.
+// Edges are independent: the reference evaluates every edge of a topology on the positions before
+// any removal.
+// ------------------------------------------------------------------------------------------------
+__global__ void k_break_bonds(SysDev s, const int4 *__restrict__ edges, int n_edges, const double2 *__restrict__ bond_kl,
+                              const double *__restrict__ thr, const uint64_t *__restrict__ coin, int T, uint64_t seed,
+                              uint64_t counter, int *out, int *out_n) {
+    const Geo &g = s.geo;
+    GRID_STRIDE(e, n_edges) {
+        const int4 E = edges[e];
+        const int i = s.tloc[E.x], j = s.tloc[E.y];
+        const float4 pi = s.pos[i], pj = s.pos[j];
+        const int ti = itype(pi), tj = itype(pj);
+        if (ti < 0 || tj < 0 || ti >= T || tj >= T) continue;
+        const double th = thr[ti * T + tj];
+        if (th != th) continue;  // NaN: the type pair is not breakable
+        double x[3] = {(double)pj.x - (double)pi.x, (double)pj.y - (double)pi.y, (double)pj.z - (double)pi.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            if (g.pbc[a]) {
+                const double L = (double)g.L[a];
+                if (x[a] > 0.5 * L) x[a] -= L;
+                else if (x[a] <= -0.5 * L) x[a] += L;
+            }
+        const double d = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        double energy = 0.0;
+        for (int b = E.z; b < E.z + E.w; ++b) {
+            const double2 kl = bond_kl[b];
+            energy += kl.x * (d - kl.y) * (d - kl.y);
+        }
+        if (!(energy > th)) continue;
+        const uint32_t a = s.id[i], b = s.id[j];
+        const U4 u = rng_draw(seed, min(a, b), max(a, b), counter, RNG_BREAK, 0u);
+        if (coin_bits(u) < coin[ti * T + tj]) out[atomicAdd(out_n, 1)] = e;
+    }
+}
+
+void launch_break_bonds(const SysDev &s, const int4 *edges, int n_edges, const double2 *bond_kl, const double *thr,
+                        const uint64_t *coin, int T, uint64_t seed, uint64_t counter, int *out, int *out_n,
+                        cudaStream_t st) {
+    RDC_CUDA(cudaMemsetAsync(out_n, 0, sizeof(int), st));
+    if (n_edges > 0)
+        k_break_bonds<<<std::min((n_edges + 255) / 256, GRID_BLOCKS), 256, 0, st>>>(s, edges, n_edges, bond_kl, thr, coin,
+                                                                               T, seed, counter, out, out_n);
+}
+
 __global__ void k_energy_final(SysDev s, int pair, int bonded) {
     double v = 0.0;
     if (pair)

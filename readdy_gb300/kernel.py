@@ -64,6 +64,14 @@ class Context:
         N.check(self._lib.rdc_context_set_record_virial(self._h, int(bool(value))))
         self._record_virial = bool(value)
 
+    # particle flavors of ParticleTypeRegistry::add (ParticleTypeRegistry.h:58-63)
+    NORMAL, TOPOLOGY, MEMBRANE = 0, 1, 2
+
+    def set_particle_flavor(self, particle_type, flavor):
+        """The flavor of a species (NORMAL by default); BreakBonds drops one-particle pieces of NORMAL types
+        from the topologies."""
+        N.check(self._lib.rdc_context_set_particle_flavor(self._h, particle_type, flavor))
+
     # PotentialRegistry
     def add_harmonic_repulsion(self, t1, t2, force_constant, interaction_distance):
         N.check(self._lib.rdc_context_add_harmonic_repulsion(self._h, t1, t2, force_constant, interaction_distance))
@@ -177,14 +185,53 @@ class CUDAKernel:
                                             _p(ids, C.c_uint64)))
         return ids
 
-    def add_topology(self, positions, types, edges):
+    def add_topology(self, positions, types, edges, topology_type=0):
+        """StateModel::addTopology with the graph's edges (local vertex indices); returns the particle ids."""
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(types, dtype=np.int32), (len(pos),)))
         e = np.ascontiguousarray(np.asarray(edges, dtype=np.int64).reshape(-1, 2))
         ids = np.zeros(len(pos), np.uint64)
-        N.check(self._lib.rdc_add_topology(self._h, len(pos), _p(pos, C.c_double), _p(t, C.c_int), len(e),
-                                           _p(e, C.c_int64), _p(ids, C.c_uint64)))
+        N.check(self._lib.rdc_add_topology_typed(self._h, int(topology_type), len(pos), _p(pos, C.c_double),
+                                                 _p(t, C.c_int), len(e), _p(e, C.c_int64), _p(ids, C.c_uint64)))
         return ids
+
+    def break_bonds(self, time_step, breakable_pairs):
+        """BreakBonds (Actions.h:190-290) with a BreakConfig of (type1, type2, threshold_energy, rate)
+        entries; returns the number of edges removed."""
+        pairs = list(breakable_pairs)
+        t1 = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
+        t2 = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
+        thr = np.ascontiguousarray([p[2] for p in pairs], dtype=np.float64)
+        rate = np.ascontiguousarray([p[3] for p in pairs], dtype=np.float64)
+        nb = C.c_int64()
+        N.check(self._lib.rdc_break_bonds(self._h, float(time_step), len(pairs), _p(t1, C.c_int), _p(t2, C.c_int),
+                                          _p(thr, C.c_double), _p(rate, C.c_double), C.byref(nb)))
+        return nb.value
+
+    def get_topologies(self):
+        """StateModel::getTopologies: a list of (topology type, particle ids[] uint64)."""
+        nt, nid = C.c_int64(), C.c_int64()
+        st = self._lib.rdc_get_topologies(self._h, 0, None, None, 0, None, C.byref(nt), C.byref(nid))
+        if st not in (N.RDC_OK, N.RDC_ERR_CAPACITY):
+            N.check(st)
+        types = np.zeros(nt.value, np.int32)
+        off = np.zeros(nt.value + 1, np.int64)
+        ids = np.zeros(nid.value, np.uint64)
+        N.check(self._lib.rdc_get_topologies(self._h, nt.value, _p(types, C.c_int), _p(off, C.c_int64), nid.value,
+                                             _p(ids, C.c_uint64), C.byref(nt), C.byref(nid)))
+        return [(int(types[k]), ids[off[k]:off[k + 1]]) for k in range(nt.value)]
+
+    def get_topology_edges(self):
+        """The graph edges of every topology, in the order of get_topologies: a list of (m, 2) id arrays."""
+        nt, ne = C.c_int64(), C.c_int64()
+        st = self._lib.rdc_get_topology_edges(self._h, 0, None, 0, None, C.byref(nt), C.byref(ne))
+        if st not in (N.RDC_OK, N.RDC_ERR_CAPACITY):
+            N.check(st)
+        off = np.zeros(nt.value + 1, np.int64)
+        edges = np.zeros((ne.value, 2), np.uint64)
+        N.check(self._lib.rdc_get_topology_edges(self._h, nt.value, _p(off, C.c_int64), ne.value,
+                                                 _p(edges, C.c_uint64), C.byref(nt), C.byref(ne)))
+        return [edges[off[k]:off[k + 1]] for k in range(nt.value)]
 
     @property
     def n_particles(self) -> int:

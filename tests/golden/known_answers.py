@@ -211,3 +211,38 @@ def per_particle_forces(case):
             out[i][d] += f[d]
             out[j][d] -= f[d]
     return [tuple(v) for v in out]
+
+
+# ---------------------------------------------------------------------------------------------
+# BreakBonds (readdy/test/TestBreakingBonds.cpp): box 10^3 (periodic), kBT 1, species A, B, C of
+# TOPOLOGY flavor with D = 1, one topology type, time step 1, harmonic bonds k = 1, l0 = 1 (energy of a
+# bond stretched to 2: 1).  Breakable pairs are (type1, type2, threshold energy, rate); rate 1e10 makes
+# the coin certain.  `after` lists the expected sizes of the topologies, sorted; `partners` the type
+# multiset of the two-particle piece where the test checks it.
+# ---------------------------------------------------------------------------------------------
+BREAK_BONDS_CASES = [
+    dict(name="dimer_low_threshold", source="readdy/test/TestBreakingBonds.cpp:68-98",
+         bonds=[(0, 0)], topologies=[dict(positions=[(0, 0, 0), (0, 0, 2)], types=[0, 0], edges=[(0, 1)])],
+         rounds=[[(0, 0, 0.9, 1e10)]], after=[1, 1]),
+    dict(name="dimer_high_threshold", source="readdy/test/TestBreakingBonds.cpp:100-112",
+         bonds=[(0, 0)], topologies=[dict(positions=[(0, 0, 0), (0, 0, 2)], types=[0, 0], edges=[(0, 1)])],
+         rounds=[[(0, 0, 1.1, 1e10)]], after=[2]),
+    dict(name="trimer_break_AB", source="readdy/test/TestBreakingBonds.cpp:129-172",
+         bonds=[(0, 0), (1, 0)],
+         topologies=[dict(positions=[(0, 0, -1), (0, 0, 1), (0, 0, 3)], types=[0, 0, 1], edges=[(0, 1), (1, 2)])],
+         rounds=[[(0, 1, 0.9, 1e10)]], after=[1, 2], partners=[0, 0]),
+    dict(name="trimer_break_AA", source="readdy/test/TestBreakingBonds.cpp:174-195",
+         bonds=[(0, 0), (1, 0)],
+         topologies=[dict(positions=[(0, 0, -1), (0, 0, 1), (0, 0, 3)], types=[0, 0, 1], edges=[(0, 1), (1, 2)])],
+         rounds=[[(0, 0, 0.9, 1e10)]], after=[1, 2], partners=[0, 1]),
+    dict(name="trimer_high_threshold", source="readdy/test/TestBreakingBonds.cpp:197-208",
+         bonds=[(0, 0), (1, 0)],
+         topologies=[dict(positions=[(0, 0, -1), (0, 0, 1), (0, 0, 3)], types=[0, 0, 1], edges=[(0, 1), (1, 2)])],
+         rounds=[[(0, 0, 1.1, 1e10), (0, 1, 1.1, 1e10)]], after=[3]),
+    dict(name="three_dimers_one_after_the_other", source="readdy/test/TestBreakingBonds.cpp:263-310",
+         bonds=[(0, 0), (1, 1), (2, 2)],
+         topologies=[dict(positions=[(0, 0, 0), (0, 0, 2)], types=[t, t], edges=[(0, 1)]) for t in (0, 1, 2)],
+         rounds=[[(0, 0, 0.9, 1e10)], [(0, 0, 0.9, 1e10), (1, 1, 0.9, 1e10)],
+                 [(0, 0, 0.9, 1e10), (1, 1, 0.9, 1e10), (2, 2, 0.9, 1e10)]],
+         after=[1, 1, 1, 1, 1, 1]),
+]
