@@ -203,6 +203,9 @@ rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx) {
     rdc_context *c = nullptr;
     check(rdc_context_create(&c, b, p, ctx.kBT(), (int)D.size(), D.data()));
     try {
+        // flavors (ParticleTypeRegistry.h:58-63): BreakBonds drops one-particle pieces of NORMAL types
+        for (const auto &[name, id] : types.typeMapping())
+            check(rdc_context_set_particle_flavor(c, (int)id, (int)types.infoOf(id).flavor));
         // each unordered type pair once: the registry files a pair's potentials under both orders
         std::set<const pot::PotentialOrder2 *> seen;
         for (const auto &[key, pots] : ctx.potentials().potentialsOrder2())
@@ -330,7 +333,8 @@ void CUDAStateModel::flushTopologies() {
             edges.push_back((int64_t)g.vertices().at(v2)->particleIndex);
         }
         std::vector<uint64_t> ids(n);
-        check(rdc_add_topology(s, (int64_t)n, x.data(), t.data(), (int64_t)(edges.size() / 2), edges.data(), ids.data()));
+        check(rdc_add_topology_typed(s, (int)pt.top->type(), (int64_t)n, x.data(), t.data(),
+                                     (int64_t)(edges.size() / 2), edges.data(), ids.data()));
         // from now on a vertex refers to its particle by the device id
         model::top::Graph relabelled;
         std::unordered_map<std::size_t, std::size_t> local;
@@ -342,6 +346,38 @@ void CUDAStateModel::flushTopologies() {
         _topologies.push_back(std::move(pt.top));
     }
     _pending.clear();
+}
+
+// the host topologies again from the device's (after BreakBonds split or shrank some): vertices hold
+// device ids, edges connect local vertices
+void CUDAStateModel::reloadTopologies() {
+    rdc_system *s = _kernel->sysIfCreated();
+    if (!s) return;
+    int64_t nt = 0, ni = 0, ne = 0;
+    int st = rdc_get_topologies(s, 0, nullptr, nullptr, 0, nullptr, &nt, &ni);
+    if (st != RDC_OK && st != RDC_ERR_CAPACITY) check(st);
+    std::vector<int> types(nt);
+    std::vector<int64_t> off(nt + 1), eoff(nt + 1);
+    std::vector<uint64_t> ids(ni);
+    check(rdc_get_topologies(s, nt, types.data(), off.data(), ni, ids.data(), &nt, &ni));
+    st = rdc_get_topology_edges(s, 0, nullptr, 0, nullptr, &nt, &ne);
+    if (st != RDC_OK && st != RDC_ERR_CAPACITY) check(st);
+    std::vector<uint64_t> edges(2 * ne);
+    check(rdc_get_topology_edges(s, nt, eoff.data(), ne, edges.data(), &nt, &ne));
+    _topologies.clear();
+    for (int64_t k = 0; k < nt; ++k) {
+        model::top::Graph graph;
+        std::unordered_map<uint64_t, std::size_t> local;
+        for (int64_t v = off[k]; v < off[k + 1]; ++v) {
+            local[ids[v]] = (std::size_t)(v - off[k]);
+            graph.addVertex(model::top::VertexData{(std::size_t)ids[v]});
+        }
+        for (int64_t e = eoff[k]; e < eoff[k + 1]; ++e)
+            graph.addEdge(graph.vertices().begin_persistent() + local.at(edges[2 * e]),
+                          graph.vertices().begin_persistent() + local.at(edges[2 * e + 1]));
+        _topologies.push_back(std::make_unique<model::top::GraphTopology>((TopologyTypeId)types[k], std::move(graph),
+                                                                          _kernel->context(), this));
+    }
 }
 
 std::vector<model::top::GraphTopology *> CUDAStateModel::getTopologies() {
@@ -447,8 +483,27 @@ std::unique_ptr<act::top::EvaluateTopologyReactions> CUDAActionFactory::evaluate
             throw std::logic_error("CUDA kernel: topology reactions are not supported");
     }, dt);
 }
-std::unique_ptr<act::top::BreakBonds> CUDAActionFactory::breakBonds(scalar, act::top::BreakConfig) const {
-    throw std::logic_error("CUDA kernel: BreakBonds is not supported");
+// BreakBonds (include/readdy/model/actions/Actions.h:213-290): the break configuration's pairs go to
+// rdc_break_bonds; the host topologies are then read back from the device
+std::unique_ptr<act::top::BreakBonds> CUDAActionFactory::breakBonds(scalar dt, act::top::BreakConfig config) const {
+    struct Break : act::top::BreakBonds {
+        CUDAKernel *k;
+        Break(CUDAKernel *k, scalar dt, act::top::BreakConfig c) : act::top::BreakBonds(dt, std::move(c)), k(k) {}
+        void perform() override {
+            std::vector<int> t1, t2;
+            std::vector<double> thr, rate;
+            for (const auto &[key, e] : thresholdEnergies()) {
+                t1.push_back((int)std::get<0>(key));
+                t2.push_back((int)std::get<1>(key));
+                thr.push_back(e);
+                rate.push_back(breakRates().at(key));
+            }
+            check(rdc_break_bonds(k->sys(), timeStep(), (int)t1.size(), t1.data(), t2.data(), thr.data(), rate.data(),
+                                  nullptr));
+            k->cudaStateModel().reloadTopologies();
+        }
+    };
+    return std::make_unique<Break>(_kernel, dt, std::move(config));
 }
 std::unique_ptr<act::EvaluateObservables> CUDAActionFactory::evaluateObservables() const {
     struct Evaluate : act::EvaluateObservables {

@@ -56,6 +56,8 @@ public:
 
     // uploads the pending topologies (particles and graph edges) to the device
     void flushTopologies();
+    // rebuilds the host topologies from the device's
+    void reloadTopologies();
 
 private:
     struct PendingTopology {
@@ -131,7 +133,7 @@ public:
     model::actions::ActionFactory &actions() override { return _actions; }
     const model::observables::ObservableFactory &observe() const override { return _observables; }
     model::observables::ObservableFactory &observe() override { return _observables; }
-    // topology reactions and BreakBonds are not provided; static topologies are (bonds, angles, dihedrals)
+    // topology reactions are not provided; static topologies (bonds, angles, dihedrals) and BreakBonds are
     const model::top::TopologyActionFactory *const getTopologyActionFactory() const override { return nullptr; }
     model::top::TopologyActionFactory *const getTopologyActionFactory() override { return nullptr; }
     void initialize() override;
@@ -141,6 +143,7 @@ public:
     // first, so every action sees all particles
     rdc_system *sys();
     rdc_system *sysIfCreated() const { return _sys; }
+    CUDAStateModel &cudaStateModel() { return _state; }
     // reference reaction id -> device reaction id (-1: not registered on the device)
     const std::vector<int> &reactionIds() const { return _rx; }
 
