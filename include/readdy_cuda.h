@@ -267,6 +267,21 @@ int rdc_batch_get_forces(rdc_batch *b, int replica, int64_t capacity, double *fo
  * a time series, include/readdy/model/observables/io/TimeSeriesWriter.h:56-92).  The records stay on the
  * device until polled. */
 int rdc_batch_record_counts(rdc_batch *b, int64_t stride, int64_t max_records);
+/* Trajectory observable (readdy/main/model/observables/Trajectory.cpp:100-160) of the replicas
+ * replicas[0, n_replicas), streamed: a frame of their live particles is taken now and at every step
+ * count that is a multiple of `stride` (as observables with a stride are evaluated), up to max_frames
+ * frames (later ones are dropped).  The frames stay on the
+ * device until polled; the buffer holds max_frames x the replicas' capacities.  n_replicas = 0 switches
+ * the trajectory off; rdc_batch_set_particles* ends it. */
+int rdc_batch_record_trajectory(rdc_batch *b, int n_replicas, const int *replicas, int64_t stride, int64_t max_frames);
+/* The frames taken since the last poll, whole frames only, as many as capacity_frames and
+ * capacity_entries take, copied on a stream of their own once the batch's stream has reached this call.
+ * Per frame f: its step in steps[f] and, per selected replica k, its particle count in
+ * counts[f * n_replicas + k]; the particles (positions3, types, ids) follow frame by frame and replica by
+ * replica.  RDC_ERR_CAPACITY if not even the next frame fits (n_entries then holds its size). */
+int rdc_batch_poll_trajectory(rdc_batch *b, int64_t capacity_frames, int64_t capacity_entries, int64_t *steps,
+                              int64_t *counts, double *positions3, int *types, uint64_t *ids, int64_t *n_frames,
+                              int64_t *n_entries);
 /* copies the records written since the last poll (at most capacity records): steps[k] is the time step of
  * record k, counts holds n_replicas * n_types values per record (record-major).  The copy runs on a stream
  * of its own after the steps already queued; the batch's own stream keeps going.  *n_out = records copied */

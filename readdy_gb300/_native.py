@@ -110,6 +110,8 @@ def _sig(lib):
         "rdc_batch_reaction_counts": (i, [vp, i, P(i64)]),
         "rdc_batch_get_virial": (i, [vp, P(d)]),
         "rdc_batch_record_counts": (i, [vp, i64, i64]),
+        "rdc_batch_record_trajectory": (i, [vp, i, P(i), i64, i64]),
+        "rdc_batch_poll_trajectory": (i, [vp, i64, i64, P(i64), P(i64), P(d), P(i), P(u64), P(i64), P(i64)]),
         "rdc_batch_poll_count_records": (i, [vp, i64, P(i64), P(i64), P(i64)]),
         "rdc_batch_replica_grid": (i, [vp, i, P(i), P(i)]),
         "rdc_batch_synchronize": (i, [vp]),

@@ -131,6 +131,38 @@ class ReplicaBatch:
                                                        C.byref(n)))
         return steps[:n.value], counts[:n.value]
 
+    def record_trajectory(self, replicas, stride: int, max_frames: int):
+        """From now on a frame of the given replicas' particles is taken every `stride` steps (frame 0 now),
+        up to max_frames frames kept on the device until polled; replicas=[] switches it off."""
+        sel = np.ascontiguousarray(replicas, dtype=np.int32).reshape(-1)
+        N.check(self._lib.rdc_batch_record_trajectory(self._h, len(sel), _p(sel, C.c_int), int(stride),
+                                                      int(max_frames)))
+        self._traj_sel = sel.copy()
+        self._traj_max = int(max_frames)
+
+    def poll_trajectory(self):
+        """The frames taken since the last poll: (steps (f,), frames) with frames[f][k] = (positions (n, 3),
+        types (n,), ids (n,)) of the k-th recorded replica."""
+        sel = getattr(self, "_traj_sel", np.zeros(0, np.int32))
+        nf_cap = max(getattr(self, "_traj_max", 0), 1)
+        cap = int(self.capacities[sel].sum()) * nf_cap if len(sel) else 1
+        steps = np.zeros(nf_cap, np.int64)
+        counts = np.zeros((nf_cap, max(len(sel), 1)), np.int64)
+        pos = np.zeros((cap, 3)); types = np.zeros(cap, np.int32); ids = np.zeros(cap, np.uint64)
+        nf, ne = C.c_int64(), C.c_int64()
+        N.check(self._lib.rdc_batch_poll_trajectory(self._h, nf_cap, cap, _p(steps, C.c_int64), _p(counts, C.c_int64),
+                                                    _p(pos, C.c_double), _p(types, C.c_int), _p(ids, C.c_uint64),
+                                                    C.byref(nf), C.byref(ne)))
+        frames, at = [], 0
+        for f in range(nf.value):
+            per = []
+            for k in range(len(sel)):
+                c = int(counts[f, k])
+                per.append((pos[at:at + c], types[at:at + c], ids[at:at + c]))
+                at += c
+            frames.append(per)
+        return steps[:nf.value], frames
+
     def virial(self):
         """Pair virial of every replica's current state, (n_replicas, 3, 3); needs carried forces off."""
         out = np.zeros((self.n_replicas, 3, 3))

@@ -117,6 +117,17 @@ struct rdc_batch {
     int64_t rec_stride = 0, rec_max = 0, rec_polled = 0, rec_start = 0;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copy = nullptr;
+    // trajectory frames of selected replicas streamed to the host (Trajectory observable): frame f holds,
+    // per selected replica k, up to its capacity of particles at slot traj_off[k] of the frame
+    std::vector<int> traj_sel;
+    std::vector<int64_t> traj_off;  // n_sel + 1 slot offsets; traj_off[n_sel] = entries per frame
+    int *traj_sel_dev = nullptr;
+    int64_t *traj_off_dev = nullptr;
+    float4 *traj_pos = nullptr;
+    uint32_t *traj_id = nullptr;
+    int *traj_n = nullptr;
+    int64_t traj_stride = 0, traj_max = 0, traj_polled = 0, traj_now = 0;
+    std::vector<int64_t> traj_steps;  // step of every frame written
 
     ~rdc_batch() { release(); }
 
@@ -131,6 +142,7 @@ struct rdc_batch {
         if (ev1) cudaEventDestroy(ev1);
         if (ev_copy) cudaEventDestroy(ev_copy);
         bfree(records);
+        traj_off_all();
         if (copy_stream) cudaStreamDestroy(copy_stream);
         copy_stream = nullptr;
         if (stream) cudaStreamDestroy(stream);
@@ -138,6 +150,24 @@ struct rdc_batch {
     }
 
     void sync() { RDC_CUDA(cudaStreamSynchronize(stream)); }
+
+    void traj_off_all() {
+        bfree(traj_sel_dev); bfree(traj_off_dev); bfree(traj_pos); bfree(traj_id); bfree(traj_n);
+        traj_sel.clear();
+        traj_off.clear();
+        traj_steps.clear();
+        traj_stride = traj_max = traj_polled = 0;
+    }
+    // the next trajectory frame, taken now (dropped once max_frames are written)
+    void traj_snapshot() {
+        const int64_t f = (int64_t)traj_steps.size();
+        if (f >= traj_max) return;
+        const int ns = (int)traj_sel.size();
+        const int64_t per = traj_off[ns];
+        launch_engine_snapshot(e, traj_sel_dev, ns, traj_off_dev, traj_pos + f * per, traj_id + f * per,
+                               traj_n + f * ns, stream);
+        traj_steps.push_back(traj_now);
+    }
 
     void invalidate_graph() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -284,7 +314,14 @@ struct rdc_batch {
             RDC_CUDA(cudaGraphInstantiate(&graph, g, 0));
             cudaGraphDestroy(g);
         }
-        for (int64_t k = 0; k < n; ++k) RDC_CUDA(cudaGraphLaunch(graph, stream));
+        if (!traj_stride) {
+            for (int64_t k = 0; k < n; ++k) RDC_CUDA(cudaGraphLaunch(graph, stream));
+            return;
+        }
+        for (int64_t k = 0; k < n; ++k) {
+            RDC_CUDA(cudaGraphLaunch(graph, stream));
+            if (++traj_now % traj_stride == 0) traj_snapshot();  // observable strides count absolute steps
+        }
     }
 
     std::vector<RepState> states() {
@@ -440,6 +477,7 @@ void set_particles_impl(rdc_batch *b, const int64_t *n, const double *const *pos
     RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * R, cudaMemcpyHostToDevice, b->stream));
     b->rec_polled = 0;  // with records on, the admission below writes record 0 again (t = 0)
     b->rec_start = 0;
+    b->traj_off_all();  // new replicas: a trajectory of the old ones ends
     b->set_order(std::vector<int64_t>(n, n + R));
     b->sort_all(true);
     b->sync();
@@ -671,6 +709,119 @@ int rdc_batch_record_counts(rdc_batch *b, int64_t stride, int64_t max_records) {
         for (auto &x : st) x.rec = 1;
         RDC_CUDA(cudaMemcpyAsync(b->state_dev, st.data(), sizeof(RepState) * b->R, cudaMemcpyHostToDevice, b->stream));
         b->sync();
+    });
+}
+
+int rdc_batch_record_trajectory(rdc_batch *b, int n_replicas, const int *replicas, int64_t stride, int64_t max_frames) {
+    BATCH_CALL({
+        if (!b || (n_replicas > 0 && !replicas)) throw std::invalid_argument("null argument");
+        if (n_replicas < 0) throw std::invalid_argument("n_replicas must be >= 0");
+        b->sync();
+        b->traj_off_all();
+        if (n_replicas == 0) return;
+        if (stride <= 0) throw std::invalid_argument("stride must be > 0");
+        if (max_frames <= 0) throw std::invalid_argument("max_frames must be > 0");
+        std::vector<int64_t> off(n_replicas + 1, 0);
+        for (int k = 0; k < n_replicas; ++k) {
+            if (replicas[k] < 0 || replicas[k] >= b->R) throw std::invalid_argument("replica out of range");
+            off[k + 1] = off[k] + b->caps[replicas[k]];
+        }
+        const int64_t per = off[n_replicas];
+        if (per * max_frames > (int64_t)1 << 34)
+            throw std::invalid_argument("trajectory buffer above 2^34 entries: fewer replicas or frames");
+        auto st = b->states();
+        b->check_status(st);
+        b->traj_sel.assign(replicas, replicas + n_replicas);
+        b->traj_off = off;
+        b->traj_sel_dev = balloc<int>(n_replicas);
+        b->traj_off_dev = balloc<int64_t>(n_replicas + 1);
+        b->traj_pos = balloc<float4>(per * max_frames);
+        b->traj_id = balloc<uint32_t>(per * max_frames);
+        b->traj_n = balloc<int>(n_replicas * max_frames);
+        RDC_CUDA(cudaMemcpyAsync(b->traj_sel_dev, replicas, sizeof(int) * n_replicas, cudaMemcpyHostToDevice, b->stream));
+        RDC_CUDA(cudaMemcpyAsync(b->traj_off_dev, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice,
+                                 b->stream));
+        b->traj_stride = stride;
+        b->traj_max = max_frames;
+        b->traj_now = st.empty() ? 0 : st[0].step;
+        if (!b->copy_stream) {
+            RDC_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+            RDC_CUDA(cudaEventCreateWithFlags(&b->ev_copy, cudaEventDisableTiming));
+        }
+        b->traj_snapshot();  // frame 0: now
+        b->sync();
+    });
+}
+
+int rdc_batch_poll_trajectory(rdc_batch *b, int64_t capacity_frames, int64_t capacity_entries, int64_t *steps,
+                              int64_t *counts, double *positions3, int *types, uint64_t *ids, int64_t *n_frames,
+                              int64_t *n_entries) {
+    BATCH_CALL({
+        if (!b) throw std::invalid_argument("null argument");
+        if (!b->traj_stride) throw std::logic_error("the trajectory is off (rdc_batch_record_trajectory switches it on)");
+        if (n_frames) *n_frames = 0;
+        if (n_entries) *n_entries = 0;
+        // the frames written so far, copied on the copy stream once the batch's stream has reached this point
+        RDC_CUDA(cudaEventRecord(b->ev_copy, b->stream));
+        RDC_CUDA(cudaStreamWaitEvent(b->copy_stream, b->ev_copy, 0));
+        const int ns = (int)b->traj_sel.size();
+        const int64_t per = b->traj_off[ns];
+        const int64_t avail = (int64_t)b->traj_steps.size() - b->traj_polled;
+        int64_t nf = std::max<int64_t>(0, std::min(avail, capacity_frames));
+        std::vector<int> cnt((size_t)nf * ns);
+        if (nf > 0)
+            RDC_CUDA(cudaMemcpyAsync(cnt.data(), b->traj_n + b->traj_polled * ns, sizeof(int) * cnt.size(),
+                                     cudaMemcpyDeviceToHost, b->copy_stream));
+        RDC_CUDA(cudaStreamSynchronize(b->copy_stream));
+        // whole frames only, as many as the entry capacity takes
+        int64_t total = 0, fit = 0;
+        for (int64_t f = 0; f < nf; ++f) {
+            int64_t t = 0;
+            for (int k = 0; k < ns; ++k) t += cnt[f * ns + k];
+            if (total + t > capacity_entries) {
+                if (fit == 0) {
+                    if (n_entries) *n_entries = t;
+                    throw rdc::CapacityError("entry capacity too small for the next trajectory frame");
+                }
+                break;
+            }
+            total += t;
+            ++fit;
+        }
+        nf = fit;
+        std::vector<float4> hp((size_t)total);
+        std::vector<uint32_t> hid((size_t)total);
+        int64_t at = 0;
+        for (int64_t f = 0; f < nf; ++f)
+            for (int k = 0; k < ns; ++k) {
+                const int64_t c = cnt[f * ns + k];
+                const int64_t src = (b->traj_polled + f) * per + b->traj_off[k];
+                if (c > 0) {
+                    RDC_CUDA(cudaMemcpyAsync(hp.data() + at, b->traj_pos + src, sizeof(float4) * c,
+                                             cudaMemcpyDeviceToHost, b->copy_stream));
+                    RDC_CUDA(cudaMemcpyAsync(hid.data() + at, b->traj_id + src, sizeof(uint32_t) * c,
+                                             cudaMemcpyDeviceToHost, b->copy_stream));
+                }
+                at += c;
+            }
+        RDC_CUDA(cudaStreamSynchronize(b->copy_stream));
+        for (int64_t f = 0; f < nf; ++f) {
+            if (steps) steps[f] = b->traj_steps[b->traj_polled + f];
+            if (counts)
+                for (int k = 0; k < ns; ++k) counts[f * ns + k] = cnt[f * ns + k];
+        }
+        for (int64_t i = 0; i < total; ++i) {
+            if (positions3) {
+                positions3[3 * i] = hp[i].x;
+                positions3[3 * i + 1] = hp[i].y;
+                positions3[3 * i + 2] = hp[i].z;
+            }
+            if (types) std::memcpy(&types[i], &hp[i].w, 4);
+            if (ids) ids[i] = hid[i];
+        }
+        b->traj_polled += nf;
+        if (n_frames) *n_frames = nf;
+        if (n_entries) *n_entries = total;
     });
 }
 

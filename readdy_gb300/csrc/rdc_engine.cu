@@ -896,6 +896,42 @@ __global__ void k_engine_record_now(EngineDev E, int R, int T, int rec) {
     }
 }
 
+// One frame of the Trajectory observable (FlatTrajectory records, readdy/main/model/observables/
+// Trajectory.cpp:100-160) for the selected replicas sel[0, n_sel): the live particles of replica sel[k]
+// (removed ones skipped, storage order kept) into slot k, positions with their type bits at
+// out_pos + slot_off[k], ids at out_id + slot_off[k], their number in out_n[k].  One CTA per selected
+// replica compacts by block scans.
+__global__ void k_engine_snapshot(EngineDev E, const int *sel, int n_sel, const int64_t *slot_off, float4 *out_pos,
+                                  uint32_t *out_id, int *out_n) {
+    for (int k = blockIdx.x; k < n_sel; k += gridDim.x) {
+        const RepDesc &D = E.desc[sel[k]];
+        const RepState st = E.state[sel[k]];
+        const float4 *pos = D.pos[st.cur];
+        const uint32_t *id = D.id[st.cur];
+        float4 *op = out_pos + slot_off[k];
+        uint32_t *oi = out_id + slot_off[k];
+        int base = 0;
+        for (int c = 0; c < st.n; c += blockDim.x) {
+            const int i = c + threadIdx.x;
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+            int live = 0;
+            if (i < st.n) {
+                p = pos[i];
+                live = itype(p) >= 0;
+            }
+            int total = 0;
+            const int at = block_exclusive_scan(live, total);
+            if (live) {
+                op[base + at] = p;
+                oi[base + at] = id[i];
+            }
+            base += total;
+        }
+        if (threadIdx.x == 0) out_n[k] = base;
+        __syncthreads();
+    }
+}
+
 __global__ void k_engine_count(EngineDev E, int R, int T, unsigned long long *out) {
     for (int r = blockIdx.x; r < R; r += gridDim.x) {
         const RepDesc &D = E.desc[r];
@@ -1044,6 +1080,13 @@ void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long lo
 
 void launch_engine_record_now(const EngineDev &E, int R, int ntypes, int rec, cudaStream_t st) {
     if (R > 0) k_engine_record_now<<<std::min(R, 4 * sm_count()), 256, 0, st>>>(E, R, ntypes, rec);
+}
+
+void launch_engine_snapshot(const EngineDev &E, const int *sel, int n_sel, const int64_t *slot_off, float4 *out_pos,
+                            uint32_t *out_id, int *out_n, cudaStream_t st) {
+    if (n_sel > 0)
+        k_engine_snapshot<<<std::min(n_sel, 4 * sm_count()), 256, 0, st>>>(E, sel, n_sel, slot_off, out_pos, out_id,
+                                                                           out_n);
 }
 
 void launch_engine_virial(const EngineDev &E, int R, double *out, cudaStream_t st) {

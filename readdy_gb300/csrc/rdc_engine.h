@@ -111,6 +111,9 @@ void launch_engine_count(const EngineDev &E, int R, int ntypes, unsigned long lo
 void launch_engine_forces(const EngineDev &E, int r, int n, float4 *out, cudaStream_t st);
 // current per-type counts of replicas [0, R) written as count record `rec` of each
 void launch_engine_record_now(const EngineDev &E, int R, int ntypes, int rec, cudaStream_t st);
+// the live particles of replicas sel[0, n_sel) into the slots slot_off[k] of a trajectory frame
+void launch_engine_snapshot(const EngineDev &E, const int *sel, int n_sel, const int64_t *slot_off, float4 *out_pos,
+                            uint32_t *out_id, int *out_n, cudaStream_t st);
 // pair virial (9 doubles, row-major) of replicas [0, R) on their current states into out (R x 9); NaN for a
 // replica that carries its forces (its state is not sorted)
 void launch_engine_virial(const EngineDev &E, int R, double *out, cudaStream_t st);

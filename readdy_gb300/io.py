@@ -57,6 +57,16 @@ def flat_trajectory_layout(frames, steps, name: str = "") -> dict:
     return {f"{group}/records": records, f"{group}/limits": limits, f"{group}/time": np.asarray(steps, np.uint64)}
 
 
+def batch_trajectory_layout(steps, frames, replicas, name: str = "") -> dict:
+    """One FlatTrajectory per recorded replica of a batch, under <name>/replica_<r>: `frames[f][k]` is the
+    (positions, types, ids) snapshot of replica replicas[k] at steps[f] (ReplicaBatch.poll_trajectory)."""
+    out = {}
+    for k, r in enumerate(replicas):
+        sub = f"{name}/replica_{int(r)}" if name else f"replica_{int(r)}"
+        out.update(flat_trajectory_layout([fr[k] for fr in frames], steps, sub))
+    return out
+
+
 def save_layout(path: str, *layouts: dict) -> None:
     """Writes the datasets of the given layouts into one .npz archive keyed by dataset path."""
     merged = {}

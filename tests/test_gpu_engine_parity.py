@@ -283,3 +283,60 @@ def test_plain_path_abc2000_ensemble_matches_oracle_ensemble(rg, handler):
         c = k.run(s["steps"], s["dt"], handler=handler, count_stride=s["steps"])
         gpu.append([c[-1, 2], *k.reaction_counts()[:2]])
     _within_3_sigma(np.array(gpu, float), oracle_ensemble("abc2000", handler), "plain abc2000")
+
+
+def test_streamed_trajectory_equals_the_particles_at_the_same_steps(rg):
+    """Trajectory frames streamed from a batch (switched on after 7 steps, polled twice while steps
+    continue) equal the particles of an identical batch read at the same steps, and fill ReaDDy's
+    FlatTrajectory layout."""
+    from readdy_gb300.batch import ReplicaBatch
+    from readdy_gb300 import io
+    rng = np.random.default_rng(43)
+    sizes = [300, 1500, 14000]  # the last replica runs on widened cells
+    poss, typess, boxes = [], [], []
+    spec = None
+    for n in sizes:
+        L = _box(n)
+        s_, pos, types = abc_spec(n=n, box=L, seed=int(rng.integers(1 << 30)))
+        spec = spec or s_
+        poss.append(f32(pos))
+        typess.append(types)
+        boxes.append((L, L, L))
+
+    def batch():
+        b = ReplicaBatch(make_context(spec), boxes, [2 * n for n in sizes], seed=77)
+        b.set_particles(poss, typess)
+        b.configure(handler=1, dt=1e-3, cell_width_scale=1.0, threads_per_block=256)
+        return b
+
+    a, ref = batch(), batch()
+    sel = [0, 2]
+    a.step(7)
+    a.record_trajectory(sel, stride=10, max_frames=8)
+    a.step(23)
+    s1, f1 = a.poll_trajectory()
+    a.step(20)
+    s2, f2 = a.poll_trajectory()
+    steps, frames = np.concatenate([s1, s2]), f1 + f2
+    np.testing.assert_array_equal(steps, [7, 10, 20, 30, 40, 50])
+    at = 0
+    for s, fr in zip(steps, frames):
+        ref.step(int(s) - at)
+        at = int(s)
+        for k, r in enumerate(sel):
+            pr, tr, ir = ref.get_particles(r)
+            pg, tg, ig = fr[k]
+            og, orr = np.argsort(ig), np.argsort(ir)
+            np.testing.assert_array_equal(ig[og], ir[orr])
+            np.testing.assert_array_equal(tg[og], tr[orr])
+            np.testing.assert_array_equal(pg[og], pr[orr])
+    lay = io.batch_trajectory_layout(steps, frames, sel)
+    for k, r in enumerate(sel):
+        g = f"readdy/trajectory/replica_{r}"
+        lim = lay[f"{g}/limits"]
+        assert len(lim) == len(steps) and lim[0, 0] == 0 and lim[-1, 1] == len(lay[f"{g}/records"])
+        np.testing.assert_array_equal(lim[:, 1] - lim[:, 0], [len(fr[k][2]) for fr in frames])
+        np.testing.assert_array_equal(lay[f"{g}/time"], steps)
+    a.record_trajectory([], 1, 1)  # off
+    with pytest.raises(RuntimeError):
+        a.poll_trajectory()
