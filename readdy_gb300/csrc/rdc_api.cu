@@ -346,6 +346,9 @@ struct rdc_system {
     uint64_t break_calls = 0;         // BreakBonds calls so far: keys their coins
     int4 *edge_dev = nullptr;
     double2 *bond_kl_dev = nullptr;
+    int2 *bond_at_dev = nullptr;
+    int4 *angle_at_dev = nullptr, *dih_at_dev = nullptr;
+    float4 *term_force_dev = nullptr;
     int *top_off_dev = nullptr, *top_terms_dev = nullptr;
     int4 *bond_idx_dev = nullptr, *angle_idx_dev = nullptr, *dih_idx_dev = nullptr;
     float4 *bond_par_dev = nullptr, *angle_par_dev = nullptr;
@@ -374,6 +377,7 @@ struct rdc_system {
         dfree(bond_idx_dev); dfree(angle_idx_dev); dfree(dih_idx_dev);
         dfree(bond_par_dev); dfree(angle_par_dev); dfree(dih_par_dev);
         dfree(edge_dev); dfree(bond_kl_dev);
+        dfree(bond_at_dev); dfree(angle_at_dev); dfree(dih_at_dev); dfree(term_force_dev);
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -889,6 +893,14 @@ void rdc_system::upload_topology(bool sort_new_particles) {
         off[t + 1] = off[t] + (int)per[t].size();
         terms.insert(terms.end(), per[t].begin(), per[t].end());
     }
+    // each term's entries in the lists, by role: the term kernel writes its role forces there
+    std::vector<int2> bond_at(top.bonds.size());
+    std::vector<int4> angle_at(top.angles.size()), dih_at(top.dihedrals.size());
+    for (int q = 0; q < (int)terms.size(); ++q) {
+        const int kind = terms[q] >> 28, role = (terms[q] >> 24) & 0xf, idx = terms[q] & 0xffffff;
+        int *slot = kind == 0 ? &bond_at[idx].x : (kind == 1 ? &angle_at[idx].x : &dih_at[idx].x);
+        slot[role] = q;
+    }
     auto up = [&](auto *&dptr, const auto &vec) {
         using T = std::remove_reference_t<decltype(*dptr)>;
         dfree(dptr);
@@ -906,6 +918,18 @@ void rdc_system::upload_topology(bool sort_new_particles) {
     up(dih_par_dev, top.dih_par);
     up(edge_dev, top.edges);
     up(bond_kl_dev, top.bond_kl);
+    up(bond_at_dev, bond_at);
+    up(angle_at_dev, angle_at);
+    up(dih_at_dev, dih_at);
+    dfree(term_force_dev);
+    term_force_dev = dalloc<float4>(terms.size());
+    d.n_bonds = (int)top.bonds.size();
+    d.n_angles = (int)top.angles.size();
+    d.n_dihedrals = (int)top.dihedrals.size();
+    d.bond_at = bond_at_dev;
+    d.angle_at = angle_at_dev;
+    d.dih_at = dih_at_dev;
+    d.term_force = term_force_dev;
     d.n_top = n_top;
     d.top_off = top_off_dev;
     d.top_terms = top_terms_dev;

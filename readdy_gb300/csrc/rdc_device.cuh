@@ -455,8 +455,8 @@ __device__ inline void pair_force(const PairPot &pp, const PairGeom &g, float4 l
 }
 
 // ------------------------------------------------------------------------------------------------
-// bonded terms.  Each participant evaluates the whole term and keeps only its own force
-// (no atomics, deterministic); 'role' selects the participant.
+// bonded terms.  Each term is evaluated once and yields the force on every participant (its roles);
+// the forces are summed per particle in a fixed order by a gather (no atomics, deterministic).
 // ------------------------------------------------------------------------------------------------
 struct F3 { float x, y, z; };
 __device__ inline F3 f3(float x, float y, float z) { return F3{x, y, z}; }
@@ -508,6 +508,16 @@ __device__ inline D3 dcross(D3 a, D3 b) {
 }
 __device__ inline D3 dneg(D3 a) { return D3{-a.x, -a.y, -a.z}; }
 __device__ inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ inline D3 dadd(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ inline D3 dsub(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ inline D3 dlin(double a, D3 u, double b, D3 v) {
+    return D3{a * u.x + b * v.x, a * u.y + b * v.y, a * u.z + b * v.z};
+}
+__device__ inline F3 f3of(D3 a) { return F3{(float)a.x, (float)a.y, (float)a.z}; }
+__device__ inline D3 operator+(D3 a, D3 b) { return dadd(a, b); }
+__device__ inline D3 operator-(D3 a, D3 b) { return dsub(a, b); }
+__device__ inline D3 operator-(D3 a) { return dneg(a); }
+__device__ inline D3 operator*(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
 
 // harmonic bond: E = k (r - l0)^2, force on i = 2k (r-l0)/r x_ij, on j its negative
 // (BondedPotential.h:105-113, CPUTopologyActions.cpp:61-74); r - l0 = (d2 - l0^2) / (r + l0)
@@ -669,14 +679,15 @@ __device__ inline void order1_force(float4 p, const O1Pot *pots, int first, int 
     }
 }
 
-__device__ inline F3 bond_force(float4 pi, float4 pj, float4 P, const Geo &g, int role, float &e) {
+// harmonic bond, E = k (|x_ij| - l0)^2 (BondedPotential.h): the force on particle i (role 0); particle j
+// (role 1) takes its negative
+__device__ inline F3 bond_force(float4 pi, float4 pj, float4 P, const Geo &g, float &e) {
     const PairExact x = pair_exact(pi, pj, g);
     const float r = sqrtf(__fadd_rn(x.d2.hi, x.d2.lo));
     const float rd = ff_sub(x.d2, P.z, P.w) / (r + P.y);
     e = P.x * rd * rd;
     const float s = 2.0f * P.x * rd / r;
-    const F3 v = f3(x.dx, x.dy, x.dz);
-    return role == 0 ? s * v : (-s) * v;
+    return s * f3(x.dx, x.dy, x.dz);
 }
 
 // harmonic angle, E = k (theta - theta0)^2 (AnglePotential.cpp:58-104) with the reference's clamps
@@ -684,7 +695,7 @@ __device__ inline F3 bond_force(float4 pi, float4 pj, float4 P, const Geo &g, in
 // (cross product by Kahan's difference of products); for obtuse angles theta - theta0 is formed as
 // (pi - theta0) - atan2(|cross|, -dot), which stays exact at the straight-chain minimum theta0 = pi.
 // P = (k, theta0, pi - theta0, -)
-__device__ inline F3 angle_force(float4 pi, float4 pj, float4 pk, float4 P, const Geo &g, int role, float &e) {
+__device__ inline void angle_force(float4 pi, float4 pj, float4 pk, float4 P, const Geo &g, F3 f[3], float &e) {
     const float SMALL = 1e-10f;
     const float kf = P.x;
     F3 a, la, b, lb;
@@ -707,21 +718,21 @@ __device__ inline F3 angle_force(float4 pi, float4 pj, float4 pk, float4 P, cons
     const float q = 2.0f * kf * dth / fmaxf(cn, SMALL * np);
     const F3 fi = (-q / na2) * cross_k(cr, a);
     const F3 fk = (-q / nb2) * cross_k(b, cr);
-    if (role == 0) return (-1.0f) * fi;
-    if (role == 1) return fi + fk;
-    return (-1.0f) * fk;
+    f[0] = (-1.0f) * fi;
+    f[1] = fi + fk;
+    f[2] = (-1.0f) * fk;
 }
 
 // cosine dihedral, the analytic gradient of TorsionPotential.cpp:70-153 written with explicit
-// cross products; same clamps (1e-4) and the same zero-force rule for |cos phi| < 1e-4
-__device__ inline F3 dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl, float kf, float mult, float phi0,
-                                    const Geo &g, int role, float &e) {
+// cross products; same clamps (1e-4) and the same zero-force rule for |cos phi| < 1e-4.  f[r] receives
+// the force on the term's particle r (i, j, k, l)
+__device__ inline void dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl, float kf, float mult, float phi0,
+                                      const Geo &g, F3 f[4], float &e) {
     const float SMALL = 1e-4f;
     F3 xji, lji, xkj, lkj, xkl, lkl;
     shortest3_ff(pj, pi, g, xji, lji);  // x_i - x_j
     shortest3_ff(pk, pj, g, xkj, lkj);  // x_j - x_k
     shortest3_ff(pk, pl, g, xkl, lkl);  // x_l - x_k
-    const F3 xjk = (-1.0f) * xkj;
     // m = x_ji x x_kj and n = x_kl x x_jk are formed from the exact differences: near a straight bond
     // angle m or n is short, and rounded differences would cost it most of its digits.
     // The dihedral angle is taken in FP64 from the exact differences.  Its force is dV/dphi times a
@@ -740,98 +751,88 @@ __device__ inline F3 dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl, 
     // force (TorsionPotential.cpp:70-159): clamps on |x_jk|^2, |m|^2, |n|^2 and |m||n|
     const double nmn_d = fmax(sqrt(fmax(mm_d, (double)SMALL)) * sqrt(fmax(nn_d, (double)SMALL)), (double)SMALL);
     const double cphi_d = m_n / nmn_d;
-    if (fabs(cphi_d) < (double)SMALL) return f3(0.f, 0.f, 0.f);
+    if (fabs(cphi_d) < (double)SMALL) {
+        f[0] = f[1] = f[2] = f[3] = f3(0.f, 0.f, 0.f);
+        return;
+    }
     const double sphi_d = mxn_jk / (nmn_d * sqrt(fmax(jk2_d, (double)SMALL)));
     const double phi_d = -atan2(sphi_d, cphi_d);
-    const float dVdphi = (float)(-(double)kf * (double)mult * sin((double)mult * phi_d - (double)phi0));
+    const double dVdphi_d = -(double)kf * (double)mult * sin((double)mult * phi_d - (double)phi0);
     if (jk2_d >= SMALL && mm_d >= SMALL && nn_d >= SMALL && sqrt(mm_d) * sqrt(nn_d) >= SMALL) {
         // No clamp of the reference is active, so its gradient equals the analytic one.  Taken in the
         // form of Blondel & Karplus (J. Comput. Chem. 17, 1132 (1996)) with F = x_ji, G = x_kj,
-        // H = x_kl, A = F x G (= m), B = H x G (= -n), in FP32: no term cancels unless A or B
-        // vanishes.  The coefficients of the middle atoms, |G|/|A|^2 + F.G/(|A|^2 |G|) and
-        // H.G/(|B|^2 |G|) - |G|/|B|^2, are G.(x_i - x_k)/(|A|^2 |G|) and G.(x_l - x_j)/(|B|^2 |G|),
-        // formed from exact sums so that they keep their digits when the two parts cancel.  The
-        // reference's phi is -(phi_BK +- pi), so its force -dV/dphi dphi/dx = dV/dphi dphi_BK/dx.
-        const F3 A = cross_ff(xji, lji, xkj, lkj), B = cross_ff(xkl, lkl, xkj, lkj);
-        const float A2 = dot(A, A), B2 = dot(B, B);
-        const float Gn = sqrtf(dot(xkj, xkj));
-        F3 gr;
-        if (role == 0) {
-            gr = (-Gn / A2) * A;
-        } else if (role == 3) {
-            gr = (Gn / B2) * B;
-        } else if (role == 1) {
-            const F3 xik = ff_sum3(xji, lji, xkj, lkj, 1.0f);  // x_i - x_k
-            gr = (dot(xkj, xik) / (A2 * Gn)) * A - (dot(xkl, xkj) / (B2 * Gn)) * B;
-        } else {
-            const F3 xlj = ff_sum3(xkl, lkl, xkj, lkj, -1.0f);  // x_l - x_j
-            gr = (dot(xkj, xlj) / (B2 * Gn)) * B - (dot(xji, xkj) / (A2 * Gn)) * A;
-        }
-        return dVdphi * gr;
+        // H = x_kl, A = F x G (= m), B = H x G (= -n).  The coefficients of the middle atoms,
+        // |G|/|A|^2 + F.G/(|A|^2 |G|) and H.G/(|B|^2 |G|) - |G|/|B|^2, are G.(x_i - x_k)/(|A|^2 |G|) and
+        // G.(x_l - x_j)/(|B|^2 |G|).  The middle atoms' forces are differences of an A and a B part that
+        // can cancel, so the gradient is formed in FP64 from the exact differences (once per term, next
+        // to the FP64 angle).  The reference's phi is -(phi_BK +- pi), so its force
+        // -dV/dphi dphi/dx = dV/dphi dphi_BK/dx.
+        const D3 Ad = md, Bd = dneg(nd);
+        const double A2 = mm_d, B2 = nn_d, Gn = sqrt(jk2_d);
+        const D3 xik = dadd(Fd, Gd), xlj = dsub(Hd, Gd);  // x_i - x_k, x_l - x_j
+        const double cA = dVdphi_d / (A2 * Gn), cB = dVdphi_d / (B2 * Gn);
+        f[0] = f3of(dlin(-dVdphi_d * Gn / A2, Ad, 0.0, Bd));
+        f[1] = f3of(dlin(cA * ddot(Gd, xik), Ad, -cB * ddot(Hd, Gd), Bd));
+        f[2] = f3of(dlin(-cA * ddot(Fd, Gd), Ad, cB * ddot(Gd, xlj), Bd));
+        f[3] = f3of(dlin(0.0, Ad, dVdphi_d * Gn / B2, Bd));
+        return;
     }
-    // a clamp is active: the reference's own gradient expression, in FP32 (m and n of the reference)
-    const F3 m = cross_ff(xji, lji, xkj, lkj);
-    const F3 n = (-1.0f) * cross_ff(xkl, lkl, xkj, lkj);
-    const float mm_raw = dot(m, m), nn_raw = dot(n, n), jk2_raw = dot(xjk, xjk);
-    const float xjkn2 = fmaxf(jk2_raw, SMALL);
-    const float xjkn = sqrtf(xjkn2);
-    const float mn2 = fmaxf(mm_raw, SMALL), nn2 = fmaxf(nn_raw, SMALL);
-    const float mn = sqrtf(mn2), nn = sqrtf(nn2);
-    const float nmn = fmaxf(mn * nn, SMALL);
-    const F3 mxn = cross(m, n);
-    const float cphi = (float)cphi_d, sphi = (float)sphi_d;
-    const float sbc = sphi / cphi;
-    const float ppre = -1.0f / (cphi * (1.0f + sbc * sbc));
-    const float cpre = 1.0f / nmn;
-    const float spre = 1.0f / (nmn * xjkn);
-    // gradients of |m| and |n| (TorsionPotential.cpp:95-106)
-    const float jikj = dot(xji, xkj), kljk = dot(xkl, xjk);
-    const F3 dmn2_dxi = (2.0f * xjkn2) * xji - (2.0f * jikj) * xkj;
-    const F3 dmn2_dxk = (-2.0f * dot(xji, xji)) * xkj + (2.0f * jikj) * xji;
-    const F3 dnn2_dxl = (2.0f * xjkn2) * xkl - (2.0f * kljk) * xjk;
-    const F3 dnn2_dxj = (-2.0f * dot(xkl, xkl)) * xjk + (2.0f * kljk) * xkl;
-    const float i2m = 1.0f / (2.0f * mn), i2n = 1.0f / (2.0f * nn);
-    // the participant's derivatives.  With the skew tensors of the reference:
+    // A clamp is active: the reference's own gradient expression (TorsionPotential.cpp:70-159), with m
+    // and n of the reference, in FP64 from the exact differences (near-collinear atoms make it
+    // ill-conditioned).  With the skew tensors of the reference:
     //   v * dm_dxi = x_kj x v, v * dm_dxk = x_ji x v, v * dn_dxj = x_kl x v, v * dn_dxl = -(x_kj x v)
     //   x_jk * dmxn_dx = d(m x n) contracted with x_jk
-    F3 dc, ds;
-    if (role == 0) {  // x_i: m depends on x_ji, n does not
-        const F3 dmn = i2m * dmn2_dxi;
-        const F3 n_dm = cross(xkj, n);
-        dc = cpre * (n_dm - (cphi * nn) * dmn);
+    const D3 &xji_d = Fd, &xkj_d = Gd, &xkl_d = Hd, &xjk_d = jkd, &m = md, &n = nd;
+    const double S = (double)SMALL;
+    const double xjkn2 = fmax(jk2_d, S), xjkn = sqrt(xjkn2);
+    const double mn = sqrt(fmax(mm_d, S)), nn = sqrt(fmax(nn_d, S));
+    const double nmn = fmax(mn * nn, S);
+    const D3 mxn = dcross(m, n);
+    const double cphi = cphi_d, sphi = sphi_d;
+    const double sbc = sphi / cphi;
+    const double ppre = -1.0 / (cphi * (1.0 + sbc * sbc));
+    const double cpre = 1.0 / nmn, spre = 1.0 / (nmn * xjkn);
+    // gradients of |m| and |n| (TorsionPotential.cpp:95-106)
+    const double jikj = ddot(xji_d, xkj_d), kljk = ddot(xkl_d, xjk_d);
+    const D3 dmn2_dxi = (2.0 * xjkn2) * xji_d - (2.0 * jikj) * xkj_d;
+    const D3 dmn2_dxk = (-2.0 * ddot(xji_d, xji_d)) * xkj_d + (2.0 * jikj) * xji_d;
+    const D3 dnn2_dxl = (2.0 * xjkn2) * xkl_d - (2.0 * kljk) * xjk_d;
+    const D3 dnn2_dxj = (-2.0 * ddot(xkl_d, xkl_d)) * xjk_d + (2.0 * kljk) * xkl_d;
+    const double i2m = 1.0 / (2.0 * mn), i2n = 1.0 / (2.0 * nn);
+    const D3 nxj = dcross(n, xjk_d), jxm = dcross(xjk_d, m);
+    auto force_of = [&](const D3 &dc, const D3 &ds) { return f3of((-dVdphi_d * ppre) * (ds - sbc * dc)); };
+    {  // x_i: m depends on x_ji, n does not
+        const D3 dmn = i2m * dmn2_dxi;
+        const D3 dc = cpre * (dcross(xkj_d, n) - (cphi * nn) * dmn);
         // x_jk . (dm/dxi_c x n) = (n x x_jk) . dm/dxi_c = (x_kj x (n x x_jk))_c
-        const F3 v = cross(xkj, cross(n, xjk));
-        ds = spre * (v - (sphi * nn * xjkn) * dmn);
-    } else if (role == 3) {  // x_l: only n depends on x_kl
-        const F3 dnn = i2n * dnn2_dxl;
-        const F3 m_dn = (-1.0f) * cross(xkj, m);
-        dc = cpre * (m_dn - (cphi * mn) * dnn);
-        // x_jk . (m x dn/dxl_c) = (x_jk x m) . dn/dxl_c ; dn/dxl_c = -(skew(x_kj) col c)
-        const F3 v = (-1.0f) * cross(xkj, cross(xjk, m));
-        ds = spre * (v - (sphi * mn * xjkn) * dnn);
-    } else if (role == 1) {  // x_j
-        const F3 dmn = i2m * ((-1.0f) * (dmn2_dxi + dmn2_dxk));
-        const F3 dnn = i2n * dnn2_dxj;
-        // dm_dxj = -(dm_dxk + dm_dxi), dn_dxj = skew(x_kl)
-        const F3 n_dm = (-1.0f) * (cross(xji, n) + cross(xkj, n));
-        const F3 m_dn = cross(xkl, m);
-        dc = cpre * (n_dm + m_dn - (cphi * nn) * dmn - (cphi * mn) * dnn);
-        const F3 nxj = cross(n, xjk), jxm = cross(xjk, m);
-        const F3 v = (-1.0f) * (cross(xji, nxj) + cross(xkj, nxj)) + cross(xkl, jxm);
-        ds = spre * (v - mxn - (sphi * nn * xjkn) * dmn - (sphi * mn * xjkn) * dnn + (sphi * nmn / xjkn) * xjk);
-    } else {  // role 2, x_k
-        const F3 dmn = i2m * dmn2_dxk;
-        const F3 dnn = i2n * ((-1.0f) * (dnn2_dxl + dnn2_dxj));
-        // dm_dxk = skew(x_ji), dn_dxk = -(dn_dxj + dn_dxl) = -(skew(x_kl) - skew(x_kj))
-        const F3 n_dm = cross(xji, n);
-        const F3 m_dn = (-1.0f) * (cross(xkl, m) - cross(xkj, m));
-        dc = cpre * (n_dm + m_dn - (cphi * nn) * dmn - (cphi * mn) * dnn);
-        const F3 nxj = cross(n, xjk), jxm = cross(xjk, m);
-        const F3 v = cross(xji, nxj) - (cross(xkl, jxm) - cross(xkj, jxm));
-        ds = spre * (v + mxn - (sphi * nn * xjkn) * dmn - (sphi * mn * xjkn) * dnn - (sphi * nmn / xjkn) * xjk);
+        const D3 ds = spre * (dcross(xkj_d, nxj) - (sphi * nn * xjkn) * dmn);
+        f[0] = force_of(dc, ds);
     }
-    const F3 dphi = ppre * (ds - sbc * dc);
-    return (-dVdphi) * dphi;
+    {  // x_j: dm_dxj = -(dm_dxk + dm_dxi), dn_dxj = skew(x_kl)
+        const D3 dmn = i2m * (-(dmn2_dxi + dmn2_dxk));
+        const D3 dnn = i2n * dnn2_dxj;
+        const D3 n_dm = -(dcross(xji_d, n) + dcross(xkj_d, n));
+        const D3 dc = cpre * (n_dm + dcross(xkl_d, m) - (cphi * nn) * dmn - (cphi * mn) * dnn);
+        const D3 v = -(dcross(xji_d, nxj) + dcross(xkj_d, nxj)) + dcross(xkl_d, jxm);
+        const D3 ds = spre * (v - mxn - (sphi * nn * xjkn) * dmn - (sphi * mn * xjkn) * dnn + (sphi * nmn / xjkn) * xjk_d);
+        f[1] = force_of(dc, ds);
+    }
+    {  // x_k: dm_dxk = skew(x_ji), dn_dxk = -(dn_dxj + dn_dxl) = -(skew(x_kl) - skew(x_kj))
+        const D3 dmn = i2m * dmn2_dxk;
+        const D3 dnn = i2n * (-(dnn2_dxl + dnn2_dxj));
+        const D3 m_dn = -(dcross(xkl_d, m) - dcross(xkj_d, m));
+        const D3 dc = cpre * (dcross(xji_d, n) + m_dn - (cphi * nn) * dmn - (cphi * mn) * dnn);
+        const D3 v = dcross(xji_d, nxj) - (dcross(xkl_d, jxm) - dcross(xkj_d, jxm));
+        const D3 ds = spre * (v + mxn - (sphi * nn * xjkn) * dmn - (sphi * mn * xjkn) * dnn - (sphi * nmn / xjkn) * xjk_d);
+        f[2] = force_of(dc, ds);
+    }
+    {  // x_l: only n depends on x_kl; dn/dxl_c = -(skew(x_kj) col c)
+        const D3 dnn = i2n * dnn2_dxl;
+        const D3 dc = cpre * (-dcross(xkj_d, m) - (cphi * mn) * dnn);
+        // x_jk . (m x dn/dxl_c) = (x_jk x m) . dn/dxl_c
+        const D3 ds = spre * (-dcross(xkj_d, jxm) - (sphi * mn * xjkn) * dnn);
+        f[3] = force_of(dc, ds);
+    }
 }
 
 }  // namespace rdc

@@ -153,6 +153,13 @@ struct SysDev {
     const float4 *angle_par; // (k, theta0, pi - theta0, -)
     const int4 *dih_idx;
     const float4 *dih_par;
+    // where each term's role forces go: its entries in top_terms (bond: x, y; angle: x, y, z; dihedral:
+    // x, y, z, w), and the per-entry forces (w: the term's energy on its role-0 entry)
+    int n_bonds, n_angles, n_dihedrals;
+    const int2 *bond_at;
+    const int4 *angle_at;
+    const int4 *dih_at;
+    float4 *term_force;
     // observables
     unsigned long long *counts_ring;
     int counts_stride;
@@ -163,7 +170,7 @@ struct SysDev {
 constexpr int FORCE_BLOCKS = 4 * 152;
 constexpr int FORCE_THREADS = 256;
 #ifndef RDC_BONDED_BLOCKS
-#define RDC_BONDED_BLOCKS 152
+#define RDC_BONDED_BLOCKS (4 * 152)
 #endif
 constexpr int BONDED_BLOCKS = RDC_BONDED_BLOCKS;
 constexpr int GRID_BLOCKS = 8 * 152;

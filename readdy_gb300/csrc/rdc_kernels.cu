@@ -284,44 +284,65 @@ __global__ void k_virial_final(SysDev s) {
 }
 
 // ------------------------------------------------------------------------------------------------
-// K4 bonded terms, one thread per topology particle gathering every term it takes part in
+// K4 bonded terms: one thread per term evaluates it once and writes every participant's force to the
+// term's entries of the per-particle term lists; one thread per topology particle then sums its
+// entries in list order and adds them to its force
 // ------------------------------------------------------------------------------------------------
-__global__ void k_bonded(SysDev s) {
+__global__ void k_bonded_terms(SysDev s) {
     const Geo &g = s.geo;
+    const int nb = s.n_bonds, na = s.n_angles, nd = s.n_dihedrals;
     double esum = 0.0;
+    GRID_STRIDE(t, nb + na + nd) {
+        float e = 0.f;
+        if (t < nb) {
+            const int4 I = s.bond_idx[t];
+            const float4 P = s.bond_par[t];
+            const int2 at = s.bond_at[t];
+            F3 f = f3(0.f, 0.f, 0.f);
+            if (P.x != 0.0f)  // terms with k = 0 are skipped (CPUTopologyActions.cpp:62)
+                f = bond_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], P, g, e);
+            s.term_force[at.x] = make_float4(f.x, f.y, f.z, e);
+            s.term_force[at.y] = make_float4(-f.x, -f.y, -f.z, 0.f);
+        } else if (t < nb + na) {
+            const int k = t - nb;
+            const int4 I = s.angle_idx[k];
+            const int4 at = s.angle_at[k];
+            F3 f[3];
+            angle_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], s.angle_par[k], g, f, e);
+            s.term_force[at.x] = make_float4(f[0].x, f[0].y, f[0].z, e);
+            s.term_force[at.y] = make_float4(f[1].x, f[1].y, f[1].z, 0.f);
+            s.term_force[at.z] = make_float4(f[2].x, f[2].y, f[2].z, 0.f);
+        } else {
+            const int k = t - nb - na;
+            const int4 I = s.dih_idx[k];
+            const float4 P = s.dih_par[k];
+            const int4 at = s.dih_at[k];
+            F3 f[4];
+            dihedral_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], s.pos[s.tloc[I.w]], P.x, P.y,
+                           P.z, g, f, e);
+            s.term_force[at.x] = make_float4(f[0].x, f[0].y, f[0].z, e);
+            s.term_force[at.y] = make_float4(f[1].x, f[1].y, f[1].z, 0.f);
+            s.term_force[at.z] = make_float4(f[2].x, f[2].y, f[2].z, 0.f);
+            s.term_force[at.w] = make_float4(f[3].x, f[3].y, f[3].z, 0.f);
+        }
+        esum += (double)e;
+    }
+    const double b = block_sum_double(esum);
+    if (threadIdx.x == 0) s.epart[FORCE_BLOCKS + blockIdx.x] = b;
+}
+
+__global__ void k_bonded_gather(SysDev s) {
     GRID_STRIDE(t, s.n_top) {
         const int j = s.tloc[t];
         float fx = 0.f, fy = 0.f, fz = 0.f, eown = 0.f;
         for (int q = s.top_off[t]; q < s.top_off[t + 1]; ++q) {
-            const int ref = s.top_terms[q];
-            const int kind = ref >> 28, role = (ref >> 24) & 0xf, idx = ref & 0xffffff;
-            float e = 0.f;
-            F3 f;
-            if (kind == 0) {
-                const int4 I = s.bond_idx[idx];
-                const float4 P = s.bond_par[idx];
-                if (P.x == 0.0f) continue;  // terms with k = 0 are skipped (CPUTopologyActions.cpp:62)
-                f = bond_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], P, g, role, e);
-            } else if (kind == 1) {
-                const int4 I = s.angle_idx[idx];
-                const float4 P = s.angle_par[idx];
-                f = angle_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], P, g, role, e);
-            } else {
-                const int4 I = s.dih_idx[idx];
-                const float4 P = s.dih_par[idx];
-                f = dihedral_force(s.pos[s.tloc[I.x]], s.pos[s.tloc[I.y]], s.pos[s.tloc[I.z]], s.pos[s.tloc[I.w]],
-                                   P.x, P.y, P.z, g, role, e);
-            }
-            fx += f.x; fy += f.y; fz += f.z;
-            if (role == 0) eown += e;  // each term's energy counted once
+            const float4 f = s.term_force[q];
+            fx += f.x; fy += f.y; fz += f.z; eown += f.w;
         }
         float4 cur = s.force[j];
         cur.x += fx; cur.y += fy; cur.z += fz; cur.w += eown;
         s.force[j] = cur;
-        esum += (double)eown;
     }
-    const double b = block_sum_double(esum);
-    if (threadIdx.x == 0) s.epart[FORCE_BLOCKS + blockIdx.x] = b;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -544,7 +565,10 @@ void launch_force_finals(const SysDev &s, bool bonded, cudaStream_t st) {
 void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st, bool finals) {
     if (s.virial) k_pair_forces<true><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
     else k_pair_forces<false><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
-    if (bonded && s.n_top > 0) k_bonded<<<BONDED_BLOCKS, 256, 0, st>>>(s);
+    if (bonded && s.n_top > 0) {
+        k_bonded_terms<<<BONDED_BLOCKS, 256, 0, st>>>(s);
+        k_bonded_gather<<<BONDED_BLOCKS, 256, 0, st>>>(s);
+    }
     if (finals) launch_force_finals(s, bonded, st);
     (void)pair;
 }
