@@ -41,9 +41,9 @@ N_MIN, N_MAX = 200, 20000
 # capture of k_engine_step on the first 512 replicas of the ensemble, divided by its particles), and the
 # same capture's warp instructions per particle-step and issue activity: the bound that applies to this
 # kernel is the instruction stream, not DRAM bandwidth.
-DRAM_BYTES_PER_PARTICLE = (95.71e6 + 99.75e6) / 2097522
-WARP_INST_PER_PARTICLE = 319.44e6 / 2097522
-ISSUE_ACTIVE_PCT = 54.0
+DRAM_BYTES_PER_PARTICLE = (99.62e6 + 104.93e6) / 2097522
+WARP_INST_PER_PARTICLE = 304.89e6 / 2097522
+ISSUE_ACTIVE_PCT = 52.8
 # algorithmic bytes of one fused step per particle: the particle state (float4 position with the type,
 # uint32 id) read once and written once (the pair forces carried between steps, 2 x 16 bytes, are a
 # choice of the implementation and count as traffic, not as algorithmic bytes)

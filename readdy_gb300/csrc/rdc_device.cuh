@@ -742,23 +742,30 @@ __device__ inline void dihedral_force(float4 pi, float4 pj, float4 pk, float4 pl
     const D3 md = dcross(Fd, Gd), nd = dneg(dcross(Hd, Gd)), jkd = dneg(Gd);  // m, n, x_jk of the reference
     const double mm_d = ddot(md, md), nn_d = ddot(nd, nd), jk2_d = ddot(jkd, jkd);
     const double mxn_jk = ddot(dcross(md, nd), jkd), m_n = ddot(md, nd);
-    {   // energy (TorsionPotential.cpp:53-68): clamps on |x_jk| and |m||n|
+    // force (TorsionPotential.cpp:70-159): clamps on |x_jk|^2, |m|^2, |n|^2 and |m||n|
+    const double nmn_d = fmax(sqrt(fmax(mm_d, (double)SMALL)) * sqrt(fmax(nn_d, (double)SMALL)), (double)SMALL);
+    const double cphi_d = m_n / nmn_d;
+    const double sphi_d = mxn_jk / (nmn_d * sqrt(fmax(jk2_d, (double)SMALL)));
+    const bool unclamped = jk2_d >= SMALL && mm_d >= SMALL && nn_d >= SMALL && sqrt(mm_d) * sqrt(nn_d) >= SMALL;
+    double sn, cs;
+    if (unclamped) {
+        // the energy's clamps (TorsionPotential.cpp:53-68, on |x_jk| and |m||n|) are inactive as well: its
+        // angle is the force's, bit for bit, and one sincos gives both
+        sincos((double)mult * -atan2(sphi_d, cphi_d) - (double)phi0, &sn, &cs);
+        e = (float)((double)kf * (1.0 + cs));
+    } else {
         const double xjkn_e = fmax(sqrt(jk2_d), (double)SMALL);
         const double mnn_e = fmax(sqrt(mm_d) * sqrt(nn_d), (double)SMALL);
         const double dih = -atan2(mxn_jk / (mnn_e * xjkn_e), m_n / mnn_e);
         e = (float)((double)kf * (1.0 + cos((double)mult * dih - (double)phi0)));
+        sn = sin((double)mult * -atan2(sphi_d, cphi_d) - (double)phi0);
     }
-    // force (TorsionPotential.cpp:70-159): clamps on |x_jk|^2, |m|^2, |n|^2 and |m||n|
-    const double nmn_d = fmax(sqrt(fmax(mm_d, (double)SMALL)) * sqrt(fmax(nn_d, (double)SMALL)), (double)SMALL);
-    const double cphi_d = m_n / nmn_d;
     if (fabs(cphi_d) < (double)SMALL) {
         f[0] = f[1] = f[2] = f[3] = f3(0.f, 0.f, 0.f);
         return;
     }
-    const double sphi_d = mxn_jk / (nmn_d * sqrt(fmax(jk2_d, (double)SMALL)));
-    const double phi_d = -atan2(sphi_d, cphi_d);
-    const double dVdphi_d = -(double)kf * (double)mult * sin((double)mult * phi_d - (double)phi0);
-    if (jk2_d >= SMALL && mm_d >= SMALL && nn_d >= SMALL && sqrt(mm_d) * sqrt(nn_d) >= SMALL) {
+    const double dVdphi_d = -(double)kf * (double)mult * sn;
+    if (unclamped) {
         // No clamp of the reference is active, so its gradient equals the analytic one.  Taken in the
         // form of Blondel & Karplus (J. Comput. Chem. 17, 1132 (1996)) with F = x_ji, G = x_kj,
         // H = x_kl, A = F x G (= m), B = H x G (= -n).  The coefficients of the middle atoms,
