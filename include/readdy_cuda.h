@@ -53,6 +53,20 @@ int rdc_set_device(int device);
 int rdc_context_create(rdc_context **out, const double box[3], const int periodic[3], double kbt, int n_types,
                        const double *diffusion);
 int rdc_context_destroy(rdc_context *ctx);
+/* TopologyRegistry::addSpatialReaction (readdy/main/model/topologies/TopologyRegistry.cpp:195-236;
+ * SpatialTopologyReaction.h:64-191): (type1 in a topology of topology_type1) + (type2 in a topology of
+ * topology_type2, or a free particle: topology_type2 = -1) -> (type_to1, topology_type_to1) +
+ * (type_to2, topology_type_to2) with a constant rate within radius.  mode in STRMode order: 0 TT_ENZYMATIC,
+ * 1 TT_FUSION, 2 TT_FUSION_ALLOW_SELF, 3 TP_ENZYMATIC, 4 TP_FUSION; a fusion adds the edge between the two
+ * and the result takes topology_type_to1; a self fusion needs the two more than min_graph_distance edges
+ * apart (the descriptor's "distance>").  At least one educt type must be TOPOLOGY flavored (checked when a
+ * system is created). */
+int rdc_context_add_spatial_topology_reaction(rdc_context *ctx, int mode, int type1, int topology_type1, int type2,
+                                              int topology_type2, int type_to1, int topology_type_to1, int type_to2,
+                                              int topology_type_to2, double rate, double radius,
+                                              int min_graph_distance, int *reaction_id);
+/* Context::legacyTopologySelfFusion: with 1, self fusions may also join vertices that share an edge */
+int rdc_context_set_legacy_topology_self_fusion(rdc_context *ctx, int legacy);
 /* ParticleTypeRegistry::add(name, D, flavor) (include/readdy/model/ParticleTypeRegistry.h:58-63,114):
  * 0 NORMAL (the default), 1 TOPOLOGY, 2 MEMBRANE.  Read by rdc_break_bonds. */
 int rdc_context_set_particle_flavor(rdc_context *ctx, int type, int flavor);
@@ -143,6 +157,15 @@ int rdc_add_topology_typed(rdc_system *s, int topology_type, int64_t n, const do
  * they were until the next rdc_calculate_forces.  n_broken (may be NULL) receives the edges removed. */
 int rdc_break_bonds(rdc_system *s, double time_step, int n_pairs, const int *type1, const int *type2,
                     const double *threshold_energy, const double *rate, int64_t *n_broken);
+/* EvaluateTopologyReactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp:86-475) for the spatial
+ * topology reactions of the context: candidate pairs found on the device, events drawn as algo::performEvents
+ * draws them (proportional to rate, without replacement, an accepted event removing those that share its
+ * topologies or free particle), then type changes, graph merges, self edges and particles taken into
+ * topologies; bonded terms derived again.  Needs the neighbor list.  rdc_run evaluates them every step
+ * between the reactions and the forces when the context has any.  n_performed may be NULL. */
+int rdc_evaluate_topology_reactions(rdc_system *s, double time_step, int64_t *n_performed);
+/* performed events per spatial topology reaction (n = the number registered) since creation */
+int rdc_get_topology_reaction_counts(rdc_system *s, int n, int64_t *counts);
 /* StateModel::getTopologies (StateModel.h:69-117): the active topologies as CSR, topology k has type
  * topology_types[k] and the particles ids[offsets[k] .. offsets[k+1]) (offsets holds n_topologies + 1
  * entries).  n_topologies and n_ids are written first; RDC_ERR_CAPACITY if either capacity is smaller.

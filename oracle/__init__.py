@@ -70,6 +70,10 @@ def _load():
             "orc_break_bonds": (i, [vp, d, i, P(i), P(i), P(d), P(d), P(i64)]),
             "orc_get_topologies": (i, [vp, P(i), P(i64), P(u64), P(i64), P(i64)]),
             "orc_get_topology_edges": (i, [vp, P(i64), P(u64), P(i64)]),
+            "orc_add_spatial_topology_reaction": (i, [vp, i, i, i, i, i, i, i, i, i, d, d, i]),
+            "orc_set_legacy_topology_self_fusion": (i, [vp, i]),
+            "orc_evaluate_topology_reactions": (i, [vp, d, P(i64)]),
+            "orc_topology_reaction_counts": (i, [vp, P(i64), i]),
             "orc_add_particles": (i, [vp, i, P(d), P(i)]),
             "orc_n_particles": (i, [vp]),
             "orc_n_entries": (i, [vp]),
@@ -257,6 +261,29 @@ class OracleSystem:
         self._check(self._lib.orc_break_bonds(self._h, dt, len(pairs), _ptr(t1, C.c_int), _ptr(t2, C.c_int),
                                               _ptr(thr, C.c_double), _ptr(rate, C.c_double), C.byref(nb)))
         return nb.value
+
+    def add_spatial_topology_reaction(self, mode, educt1, educt2, product1, product2, rate, radius,
+                                      min_graph_distance=0):
+        tt2 = -1 if educt2[1] is None else int(educt2[1])
+        tto2 = -1 if product2[1] is None else int(product2[1])
+        self._n_spatial = getattr(self, "_n_spatial", 0) + 1
+        return self._check(self._lib.orc_add_spatial_topology_reaction(
+            self._h, mode, educt1[0], educt1[1], educt2[0], tt2, product1[0], product1[1], product2[0], tto2,
+            rate, radius, min_graph_distance))
+
+    def set_legacy_topology_self_fusion(self, legacy):
+        return self._check(self._lib.orc_set_legacy_topology_self_fusion(self._h, int(bool(legacy))))
+
+    def evaluate_topology_reactions(self, dt):
+        n = C.c_int64()
+        self._check(self._lib.orc_evaluate_topology_reactions(self._h, dt, C.byref(n)))
+        return n.value
+
+    def topology_reaction_counts(self):
+        n = getattr(self, "_n_spatial", 0)
+        out = np.zeros(max(n, 1), np.int64)
+        self._lib.orc_topology_reaction_counts(self._h, _ptr(out, C.c_int64), n)
+        return out[:n]
 
     def topologies(self):
         """[(topology type, particle ids[] uint64)]"""

@@ -410,6 +410,20 @@ struct orc_system {
     std::vector<Graph> graphs;
     uint64_t breakCalls = 0;
 
+    /* spatial topology reactions (SpatialTopologyReaction.h:64-191), STRMode order */
+    struct Spatial {
+        int mode;
+        int t1, tt1, t2, tt2, to1, tto1, to2, tto2;
+        double rate, radius;
+        int minGraphDistance;
+        bool allowSelf() const { return mode == 2; }
+        bool fusion() const { return mode == 1 || mode == 2 || mode == 4; }
+        bool tp() const { return tt2 == -1; }
+    };
+    std::vector<Spatial> spatial;
+    bool legacySelfFusion = false;
+    std::vector<int64_t> spatialCounts;
+
     std::vector<Entry> entries;
     std::vector<size_t> blanks;
     uint64_t nextId = 0;
@@ -516,6 +530,185 @@ struct orc_system {
         for (auto &g : graphs) configureGraph(g, ids);
     }
 
+    /* CPUEvaluateTopologyReactions::perform for the spatial reactions
+     * (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp:86-475): gatherEvents over the cells,
+     * algo::performEvents (include/readdy/common/algorithm.h:62-136) with eventsDependent, and the
+     * handlers handleTopologyParticleReaction / handleTopologyTopologyReaction; bonded terms derived again
+     * at the end (each handler configures its topology; configure depends on the graph only). */
+    struct TREvent {
+        double rate, cumulativeRate;
+        long g1, g2;  // topology indices (g2 = -1: topology-particle)
+        const Spatial *r;
+        size_t idx1, idx2;  // idx1 belongs to a topology
+    };
+    int64_t evaluateTopologyReactions(double dt) {
+        if (spatialCounts.size() != spatial.size()) spatialCounts.assign(spatial.size(), 0);
+        if (spatial.empty() || graphs.empty()) return 0;
+        if (!nlSetUp) throw std::logic_error("neighbor list not set up");
+        const IdMap idx = idMap();
+        std::vector<long> topOf(entries.size(), -1);
+        std::vector<int> vertexOf(entries.size(), -1);
+        for (size_t gi = 0; gi < graphs.size(); ++gi)
+            for (size_t v = 0; v < graphs[gi].ids.size(); ++v) {
+                const size_t pi = indexOf(idx, graphs[gi].ids[v]);
+                topOf[pi] = (long)gi;
+                vertexOf[pi] = (int)v;
+            }
+        std::vector<char> spatialType(nTypes, 0);
+        for (auto &r : spatial) spatialType[r.t1] = spatialType[r.t2] = 1;
+        auto graphDistance = [&](const Graph &g, int from, int to) {
+            std::vector<std::vector<int>> nb(g.ids.size());
+            for (auto &e : g.edges) { nb[e.first].push_back(e.second); nb[e.second].push_back(e.first); }
+            std::vector<int> dist(g.ids.size(), -1);
+            std::vector<int> q{from};
+            dist[from] = 0;
+            for (size_t k = 0; k < q.size(); ++k)
+                for (int w : nb[q[k]]) if (dist[w] < 0) { dist[w] = dist[q[k]] + 1; q.push_back(w); }
+            return dist[to];
+        };
+        std::vector<TREvent> events;
+        for (size_t cell = 0; cell < adjacency.size(); ++cell) {
+            forEachInCell(cell, [&](size_t ip) {
+                const Entry &en = entries[ip];
+                if (en.deactivated || !spatialType[en.type]) return;
+                const bool hasEntryTop = topOf[ip] >= 0;
+                forEachNeighbor(ip, cell, [&](size_t jn) {
+                    const Entry &nb = entries[jn];
+                    if (nb.deactivated) return;
+                    const bool hasNbTop = topOf[jn] >= 0;
+                    if ((!hasEntryTop && !hasNbTop) || (hasNbTop && ip > jn)) return;
+                    const long tt1 = hasEntryTop ? graphs[topOf[ip]].type : -1;
+                    const long tt2 = hasNbTop ? graphs[topOf[jn]].type : -1;
+                    const double d2 = box.dist2(en.pos, nb.pos);
+                    for (const auto &r : spatial) {
+                        // spatialReactionsByType: the key matches in either order (TopologyParticleTypeMap.h:60-92)
+                        const bool fwd = r.t1 == en.type && r.tt1 == tt1 && r.t2 == nb.type && r.tt2 == tt2;
+                        const bool bwd = r.t1 == nb.type && r.tt1 == tt2 && r.t2 == en.type && r.tt2 == tt1;
+                        if (!fwd && !bwd) continue;
+                        if (!r.allowSelf() && topOf[ip] == topOf[jn]) continue;
+                        if (!(d2 < r.radius * r.radius)) continue;
+                        TREvent ev{r.rate, 0, -1, -1, &r, ip, jn};
+                        if (hasEntryTop && !hasNbTop) { ev.g1 = topOf[ip]; ev.idx1 = ip; ev.idx2 = jn; }
+                        else if (!hasEntryTop && hasNbTop) { ev.g1 = topOf[jn]; ev.idx1 = jn; ev.idx2 = ip; }
+                        else { ev.g1 = topOf[ip]; ev.g2 = topOf[jn]; }
+                        if (r.allowSelf() && topOf[ip] == topOf[jn]) {
+                            const int dg = graphDistance(graphs[topOf[ip]], vertexOf[ev.idx1], vertexOf[ev.idx2]);
+                            if ((dg != -1 && dg <= r.minGraphDistance) || (!legacySelfFusion && dg == 1)) continue;
+                        }
+                        events.push_back(ev);
+                    }
+                });
+            });
+        }
+        auto dependent = [](const TREvent &a, const TREvent &b) {  // eventsDependent, :459-468
+            if (a.g1 == b.g1 || a.g1 == b.g2) return true;
+            if (a.g2 < 0 && b.g2 < 0 && a.idx2 == b.idx2) return true;
+            return a.g2 >= 0 && (a.g2 == b.g1 || a.g2 == b.g2);
+        };
+        std::vector<char> dead(graphs.size(), 0);
+        int64_t performed = 0;
+        auto eval = [&](const TREvent &ev) {
+            const Spatial &r = *ev.r;
+            Entry &e1 = entries[ev.idx1];
+            Entry &e2 = entries[ev.idx2];
+            Graph &t1 = graphs[ev.g1];
+            if (ev.g2 < 0) {  // handleTopologyParticleReaction, :322-358
+                const bool first = e1.type == r.t1;
+                const int n1 = first ? r.to1 : r.to2, n2 = first ? r.to2 : r.to1;
+                e1.type = n1;
+                e2.type = n2;
+                if (r.fusion()) {
+                    t1.ids.push_back(e2.id);
+                    t1.edges.push_back({(int)t1.ids.size() - 1, vertexOf[ev.idx1]});
+                    topOf[ev.idx2] = ev.g1;
+                    vertexOf[ev.idx2] = (int)t1.ids.size() - 1;
+                }
+                t1.type = t1.type == r.tt1 ? r.tto1 : r.tto2;
+            } else {  // handleTopologyTopologyReaction, :360-457
+                Graph &t2 = graphs[ev.g2];
+                if (r.fusion() && ev.g1 == ev.g2) {
+                    const int a = vertexOf[ev.idx1], b = vertexOf[ev.idx2];
+                    bool present = false;
+                    for (auto &e : t1.edges) present |= (e.first == a && e.second == b) || (e.first == b && e.second == a);
+                    if (!present) t1.edges.push_back({a, b});
+                    t1.type = r.tto1;
+                    const bool first = e1.type == r.t1;
+                    const int n1 = first ? r.to1 : r.to2, n2 = first ? r.to2 : r.to1;
+                    e1.type = n1;
+                    e2.type = n2;
+                } else {
+                    int tto1 = r.tto1, tto2 = r.tto2;
+                    if (e1.type == r.t1 && t1.type == r.tt1) { e1.type = r.to1; e2.type = r.to2; }
+                    else { std::swap(tto1, tto2); e1.type = r.to2; e2.type = r.to1; }
+                    if (r.fusion()) {  // GraphTopology::appendTopology: t2 joins t1 with the edge idx1 -- idx2
+                        const int off = (int)t1.ids.size();
+                        for (size_t v = 0; v < t2.ids.size(); ++v) {
+                            t1.ids.push_back(t2.ids[v]);
+                            const size_t pi = indexOf(idx, t2.ids[v]);
+                            topOf[pi] = ev.g1;
+                            vertexOf[pi] = off + (int)v;
+                        }
+                        for (auto &e : t2.edges) t1.edges.push_back({off + e.first, off + e.second});
+                        t1.edges.push_back({vertexOf[ev.idx2], vertexOf[ev.idx1]});
+                        t1.type = r.tto1;
+                        t2.ids.clear();
+                        t2.edges.clear();
+                        dead[ev.g2] = 1;
+                    } else {
+                        t1.type = tto1;
+                        t2.type = tto2;
+                    }
+                }
+            }
+            ++spatialCounts[ev.r - spatial.data()];
+            ++performed;
+        };
+        if (!events.empty()) {  // algo::performEvents
+            size_t nDeact = 0;
+            const size_t nEvents = events.size();
+            double cum = 0;
+            for (auto &ev : events) { ev.cumulativeRate = ev.rate + cum; cum = ev.cumulativeRate; }
+            while (nDeact < nEvents) {
+                const double cr = (events.end() - nDeact - 1)->cumulativeRate;
+                const double x = uniform(0, 0., cr);
+                auto it = std::lower_bound(events.begin(), events.end() - nDeact, x,
+                                           [](const TREvent &e, double v) { return e.cumulativeRate < v; });
+                if (it == events.end()) throw std::logic_error("performEvents: no event could be selected");
+                if (coin(0, it->rate, dt)) {
+                    const TREvent done = *it;
+                    eval(done);
+                    auto j = events.begin();
+                    double cs = 0;
+                    while (j < events.end() - nDeact) {
+                        if (dependent(*j, done)) {
+                            ++nDeact;
+                            std::iter_swap(j, events.end() - nDeact);
+                        } else {
+                            cs += j->rate;
+                            j->cumulativeRate = cs;
+                            ++j;
+                        }
+                    }
+                } else {
+                    ++nDeact;
+                    std::iter_swap(it, events.end() - nDeact);
+                    it->cumulativeRate = it->rate;
+                    if (it > events.begin()) it->cumulativeRate += (it - 1)->cumulativeRate;
+                    double c2 = it->cumulativeRate;
+                    for (auto j = it + 1; j < events.end() - nDeact; ++j) { c2 += j->rate; j->cumulativeRate = c2; }
+                }
+            }
+        }
+        if (performed > 0) {
+            std::vector<Graph> kept;
+            for (size_t gi = 0; gi < graphs.size(); ++gi)
+                if (!dead[gi]) kept.push_back(std::move(graphs[gi]));
+            graphs = std::move(kept);
+            configureTopologies();
+        }
+        return performed;
+    }
+
     /* BreakBonds::genericPerform (include/readdy/model/actions/Actions.h:236-290): per topology and per
      * edge, the energy of the edge's bond configurations (evaluateEdgeEnergy, :292-342; harmonic bond
      * energy of BondedPotential.h) against the type pair's threshold, then a coin
@@ -609,6 +802,7 @@ struct orc_system {
         double c = 0;
         for (auto &e : pot2) for (auto &p : e.second) c = std::max(c, std::sqrt(p.cutoff2));
         for (auto &e : o2) for (auto *r : e.second) c = std::max(c, r->eductDistance);
+        for (auto &r : spatial) c = std::max(c, r.radius);  // Context::calculateMaxCutoff
         return c;
     }
 
@@ -1396,6 +1590,30 @@ int orc_break_bonds(orc_system *s, double dt, int n, const int *t1, const int *t
         return -1;
     }
 }
+int orc_add_spatial_topology_reaction(orc_system *s, int mode, int t1, int tt1, int t2, int tt2, int to1, int tto1,
+                                      int to2, int tto2, double rate, double radius, int min_graph_distance) {
+    s->spatial.push_back({mode, t1, tt1, t2, tt2, to1, tto1, to2, tt2 == -1 ? -1 : tto2, rate, radius,
+                          min_graph_distance});
+    return (int)s->spatial.size() - 1;
+}
+int orc_set_legacy_topology_self_fusion(orc_system *s, int legacy) {
+    s->legacySelfFusion = legacy != 0;
+    return 0;
+}
+int orc_evaluate_topology_reactions(orc_system *s, double dt, int64_t *n_performed) {
+    try {
+        const int64_t n = s->evaluateTopologyReactions(dt);
+        if (n_performed) *n_performed = n;
+        return 0;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+int orc_topology_reaction_counts(const orc_system *s, int64_t *counts, int n) {
+    for (int k = 0; k < n; ++k) counts[k] = k < (int)s->spatialCounts.size() ? s->spatialCounts[k] : 0;
+    return 0;
+}
 /* topologies as CSR over particle ids (any output may be NULL; sizes first) */
 int orc_get_topologies(const orc_system *s, int *types, int64_t *offsets, uint64_t *ids, int64_t *n_top,
                        int64_t *n_ids) {
@@ -1554,6 +1772,12 @@ int orc_run(orc_system *s, int64_t n_steps, double dt, int handler, int stride, 
             if (!s->reactions.empty()) {
                 if (handler == ORC_GILLESPIE) s->gillespie(dt);
                 else s->uncontrolledApproximation(dt);
+            }
+            // runTopologyReactions (SimulationLoop.h:285); the cells are refreshed first so that particles the
+            // reactions created take part
+            if (!s->spatial.empty() && !s->graphs.empty()) {
+                if (nl) s->nlUpdate();
+                s->evaluateTopologyReactions(dt);
             }
             if (nl) s->nlUpdate();
             s->calculateForces();

@@ -76,6 +76,13 @@ int orc_break_bonds(orc_system *s, double dt, int n, const int *t1, const int *t
 int orc_get_topologies(const orc_system *s, int *types, int64_t *offsets, uint64_t *ids, int64_t *n_top,
                        int64_t *n_ids);
 int orc_get_topology_edges(const orc_system *s, int64_t *offsets, uint64_t *edges2, int64_t *n_edges);
+/* spatial topology reactions (TopologyRegistry::addSpatialReaction; mode in STRMode order, tt2 = -1 for a free
+ * particle) and EvaluateTopologyReactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp) */
+int orc_add_spatial_topology_reaction(orc_system *s, int mode, int t1, int tt1, int t2, int tt2, int to1, int tto1,
+                                      int to2, int tto2, double rate, double radius, int min_graph_distance);
+int orc_set_legacy_topology_self_fusion(orc_system *s, int legacy);
+int orc_evaluate_topology_reactions(orc_system *s, double dt, int64_t *n_performed);
+int orc_topology_reaction_counts(const orc_system *s, int64_t *counts, int n);
 
 /* particles */
 int orc_add_particles(orc_system *s, int n, const double *pos3, const int *types);

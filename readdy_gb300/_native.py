@@ -46,6 +46,8 @@ def _sig(lib):
         "rdc_context_max_cutoff": (i, [vp, P(d)]),
         "rdc_context_set_record_virial": (i, [vp, i]),
         "rdc_context_set_particle_flavor": (i, [vp, i, i]),
+        "rdc_context_add_spatial_topology_reaction": (i, [vp, i, i, i, i, i, i, i, i, i, d, d, i, P(i)]),
+        "rdc_context_set_legacy_topology_self_fusion": (i, [vp, i]),
         "rdc_get_virial": (i, [vp, P(d)]),
         "rdc_context_add_harmonic_repulsion": (i, [vp, i, i, d, d]),
         "rdc_context_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
@@ -71,6 +73,8 @@ def _sig(lib):
         "rdc_add_topology_typed": (i, [vp, i, i64, P(d), P(i), i64, P(i64), P(u64)]),
         "rdc_break_bonds": (i, [vp, d, i, P(i), P(i), P(d), P(d), P(i64)]),
         "rdc_get_topologies": (i, [vp, i64, P(i), P(i64), i64, P(u64), P(i64), P(i64)]),
+        "rdc_evaluate_topology_reactions": (i, [vp, d, P(i64)]),
+        "rdc_get_topology_reaction_counts": (i, [vp, i, P(i64)]),
         "rdc_get_topology_edges": (i, [vp, i64, P(i64), i64, P(u64), P(i64), P(i64)]),
         "rdc_get_n_particles": (i, [vp, P(i64)]),
         "rdc_get_particles": (i, [vp, i64, P(d), P(i), P(u64), P(i64)]),

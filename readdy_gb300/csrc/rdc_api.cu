@@ -12,9 +12,11 @@
 #include <memory>
 #include <string>
 #include <tuple>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/readdy_cuda.h"
+#include "rdc_device.cuh"  // Philox streams (rng_draw) for the host's topology-reaction draws
 #include "rdc_host.h"
 
 using namespace rdc;
@@ -112,6 +114,7 @@ double ContextData::max_cutoff() const {
     for (auto &p : pots) c = std::max(c, p.cutoff);
     for (auto &r : reactions)
         if (r.n_educts == 2) c = std::max(c, r.educt_distance);
+    for (auto &r : spatial_top) c = std::max(c, r.radius);  // Context::calculateMaxCutoff
     return c;
 }
 
@@ -344,6 +347,11 @@ struct rdc_system {
     std::vector<int> slot_type;       // particle type per topology slot
     std::vector<uint32_t> slot_id;    // particle id per topology slot
     uint64_t break_calls = 0;         // BreakBonds calls so far: keys their coins
+    uint64_t topo_calls = 0;          // topology reaction evaluations so far: keys their clocks and coins
+    std::vector<uint64_t> topo_counts;  // performed events per spatial topology reaction
+    TopCandidate *cand_dev = nullptr;
+    int cand_cap = 0;
+    double topo_dt = 0;               // > 0: run() evaluates topology reactions every step with this time step
     int4 *edge_dev = nullptr;
     double2 *bond_kl_dev = nullptr;
     int2 *bond_at_dev = nullptr;
@@ -378,6 +386,7 @@ struct rdc_system {
         dfree(bond_par_dev); dfree(angle_par_dev); dfree(dih_par_dev);
         dfree(edge_dev); dfree(bond_kl_dev);
         dfree(bond_at_dev); dfree(angle_at_dev); dfree(dih_at_dev); dfree(term_force_dev);
+        dfree(cand_dev);
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -615,6 +624,8 @@ struct rdc_system {
     void upload_topology(bool sort_new_particles = true);
     int64_t break_bonds(double dt, int n_pairs, const int *t1, const int *t2, const double *threshold,
                         const double *rate);
+    int64_t evaluate_topology_reactions(double dt);
+    void grow_topology_slots(int n_new);
 
     // ---- SimulationLoop::run ----
     void run(int64_t n_steps, double dt, int handler, int64_t stride, int64_t *counts, int64_t max_rec,
@@ -868,6 +879,220 @@ int64_t rdc_system::break_bonds(double dt, int n_pairs, const int *t1, const int
     return nb;
 }
 
+// the slot -> storage map grows by n_new slots, its entries kept
+void rdc_system::grow_topology_slots(int n_new) {
+    if (n_new <= 0) return;
+    int *tloc_new = dalloc<int>(n_top + n_new);
+    if (n_top > 0 && d.tloc)
+        RDC_CUDA(cudaMemcpyAsync(tloc_new, d.tloc, sizeof(int) * n_top, cudaMemcpyDeviceToDevice, stream));
+    sync();
+    dfree(d.tloc);
+    d.tloc = tloc_new;
+    n_top += n_new;
+    d.tloc_size = n_top;
+}
+
+// EvaluateTopologyReactions for the spatial reactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp:
+// 86-475).  The device lists the candidate pairs (k_topology_candidates); here each pair becomes an event per
+// reaction that matches its particle and topology types in either order, within the reaction's radius (a
+// self fusion also needs a graph distance above min_graph_distance and, unless the legacy rule is set,
+// above 1).  Events are drawn as algo::performEvents does (include/readdy/common/algorithm.h:62-136) --
+// proportional to rate, without replacement, each with its coin u < 1 - exp(-rate dt), an accepted event
+// removing the events that share one of its topologies or its free particle -- by exponential clocks
+// E/rate with the coins drawn up front (the same distribution; Philox keyed by the ordered ids, the call
+// count and the reaction).  Accepted events change particle and topology types, merge graphs (fusion of
+// two topologies), add an edge (self fusion) or take a free particle into a topology (topology-particle
+// fusion); the bonded terms are then derived again from the graphs.  Each pair is one candidate; the
+// reference lists a topology-particle pair a second time from the free particle's side when that
+// particle's storage index is the lower one.
+int64_t rdc_system::evaluate_topology_reactions(double dt) {
+    require(dt > 0, "time step must be > 0");
+    const auto &RS = ctx.spatial_top;
+    const uint64_t call = topo_calls++;
+    if (topo_counts.size() != RS.size()) topo_counts.assign(RS.size(), 0);
+    if (RS.empty() || graphs.empty()) return 0;
+    if (!nl_ready) throw LogicError("topology reactions: the neighbor list is not set up");
+    const int T = ctx.ntypes;
+    std::vector<uint32_t> mask(T, 0u);
+    double rmax = 0;
+    for (const auto &r : RS) {
+        mask[r.t1] |= 1u << r.t2;
+        mask[r.t2] |= 1u << r.t1;
+        rmax = std::max(rmax, r.radius);
+    }
+    uint32_t *mask_dev = dalloc<uint32_t>(T);
+    int *n_dev = dalloc<int>(1);
+    RDC_CUDA(cudaMemcpyAsync(mask_dev, mask.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, stream));
+    const double r2max = rmax * rmax;
+    const float r2screen = (float)r2max + 2.0f * band_for(rmax, d.geo.L);
+    int nc = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (cand_cap == 0) {
+            cand_cap = 4096;
+            cand_dev = dalloc<TopCandidate>(cand_cap);
+        }
+        launch_topology_candidates(d, mask_dev, r2max, r2screen, cand_dev, n_dev, cand_cap, stream);
+        RDC_CUDA(cudaMemcpyAsync(&nc, n_dev, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        sync();
+        if (nc <= cand_cap) break;
+        dfree(cand_dev);
+        cand_cap = nc + nc / 2;
+        cand_dev = dalloc<TopCandidate>(cand_cap);
+    }
+    dfree(mask_dev);
+    dfree(n_dev);
+    std::vector<TopCandidate> cand(std::min(nc, cand_cap));
+    if (!cand.empty())
+        RDC_CUDA(cudaMemcpyAsync(cand.data(), cand_dev, sizeof(TopCandidate) * cand.size(), cudaMemcpyDeviceToHost,
+                                 stream));
+    sync();
+    // topology and vertex of every slot
+    std::vector<int> slot_graph(n_top, -1), slot_vertex(n_top, -1);
+    for (size_t gi = 0; gi < graphs.size(); ++gi)
+        for (size_t v = 0; v < graphs[gi].slots.size(); ++v) {
+            slot_graph[graphs[gi].slots[v]] = (int)gi;
+            slot_vertex[graphs[gi].slots[v]] = (int)v;
+        }
+    auto graph_of = [&](int slot) { return slot >= 0 && slot < n_top ? slot_graph[slot] : -1; };
+    // graph distance (breadth first) between two vertices of one graph, -1 if not connected
+    auto graph_distance = [&](const TopGraph &g, int from, int to) {
+        const int n = (int)g.slots.size();
+        std::vector<std::vector<int>> adj(n);
+        for (auto &e : g.edges) {
+            adj[e.first].push_back(e.second);
+            adj[e.second].push_back(e.first);
+        }
+        std::vector<int> dist(n, -1);
+        std::vector<int> queue{from};
+        dist[from] = 0;
+        for (size_t q = 0; q < queue.size(); ++q)
+            for (int w : adj[queue[q]])
+                if (dist[w] < 0) {
+                    dist[w] = dist[queue[q]] + 1;
+                    queue.push_back(w);
+                }
+        return dist[to];
+    };
+    struct Event {
+        int r;          // reaction
+        int c;          // candidate
+        bool swap;      // the candidate's j side is the reaction's first educt
+        int g1, g2;     // topologies of the first and second educt (g2 = -1: free particle)
+        double clock;
+        bool fire;
+    };
+    std::vector<Event> ev;
+    for (int c = 0; c < (int)cand.size(); ++c) {
+        const TopCandidate &q = cand[c];
+        const int ga = graph_of(q.si), gb = graph_of(q.sj);
+        if (ga < 0 && gb < 0) continue;
+        const int tta = ga >= 0 ? graphs[ga].type : -1, ttb = gb >= 0 ? graphs[gb].type : -1;
+        for (int k = 0; k < (int)RS.size(); ++k) {
+            const auto &r = RS[k];
+            const bool fwd = r.t1 == q.ti && r.tt1 == tta && r.t2 == q.tj && r.tt2 == ttb;
+            const bool bwd = r.t1 == q.tj && r.tt1 == ttb && r.t2 == q.ti && r.tt2 == tta;
+            if (!fwd && !bwd) continue;
+            const bool swap = !fwd;
+            const int g1 = swap ? gb : ga, g2 = swap ? ga : gb;
+            if (g1 < 0) continue;
+            const bool self = g2 >= 0 && g1 == g2;
+            if (self && r.mode != STR_TT_FUSION_ALLOW_SELF) continue;
+            if (!(q.d2 < r.radius * r.radius)) continue;
+            if (self) {
+                const int dgr = graph_distance(graphs[g1], slot_vertex[q.si], slot_vertex[q.sj]);
+                if ((dgr != -1 && dgr <= r.min_graph_distance) || (!ctx.legacy_self_fusion && dgr == 1)) continue;
+            }
+            const U4 u = rng_draw(seed, std::min(q.idi, q.idj), std::max(q.idi, q.idj), call, RNG_TOPOLOGY, (uint32_t)k);
+            const double e1 = -std::log(((double)(u.x >> 8) + 0.5) * (1.0 / 16777216.0));
+            const bool fire = (((uint64_t)u.y << 32) | u.z) < coin_threshold(r.rate, dt);
+            ev.push_back(Event{k, c, swap, g1, g2, e1 / r.rate, fire});
+        }
+    }
+    if (ev.empty()) return 0;
+    std::vector<int> order(ev.size());
+    for (size_t k = 0; k < ev.size(); ++k) order[k] = (int)k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ev[a].clock < ev[b].clock; });
+    std::vector<char> used(graphs.size(), 0), dead(graphs.size(), 0);
+    std::unordered_set<uint32_t> used_free;
+    std::vector<int4> edits;  // (storage index, type, new slot or -1, -)
+    int64_t performed = 0;
+    for (int k : order) {
+        const Event &e = ev[k];
+        const TopCandidate &q = cand[e.c];
+        const uint32_t free_id = e.g2 < 0 ? (e.swap ? q.idi : q.idj) : 0;
+        if (used[e.g1] || (e.g2 >= 0 && used[e.g2]) || (e.g2 < 0 && used_free.count(free_id))) continue;
+        if (!e.fire) continue;  // a rejected event blocks nothing
+        const auto &r = RS[e.r];
+        // first and second educt: storage index, slot
+        const int i1 = e.swap ? q.j : q.i, i2 = e.swap ? q.i : q.j;
+        const int s1 = e.swap ? q.sj : q.si, s2 = e.swap ? q.si : q.sj;
+        const uint32_t id2 = e.swap ? q.idi : q.idj;
+        TopGraph &g1 = graphs[e.g1];
+        edits.push_back(make_int4(i1, r.to1, -1, 0));
+        slot_type[s1] = r.to1;
+        if (r.mode == STR_TP_ENZYMATIC || r.mode == STR_TP_FUSION) {
+            if (r.mode == STR_TP_FUSION) {
+                const int slot = n_top;
+                grow_topology_slots(1);
+                slot_type.push_back(r.to2);
+                slot_id.push_back(id2);
+                g1.slots.push_back(slot);
+                g1.edges.emplace_back(slot_vertex[s1], (int)g1.slots.size() - 1);
+                edits.push_back(make_int4(i2, r.to2, slot, 0));
+            } else {
+                edits.push_back(make_int4(i2, r.to2, -1, 0));
+            }
+            g1.type = r.tto1;
+            used_free.insert(free_id);
+        } else {
+            edits.push_back(make_int4(i2, r.to2, -1, 0));
+            slot_type[s2] = r.to2;
+            TopGraph &g2 = graphs[e.g2];
+            if (e.g1 == e.g2) {  // self fusion: the edge unless present
+                const std::pair<int, int> edge(slot_vertex[s1], slot_vertex[s2]);
+                bool present = false;
+                for (auto &x : g1.edges)
+                    present |= (x.first == edge.first && x.second == edge.second) ||
+                               (x.first == edge.second && x.second == edge.first);
+                if (!present) g1.edges.push_back(edge);
+                g1.type = r.tto1;
+            } else if (r.mode == STR_TT_ENZYMATIC) {
+                g1.type = r.tto1;
+                g2.type = r.tto2;
+            } else {  // fusion of two topologies: the second joins the first with the new edge
+                const int off = (int)g1.slots.size();
+                for (int sl : g2.slots) g1.slots.push_back(sl);
+                for (auto &x : g2.edges) g1.edges.emplace_back(x.first + off, x.second + off);
+                g1.edges.emplace_back(slot_vertex[s1], off + slot_vertex[s2]);
+                for (size_t v = 0; v < g2.slots.size(); ++v) slot_vertex[g2.slots[v]] = off + (int)v;
+                g1.type = r.tto1;
+                g2.slots.clear();
+                g2.edges.clear();
+                dead[e.g2] = 1;
+            }
+            used[e.g2] = 1;
+        }
+        used[e.g1] = 1;
+        ++topo_counts[e.r];
+        ++performed;
+    }
+    if (performed == 0) return 0;
+    int4 *edit_dev = dalloc<int4>(edits.size());
+    RDC_CUDA(cudaMemcpyAsync(edit_dev, edits.data(), sizeof(int4) * edits.size(), cudaMemcpyHostToDevice, stream));
+    launch_particle_edits(d, edit_dev, (int)edits.size(), stream);
+    sync();
+    dfree(edit_dev);
+    std::vector<TopGraph> kept;
+    for (size_t gi = 0; gi < graphs.size(); ++gi)
+        if (!dead[gi]) kept.push_back(std::move(graphs[gi]));
+    graphs = std::move(kept);
+    Topology fresh;
+    for (size_t gi = 0; gi < graphs.size(); ++gi) configure(graphs[gi], (int)gi, fresh);
+    top = std::move(fresh);
+    upload_topology(false);
+    return performed;
+}
+
 void rdc_system::upload_topology(bool sort_new_particles) {
     // CSR: per topology slot, every (kind, role, term) it takes part in
     std::vector<std::vector<int>> per(n_top);
@@ -961,6 +1186,9 @@ void rdc_system::step_sequence(int handler, bool reactions, bool structural, int
                 swap_buffers();
             }
         }
+        // runTopologyReactions (SimulationLoop.h:285): host work, so a run with spatial topology reactions
+        // is not replayed from a graph
+        if (topo_dt > 0) evaluate_topology_reactions(topo_dt);
         launch_forces(d, true, n_top > 0, stream, false);  // energy and virial: once, after the run
         launch_record_counts(d, stream);
     }
@@ -1005,7 +1233,10 @@ void rdc_system::run(int64_t n_steps, double dt, int handler, int64_t stride, in
     const int per_graph = (swaps % 2 == 0) ? 1 : 2;
     // the device state pointers are baked into the graph; a graph of an even number of buffer
     // swaps starts and ends on the same buffers and can be replayed
-    const int64_t reps = n_steps / per_graph;
+    // with spatial topology reactions every step evaluates them on the host, between the reactions and the
+    // forces: the steps run one by one
+    topo_dt = (!ctx.spatial_top.empty() && !graphs.empty()) ? dt : 0.0;
+    const int64_t reps = topo_dt > 0 ? 0 : n_steps / per_graph;
     if (reps > 0) {
         invalidate_graph();
         cudaGraph_t g;
@@ -1023,7 +1254,13 @@ void rdc_system::run(int64_t n_steps, double dt, int handler, int64_t stride, in
         for (int64_t r = 0; r < reps; ++r) RDC_CUDA(cudaGraphLaunch(graph, stream));
     }
     const int64_t rest = n_steps - reps * per_graph;
-    if (rest > 0) step_sequence(handler, reactions, structural, (int)rest);
+    if (topo_dt > 0) {
+        for (int64_t k = 0; k < rest; ++k) step_sequence(handler, reactions, structural, 1);
+        invalidate_graph();
+    } else if (rest > 0) {
+        step_sequence(handler, reactions, structural, (int)rest);
+    }
+    topo_dt = 0;
     // the energy and virial of the last force calculation (its per-block partials are still in place)
     if (n_steps > 0) launch_force_finals(d, n_top > 0, stream);
     forces_live = true;
@@ -1311,9 +1548,42 @@ int rdc_context_configure_cosine_dihedral(rdc_context *ctx, int t1, int t2, int 
     });
 }
 
+int rdc_context_add_spatial_topology_reaction(rdc_context *ctx, int mode, int type1, int topology_type1, int type2,
+                                              int topology_type2, int type_to1, int topology_type_to1, int type_to2,
+                                              int topology_type_to2, double rate, double radius,
+                                              int min_graph_distance, int *reaction_id) {
+    return guarded([&] {
+        check_types(ctx, {type1, type2, type_to1, type_to2});
+        require(mode >= STR_TT_ENZYMATIC && mode <= STR_TP_FUSION, "unknown spatial topology reaction mode");
+        const bool tp = mode == STR_TP_ENZYMATIC || mode == STR_TP_FUSION;
+        require(topology_type1 >= 0 && topology_type_to1 >= 0, "topology types must be >= 0");
+        require(tp ? topology_type2 == -1 : (topology_type2 >= 0 && topology_type_to2 >= 0),
+                "topology-particle reactions take topology_type2 = -1, topology-topology ones a type >= 0");
+        // SpatialTopologyReaction.h:88-91, TopologyRegistry.cpp:238-242
+        if (!(rate > 0)) throw InvalidArgument("The rate of a spatial topology reaction should always be positive");
+        if (!(radius > 0)) throw InvalidArgument("The radius of a spatial topology reaction should always be positive");
+        require(min_graph_distance >= 0, "min_graph_distance must be >= 0");
+        ctx->d.spatial_top.push_back(SpatialTopReaction{mode, type1, topology_type1, type2, topology_type2, type_to1,
+                                                        topology_type_to1, type_to2, tp ? -1 : topology_type_to2, rate,
+                                                        radius, min_graph_distance});
+        if (reaction_id) *reaction_id = (int)ctx->d.spatial_top.size() - 1;
+    });
+}
+int rdc_context_set_legacy_topology_self_fusion(rdc_context *ctx, int legacy) {
+    return guarded([&] {
+        require(ctx != nullptr, "null context");
+        ctx->d.legacy_self_fusion = legacy != 0;
+    });
+}
+
 int rdc_system_create(rdc_system **out, const rdc_context *ctx, uint64_t seed) {
     return guarded([&] {
         require(out && ctx, "null argument");
+        // TopologyRegistry::validateSpatialReaction (TopologyRegistry.cpp:243-253)
+        for (const auto &r : ctx->d.spatial_top)
+            if (ctx->d.flavor[r.t1] != FLAVOR_TOPOLOGY && ctx->d.flavor[r.t2] != FLAVOR_TOPOLOGY)
+                throw InvalidArgument("At least one of the educt types of a spatial topology reaction needs to be "
+                                      "topology flavored");
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
             cudaGetLastError();
@@ -1357,6 +1627,20 @@ int rdc_break_bonds(rdc_system *s, double time_step, int n_pairs, const int *typ
         require(s && (n_pairs == 0 || (type1 && type2 && threshold_energy && rate)), "null argument");
         const int64_t nb = s->break_bonds(time_step, n_pairs, type1, type2, threshold_energy, rate);
         if (n_broken) *n_broken = nb;
+    });
+}
+int rdc_evaluate_topology_reactions(rdc_system *s, double time_step, int64_t *n_performed) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        const int64_t n = s->evaluate_topology_reactions(time_step);
+        if (n_performed) *n_performed = n;
+    });
+}
+int rdc_get_topology_reaction_counts(rdc_system *s, int n, int64_t *counts) {
+    return guarded([&] {
+        require(s && (n == 0 || counts), "null argument");
+        require(n == (int)s->ctx.spatial_top.size(), "n must equal the number of spatial topology reactions");
+        for (int k = 0; k < n; ++k) counts[k] = k < (int)s->topo_counts.size() ? (int64_t)s->topo_counts[k] : 0;
     });
 }
 int rdc_get_topologies(rdc_system *s, int64_t capacity_topologies, int *topology_types, int64_t *offsets,

@@ -50,6 +50,19 @@ struct DihedralCfg { int t1, t2, t3, t4; double k, mult, phi0; };
 // particle flavors (include/readdy/model/ParticleTypeRegistry.h:58-63)
 constexpr int FLAVOR_NORMAL = 0, FLAVOR_TOPOLOGY = 1, FLAVOR_MEMBRANE = 2;
 
+// spatial topology reaction (include/readdy/model/topologies/reactions/SpatialTopologyReaction.h:64-191):
+// educts (t1 in a topology of type tt1) + (t2 in a topology of type tt2, or tt2 = -1: a free particle),
+// products (to1, tto1) and (to2, tto2); fusions add the edge to1 -- to2 and the merged topology takes
+// tto1.  Modes in STRMode order.
+enum : int { STR_TT_ENZYMATIC = 0, STR_TT_FUSION = 1, STR_TT_FUSION_ALLOW_SELF = 2, STR_TP_ENZYMATIC = 3,
+             STR_TP_FUSION = 4 };
+struct SpatialTopReaction {
+    int mode;
+    int t1, tt1, t2, tt2, to1, tto1, to2, tto2;
+    double rate, radius;
+    int min_graph_distance;  // self fusion: vertices at most this far apart in the graph do not react
+};
+
 struct ContextData {
     double box[3];
     int pbc[3];
@@ -64,6 +77,8 @@ struct ContextData {
     std::vector<BondCfg> bonds;
     std::vector<AngleCfg> angles;
     std::vector<DihedralCfg> dihedrals;
+    std::vector<SpatialTopReaction> spatial_top;
+    bool legacy_self_fusion = false;  // Context::legacyTopologySelfFusion: graph neighbours may self-fuse
 
     double max_cutoff() const;
     bool structural_reactions() const;  // fusion, fission or decay present (particles appear/vanish/move)
@@ -197,6 +212,20 @@ void launch_step_advance(const SysDev &s, cudaStream_t st);
 void launch_pairs(const SysDev &s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out,
                   cudaStream_t st);
 void launch_fill_ids(uint32_t *id, uint32_t first, int n, cudaStream_t st);
+// spatial topology reaction candidates: pairs (i < j) of particles in cells whose types pair_mask names
+// (bit u of pair_mask[t]) within sqrt(r2max), as TopCandidate records; the count in out_n (capped at cap)
+struct TopCandidate {
+    int i, j;          // storage indices
+    int ti, tj;        // particle types
+    int si, sj;        // topology slots (-1: none)
+    uint32_t idi, idj;
+    double d2;         // squared minimum-image distance in FP64 from the FP32 positions
+};
+// (r2screen: an FP32 screen above r2max by the rounding of an FP32 squared distance)
+void launch_topology_candidates(const SysDev &s, const uint32_t *pair_mask, double r2max, float r2screen,
+                                TopCandidate *out, int *out_n, int cap, cudaStream_t st);
+// writes (storage index, new type, new topology slot or -1 to keep) edits; a new slot also maps to the index
+void launch_particle_edits(const SysDev &s, const int4 *edits, int n, cudaStream_t st);
 // edges: (slot1, slot2, first bond term, bond terms); thr and coin: T x T per type pair
 void launch_break_bonds(const SysDev &s, const int4 *edges, int n_edges, const double2 *bond_kl, const double *thr,
                         const uint64_t *coin, int T, uint64_t seed, uint64_t counter, int *out, int *out_n,

@@ -390,6 +390,68 @@ __global__ void k_break_bonds(SysDev s, const int4 *__restrict__ edges, int n_ed
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Spatial topology reactions, device part: the candidate pairs of the event gathering of
+// CPUEvaluateTopologyReactions::gatherEvents (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp:
+// 225-320) -- pairs of particles in cells whose types some spatial reaction names, closer than the largest
+// reaction radius -- one thread per particle over the stencil cells, each unordered pair once (j > i).
+// The squared distance is bcs::distSquared in FP64 from the FP32 positions; the host applies each
+// reaction's own radius, the topology conditions and the selection.
+// ------------------------------------------------------------------------------------------------
+__global__ void k_topology_candidates(SysDev s, const uint32_t *__restrict__ pair_mask, float r2screen, double r2max,
+                                      TopCandidate *out, int *out_n, int cap) {
+    const GeoR g = geo_r(s.geo);
+    const int n_in = s.counters[C_N_INCELLS];
+    GRID_STRIDE(i, n_in) {
+        const float4 p = s.pos[i];
+        const int ti = itype(p);
+        if (ti < 0) continue;
+        const uint32_t mi = pair_mask[ti];
+        if (!mi) continue;
+        for_each_candidate(p, g, s.start, s.radius, i + 1, [&](int j) {
+            const float4 q = s.pos[j];
+            const int tj = itype(q);
+            if (tj < 0 || !((mi >> tj) & 1u)) return;
+            if (screen_d2(p, q, g) > r2screen) return;
+            double x[3] = {(double)q.x - (double)p.x, (double)q.y - (double)p.y, (double)q.z - (double)p.z};
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                if (g.pbc[a]) {
+                    const double L = (double)g.L[a];
+                    if (x[a] > 0.5 * L) x[a] -= L;
+                    else if (x[a] <= -0.5 * L) x[a] += L;
+                }
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(x[0], x[0]), __dmul_rn(x[1], x[1])), __dmul_rn(x[2], x[2]));
+            if (!(d2 < r2max)) return;
+            const int k = atomicAdd(out_n, 1);
+            if (k < cap) out[k] = TopCandidate{i, j, ti, tj, s.tslot[i], s.tslot[j], s.id[i], s.id[j], d2};
+        });
+    }
+}
+
+void launch_topology_candidates(const SysDev &s, const uint32_t *pair_mask, double r2max, float r2screen,
+                                TopCandidate *out, int *out_n, int cap, cudaStream_t st) {
+    RDC_CUDA(cudaMemsetAsync(out_n, 0, sizeof(int), st));
+    k_topology_candidates<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, pair_mask, r2screen, r2max, out, out_n, cap);
+}
+
+__global__ void k_particle_edits(SysDev s, const int4 *__restrict__ edits, int n) {
+    GRID_STRIDE(k, n) {
+        const int4 e = edits[k];
+        float4 p = s.pos[e.x];
+        p.w = __int_as_float(e.y);
+        s.pos[e.x] = p;
+        if (e.z >= 0) {
+            s.tslot[e.x] = e.z;
+            if (e.z < s.tloc_size) s.tloc[e.z] = e.x;
+        }
+    }
+}
+
+void launch_particle_edits(const SysDev &s, const int4 *edits, int n, cudaStream_t st) {
+    if (n > 0) k_particle_edits<<<std::min((n + 255) / 256, GRID_BLOCKS), 256, 0, st>>>(s, edits, n);
+}
+
 void launch_break_bonds(const SysDev &s, const int4 *edges, int n_edges, const double2 *bond_kl, const double *thr,
                         const uint64_t *coin, int T, uint64_t seed, uint64_t counter, int *out, int *out_n,
                         cudaStream_t st) {

@@ -72,6 +72,33 @@ class Context:
         from the topologies."""
         N.check(self._lib.rdc_context_set_particle_flavor(self._h, particle_type, flavor))
 
+    # TopologyRegistry spatial reactions (SpatialTopologyReaction.h:64-191), modes in STRMode order
+    TT_ENZYMATIC, TT_FUSION, TT_FUSION_ALLOW_SELF, TP_ENZYMATIC, TP_FUSION = 0, 1, 2, 3, 4
+
+    def add_spatial_topology_reaction(self, mode, educt1, educt2, product1, product2, rate, radius,
+                                      min_graph_distance=0):
+        """TopologyRegistry::addSpatialReaction with the parsed descriptor: educt1/product1 are
+        (particle type, topology type), educt2/product2 the same or (particle type, None) for a free
+        particle (topology-particle modes).  A fusion's result takes product1's topology type; a self
+        fusion (TT_FUSION_ALLOW_SELF) needs more than min_graph_distance edges between the two.  Returns
+        the reaction's index."""
+        tt2 = -1 if educt2[1] is None else int(educt2[1])
+        tto2 = -1 if product2[1] is None else int(product2[1])
+        rid = C.c_int()
+        N.check(self._lib.rdc_context_add_spatial_topology_reaction(
+            self._h, int(mode), int(educt1[0]), int(educt1[1]), int(educt2[0]), tt2, int(product1[0]),
+            int(product1[1]), int(product2[0]), tto2, float(rate), float(radius), int(min_graph_distance),
+            C.byref(rid)))
+        self._n_spatial = getattr(self, "_n_spatial", 0) + 1
+        return rid.value
+
+    @property
+    def n_spatial_topology_reactions(self) -> int:
+        return getattr(self, "_n_spatial", 0)
+
+    def set_legacy_topology_self_fusion(self, legacy: bool):
+        N.check(self._lib.rdc_context_set_legacy_topology_self_fusion(self._h, int(bool(legacy))))
+
     # PotentialRegistry
     def add_harmonic_repulsion(self, t1, t2, force_constant, interaction_distance):
         N.check(self._lib.rdc_context_add_harmonic_repulsion(self._h, t1, t2, force_constant, interaction_distance))
@@ -207,6 +234,19 @@ class CUDAKernel:
         N.check(self._lib.rdc_break_bonds(self._h, float(time_step), len(pairs), _p(t1, C.c_int), _p(t2, C.c_int),
                                           _p(thr, C.c_double), _p(rate, C.c_double), C.byref(nb)))
         return nb.value
+
+    def evaluate_topology_reactions(self, time_step):
+        """EvaluateTopologyReactions (spatial reactions); returns the number of events performed."""
+        n = C.c_int64()
+        N.check(self._lib.rdc_evaluate_topology_reactions(self._h, float(time_step), C.byref(n)))
+        return n.value
+
+    def topology_reaction_counts(self):
+        """Performed events per spatial topology reaction since creation."""
+        n = self.context.n_spatial_topology_reactions
+        out = np.zeros(max(n, 1), np.int64)
+        N.check(self._lib.rdc_get_topology_reaction_counts(self._h, n, _p(out, C.c_int64)))
+        return out[:n]
 
     def get_topologies(self):
         """StateModel::getTopologies: a list of (topology type, particle ids[] uint64)."""

@@ -246,3 +246,55 @@ BREAK_BONDS_CASES = [
                  [(0, 0, 0.9, 1e10), (1, 1, 0.9, 1e10), (2, 2, 0.9, 1e10)]],
          after=[1, 1, 1, 1, 1, 1]),
 ]
+
+
+# ---------------------------------------------------------------------------------------------
+# Spatial topology reactions (readdy/test/TestTopologyReactions.cpp:422-680,
+# readdy/test/TestTopologyReactionsExternal.cpp:296-380).  Every species is TOPOLOGY flavored with D = 0;
+# bonds are (type1, type2, k, l0); reactions are (mode, (t1, tt1), (t2, tt2), (to1, tto1), (to2, tto2),
+# rate, radius, min graph distance) with modes in STRMode order (1 TT_FUSION, 2 TT_FUSION_ALLOW_SELF);
+# topologies are (topology type, positions, particle types, edges).  `expect` holds what the reference
+# test requires after `steps` steps of length dt.
+# ---------------------------------------------------------------------------------------------
+_NET_CHAINS = [
+    [(-1, 0, 0), (0, 0, 0), (1, 0, 0), (2, 0, 0), (3, 0, 0), (4, 0, 0)],
+    [(3, 1, 1), (3, 0, 1), (3, -1, 1), (3, -2, 1), (3, -3, 1), (3, -4, 1)],
+    [(4, -3, 0), (3, -3, 0), (2, -3, 0), (1, -3, 0), (0, -3, 0), (-1, -3, 0)],
+    [(0, -4, 1), (0, -3, 1), (0, -2, 1), (0, -1, 1), (0, 0, 1), (0, 1, 1)],
+]
+_NET_BONDS = [(0, 1, 0., .01), (1, 2, 0., .01), (1, 1, 0., .01), (1, 3, 0., .01), (0, 3, 0., .01), (2, 3, 0., .01),
+              (3, 3, 0., .01)]  # head 0, core 1, tail 2, link 3
+TOPOLOGY_REACTION_CASES = [
+    dict(name="tt_fusion", source="readdy/test/TestTopologyReactions.cpp:423-476",
+         box=(10., 10., 10.), n_types=4, bonds=[(2, 3, 0., .1)],  # X1 0, X2 1, Y 2, Z 3; T 0, T2 1
+         reactions=[(1, (0, 0), (1, 0), (2, 1), (3, 1), 1e10, 1.0, 0)],
+         topologies=[(0, [(0, 0, 0)], [0], []), (0, [(0, 0, 0)], [1], [])],
+         steps=1, dt=1e-3,
+         expect=dict(sizes=[2], types_of_topologies=[1], particle_types=[[2, 3]])),
+    dict(name="tt_self_fusion", source="readdy/test/TestTopologyReactions.cpp:478-525",
+         box=(10., 10., 10.), n_types=3,  # X 0, Y 1, Z 2; T 0, T2 1
+         bonds=[(1, 2, 0., .01), (0, 0, 0., .01), (0, 1, 0., .01), (0, 2, 0., .01)],
+         reactions=[(2, (0, 0), (0, 0), (1, 1), (2, 1), 1e10, 1.0, 0)],
+         topologies=[(0, [(0, 0, -.01), (0, 0, 0), (0, 0, .01)], [0, 0, 0], [(0, 1), (1, 2)])],
+         steps=10, dt=1e-3,
+         expect=dict(sizes=[3], types_of_topologies=[1], particle_types=[[0, 1, 2]])),
+    dict(name="tt_fusion_network_distance_above_16", source="readdy/test/TestTopologyReactions.cpp:527-618",
+         box=(30., 30., 30.), n_types=4, bonds=_NET_BONDS,
+         reactions=[(2, (1, 0), (1, 0), (3, 0), (3, 0), 1e10, 1.1, 16)],
+         topologies=[(0, c, [0, 1, 1, 1, 1, 2], [(i, i + 1) for i in range(5)]) for c in _NET_CHAINS],
+         steps=3, dt=1e-3,
+         expect=dict(sizes=[24], links=6)),
+    dict(name="tt_fusion_network_distance_above_14", source="readdy/test/TestTopologyReactions.cpp:620-680",
+         box=(30., 30., 30.), n_types=4, bonds=_NET_BONDS,
+         reactions=[(2, (1, 0), (1, 0), (3, 0), (3, 0), 1e10, 1.01, 14)],
+         topologies=[(0, c, [0, 1, 1, 1, 1, 2], [(i, i + 1) for i in range(5)]) for c in _NET_CHAINS],
+         steps=10, dt=1e-3,
+         expect=dict(sizes=[24], links=8)),
+    dict(name="attach_topologies", source="readdy/test/TestTopologyReactionsExternal.cpp:296-380",
+         box=(15., 15., 15.), n_types=2, bonds=[(0, 0, 1e-8, 1.), (0, 1, 1e-8, 1.), (1, 1, 1e-8, 1.)],  # middle 0, end 1
+         reactions=[(1, (1, 0), (1, 0), (0, 0), (0, 0), 1e3, 1.5, 0)],
+         topologies=[(0, [(-4 + 3 * i, 0, 0), (-3 + 3 * i, 0, 0), (-2 + 3 * i, 0, 0)], [1, 0, 1], [(0, 1), (1, 2)])
+                     for i in range(3)],
+         steps=6, dt=1.0,
+         expect=dict(sizes=[9], linear=True, end_x=[-4., 4.])),
+]

@@ -1,5 +1,6 @@
 """Builds the same system on the CUDA kernel and on the FP64 oracle from one description."""
 import numpy as np
+import pytest
 
 import oracle
 
@@ -142,3 +143,52 @@ def externals_spec(n=4000, box=20.0, seed=0, pair=False):
     spec = dict(box=(box, box, box), periodic=(True, True, True), diffusion=(1.0,) * 9, potentials=pots,
                 externals=ext)
     return spec, pos, types
+
+
+def topology_case_system(case, make, seed=1):
+    """Builds a spatial topology reaction case (tests/golden/known_answers.py TOPOLOGY_REACTION_CASES) on the
+    oracle (make = "oracle") or on the device (make = a readdy_gb300 module); returns (system, ids per topology
+    as added)."""
+    n = case["n_types"]
+    if make == "oracle":
+        s = oracle.OracleSystem(list(case["box"]), (True, True, True), 1.0, (0.0,) * n, seed=seed)
+        target = s
+    else:
+        ctx = make.Context(case["box"], (True, True, True), 1.0, (0.0,) * n)
+        target = ctx
+    for t in range(n):
+        target.set_particle_flavor(t, 1)
+    for a, b, k, l0 in case["bonds"]:
+        target.configure_harmonic_bond(a, b, k, l0)
+    for mode, e1, e2, p1, p2, rate, radius, dmin in case["reactions"]:
+        target.add_spatial_topology_reaction(mode, e1, e2, p1, p2, rate, radius, dmin)
+    if make != "oracle":
+        s = make.CUDAKernel(ctx, seed=seed)
+    ids = []
+    for tt, pos, types, edges in case["topologies"]:
+        ids.append(s.add_topology(np.asarray(pos, float), np.asarray(types, np.int32), edges, topology_type=tt))
+    return s, ids
+
+
+def check_topology_case(case, tops, types_by_id, pos_by_id, edges):
+    """Asserts the reference test's expectations on the topologies [(type, ids)], the particle types and
+    positions by id and the edges per topology [(m, 2) ids]."""
+    exp = case["expect"]
+    assert sorted(len(i) for _, i in tops) == exp["sizes"], [len(i) for _, i in tops]
+    if "types_of_topologies" in exp:
+        assert sorted(t for t, _ in tops) == exp["types_of_topologies"]
+    if "particle_types" in exp:
+        got = sorted(sorted(types_by_id[int(i)] for i in ids) for _, ids in tops)
+        assert got == sorted(exp["particle_types"]), got
+    if "links" in exp:
+        assert sum(1 for _, ids in tops for i in ids if types_by_id[int(i)] == 3) == exp["links"]
+    if exp.get("linear"):
+        (_, ids), = tops
+        deg = {int(i): 0 for i in ids}
+        for a, b in edges[0]:
+            deg[int(a)] += 1
+            deg[int(b)] += 1
+        assert max(deg.values()) <= 2 and len(edges[0]) == len(ids) - 1
+        ends = sorted(i for i, d in deg.items() if d == 1)
+        assert all(types_by_id[i] == 1 for i in ends)
+        assert sorted(pos_by_id[i][0] for i in ends) == pytest.approx(exp["end_x"])
