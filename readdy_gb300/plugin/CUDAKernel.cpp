@@ -206,6 +206,23 @@ rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx) {
         // flavors (ParticleTypeRegistry.h:58-63): BreakBonds drops one-particle pieces of NORMAL types
         for (const auto &[name, id] : types.typeMapping())
             check(rdc_context_set_particle_flavor(c, (int)id, (int)types.infoOf(id).flavor));
+        // spatial topology reactions (TopologyRegistry.h:265-281; each reaction sits in one bucket of the
+        // reversal-symmetric map); constant rates only: rate() throws for a rate function
+        auto top_id = [](TopologyTypeId t) { return t == EmptyTopologyId ? -1 : (int)t; };
+        for (const auto &[key, reactions] : ctx.topologyRegistry().spatialReactionRegistry())
+            for (const auto &r : reactions) {
+                double rate = 0;
+                try {
+                    rate = r.rate();
+                } catch (const std::runtime_error &) {
+                    throw std::logic_error("CUDA kernel: spatial topology reactions with rate functions are not supported");
+                }
+                check(rdc_context_add_spatial_topology_reaction(
+                        c, (int)r.mode(), (int)r.type1(), top_id(r.top_type1()), (int)r.type2(), top_id(r.top_type2()),
+                        (int)r.type_to1(), top_id(r.top_type_to1()), (int)r.type_to2(), top_id(r.top_type_to2()), rate,
+                        r.radius(), (int)r.min_graph_distance(), nullptr));
+            }
+        check(rdc_context_set_legacy_topology_self_fusion(c, ctx.legacyTopologySelfFusion() ? 1 : 0));
         // each unordered type pair once: the registry files a pair's potentials under both orders
         std::set<const pot::PotentialOrder2 *> seen;
         for (const auto &[key, pots] : ctx.potentials().potentialsOrder2())
@@ -475,12 +492,18 @@ std::unique_ptr<act::reactions::Gillespie> CUDAActionFactory::gillespie(scalar d
 std::unique_ptr<act::reactions::DetailedBalance> CUDAActionFactory::detailedBalance(scalar) const {
     throw std::logic_error("CUDA kernel: the detailed-balance reaction handler is not supported");
 }
+// EvaluateTopologyReactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp): the spatial
+// reactions run through rdc_evaluate_topology_reactions, and the host topologies are read back when any
+// event was performed; structural reactions call user functions on the host graph and are not provided
 std::unique_ptr<act::top::EvaluateTopologyReactions> CUDAActionFactory::evaluateTopologyReactions(scalar dt) const {
     auto *k = _kernel;
-    return std::make_unique<CallAction<act::top::EvaluateTopologyReactions, scalar>>([k] {
-        if (k->context().topologyRegistry().nStructuralReactions() > 0 ||
-            !k->context().topologyRegistry().spatialReactionRegistry().empty())
-            throw std::logic_error("CUDA kernel: topology reactions are not supported");
+    return std::make_unique<CallAction<act::top::EvaluateTopologyReactions, scalar>>([k, dt] {
+        if (k->context().topologyRegistry().nStructuralReactions() > 0)
+            throw std::logic_error("CUDA kernel: structural topology reactions are not supported");
+        if (k->context().topologyRegistry().spatialReactionRegistry().empty()) return;
+        int64_t performed = 0;
+        check(rdc_evaluate_topology_reactions(k->sys(), dt, &performed));
+        if (performed > 0) k->cudaStateModel().reloadTopologies();
     }, dt);
 }
 // BreakBonds (include/readdy/model/actions/Actions.h:213-290): the break configuration's pairs go to
