@@ -352,6 +352,12 @@ int rdc_server_poll(rdc_server *s, int64_t capacity, int64_t *ids, int64_t *n_ou
  * submit, admit and finish times in seconds since the server was created */
 int rdc_server_result(rdc_server *s, int64_t id, int64_t capacity, int64_t *counts, int64_t *n_records, int *status,
                       double *times3);
+/* The count records request `id` has written so far, streamed while it runs: a request in the engine leg
+ * shows the records of the steps done by the last rdc_server_progress call, a per-system request those of
+ * its completed chunks (its run goes in chunks of about 2000 steps, a whole number of strides), a finished
+ * request all of them (as rdc_server_result).  n_records is written first; RDC_ERR_CAPACITY if capacity
+ * (in int64 entries) is below n_records x ntypes.  counts may be NULL. */
+int rdc_server_peek_records(rdc_server *s, int64_t id, int64_t capacity, int64_t *counts, int64_t *n_records);
 /* forget a finished request */
 int rdc_server_release(rdc_server *s, int64_t id);
 /* particles advanced so far (summed over requests and steps), device bytes held by admitted requests,

@@ -127,6 +127,7 @@ def _sig(lib):
         "rdc_server_progress": (i, [vp, i64, P(i64)]),
         "rdc_server_poll": (i, [vp, i64, P(i64), P(i64)]),
         "rdc_server_result": (i, [vp, i64, i64, P(i64), P(i64), P(i), P(d)]),
+        "rdc_server_peek_records": (i, [vp, i64, i64, P(i64), P(i64)]),
         "rdc_server_release": (i, [vp, i64]),
         "rdc_server_stats": (i, [vp, P(u64), P(u64), P(i64), P(i64)]),
         "rdc_forces_noalloc": (i, [vp, i64, vp, vp, vp, vp, vp]),

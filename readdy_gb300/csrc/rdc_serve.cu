@@ -99,10 +99,14 @@ struct Request {
     void *block = nullptr;
     EngineLayout L{};
     int64_t steps_done = 0;
-    // plain leg (run by a worker of the pool)
+    // plain leg (run by a worker of the pool); the worker runs in chunks and appends each chunk's count
+    // records to `partial` so that rdc_server_peek_records can stream them
     std::atomic<int> worker_done{0};
     int worker_rc = RDC_OK;
     std::string worker_err;
+    std::mutex partial_mutex;
+    std::vector<int64_t> partial;  // n_partial x ntypes
+    int64_t n_partial = 0;
     // result
     double t_submit = 0, t_admit = -1, t_finish = -1;
     int status = RDC_OK;
@@ -254,15 +258,39 @@ struct rdc_server {
             x[3 * i] = q->pos[i].x; x[3 * i + 1] = q->pos[i].y; x[3 * i + 2] = q->pos[i].z;
             std::memcpy(&t[i], &q->pos[i].w, 4);
         }
-        std::vector<int64_t> counts((size_t)q->max_records * q->ctx.ntypes, 0);
+        const int T = q->ctx.ntypes;
+        std::vector<int64_t> counts((size_t)q->max_records * T, 0);
         int64_t nrec = 0;
         uint64_t advanced = 0;
         rc = rdc_system_create(&sys, ctx, q->seed);
         if (rc == RDC_OK) rc = rdc_reserve(sys, q->cap);
         if (rc == RDC_OK) rc = rdc_add_particles(sys, q->n, x.data(), t.data(), nullptr);
-        if (rc == RDC_OK)
-            rc = rdc_run(sys, q->n_steps, q->dt, handler, q->stride, q->max_records > 0 ? counts.data() : nullptr,
-                         q->max_records, &nrec);
+        if (rc == RDC_OK && q->max_records > 0) {
+            // SimulationLoop::run in chunks of whole strides (about 2000 steps): each chunk starts where the
+            // last one ended (its neighbour list and forces are rebuilt from the same state, and the random
+            // streams are keyed by the step counters), so the trajectory is the single run's; the first
+            // record of a later chunk repeats the previous chunk's last one
+            const int64_t chunk = q->stride * std::max<int64_t>(1, (2000 + q->stride - 1) / q->stride);
+            std::vector<int64_t> buf;
+            for (int64_t done = 0; done < q->n_steps && rc == RDC_OK;) {
+                const int64_t m = std::min(chunk, q->n_steps - done);
+                const int64_t cap = m / q->stride + 1;
+                buf.assign((size_t)cap * T, 0);
+                int64_t got = 0;
+                rc = rdc_run(sys, m, q->dt, handler, q->stride, buf.data(), cap, &got);
+                const int64_t first = done > 0 ? 1 : 0;
+                for (int64_t r = first; r < got && nrec < q->max_records; ++r, ++nrec)
+                    std::copy(buf.begin() + r * T, buf.begin() + (r + 1) * T, counts.begin() + nrec * T);
+                {
+                    std::lock_guard<std::mutex> g(q->partial_mutex);
+                    q->partial.assign(counts.begin(), counts.begin() + nrec * T);
+                    q->n_partial = nrec;
+                }
+                done += m;
+            }
+        } else if (rc == RDC_OK) {
+            rc = rdc_run(sys, q->n_steps, q->dt, handler, q->stride, nullptr, 0, &nrec);
+        }
         if (rc == RDC_OK) rc = rdc_get_particle_steps(sys, &advanced);  // counted on the device
         if (rc != RDC_OK) q->worker_err = rdc_last_error();
         q->particle_steps = advanced;
@@ -607,6 +635,43 @@ int rdc_server_result(rdc_server *s, int64_t id, int64_t capacity, int64_t *coun
         if (counts) {
             if (capacity < need) throw rdc::CapacityError("count buffer too small for the request's records");
             for (int64_t k = 0; k < need; ++k) counts[k] = q.records[k];
+        }
+    });
+}
+
+int rdc_server_peek_records(rdc_server *s, int64_t id, int64_t capacity, int64_t *counts, int64_t *n_records) {
+    SERVE_CALL({
+        if (!s) throw std::invalid_argument("null argument");
+        auto it = s->requests.find(id);
+        if (it == s->requests.end()) throw std::invalid_argument("unknown request id");
+        Request &q = *it->second;
+        const int T = q.ctx.ntypes;
+        std::vector<int64_t> h;
+        int64_t n = 0;
+        if (q.finished) {
+            n = q.n_records;
+            h.assign(q.records.begin(), q.records.begin() + n * T);
+        } else if (q.plain) {
+            std::lock_guard<std::mutex> g(q.partial_mutex);
+            n = q.n_partial;
+            h = q.partial;
+        } else if (q.slot >= 0) {
+            // the engine is idle between rdc_server_progress calls: its records so far, on the server's stream
+            RepState st{};
+            RDC_CUDA(cudaMemcpyAsync(&st, s->state_dev + q.slot, sizeof(RepState), cudaMemcpyDeviceToHost, s->stream));
+            RDC_CUDA(cudaStreamSynchronize(s->stream));
+            n = std::min<int64_t>(st.rec, q.max_records);
+            std::vector<unsigned long long> u((size_t)n * T);
+            if (n > 0)
+                RDC_CUDA(cudaMemcpyAsync(u.data(), static_cast<unsigned char *>(q.block) + q.L.records,
+                                         sizeof(unsigned long long) * u.size(), cudaMemcpyDeviceToHost, s->stream));
+            RDC_CUDA(cudaStreamSynchronize(s->stream));
+            h.assign(u.begin(), u.end());
+        }
+        if (n_records) *n_records = n;
+        if (counts) {
+            if (capacity < n * T) throw rdc::CapacityError("count buffer too small for the request's records");
+            for (int64_t k = 0; k < n * T; ++k) counts[k] = h[k];
         }
     });
 }

@@ -92,6 +92,17 @@ class Server:
                                                 C.byref(nrec), C.byref(st), None))
         return dict(counts=counts, status=st.value, submit=times[0], admit=times[1], finish=times[2])
 
+    def peek_records(self, request_id: int):
+        """The count records the request has written so far, (n_records, n_types) int64, while it runs."""
+        nrec = C.c_int64()
+        N.check(self._lib.rdc_server_peek_records(self._h, int(request_id), 0, None, C.byref(nrec)))
+        T = self._types[request_id]
+        counts = np.zeros((nrec.value, T), np.int64)
+        if nrec.value:
+            N.check(self._lib.rdc_server_peek_records(self._h, int(request_id), counts.size, _p(counts, C.c_int64),
+                                                      C.byref(nrec)))
+        return counts[:nrec.value]
+
     def release(self, request_id: int):
         N.check(self._lib.rdc_server_release(self._h, int(request_id)))
         self._types.pop(request_id, None)

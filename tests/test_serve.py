@@ -97,3 +97,37 @@ def test_particle_steps_are_counted_on_the_device_in_both_legs(rg):
         srv.progress(32)
         done += len(srv.poll())
     assert srv.stats()["particle_steps"] == sum(len(s.positions) * s.n_steps for s in specs)
+
+
+def test_records_stream_while_requests_run(rg):
+    """rdc_server_peek_records: while requests run, their records so far are a prefix of the final ones, in
+    the engine leg (after each progress call) and in the per-system leg (after each chunk of its run); a
+    per-system request run in chunks gives the records of one uninterrupted run."""
+    from readdy_gb300.serve import Server
+    specs = small_stream(2, seed=31)
+    specs[0].n_steps, specs[0].count_stride = 1000, 50    # engine leg
+    specs[1].n_steps, specs[1].count_stride = 4500, 100   # per-system leg, three chunks
+    thr = len(specs[1].positions)
+    assert len(specs[0].positions) < thr
+    srv = Server(1 << 30, plain_threshold=thr)
+    ids = [srv.submit(s.context(), s.positions, s.types, s.n_steps, s.dt, s.count_stride, s.seed) for s in specs]
+    peeks = {rid: [] for rid in ids}
+    done = {}
+    while len(done) < len(ids):
+        srv.progress(64)
+        for rid in ids:
+            if rid not in done:
+                peeks[rid].append(srv.peek_records(rid))
+        for rid in srv.poll():
+            done[rid] = srv.result(rid)
+    for rid, s in zip(ids, specs):
+        final = done[rid]["counts"]
+        assert done[rid]["status"] == 0 and len(final) == s.n_steps // s.count_stride + 1
+        for p in peeks[rid]:
+            np.testing.assert_array_equal(p, final[:len(p)])
+        np.testing.assert_array_equal(srv.peek_records(rid), final)
+    assert any(0 < len(p) < len(done[ids[0]]["counts"]) for p in peeks[ids[0]])
+    k = rg.CUDAKernel(specs[1].context(), seed=specs[1].seed)
+    k.add_particles(specs[1].positions, specs[1].types)
+    ref = k.run(specs[1].n_steps, specs[1].dt, handler=rg.GILLESPIE, count_stride=specs[1].count_stride)
+    np.testing.assert_array_equal(done[ids[1]]["counts"], ref)
