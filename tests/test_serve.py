@@ -104,7 +104,7 @@ def test_records_stream_while_requests_run(rg):
     the engine leg (after each progress call) and in the per-system leg (after each chunk of its run); a
     per-system request run in chunks gives the records of one uninterrupted run."""
     from readdy_gb300.serve import Server
-    specs = small_stream(2, seed=31)
+    specs = sorted(small_stream(2, seed=31), key=lambda s: len(s.positions))
     specs[0].n_steps, specs[0].count_stride = 1000, 50    # engine leg
     specs[1].n_steps, specs[1].count_stride = 4500, 100   # per-system leg, three chunks
     thr = len(specs[1].positions)
