@@ -351,6 +351,10 @@ struct rdc_system {
     std::vector<uint64_t> topo_counts;  // performed events per spatial topology reaction
     TopCandidate *cand_dev = nullptr;
     int cand_cap = 0;
+    uint32_t *top_mask_dev = nullptr;  // MAX_TYPES pair masks of the spatial reactions
+    int *top_n_dev = nullptr;
+    int4 *edit_dev = nullptr;
+    int edit_cap = 0;
     double topo_dt = 0;               // > 0: run() evaluates topology reactions every step with this time step
     int4 *edge_dev = nullptr;
     double2 *bond_kl_dev = nullptr;
@@ -386,7 +390,7 @@ struct rdc_system {
         dfree(bond_par_dev); dfree(angle_par_dev); dfree(dih_par_dev);
         dfree(edge_dev); dfree(bond_kl_dev);
         dfree(bond_at_dev); dfree(angle_at_dev); dfree(dih_at_dev); dfree(term_force_dev);
-        dfree(cand_dev);
+        dfree(cand_dev); dfree(top_mask_dev); dfree(top_n_dev); dfree(edit_dev);
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -920,8 +924,12 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
         mask[r.t2] |= 1u << r.t1;
         rmax = std::max(rmax, r.radius);
     }
-    uint32_t *mask_dev = dalloc<uint32_t>(T);
-    int *n_dev = dalloc<int>(1);
+    if (!top_mask_dev) {
+        top_mask_dev = dalloc<uint32_t>(MAX_TYPES);
+        top_n_dev = dalloc<int>(1);
+    }
+    uint32_t *mask_dev = top_mask_dev;
+    int *n_dev = top_n_dev;
     RDC_CUDA(cudaMemcpyAsync(mask_dev, mask.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, stream));
     const double r2max = rmax * rmax;
     const float r2screen = (float)r2max + 2.0f * band_for(rmax, d.geo.L);
@@ -935,12 +943,10 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
         RDC_CUDA(cudaMemcpyAsync(&nc, n_dev, sizeof(int), cudaMemcpyDeviceToHost, stream));
         sync();
         if (nc <= cand_cap) break;
-        dfree(cand_dev);
+        dfree(cand_dev); dfree(top_mask_dev); dfree(top_n_dev); dfree(edit_dev);
         cand_cap = nc + nc / 2;
         cand_dev = dalloc<TopCandidate>(cand_cap);
     }
-    dfree(mask_dev);
-    dfree(n_dev);
     std::vector<TopCandidate> cand(std::min(nc, cand_cap));
     if (!cand.empty())
         RDC_CUDA(cudaMemcpyAsync(cand.data(), cand_dev, sizeof(TopCandidate) * cand.size(), cudaMemcpyDeviceToHost,
@@ -1077,11 +1083,14 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
         ++performed;
     }
     if (performed == 0) return 0;
-    int4 *edit_dev = dalloc<int4>(edits.size());
+    if ((int)edits.size() > edit_cap) {
+        dfree(edit_dev);
+        edit_cap = (int)edits.size() * 2;
+        edit_dev = dalloc<int4>(edit_cap);
+    }
     RDC_CUDA(cudaMemcpyAsync(edit_dev, edits.data(), sizeof(int4) * edits.size(), cudaMemcpyHostToDevice, stream));
     launch_particle_edits(d, edit_dev, (int)edits.size(), stream);
     sync();
-    dfree(edit_dev);
     std::vector<TopGraph> kept;
     for (size_t gi = 0; gi < graphs.size(); ++gi)
         if (!dead[gi]) kept.push_back(std::move(graphs[gi]));
