@@ -166,6 +166,38 @@ int rdc_break_bonds(rdc_system *s, double time_step, int n_pairs, const int *typ
 int rdc_evaluate_topology_reactions(rdc_system *s, double time_step, int64_t *n_performed);
 /* performed events per spatial topology reaction (n = the number registered) since creation */
 int rdc_get_topology_reaction_counts(rdc_system *s, int n, int64_t *counts);
+
+/* ---- structural topology reactions (TopologyRegistry::addStructuralReaction,
+ * include/readdy/model/topologies/reactions/StructuralTopologyReaction.h): functions of the embedding ---- */
+typedef struct rdc_recipe rdc_recipe;
+/* rate of a structural reaction for the topology with index `topology` (rdc_get_topologies order); called
+ * when the topology is created or changed (GraphTopology::updateReactionRates) and cached until then */
+typedef double (*rdc_topology_rate_fn)(void *user, rdc_system *s, int64_t topology);
+/* the reaction function: fills `recipe` for the topology with index `topology` (Recipe.h) */
+typedef void (*rdc_topology_recipe_fn)(void *user, rdc_system *s, int64_t topology, rdc_recipe *recipe);
+/* registers a structural reaction on topologies of topology_type.  Events of all topologies join the
+ * spatial events of rdc_evaluate_topology_reactions.  With expect_connected a topology that falls apart
+ * raises RDC_ERR_LOGIC; without it the pieces become topologies of the same type (one-particle pieces of
+ * NORMAL flavor leave; StructuralTopologyReaction.cpp:70-130, Utils.h:52-81).  During the functions the
+ * system may only be read (rdc_get_topology, rdc_get_topology_positions, rdc_get_topologies ...). */
+int rdc_add_structural_topology_reaction(rdc_system *s, int topology_type, rdc_topology_rate_fn rate,
+                                         rdc_topology_recipe_fn reaction, void *user, int expect_connected,
+                                         int *reaction_id);
+/* performed events per structural reaction (n = the number registered) since registration */
+int rdc_get_structural_reaction_counts(rdc_system *s, int n, int64_t *counts);
+/* recipe steps (Recipe.h:74-110), applied in order; vertices are local indices of the topology (the order of
+ * rdc_get_topology) */
+int rdc_recipe_change_particle_type(rdc_recipe *r, int64_t vertex, int type);
+int rdc_recipe_add_edge(rdc_recipe *r, int64_t v1, int64_t v2);
+int rdc_recipe_remove_edge(rdc_recipe *r, int64_t v1, int64_t v2);
+int rdc_recipe_separate_vertex(rdc_recipe *r, int64_t vertex);
+int rdc_recipe_change_topology_type(rdc_recipe *r, int type);
+/* one topology (index k of rdc_get_topologies): type, particle ids and types by local vertex, edges as local
+ * vertex pairs; counts are written first, RDC_ERR_CAPACITY if an output does not fit; outputs may be NULL */
+int rdc_get_topology(rdc_system *s, int64_t k, int *topology_type, int64_t capacity, uint64_t *ids, int *types,
+                     int64_t *n_vertices, int64_t capacity_edges, int64_t *edges2, int64_t *n_edges);
+/* positions of topology k's particles by local vertex */
+int rdc_get_topology_positions(rdc_system *s, int64_t k, int64_t capacity, double *positions3);
 /* StateModel::getTopologies (StateModel.h:69-117): the active topologies as CSR, topology k has type
  * topology_types[k] and the particles ids[offsets[k] .. offsets[k+1]) (offsets holds n_topologies + 1
  * entries).  n_topologies and n_ids are written first; RDC_ERR_CAPACITY if either capacity is smaller.

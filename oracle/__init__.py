@@ -74,6 +74,14 @@ def _load():
             "orc_set_legacy_topology_self_fusion": (i, [vp, i]),
             "orc_evaluate_topology_reactions": (i, [vp, d, P(i64)]),
             "orc_topology_reaction_counts": (i, [vp, P(i64), i]),
+            "orc_add_structural_topology_reaction": (i, [vp, i, RATE_FN, RECIPE_FN, vp, i]),
+            "orc_structural_reaction_counts": (i, [vp, P(i64), i]),
+            "orc_recipe_change_particle_type": (i, [vp, i64, i]),
+            "orc_recipe_add_edge": (i, [vp, i64, i64]),
+            "orc_recipe_remove_edge": (i, [vp, i64, i64]),
+            "orc_recipe_separate_vertex": (i, [vp, i64]),
+            "orc_recipe_change_topology_type": (i, [vp, i]),
+            "orc_get_topology": (i, [vp, i64, P(i), P(u64), P(i), P(d), P(i64), P(i64), P(i64)]),
             "orc_add_particles": (i, [vp, i, P(d), P(i)]),
             "orc_n_particles": (i, [vp]),
             "orc_n_entries": (i, [vp]),
@@ -100,6 +108,31 @@ def _load():
             f.argtypes = args
         _lib = lib
         return lib
+
+
+RATE_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_void_p, C.c_int64)
+RECIPE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p)
+
+
+class TopologyView:
+    """One oracle topology as structural reaction functions see it: index, type, ids, types and positions by
+    local vertex, edges as local vertex pairs."""
+
+    def __init__(self, lib, h, index):
+        self.index = int(index)
+        tt, nv, ne = C.c_int(), C.c_int64(), C.c_int64()
+        lib.orc_get_topology(h, self.index, C.byref(tt), None, None, None, C.byref(nv), None, C.byref(ne))
+        self.type = tt.value
+        self.ids = np.zeros(nv.value, np.uint64)
+        self.types = np.zeros(nv.value, np.int32)
+        self.positions = np.zeros((nv.value, 3))
+        self.edges = np.zeros((ne.value, 2), np.int64)
+        lib.orc_get_topology(h, self.index, None, _ptr(self.ids, C.c_uint64), _ptr(self.types, C.c_int),
+                             _ptr(self.positions, C.c_double), C.byref(nv), _ptr(self.edges, C.c_int64), C.byref(ne))
+
+    @property
+    def n_particles(self):
+        return len(self.ids)
 
 
 def _ptr(a, ctype):
@@ -276,7 +309,11 @@ class OracleSystem:
 
     def evaluate_topology_reactions(self, dt):
         n = C.c_int64()
-        self._check(self._lib.orc_evaluate_topology_reactions(self._h, dt, C.byref(n)))
+        rc = self._lib.orc_evaluate_topology_reactions(self._h, dt, C.byref(n))
+        err, self._callback_error = getattr(self, "_callback_error", None), None
+        if err is not None:
+            raise err
+        self._check(rc)
         return n.value
 
     def topology_reaction_counts(self):
@@ -284,6 +321,40 @@ class OracleSystem:
         out = np.zeros(max(n, 1), np.int64)
         self._lib.orc_topology_reaction_counts(self._h, _ptr(out, C.c_int64), n)
         return out[:n]
+
+    def add_structural_topology_reaction(self, topology_type, rate_function, reaction_function,
+                                         expect_connected=True):
+        lib, h = self._lib, self._h
+
+        def rate_cb(_u, _s, k):
+            try:
+                return float(rate_function(TopologyView(lib, h, k)))
+            except BaseException as e:
+                self._callback_error = getattr(self, "_callback_error", None) or e
+                return 0.0
+
+        def recipe_cb(_u, _s, k, recipe):
+            try:
+                for step in reaction_function(TopologyView(lib, h, k)) or ():
+                    getattr(lib, "orc_recipe_" + step[0])(recipe, *[int(a) for a in step[1:]])
+            except BaseException as e:
+                self._callback_error = getattr(self, "_callback_error", None) or e
+                lib.orc_recipe_change_particle_type(recipe, -1, 0)
+
+        cbs = (RATE_FN(rate_cb), RECIPE_FN(recipe_cb))
+        self._callbacks = getattr(self, "_callbacks", []) + [cbs]
+        self._n_structural = getattr(self, "_n_structural", 0) + 1
+        return self._check(lib.orc_add_structural_topology_reaction(h, topology_type, cbs[0], cbs[1], None,
+                                                                    int(bool(expect_connected))))
+
+    def structural_reaction_counts(self):
+        n = getattr(self, "_n_structural", 0)
+        out = np.zeros(max(n, 1), np.int64)
+        self._lib.orc_structural_reaction_counts(self._h, _ptr(out, C.c_int64), n)
+        return out[:n]
+
+    def topology(self, index):
+        return TopologyView(self._lib, self._h, index)
 
     def topologies(self):
         """[(topology type, particle ids[] uint64)]"""

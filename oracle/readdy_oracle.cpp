@@ -371,6 +371,11 @@ inline std::pair<size_t, size_t> chunk(size_t n, int parts, int t) {
 
 }  // namespace
 
+struct orc_recipe {
+    struct Op { int kind; int64_t a, b; int type; };
+    std::vector<Op> ops;
+};
+
 struct orc_system {
     Box box;
     double kbt;
@@ -423,6 +428,19 @@ struct orc_system {
     std::vector<Spatial> spatial;
     bool legacySelfFusion = false;
     std::vector<int64_t> spatialCounts;
+
+    /* structural reactions: functions of the caller (StructuralTopologyReaction.h), rates cached per
+     * topology until it changes (GraphTopology::updateReactionRates) */
+    struct Structural {
+        int topologyType;
+        orc_topology_rate_fn rate;
+        orc_topology_recipe_fn reaction;
+        void *user;
+        bool expectConnected;
+    };
+    std::vector<Structural> structural;
+    std::vector<int64_t> structuralCounts;
+    std::vector<std::vector<double>> graphRates;  // per graph; empty = to be evaluated
 
     std::vector<Entry> entries;
     std::vector<size_t> blanks;
@@ -537,14 +555,24 @@ struct orc_system {
      * at the end (each handler configures its topology; configure depends on the graph only). */
     struct TREvent {
         double rate, cumulativeRate;
-        long g1, g2;  // topology indices (g2 = -1: topology-particle)
+        long g1, g2;  // topology indices (g2 = -1: topology-particle or structural)
         const Spatial *r;
         size_t idx1, idx2;  // idx1 belongs to a topology
+        int structuralIndex;  // >= 0: a structural event
     };
     int64_t evaluateTopologyReactions(double dt) {
         if (spatialCounts.size() != spatial.size()) spatialCounts.assign(spatial.size(), 0);
-        if (spatial.empty() || graphs.empty()) return 0;
-        if (!nlSetUp) throw std::logic_error("neighbor list not set up");
+        if (structuralCounts.size() != structural.size()) structuralCounts.assign(structural.size(), 0);
+        if ((spatial.empty() && structural.empty()) || graphs.empty()) return 0;
+        if (!spatial.empty() && !nlSetUp) throw std::logic_error("neighbor list not set up");
+        graphRates.resize(graphs.size());
+        for (size_t gi = 0; gi < graphs.size(); ++gi)
+            if (graphRates[gi].empty() && !structural.empty()) {
+                graphRates[gi].assign(structural.size(), 0.0);
+                for (size_t k = 0; k < structural.size(); ++k)
+                    if (structural[k].topologyType == graphs[gi].type)
+                        graphRates[gi][k] = structural[k].rate(structural[k].user, this, (int64_t)gi);
+            }
         const IdMap idx = idMap();
         std::vector<long> topOf(entries.size(), -1);
         std::vector<int> vertexOf(entries.size(), -1);
@@ -567,7 +595,13 @@ struct orc_system {
             return dist[to];
         };
         std::vector<TREvent> events;
-        for (size_t cell = 0; cell < adjacency.size(); ++cell) {
+        // gatherEvents, :199-219: the structural events first (second topology -1 and second particle 0, as
+        // TREvent's defaults leave them)
+        for (size_t gi = 0; gi < graphs.size() && !structural.empty(); ++gi)
+            for (size_t k = 0; k < structural.size(); ++k)
+                if (graphRates[gi][k] > 0)
+                    events.push_back(TREvent{graphRates[gi][k], 0, (long)gi, -1, nullptr, 0, 0, (int)k});
+        for (size_t cell = 0; cell < adjacency.size() && !spatial.empty(); ++cell) {
             forEachInCell(cell, [&](size_t ip) {
                 const Entry &en = entries[ip];
                 if (en.deactivated || !spatialType[en.type]) return;
@@ -587,7 +621,7 @@ struct orc_system {
                         if (!fwd && !bwd) continue;
                         if (!r.allowSelf() && topOf[ip] == topOf[jn]) continue;
                         if (!(d2 < r.radius * r.radius)) continue;
-                        TREvent ev{r.rate, 0, -1, -1, &r, ip, jn};
+                        TREvent ev{r.rate, 0, -1, -1, &r, ip, jn, -1};
                         if (hasEntryTop && !hasNbTop) { ev.g1 = topOf[ip]; ev.idx1 = ip; ev.idx2 = jn; }
                         else if (!hasEntryTop && hasNbTop) { ev.g1 = topOf[jn]; ev.idx1 = jn; ev.idx2 = ip; }
                         else { ev.g1 = topOf[ip]; ev.g2 = topOf[jn]; }
@@ -606,8 +640,83 @@ struct orc_system {
             return a.g2 >= 0 && (a.g2 == b.g1 || a.g2 == b.g2);
         };
         std::vector<char> dead(graphs.size(), 0);
+        std::vector<Graph> children;
+        std::vector<char> changed(graphs.size(), 0);
         int64_t performed = 0;
+        auto evalStructural = [&](const TREvent &ev) {  // executeStructuralReaction, Utils.h:52-81
+            const Structural &sr = structural[ev.structuralIndex];
+            orc_recipe recipe;
+            sr.reaction(sr.user, this, (int64_t)ev.g1, &recipe);
+            Graph &g = graphs[ev.g1];
+            const int nv = (int)g.ids.size();
+            auto vtx = [&](int64_t v) {
+                if (v < 0 || v >= nv) throw std::invalid_argument("recipe vertex index out of range");
+                return (int)v;
+            };
+            auto findEdge = [&](int a, int b) {
+                for (size_t x = 0; x < g.edges.size(); ++x)
+                    if ((g.edges[x].first == a && g.edges[x].second == b) || (g.edges[x].first == b && g.edges[x].second == a))
+                        return (long)x;
+                return -1L;
+            };
+            for (const auto &op : recipe.ops) {
+                if (op.kind == 0) entries[indexOf(idx, g.ids[vtx(op.a)])].type = op.type;
+                else if (op.kind == 1) {
+                    const int a = vtx(op.a), b = vtx(op.b);
+                    if (findEdge(a, b) < 0) g.edges.push_back({a, b});
+                } else if (op.kind == 2) {
+                    const long x = findEdge(vtx(op.a), vtx(op.b));
+                    if (x < 0) throw std::invalid_argument("recipe: the edge to remove does not exist");
+                    g.edges.erase(g.edges.begin() + x);
+                } else if (op.kind == 3) {
+                    const int v = vtx(op.a);
+                    std::vector<std::pair<int, int>> kept;
+                    for (auto &e : g.edges) if (e.first != v && e.second != v) kept.push_back(e);
+                    g.edges = std::move(kept);
+                } else if (op.kind == 4) {
+                    g.type = op.type;
+                }
+            }
+            changed[ev.g1] = 1;
+            std::vector<std::vector<int>> nb(nv);
+            for (auto &e : g.edges) { nb[e.first].push_back(e.second); nb[e.second].push_back(e.first); }
+            std::vector<int> comp(nv, -1);
+            int nc = 0;
+            for (int v = 0; v < nv; ++v) {
+                if (comp[v] >= 0) continue;
+                std::vector<int> todo{v};
+                comp[v] = nc;
+                while (!todo.empty()) {
+                    const int u = todo.back();
+                    todo.pop_back();
+                    for (int w : nb[u]) if (comp[w] < 0) { comp[w] = nc; todo.push_back(w); }
+                }
+                ++nc;
+            }
+            auto normalSingle = [&](const Graph &x) {
+                return x.ids.size() == 1 && flavor[entries[indexOf(idx, x.ids[0])].type] == 0;
+            };
+            if (nc > 1) {
+                if (sr.expectConnected)
+                    throw std::logic_error("The topology was expected to still be connected after the reaction");
+                std::vector<Graph> parts(nc);
+                std::vector<int> local(nv);
+                for (int v = 0; v < nv; ++v) {
+                    local[v] = (int)parts[comp[v]].ids.size();
+                    parts[comp[v]].ids.push_back(g.ids[v]);
+                    parts[comp[v]].type = g.type;
+                }
+                for (auto &e : g.edges) parts[comp[e.first]].edges.push_back({local[e.first], local[e.second]});
+                for (auto &part : parts) if (!normalSingle(part)) children.push_back(std::move(part));
+                dead[ev.g1] = 1;
+            } else if (normalSingle(g)) {
+                dead[ev.g1] = 1;
+            }
+            ++structuralCounts[ev.structuralIndex];
+            ++performed;
+        };
         auto eval = [&](const TREvent &ev) {
+            if (ev.structuralIndex >= 0) { evalStructural(ev); return; }
             const Spatial &r = *ev.r;
             Entry &e1 = entries[ev.idx1];
             Entry &e2 = entries[ev.idx2];
@@ -660,6 +769,8 @@ struct orc_system {
                     }
                 }
             }
+            changed[ev.g1] = 1;
+            if (ev.g2 >= 0) changed[ev.g2] = 1;
             ++spatialCounts[ev.r - spatial.data()];
             ++performed;
         };
@@ -701,9 +812,18 @@ struct orc_system {
         }
         if (performed > 0) {
             std::vector<Graph> kept;
+            std::vector<std::vector<double>> keptRates;
             for (size_t gi = 0; gi < graphs.size(); ++gi)
-                if (!dead[gi]) kept.push_back(std::move(graphs[gi]));
+                if (!dead[gi]) {
+                    kept.push_back(std::move(graphs[gi]));
+                    keptRates.push_back(changed[gi] ? std::vector<double>{} : graphRates[gi]);
+                }
+            for (auto &c : children) {
+                kept.push_back(std::move(c));
+                keptRates.emplace_back();
+            }
             graphs = std::move(kept);
+            graphRates = std::move(keptRates);
             configureTopologies();
         }
         return performed;
@@ -775,6 +895,7 @@ struct orc_system {
             }
         }
         graphs = std::move(result);
+        graphRates.clear();  // structural rates of every topology are evaluated again
         configureTopologies();
         return removed;
     }
@@ -1610,6 +1731,39 @@ int orc_evaluate_topology_reactions(orc_system *s, double dt, int64_t *n_perform
         return -1;
     }
 }
+int orc_add_structural_topology_reaction(orc_system *s, int topology_type, orc_topology_rate_fn rate,
+                                         orc_topology_recipe_fn reaction, void *user, int expect_connected) {
+    s->structural.push_back({topology_type, rate, reaction, user, expect_connected != 0});
+    s->graphRates.clear();
+    return (int)s->structural.size() - 1;
+}
+int orc_structural_reaction_counts(const orc_system *s, int64_t *counts, int n) {
+    for (int k = 0; k < n; ++k) counts[k] = k < (int)s->structuralCounts.size() ? s->structuralCounts[k] : 0;
+    return 0;
+}
+int orc_recipe_change_particle_type(orc_recipe *r, int64_t v, int type) { r->ops.push_back({0, v, 0, type}); return 0; }
+int orc_recipe_add_edge(orc_recipe *r, int64_t a, int64_t b) { r->ops.push_back({1, a, b, 0}); return 0; }
+int orc_recipe_remove_edge(orc_recipe *r, int64_t a, int64_t b) { r->ops.push_back({2, a, b, 0}); return 0; }
+int orc_recipe_separate_vertex(orc_recipe *r, int64_t v) { r->ops.push_back({3, v, 0, 0}); return 0; }
+int orc_recipe_change_topology_type(orc_recipe *r, int type) { r->ops.push_back({4, 0, 0, type}); return 0; }
+int orc_get_topology(const orc_system *s, int64_t k, int *type, uint64_t *ids, int *types, double *pos3,
+                     int64_t *n_vertices, int64_t *edges2, int64_t *n_edges) {
+    if (k < 0 || k >= (int64_t)s->graphs.size()) { g_err = "topology index out of range"; return -1; }
+    const auto &g = s->graphs[k];
+    const auto idx = s->idMap();
+    if (type) *type = g.type;
+    if (n_vertices) *n_vertices = (int64_t)g.ids.size();
+    if (n_edges) *n_edges = (int64_t)g.edges.size();
+    for (size_t v = 0; v < g.ids.size(); ++v) {
+        const auto &e = s->entries[orc_system::indexOf(idx, g.ids[v])];
+        if (ids) ids[v] = g.ids[v];
+        if (types) types[v] = e.type;
+        if (pos3) { pos3[3 * v] = e.pos.x; pos3[3 * v + 1] = e.pos.y; pos3[3 * v + 2] = e.pos.z; }
+    }
+    if (edges2)
+        for (size_t e = 0; e < g.edges.size(); ++e) { edges2[2 * e] = g.edges[e].first; edges2[2 * e + 1] = g.edges[e].second; }
+    return 0;
+}
 int orc_topology_reaction_counts(const orc_system *s, int64_t *counts, int n) {
     for (int k = 0; k < n; ++k) counts[k] = k < (int)s->spatialCounts.size() ? s->spatialCounts[k] : 0;
     return 0;
@@ -1775,7 +1929,7 @@ int orc_run(orc_system *s, int64_t n_steps, double dt, int handler, int stride, 
             }
             // runTopologyReactions (SimulationLoop.h:285); the cells are refreshed first so that particles the
             // reactions created take part
-            if (!s->spatial.empty() && !s->graphs.empty()) {
+            if ((!s->spatial.empty() || !s->structural.empty()) && !s->graphs.empty()) {
                 if (nl) s->nlUpdate();
                 s->evaluateTopologyReactions(dt);
             }

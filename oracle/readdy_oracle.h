@@ -17,6 +17,10 @@ extern "C" {
 #endif
 
 typedef struct orc_system orc_system;
+/* structural topology reactions: functions of the caller (StructuralTopologyReaction.h) */
+typedef struct orc_recipe orc_recipe;
+typedef double (*orc_topology_rate_fn)(void *user, orc_system *s, int64_t topology);
+typedef void (*orc_topology_recipe_fn)(void *user, orc_system *s, int64_t topology, orc_recipe *recipe);
 
 enum orc_handler { ORC_UNCONTROLLED_APPROXIMATION = 0, ORC_GILLESPIE = 1 };
 
@@ -83,6 +87,18 @@ int orc_add_spatial_topology_reaction(orc_system *s, int mode, int t1, int tt1, 
 int orc_set_legacy_topology_self_fusion(orc_system *s, int legacy);
 int orc_evaluate_topology_reactions(orc_system *s, double dt, int64_t *n_performed);
 int orc_topology_reaction_counts(const orc_system *s, int64_t *counts, int n);
+int orc_add_structural_topology_reaction(orc_system *s, int topology_type, orc_topology_rate_fn rate,
+                                         orc_topology_recipe_fn reaction, void *user, int expect_connected);
+int orc_structural_reaction_counts(const orc_system *s, int64_t *counts, int n);
+/* recipe steps (Recipe.h:74-110), vertices by local index */
+int orc_recipe_change_particle_type(orc_recipe *r, int64_t vertex, int type);
+int orc_recipe_add_edge(orc_recipe *r, int64_t v1, int64_t v2);
+int orc_recipe_remove_edge(orc_recipe *r, int64_t v1, int64_t v2);
+int orc_recipe_separate_vertex(orc_recipe *r, int64_t vertex);
+int orc_recipe_change_topology_type(orc_recipe *r, int type);
+/* topology k: type, particle ids, types and positions by local vertex, edges as local pairs (outputs may be NULL) */
+int orc_get_topology(const orc_system *s, int64_t k, int *type, uint64_t *ids, int *types, double *pos3,
+                     int64_t *n_vertices, int64_t *edges2, int64_t *n_edges);
 
 /* particles */
 int orc_add_particles(orc_system *s, int n, const double *pos3, const int *types);

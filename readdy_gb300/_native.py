@@ -32,6 +32,11 @@ class CapacityError(CudaKernelError):
     pass
 
 
+# structural topology reaction functions (include/readdy_cuda.h: rdc_topology_rate_fn, rdc_topology_recipe_fn)
+TOPOLOGY_RATE_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_void_p, C.c_int64)
+TOPOLOGY_RECIPE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p)
+
+
 def _sig(lib):
     d, i, u64, i64, vp = C.c_double, C.c_int, C.c_uint64, C.c_int64, C.c_void_p
     P = C.POINTER
@@ -75,6 +80,15 @@ def _sig(lib):
         "rdc_get_topologies": (i, [vp, i64, P(i), P(i64), i64, P(u64), P(i64), P(i64)]),
         "rdc_evaluate_topology_reactions": (i, [vp, d, P(i64)]),
         "rdc_get_topology_reaction_counts": (i, [vp, i, P(i64)]),
+        "rdc_add_structural_topology_reaction": (i, [vp, i, TOPOLOGY_RATE_FN, TOPOLOGY_RECIPE_FN, vp, i, P(i)]),
+        "rdc_get_structural_reaction_counts": (i, [vp, i, P(i64)]),
+        "rdc_recipe_change_particle_type": (i, [vp, i64, i]),
+        "rdc_recipe_add_edge": (i, [vp, i64, i64]),
+        "rdc_recipe_remove_edge": (i, [vp, i64, i64]),
+        "rdc_recipe_separate_vertex": (i, [vp, i64]),
+        "rdc_recipe_change_topology_type": (i, [vp, i]),
+        "rdc_get_topology": (i, [vp, i64, P(i), i64, P(u64), P(i), P(i64), i64, P(i64), P(i64)]),
+        "rdc_get_topology_positions": (i, [vp, i64, i64, P(d)]),
         "rdc_get_topology_edges": (i, [vp, i64, P(i64), i64, P(u64), P(i64), P(i64)]),
         "rdc_get_n_particles": (i, [vp, P(i64)]),
         "rdc_get_particles": (i, [vp, i64, P(d), P(i), P(u64), P(i64)]),

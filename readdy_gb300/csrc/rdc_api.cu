@@ -327,6 +327,29 @@ struct TopGraph {
     int type = 0;
     std::vector<int> slots;
     std::vector<std::pair<int, int>> edges;
+    std::vector<double> rates;  // per structural reaction, from its rate function
+    bool rates_valid = false;   // false once the topology was created or changed
+};
+
+// recipe operations of a structural topology reaction (include/readdy/model/topologies/reactions/Recipe.h)
+enum : int { RECIPE_CHANGE_PARTICLE_TYPE = 0, RECIPE_ADD_EDGE = 1, RECIPE_REMOVE_EDGE = 2, RECIPE_SEPARATE_VERTEX = 3,
+             RECIPE_CHANGE_TOPOLOGY_TYPE = 4 };
+struct RecipeOp {
+    int kind;
+    int64_t a, b;
+    int type;
+};
+
+struct StructuralReaction {
+    int topology_type;
+    rdc_topology_rate_fn rate;
+    rdc_topology_recipe_fn reaction;
+    void *user;
+    bool expect_connected;
+};
+
+struct rdc_recipe {
+    std::vector<RecipeOp> ops;
 };
 
 struct rdc_system {
@@ -349,6 +372,9 @@ struct rdc_system {
     uint64_t break_calls = 0;         // BreakBonds calls so far: keys their coins
     uint64_t topo_calls = 0;          // topology reaction evaluations so far: keys their clocks and coins
     std::vector<uint64_t> topo_counts;  // performed events per spatial topology reaction
+    std::vector<StructuralReaction> structural;  // registered with callbacks of the embedding
+    std::vector<uint64_t> structural_counts;
+    bool in_callback = false;           // a structural reaction's function is running
     TopCandidate *cand_dev = nullptr;
     int cand_cap = 0;
     uint32_t *top_mask_dev = nullptr;  // MAX_TYPES pair masks of the spatial reactions
@@ -896,62 +922,87 @@ void rdc_system::grow_topology_slots(int n_new) {
     d.tloc_size = n_top;
 }
 
-// EvaluateTopologyReactions for the spatial reactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp:
-// 86-475).  The device lists the candidate pairs (k_topology_candidates); here each pair becomes an event per
-// reaction that matches its particle and topology types in either order, within the reaction's radius (a
-// self fusion also needs a graph distance above min_graph_distance and, unless the legacy rule is set,
-// above 1).  Events are drawn as algo::performEvents does (include/readdy/common/algorithm.h:62-136) --
-// proportional to rate, without replacement, each with its coin u < 1 - exp(-rate dt), an accepted event
-// removing the events that share one of its topologies or its free particle -- by exponential clocks
-// E/rate with the coins drawn up front (the same distribution; Philox keyed by the ordered ids, the call
-// count and the reaction).  Accepted events change particle and topology types, merge graphs (fusion of
-// two topologies), add an edge (self fusion) or take a free particle into a topology (topology-particle
-// fusion); the bonded terms are then derived again from the graphs.  Each pair is one candidate; the
-// reference lists a topology-particle pair a second time from the free particle's side when that
-// particle's storage index is the lower one.
+// EvaluateTopologyReactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp:86-475).
+// Structural reactions: every topology contributes one event per structural reaction of its type, at the
+// rate its rate function gave when the topology was created or last changed (GraphTopology::
+// updateReactionRates).  Spatial reactions: the device lists the candidate pairs (k_topology_candidates);
+// each pair becomes an event per reaction that matches its particle and topology types in either order,
+// within the reaction's radius (a self fusion also needs a graph distance above min_graph_distance and,
+// unless the legacy rule is set, above 1).  Events are drawn as algo::performEvents does
+// (include/readdy/common/algorithm.h:62-136) -- proportional to rate, without replacement, each with its
+// coin u < 1 - exp(-rate dt), an accepted event removing the events that share one of its topologies or its
+// free particle -- by exponential clocks E/rate with the coins drawn up front (the same distribution;
+// Philox keyed by the ordered ids or the topology's first particle, the call count and the reaction).
+// Accepted events are applied in clock order, so a reaction function sees the topologies as the earlier
+// events left them: structural ones apply their recipe (a topology that falls apart becomes its
+// components, or raises when the reaction expects it connected; Utils.h:52-81,
+// StructuralTopologyReaction.cpp:70-130), spatial ones change types, merge graphs, add an edge or take a free
+// particle into a topology.  The bonded terms are then derived again from the graphs.  Each spatial pair is
+// one candidate; the reference lists a topology-particle pair a second time from the free particle's side
+// when that particle's storage index is the lower one.
 int64_t rdc_system::evaluate_topology_reactions(double dt) {
     require(dt > 0, "time step must be > 0");
+    if (in_callback) throw LogicError("topology reactions cannot be evaluated from a reaction's own function");
     const auto &RS = ctx.spatial_top;
     const uint64_t call = topo_calls++;
     if (topo_counts.size() != RS.size()) topo_counts.assign(RS.size(), 0);
-    if (RS.empty() || graphs.empty()) return 0;
-    if (!nl_ready) throw LogicError("topology reactions: the neighbor list is not set up");
-    const int T = ctx.ntypes;
-    std::vector<uint32_t> mask(T, 0u);
-    double rmax = 0;
-    for (const auto &r : RS) {
-        mask[r.t1] |= 1u << r.t2;
-        mask[r.t2] |= 1u << r.t1;
-        rmax = std::max(rmax, r.radius);
-    }
-    if (!top_mask_dev) {
-        top_mask_dev = dalloc<uint32_t>(MAX_TYPES);
-        top_n_dev = dalloc<int>(1);
-    }
-    uint32_t *mask_dev = top_mask_dev;
-    int *n_dev = top_n_dev;
-    RDC_CUDA(cudaMemcpyAsync(mask_dev, mask.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, stream));
-    const double r2max = rmax * rmax;
-    const float r2screen = (float)r2max + 2.0f * band_for(rmax, d.geo.L);
-    int nc = 0;
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        if (cand_cap == 0) {
-            cand_cap = 4096;
+    if (structural_counts.size() != structural.size()) structural_counts.assign(structural.size(), 0);
+    if ((RS.empty() && structural.empty()) || graphs.empty()) return 0;
+    // structural rates of topologies created or changed since their last evaluation
+    if (!structural.empty())
+        for (size_t gi = 0; gi < graphs.size(); ++gi) {
+            TopGraph &g = graphs[gi];
+            if (g.rates_valid) continue;
+            g.rates.assign(structural.size(), 0.0);
+            for (size_t k = 0; k < structural.size(); ++k)
+                if (structural[k].topology_type == g.type) {
+                    in_callback = true;
+                    const double r = structural[k].rate(structural[k].user, this, (int64_t)gi);
+                    in_callback = false;
+                    if (!(r >= 0)) throw std::runtime_error("a structural topology reaction's rate function gave a rate "
+                                                            "below 0 or not a number");
+                    g.rates[k] = r;
+                }
+            g.rates_valid = true;
+        }
+    std::vector<TopCandidate> cand;
+    if (!RS.empty()) {
+        if (!nl_ready) throw LogicError("topology reactions: the neighbor list is not set up");
+        const int T = ctx.ntypes;
+        std::vector<uint32_t> mask(T, 0u);
+        double rmax = 0;
+        for (const auto &r : RS) {
+            mask[r.t1] |= 1u << r.t2;
+            mask[r.t2] |= 1u << r.t1;
+            rmax = std::max(rmax, r.radius);
+        }
+        if (!top_mask_dev) {
+            top_mask_dev = dalloc<uint32_t>(MAX_TYPES);
+            top_n_dev = dalloc<int>(1);
+        }
+        RDC_CUDA(cudaMemcpyAsync(top_mask_dev, mask.data(), sizeof(uint32_t) * T, cudaMemcpyHostToDevice, stream));
+        const double r2max = rmax * rmax;
+        const float r2screen = (float)r2max + 2.0f * band_for(rmax, d.geo.L);
+        int nc = 0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            if (cand_cap == 0) {
+                cand_cap = 4096;
+                cand_dev = dalloc<TopCandidate>(cand_cap);
+            }
+            launch_topology_candidates(d, top_mask_dev, r2max, r2screen, cand_dev, top_n_dev, cand_cap, stream);
+            RDC_CUDA(cudaMemcpyAsync(&nc, top_n_dev, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            sync();
+            if (nc <= cand_cap) break;
+            dfree(cand_dev);
+            cand_cap = nc + nc / 2;
             cand_dev = dalloc<TopCandidate>(cand_cap);
         }
-        launch_topology_candidates(d, mask_dev, r2max, r2screen, cand_dev, n_dev, cand_cap, stream);
-        RDC_CUDA(cudaMemcpyAsync(&nc, n_dev, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        cand.resize(std::min(nc, cand_cap));
+        if (!cand.empty())
+            RDC_CUDA(cudaMemcpyAsync(cand.data(), cand_dev, sizeof(TopCandidate) * cand.size(), cudaMemcpyDeviceToHost,
+                                     stream));
         sync();
-        if (nc <= cand_cap) break;
-        dfree(cand_dev); dfree(top_mask_dev); dfree(top_n_dev); dfree(edit_dev);
-        cand_cap = nc + nc / 2;
-        cand_dev = dalloc<TopCandidate>(cand_cap);
     }
-    std::vector<TopCandidate> cand(std::min(nc, cand_cap));
-    if (!cand.empty())
-        RDC_CUDA(cudaMemcpyAsync(cand.data(), cand_dev, sizeof(TopCandidate) * cand.size(), cudaMemcpyDeviceToHost,
-                                 stream));
-    sync();
     // topology and vertex of every slot
     std::vector<int> slot_graph(n_top, -1), slot_vertex(n_top, -1);
     for (size_t gi = 0; gi < graphs.size(); ++gi)
@@ -980,14 +1031,23 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
         return dist[to];
     };
     struct Event {
-        int r;          // reaction
-        int c;          // candidate
+        int r;          // reaction (spatial or structural)
+        int c;          // spatial: candidate; structural: -1
         bool swap;      // the candidate's j side is the reaction's first educt
-        int g1, g2;     // topologies of the first and second educt (g2 = -1: free particle)
+        int g1, g2;     // topologies of the first and second educt (g2 = -1: free particle or structural)
         double clock;
         bool fire;
     };
     std::vector<Event> ev;
+    for (size_t gi = 0; gi < graphs.size() && !structural.empty(); ++gi)
+        for (int k = 0; k < (int)structural.size(); ++k) {
+            const double rate = graphs[gi].rates[k];
+            if (!(rate > 0)) continue;
+            const U4 u = rng_draw(seed, slot_id[graphs[gi].slots[0]], (uint32_t)k, call, RNG_STRUCTURAL, 0u);
+            const double e1 = -std::log(((double)(u.x >> 8) + 0.5) * (1.0 / 16777216.0));
+            const bool fire = (((uint64_t)u.y << 32) | u.z) < coin_threshold(rate, dt);
+            ev.push_back(Event{k, -1, false, (int)gi, -1, e1 / rate, fire});
+        }
     for (int c = 0; c < (int)cand.size(); ++c) {
         const TopCandidate &q = cand[c];
         const int ga = graph_of(q.si), gb = graph_of(q.sj);
@@ -1019,11 +1079,121 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
     for (size_t k = 0; k < ev.size(); ++k) order[k] = (int)k;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ev[a].clock < ev[b].clock; });
     std::vector<char> used(graphs.size(), 0), dead(graphs.size(), 0);
+    std::vector<TopGraph> children;  // pieces of topologies that structural reactions split
     std::unordered_set<uint32_t> used_free;
-    std::vector<int4> edits;  // (storage index, type, new slot or -1, -)
+    std::vector<int4> edits;  // (storage index or topology slot, type, new slot or -1, 1: x is a slot)
     int64_t performed = 0;
+    // The reference's structural events all carry the second particle index 0 and no second topology, so its
+    // eventsDependent (CPUEvaluateTopologyReactions.cpp:459-468) takes any two of them as dependent: one
+    // accepted structural event removes every other one of the evaluation
+    bool structural_done = false;
     for (int k : order) {
         const Event &e = ev[k];
+        if (e.c < 0) {  // structural
+            if (used[e.g1] || structural_done) continue;
+            if (!e.fire) continue;
+            structural_done = true;
+            const auto &sr = structural[e.r];
+            rdc_recipe recipe;
+            in_callback = true;
+            sr.reaction(sr.user, this, (int64_t)e.g1, &recipe);
+            in_callback = false;
+            TopGraph &g = graphs[e.g1];
+            const int nv = (int)g.slots.size();
+            for (const auto &op : recipe.ops) {
+                auto vertex = [&](int64_t v) {
+                    if (v < 0 || v >= nv) throw InvalidArgument("recipe vertex index out of range");
+                    return (int)v;
+                };
+                auto find_edge = [&](int a, int b) {
+                    for (size_t x = 0; x < g.edges.size(); ++x)
+                        if ((g.edges[x].first == a && g.edges[x].second == b) ||
+                            (g.edges[x].first == b && g.edges[x].second == a))
+                            return (int)x;
+                    return -1;
+                };
+                switch (op.kind) {
+                    case RECIPE_CHANGE_PARTICLE_TYPE: {
+                        const int v = vertex(op.a);
+                        if (op.type < 0 || op.type >= ctx.ntypes) throw InvalidArgument("particle type out of range");
+                        slot_type[g.slots[v]] = op.type;
+                        edits.push_back(make_int4(g.slots[v], op.type, -1, 1));
+                        break;
+                    }
+                    case RECIPE_ADD_EDGE: {
+                        const int a = vertex(op.a), b = vertex(op.b);
+                        if (a == b) throw InvalidArgument("recipe: an edge needs two vertices");
+                        if (find_edge(a, b) < 0) g.edges.emplace_back(a, b);
+                        break;
+                    }
+                    case RECIPE_REMOVE_EDGE: {
+                        const int x = find_edge(vertex(op.a), vertex(op.b));
+                        if (x < 0) throw InvalidArgument("recipe: the edge to remove does not exist");
+                        g.edges.erase(g.edges.begin() + x);
+                        break;
+                    }
+                    case RECIPE_SEPARATE_VERTEX: {
+                        const int v = vertex(op.a);
+                        std::vector<std::pair<int, int>> kept;
+                        for (auto &x : g.edges)
+                            if (x.first != v && x.second != v) kept.push_back(x);
+                        g.edges = std::move(kept);
+                        break;
+                    }
+                    case RECIPE_CHANGE_TOPOLOGY_TYPE:
+                        if (op.type < 0) throw InvalidArgument("topology type must be >= 0");
+                        g.type = op.type;
+                        break;
+                }
+            }
+            g.rates_valid = false;
+            // connected components: a topology that falls apart becomes its pieces (or raises)
+            std::vector<std::vector<int>> adj(nv);
+            for (auto &x : g.edges) {
+                adj[x.first].push_back(x.second);
+                adj[x.second].push_back(x.first);
+            }
+            std::vector<int> comp(nv, -1);
+            int ncomp = 0;
+            for (int v = 0; v < nv; ++v) {
+                if (comp[v] >= 0) continue;
+                std::vector<int> stack{v};
+                comp[v] = ncomp;
+                while (!stack.empty()) {
+                    const int u = stack.back();
+                    stack.pop_back();
+                    for (int w : adj[u])
+                        if (comp[w] < 0) {
+                            comp[w] = ncomp;
+                            stack.push_back(w);
+                        }
+                }
+                ++ncomp;
+            }
+            if (ncomp > 1) {
+                if (sr.expect_connected)
+                    throw LogicError("The topology was expected to still be connected after the reaction, but it was "
+                                     "not");
+                std::vector<TopGraph> parts(ncomp);
+                std::vector<int> local(nv);
+                for (int v = 0; v < nv; ++v) {
+                    local[v] = (int)parts[comp[v]].slots.size();
+                    parts[comp[v]].slots.push_back(g.slots[v]);
+                    parts[comp[v]].type = g.type;
+                }
+                for (auto &x : g.edges) parts[comp[x.first]].edges.emplace_back(local[x.first], local[x.second]);
+                for (auto &part : parts)
+                    if (!(part.slots.size() == 1 && ctx.flavor[slot_type[part.slots[0]]] == FLAVOR_NORMAL))
+                        children.push_back(std::move(part));
+                dead[e.g1] = 1;
+            } else if (nv == 1 && ctx.flavor[slot_type[g.slots[0]]] == FLAVOR_NORMAL) {
+                dead[e.g1] = 1;  // a single particle of NORMAL flavor is no topology (Utils.h:70-80)
+            }
+            used[e.g1] = 1;
+            ++structural_counts[e.r];
+            ++performed;
+            continue;
+        }
         const TopCandidate &q = cand[e.c];
         const uint32_t free_id = e.g2 < 0 ? (e.swap ? q.idi : q.idj) : 0;
         if (used[e.g1] || (e.g2 >= 0 && used[e.g2]) || (e.g2 < 0 && used_free.count(free_id))) continue;
@@ -1076,24 +1246,29 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
                 g2.edges.clear();
                 dead[e.g2] = 1;
             }
+            g2.rates_valid = false;
             used[e.g2] = 1;
         }
+        g1.rates_valid = false;
         used[e.g1] = 1;
         ++topo_counts[e.r];
         ++performed;
     }
     if (performed == 0) return 0;
-    if ((int)edits.size() > edit_cap) {
-        dfree(edit_dev);
-        edit_cap = (int)edits.size() * 2;
-        edit_dev = dalloc<int4>(edit_cap);
+    if (!edits.empty()) {
+        if ((int)edits.size() > edit_cap) {
+            dfree(edit_dev);
+            edit_cap = (int)edits.size() * 2;
+            edit_dev = dalloc<int4>(edit_cap);
+        }
+        RDC_CUDA(cudaMemcpyAsync(edit_dev, edits.data(), sizeof(int4) * edits.size(), cudaMemcpyHostToDevice, stream));
+        launch_particle_edits(d, edit_dev, (int)edits.size(), stream);
+        sync();
     }
-    RDC_CUDA(cudaMemcpyAsync(edit_dev, edits.data(), sizeof(int4) * edits.size(), cudaMemcpyHostToDevice, stream));
-    launch_particle_edits(d, edit_dev, (int)edits.size(), stream);
-    sync();
     std::vector<TopGraph> kept;
     for (size_t gi = 0; gi < graphs.size(); ++gi)
         if (!dead[gi]) kept.push_back(std::move(graphs[gi]));
+    for (auto &c : children) kept.push_back(std::move(c));
     graphs = std::move(kept);
     Topology fresh;
     for (size_t gi = 0; gi < graphs.size(); ++gi) configure(graphs[gi], (int)gi, fresh);
@@ -1244,7 +1419,7 @@ void rdc_system::run(int64_t n_steps, double dt, int handler, int64_t stride, in
     // swaps starts and ends on the same buffers and can be replayed
     // with spatial topology reactions every step evaluates them on the host, between the reactions and the
     // forces: the steps run one by one
-    topo_dt = (!ctx.spatial_top.empty() && !graphs.empty()) ? dt : 0.0;
+    topo_dt = ((!ctx.spatial_top.empty() || !this->structural.empty()) && !graphs.empty()) ? dt : 0.0;
     const int64_t reps = topo_dt > 0 ? 0 : n_steps / per_graph;
     if (reps > 0) {
         invalidate_graph();
@@ -1643,6 +1818,92 @@ int rdc_evaluate_topology_reactions(rdc_system *s, double time_step, int64_t *n_
         require(s != nullptr, "null argument");
         const int64_t n = s->evaluate_topology_reactions(time_step);
         if (n_performed) *n_performed = n;
+    });
+}
+int rdc_add_structural_topology_reaction(rdc_system *s, int topology_type, rdc_topology_rate_fn rate,
+                                         rdc_topology_recipe_fn reaction, void *user, int expect_connected,
+                                         int *reaction_id) {
+    return guarded([&] {
+        require(s && rate && reaction, "null argument");
+        require(topology_type >= 0, "topology type must be >= 0");
+        if (s->in_callback) throw LogicError("reactions cannot be added from a reaction's own function");
+        s->structural.push_back(StructuralReaction{topology_type, rate, reaction, user, expect_connected != 0});
+        for (auto &g : s->graphs) g.rates_valid = false;
+        if (reaction_id) *reaction_id = (int)s->structural.size() - 1;
+    });
+}
+int rdc_get_structural_reaction_counts(rdc_system *s, int n, int64_t *counts) {
+    return guarded([&] {
+        require(s && (n == 0 || counts), "null argument");
+        require(n == (int)s->structural.size(), "n must equal the number of structural topology reactions");
+        for (int k = 0; k < n; ++k)
+            counts[k] = k < (int)s->structural_counts.size() ? (int64_t)s->structural_counts[k] : 0;
+    });
+}
+static int recipe_op(rdc_recipe *r, RecipeOp op) {
+    return guarded([&] {
+        require(r != nullptr, "null recipe");
+        r->ops.push_back(op);
+    });
+}
+int rdc_recipe_change_particle_type(rdc_recipe *r, int64_t vertex, int type) {
+    return recipe_op(r, RecipeOp{RECIPE_CHANGE_PARTICLE_TYPE, vertex, 0, type});
+}
+int rdc_recipe_add_edge(rdc_recipe *r, int64_t v1, int64_t v2) { return recipe_op(r, RecipeOp{RECIPE_ADD_EDGE, v1, v2, 0}); }
+int rdc_recipe_remove_edge(rdc_recipe *r, int64_t v1, int64_t v2) {
+    return recipe_op(r, RecipeOp{RECIPE_REMOVE_EDGE, v1, v2, 0});
+}
+int rdc_recipe_separate_vertex(rdc_recipe *r, int64_t vertex) {
+    return recipe_op(r, RecipeOp{RECIPE_SEPARATE_VERTEX, vertex, 0, 0});
+}
+int rdc_recipe_change_topology_type(rdc_recipe *r, int type) {
+    return recipe_op(r, RecipeOp{RECIPE_CHANGE_TOPOLOGY_TYPE, 0, 0, type});
+}
+int rdc_get_topology(rdc_system *s, int64_t k, int *topology_type, int64_t capacity, uint64_t *ids, int *types,
+                     int64_t *n_vertices, int64_t capacity_edges, int64_t *edges2, int64_t *n_edges) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        require(k >= 0 && k < (int64_t)s->graphs.size(), "topology index out of range");
+        const TopGraph &g = s->graphs[k];
+        if (topology_type) *topology_type = g.type;
+        if (n_vertices) *n_vertices = (int64_t)g.slots.size();
+        if (n_edges) *n_edges = (int64_t)g.edges.size();
+        if ((ids || types) && capacity < (int64_t)g.slots.size())
+            throw CapacityError("output capacity too small for the topology's particles");
+        if (edges2 && capacity_edges < (int64_t)g.edges.size())
+            throw CapacityError("output capacity too small for the topology's edges");
+        for (size_t v = 0; v < g.slots.size(); ++v) {
+            if (ids) ids[v] = s->slot_id[g.slots[v]];
+            if (types) types[v] = s->slot_type[g.slots[v]];
+        }
+        if (edges2)
+            for (size_t e = 0; e < g.edges.size(); ++e) {
+                edges2[2 * e] = g.edges[e].first;
+                edges2[2 * e + 1] = g.edges[e].second;
+            }
+    });
+}
+int rdc_get_topology_positions(rdc_system *s, int64_t k, int64_t capacity, double *positions3) {
+    return guarded([&] {
+        require(s && positions3, "null argument");
+        require(k >= 0 && k < (int64_t)s->graphs.size(), "topology index out of range");
+        const TopGraph &g = s->graphs[k];
+        const int n = (int)g.slots.size();
+        if (capacity < n) throw CapacityError("output capacity too small for the topology's particles");
+        int *slots_dev = dalloc<int>(n);
+        float4 *out_dev = dalloc<float4>(n);
+        RDC_CUDA(cudaMemcpyAsync(slots_dev, g.slots.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+        launch_gather_slots(s->d, slots_dev, n, out_dev, s->stream);
+        std::vector<float4> h(n);
+        RDC_CUDA(cudaMemcpyAsync(h.data(), out_dev, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+        s->sync();
+        dfree(slots_dev);
+        dfree(out_dev);
+        for (int v = 0; v < n; ++v) {
+            positions3[3 * v] = h[v].x;
+            positions3[3 * v + 1] = h[v].y;
+            positions3[3 * v + 2] = h[v].z;
+        }
     });
 }
 int rdc_get_topology_reaction_counts(rdc_system *s, int n, int64_t *counts) {

@@ -46,7 +46,7 @@ __host__ __device__ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
 // purposes (the 4th counter word) keep the streams of different uses disjoint
 enum : uint32_t {
     RNG_BD = 1u, RNG_COIN1 = 2u, RNG_COIN2 = 3u, RNG_PRIO1 = 4u, RNG_PRIO2 = 5u, RNG_FISSION = 6u, RNG_BREAK = 7u,
-    RNG_TOPOLOGY = 8u
+    RNG_TOPOLOGY = 8u, RNG_STRUCTURAL = 9u
 };
 
 __host__ __device__ inline U4 rng_draw(uint64_t seed, uint32_t a, uint32_t b, uint64_t step, uint32_t purpose,

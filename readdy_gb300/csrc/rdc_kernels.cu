@@ -438,14 +438,31 @@ void launch_topology_candidates(const SysDev &s, const uint32_t *pair_mask, doub
 __global__ void k_particle_edits(SysDev s, const int4 *__restrict__ edits, int n) {
     GRID_STRIDE(k, n) {
         const int4 e = edits[k];
-        float4 p = s.pos[e.x];
+        int i = e.x;
+        if (e.w == 1) {  // x names a topology slot
+            if (e.x < 0 || e.x >= s.tloc_size) continue;
+            i = s.tloc[e.x];
+        }
+        float4 p = s.pos[i];
         p.w = __int_as_float(e.y);
-        s.pos[e.x] = p;
+        s.pos[i] = p;
         if (e.z >= 0) {
-            s.tslot[e.x] = e.z;
-            if (e.z < s.tloc_size) s.tloc[e.z] = e.x;
+            s.tslot[i] = e.z;
+            if (e.z < s.tloc_size) s.tloc[e.z] = i;
         }
     }
+}
+
+// positions of the particles of topology slots slots[0, n)
+__global__ void k_gather_slots(SysDev s, const int *__restrict__ slots, int n, float4 *out) {
+    GRID_STRIDE(k, n) {
+        const int t = slots[k];
+        out[k] = (t >= 0 && t < s.tloc_size) ? s.pos[s.tloc[t]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+void launch_gather_slots(const SysDev &s, const int *slots, int n, float4 *out, cudaStream_t st) {
+    if (n > 0) k_gather_slots<<<std::min((n + 255) / 256, GRID_BLOCKS), 256, 0, st>>>(s, slots, n, out);
 }
 
 void launch_particle_edits(const SysDev &s, const int4 *edits, int n, cudaStream_t st) {

@@ -185,6 +185,48 @@ class Context:
                                                                 float(multiplicity), phi0))
 
 
+class TopologyView:
+    """One topology as a structural reaction's functions see it (GraphTopology): its index, its type, the ids
+    and types of its particles by local vertex, its edges as local vertex pairs, and on request the
+    positions."""
+
+    def __init__(self, lib, handle, index):
+        self._lib, self._h, self.index = lib, handle, int(index)
+        tt, nv, ne = C.c_int(), C.c_int64(), C.c_int64()
+        N.check(lib.rdc_get_topology(handle, self.index, C.byref(tt), 0, None, None, C.byref(nv), 0, None,
+                                     C.byref(ne)))
+        self.type = tt.value
+        self.ids = np.zeros(nv.value, np.uint64)
+        self.types = np.zeros(nv.value, np.int32)
+        edges = np.zeros((ne.value, 2), np.int64)
+        N.check(lib.rdc_get_topology(handle, self.index, None, nv.value, _p(self.ids, C.c_uint64),
+                                     _p(self.types, C.c_int), C.byref(nv), ne.value, _p(edges, C.c_int64),
+                                     C.byref(ne)))
+        self.edges = edges
+
+    @property
+    def n_particles(self) -> int:
+        return len(self.ids)
+
+    @property
+    def positions(self):
+        out = np.zeros((len(self.ids), 3))
+        N.check(self._lib.rdc_get_topology_positions(self._h, self.index, len(self.ids), _p(out, C.c_double)))
+        return out
+
+
+# recipe steps (Recipe.h:74-110) as the reaction function returns them
+RECIPE_STEPS = ("change_particle_type", "add_edge", "remove_edge", "separate_vertex", "change_topology_type")
+
+
+def _apply_recipe(lib, recipe, steps):
+    for step in steps or ():
+        name, args = step[0], [int(a) for a in step[1:]]
+        if name not in RECIPE_STEPS:
+            raise ValueError(f"unknown recipe step {name!r}")
+        N.check(getattr(lib, "rdc_recipe_" + name)(recipe, *args))
+
+
 class CUDAKernel:
     """One simulation on the GPU: state model plus the ActionFactory's actions."""
 
@@ -235,10 +277,58 @@ class CUDAKernel:
                                           _p(thr, C.c_double), _p(rate, C.c_double), C.byref(nb)))
         return nb.value
 
+    def _check_callbacks(self, rc):
+        """Status of a call that may run structural reaction functions: their own exception first."""
+        err = getattr(self, "_callback_error", None)
+        self._callback_error = None
+        if err is not None:
+            raise err
+        N.check(rc)
+
+    def add_structural_topology_reaction(self, topology_type, rate_function, reaction_function,
+                                         expect_connected=True):
+        """StructuralTopologyReaction on topologies of topology_type: rate_function(view) -> rate,
+        reaction_function(view) -> recipe steps, e.g. [("remove_edge", 3, 4), ("change_particle_type", 0, 2)]
+        (RECIPE_STEPS; vertices by local index of the view).  Without expect_connected a topology that falls
+        apart becomes its pieces.  Returns the reaction's index."""
+        lib = self._lib
+
+        def rate_cb(_user, _sys, k):
+            try:
+                return float(rate_function(TopologyView(lib, self._h, k)))
+            except BaseException as e:  # reported by the call that ran the function
+                self._callback_error = getattr(self, "_callback_error", None) or e
+                return float("nan")
+
+        def recipe_cb(_user, _sys, k, recipe):
+            try:
+                _apply_recipe(lib, recipe, reaction_function(TopologyView(lib, self._h, k)))
+            except BaseException as e:
+                self._callback_error = getattr(self, "_callback_error", None) or e
+                lib.rdc_recipe_change_particle_type(recipe, -1, 0)  # makes the evaluation fail
+
+        cbs = (N.TOPOLOGY_RATE_FN(rate_cb), N.TOPOLOGY_RECIPE_FN(recipe_cb))
+        self._callbacks = getattr(self, "_callbacks", []) + [cbs]
+        rid = C.c_int()
+        N.check(lib.rdc_add_structural_topology_reaction(self._h, int(topology_type), cbs[0], cbs[1], None,
+                                                        int(bool(expect_connected)), C.byref(rid)))
+        self._n_structural = getattr(self, "_n_structural", 0) + 1
+        return rid.value
+
+    def structural_reaction_counts(self):
+        n = getattr(self, "_n_structural", 0)
+        out = np.zeros(max(n, 1), np.int64)
+        N.check(self._lib.rdc_get_structural_reaction_counts(self._h, n, _p(out, C.c_int64)))
+        return out[:n]
+
+    def get_topology(self, index):
+        """TopologyView of the topology with this index (the order of get_topologies)."""
+        return TopologyView(self._lib, self._h, index)
+
     def evaluate_topology_reactions(self, time_step):
-        """EvaluateTopologyReactions (spatial reactions); returns the number of events performed."""
+        """EvaluateTopologyReactions (structural and spatial); returns the number of events performed."""
         n = C.c_int64()
-        N.check(self._lib.rdc_evaluate_topology_reactions(self._h, float(time_step), C.byref(n)))
+        self._check_callbacks(self._lib.rdc_evaluate_topology_reactions(self._h, float(time_step), C.byref(n)))
         return n.value
 
     def topology_reaction_counts(self):
@@ -383,8 +473,8 @@ class CUDAKernel:
         nrec = (n_steps // count_stride + 1) if count_stride > 0 else 0
         counts = np.zeros((max(nrec, 1), self.context.n_types), np.int64)
         got = C.c_int64()
-        N.check(self._lib.rdc_run(self._h, int(n_steps), float(dt), int(handler), int(count_stride),
-                                  _p(counts, C.c_int64) if nrec else None, nrec, C.byref(got)))
+        self._check_callbacks(self._lib.rdc_run(self._h, int(n_steps), float(dt), int(handler), int(count_stride),
+                                                _p(counts, C.c_int64) if nrec else None, nrec, C.byref(got)))
         return counts[:got.value]
 
     def neighbor_pairs(self, cutoff):

@@ -192,3 +192,30 @@ def check_topology_case(case, tops, types_by_id, pos_by_id, edges):
         ends = sorted(i for i, d in deg.items() if d == 1)
         assert all(types_by_id[i] == 1 for i in ends)
         assert sorted(pos_by_id[i][0] for i in ends) == pytest.approx(exp["end_x"])
+
+
+def structural_system(make, n_small=1, chain=None, seed=1):
+    """The fixture of readdy/test/TestTopologyReactions.cpp:82-95 on the oracle (make = "oracle") or the device
+    (make = a readdy_gb300 module): Topology A 0, Topology B 1, Topology Invalid Type 2 (TOPOLOGY flavor),
+    A 3 (NORMAL), bonds k = 10, l0 = 10 among the topology types, box 10.  Diffusion is 0: the cases test
+    the topology structure only.  Adds n_small copies of setUpSmallTopology (:55-67; three particles at
+    the origin, edges 0-1, 1-2) or, with `chain`, one chain of that many particles along x (:247-270)."""
+    box = (10.0, 10.0, 10.0)
+    if make == "oracle":
+        s = oracle.OracleSystem(list(box), (True, True, True), 1.0, (0.0,) * 4, seed=seed)
+        target = s
+    else:
+        ctx = make.Context(box, (True, True, True), 1.0, (0.0,) * 4)
+        target = ctx
+    for t, fl in ((0, 1), (1, 1), (2, 1), (3, 0)):
+        target.set_particle_flavor(t, fl)
+    for a, b in ((0, 0), (0, 1), (1, 1)):
+        target.configure_harmonic_bond(a, b, 10.0, 10.0)
+    if make != "oracle":
+        s = make.CUDAKernel(ctx, seed=seed)
+    if chain:
+        pos = np.stack([-5 + np.arange(chain) * 10.0 / chain, np.zeros(chain), np.zeros(chain)], 1)
+        s.add_topology(pos, np.zeros(chain, np.int32), [(i, i + 1) for i in range(chain - 1)])
+    for _ in range(n_small):
+        s.add_topology(np.zeros((3, 3)), np.zeros(3, np.int32), [(0, 1), (1, 2)])
+    return s
