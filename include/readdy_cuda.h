@@ -192,6 +192,12 @@ int rdc_recipe_add_edge(rdc_recipe *r, int64_t v1, int64_t v2);
 int rdc_recipe_remove_edge(rdc_recipe *r, int64_t v1, int64_t v2);
 int rdc_recipe_separate_vertex(rdc_recipe *r, int64_t vertex);
 int rdc_recipe_change_topology_type(rdc_recipe *r, int type);
+/* a new particle of `type` at pos3, joined to the given vertices (CPUAppendParticle,
+ * include/readdy/kernel/cpu/actions/topologies/CPUTopologyActions.h:112-131); it becomes the topology's last vertex */
+int rdc_recipe_append_particle(rdc_recipe *r, int64_t n_neighbors, const int64_t *neighbors, int type,
+                               const double *pos3);
+/* moves a vertex's particle to pos3 (wrapped into the box on periodic axes) */
+int rdc_recipe_change_particle_position(rdc_recipe *r, int64_t vertex, const double *pos3);
 /* one topology (index k of rdc_get_topologies): type, particle ids and types by local vertex, edges as local
  * vertex pairs; counts are written first, RDC_ERR_CAPACITY if an output does not fit; outputs may be NULL */
 int rdc_get_topology(rdc_system *s, int64_t k, int *topology_type, int64_t capacity, uint64_t *ids, int *types,

@@ -81,6 +81,8 @@ def _load():
             "orc_recipe_remove_edge": (i, [vp, i64, i64]),
             "orc_recipe_separate_vertex": (i, [vp, i64]),
             "orc_recipe_change_topology_type": (i, [vp, i]),
+            "orc_recipe_append_particle": (i, [vp, i64, P(i64), i, P(d)]),
+            "orc_recipe_change_particle_position": (i, [vp, i64, P(d)]),
             "orc_get_topology": (i, [vp, i64, P(i), P(u64), P(i), P(d), P(i64), P(i64), P(i64)]),
             "orc_add_particles": (i, [vp, i, P(d), P(i)]),
             "orc_n_particles": (i, [vp]),
@@ -336,7 +338,16 @@ class OracleSystem:
         def recipe_cb(_u, _s, k, recipe):
             try:
                 for step in reaction_function(TopologyView(lib, h, k)) or ():
-                    getattr(lib, "orc_recipe_" + step[0])(recipe, *[int(a) for a in step[1:]])
+                    if step[0] == "append_particle":
+                        nb = np.ascontiguousarray(step[1], dtype=np.int64)
+                        pos = np.ascontiguousarray(step[3], dtype=np.float64)
+                        lib.orc_recipe_append_particle(recipe, len(nb), _ptr(nb, C.c_int64), int(step[2]),
+                                                       _ptr(pos, C.c_double))
+                    elif step[0] == "change_particle_position":
+                        pos = np.ascontiguousarray(step[2], dtype=np.float64)
+                        lib.orc_recipe_change_particle_position(recipe, int(step[1]), _ptr(pos, C.c_double))
+                    else:
+                        getattr(lib, "orc_recipe_" + step[0])(recipe, *[int(a) for a in step[1:]])
             except BaseException as e:
                 self._callback_error = getattr(self, "_callback_error", None) or e
                 lib.orc_recipe_change_particle_type(recipe, -1, 0)

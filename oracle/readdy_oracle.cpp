@@ -372,7 +372,13 @@ inline std::pair<size_t, size_t> chunk(size_t n, int parts, int t) {
 }  // namespace
 
 struct orc_recipe {
-    struct Op { int kind; int64_t a, b; int type; };
+    struct Op {
+        int kind;
+        int64_t a, b;
+        int type;
+        std::vector<int64_t> neighbors;
+        double pos[3];
+    };
     std::vector<Op> ops;
 };
 
@@ -573,7 +579,7 @@ struct orc_system {
                     if (structural[k].topologyType == graphs[gi].type)
                         graphRates[gi][k] = structural[k].rate(structural[k].user, this, (int64_t)gi);
             }
-        const IdMap idx = idMap();
+        IdMap idx = idMap();
         std::vector<long> topOf(entries.size(), -1);
         std::vector<int> vertexOf(entries.size(), -1);
         for (size_t gi = 0; gi < graphs.size(); ++gi)
@@ -648,9 +654,8 @@ struct orc_system {
             orc_recipe recipe;
             sr.reaction(sr.user, this, (int64_t)ev.g1, &recipe);
             Graph &g = graphs[ev.g1];
-            const int nv = (int)g.ids.size();
             auto vtx = [&](int64_t v) {
-                if (v < 0 || v >= nv) throw std::invalid_argument("recipe vertex index out of range");
+                if (v < 0 || v >= (int64_t)g.ids.size()) throw std::invalid_argument("recipe vertex index out of range");
                 return (int)v;
             };
             auto findEdge = [&](int a, int b) {
@@ -675,8 +680,27 @@ struct orc_system {
                     g.edges = std::move(kept);
                 } else if (op.kind == 4) {
                     g.type = op.type;
+                } else if (op.kind == 5) {  // CPUAppendParticle, CPUTopologyActions.h:112-131
+                    if (op.neighbors.empty()) throw std::invalid_argument("recipe: a new particle needs a neighbour");
+                    std::vector<int> nb;
+                    for (int64_t x : op.neighbors) nb.push_back(vtx(x));
+                    Entry en;
+                    en.pos = {op.pos[0], op.pos[1], op.pos[2]};
+                    box.fix(en.pos);
+                    en.type = op.type;
+                    en.id = nextId++;
+                    idx[en.id] = addEntry(en);
+                    g.ids.push_back(en.id);
+                    const int nvx = (int)g.ids.size() - 1;
+                    for (int v : nb)
+                        if (findEdge(v, nvx) < 0) g.edges.push_back({v, nvx});
+                } else if (op.kind == 6) {
+                    V3 p{op.pos[0], op.pos[1], op.pos[2]};
+                    box.fix(p);
+                    entries[indexOf(idx, g.ids[vtx(op.a)])].pos = p;
                 }
             }
+            const int nv = (int)g.ids.size();
             changed[ev.g1] = 1;
             std::vector<std::vector<int>> nb(nv);
             for (auto &e : g.edges) { nb[e.first].push_back(e.second); nb[e.second].push_back(e.first); }
@@ -1746,6 +1770,14 @@ int orc_recipe_add_edge(orc_recipe *r, int64_t a, int64_t b) { r->ops.push_back(
 int orc_recipe_remove_edge(orc_recipe *r, int64_t a, int64_t b) { r->ops.push_back({2, a, b, 0}); return 0; }
 int orc_recipe_separate_vertex(orc_recipe *r, int64_t v) { r->ops.push_back({3, v, 0, 0}); return 0; }
 int orc_recipe_change_topology_type(orc_recipe *r, int type) { r->ops.push_back({4, 0, 0, type}); return 0; }
+int orc_recipe_append_particle(orc_recipe *r, int64_t n, const int64_t *nb, int type, const double *pos3) {
+    r->ops.push_back({5, 0, 0, type, std::vector<int64_t>(nb, nb + n), {pos3[0], pos3[1], pos3[2]}});
+    return 0;
+}
+int orc_recipe_change_particle_position(orc_recipe *r, int64_t v, const double *pos3) {
+    r->ops.push_back({6, v, 0, 0, {}, {pos3[0], pos3[1], pos3[2]}});
+    return 0;
+}
 int orc_get_topology(const orc_system *s, int64_t k, int *type, uint64_t *ids, int *types, double *pos3,
                      int64_t *n_vertices, int64_t *edges2, int64_t *n_edges) {
     if (k < 0 || k >= (int64_t)s->graphs.size()) { g_err = "topology index out of range"; return -1; }

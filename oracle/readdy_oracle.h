@@ -96,6 +96,8 @@ int orc_recipe_add_edge(orc_recipe *r, int64_t v1, int64_t v2);
 int orc_recipe_remove_edge(orc_recipe *r, int64_t v1, int64_t v2);
 int orc_recipe_separate_vertex(orc_recipe *r, int64_t vertex);
 int orc_recipe_change_topology_type(orc_recipe *r, int type);
+int orc_recipe_append_particle(orc_recipe *r, int64_t n_neighbors, const int64_t *neighbors, int type, const double *pos3);
+int orc_recipe_change_particle_position(orc_recipe *r, int64_t vertex, const double *pos3);
 /* topology k: type, particle ids, types and positions by local vertex, edges as local pairs (outputs may be NULL) */
 int orc_get_topology(const orc_system *s, int64_t k, int *type, uint64_t *ids, int *types, double *pos3,
                      int64_t *n_vertices, int64_t *edges2, int64_t *n_edges);

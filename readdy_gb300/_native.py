@@ -87,6 +87,8 @@ def _sig(lib):
         "rdc_recipe_remove_edge": (i, [vp, i64, i64]),
         "rdc_recipe_separate_vertex": (i, [vp, i64]),
         "rdc_recipe_change_topology_type": (i, [vp, i]),
+        "rdc_recipe_append_particle": (i, [vp, i64, P(i64), i, P(d)]),
+        "rdc_recipe_change_particle_position": (i, [vp, i64, P(d)]),
         "rdc_get_topology": (i, [vp, i64, P(i), i64, P(u64), P(i), P(i64), i64, P(i64), P(i64)]),
         "rdc_get_topology_positions": (i, [vp, i64, i64, P(d)]),
         "rdc_get_topology_edges": (i, [vp, i64, P(i64), i64, P(u64), P(i64), P(i64)]),

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -12,6 +13,7 @@
 #include <memory>
 #include <string>
 #include <tuple>
+#include <unordered_map>
 #include <unordered_set>
 #include <vector>
 
@@ -333,11 +335,13 @@ struct TopGraph {
 
 // recipe operations of a structural topology reaction (include/readdy/model/topologies/reactions/Recipe.h)
 enum : int { RECIPE_CHANGE_PARTICLE_TYPE = 0, RECIPE_ADD_EDGE = 1, RECIPE_REMOVE_EDGE = 2, RECIPE_SEPARATE_VERTEX = 3,
-             RECIPE_CHANGE_TOPOLOGY_TYPE = 4 };
+             RECIPE_CHANGE_TOPOLOGY_TYPE = 4, RECIPE_APPEND_PARTICLE = 5, RECIPE_CHANGE_PARTICLE_POSITION = 6 };
 struct RecipeOp {
     int kind;
     int64_t a, b;
     int type;
+    std::vector<int64_t> neighbors;  // append: the new particle's neighbours
+    double pos[3];                   // append, change position
 };
 
 struct StructuralReaction {
@@ -1082,6 +1086,23 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
     std::vector<TopGraph> children;  // pieces of topologies that structural reactions split
     std::unordered_set<uint32_t> used_free;
     std::vector<int4> edits;  // (storage index or topology slot, type, new slot or -1, 1: x is a slot)
+    std::vector<int2> moved;  // position changes: (storage index or topology slot, 1: x is a slot)
+    std::vector<float4> moved_to;
+    std::unordered_map<int, int> appended;  // topology slot -> storage index of particles appended now
+    auto target_of = [&](int slot) {       // a slot's particle for the edit kernels
+        auto it = appended.find(slot);
+        return it != appended.end() ? make_int2(it->second, 0) : make_int2(slot, 1);
+    };
+    auto wrapped = [&](const double p[3]) {  // bcs::fixPosition on the periodic axes
+        double q[3] = {p[0], p[1], p[2]};
+        for (int a = 0; a < 3; ++a)
+            if (ctx.pbc[a]) {
+                const double L = (double)d.geo.L[a];
+                q[a] -= L * std::floor(q[a] / L + 0.5);
+                if (q[a] >= 0.5 * L) q[a] -= L;
+            }
+        return std::array<double, 3>{q[0], q[1], q[2]};
+    };
     int64_t performed = 0;
     // The reference's structural events all carry the second particle index 0 and no second topology, so its
     // eventsDependent (CPUEvaluateTopologyReactions.cpp:459-468) takes any two of them as dependent: one
@@ -1099,10 +1120,10 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
             sr.reaction(sr.user, this, (int64_t)e.g1, &recipe);
             in_callback = false;
             TopGraph &g = graphs[e.g1];
-            const int nv = (int)g.slots.size();
             for (const auto &op : recipe.ops) {
+                const int nv_now = (int)g.slots.size();
                 auto vertex = [&](int64_t v) {
-                    if (v < 0 || v >= nv) throw InvalidArgument("recipe vertex index out of range");
+                    if (v < 0 || v >= nv_now) throw InvalidArgument("recipe vertex index out of range");
                     return (int)v;
                 };
                 auto find_edge = [&](int a, int b) {
@@ -1117,7 +1138,37 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
                         const int v = vertex(op.a);
                         if (op.type < 0 || op.type >= ctx.ntypes) throw InvalidArgument("particle type out of range");
                         slot_type[g.slots[v]] = op.type;
-                        edits.push_back(make_int4(g.slots[v], op.type, -1, 1));
+                        const int2 t = target_of(g.slots[v]);
+                        edits.push_back(make_int4(t.x, op.type, -1, t.y));
+                        break;
+                    }
+                    case RECIPE_CHANGE_PARTICLE_POSITION: {
+                        const int v = vertex(op.a);
+                        const auto q = wrapped(op.pos);
+                        moved.push_back(target_of(g.slots[v]));
+                        moved_to.push_back(make_float4((float)q[0], (float)q[1], (float)q[2], 0.f));
+                        break;
+                    }
+                    case RECIPE_APPEND_PARTICLE: {  // CPUAppendParticle (CPUTopologyActions.h:112-131)
+                        if (op.neighbors.empty()) throw InvalidArgument("recipe: a new particle needs a neighbour");
+                        if (op.type < 0 || op.type >= ctx.ntypes) throw InvalidArgument("particle type out of range");
+                        std::vector<int> nbrs;
+                        for (int64_t x : op.neighbors) nbrs.push_back(vertex(x));
+                        const auto q = wrapped(op.pos);
+                        const double xyz[3] = {q[0], q[1], q[2]};
+                        int c[C_COUNT];
+                        read_counters(c);
+                        const int slot = n_top;
+                        grow_topology_slots(1);
+                        uint64_t id = 0;
+                        append(1, xyz, &op.type, &slot, &id);
+                        appended[slot] = c[C_N_TOTAL];
+                        slot_type.push_back(op.type);
+                        slot_id.push_back((uint32_t)id);
+                        g.slots.push_back(slot);
+                        const int nvx = (int)g.slots.size() - 1;
+                        for (int nb : nbrs)
+                            if (find_edge(nb, nvx) < 0) g.edges.emplace_back(nb, nvx);
                         break;
                     }
                     case RECIPE_ADD_EDGE: {
@@ -1147,6 +1198,7 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
                 }
             }
             g.rates_valid = false;
+            const int nv = (int)g.slots.size();
             // connected components: a topology that falls apart becomes its pieces (or raises)
             std::vector<std::vector<int>> adj(nv);
             for (auto &x : g.edges) {
@@ -1255,6 +1307,16 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
         ++performed;
     }
     if (performed == 0) return 0;
+    if (!moved.empty()) {
+        int2 *t_dev = dalloc<int2>(moved.size());
+        float4 *p_dev = dalloc<float4>(moved.size());
+        RDC_CUDA(cudaMemcpyAsync(t_dev, moved.data(), sizeof(int2) * moved.size(), cudaMemcpyHostToDevice, stream));
+        RDC_CUDA(cudaMemcpyAsync(p_dev, moved_to.data(), sizeof(float4) * moved.size(), cudaMemcpyHostToDevice, stream));
+        launch_position_edits(d, t_dev, p_dev, (int)moved.size(), stream);
+        sync();
+        dfree(t_dev);
+        dfree(p_dev);
+    }
     if (!edits.empty()) {
         if ((int)edits.size() > edit_cap) {
             dfree(edit_dev);
@@ -1273,7 +1335,8 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
     Topology fresh;
     for (size_t gi = 0; gi < graphs.size(); ++gi) configure(graphs[gi], (int)gi, fresh);
     top = std::move(fresh);
-    upload_topology(false);
+    // appended particles join the cells (and the slot map) with a sort; moved ones likewise
+    upload_topology(!appended.empty() || !moved.empty());
     return performed;
 }
 
@@ -1858,6 +1921,21 @@ int rdc_recipe_separate_vertex(rdc_recipe *r, int64_t vertex) {
 }
 int rdc_recipe_change_topology_type(rdc_recipe *r, int type) {
     return recipe_op(r, RecipeOp{RECIPE_CHANGE_TOPOLOGY_TYPE, 0, 0, type});
+}
+int rdc_recipe_change_particle_position(rdc_recipe *r, int64_t vertex, const double *pos3) {
+    return guarded([&] {
+        require(r && pos3, "null argument");
+        r->ops.push_back(RecipeOp{RECIPE_CHANGE_PARTICLE_POSITION, vertex, 0, 0, {}, {pos3[0], pos3[1], pos3[2]}});
+    });
+}
+int rdc_recipe_append_particle(rdc_recipe *r, int64_t n_neighbors, const int64_t *neighbors, int type,
+                               const double *pos3) {
+    return guarded([&] {
+        require(r && pos3 && (n_neighbors == 0 || neighbors), "null argument");
+        require(n_neighbors >= 0, "n_neighbors must be >= 0");
+        r->ops.push_back(RecipeOp{RECIPE_APPEND_PARTICLE, 0, 0, type,
+                                  std::vector<int64_t>(neighbors, neighbors + n_neighbors), {pos3[0], pos3[1], pos3[2]}});
+    });
 }
 int rdc_get_topology(rdc_system *s, int64_t k, int *topology_type, int64_t capacity, uint64_t *ids, int *types,
                      int64_t *n_vertices, int64_t capacity_edges, int64_t *edges2, int64_t *n_edges) {

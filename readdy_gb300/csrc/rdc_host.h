@@ -228,6 +228,7 @@ void launch_topology_candidates(const SysDev &s, const uint32_t *pair_mask, doub
 // index; with w = 1 the x names the topology slot of the particle instead of its storage index
 void launch_particle_edits(const SysDev &s, const int4 *edits, int n, cudaStream_t st);
 void launch_gather_slots(const SysDev &s, const int *slots, int n, float4 *out, cudaStream_t st);
+void launch_position_edits(const SysDev &s, const int2 *targets, const float4 *to, int n, cudaStream_t st);
 // edges: (slot1, slot2, first bond term, bond terms); thr and coin: T x T per type pair
 void launch_break_bonds(const SysDev &s, const int4 *edges, int n_edges, const double2 *bond_kl, const double *thr,
                         const uint64_t *coin, int T, uint64_t seed, uint64_t counter, int *out, int *out_n,

@@ -453,6 +453,27 @@ __global__ void k_particle_edits(SysDev s, const int4 *__restrict__ edits, int n
     }
 }
 
+// position changes: target x is a storage index (y = 0) or a topology slot (y = 1); the type is kept
+__global__ void k_position_edits(SysDev s, const int2 *__restrict__ targets, const float4 *__restrict__ to, int n) {
+    GRID_STRIDE(k, n) {
+        const int2 t = targets[k];
+        int i = t.x;
+        if (t.y == 1) {
+            if (t.x < 0 || t.x >= s.tloc_size) continue;
+            i = s.tloc[t.x];
+        }
+        float4 p = s.pos[i];
+        p.x = to[k].x;
+        p.y = to[k].y;
+        p.z = to[k].z;
+        s.pos[i] = p;
+    }
+}
+
+void launch_position_edits(const SysDev &s, const int2 *targets, const float4 *to, int n, cudaStream_t st) {
+    if (n > 0) k_position_edits<<<std::min((n + 255) / 256, GRID_BLOCKS), 256, 0, st>>>(s, targets, to, n);
+}
+
 // positions of the particles of topology slots slots[0, n)
 __global__ void k_gather_slots(SysDev s, const int *__restrict__ slots, int n, float4 *out) {
     GRID_STRIDE(k, n) {

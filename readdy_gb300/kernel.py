@@ -215,16 +215,28 @@ class TopologyView:
         return out
 
 
-# recipe steps (Recipe.h:74-110) as the reaction function returns them
-RECIPE_STEPS = ("change_particle_type", "add_edge", "remove_edge", "separate_vertex", "change_topology_type")
+# recipe steps (Recipe.h:74-110) as the reaction function returns them: ("change_particle_type", v, type),
+# ("add_edge", v1, v2), ("remove_edge", v1, v2), ("separate_vertex", v), ("change_topology_type", type),
+# ("append_particle", [neighbour vertices], type, (x, y, z)), ("change_particle_position", v, (x, y, z))
+RECIPE_STEPS = ("change_particle_type", "add_edge", "remove_edge", "separate_vertex", "change_topology_type",
+                "append_particle", "change_particle_position")
 
 
 def _apply_recipe(lib, recipe, steps):
     for step in steps or ():
-        name, args = step[0], [int(a) for a in step[1:]]
+        name = step[0]
         if name not in RECIPE_STEPS:
             raise ValueError(f"unknown recipe step {name!r}")
-        N.check(getattr(lib, "rdc_recipe_" + name)(recipe, *args))
+        if name == "append_particle":
+            nb = np.ascontiguousarray(step[1], dtype=np.int64)
+            pos = np.ascontiguousarray(step[3], dtype=np.float64)
+            N.check(lib.rdc_recipe_append_particle(recipe, len(nb), _p(nb, C.c_int64), int(step[2]),
+                                                   _p(pos, C.c_double)))
+        elif name == "change_particle_position":
+            pos = np.ascontiguousarray(step[2], dtype=np.float64)
+            N.check(lib.rdc_recipe_change_particle_position(recipe, int(step[1]), _p(pos, C.c_double)))
+        else:
+            N.check(getattr(lib, "rdc_recipe_" + name)(recipe, *[int(a) for a in step[1:]]))
 
 
 class CUDAKernel:

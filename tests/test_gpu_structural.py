@@ -135,3 +135,72 @@ def test_structural_recipe_matches_oracle_topologies_and_forces(rg):
     err = np.linalg.norm(fg - fo, axis=1) / np.maximum(np.linalg.norm(fo, axis=1), 1e-5 * scale)
     assert err.max() < 1e-5, err.max()
     np.testing.assert_allclose(k.energy, e_o, rtol=1e-5)
+
+
+def test_structural_append_and_move(rg):
+    """Recipe steps that add a particle (joined to vertices 0 and 2) and move one, with and without a
+    neighbour list; the new particle is on the device with its id, type and position."""
+    for with_nl in (False, True):
+        k = structural_system(rg)
+        if with_nl:
+            k.create_neighbor_list(1.0)
+        k.add_structural_topology_reaction(0, lambda v: 1e10 if v.n_particles == 3 else 0.0,
+                                           lambda v: [("append_particle", [0, 2], 1, (1.0, 2.0, 3.0)),
+                                                      ("change_particle_position", 1, (6.0, 0.5, -0.5))])
+        k.evaluate_topology_reactions(1.0)
+        v = k.get_topology(0)
+        assert v.n_particles == 4 and v.types.tolist() == [0, 0, 0, 1]
+        assert {frozenset(e) for e in v.edges.tolist()} == {frozenset(x) for x in ((0, 1), (1, 2), (0, 3), (2, 3))}
+        np.testing.assert_allclose(v.positions[3], (1.0, 2.0, 3.0))
+        np.testing.assert_allclose(v.positions[1], (-4.0, 0.5, -0.5))  # wrapped into the box
+        pos, t, ids = k.get_particles()
+        assert k.n_particles == 4 and int(v.ids[3]) in ids.tolist()
+        k.create_neighbor_list(1.0)
+        k.calculate_forces()
+        assert np.isfinite(k.energy)
+
+
+def test_structural_append_matches_oracle_forces(rg):
+    """A chain of 6: the recipe appends a particle joined to the last vertex and moves vertex 2; pieces, edges,
+    positions and bonded forces agree with the oracle's (1e-5)."""
+    rng = np.random.default_rng(4)
+    n = 6
+    steps = rng.normal(size=(n, 3))
+    steps /= np.linalg.norm(steps, axis=1, keepdims=True)
+    pos = f32(np.cumsum(steps, axis=0) * 0.3)
+    new_at = tuple(f32(pos[-1] + (0.25, 0.1, 0.0)))
+    moved_to = tuple(f32(pos[2] + (0.05, -0.05, 0.02)))
+    box = (10.0, 10.0, 10.0)
+    ctx = rg.Context(box, (True, True, True), 1.0, (0.0,) * 4)
+    o = oracle.OracleSystem(list(box), (True, True, True), 1.0, (0.0,) * 4, seed=3)
+    for sys_ in (ctx, o):
+        for t, fl in ((0, 1), (1, 1), (2, 1), (3, 0)):
+            sys_.set_particle_flavor(t, fl)
+        for a, b in ((0, 0), (0, 1), (1, 1)):
+            sys_.configure_harmonic_bond(a, b, 10.0, 0.3)
+        sys_.configure_harmonic_angle(0, 0, 1, 2.0, 2.5)
+    k = rg.CUDAKernel(ctx, seed=5)
+    edges = [(i, i + 1) for i in range(n - 1)]
+    k.add_topology(pos, np.zeros(n, np.int32), edges)
+    o.add_topology(pos, np.zeros(n, np.int32), edges)
+    recipe = [("append_particle", [n - 1], 1, new_at), ("change_particle_position", 2, moved_to)]
+    for sys_ in (k, o):
+        sys_.add_structural_topology_reaction(0, lambda v: 1e10 if v.n_particles == n else 0.0, lambda v: recipe)
+    k.create_neighbor_list(1.0)
+    o.nl_setup(1.0)
+    assert k.evaluate_topology_reactions(1e-3) == o.evaluate_topology_reactions(1e-3) == 1
+    vg, vo = k.get_topology(0), o.topology(0)
+    np.testing.assert_array_equal(vg.ids, vo.ids)
+    np.testing.assert_array_equal(vg.types, vo.types)
+    assert {frozenset(e) for e in vg.edges.tolist()} == {frozenset(e) for e in vo.edges.tolist()}
+    np.testing.assert_allclose(vg.positions, vo.positions, atol=1e-6)
+    o.nl_update()
+    k.calculate_forces()
+    e_o = o.calculate_forces()
+    fg, ig = k.get_forces()
+    _, _, io, fo, _ = o.particles()
+    fg, fo = fg[np.argsort(ig)], fo[np.argsort(io)]
+    scale = np.abs(fo).max()
+    err = np.linalg.norm(fg - fo, axis=1) / np.maximum(np.linalg.norm(fo, axis=1), 1e-5 * scale)
+    assert err.max() < 1e-5, err.max()
+    np.testing.assert_allclose(k.energy, e_o, rtol=1e-5)

@@ -75,3 +75,18 @@ def test_oracle_one_structural_event_per_evaluation():
         assert s.evaluate_topology_reactions(1.0) == 1
     changed = sum(1 for k in range(40) if s.topology(k).types[0] == 1)
     assert changed == 10 and list(s.structural_reaction_counts()) == [10]
+
+
+def test_oracle_structural_append_and_move():
+    """Recipe steps that add a particle (joined to vertices 0 and 2) and move one."""
+    s = structural_system("oracle")
+    s.add_structural_topology_reaction(0, lambda v: 1e10 if v.n_particles == 3 else 0.0,
+                                       lambda v: [("append_particle", [0, 2], 1, (1.0, 2.0, 3.0)),
+                                                  ("change_particle_position", 1, (6.0, 0.5, -0.5))])
+    s.evaluate_topology_reactions(1.0)
+    v = s.topology(0)
+    assert v.n_particles == 4 and v.types.tolist() == [0, 0, 0, 1]
+    assert {frozenset(e) for e in v.edges.tolist()} == {frozenset(x) for x in ((0, 1), (1, 2), (0, 3), (2, 3))}
+    np.testing.assert_allclose(v.positions[3], (1.0, 2.0, 3.0))
+    np.testing.assert_allclose(v.positions[1], (-4.0, 0.5, -0.5))  # wrapped into the box
+    assert s.n_particles == 4
