@@ -222,6 +222,10 @@ int rdc_get_particles(rdc_system *s, int64_t capacity, double *positions3, int *
                       int64_t *n_out);
 /* Forces observable (CPUObservables.cpp): per-particle forces, same order as rdc_get_particles */
 int rdc_get_forces(rdc_system *s, int64_t capacity, double *forces3, uint64_t *ids, int64_t *n_out);
+/* each particle's share of the energy of the last force calculation: half of each of its pair energies,
+ * its order-1 energies and the energies of the bonded terms it is listed first in; the shares sum to
+ * StateModel::energy() (CPUCalculateForces.cpp:46-212 sums the same terms); same order as rdc_get_particles */
+int rdc_get_particle_energies(rdc_system *s, int64_t capacity, double *energies, uint64_t *ids, int64_t *n_out);
 /* StateModel::virial() after the last CalculateForces (row-major 3x3): the sum over pairs of
  * outer(-x_ij, f_i) (CPUCalculateForces.cpp:247-249); zero unless the context records the virial */
 int rdc_get_virial(rdc_system *s, double *virial9);

@@ -95,6 +95,7 @@ def _sig(lib):
         "rdc_get_n_particles": (i, [vp, P(i64)]),
         "rdc_get_particles": (i, [vp, i64, P(d), P(i), P(u64), P(i64)]),
         "rdc_get_forces": (i, [vp, i64, P(d), P(u64), P(i64)]),
+        "rdc_get_particle_energies": (i, [vp, i64, P(d), P(u64), P(i64)]),
         "rdc_get_energy": (i, [vp, P(d)]),
         "rdc_count_types": (i, [vp, P(i64)]),
         "rdc_get_particle_steps": (i, [vp, P(u64)]),

@@ -2116,6 +2116,27 @@ int rdc_get_forces(rdc_system *s, int64_t cap, double *forces, uint64_t *ids, in
         if (k > cap) throw CapacityError("output capacity too small for the particles");
     });
 }
+int rdc_get_particle_energies(rdc_system *s, int64_t cap, double *energies, uint64_t *ids, int64_t *n_out) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        std::vector<float4> p, f;
+        std::vector<uint32_t> id;
+        fetch(s, p, id, &f);
+        int64_t k = 0;
+        for (size_t i = 0; i < p.size(); ++i) {
+            int t;
+            std::memcpy(&t, &p[i].w, 4);
+            if (t < 0) continue;
+            if (k < cap) {
+                if (energies) energies[k] = f[i].w;
+                if (ids) ids[k] = id[i];
+            }
+            ++k;
+        }
+        if (n_out) *n_out = k;
+        if (k > cap) throw CapacityError("output capacity too small for the particles");
+    });
+}
 int rdc_get_virial(rdc_system *s, double *virial9) {
     return guarded([&] {
         require(s && virial9, "null argument");

@@ -397,6 +397,15 @@ class CUDAKernel:
         N.check(self._lib.rdc_get_forces(self._h, n, _p(f, C.c_double), _p(ids, C.c_uint64), C.byref(got)))
         return f[:got.value], ids[:got.value]
 
+    def get_particle_energies(self):
+        """(energies[n], ids[n]): each particle's share of the last force calculation's energy."""
+        n = self.n_particles
+        e = np.zeros(n); ids = np.zeros(n, np.uint64)
+        got = C.c_int64()
+        N.check(self._lib.rdc_get_particle_energies(self._h, n, _p(e, C.c_double), _p(ids, C.c_uint64),
+                                                    C.byref(got)))
+        return e[:got.value], ids[:got.value]
+
     @property
     def energy(self) -> float:
         e = C.c_double()

@@ -64,6 +64,9 @@ def test_pair_potential_known_answers(rg, case):
     exp = np.array(ka.per_particle_forces(case))
     scale = max(np.abs(exp).max(), 1e-12)
     np.testing.assert_allclose(f, exp, rtol=0, atol=max(case["force_atol"], FORCE_RTOL * scale))
+    # the per-particle shares of the energy sum to it
+    pe, _ = k.get_particle_energies()
+    assert pe.sum() == pytest.approx(e, rel=1e-6, abs=1e-12)
 
 
 @pytest.mark.parametrize("case", ka.BONDED_CASES, ids=lambda c: c["name"])
