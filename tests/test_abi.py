@@ -89,3 +89,34 @@ def test_null_arguments_are_rejected_before_any_device_call():
             f.argtypes = [v] * nargs
         assert f(*args) == 1, name
         assert "null argument" in lib.rdc_last_error().decode()
+
+
+def test_topology_registries_validate_like_the_reference():
+    """Spatial topology reactions and flavors are checked without a device (SpatialTopologyReaction.h:88-91,
+    TopologyRegistry.cpp:238-242, ParticleTypeRegistry.h:58-63); their radius counts in the largest cutoff
+    (Context::calculateMaxCutoff)."""
+    import readdy_gb300 as rg
+    ctx = rg.Context((10, 10, 10), diffusion_constants=(1.0, 1.0, 1.0))
+    with pytest.raises(ValueError, match="flavor"):
+        ctx.set_particle_flavor(0, 7)
+    with pytest.raises(ValueError, match="rate"):
+        ctx.add_spatial_topology_reaction(ctx.TT_FUSION, (0, 0), (1, 0), (2, 1), (2, 1), 0.0, 1.0)
+    with pytest.raises(ValueError, match="radius"):
+        ctx.add_spatial_topology_reaction(ctx.TT_FUSION, (0, 0), (1, 0), (2, 1), (2, 1), 1.0, -1.0)
+    with pytest.raises(ValueError, match="mode"):
+        ctx.add_spatial_topology_reaction(9, (0, 0), (1, 0), (2, 1), (2, 1), 1.0, 1.0)
+    with pytest.raises(ValueError, match="topology_type2"):  # a topology-particle mode with two topologies
+        ctx.add_spatial_topology_reaction(ctx.TP_FUSION, (0, 0), (1, 0), (2, 1), (2, None), 1.0, 1.0)
+    with pytest.raises(ValueError, match="type out of range"):
+        ctx.add_spatial_topology_reaction(ctx.TT_FUSION, (0, 0), (5, 0), (2, 1), (2, 1), 1.0, 1.0)
+    assert ctx.add_spatial_topology_reaction(ctx.TP_FUSION, (0, 0), (1, None), (2, 0), (2, None), 1.0, 2.5) == 0
+    assert ctx.calculate_max_cutoff() == pytest.approx(2.5)
+    ctx.set_legacy_topology_self_fusion(True)
+
+
+def test_recipe_steps_reject_null_arguments():
+    from readdy_gb300 import _native
+    lib = _native.load()
+    assert lib.rdc_recipe_add_edge(None, 0, 1) == 1
+    assert lib.rdc_recipe_append_particle(None, 0, None, 0, None) == 1
+    assert lib.rdc_recipe_change_particle_position(None, 0, None) == 1
