@@ -7,8 +7,9 @@
 //
 // Two legs share the GPU:
 //  * requests of up to plain_threshold particles become replicas of the fused engine (rdc_engine.h):
-//    every engine step is one persistent launch over all of them, replayed from one CUDA graph, and
-//    requests join and leave between chunks of steps (continuous batching);
+//    every engine step is one persistent launch over all of them with as many CTAs as active requests
+//    (at most one per SM; the other SMs stay free for the per-system leg), replayed from a CUDA graph
+//    captured per grid size, and requests join and leave between chunks of steps (continuous batching);
 //  * larger requests run as plain per-system simulations (rdc_run: grid-wide kernels replayed from a
 //    CUDA graph), each on its own stream, taken by a fixed pool of host worker threads (at most that many
 //    run at once), because one CTA per replica would make their steps the longest of every engine launch.
@@ -149,7 +150,7 @@ struct rdc_server {
     uint64_t plain_particle_steps = 0;
     int threads = ENGINE_THREADS_MAX, blocks = 0;
     size_t smem = 0;
-    cudaGraphExec_t graph = nullptr;
+    std::map<int, cudaGraphExec_t> graphs;  // the engine step captured per grid size
 
     ~rdc_server() {
         {
@@ -162,7 +163,8 @@ struct rdc_server {
         if (stream) cudaStreamSynchronize(stream);
         for (auto &kv : requests)
             if (kv.second->block) cudaFreeAsync(kv.second->block, stream);
-        if (graph) cudaGraphExecDestroy(graph);
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
         cudaFree(desc_dev); cudaFree(state_dev); cudaFree(tabs_dev); cudaFree(order_dev);
         cudaFree(n_work_dev); cudaFree(work_dev); cudaFree(list_dev); cudaFree(particle_steps_dev);
         if (stream) {
@@ -214,12 +216,6 @@ struct rdc_server {
         e.particle_steps = particle_steps_dev;
         smem = engine_smem_bytes(e.max_events_sm);
         blocks = engine_grid(threads, smem);
-        cudaGraph_t g;
-        RDC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        launch_engine_step(e, blocks, threads, smem, stream);
-        RDC_CUDA(cudaStreamEndCapture(stream, &g));
-        RDC_CUDA(cudaGraphInstantiate(&graph, g, 0));
-        cudaGraphDestroy(g);
         RDC_CUDA(cudaStreamSynchronize(stream));
         for (int k = 0; k < plain_workers; ++k) workers.emplace_back([this] { worker_loop(); });
     }
@@ -381,6 +377,22 @@ struct rdc_server {
     }
 
     // work list: active engine requests, largest first
+    // the engine step (k_engine_step + k_engine_reset) with `nb` CTAs, captured once per grid size
+    cudaGraphExec_t graph_for(int nb) {
+        nb = std::max(nb, 1);
+        auto it = graphs.find(nb);
+        if (it != graphs.end()) return it->second;
+        cudaGraph_t g;
+        cudaGraphExec_t x = nullptr;
+        RDC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        launch_engine_step(e, nb, threads, smem, stream);
+        RDC_CUDA(cudaStreamEndCapture(stream, &g));
+        RDC_CUDA(cudaGraphInstantiate(&x, g, 0));
+        cudaGraphDestroy(g);
+        graphs[nb] = x;
+        return x;
+    }
+
     void set_order() {
         std::vector<int> ord;
         for (int k = 0; k < max_active; ++k)
@@ -413,7 +425,10 @@ struct rdc_server {
             int64_t K = max_steps;
             for (int64_t id : active) K = std::min(K, requests[id]->n_steps - requests[id]->steps_done);
             K = std::max<int64_t>(K, 1);
-            for (int64_t k = 0; k < K; ++k) RDC_CUDA(cudaGraphLaunch(graph, stream));
+            // as many persistent CTAs as active engine requests (one request takes one CTA at a time): the
+            // other SMs stay free for the per-system workers' kernels
+            cudaGraphExec_t step_graph = graph_for((int)std::min<size_t>((size_t)blocks, active.size()));
+            for (int64_t k = 0; k < K; ++k) RDC_CUDA(cudaGraphLaunch(step_graph, stream));
             std::vector<RepState> st(max_active);
             RDC_CUDA(cudaMemcpyAsync(st.data(), state_dev, sizeof(RepState) * max_active, cudaMemcpyDeviceToHost,
                                      stream));
