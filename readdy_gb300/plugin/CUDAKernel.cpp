@@ -5,6 +5,10 @@
 #include <readdy/model/potentials/PotentialsOrder1.h>
 #include <readdy/model/potentials/PotentialsOrder2.h>
 #include <readdy/model/reactions/Reaction.h>
+#include <readdy/model/topologies/reactions/Operations.h>
+#include <readdy/model/topologies/reactions/Recipe.h>
+#include <readdy/model/topologies/reactions/StructuralTopologyReaction.h>
+#include <readdy/model/topologies/reactions/TopologyReactionActionFactory.h>
 
 #include <algorithm>
 #include <cstdlib>
@@ -182,12 +186,6 @@ uint64_t seedFromEnvironment() {
     return ((uint64_t)rd() << 32) ^ rd();
 }
 
-std::vector<ParticleTypeId> typeIds(const model::Context &ctx, const std::vector<std::string> &names) {
-    std::vector<ParticleTypeId> ids;
-    for (const auto &n : names) ids.push_back(ctx.particleTypes().idOf(n));
-    return ids;
-}
-
 }  // namespace
 
 rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx) {
@@ -299,6 +297,7 @@ std::vector<model::Particle> CUDAStateModel::getParticles() const {
 
 // the particle whose device id is `index` (topology vertices hold device ids as their particle index)
 model::Particle CUDAStateModel::getParticleForIndex(std::size_t index) const {
+    if (const auto it = _view.find(index); it != _view.end()) return it->second;
     for (const auto &p : getParticles())
         if (p.id() == index) return p;
     throw std::out_of_range("CUDA kernel: no particle with index " + std::to_string(index));
@@ -397,6 +396,32 @@ void CUDAStateModel::reloadTopologies() {
     }
 }
 
+std::unique_ptr<model::top::GraphTopology> CUDAStateModel::deviceTopology(int64_t k) {
+    rdc_system *s = _kernel->sysIfCreated();
+    int type = 0;
+    int64_t nv = 0, ne = 0;
+    int st = rdc_get_topology(s, k, &type, 0, nullptr, nullptr, &nv, 0, nullptr, &ne);
+    if (st != RDC_OK && st != RDC_ERR_CAPACITY) check(st);
+    std::vector<uint64_t> ids(nv);
+    std::vector<int> types(nv);
+    std::vector<int64_t> edges(2 * ne);
+    std::vector<double> x(3 * nv);
+    check(rdc_get_topology(s, k, &type, nv, ids.data(), types.data(), &nv, ne, edges.data(), &ne));
+    check(rdc_get_topology_positions(s, k, nv, x.data()));
+    _view.clear();
+    model::top::Graph graph;
+    for (int64_t v = 0; v < nv; ++v) {
+        graph.addVertex(model::top::VertexData{(std::size_t)ids[v]});
+        _view.emplace((std::size_t)ids[v], model::Particle(Vec3(x[3 * v], x[3 * v + 1], x[3 * v + 2]),
+                                                           (ParticleTypeId)types[v], (ParticleId)ids[v]));
+    }
+    for (int64_t e = 0; e < ne; ++e)
+        graph.addEdge(graph.vertices().begin_persistent() + edges[2 * e],
+                      graph.vertices().begin_persistent() + edges[2 * e + 1]);
+    return std::make_unique<model::top::GraphTopology>((TopologyTypeId)type, std::move(graph), _kernel->context(),
+                                                       this);
+}
+
 std::vector<model::top::GraphTopology *> CUDAStateModel::getTopologies() {
     std::vector<model::top::GraphTopology *> out;
     for (auto &t : _topologies) out.push_back(t.get());
@@ -492,18 +517,19 @@ std::unique_ptr<act::reactions::Gillespie> CUDAActionFactory::gillespie(scalar d
 std::unique_ptr<act::reactions::DetailedBalance> CUDAActionFactory::detailedBalance(scalar) const {
     throw std::logic_error("CUDA kernel: the detailed-balance reaction handler is not supported");
 }
-// EvaluateTopologyReactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp): the spatial
-// reactions run through rdc_evaluate_topology_reactions, and the host topologies are read back when any
-// event was performed; structural reactions call user functions on the host graph and are not provided
+// EvaluateTopologyReactions (kernels/cpu/src/actions/CPUEvaluateTopologyReactions.cpp): spatial and
+// structural reactions run through rdc_evaluate_topology_reactions (the structural ones call back into the
+// registry's functions), and the host topologies are read back when any event was performed
 std::unique_ptr<act::top::EvaluateTopologyReactions> CUDAActionFactory::evaluateTopologyReactions(scalar dt) const {
     auto *k = _kernel;
     return std::make_unique<CallAction<act::top::EvaluateTopologyReactions, scalar>>([k, dt] {
-        if (k->context().topologyRegistry().nStructuralReactions() > 0)
-            throw std::logic_error("CUDA kernel: structural topology reactions are not supported");
-        if (k->context().topologyRegistry().spatialReactionRegistry().empty()) return;
+        const auto &reg = k->context().topologyRegistry();
+        if (reg.nStructuralReactions() == 0 && reg.spatialReactionRegistry().empty()) return;
         int64_t performed = 0;
-        check(rdc_evaluate_topology_reactions(k->sys(), dt, &performed));
-        if (performed > 0) k->cudaStateModel().reloadTopologies();
+        const int rc = rdc_evaluate_topology_reactions(k->sys(), dt, &performed);
+        if (rc == RDC_OK && performed > 0) k->cudaStateModel().reloadTopologies();
+        k->rethrowCallbackError();
+        check(rc);
     }, dt);
 }
 // BreakBonds (include/readdy/model/actions/Actions.h:213-290): the break configuration's pairs go to
@@ -753,8 +779,137 @@ void CUDAKernel::initialize() {
     if (_ctx) rdc_context_destroy(_ctx);
     _ctx = c;
     _sys = s;
+    registerStructuralReactions();
     if (!keep.empty()) _state.addParticles(keep);
     check(rdc_initialize(_sys));
+}
+
+namespace {
+
+namespace rop = model::top::reactions::op;
+namespace ract = model::top::reactions::actions;
+
+// A recipe's steps (Recipe.h) hand their data only to the action factory that Operation::create_action
+// (Operations.h) is given.  This factory passes each step on to the rdc_recipe being filled and returns an
+// action that does nothing; the library applies the steps to the device topology.
+class RecipeRecorder : public ract::TopologyReactionActionFactory {
+public:
+    RecipeRecorder(rdc_recipe *recipe, const model::Context &ctx) : _r(recipe), _ctx(ctx) {}
+
+    ActionPtr createChangeParticleType(model::top::GraphTopology *top, const model::top::Graph::PersistentVertexIndex &v,
+                                       const ParticleTypeId &type_to) const override {
+        check(rdc_recipe_change_particle_type(_r, (int64_t)v.value, (int)type_to));
+        return done(top);
+    }
+    ActionPtr createChangeParticlePosition(model::top::GraphTopology *top,
+                                           const model::top::Graph::PersistentVertexIndex &v, Vec3 pos) const override {
+        const double x[3] = {pos[0], pos[1], pos[2]};
+        check(rdc_recipe_change_particle_position(_r, (int64_t)v.value, x));
+        return done(top);
+    }
+    ActionPtr createAppendParticle(model::top::GraphTopology *top,
+                                   const std::vector<model::top::Graph::PersistentVertexIndex> &neighbors,
+                                   ParticleTypeId type, const Vec3 &pos) const override {
+        std::vector<int64_t> nb;
+        for (const auto &v : neighbors) nb.push_back((int64_t)v.value);
+        const double x[3] = {pos[0], pos[1], pos[2]};
+        check(rdc_recipe_append_particle(_r, (int64_t)nb.size(), nb.data(), (int)type, x));
+        return done(top);
+    }
+    ActionPtr createChangeTopologyType(model::top::GraphTopology *top, const std::string &type_to) const override {
+        check(rdc_recipe_change_topology_type(_r, (int)_ctx.topologyRegistry().idOf(type_to)));
+        return done(top);
+    }
+
+private:
+    struct Done : ract::TopologyReactionAction {
+        using ract::TopologyReactionAction::TopologyReactionAction;
+        void execute() override {}
+    };
+    static ActionPtr done(model::top::GraphTopology *top) { return std::make_unique<Done>(top); }
+    rdc_recipe *_r;
+    const model::Context &_ctx;
+};
+
+// op::AddEdge and op::RemoveEdge keep their edge private and pass it only to the factory's non-virtual
+// createAddEdge/createRemoveEdge.  Access is not checked for the names in an explicit instantiation
+// ([temp.spec.general]), so the two instantiations below form pointers to those members.
+template <typename Tag, typename Tag::type M>
+struct MemberOf {
+    friend typename Tag::type member(Tag) { return M; }
+};
+struct AddEdgeMember {
+    using type = model::top::Graph::Edge rop::AddEdge::*;
+    friend type member(AddEdgeMember);
+};
+struct RemoveEdgeMember {
+    using type = model::top::Graph::Edge rop::RemoveEdge::*;
+    friend type member(RemoveEdgeMember);
+};
+template struct MemberOf<AddEdgeMember, &rop::AddEdge::_edge>;
+template struct MemberOf<RemoveEdgeMember, &rop::RemoveEdge::_edge>;
+
+// rdc_topology_rate_fn: StructuralTopologyReaction::rate on the device topology k
+double structuralRate(void *user, rdc_system *, int64_t k) {
+    auto *b = static_cast<CUDAKernel::StructuralBinding *>(user);
+    auto &state = b->kernel->cudaStateModel();
+    double rate = 0;
+    try {
+        const auto top = state.deviceTopology(k);
+        rate = b->reaction->rate(*top);
+    } catch (...) {
+        b->kernel->keepCallbackError(std::current_exception());
+    }
+    state.clearTopologyView();
+    return rate;
+}
+
+// rdc_topology_recipe_fn: StructuralTopologyReaction::operations on the device topology k, its steps in
+// order into the rdc_recipe (vertex v of a step is local vertex v of rdc_get_topology)
+void structuralRecipe(void *user, rdc_system *, int64_t k, rdc_recipe *recipe) {
+    auto *b = static_cast<CUDAKernel::StructuralBinding *>(user);
+    auto &state = b->kernel->cudaStateModel();
+    try {
+        auto top = state.deviceTopology(k);
+        const auto steps = b->reaction->operations(*top);
+        const RecipeRecorder rec(recipe, b->kernel->context());
+        for (const auto &op : steps.steps()) {
+            if (const auto *a = dynamic_cast<const rop::AddEdge *>(op.get())) {
+                const auto &e = a->*member(AddEdgeMember{});
+                check(rdc_recipe_add_edge(recipe, (int64_t)std::get<0>(e).value, (int64_t)std::get<1>(e).value));
+            } else if (const auto *r = dynamic_cast<const rop::RemoveEdge *>(op.get())) {
+                const auto &e = r->*member(RemoveEdgeMember{});
+                check(rdc_recipe_remove_edge(recipe, (int64_t)std::get<0>(e).value, (int64_t)std::get<1>(e).value));
+            } else {
+                op->create_action(top.get(), &rec);
+            }
+        }
+    } catch (...) {
+        b->kernel->keepCallbackError(std::current_exception());
+    }
+    state.clearTopologyView();
+}
+
+}  // namespace
+
+// every structural reaction of the topology registry (TopologyRegistry.h:91-113), with its mode
+// (StructuralTopologyReaction.h: expect connected or create children)
+void CUDAKernel::registerStructuralReactions() {
+    _structural.clear();
+    for (const auto &tt : context().topologyRegistry().types())
+        for (const auto &r : tt.structuralReactions) {
+            _structural.push_back(std::make_unique<StructuralBinding>(StructuralBinding{this, &r}));
+            check(rdc_add_structural_topology_reaction(_sys, (int)tt.type, structuralRate, structuralRecipe,
+                                                       _structural.back().get(),
+                                                       r.expects_connected_after_reaction() ? 1 : 0, nullptr));
+        }
+}
+
+void CUDAKernel::rethrowCallbackError() {
+    if (!_callbackError) return;
+    std::exception_ptr e;
+    std::swap(e, _callbackError);
+    std::rethrow_exception(e);
 }
 
 rdc_system *CUDAKernel::sys() {

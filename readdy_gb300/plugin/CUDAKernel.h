@@ -13,8 +13,10 @@
 #include <readdy/model/topologies/GraphTopology.h>
 #include <readdy_cuda.h>
 
+#include <exception>
 #include <memory>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 namespace readdy::kernel::cuda {
@@ -58,6 +60,11 @@ public:
     void flushTopologies();
     // rebuilds the host topologies from the device's
     void reloadTopologies();
+    // topology k of the device (rdc_get_topologies order) as a host GraphTopology for a structural reaction's
+    // functions: local vertex v has persistent index v and holds the device id; until the next call,
+    // getParticleForIndex serves its particles without reading the whole system back
+    std::unique_ptr<model::top::GraphTopology> deviceTopology(int64_t k);
+    void clearTopologyView() { _view.clear(); }
 
 private:
     struct PendingTopology {
@@ -67,6 +74,7 @@ private:
     CUDAKernel *_kernel;
     std::vector<PendingTopology> _pending;
     std::vector<std::unique_ptr<model::top::GraphTopology>> _topologies;
+    std::unordered_map<std::size_t, model::Particle> _view;  // particles of the last deviceTopology
     mutable scalar _energy = 0;
     scalar _time = 0;
 };
@@ -133,7 +141,7 @@ public:
     model::actions::ActionFactory &actions() override { return _actions; }
     const model::observables::ObservableFactory &observe() const override { return _observables; }
     model::observables::ObservableFactory &observe() override { return _observables; }
-    // topology reactions are not provided; static topologies (bonds, angles, dihedrals) and BreakBonds are
+    // topology reactions and BreakBonds run in the C ABI (no per-operation actions are created)
     const model::top::TopologyActionFactory *const getTopologyActionFactory() const override { return nullptr; }
     model::top::TopologyActionFactory *const getTopologyActionFactory() override { return nullptr; }
     void initialize() override;
@@ -147,10 +155,26 @@ public:
     // reference reaction id -> device reaction id (-1: not registered on the device)
     const std::vector<int> &reactionIds() const { return _rx; }
 
+    // A structural topology reaction of the registry, registered with rdc_add_structural_topology_reaction;
+    // its rate and reaction functions run on a host GraphTopology of the device topology.  An exception they
+    // throw cannot cross the C ABI: the first one is kept and rethrown when the library call returns.
+    struct StructuralBinding {
+        CUDAKernel *kernel;
+        const model::top::reactions::StructuralTopologyReaction *reaction;
+    };
+    void keepCallbackError(std::exception_ptr e) {
+        if (!_callbackError) _callbackError = std::move(e);
+    }
+    void rethrowCallbackError();
+
 private:
+    void registerStructuralReactions();
+
     rdc_context *_ctx = nullptr;
     rdc_system *_sys = nullptr;
     std::vector<int> _rx;
+    std::vector<std::unique_ptr<StructuralBinding>> _structural;
+    std::exception_ptr _callbackError;
     CUDAStateModel _state;
     CUDAActionFactory _actions;
     CUDAObservableFactory _observables;
