@@ -856,7 +856,7 @@ double structuralRate(void *user, rdc_system *, int64_t k) {
     double rate = 0;
     try {
         const auto top = state.deviceTopology(k);
-        rate = b->reaction->rate(*top);
+        rate = b->reaction.rate(*top);
     } catch (...) {
         b->kernel->keepCallbackError(std::current_exception());
     }
@@ -871,7 +871,7 @@ void structuralRecipe(void *user, rdc_system *, int64_t k, rdc_recipe *recipe) {
     auto &state = b->kernel->cudaStateModel();
     try {
         auto top = state.deviceTopology(k);
-        const auto steps = b->reaction->operations(*top);
+        const auto steps = b->reaction.operations(*top);
         const RecipeRecorder rec(recipe, b->kernel->context());
         for (const auto &op : steps.steps()) {
             if (const auto *a = dynamic_cast<const rop::AddEdge *>(op.get())) {
@@ -898,7 +898,7 @@ void CUDAKernel::registerStructuralReactions() {
     _structural.clear();
     for (const auto &tt : context().topologyRegistry().types())
         for (const auto &r : tt.structuralReactions) {
-            _structural.push_back(std::make_unique<StructuralBinding>(StructuralBinding{this, &r}));
+            _structural.push_back(std::make_unique<StructuralBinding>(StructuralBinding{this, r}));
             check(rdc_add_structural_topology_reaction(_sys, (int)tt.type, structuralRate, structuralRecipe,
                                                        _structural.back().get(),
                                                        r.expects_connected_after_reaction() ? 1 : 0, nullptr));

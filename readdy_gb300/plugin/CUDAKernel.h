@@ -155,12 +155,13 @@ public:
     // reference reaction id -> device reaction id (-1: not registered on the device)
     const std::vector<int> &reactionIds() const { return _rx; }
 
-    // A structural topology reaction of the registry, registered with rdc_add_structural_topology_reaction;
+    // A structural topology reaction of the registry (a copy, so that later changes of the registry leave
+    // the registered system's functions in place), registered with rdc_add_structural_topology_reaction;
     // its rate and reaction functions run on a host GraphTopology of the device topology.  An exception they
     // throw cannot cross the C ABI: the first one is kept and rethrown when the library call returns.
     struct StructuralBinding {
         CUDAKernel *kernel;
-        const model::top::reactions::StructuralTopologyReaction *reaction;
+        model::top::reactions::StructuralTopologyReaction reaction;
     };
     void keepCallbackError(std::exception_ptr e) {
         if (!_callbackError) _callbackError = std::move(e);
