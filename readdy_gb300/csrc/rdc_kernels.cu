@@ -271,6 +271,13 @@ __global__ void __launch_bounds__(FORCE_THREADS, 3) k_pair_forces(SysDev s) {
             if (threadIdx.x == 0) s.vpart[9 * blockIdx.x + k] = v;
         }
     }
+    // the final sums read FORCE_BLOCKS partials: those of the blocks this launch has not are zero
+    if (blockIdx.x == 0)
+        for (int k = gridDim.x + threadIdx.x; k < FORCE_BLOCKS; k += blockDim.x) {
+            s.epart[k] = 0.0;
+            if (VIRIAL)
+                for (int c = 0; c < 9; ++c) s.vpart[9 * k + c] = 0.0;
+        }
 }
 
 // virial of the last force calculation: block partials summed in a fixed order
@@ -643,9 +650,16 @@ void init_kernel_attributes() {
                                   (int)resolve_smem_bytes()));
 }
 
+// Blocks of a grid-stride launch over `items` particles or cells: one item per thread, at most `cap`
+// blocks.  A small system's kernels then start and drain sooner, and leave the SMs to kernels of other
+// systems on other streams (the served form runs several per-system requests at once).  Particle
+// launches are sized by the capacity, which bounds the particles of every step a graph replays.
+inline int blocks_for(int items, int cap) { return std::max(1, std::min(cap, (items + 255) / 256)); }
+inline int particle_blocks(const SysDev &s) { return blocks_for(s.capacity, GRID_BLOCKS); }
+
 void launch_integrate_bin(const SysDev &s, bool integrate, cudaStream_t st) {
     RDC_CUDA(cudaMemsetAsync(s.cnt, 0, sizeof(int) * (s.geo.ncells + 2), st));
-    k_integrate_bin<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, integrate ? 1 : 0, 1);
+    k_integrate_bin<<<particle_blocks(s), GRID_THREADS, 0, st>>>(s, integrate ? 1 : 0, 1);
 }
 
 void launch_bin(const SysDev &s, cudaStream_t st) { launch_integrate_bin(s, false, st); }
@@ -653,10 +667,10 @@ void launch_bin(const SysDev &s, cudaStream_t st) { launch_integrate_bin(s, fals
 void launch_sort(const SysDev &s, bool permute_force, cudaStream_t st) {
     const int nb = s.geo.ncells + 2;
     launch_scan(s.cnt, s.start, s.scan_blocks, nb, st);
-    k_scatter<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
-    k_cell_order<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
+    k_scatter<<<particle_blocks(s), GRID_THREADS, 0, st>>>(s);
+    k_cell_order<<<blocks_for(s.geo.ncells, GRID_BLOCKS), GRID_THREADS, 0, st>>>(s);
     k_big_cell_order<<<152, 512, 0, st>>>(s);
-    k_gather<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, permute_force ? 1 : 0);
+    k_gather<<<particle_blocks(s), GRID_THREADS, 0, st>>>(s, permute_force ? 1 : 0);
 }
 
 void launch_force_finals(const SysDev &s, bool bonded, cudaStream_t st) {
@@ -665,8 +679,9 @@ void launch_force_finals(const SysDev &s, bool bonded, cudaStream_t st) {
 }
 
 void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st, bool finals) {
-    if (s.virial) k_pair_forces<true><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
-    else k_pair_forces<false><<<FORCE_BLOCKS, FORCE_THREADS, 0, st>>>(s);
+    const int fb = blocks_for(s.capacity, FORCE_BLOCKS);
+    if (s.virial) k_pair_forces<true><<<fb, FORCE_THREADS, 0, st>>>(s);
+    else k_pair_forces<false><<<fb, FORCE_THREADS, 0, st>>>(s);
     if (bonded && s.n_top > 0) {
         k_bonded_terms<<<BONDED_BLOCKS, 256, 0, st>>>(s);
         k_bonded_gather<<<BONDED_BLOCKS, 256, 0, st>>>(s);
@@ -676,7 +691,7 @@ void launch_forces(const SysDev &s, bool pair, bool bonded, cudaStream_t st, boo
 }
 
 void launch_events(const SysDev &s, int handler, cudaStream_t st) {
-    k_events<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s, handler);
+    k_events<<<particle_blocks(s), GRID_THREADS, 0, st>>>(s, handler);
 }
 
 void launch_resolve_apply(const SysDev &s, int handler, cudaStream_t st) {
@@ -817,7 +832,7 @@ void launch_count_types(const SysDev &s, unsigned long long *out, cudaStream_t s
 }
 
 void launch_record_counts(const SysDev &s, cudaStream_t st) {
-    k_record_counts<<<GRID_BLOCKS, GRID_THREADS, 0, st>>>(s);
+    k_record_counts<<<particle_blocks(s), GRID_THREADS, 0, st>>>(s);
 }
 
 void launch_pairs(const SysDev &s, float c2f, float band, double c2, uint64_t *out, int cap, int *n_out,
