@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--single-systems", type=int, default=1, help="time the three single-system workloads (0: skip)")
     ap.add_argument("--plain-threshold", type=int, default=4096,
                     help="requests above this many particles take the per-system leg of the server")
-    ap.add_argument("--plain-workers", type=int, default=8,
+    ap.add_argument("--plain-workers", type=int, default=24,
                     help="per-system requests the server runs at once, each on its own stream")
     ap.add_argument("--profile-system", choices=["abc_2k", "crowded_200k", "polymer_200k"], default=None,
                     help="only run one single-system workload through the per-system path (--warmup then "
@@ -391,7 +391,7 @@ def profile_system(name, warmup, steps):
     return {"profile_system": name, "particles": int(n), "steps": steps, "ms_per_step": dt * 1e3}
 
 
-def serving(n_requests, time_limit, plain_threshold, seed=7, plain_workers=8):
+def serving(n_requests, time_limit, plain_threshold, seed=7, plain_workers=24):
     """The served form on the first n_requests of the seeded serving stream (Poisson arrivals at 20/s;
     2-6 species; N log-uniform in [500, 200000] at density 0.1-0.5; 1k-100k steps; counts every 100
     steps), replayed in wall-clock time against a 150 GB device-memory budget."""

@@ -375,7 +375,7 @@ int rdc_batch_synchronize(rdc_batch *b);
 typedef struct rdc_server rdc_server;
 int rdc_server_create(rdc_server **out, uint64_t budget_bytes, int max_active, int handler, int64_t plain_threshold);
 int rdc_server_destroy(rdc_server *s);
-/* how many per-system requests run at once, each on its own stream and pool thread (default 8) */
+/* how many per-system requests run at once, each on its own stream and pool thread (default 24) */
 int rdc_server_set_plain_workers(rdc_server *s, int n);
 /* device bytes a request would hold while active, and whether it would take the per-system leg
  * (host arithmetic only, no device needed) */

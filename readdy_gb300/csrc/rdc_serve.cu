@@ -134,7 +134,7 @@ struct rdc_server {
     std::vector<int64_t> plain_running;
     std::vector<int64_t> unpolled;
     // worker pool of the per-system leg: admitted requests wait in plain_queue for a worker
-    int plain_workers = 8;
+    int plain_workers = 24;
     std::vector<std::thread> workers;
     std::deque<Request *> plain_queue;
     std::mutex plain_mutex;
