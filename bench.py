@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=200, help="requests of the served-stream sample (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=120.0, help="wall-time limit of the served-stream sample")
     ap.add_argument("--single-systems", type=int, default=1, help="time the three single-system workloads (0: skip)")
-    ap.add_argument("--plain-threshold", type=int, default=4096,
+    ap.add_argument("--plain-threshold", type=int, default=32768,
                     help="requests above this many particles take the per-system leg of the server")
     ap.add_argument("--plain-workers", type=int, default=24,
                     help="per-system requests the server runs at once, each on its own stream")

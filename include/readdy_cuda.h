@@ -385,8 +385,9 @@ int rdc_server_request_bytes(const rdc_context *ctx, int64_t n, int64_t n_steps,
  * the whole budget returns RDC_ERR_INVALID_ARGUMENT. */
 int rdc_server_submit(rdc_server *s, const rdc_context *ctx, int64_t n, const double *positions3, const int *types,
                       int64_t n_steps, double dt, int64_t count_stride, uint64_t seed, int64_t *request_id);
-/* admit what fits, advance the engine requests by up to max_steps (fewer when one of them finishes
- * first), retire finished requests of both legs */
+/* admit what fits, advance the engine requests by up to max_steps engine launches (fewer when one of them
+ * finishes first; in one launch a request takes as many steps as fit into one step of the largest active
+ * engine request), retire finished requests of both legs */
 int rdc_server_progress(rdc_server *s, int64_t max_steps, int64_t *n_finished);
 /* ids of requests finished since the last poll */
 int rdc_server_poll(rdc_server *s, int64_t capacity, int64_t *ids, int64_t *n_out);

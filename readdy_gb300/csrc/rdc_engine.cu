@@ -846,8 +846,20 @@ __global__ void __launch_bounds__(ENGINE_THREADS_MAX, 1) k_engine_step(EngineDev
             if (threadIdx.x == 0) sh_table = D.table;
         }
         __syncthreads();
-        if (D.smem_cells) replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, S.cells);
-        else replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, D.start);
+        const int m = E.launch_steps ? max(1, E.launch_steps[r]) : 1;
+        for (int k = 0;;) {
+            if (D.smem_cells) replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, S.cells);
+            else replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, D.start);
+            if (++k >= m) break;
+            // the replica's next step: its state as the body stored it (the body ended at a barrier)
+            if (threadIdx.x == 0) {
+                st = E.state[r];
+                sh_nev = 0;
+                sh_status = 0;
+            }
+            __syncthreads();
+            if (st.step >= D.n_steps || st.status != 0) break;
+        }
     }
 }
 

@@ -89,6 +89,9 @@ struct EngineDev {
     int handler;
     int max_events_sm;  // events one replica step resolves in shared memory
     unsigned long long *particle_steps;  // particles advanced, summed over replicas and steps
+    // steps each replica takes per launch, one after the other on its CTA (null: one).  The served form
+    // gives small requests more, so that a launch's length is not the largest request's step for all.
+    const int *launch_steps;
 };
 
 // decides the cell grid of a replica: cells at least cutoff * cell_scale wide, widened until the

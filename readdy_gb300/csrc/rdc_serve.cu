@@ -7,12 +7,14 @@
 //
 // Two legs share the GPU:
 //  * requests of up to plain_threshold particles become replicas of the fused engine (rdc_engine.h):
-//    every engine step is one persistent launch over all of them with as many CTAs as active requests
+//    each engine launch is one persistent kernel over all of them with as many CTAs as active requests
 //    (at most one per SM; the other SMs stay free for the per-system leg), replayed from a CUDA graph
-//    captured per grid size, and requests join and leave between chunks of steps (continuous batching);
+//    captured per grid size, and requests join and leave between chunks of launches (continuous
+//    batching).  In one launch a request takes as many steps as fit into one step of the largest active
+//    request, so small requests are not held to the large ones' pace;
 //  * larger requests run as plain per-system simulations (rdc_run: grid-wide kernels replayed from a
 //    CUDA graph), each on its own stream, taken by a fixed pool of host worker threads (at most that many
-//    run at once), because one CTA per replica would make their steps the longest of every engine launch.
+//    run at once): on one CTA their steps would take too long for their own latency.
 // A request's random streams are keyed by its own seed, particle ids and step counter, and its cell grid
 // by its own box, so its result does not depend on which other requests share the GPU.
 #include <cuda_runtime.h>
@@ -78,6 +80,11 @@ size_t plain_bytes(int64_t cap, int64_t ncells, int max_records, int ntypes) {
 double now_s(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
+
+// The cost of one engine step of a replica on its CTA, measured: about 20 us plus 0.027 us per particle,
+// i.e. the fixed part is worth about 740 particles.
+constexpr double ENGINE_FIXED_PARTICLES = 740.0;
+constexpr int ENGINE_MAX_LAUNCH_STEPS = 64;
 
 // particle capacity of a request: reactions may add particles (fission, two-product conversions), so
 // room for a quarter more plus a margin; a request that outgrows it ends with RDC_ERR_CAPACITY status
@@ -146,6 +153,8 @@ struct rdc_server {
     RepState *state_dev = nullptr;
     Tables *tabs_dev = nullptr;
     int *order_dev = nullptr, *n_work_dev = nullptr, *work_dev = nullptr, *list_dev = nullptr;
+    int *launch_steps_dev = nullptr;    // steps per launch of each engine slot
+    std::vector<int> launch_steps;      // the same on the host
     unsigned long long *particle_steps_dev = nullptr;
     uint64_t plain_particle_steps = 0;
     int threads = ENGINE_THREADS_MAX, blocks = 0;
@@ -167,6 +176,7 @@ struct rdc_server {
         graphs.clear();
         cudaFree(desc_dev); cudaFree(state_dev); cudaFree(tabs_dev); cudaFree(order_dev);
         cudaFree(n_work_dev); cudaFree(work_dev); cudaFree(list_dev); cudaFree(particle_steps_dev);
+        cudaFree(launch_steps_dev);
         if (stream) {
             cudaStreamSynchronize(stream);
             cudaStreamDestroy(stream);
@@ -197,6 +207,10 @@ struct rdc_server {
         tabs_dev = dalloc<Tables>(max_active);
         order_dev = dalloc<int>(max_active);
         list_dev = dalloc<int>(max_active);
+        launch_steps_dev = dalloc<int>(max_active);
+        launch_steps.assign(max_active, 1);
+        RDC_CUDA(cudaMemcpyAsync(launch_steps_dev, launch_steps.data(), sizeof(int) * max_active,
+                                 cudaMemcpyHostToDevice, stream));
         n_work_dev = dalloc<int>(1);
         work_dev = dalloc<int>(1);
         particle_steps_dev = dalloc<unsigned long long>(1);
@@ -214,6 +228,7 @@ struct rdc_server {
         e.handler = handler;
         e.max_events_sm = ENGINE_MAX_EVENTS_SM;
         e.particle_steps = particle_steps_dev;
+        e.launch_steps = launch_steps_dev;
         smem = engine_smem_bytes(e.max_events_sm);
         blocks = engine_grid(threads, smem);
         RDC_CUDA(cudaStreamSynchronize(stream));
@@ -393,6 +408,9 @@ struct rdc_server {
         return x;
     }
 
+    // Steps per launch: a request takes as many steps as fit into one step of the largest active request
+    // (by the cost model above), so that every request advances at the pace its own size allows and the
+    // launches stay about one large step long.
     void set_order() {
         std::vector<int> ord;
         for (int k = 0; k < max_active; ++k)
@@ -400,8 +418,16 @@ struct rdc_server {
         std::stable_sort(ord.begin(), ord.end(),
                          [&](int a, int b) { return requests[slot_owner[a]]->n > requests[slot_owner[b]]->n; });
         const int nw = (int)ord.size();
-        if (nw > 0)
+        if (nw > 0) {
+            const double big = ENGINE_FIXED_PARTICLES + (double)requests[slot_owner[ord[0]]]->n;
+            for (int k : ord) {
+                const double own = ENGINE_FIXED_PARTICLES + (double)requests[slot_owner[k]]->n;
+                launch_steps[k] = std::max(1, std::min(ENGINE_MAX_LAUNCH_STEPS, (int)(big / own)));
+            }
+            RDC_CUDA(cudaMemcpyAsync(launch_steps_dev, launch_steps.data(), sizeof(int) * max_active,
+                                     cudaMemcpyHostToDevice, stream));
             RDC_CUDA(cudaMemcpyAsync(order_dev, ord.data(), sizeof(int) * nw, cudaMemcpyHostToDevice, stream));
+        }
         RDC_CUDA(cudaMemcpyAsync(n_work_dev, &nw, sizeof(int), cudaMemcpyHostToDevice, stream));
         RDC_CUDA(cudaStreamSynchronize(stream));
     }
@@ -413,7 +439,7 @@ struct rdc_server {
         unpolled.push_back(q.id);
     }
 
-    // advance the engine requests by up to max_steps (stopping early when one of them finishes),
+    // advance the engine requests by up to max_steps launches (stopping early when one of them finishes),
     // retire finished requests of both legs; returns the requests finished by this call
     int64_t progress(int64_t max_steps) {
         admit();
@@ -422,8 +448,13 @@ struct rdc_server {
         for (int k = 0; k < max_active; ++k)
             if (slot_owner[k]) active.push_back(slot_owner[k]);
         if (!active.empty()) {
+            // launches until the first request finishes (each launch takes a request launch_steps steps)
             int64_t K = max_steps;
-            for (int64_t id : active) K = std::min(K, requests[id]->n_steps - requests[id]->steps_done);
+            for (int64_t id : active) {
+                const Request &q = *requests[id];
+                const int64_t m = launch_steps[q.slot];
+                K = std::min(K, (q.n_steps - q.steps_done + m - 1) / m);
+            }
             K = std::max<int64_t>(K, 1);
             // as many persistent CTAs as active engine requests (one request takes one CTA at a time): the
             // other SMs stay free for the per-system workers' kernels

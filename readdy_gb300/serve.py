@@ -27,7 +27,7 @@ def _p(a, t):
 
 class Server:
     def __init__(self, budget_bytes: int, max_active: int = 1024, handler: int = N.GILLESPIE,
-                 plain_threshold: int = 4096, plain_workers: int = 24):
+                 plain_threshold: int = 32768, plain_workers: int = 24):
         self._lib = N.load()
         h = C.c_void_p()
         N.check(self._lib.rdc_server_create(C.byref(h), int(budget_bytes), int(max_active), int(handler),
@@ -47,7 +47,7 @@ class Server:
             self._h = None
 
     @staticmethod
-    def request_bytes(context: Context, n: int, n_steps: int, count_stride: int, plain_threshold: int = 4096):
+    def request_bytes(context: Context, n: int, n_steps: int, count_stride: int, plain_threshold: int = 32768):
         """(device bytes, takes the per-system leg) of a request; host arithmetic only."""
         lib = N.load()
         b = C.c_uint64()

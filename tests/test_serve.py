@@ -131,3 +131,32 @@ def test_records_stream_while_requests_run(rg):
     k.add_particles(specs[1].positions, specs[1].types)
     ref = k.run(specs[1].n_steps, specs[1].dt, handler=rg.GILLESPIE, count_stride=specs[1].count_stride)
     np.testing.assert_array_equal(done[ids[1]]["counts"], ref)
+
+
+def test_small_engine_requests_take_more_steps_per_launch(rg):
+    """In one engine launch a request takes as many steps as fit into one step of the largest active engine
+    request, by the cost model of a replica-step (a fixed part worth 740 particles plus its particles):
+    after one launch a 200-particle request beside a 6000-particle one has taken (740 + 6000) // (740 + 200)
+    = 7 steps, the large one 1; both end with their results alone."""
+    from readdy_gb300.serve import Server, RequestSpec
+    rng = np.random.default_rng(8)
+    specs = []
+    for n in (6000, 200):
+        L = float(np.float32((n / 0.3) ** (1 / 3)))
+        specs.append(RequestSpec(arrival=0.0, n_types=2, diffusion=[1.0, 0.5], box=L,
+                                 reactions=[("conversion", (0, 1, 0.5)), ("conversion", (1, 0, 0.5))],
+                                 positions=(rng.random((n, 3)) - 0.5) * L, types=np.zeros(n, np.int32),
+                                 n_steps=40, seed=int(rng.integers(1 << 40)), count_stride=1, mass=[1, 1]))
+    srv = Server(1 << 32, plain_threshold=1 << 30)
+    ids = [srv.submit(s.context(), s.positions, s.types, s.n_steps, s.dt, s.count_stride, s.seed) for s in specs]
+    srv.progress(1)
+    assert len(srv.peek_records(ids[0])) == 1 + 1
+    assert len(srv.peek_records(ids[1])) == 1 + 7
+    done = {}
+    while len(done) < 2:
+        srv.progress(64)
+        for rid in srv.poll():
+            done[rid] = srv.result(rid)
+    for rid, s in zip(ids, specs):
+        alone, _ = run_all([s])
+        np.testing.assert_array_equal(done[rid]["counts"], alone[0]["counts"])
