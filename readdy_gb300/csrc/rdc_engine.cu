@@ -806,6 +806,10 @@ __device__ inline RxnTables stage_tables(const Tables *tab, const SmemLayout &S,
     return stage_rxn_tables(tab, rt_ints, rt_screen, rt_rx);
 }
 
+// MULTI: replicas may take several steps per launch (E.launch_steps).  A separate instantiation, so that
+// the batched form, which always takes one, keeps the register allocation of the single step (the loop
+// cost it 5 %).
+template <bool MULTI>
 __global__ void __launch_bounds__(ENGINE_THREADS_MAX, 1) k_engine_step(EngineDev E) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int sh_r, sh_table, sh_nev, sh_status;
@@ -846,19 +850,24 @@ __global__ void __launch_bounds__(ENGINE_THREADS_MAX, 1) k_engine_step(EngineDev
             if (threadIdx.x == 0) sh_table = D.table;
         }
         __syncthreads();
-        const int m = E.launch_steps ? max(1, E.launch_steps[r]) : 1;
-        for (int k = 0;;) {
+        if constexpr (!MULTI) {
             if (D.smem_cells) replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, S.cells);
             else replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, D.start);
-            if (++k >= m) break;
-            // the replica's next step: its state as the body stored it (the body ended at a barrier)
-            if (threadIdx.x == 0) {
-                st = E.state[r];
-                sh_nev = 0;
-                sh_status = 0;
+        } else {
+            const int m = max(1, E.launch_steps[r]);
+            for (int k = 0;;) {
+                if (D.smem_cells) replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, S.cells);
+                else replica_body(E, r, S, rt, tab, D, st, sh_nev, sh_status, D.start);
+                if (++k >= m) break;
+                // the replica's next step: its state as the body stored it (the body ended at a barrier)
+                if (threadIdx.x == 0) {
+                    st = E.state[r];
+                    sh_nev = 0;
+                    sh_status = 0;
+                }
+                __syncthreads();
+                if (st.step >= D.n_steps || st.status != 0) break;
             }
-            __syncthreads();
-            if (st.step >= D.n_steps || st.status != 0) break;
         }
     }
 }
@@ -1060,7 +1069,8 @@ int sm_count() {
 }
 
 int engine_grid(int threads, size_t smem) {
-    RDC_CUDA(cudaFuncSetAttribute(k_engine_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RDC_CUDA(cudaFuncSetAttribute(k_engine_step<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    RDC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, sms = 0, smem_sm = 0;
     RDC_CUDA(cudaGetDevice(&dev));
     RDC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1068,17 +1078,19 @@ int engine_grid(int threads, size_t smem) {
     // Ask for just the shared memory one CTA needs: the rest of the SM's unified L1/shared array stays
     // L1, which caches the neighbour positions of the candidate walks (a 100 % carveout leaves 28 KB).
     cudaFuncAttributes fa{};
-    RDC_CUDA(cudaFuncGetAttributes(&fa, k_engine_step));
+    RDC_CUDA(cudaFuncGetAttributes(&fa, k_engine_step<false>));
     const size_t need = smem + fa.sharedSizeBytes + 1024;  // + the per-CTA reservation
     const int carveout = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / std::max(smem_sm, 1));
-    RDC_CUDA(cudaFuncSetAttribute(k_engine_step, cudaFuncAttributePreferredSharedMemoryCarveout, carveout));
+    RDC_CUDA(cudaFuncSetAttribute(k_engine_step<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout));
+    RDC_CUDA(cudaFuncSetAttribute(k_engine_step<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout));
     int per_sm = 0;
-    RDC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_step, threads, smem));
+    RDC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_step<false>, threads, smem));
     return std::max(1, per_sm) * sms;
 }
 
 void launch_engine_step(const EngineDev &E, int blocks, int threads, size_t smem, cudaStream_t st) {
-    k_engine_step<<<blocks, threads, smem, st>>>(E);
+    if (E.launch_steps) k_engine_step<true><<<blocks, threads, smem, st>>>(E);
+    else k_engine_step<false><<<blocks, threads, smem, st>>>(E);
     k_engine_reset<<<1, 1, 0, st>>>(E);
 }
 
