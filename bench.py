@@ -184,8 +184,9 @@ def reference_cpu(ns, boxes, pos, types, seed, steps, warmup, budget_s=60.0):
     the reference's own pthread CPU kernel (kernels/cpu built from the reference sources into
     oracle/_ref; SimulationLoop::run with Gillespie) when it could be built, otherwise the FP64 oracle
     restatement.  Every sampled replica runs `warmup` untimed steps, then `steps` timed steps with all host
-    threads; no further replica starts once budget_s is spent.  Returns (particle-steps/s, particles of the
-    replicas run, cpu_baseline description).  The in-run baseline of the GPU arm and the reference arm call
+    threads; no further replica starts once budget_s is spent.  The reference kernel's own default thread count
+    (4 x cores when READDY_N_CORES is unset, include/readdy/common/common.h:80-95) is timed beside it on the
+    same replicas.  Returns (particle-steps/s, particles of the replicas run, cpu_baseline description).  The in-run baseline of the GPU arm and the reference arm call
     this with the same sample, step counts and budget."""
     import oracle
     from oracle import ref_build, reference_kernel
@@ -193,22 +194,27 @@ def reference_cpu(ns, boxes, pos, types, seed, steps, warmup, budget_s=60.0):
     sample = np.random.default_rng(seed + 5).choice(len(ns), size=min(CPU_SAMPLE, len(ns)), replace=False)
     use_ref = reference_kernel.available()
     spent, done, ran = 0.0, 0, []
+    spent_default = 0.0  # the same replicas and steps at the reference's default thread count
     for r in sample:
         if ran and spent > budget_s:
             break
         ran.append(int(r))
         box = tuple(float(x) for x in boxes[r])
         if use_ref:
-            k = reference_kernel.ReferenceKernel(box, (True, True, True), 1.0, (1.0, 1.0, 0.5), n_threads=cores)
-            for a in range(3):
-                for b in range(a, 3):
-                    k.add_harmonic_repulsion(a, b, 10.0, 1.0)
-            k.add_fusion(0, 1, 2, 1.0, 1.0)
-            k.add_fission(2, 0, 1, 0.1, 1.0)
-            k.add_particles(pos[r], types[r])
-            if warmup:
-                k.run(warmup, 1e-3, handler=reference_kernel.GILLESPIE)
-            _, sec = k.run(steps, 1e-3, handler=reference_kernel.GILLESPIE)
+            def timed(n_threads):
+                k = reference_kernel.ReferenceKernel(box, (True, True, True), 1.0, (1.0, 1.0, 0.5),
+                                                     n_threads=n_threads)
+                for a in range(3):
+                    for b in range(a, 3):
+                        k.add_harmonic_repulsion(a, b, 10.0, 1.0)
+                k.add_fusion(0, 1, 2, 1.0, 1.0)
+                k.add_fission(2, 0, 1, 0.1, 1.0)
+                k.add_particles(pos[r], types[r])
+                if warmup:
+                    k.run(warmup, 1e-3, handler=reference_kernel.GILLESPIE)
+                return k.run(steps, 1e-3, handler=reference_kernel.GILLESPIE)[1]
+            sec = timed(cores)
+            spent_default += timed(4 * cores)
         else:
             oracle.build()
             o = oracle_system(box, pos[r], types[r], seed + int(r), cores)
@@ -227,6 +233,7 @@ def reference_cpu(ns, boxes, pos, types, seed, steps, warmup, budget_s=60.0):
     n_run = int(ns[ran].sum())
     return v, n_run, {"value": v, "unit": UNIT, "cores": cores, "kind": "reference" if use_ref else "port",
                "threads": cores, "reference_default_threads": 4 * cores,
+               "value_at_default_threads": (done / spent_default) if use_ref and spent_default > 0 else None,
                "sample": f"{len(ran)} random replicas of the ensemble ({n_run} particles) x "
                          f"{steps} steps after {warmup} warm-up steps, {what}, {cores} threads per replica; "
                          f"{done} particle-steps in {spent:.1f} s"}
