@@ -2,7 +2,7 @@
 // (rdc_serve.cu).  A replica is one independent system: its own box, particles, seed, step counter
 // and reaction/potential tables.  Every step is ONE persistent launch over the replicas of a work
 // list: each CTA takes replicas from a work counter (largest first) and runs the whole step of one
-// replica in block-level phases
+// replica in block-level phases (the served form lets a small replica take several steps in a launch)
 //
 //   forces (pair stencil) -> Euler BD -> bin -> counting sort -> reaction events -> conflict
 //   resolution + application -> (re-sort if particles appeared or vanished) -> observables
@@ -102,7 +102,8 @@ Geo replica_geo(const double box[3], const int pbc[3], double cutoff, double cel
 size_t engine_smem_bytes(int max_events_sm);
 // kernel attributes for the dynamic shared memory; returns the persistent grid (CTAs resident at once)
 int engine_grid(int threads, size_t smem);
-// one step of every listed replica, then the work counter reset (both captured in the step graph)
+// one step of every listed replica (or, with E.launch_steps, that many steps of each), then the work
+// counter reset (both captured in the step graph)
 void launch_engine_step(const EngineDev &E, int blocks, int threads, size_t smem, cudaStream_t st);
 // binning and sort of the listed replicas (list: device array of replica indices), after setting the
 // ids to 0..n-1 when fill_ids; replicas with records and none written yet get their t = 0 record
