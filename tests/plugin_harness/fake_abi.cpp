@@ -1,12 +1,18 @@
 // TEST INFRASTRUCTURE ONLY: a host-side stand-in for the part of libreaddy_cuda_core.so that the ReaDDy
-// plugin's structural topology reactions use, so that the plugin's mapping of ReaDDy's recipes onto the C
-// ABI runs without a GPU.  It holds one topology (a chain of three TOPOLOGY particles, ids 10 11 12, types
-// 0 0 0, x = 1 2 3), records every rdc_recipe_* call on stdout, and makes rdc_evaluate_topology_reactions call
-// each registered reaction's rate function and then its reaction function on that topology.  The plugin's
-// other C-ABI calls resolve to stubs that return RDC_OK (generated by the test).
+// plugin calls while it sets a system up and runs structural topology reactions, so that the plugin's
+// mapping of ReaDDy's context and recipes onto the C ABI runs without a GPU.
+//  * Structural reactions: it holds one topology (a chain of three TOPOLOGY particles, ids 10 11 12, types
+//    0 0 0, x = 1 2 3), records every rdc_recipe_* call on stdout, and makes rdc_evaluate_topology_reactions
+//    call each registered reaction's rate function and then its reaction function on that topology.
+//  * Context: after fake_abi_log_context(1) it records every rdc_context_* call with its arguments (doubles
+//    in the shortest form that reads back exactly).
+// The plugin's other C-ABI calls resolve to stubs that return RDC_OK (generated by the test).
 #include <readdy_cuda.h>
 
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
 #include <vector>
 
 namespace {
@@ -18,6 +24,22 @@ struct Registered {
 };
 std::vector<Registered> g_reactions;
 int g_dummy;
+int g_log_context = 0;
+int g_reaction_ids = 0;
+
+// the shortest %.*g form of x that reads back as x, without an exponent where one of at most 17 digits does
+std::string num(double x) {
+    char b[40];
+    std::string first;
+    for (int p = 1; p <= 17; ++p) {
+        std::snprintf(b, sizeof b, "%.*g", p, x);
+        if (std::strtod(b, nullptr) != x) continue;
+        if (!std::strchr(b, 'e')) return b;
+        if (first.empty()) first = b;
+    }
+    return first.empty() ? std::string(b) : first;
+}
+std::string vec3(const double *v) { return "(" + num(v[0]) + " " + num(v[1]) + " " + num(v[2]) + ")"; }
 const uint64_t IDS[3] = {10, 11, 12};
 const int64_t EDGES[4] = {0, 1, 1, 2};
 }  // namespace
@@ -27,8 +49,145 @@ extern "C" {
 const char *rdc_last_error(void) { return "fake"; }
 const char *rdc_kernel_name(void) { return "CUDA"; }
 
-int rdc_context_create(rdc_context **c, const double *, const int *, double, int, const double *) {
+void fake_abi_log_context(int on) { g_log_context = on; }
+
+int rdc_context_create(rdc_context **c, const double *box, const int *pbc, double kbt, int n_types,
+                       const double *D) {
     *c = reinterpret_cast<rdc_context *>(&g_dummy);
+    g_reaction_ids = 0;
+    if (g_log_context) {
+        std::printf("context box %s pbc %d %d %d kbt %s D", vec3(box).c_str(), pbc[0], pbc[1], pbc[2], num(kbt).c_str());
+        for (int t = 0; t < n_types; ++t) std::printf(" %s", num(D[t]).c_str());
+        std::printf("\n");
+    }
+    return RDC_OK;
+}
+int rdc_context_set_particle_flavor(rdc_context *, int type, int flavor) {
+    if (g_log_context) std::printf("flavor %d %d\n", type, flavor);
+    return RDC_OK;
+}
+int rdc_context_add_spatial_topology_reaction(rdc_context *, int mode, int type1, int topology_type1, int type2,
+                                              int topology_type2, int type_to1, int topology_type_to1, int type_to2,
+                                              int topology_type_to2, double rate, double radius,
+                                              int min_graph_distance, int *reaction_id) {
+    if (g_log_context)
+        std::printf("spatial mode %d %d/%d + %d/%d -> %d/%d + %d/%d rate %s radius %s distance %d\n", mode, type1,
+                    topology_type1, type2, topology_type2, type_to1, topology_type_to1, type_to2, topology_type_to2,
+                    num(rate).c_str(), num(radius).c_str(), min_graph_distance);
+    if (reaction_id) *reaction_id = 0;
+    return RDC_OK;
+}
+int rdc_context_set_legacy_topology_self_fusion(rdc_context *, int legacy) {
+    if (g_log_context) std::printf("legacy self fusion %d\n", legacy);
+    return RDC_OK;
+}
+int rdc_context_set_record_virial(rdc_context *, int record) {
+    if (g_log_context) std::printf("record virial %d\n", record);
+    return RDC_OK;
+}
+int rdc_context_add_harmonic_repulsion(rdc_context *, int t1, int t2, double k, double d) {
+    if (g_log_context) std::printf("harmonic repulsion %d %d k %s d %s\n", t1, t2, num(k).c_str(), num(d).c_str());
+    return RDC_OK;
+}
+int rdc_context_add_weak_interaction_piecewise_harmonic(rdc_context *, int t1, int t2, double k, double desired,
+                                                        double depth, double cutoff) {
+    if (g_log_context)
+        std::printf("weak interaction %d %d k %s desired %s depth %s cutoff %s\n", t1, t2, num(k).c_str(), num(desired).c_str(),
+                    num(depth).c_str(), num(cutoff).c_str());
+    return RDC_OK;
+}
+int rdc_context_add_lennard_jones(rdc_context *, int t1, int t2, unsigned m, unsigned n, double cutoff, int shift,
+                                  double epsilon, double sigma) {
+    if (g_log_context)
+        std::printf("lennard jones %d %d m %u n %u cutoff %s shift %d epsilon %s sigma %s\n", t1, t2, m, n,
+                    num(cutoff).c_str(), shift, num(epsilon).c_str(), num(sigma).c_str());
+    return RDC_OK;
+}
+int rdc_context_add_screened_electrostatics(rdc_context *, int t1, int t2, double strength, double inverse_depth,
+                                            double repulsion, double repulsion_distance, unsigned exponent,
+                                            double cutoff) {
+    if (g_log_context)
+        std::printf("screened electrostatics %d %d strength %s kappa %s repulsion %s sigma %s exponent %u cutoff %s\n",
+                    t1, t2, num(strength).c_str(), num(inverse_depth).c_str(), num(repulsion).c_str(), num(repulsion_distance).c_str(), exponent,
+                    num(cutoff).c_str());
+    return RDC_OK;
+}
+int rdc_context_add_box(rdc_context *, int t, double k, const double *origin, const double *extent, int inclusion) {
+    if (g_log_context)
+        std::printf("box %d k %s origin %s extent %s inclusion %d\n", t, num(k).c_str(), vec3(origin).c_str(), vec3(extent).c_str(), inclusion);
+    return RDC_OK;
+}
+int rdc_context_add_sphere(rdc_context *, int t, double k, const double *origin, double radius, int inclusion) {
+    if (g_log_context)
+        std::printf("sphere %d k %s origin %s radius %s inclusion %d\n", t, num(k).c_str(), vec3(origin).c_str(), num(radius).c_str(), inclusion);
+    return RDC_OK;
+}
+int rdc_context_add_capsule(rdc_context *, int t, double k, const double *center, const double *direction,
+                            double length, double radius, int inclusion) {
+    if (g_log_context)
+        std::printf("capsule %d k %s center %s direction %s length %s radius %s inclusion %d\n", t, num(k).c_str(),
+                    vec3(center).c_str(), vec3(direction).c_str(), num(length).c_str(), num(radius).c_str(), inclusion);
+    return RDC_OK;
+}
+int rdc_context_add_spherical_barrier(rdc_context *, int t, double height, double width, const double *origin,
+                                      double radius) {
+    if (g_log_context)
+        std::printf("spherical barrier %d height %s width %s origin %s radius %s\n", t, num(height).c_str(), num(width).c_str(),
+                    vec3(origin).c_str(), num(radius).c_str());
+    return RDC_OK;
+}
+int rdc_context_add_cylinder(rdc_context *, int t, double k, const double *origin, const double *normal,
+                             double radius, int inclusion) {
+    if (g_log_context)
+        std::printf("cylinder %d k %s origin %s normal %s radius %s inclusion %d\n", t, num(k).c_str(), vec3(origin).c_str(),
+                    vec3(normal).c_str(), num(radius).c_str(), inclusion);
+    return RDC_OK;
+}
+int rdc_context_add_conversion(rdc_context *, int from, int to, double rate, int *id) {
+    if (g_log_context) std::printf("conversion %d -> %d rate %s\n", from, to, num(rate).c_str());
+    if (id) *id = g_reaction_ids++;
+    return RDC_OK;
+}
+int rdc_context_add_decay(rdc_context *, int from, double rate, int *id) {
+    if (g_log_context) std::printf("decay %d rate %s\n", from, num(rate).c_str());
+    if (id) *id = g_reaction_ids++;
+    return RDC_OK;
+}
+int rdc_context_add_fusion(rdc_context *, int from1, int from2, int to, double rate, double distance, double w1,
+                           double w2, int *id) {
+    if (g_log_context)
+        std::printf("fusion %d + %d -> %d rate %s distance %s weights %s %s\n", from1, from2, to, num(rate).c_str(),
+                    num(distance).c_str(), num(w1).c_str(), num(w2).c_str());
+    if (id) *id = g_reaction_ids++;
+    return RDC_OK;
+}
+int rdc_context_add_fission(rdc_context *, int from, int to1, int to2, double rate, double distance, double w1,
+                            double w2, int *id) {
+    if (g_log_context)
+        std::printf("fission %d -> %d + %d rate %s distance %s weights %s %s\n", from, to1, to2, num(rate).c_str(),
+                    num(distance).c_str(), num(w1).c_str(), num(w2).c_str());
+    if (id) *id = g_reaction_ids++;
+    return RDC_OK;
+}
+int rdc_context_add_enzymatic(rdc_context *, int catalyst, int from, int to, double rate, double distance, int *id) {
+    if (g_log_context)
+        std::printf("enzymatic catalyst %d %d -> %d rate %s distance %s\n", catalyst, from, to, num(rate).c_str(),
+                    num(distance).c_str());
+    if (id) *id = g_reaction_ids++;
+    return RDC_OK;
+}
+int rdc_context_configure_harmonic_bond(rdc_context *, int t1, int t2, double k, double length) {
+    if (g_log_context) std::printf("bond %d %d k %s length %s\n", t1, t2, num(k).c_str(), num(length).c_str());
+    return RDC_OK;
+}
+int rdc_context_configure_harmonic_angle(rdc_context *, int t1, int t2, int t3, double k, double theta0) {
+    if (g_log_context) std::printf("angle %d %d %d k %s theta0 %s\n", t1, t2, t3, num(k).c_str(), num(theta0).c_str());
+    return RDC_OK;
+}
+int rdc_context_configure_cosine_dihedral(rdc_context *, int t1, int t2, int t3, int t4, double k,
+                                          double multiplicity, double phi0) {
+    if (g_log_context)
+        std::printf("dihedral %d %d %d %d k %s n %s phi0 %s\n", t1, t2, t3, t4, num(k).c_str(), num(multiplicity).c_str(), num(phi0).c_str());
     return RDC_OK;
 }
 

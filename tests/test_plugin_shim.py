@@ -69,14 +69,10 @@ rate 2.5
 change_particle_type 2 1"""
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
-def test_plugin_structural_reactions_drive_the_recipe_abi(tmp_path):
-    """The plugin registers every structural reaction of ReaDDy's topology registry and runs its rate and
-    reaction functions on the topology the C ABI describes: ReaDDy's own Recipe (Recipe.h, Recipe.cpp:55-69,
-    with separateVertex's edge removals) becomes the rdc_recipe_* calls step by step, the rate function reads
-    the topology's particles through the plugin's state model, and an exception of a reaction's function
-    reaches the caller of the EvaluateTopologyReactions action.  ReaDDy's model library comes from the
-    reference build (oracle/_ref); the C ABI is the host-side stand-in tests/plugin_harness/fake_abi.cpp."""
+def _harness(tmp_path, main_name):
+    """Links the plugin, the stand-in C ABI (tests/plugin_harness/fake_abi.cpp, with stubs returning RDC_OK for
+    the plugin's other calls) and tests/plugin_harness/<main_name> against ReaDDy's model library from the
+    reference build (oracle/_ref), runs it and returns its stdout lines."""
     import oracle.ref_build as rb
     cxx, gcc = shutil.which("g++"), shutil.which("gcc")
     fmt = _fmt_include()
@@ -89,7 +85,7 @@ def test_plugin_structural_reactions_drive_the_recipe_abi(tmp_path):
              "-I", REF_INCLUDE, "-I", os.path.join(ROOT, "include"), "-I", fmt]
     harness = os.path.join(ROOT, "tests", "plugin_harness")
     srcs = {"plugin": os.path.join(ROOT, "readdy_gb300", "plugin", "CUDAKernel.cpp"),
-            "fake": os.path.join(harness, "fake_abi.cpp"), "main": os.path.join(harness, "structural_main.cpp")}
+            "fake": os.path.join(harness, "fake_abi.cpp"), "main": os.path.join(harness, main_name)}
     objs = {}
     for name, src in srcs.items():
         objs[name] = str(tmp_path / (name + ".o"))
@@ -100,7 +96,6 @@ def test_plugin_structural_reactions_drive_the_recipe_abi(tmp_path):
         out = subprocess.run(["nm", opt, obj], capture_output=True, text=True).stdout
         return {w for line in out.splitlines() for w in line.split() if w.startswith("rdc_")}
 
-    # the plugin's other C-ABI calls: stubs that return RDC_OK
     rest = sorted(rdc_symbols(objs["plugin"], "-u") - rdc_symbols(objs["fake"], "--defined-only"))
     stubs = tmp_path / "stubs.c"
     stubs.write_text("".join(f"int {s}() {{ return 0; }}\n" for s in rest))
@@ -114,6 +109,60 @@ def test_plugin_structural_reactions_drive_the_recipe_abi(tmp_path):
     assert r.returncode == 0, r.stderr[-4000:]
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = r.stdout.strip().splitlines()
+    return r.stdout.strip().splitlines()
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
+def test_plugin_structural_reactions_drive_the_recipe_abi(tmp_path):
+    """The plugin registers every structural reaction of ReaDDy's topology registry and runs its rate and
+    reaction functions on the topology the C ABI describes: ReaDDy's own Recipe (Recipe.h, Recipe.cpp:55-69,
+    with separateVertex's edge removals) becomes the rdc_recipe_* calls step by step, the rate function reads
+    the topology's particles through the plugin's state model, and an exception of a reaction's function
+    reaches the caller of the EvaluateTopologyReactions action."""
+    lines = _harness(tmp_path, "structural_main.cpp")
     assert "\n".join(lines[:14]) == EXPECTED_STRUCTURAL_LOG
     assert lines[-1] == "caught rate failed"
+
+
+# ids A=0 B=1 C=2 D=3 (C, D TOPOLOGY flavored), topology types T1=0 T2=1; the values of context_main.cpp
+EXPECTED_CONTEXT_CALLS = """context box (10 12 14) pbc 1 1 0 kbt 1.5 D 1 0.5 0.25 2
+flavor 0 0
+flavor 1 0
+flavor 2 1
+flavor 3 1
+spatial mode 1 2/0 + 3/0 -> 2/1 + 3/-1 rate 2 radius 1.5 distance 0
+legacy self fusion 0
+harmonic repulsion 0 1 k 10 d 1.1
+weak interaction 1 1 k 5 desired 0.7 depth 0.3 cutoff 1.9
+lennard jones 0 0 m 12 n 6 cutoff 2.5 shift 1 epsilon 1.25 sigma 0.9
+screened electrostatics 0 2 strength -1 kappa 0.8 repulsion 1.2 sigma 0.6 exponent 6 cutoff 3.5
+box 0 k 2 origin (-4 -5 -6) extent (8 10 12) inclusion 1
+sphere 1 k 3 origin (0.5 0.25 -0.5) radius 4 inclusion 1
+sphere 1 k 3.5 origin (0 0 0) radius 2 inclusion 0
+capsule 2 k 4 center (0 1 0) direction (1 0 0) length 3 radius 1.5 inclusion 1
+spherical barrier 3 height 2.5 width 0.5 origin (1 1 1) radius 2
+cylinder 0 k 1.5 origin (0 0 0) normal (0 0 1) radius 3 inclusion 1
+conversion 0 -> 1 rate 0.1
+decay 1 rate 0.02
+fusion 0 + 1 -> 2 rate 1 distance 1.2 weights 0.25 0.75
+fission 2 -> 0 + 1 rate 0.5 distance 0.8 weights 0.5 0.5
+enzymatic catalyst 3 0 -> 1 rate 0.7 distance 1.1
+bond 2 3 k 10 length 1
+angle 2 3 2 k 2 theta0 3
+dihedral 2 3 3 2 k 1 n 3 phi0 0.5
+record virial 0"""
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
+def test_plugin_translates_the_context_into_the_abi(tmp_path):
+    """Kernel::initialize turns a model::Context built through ReaDDy's own registries into rdc_context_* calls
+    with exactly the values given: box, periodicity, kBT, diffusion constants and flavors; the four pair
+    potentials (the parameters ReaDDy keeps without getters, read through member pointers and describe()); the
+    five order-1 potentials, inclusion and exclusion; the five reactions with their normalised weights
+    (Fusion.h:62-68); the bonded terms of the topology registry and its spatial reaction (descriptor parsed by
+    ReaDDy).  The calls are compared as a set: the registries are hash maps."""
+    lines = _harness(tmp_path, "context_main.cpp")
+    assert lines[0] == "ids A=0 B=1 C=2 D=3 T1=0 T2=1"
+    calls = lines[1:]
+    assert len(calls) == len(set(calls))
+    assert set(calls) == set(EXPECTED_CONTEXT_CALLS.splitlines())
