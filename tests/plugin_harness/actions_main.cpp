@@ -1,0 +1,57 @@
+// TEST INFRASTRUCTURE ONLY: drives the ReaDDy plugin's state model, actions and binning observables the way
+// SimulationLoop and ReaDDy's observables do, against the logging stand-in C ABI of fake_abi.cpp, with ReaDDy's
+// model library from the reference build.  Prints the stand-in's log of the system calls and the observables'
+// results; the test compares them with the values given here.
+#include "../../readdy_gb300/plugin/CUDAKernel.h"
+
+#include <cstdio>
+
+extern "C" void fake_abi_log_context(int on);
+
+namespace top = readdy::model::top;
+using PV = top::Graph::PersistentVertexIndex;
+
+int main() {
+    readdy::kernel::cuda::CUDAKernel k;
+    auto &ctx = k.context();
+    ctx.boxSize() = {10., 10., 10.};
+    ctx.particleTypes().add("A", 1.0);
+    ctx.particleTypes().add("T", 1.0, readdy::model::particleflavor::TOPOLOGY);
+    ctx.topologyRegistry().addType("chain");
+    ctx.topologyRegistry().configureBondPotential("T", "T", {5.0, 1.0});
+    k.initialize();
+    fake_abi_log_context(2);
+    k.stateModel().addParticles({readdy::model::Particle(0.5, 1.5, -2.5, 0), readdy::model::Particle(1., 2., 3., 0)});
+    auto *t = k.stateModel().addTopology(ctx.topologyRegistry().idOf("chain"),
+                                         {readdy::model::Particle(0., 0., 0., 1), readdy::model::Particle(1., 0., 0., 1),
+                                          readdy::model::Particle(2., 0., 0.25, 1)});
+    t->addEdge(PV{0}, PV{1});
+    t->addEdge(PV{1}, PV{2});
+    // the SimulationLoop order (SimulationLoop.h:256-306)
+    auto &a = k.actions();
+    a.initializeKernel()->perform();
+    a.createNeighborList(2.5)->perform();
+    a.calculateForces()->perform();
+    a.eulerBDIntegrator(0.01)->perform();
+    a.updateNeighborList()->perform();
+    a.uncontrolledApproximation(0.02)->perform();
+    a.gillespie(0.03)->perform();
+    readdy::model::actions::top::BreakConfig cfg;
+    cfg.addBreakablePair(1, 1, 2.0, 0.5);
+    a.breakBonds(0.04, cfg)->perform();
+    a.clearNeighborList()->perform();
+    auto &o = k.observe();
+    auto n = o.nParticles(1, {"A", "T"}, [](const auto &) {});
+    n->evaluate();
+    auto h = o.histogramAlongAxis(1, {0., 1., 2.5}, {"T"}, 2, [](const auto &) {});
+    h->evaluate();
+    auto r = o.radialDistribution(1, {0., 0.5, 1.0, 2.0}, {"A"}, {"A", "T"}, 0.25, [](const auto &) {});
+    r->evaluate();
+    fake_abi_log_context(0);
+    std::printf("n particles %lu %lu\n", n->getResult()[0], n->getResult()[1]);
+    std::printf("histogram %g %g\n", h->getResult()[0], h->getResult()[1]);
+    const auto &[centers, distribution] = r->getResult();
+    std::printf("radial distribution centers %g %g %g values %g %g %g\n", centers[0], centers[1], centers[2],
+                distribution[0], distribution[1], distribution[2]);
+    return 0;
+}

@@ -6,6 +6,8 @@
 //    call each registered reaction's rate function and then its reaction function on that topology.
 //  * Context: after fake_abi_log_context(1) it records every rdc_context_* call with its arguments (doubles
 //    in the shortest form that reads back exactly).
+//  * System: after fake_abi_log_context(2) it records the state-model, action and observable calls with
+//    their arguments instead (particles, topologies with edges, time steps, break pairs, bins).
 // The plugin's other C-ABI calls resolve to stubs that return RDC_OK (generated by the test).
 #include <readdy_cuda.h>
 
@@ -24,8 +26,9 @@ struct Registered {
 };
 std::vector<Registered> g_reactions;
 int g_dummy;
-int g_log_context = 0;
+int g_log_context = 0;  // 1: context calls, 2: system calls
 int g_reaction_ids = 0;
+uint64_t g_next_id = 100;
 
 // the shortest %.*g form of x that reads back as x, without an exponent where one of at most 17 digits does
 std::string num(double x) {
@@ -55,7 +58,7 @@ int rdc_context_create(rdc_context **c, const double *box, const int *pbc, doubl
                        const double *D) {
     *c = reinterpret_cast<rdc_context *>(&g_dummy);
     g_reaction_ids = 0;
-    if (g_log_context) {
+    if (g_log_context == 1) {
         std::printf("context box %s pbc %d %d %d kbt %s D", vec3(box).c_str(), pbc[0], pbc[1], pbc[2], num(kbt).c_str());
         for (int t = 0; t < n_types; ++t) std::printf(" %s", num(D[t]).c_str());
         std::printf("\n");
@@ -63,14 +66,14 @@ int rdc_context_create(rdc_context **c, const double *box, const int *pbc, doubl
     return RDC_OK;
 }
 int rdc_context_set_particle_flavor(rdc_context *, int type, int flavor) {
-    if (g_log_context) std::printf("flavor %d %d\n", type, flavor);
+    if (g_log_context == 1) std::printf("flavor %d %d\n", type, flavor);
     return RDC_OK;
 }
 int rdc_context_add_spatial_topology_reaction(rdc_context *, int mode, int type1, int topology_type1, int type2,
                                               int topology_type2, int type_to1, int topology_type_to1, int type_to2,
                                               int topology_type_to2, double rate, double radius,
                                               int min_graph_distance, int *reaction_id) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("spatial mode %d %d/%d + %d/%d -> %d/%d + %d/%d rate %s radius %s distance %d\n", mode, type1,
                     topology_type1, type2, topology_type2, type_to1, topology_type_to1, type_to2, topology_type_to2,
                     num(rate).c_str(), num(radius).c_str(), min_graph_distance);
@@ -78,27 +81,27 @@ int rdc_context_add_spatial_topology_reaction(rdc_context *, int mode, int type1
     return RDC_OK;
 }
 int rdc_context_set_legacy_topology_self_fusion(rdc_context *, int legacy) {
-    if (g_log_context) std::printf("legacy self fusion %d\n", legacy);
+    if (g_log_context == 1) std::printf("legacy self fusion %d\n", legacy);
     return RDC_OK;
 }
 int rdc_context_set_record_virial(rdc_context *, int record) {
-    if (g_log_context) std::printf("record virial %d\n", record);
+    if (g_log_context == 1) std::printf("record virial %d\n", record);
     return RDC_OK;
 }
 int rdc_context_add_harmonic_repulsion(rdc_context *, int t1, int t2, double k, double d) {
-    if (g_log_context) std::printf("harmonic repulsion %d %d k %s d %s\n", t1, t2, num(k).c_str(), num(d).c_str());
+    if (g_log_context == 1) std::printf("harmonic repulsion %d %d k %s d %s\n", t1, t2, num(k).c_str(), num(d).c_str());
     return RDC_OK;
 }
 int rdc_context_add_weak_interaction_piecewise_harmonic(rdc_context *, int t1, int t2, double k, double desired,
                                                         double depth, double cutoff) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("weak interaction %d %d k %s desired %s depth %s cutoff %s\n", t1, t2, num(k).c_str(), num(desired).c_str(),
                     num(depth).c_str(), num(cutoff).c_str());
     return RDC_OK;
 }
 int rdc_context_add_lennard_jones(rdc_context *, int t1, int t2, unsigned m, unsigned n, double cutoff, int shift,
                                   double epsilon, double sigma) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("lennard jones %d %d m %u n %u cutoff %s shift %d epsilon %s sigma %s\n", t1, t2, m, n,
                     num(cutoff).c_str(), shift, num(epsilon).c_str(), num(sigma).c_str());
     return RDC_OK;
@@ -106,56 +109,56 @@ int rdc_context_add_lennard_jones(rdc_context *, int t1, int t2, unsigned m, uns
 int rdc_context_add_screened_electrostatics(rdc_context *, int t1, int t2, double strength, double inverse_depth,
                                             double repulsion, double repulsion_distance, unsigned exponent,
                                             double cutoff) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("screened electrostatics %d %d strength %s kappa %s repulsion %s sigma %s exponent %u cutoff %s\n",
                     t1, t2, num(strength).c_str(), num(inverse_depth).c_str(), num(repulsion).c_str(), num(repulsion_distance).c_str(), exponent,
                     num(cutoff).c_str());
     return RDC_OK;
 }
 int rdc_context_add_box(rdc_context *, int t, double k, const double *origin, const double *extent, int inclusion) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("box %d k %s origin %s extent %s inclusion %d\n", t, num(k).c_str(), vec3(origin).c_str(), vec3(extent).c_str(), inclusion);
     return RDC_OK;
 }
 int rdc_context_add_sphere(rdc_context *, int t, double k, const double *origin, double radius, int inclusion) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("sphere %d k %s origin %s radius %s inclusion %d\n", t, num(k).c_str(), vec3(origin).c_str(), num(radius).c_str(), inclusion);
     return RDC_OK;
 }
 int rdc_context_add_capsule(rdc_context *, int t, double k, const double *center, const double *direction,
                             double length, double radius, int inclusion) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("capsule %d k %s center %s direction %s length %s radius %s inclusion %d\n", t, num(k).c_str(),
                     vec3(center).c_str(), vec3(direction).c_str(), num(length).c_str(), num(radius).c_str(), inclusion);
     return RDC_OK;
 }
 int rdc_context_add_spherical_barrier(rdc_context *, int t, double height, double width, const double *origin,
                                       double radius) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("spherical barrier %d height %s width %s origin %s radius %s\n", t, num(height).c_str(), num(width).c_str(),
                     vec3(origin).c_str(), num(radius).c_str());
     return RDC_OK;
 }
 int rdc_context_add_cylinder(rdc_context *, int t, double k, const double *origin, const double *normal,
                              double radius, int inclusion) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("cylinder %d k %s origin %s normal %s radius %s inclusion %d\n", t, num(k).c_str(), vec3(origin).c_str(),
                     vec3(normal).c_str(), num(radius).c_str(), inclusion);
     return RDC_OK;
 }
 int rdc_context_add_conversion(rdc_context *, int from, int to, double rate, int *id) {
-    if (g_log_context) std::printf("conversion %d -> %d rate %s\n", from, to, num(rate).c_str());
+    if (g_log_context == 1) std::printf("conversion %d -> %d rate %s\n", from, to, num(rate).c_str());
     if (id) *id = g_reaction_ids++;
     return RDC_OK;
 }
 int rdc_context_add_decay(rdc_context *, int from, double rate, int *id) {
-    if (g_log_context) std::printf("decay %d rate %s\n", from, num(rate).c_str());
+    if (g_log_context == 1) std::printf("decay %d rate %s\n", from, num(rate).c_str());
     if (id) *id = g_reaction_ids++;
     return RDC_OK;
 }
 int rdc_context_add_fusion(rdc_context *, int from1, int from2, int to, double rate, double distance, double w1,
                            double w2, int *id) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("fusion %d + %d -> %d rate %s distance %s weights %s %s\n", from1, from2, to, num(rate).c_str(),
                     num(distance).c_str(), num(w1).c_str(), num(w2).c_str());
     if (id) *id = g_reaction_ids++;
@@ -163,30 +166,30 @@ int rdc_context_add_fusion(rdc_context *, int from1, int from2, int to, double r
 }
 int rdc_context_add_fission(rdc_context *, int from, int to1, int to2, double rate, double distance, double w1,
                             double w2, int *id) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("fission %d -> %d + %d rate %s distance %s weights %s %s\n", from, to1, to2, num(rate).c_str(),
                     num(distance).c_str(), num(w1).c_str(), num(w2).c_str());
     if (id) *id = g_reaction_ids++;
     return RDC_OK;
 }
 int rdc_context_add_enzymatic(rdc_context *, int catalyst, int from, int to, double rate, double distance, int *id) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("enzymatic catalyst %d %d -> %d rate %s distance %s\n", catalyst, from, to, num(rate).c_str(),
                     num(distance).c_str());
     if (id) *id = g_reaction_ids++;
     return RDC_OK;
 }
 int rdc_context_configure_harmonic_bond(rdc_context *, int t1, int t2, double k, double length) {
-    if (g_log_context) std::printf("bond %d %d k %s length %s\n", t1, t2, num(k).c_str(), num(length).c_str());
+    if (g_log_context == 1) std::printf("bond %d %d k %s length %s\n", t1, t2, num(k).c_str(), num(length).c_str());
     return RDC_OK;
 }
 int rdc_context_configure_harmonic_angle(rdc_context *, int t1, int t2, int t3, double k, double theta0) {
-    if (g_log_context) std::printf("angle %d %d %d k %s theta0 %s\n", t1, t2, t3, num(k).c_str(), num(theta0).c_str());
+    if (g_log_context == 1) std::printf("angle %d %d %d k %s theta0 %s\n", t1, t2, t3, num(k).c_str(), num(theta0).c_str());
     return RDC_OK;
 }
 int rdc_context_configure_cosine_dihedral(rdc_context *, int t1, int t2, int t3, int t4, double k,
                                           double multiplicity, double phi0) {
-    if (g_log_context)
+    if (g_log_context == 1)
         std::printf("dihedral %d %d %d %d k %s n %s phi0 %s\n", t1, t2, t3, t4, num(k).c_str(), num(multiplicity).c_str(), num(phi0).c_str());
     return RDC_OK;
 }
@@ -270,6 +273,107 @@ int rdc_recipe_append_particle(rdc_recipe *, int64_t n_neighbors, const int64_t 
 }
 int rdc_recipe_change_particle_position(rdc_recipe *, int64_t vertex, const double *pos3) {
     std::printf("change_particle_position %lld %g %g %g\n", (long long)vertex, pos3[0], pos3[1], pos3[2]);
+    return RDC_OK;
+}
+
+int rdc_add_particles(rdc_system *, int64_t n, const double *x, const int *types, uint64_t *ids) {
+    for (int64_t i = 0; i < n; ++i) {
+        if (g_log_context == 2) std::printf("add particle %s type %d\n", vec3(x + 3 * i).c_str(), types[i]);
+        if (ids) ids[i] = g_next_id;
+        ++g_next_id;
+    }
+    return RDC_OK;
+}
+int rdc_add_topology_typed(rdc_system *, int topology_type, int64_t n, const double *x, const int *types,
+                           int64_t n_edges, const int64_t *edges2, uint64_t *ids) {
+    if (g_log_context == 2) {
+        std::printf("add topology type %d:", topology_type);
+        for (int64_t i = 0; i < n; ++i) std::printf(" %s/%d", vec3(x + 3 * i).c_str(), types[i]);
+        std::printf(" edges");
+        for (int64_t e = 0; e < n_edges; ++e) std::printf(" %lld-%lld", (long long)edges2[2 * e], (long long)edges2[2 * e + 1]);
+        std::printf("\n");
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        if (ids) ids[i] = g_next_id;
+        ++g_next_id;
+    }
+    return RDC_OK;
+}
+int rdc_break_bonds(rdc_system *, double dt, int n_pairs, const int *t1, const int *t2, const double *thr,
+                    const double *rate, int64_t *n_broken) {
+    if (g_log_context == 2) {
+        std::printf("break bonds dt %s", num(dt).c_str());
+        for (int k = 0; k < n_pairs; ++k)
+            std::printf(" %d-%d threshold %s rate %s", t1[k], t2[k], num(thr[k]).c_str(), num(rate[k]).c_str());
+        std::printf("\n");
+    }
+    if (n_broken) *n_broken = 0;
+    return RDC_OK;
+}
+int rdc_initialize(rdc_system *) {
+    if (g_log_context == 2) std::printf("initialize\n");
+    return RDC_OK;
+}
+int rdc_nl_create(rdc_system *, double cutoff) {
+    if (g_log_context == 2) std::printf("neighbor list create %s\n", num(cutoff).c_str());
+    return RDC_OK;
+}
+int rdc_nl_update(rdc_system *) {
+    if (g_log_context == 2) std::printf("neighbor list update\n");
+    return RDC_OK;
+}
+int rdc_nl_clear(rdc_system *) {
+    if (g_log_context == 2) std::printf("neighbor list clear\n");
+    return RDC_OK;
+}
+int rdc_calculate_forces(rdc_system *) {
+    if (g_log_context == 2) std::printf("calculate forces\n");
+    return RDC_OK;
+}
+int rdc_euler_bd_integrate(rdc_system *, double dt) {
+    if (g_log_context == 2) std::printf("euler bd %s\n", num(dt).c_str());
+    return RDC_OK;
+}
+int rdc_uncontrolled_approximation(rdc_system *, double dt) {
+    if (g_log_context == 2) std::printf("uncontrolled approximation %s\n", num(dt).c_str());
+    return RDC_OK;
+}
+int rdc_gillespie(rdc_system *, double dt) {
+    if (g_log_context == 2) std::printf("gillespie %s\n", num(dt).c_str());
+    return RDC_OK;
+}
+int rdc_count_types(rdc_system *, int64_t *counts) {
+    if (g_log_context == 2) std::printf("count types\n");
+    for (int t = 0; t < 2; ++t) counts[t] = 7 + t;
+    return RDC_OK;
+}
+int rdc_histogram_along_axis(rdc_system *, int n_borders, const double *borders, int n_types, const int *types,
+                             int axis, double *counts) {
+    if (g_log_context == 2) {
+        std::printf("histogram axis %d borders", axis);
+        for (int k = 0; k < n_borders; ++k) std::printf(" %s", num(borders[k]).c_str());
+        std::printf(" types");
+        for (int k = 0; k < n_types; ++k) std::printf(" %d", types[k]);
+        std::printf("\n");
+    }
+    for (int k = 0; k + 1 < n_borders; ++k) counts[k] = k;
+    return RDC_OK;
+}
+int rdc_radial_distribution(rdc_system *, int n_borders, const double *borders, int n_from, const int *from,
+                            int n_to, const int *to, double density, double *counts, double *distribution) {
+    if (g_log_context == 2) {
+        std::printf("radial distribution borders");
+        for (int k = 0; k < n_borders; ++k) std::printf(" %s", num(borders[k]).c_str());
+        std::printf(" from");
+        for (int k = 0; k < n_from; ++k) std::printf(" %d", from[k]);
+        std::printf(" to");
+        for (int k = 0; k < n_to; ++k) std::printf(" %d", to[k]);
+        std::printf(" density %s\n", num(density).c_str());
+    }
+    for (int k = 0; k + 1 < n_borders; ++k) {
+        if (counts) counts[k] = k;
+        if (distribution) distribution[k] = 0.5 * k;
+    }
     return RDC_OK;
 }
 

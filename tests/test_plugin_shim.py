@@ -166,3 +166,33 @@ def test_plugin_translates_the_context_into_the_abi(tmp_path):
     calls = lines[1:]
     assert len(calls) == len(set(calls))
     assert set(calls) == set(EXPECTED_CONTEXT_CALLS.splitlines())
+
+
+EXPECTED_SYSTEM_CALLS = """add particle (0.5 1.5 -2.5) type 0
+add particle (1 2 3) type 0
+add topology type 0: (0 0 0)/1 (1 0 0)/1 (2 0 0.25)/1 edges 0-1 1-2
+initialize
+neighbor list create 2.5
+calculate forces
+euler bd 0.01
+neighbor list update
+uncontrolled approximation 0.02
+gillespie 0.03
+break bonds dt 0.04 1-1 threshold 2 rate 0.5
+neighbor list clear
+count types
+histogram axis 2 borders 0 1 2.5 types 1
+radial distribution borders 0 0.5 1 2 from 0 to 0 1 density 0.25
+n particles 7 8
+histogram 0 1
+radial distribution centers 0.25 0.75 1.5 values 0 0.5 1"""
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
+def test_plugin_state_model_actions_and_observables_reach_the_abi(tmp_path):
+    """The state model, the actions in SimulationLoop's order and the binning observables, driven through
+    ReaDDy's own interfaces: particles are uploaded at once, a topology with the edges added after addTopology
+    returned is uploaded at the first action, every action passes its time step or cutoff, BreakBonds its
+    configuration's pairs, and the observables their bins and type selections; the observables' results are
+    the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints)."""
+    assert _harness(tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
