@@ -69,10 +69,12 @@ rate 2.5
 change_particle_type 2 1"""
 
 
-def _harness(tmp_path, main_name):
-    """Links the plugin, the stand-in C ABI (tests/plugin_harness/fake_abi.cpp, with stubs returning RDC_OK for
-    the plugin's other calls) and tests/plugin_harness/<main_name> against ReaDDy's model library from the
-    reference build (oracle/_ref), runs it and returns its stdout lines."""
+@pytest.fixture(scope="module")
+def harness_objects(tmp_path_factory):
+    """The plugin and the stand-in C ABI (tests/plugin_harness/fake_abi.cpp) compiled once, with stubs that return
+    RDC_OK for the plugin's other calls, and ReaDDy's model library from the reference build (oracle/_ref)."""
+    if not os.path.isdir(REF_INCLUDE):
+        pytest.skip("reference headers not present")
     import oracle.ref_build as rb
     cxx, gcc = shutil.which("g++"), shutil.which("gcc")
     fmt = _fmt_include()
@@ -81,45 +83,53 @@ def _harness(tmp_path, main_name):
     lib = rb.build()
     if lib is None:
         pytest.skip(rb.unavailable_reason())
+    out = tmp_path_factory.mktemp("plugin_harness")
     flags = ["-std=c++20", "-fPIC", "-DFMT_HEADER_ONLY", "-w", "-I", os.path.join(ROOT, "oracle", "shim_include"),
              "-I", REF_INCLUDE, "-I", os.path.join(ROOT, "include"), "-I", fmt]
-    harness = os.path.join(ROOT, "tests", "plugin_harness")
     srcs = {"plugin": os.path.join(ROOT, "readdy_gb300", "plugin", "CUDAKernel.cpp"),
-            "fake": os.path.join(harness, "fake_abi.cpp"), "main": os.path.join(harness, main_name)}
+            "fake": os.path.join(ROOT, "tests", "plugin_harness", "fake_abi.cpp")}
     objs = {}
     for name, src in srcs.items():
-        objs[name] = str(tmp_path / (name + ".o"))
+        objs[name] = str(out / (name + ".o"))
         r = subprocess.run([cxx, *flags, "-c", src, "-o", objs[name]], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr[-4000:]
 
     def rdc_symbols(obj, opt):
-        out = subprocess.run(["nm", opt, obj], capture_output=True, text=True).stdout
-        return {w for line in out.splitlines() for w in line.split() if w.startswith("rdc_")}
+        text = subprocess.run(["nm", opt, obj], capture_output=True, text=True).stdout
+        return {w for line in text.splitlines() for w in line.split() if w.startswith("rdc_")}
 
     rest = sorted(rdc_symbols(objs["plugin"], "-u") - rdc_symbols(objs["fake"], "--defined-only"))
-    stubs = tmp_path / "stubs.c"
+    stubs = out / "stubs.c"
     stubs.write_text("".join(f"int {s}() {{ return 0; }}\n" for s in rest))
-    r = subprocess.run([gcc, "-std=gnu17", "-c", str(stubs), "-o", str(tmp_path / "stubs.o")], capture_output=True,
-                       text=True)
+    objs["stubs"] = str(out / "stubs.o")
+    r = subprocess.run([gcc, "-std=gnu17", "-c", str(stubs), "-o", objs["stubs"]], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+    return {"cxx": cxx, "flags": flags, "objs": objs, "libdir": os.path.dirname(lib)}
+
+
+def _harness(h, tmp_path, main_name):
+    """Links tests/plugin_harness/<main_name> with the objects of harness_objects, runs it and returns its
+    stdout lines."""
+    main_obj = str(tmp_path / "main.o")
+    r = subprocess.run([h["cxx"], *h["flags"], "-c", os.path.join(ROOT, "tests", "plugin_harness", main_name), "-o",
+                        main_obj], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
     exe = str(tmp_path / "harness")
-    libdir = os.path.dirname(lib)
-    r = subprocess.run([cxx, *objs.values(), str(tmp_path / "stubs.o"), "-L", libdir, "-lreaddy_ref",
-                        "-Wl,-rpath," + libdir, "-pthread", "-ldl", "-o", exe], capture_output=True, text=True)
+    r = subprocess.run([h["cxx"], main_obj, *h["objs"].values(), "-L", h["libdir"], "-lreaddy_ref",
+                        "-Wl,-rpath," + h["libdir"], "-pthread", "-ldl", "-o", exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stderr[-2000:]
     return r.stdout.strip().splitlines()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
-def test_plugin_structural_reactions_drive_the_recipe_abi(tmp_path):
+def test_plugin_structural_reactions_drive_the_recipe_abi(harness_objects, tmp_path):
     """The plugin registers every structural reaction of ReaDDy's topology registry and runs its rate and
     reaction functions on the topology the C ABI describes: ReaDDy's own Recipe (Recipe.h, Recipe.cpp:55-69,
     with separateVertex's edge removals) becomes the rdc_recipe_* calls step by step, the rate function reads
     the topology's particles through the plugin's state model, and an exception of a reaction's function
     reaches the caller of the EvaluateTopologyReactions action."""
-    lines = _harness(tmp_path, "structural_main.cpp")
+    lines = _harness(harness_objects, tmp_path, "structural_main.cpp")
     assert "\n".join(lines[:14]) == EXPECTED_STRUCTURAL_LOG
     assert lines[-1] == "caught rate failed"
 
@@ -153,15 +163,14 @@ dihedral 2 3 3 2 k 1 n 3 phi0 0.5
 record virial 0"""
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
-def test_plugin_translates_the_context_into_the_abi(tmp_path):
+def test_plugin_translates_the_context_into_the_abi(harness_objects, tmp_path):
     """Kernel::initialize turns a model::Context built through ReaDDy's own registries into rdc_context_* calls
     with exactly the values given: box, periodicity, kBT, diffusion constants and flavors; the four pair
     potentials (the parameters ReaDDy keeps without getters, read through member pointers and describe()); the
     five order-1 potentials, inclusion and exclusion; the five reactions with their normalised weights
     (Fusion.h:62-68); the bonded terms of the topology registry and its spatial reaction (descriptor parsed by
     ReaDDy).  The calls are compared as a set: the registries are hash maps."""
-    lines = _harness(tmp_path, "context_main.cpp")
+    lines = _harness(harness_objects, tmp_path, "context_main.cpp")
     assert lines[0] == "ids A=0 B=1 C=2 D=3 T1=0 T2=1"
     calls = lines[1:]
     assert len(calls) == len(set(calls))
@@ -188,11 +197,10 @@ histogram 0 1
 radial distribution centers 0.25 0.75 1.5 values 0 0.5 1"""
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_INCLUDE), reason="reference headers not present")
-def test_plugin_state_model_actions_and_observables_reach_the_abi(tmp_path):
+def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_objects, tmp_path):
     """The state model, the actions in SimulationLoop's order and the binning observables, driven through
     ReaDDy's own interfaces: particles are uploaded at once, a topology with the edges added after addTopology
     returned is uploaded at the first action, every action passes its time step or cutoff, BreakBonds its
     configuration's pairs, and the observables their bins and type selections; the observables' results are
     the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints)."""
-    assert _harness(tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
+    assert _harness(harness_objects, tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
