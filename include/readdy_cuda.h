@@ -229,6 +229,10 @@ int rdc_get_particle_energies(rdc_system *s, int64_t capacity, double *energies,
 /* StateModel::virial() after the last CalculateForces (row-major 3x3): the sum over pairs of
  * outer(-x_ij, f_i) (CPUCalculateForces.cpp:247-249); zero unless the context records the virial */
 int rdc_get_virial(rdc_system *s, double *virial9);
+/* Context::recordVirial for a system that exists already: ReaDDy reads the flag at every force calculation
+ * (CPUCalculateForces.cpp:154), and its Virial observable sets it after particles may have been added; from the
+ * next CalculateForces on the system records (1) or stops recording (0) the virial */
+int rdc_set_record_virial(rdc_system *s, int record);
 /* StateModel::energy() after the last CalculateForces */
 int rdc_get_energy(rdc_system *s, double *energy);
 /* particles advanced by the integrator since the system was created, summed over steps (the

@@ -54,6 +54,7 @@ def _sig(lib):
         "rdc_context_add_spatial_topology_reaction": (i, [vp, i, i, i, i, i, i, i, i, i, d, d, i, P(i)]),
         "rdc_context_set_legacy_topology_self_fusion": (i, [vp, i]),
         "rdc_get_virial": (i, [vp, P(d)]),
+        "rdc_set_record_virial": (i, [vp, i]),
         "rdc_context_add_harmonic_repulsion": (i, [vp, i, i, d, d]),
         "rdc_context_add_weak_interaction_piecewise_harmonic": (i, [vp, i, i, d, d, d, d]),
         "rdc_context_add_lennard_jones": (i, [vp, i, i, C.c_uint, C.c_uint, d, i, d, d]),

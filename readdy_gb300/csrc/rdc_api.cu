@@ -516,6 +516,26 @@ struct rdc_system {
         graph = nullptr;
     }
 
+    // Context::recordVirial switched on a live system: ReaDDy reads the flag from the context at every
+    // force calculation (CPUCalculateForces.cpp:154), and its Virial observable sets it after the state
+    // model may already hold particles.  The next force calculation records (or stops recording) the virial.
+    void set_record_virial(bool on) {
+        if (on == (d.virial != nullptr)) return;
+        sync();
+        if (on) {
+            d.vpart = dalloc<double>(9 * FORCE_BLOCKS);
+            d.virial = dalloc<double>(9);
+            RDC_CUDA(cudaMemsetAsync(d.vpart, 0, sizeof(double) * 9 * FORCE_BLOCKS, stream));
+            RDC_CUDA(cudaMemsetAsync(d.virial, 0, sizeof(double) * 9, stream));
+        } else {
+            dfree(d.vpart);
+            dfree(d.virial);
+        }
+        ctx.record_virial = on;
+        invalidate_graph();
+        sync();
+    }
+
     // grow the per-particle arrays (host-synchronous)
     void reserve(int cap) {
         if (cap <= d.capacity) return;
@@ -2135,6 +2155,12 @@ int rdc_get_particle_energies(rdc_system *s, int64_t cap, double *energies, uint
         }
         if (n_out) *n_out = k;
         if (k > cap) throw CapacityError("output capacity too small for the particles");
+    });
+}
+int rdc_set_record_virial(rdc_system *s, int record) {
+    return guarded([&] {
+        require(s != nullptr, "null argument");
+        s->set_record_virial(record != 0);
     });
 }
 int rdc_get_virial(rdc_system *s, double *virial9) {

@@ -412,6 +412,11 @@ class CUDAKernel:
         N.check(self._lib.rdc_get_energy(self._h, C.byref(e)))
         return e.value
 
+    def set_record_virial(self, record: bool = True):
+        """Context::recordVirial for this system as it is (rdc_set_record_virial): the next force calculation
+        records the virial, or stops recording it."""
+        N.check(self._lib.rdc_set_record_virial(self._h, int(bool(record))))
+
     def virial(self):
         """StateModel::virial() of the last force calculation, 3x3."""
         out = np.zeros(9)

@@ -565,9 +565,15 @@ std::unique_ptr<act::EvaluateObservables> CUDAActionFactory::evaluateObservables
 std::unique_ptr<act::MakeCheckpoint> CUDAActionFactory::makeCheckpoint(std::string, std::size_t) const {
     throw std::logic_error("CUDA kernel: checkpoints are not supported");
 }
+// InitializeKernel (CPUMiscActions.h:80-89 calls Kernel::initialize, which reads the context again): the
+// system keeps its particles and topologies; the one context flag that ReaDDy's observables set after
+// particles may have been added, recordVirial, is applied to it here
 std::unique_ptr<act::InitializeKernel> CUDAActionFactory::initializeKernel() const {
     auto *k = _kernel;
-    return std::make_unique<CallAction<act::InitializeKernel>>([k] { check(rdc_initialize(k->sys())); });
+    return std::make_unique<CallAction<act::InitializeKernel>>([k] {
+        check(rdc_set_record_virial(k->sys(), k->context().recordVirial() ? 1 : 0));
+        check(rdc_initialize(k->sys()));
+    });
 }
 
 // ---- observables ------------------------------------------------------------------------------------
@@ -703,6 +709,7 @@ std::unique_ptr<obs::Virial> CUDAObservableFactory::virial(Stride s, ObsCallback
     auto o = std::make_unique<VirialCUDA>(_kernel, s);
     o->setCallback(cb);
     _kernel->context().recordVirial() = true;
+    if (auto *sys = _kernel->sysIfCreated()) check(rdc_set_record_virial(sys, 1));
     return o;
 }
 std::unique_ptr<obs::HistogramAlongAxis>

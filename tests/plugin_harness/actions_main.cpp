@@ -27,6 +27,9 @@ int main() {
                                           readdy::model::Particle(2., 0., 0.25, 1)});
     t->addEdge(PV{0}, PV{1});
     t->addEdge(PV{1}, PV{2});
+    // a Virial observable registered after the system holds particles (the flag reaches the live system)
+    auto &o = k.observe();
+    auto v = o.virial(1, [](const auto &) {});
     // the SimulationLoop order (SimulationLoop.h:256-306)
     auto &a = k.actions();
     a.initializeKernel()->perform();
@@ -40,7 +43,7 @@ int main() {
     cfg.addBreakablePair(1, 1, 2.0, 0.5);
     a.breakBonds(0.04, cfg)->perform();
     a.clearNeighborList()->perform();
-    auto &o = k.observe();
+    v->evaluate();
     auto n = o.nParticles(1, {"A", "T"}, [](const auto &) {});
     n->evaluate();
     auto h = o.histogramAlongAxis(1, {0., 1., 2.5}, {"T"}, 2, [](const auto &) {});
@@ -48,6 +51,7 @@ int main() {
     auto r = o.radialDistribution(1, {0., 0.5, 1.0, 2.0}, {"A"}, {"A", "T"}, 0.25, [](const auto &) {});
     r->evaluate();
     fake_abi_log_context(0);
+    std::printf("virial %g %g %g\n", v->getResult().at(0, 0), v->getResult().at(1, 1), v->getResult().at(2, 2));
     std::printf("n particles %lu %lu\n", n->getResult()[0], n->getResult()[1]);
     std::printf("histogram %g %g\n", h->getResult()[0], h->getResult()[1]);
     const auto &[centers, distribution] = r->getResult();

@@ -310,6 +310,15 @@ int rdc_break_bonds(rdc_system *, double dt, int n_pairs, const int *t1, const i
     if (n_broken) *n_broken = 0;
     return RDC_OK;
 }
+int rdc_set_record_virial(rdc_system *, int record) {
+    if (g_log_context == 2) std::printf("system record virial %d\n", record);
+    return RDC_OK;
+}
+int rdc_get_virial(rdc_system *, double *virial9) {
+    if (g_log_context == 2) std::printf("get virial\n");
+    for (int k = 0; k < 9; ++k) virial9[k] = k + 1;
+    return RDC_OK;
+}
 int rdc_initialize(rdc_system *) {
     if (g_log_context == 2) std::printf("initialize\n");
     return RDC_OK;

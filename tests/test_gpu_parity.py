@@ -287,6 +287,22 @@ def test_virial_matches_oracle(rg):
     k2.add_particles(pos, types)
     k2.create_neighbor_list(ctx.calculate_max_cutoff())
     k2.calculate_forces()
+    f_off, _ = k2.get_forces()
+    assert np.all(k2.virial() == 0)
+    # switched on for the system as it is (rdc_set_record_virial: ReaDDy's Virial observable sets the flag
+    # after particles may have been added), the next force calculation records it; the forces are those of
+    # the walk that also sums the virial (each potential's force through a per-pair temporary), equal to the
+    # plain walk's within 1e-5 of the largest force
+    k2.set_record_virial(True)
+    k2.calculate_forces()
+    f_on, _ = k2.get_forces()
+    np.testing.assert_allclose(f_on, f_off, rtol=0, atol=1e-5 * np.abs(f_off).max())
+    np.testing.assert_allclose(k2.virial(), v_ref, rtol=0, atol=1e-5 * np.abs(v_ref).max())
+    # and through a run's captured graph, and off again
+    k2.run(2, 1e-4, handler=rg.UNCONTROLLED_APPROXIMATION)
+    assert np.abs(k2.virial()).max() > 0
+    k2.set_record_virial(False)
+    k2.calculate_forces()
     assert np.all(k2.virial() == 0)
 
 

@@ -179,7 +179,9 @@ def test_plugin_translates_the_context_into_the_abi(harness_objects, tmp_path):
 
 EXPECTED_SYSTEM_CALLS = """add particle (0.5 1.5 -2.5) type 0
 add particle (1 2 3) type 0
+system record virial 1
 add topology type 0: (0 0 0)/1 (1 0 0)/1 (2 0 0.25)/1 edges 0-1 1-2
+system record virial 1
 initialize
 neighbor list create 2.5
 calculate forces
@@ -189,9 +191,11 @@ uncontrolled approximation 0.02
 gillespie 0.03
 break bonds dt 0.04 1-1 threshold 2 rate 0.5
 neighbor list clear
+get virial
 count types
 histogram axis 2 borders 0 1 2.5 types 1
 radial distribution borders 0 0.5 1 2 from 0 to 0 1 density 0.25
+virial 1 5 9
 n particles 7 8
 histogram 0 1
 radial distribution centers 0.25 0.75 1.5 values 0 0.5 1"""
@@ -202,5 +206,7 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     ReaDDy's own interfaces: particles are uploaded at once, a topology with the edges added after addTopology
     returned is uploaded at the first action, every action passes its time step or cutoff, BreakBonds its
     configuration's pairs, and the observables their bins and type selections; the observables' results are
-    the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints)."""
+    the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints).  A Virial observable registered
+    after the system holds particles switches the live system's virial on, and InitializeKernel applies the
+    context's flag again, as CPUMiscActions.h:80-89 re-reads the context."""
     assert _harness(harness_objects, tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
