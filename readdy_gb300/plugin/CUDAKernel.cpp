@@ -436,7 +436,62 @@ void CUDAStateModel::removeParticle(const model::Particle &) {
 void CUDAStateModel::removeAllParticles() {
     _pending.clear();
     _topologies.clear();
-    _kernel->initialize();
+    _kernel->dropSystem();
+}
+
+CUDAStateModel::Snapshot CUDAStateModel::snapshot() const {
+    Snapshot snap;
+    rdc_system *s = _kernel->sysIfCreated();
+    if (!s) return snap;
+    const auto h = fetch(s);
+    std::unordered_map<uint64_t, std::size_t> at;  // device id -> index in h
+    for (std::size_t i = 0; i < h.ids.size(); ++i) at[h.ids[i]] = i;
+    int64_t nt = 0, ni = 0, ne = 0;
+    int st = rdc_get_topologies(s, 0, nullptr, nullptr, 0, nullptr, &nt, &ni);
+    if (st != RDC_OK && st != RDC_ERR_CAPACITY) check(st);
+    std::vector<int> types(nt);
+    std::vector<int64_t> off(nt + 1), eoff(nt + 1);
+    std::vector<uint64_t> ids(ni);
+    if (nt > 0) check(rdc_get_topologies(s, nt, types.data(), off.data(), ni, ids.data(), &nt, &ni));
+    st = rdc_get_topology_edges(s, 0, nullptr, 0, nullptr, &nt, &ne);
+    if (st != RDC_OK && st != RDC_ERR_CAPACITY) check(st);
+    std::vector<uint64_t> edges(2 * ne);
+    if (nt > 0) check(rdc_get_topology_edges(s, nt, eoff.data(), ne, edges.data(), &nt, &ne));
+    std::vector<char> in_topology(h.ids.size(), 0);
+    for (int64_t k = 0; k < nt; ++k) {
+        Snapshot::Top top;
+        top.type = types[k];
+        std::unordered_map<uint64_t, int64_t> local;
+        for (int64_t v = off[k]; v < off[k + 1]; ++v) {
+            const std::size_t i = at.at(ids[v]);
+            in_topology[i] = 1;
+            local[ids[v]] = v - off[k];
+            for (int d = 0; d < 3; ++d) top.x.push_back(h.pos[3 * i + d]);
+            top.t.push_back(h.types[i]);
+        }
+        for (int64_t e = eoff[k]; e < eoff[k + 1]; ++e) {
+            top.edges.push_back(local.at(edges[2 * e]));
+            top.edges.push_back(local.at(edges[2 * e + 1]));
+        }
+        snap.topologies.push_back(std::move(top));
+    }
+    for (std::size_t i = 0; i < h.ids.size(); ++i)
+        if (!in_topology[i])
+            snap.free.emplace_back(Vec3(h.pos[3 * i], h.pos[3 * i + 1], h.pos[3 * i + 2]), (ParticleTypeId)h.types[i],
+                                   (ParticleId)h.ids[i]);
+    return snap;
+}
+
+void CUDAStateModel::restore(const Snapshot &snap) {
+    rdc_system *s = _kernel->sysIfCreated();
+    if (!s) return;
+    if (!snap.free.empty()) addParticles(snap.free);
+    for (const auto &top : snap.topologies) {
+        std::vector<uint64_t> ids(top.t.size());
+        check(rdc_add_topology_typed(s, top.type, (int64_t)top.t.size(), top.x.data(), top.t.data(),
+                                     (int64_t)(top.edges.size() / 2), top.edges.data(), ids.data()));
+    }
+    if (!snap.topologies.empty()) reloadTopologies();
 }
 
 scalar CUDAStateModel::energy() const {
@@ -773,8 +828,8 @@ CUDAKernel::~CUDAKernel() {
 // system; particles added before are kept (read back and added to the new system)
 void CUDAKernel::initialize() {
     model::Kernel::initialize();
-    std::vector<model::Particle> keep;
-    if (_sys) keep = _state.getParticles();
+    CUDAStateModel::Snapshot keep;
+    if (_sys) keep = _state.snapshot();
     rdc_context *c = toDevice(context(), _rx);
     rdc_system *s = nullptr;
     const int rc = rdc_system_create(&s, c, seedFromEnvironment());
@@ -787,8 +842,13 @@ void CUDAKernel::initialize() {
     _ctx = c;
     _sys = s;
     registerStructuralReactions();
-    if (!keep.empty()) _state.addParticles(keep);
+    _state.restore(keep);
     check(rdc_initialize(_sys));
+}
+
+void CUDAKernel::dropSystem() {
+    if (_sys) rdc_system_destroy(_sys);
+    _sys = nullptr;
 }
 
 namespace {

@@ -60,6 +60,21 @@ public:
     void flushTopologies();
     // rebuilds the host topologies from the device's
     void reloadTopologies();
+    // The live system's particles outside topologies and its topologies (type, particles by local vertex,
+    // edges), read back so that a new system of the same state can replace it (Kernel::initialize).
+    struct Snapshot {
+        std::vector<model::Particle> free;
+        struct Top {
+            int type = 0;
+            std::vector<double> x;
+            std::vector<int> t;
+            std::vector<int64_t> edges;  // local vertex pairs
+        };
+        std::vector<Top> topologies;
+    };
+    Snapshot snapshot() const;
+    // uploads a snapshot into the current system (particle ids are those the new system gives)
+    void restore(const Snapshot &snap);
     // topology k of the device (rdc_get_topologies order) as a host GraphTopology for a structural reaction's
     // functions: local vertex v has persistent index v and holds the device id; until the next call,
     // getParticleForIndex serves its particles without reading the whole system back
@@ -144,7 +159,12 @@ public:
     // topology reactions and BreakBonds run in the C ABI (no per-operation actions are created)
     const model::top::TopologyActionFactory *const getTopologyActionFactory() const override { return nullptr; }
     model::top::TopologyActionFactory *const getTopologyActionFactory() override { return nullptr; }
+    // Kernel::initialize (CPUKernel.cpp:63-83): the context is read again into a new device system, which
+    // takes over the particles and topologies (their bonded terms derived again, reaction counts and virial
+    // reset, as the CPU kernel resets them); particle ids are renumbered
     void initialize() override;
+    // drops the system: the next use creates an empty one (StateModel::removeAllParticles)
+    void dropSystem();
     bool supportsGillespie() const override { return true; }
 
     // the device system of the current context (created by initialize); pending topologies are uploaded

@@ -50,6 +50,16 @@ int main() {
     h->evaluate();
     auto r = o.radialDistribution(1, {0., 0.5, 1.0, 2.0}, {"A"}, {"A", "T"}, 0.25, [](const auto &) {});
     r->evaluate();
+    // Kernel::initialize again (the CPU kernel's InitializeKernel action calls it): a new system takes over
+    // the free particles and the topology with its edges
+    k.initialize();
+    const auto tops = k.stateModel().getTopologies();
+    std::printf("after initialize: %zu particles, %zu topologies, %zu vertices, %zu edges\n",
+                k.stateModel().getParticles().size(), tops.size(), tops.at(0)->graph().vertices().size(),
+                tops.at(0)->graph().edges().size());
+    k.stateModel().removeAllParticles();
+    std::printf("after removeAllParticles: %zu particles, %zu topologies\n", k.stateModel().getParticles().size(),
+                k.stateModel().getTopologies().size());
     fake_abi_log_context(0);
     std::printf("virial %g %g %g\n", v->getResult().at(0, 0), v->getResult().at(1, 1), v->getResult().at(2, 2));
     std::printf("n particles %lu %lu\n", n->getResult()[0], n->getResult()[1]);

@@ -7,7 +7,9 @@
 //  * Context: after fake_abi_log_context(1) it records every rdc_context_* call with its arguments (doubles
 //    in the shortest form that reads back exactly).
 //  * System: after fake_abi_log_context(2) it records the state-model, action and observable calls with
-//    their arguments instead (particles, topologies with edges, time steps, break pairs, bins).
+//    their arguments instead (particles, topologies with edges, time steps, break pairs, bins).  It keeps
+//    the particles and topologies added since the last rdc_system_create and returns them from the
+//    particle and topology queries.
 // The plugin's other C-ABI calls resolve to stubs that return RDC_OK (generated by the test).
 #include <readdy_cuda.h>
 
@@ -29,6 +31,19 @@ int g_dummy;
 int g_log_context = 0;  // 1: context calls, 2: system calls
 int g_reaction_ids = 0;
 uint64_t g_next_id = 100;
+// the state of the one system: particles, and topologies as particle ids with id edges
+struct Part {
+    double x[3];
+    int type;
+    uint64_t id;
+};
+struct Top {
+    int type;
+    std::vector<uint64_t> ids;
+    std::vector<uint64_t> edges;
+};
+std::vector<Part> g_parts;
+std::vector<Top> g_tops;
 
 // the shortest %.*g form of x that reads back as x, without an exponent where one of at most 17 digits does
 std::string num(double x) {
@@ -197,6 +212,9 @@ int rdc_context_configure_cosine_dihedral(rdc_context *, int t1, int t2, int t3,
 int rdc_system_create(rdc_system **s, const rdc_context *, uint64_t) {
     *s = reinterpret_cast<rdc_system *>(&g_dummy);
     g_reactions.clear();
+    g_parts.clear();
+    g_tops.clear();
+    if (g_log_context == 2) std::printf("system create\n");
     return RDC_OK;
 }
 
@@ -279,9 +297,66 @@ int rdc_recipe_change_particle_position(rdc_recipe *, int64_t vertex, const doub
 int rdc_add_particles(rdc_system *, int64_t n, const double *x, const int *types, uint64_t *ids) {
     for (int64_t i = 0; i < n; ++i) {
         if (g_log_context == 2) std::printf("add particle %s type %d\n", vec3(x + 3 * i).c_str(), types[i]);
+        g_parts.push_back({{x[3 * i], x[3 * i + 1], x[3 * i + 2]}, types[i], g_next_id});
         if (ids) ids[i] = g_next_id;
         ++g_next_id;
     }
+    return RDC_OK;
+}
+int rdc_get_n_particles(rdc_system *, int64_t *n) {
+    *n = (int64_t)g_parts.size();
+    return RDC_OK;
+}
+int rdc_get_particles(rdc_system *, int64_t capacity, double *x, int *types, uint64_t *ids, int64_t *n_out) {
+    const int64_t n = (int64_t)g_parts.size();
+    if (n_out) *n_out = n;
+    if (capacity < n) return RDC_ERR_CAPACITY;
+    for (int64_t i = 0; i < n; ++i) {
+        if (x)
+            for (int d = 0; d < 3; ++d) x[3 * i + d] = g_parts[i].x[d];
+        if (types) types[i] = g_parts[i].type;
+        if (ids) ids[i] = g_parts[i].id;
+    }
+    return RDC_OK;
+}
+int rdc_get_topologies(rdc_system *, int64_t cap_t, int *types, int64_t *offsets, int64_t cap_i, uint64_t *ids,
+                       int64_t *n_t, int64_t *n_i) {
+    int64_t ni = 0;
+    for (const auto &t : g_tops) ni += (int64_t)t.ids.size();
+    *n_t = (int64_t)g_tops.size();
+    *n_i = ni;
+    if (cap_t < (int64_t)g_tops.size() || cap_i < ni) return RDC_ERR_CAPACITY;
+    int64_t at = 0;
+    for (std::size_t k = 0; k < g_tops.size(); ++k) {
+        if (types) types[k] = g_tops[k].type;
+        if (offsets) offsets[k] = at;
+        for (uint64_t id : g_tops[k].ids) {
+            if (ids) ids[at] = id;
+            ++at;
+        }
+    }
+    if (offsets) offsets[g_tops.size()] = at;
+    return RDC_OK;
+}
+int rdc_get_topology_edges(rdc_system *, int64_t cap_t, int64_t *offsets, int64_t cap_e, uint64_t *edges2,
+                           int64_t *n_t, int64_t *n_e) {
+    int64_t ne = 0;
+    for (const auto &t : g_tops) ne += (int64_t)t.edges.size() / 2;
+    *n_t = (int64_t)g_tops.size();
+    *n_e = ne;
+    if (cap_t < (int64_t)g_tops.size() || cap_e < ne) return RDC_ERR_CAPACITY;
+    int64_t at = 0;
+    for (std::size_t k = 0; k < g_tops.size(); ++k) {
+        if (offsets) offsets[k] = at;
+        for (std::size_t e = 0; e + 1 < g_tops[k].edges.size(); e += 2) {
+            if (edges2) {
+                edges2[2 * at] = g_tops[k].edges[e];
+                edges2[2 * at + 1] = g_tops[k].edges[e + 1];
+            }
+            ++at;
+        }
+    }
+    if (offsets) offsets[g_tops.size()] = at;
     return RDC_OK;
 }
 int rdc_add_topology_typed(rdc_system *, int topology_type, int64_t n, const double *x, const int *types,
@@ -293,10 +368,18 @@ int rdc_add_topology_typed(rdc_system *, int topology_type, int64_t n, const dou
         for (int64_t e = 0; e < n_edges; ++e) std::printf(" %lld-%lld", (long long)edges2[2 * e], (long long)edges2[2 * e + 1]);
         std::printf("\n");
     }
+    Top top{topology_type, {}, {}};
     for (int64_t i = 0; i < n; ++i) {
+        g_parts.push_back({{x[3 * i], x[3 * i + 1], x[3 * i + 2]}, types[i], g_next_id});
+        top.ids.push_back(g_next_id);
         if (ids) ids[i] = g_next_id;
         ++g_next_id;
     }
+    for (int64_t e = 0; e < n_edges; ++e) {
+        top.edges.push_back(top.ids[edges2[2 * e]]);
+        top.edges.push_back(top.ids[edges2[2 * e + 1]]);
+    }
+    g_tops.push_back(std::move(top));
     return RDC_OK;
 }
 int rdc_break_bonds(rdc_system *, double dt, int n_pairs, const int *t1, const int *t2, const double *thr,

@@ -195,6 +195,13 @@ get virial
 count types
 histogram axis 2 borders 0 1 2.5 types 1
 radial distribution borders 0 0.5 1 2 from 0 to 0 1 density 0.25
+system create
+add particle (0.5 1.5 -2.5) type 0
+add particle (1 2 3) type 0
+add topology type 0: (0 0 0)/1 (1 0 0)/1 (2 0 0.25)/1 edges 0-1 1-2
+initialize
+after initialize: 5 particles, 1 topologies, 3 vertices, 2 edges
+after removeAllParticles: 0 particles, 0 topologies
 virial 1 5 9
 n particles 7 8
 histogram 0 1
@@ -208,5 +215,7 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     configuration's pairs, and the observables their bins and type selections; the observables' results are
     the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints).  A Virial observable registered
     after the system holds particles switches the live system's virial on, and InitializeKernel applies the
-    context's flag again, as CPUMiscActions.h:80-89 re-reads the context."""
+    context's flag again, as CPUMiscActions.h:80-89 re-reads the context.  Kernel::initialize moves the free
+    particles and the topology, with its edges, to a new system (CPUKernel.cpp:63-83 keeps them), and
+    removeAllParticles leaves none."""
     assert _harness(harness_objects, tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
