@@ -65,6 +65,16 @@ int rdc_context_add_spatial_topology_reaction(rdc_context *ctx, int mode, int ty
                                               int topology_type2, int type_to1, int topology_type_to1, int type_to2,
                                               int topology_type_to2, double rate, double radius,
                                               int min_graph_distance, int *reaction_id);
+/* the rate of a topology-topology spatial reaction as a function of the two topologies (SpatialTopologyReaction's
+ * rate function, SpatialTopologyReaction.h:77-99,179-191): topology1 and topology2 are the indices
+ * (rdc_get_topologies order) of the topologies of the particles that take the reaction's first and second educt.
+ * It is called for every candidate pair at every evaluation (CPUEvaluateTopologyReactions.cpp:296-303), with
+ * the system only to be read; a rate below 0 or not a number raises RDC_ERR_RUNTIME. */
+typedef double (*rdc_spatial_rate_fn)(void *user, rdc_system *s, int64_t topology1, int64_t topology2);
+/* gives spatial reaction reaction_id (of rdc_context_add_spatial_topology_reaction) a rate function in place of
+ * its constant rate; topology-particle modes take constant rates only (the reference's rate() throws for them) */
+int rdc_context_set_spatial_topology_rate_function(rdc_context *ctx, int reaction_id, rdc_spatial_rate_fn rate,
+                                                   void *user);
 /* Context::legacyTopologySelfFusion: with 1, self fusions may also join vertices that share an edge */
 int rdc_context_set_legacy_topology_self_fusion(rdc_context *ctx, int legacy);
 /* ParticleTypeRegistry::add(name, D, flavor) (include/readdy/model/ParticleTypeRegistry.h:58-63,114):

@@ -75,6 +75,7 @@ def _load():
             "orc_evaluate_topology_reactions": (i, [vp, d, P(i64)]),
             "orc_topology_reaction_counts": (i, [vp, P(i64), i]),
             "orc_add_structural_topology_reaction": (i, [vp, i, RATE_FN, RECIPE_FN, vp, i]),
+            "orc_set_spatial_topology_rate_function": (i, [vp, i, SPATIAL_RATE_FN, vp]),
             "orc_structural_reaction_counts": (i, [vp, P(i64), i]),
             "orc_recipe_change_particle_type": (i, [vp, i64, i]),
             "orc_recipe_add_edge": (i, [vp, i64, i64]),
@@ -113,6 +114,7 @@ def _load():
 
 
 RATE_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_void_p, C.c_int64)
+SPATIAL_RATE_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64)
 RECIPE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p)
 
 
@@ -302,9 +304,23 @@ class OracleSystem:
         tt2 = -1 if educt2[1] is None else int(educt2[1])
         tto2 = -1 if product2[1] is None else int(product2[1])
         self._n_spatial = getattr(self, "_n_spatial", 0) + 1
-        return self._check(self._lib.orc_add_spatial_topology_reaction(
+        rid = self._check(self._lib.orc_add_spatial_topology_reaction(
             self._h, mode, educt1[0], educt1[1], educt2[0], tt2, product1[0], product1[1], product2[0], tto2,
-            rate, radius, min_graph_distance))
+            1.0 if callable(rate) else rate, radius, min_graph_distance))
+        if callable(rate):  # rate(view1, view2) of the two topologies
+            lib, h = self._lib, self._h
+
+            def rate_cb(_u, _s, g1, g2):
+                try:
+                    return float(rate(TopologyView(lib, h, g1), TopologyView(lib, h, g2)))
+                except BaseException as e:
+                    self._callback_error = getattr(self, "_callback_error", None) or e
+                    return float("nan")
+
+            cb = SPATIAL_RATE_FN(rate_cb)
+            self._callbacks = getattr(self, "_callbacks", []) + [cb]
+            self._check(self._lib.orc_set_spatial_topology_rate_function(self._h, rid, cb, None))
+        return rid
 
     def set_legacy_topology_self_fusion(self, legacy):
         return self._check(self._lib.orc_set_legacy_topology_self_fusion(self._h, int(bool(legacy))))

@@ -427,6 +427,8 @@ struct orc_system {
         int t1, tt1, t2, tt2, to1, tto1, to2, tto2;
         double rate, radius;
         int minGraphDistance;
+        orc_spatial_rate_fn rateFn = nullptr;  // topology-topology reactions: rate(top1, top2)
+        void *rateUser = nullptr;
         bool allowSelf() const { return mode == 2; }
         bool fusion() const { return mode == 1 || mode == 2 || mode == 4; }
         bool tp() const { return tt2 == -1; }
@@ -630,7 +632,17 @@ struct orc_system {
                         TREvent ev{r.rate, 0, -1, -1, &r, ip, jn, -1};
                         if (hasEntryTop && !hasNbTop) { ev.g1 = topOf[ip]; ev.idx1 = ip; ev.idx2 = jn; }
                         else if (!hasEntryTop && hasNbTop) { ev.g1 = topOf[jn]; ev.idx1 = jn; ev.idx2 = ip; }
-                        else { ev.g1 = topOf[ip]; ev.g2 = topOf[jn]; }
+                        else {
+                            ev.g1 = topOf[ip];
+                            ev.g2 = topOf[jn];
+                            // SpatialTopologyReaction::rate(top1, top2) (SpatialTopologyReaction.h:179-191)
+                            if (r.rateFn) {
+                                ev.rate = r.rateFn(r.rateUser, this, (int64_t)ev.g1, (int64_t)ev.g2);
+                                if (!(ev.rate >= 0.0))
+                                    throw std::runtime_error("a spatial topology reaction's rate function produced "
+                                                             "a rate smaller than 0");
+                            }
+                        }
                         if (r.allowSelf() && topOf[ip] == topOf[jn]) {
                             const int dg = graphDistance(graphs[topOf[ip]], vertexOf[ev.idx1], vertexOf[ev.idx2]);
                             if ((dg != -1 && dg <= r.minGraphDistance) || (!legacySelfFusion && dg == 1)) continue;
@@ -1740,6 +1752,15 @@ int orc_add_spatial_topology_reaction(orc_system *s, int mode, int t1, int tt1, 
     s->spatial.push_back({mode, t1, tt1, t2, tt2, to1, tto1, to2, tt2 == -1 ? -1 : tto2, rate, radius,
                           min_graph_distance});
     return (int)s->spatial.size() - 1;
+}
+int orc_set_spatial_topology_rate_function(orc_system *s, int reaction_id, orc_spatial_rate_fn rate, void *user) {
+    if (reaction_id < 0 || reaction_id >= (int)s->spatial.size() || s->spatial[reaction_id].tp()) {
+        g_err = "rate functions apply to topology-topology spatial reactions";
+        return -1;
+    }
+    s->spatial[reaction_id].rateFn = rate;
+    s->spatial[reaction_id].rateUser = user;
+    return 0;
 }
 int orc_set_legacy_topology_self_fusion(orc_system *s, int legacy) {
     s->legacySelfFusion = legacy != 0;

@@ -20,6 +20,10 @@ typedef struct orc_system orc_system;
 /* structural topology reactions: functions of the caller (StructuralTopologyReaction.h) */
 typedef struct orc_recipe orc_recipe;
 typedef double (*orc_topology_rate_fn)(void *user, orc_system *s, int64_t topology);
+/* SpatialTopologyReaction's rate function (SpatialTopologyReaction.h:77-99,179-191): the rate of a
+ * topology-topology event from the topologies of its two particles, in the order the reference lists them
+ * (CPUEvaluateTopologyReactions.cpp:296-303) */
+typedef double (*orc_spatial_rate_fn)(void *user, orc_system *s, int64_t topology1, int64_t topology2);
 typedef void (*orc_topology_recipe_fn)(void *user, orc_system *s, int64_t topology, orc_recipe *recipe);
 
 enum orc_handler { ORC_UNCONTROLLED_APPROXIMATION = 0, ORC_GILLESPIE = 1 };
@@ -87,6 +91,7 @@ int orc_add_spatial_topology_reaction(orc_system *s, int mode, int t1, int tt1, 
 int orc_set_legacy_topology_self_fusion(orc_system *s, int legacy);
 int orc_evaluate_topology_reactions(orc_system *s, double dt, int64_t *n_performed);
 int orc_topology_reaction_counts(const orc_system *s, int64_t *counts, int n);
+int orc_set_spatial_topology_rate_function(orc_system *s, int reaction_id, orc_spatial_rate_fn rate, void *user);
 int orc_add_structural_topology_reaction(orc_system *s, int topology_type, orc_topology_rate_fn rate,
                                          orc_topology_recipe_fn reaction, void *user, int expect_connected);
 int orc_structural_reaction_counts(const orc_system *s, int64_t *counts, int n);

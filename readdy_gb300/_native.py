@@ -35,6 +35,8 @@ class CapacityError(CudaKernelError):
 # structural topology reaction functions (include/readdy_cuda.h: rdc_topology_rate_fn, rdc_topology_recipe_fn)
 TOPOLOGY_RATE_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_void_p, C.c_int64)
 TOPOLOGY_RECIPE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p)
+# spatial topology reaction rate from two topologies (include/readdy_cuda.h: rdc_spatial_rate_fn)
+SPATIAL_RATE_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64)
 
 
 def _sig(lib):
@@ -53,6 +55,7 @@ def _sig(lib):
         "rdc_context_set_particle_flavor": (i, [vp, i, i]),
         "rdc_context_add_spatial_topology_reaction": (i, [vp, i, i, i, i, i, i, i, i, i, d, d, i, P(i)]),
         "rdc_context_set_legacy_topology_self_fusion": (i, [vp, i]),
+        "rdc_context_set_spatial_topology_rate_function": (i, [vp, i, SPATIAL_RATE_FN, vp]),
         "rdc_get_virial": (i, [vp, P(d)]),
         "rdc_set_record_virial": (i, [vp, i]),
         "rdc_context_add_harmonic_repulsion": (i, [vp, i, i, d, d]),

@@ -1092,10 +1092,20 @@ int64_t rdc_system::evaluate_topology_reactions(double dt) {
                 const int dgr = graph_distance(graphs[g1], slot_vertex[q.si], slot_vertex[q.sj]);
                 if ((dgr != -1 && dgr <= r.min_graph_distance) || (!ctx.legacy_self_fusion && dgr == 1)) continue;
             }
+            double rate = r.rate;
+            if (r.rate_fn) {  // SpatialTopologyReaction::rate(top1, top2), every candidate, every evaluation
+                in_callback = true;
+                rate = r.rate_fn(r.rate_user, this, (int64_t)g1, (int64_t)g2);
+                in_callback = false;
+                if (!(rate >= 0))
+                    throw std::runtime_error("a spatial topology reaction's rate function gave a rate below 0 or "
+                                             "not a number");
+                if (rate == 0) continue;
+            }
             const U4 u = rng_draw(seed, std::min(q.idi, q.idj), std::max(q.idi, q.idj), call, RNG_TOPOLOGY, (uint32_t)k);
             const double e1 = -std::log(((double)(u.x >> 8) + 0.5) * (1.0 / 16777216.0));
-            const bool fire = (((uint64_t)u.y << 32) | u.z) < coin_threshold(r.rate, dt);
-            ev.push_back(Event{k, c, swap, g1, g2, e1 / r.rate, fire});
+            const bool fire = (((uint64_t)u.y << 32) | u.z) < coin_threshold(rate, dt);
+            ev.push_back(Event{k, c, swap, g1, g2, e1 / rate, fire});
         }
     }
     if (ev.empty()) return 0;
@@ -1834,6 +1844,19 @@ int rdc_context_add_spatial_topology_reaction(rdc_context *ctx, int mode, int ty
                                                         topology_type_to1, type_to2, tp ? -1 : topology_type_to2, rate,
                                                         radius, min_graph_distance});
         if (reaction_id) *reaction_id = (int)ctx->d.spatial_top.size() - 1;
+    });
+}
+int rdc_context_set_spatial_topology_rate_function(rdc_context *ctx, int reaction_id, rdc_spatial_rate_fn rate,
+                                                   void *user) {
+    return guarded([&] {
+        require(ctx && rate, "null argument");
+        require(reaction_id >= 0 && reaction_id < (int)ctx->d.spatial_top.size(), "unknown spatial reaction id");
+        auto &r = ctx->d.spatial_top[reaction_id];
+        require(r.mode == STR_TT_ENZYMATIC || r.mode == STR_TT_FUSION || r.mode == STR_TT_FUSION_ALLOW_SELF,
+                "rate functions apply to topology-topology reactions (the reference's rate() throws for "
+                "topology-particle ones)");
+        r.rate_fn = rate;
+        r.rate_user = user;
     });
 }
 int rdc_context_set_legacy_topology_self_fusion(rdc_context *ctx, int legacy) {

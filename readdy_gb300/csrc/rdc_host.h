@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/readdy_cuda.h"
 #include "rdc_types.h"
 
 namespace rdc {
@@ -61,6 +62,8 @@ struct SpatialTopReaction {
     int t1, tt1, t2, tt2, to1, tto1, to2, tto2;
     double rate, radius;
     int min_graph_distance;  // self fusion: vertices at most this far apart in the graph do not react
+    rdc_spatial_rate_fn rate_fn = nullptr;  // topology-topology modes: the rate from the two topologies
+    void *rate_user = nullptr;
 };
 
 struct ContextData {

@@ -80,16 +80,31 @@ class Context:
         """TopologyRegistry::addSpatialReaction with the parsed descriptor: educt1/product1 are
         (particle type, topology type), educt2/product2 the same or (particle type, None) for a free
         particle (topology-particle modes).  A fusion's result takes product1's topology type; a self
-        fusion (TT_FUSION_ALLOW_SELF) needs more than min_graph_distance edges between the two.  Returns
-        the reaction's index."""
+        fusion (TT_FUSION_ALLOW_SELF) needs more than min_graph_distance edges between the two.  rate is a
+        number, or for topology-topology modes a function rate(view1, view2) of the TopologyViews of the
+        topologies that take the first and second educt, called for every candidate pair at every
+        evaluation.  Returns the reaction's index."""
         tt2 = -1 if educt2[1] is None else int(educt2[1])
         tto2 = -1 if product2[1] is None else int(product2[1])
         rid = C.c_int()
         N.check(self._lib.rdc_context_add_spatial_topology_reaction(
             self._h, int(mode), int(educt1[0]), int(educt1[1]), int(educt2[0]), tt2, int(product1[0]),
-            int(product1[1]), int(product2[0]), tto2, float(rate), float(radius), int(min_graph_distance),
-            C.byref(rid)))
+            int(product1[1]), int(product2[0]), tto2, 1.0 if callable(rate) else float(rate), float(radius),
+            int(min_graph_distance), C.byref(rid)))
         self._n_spatial = getattr(self, "_n_spatial", 0) + 1
+        if callable(rate):
+            lib = self._lib
+
+            def rate_cb(_user, sys, g1, g2):
+                try:
+                    return float(rate(TopologyView(lib, sys, g1), TopologyView(lib, sys, g2)))
+                except BaseException as e:  # reported by the call that ran the function
+                    self._callback_error = getattr(self, "_callback_error", None) or e
+                    return float("nan")
+
+            cb = N.SPATIAL_RATE_FN(rate_cb)
+            self._callbacks = getattr(self, "_callbacks", []) + [cb]
+            N.check(lib.rdc_context_set_spatial_topology_rate_function(self._h, rid.value, cb, None))
         return rid.value
 
     @property
@@ -290,9 +305,11 @@ class CUDAKernel:
         return nb.value
 
     def _check_callbacks(self, rc):
-        """Status of a call that may run structural reaction functions: their own exception first."""
-        err = getattr(self, "_callback_error", None)
+        """Status of a call that may run reaction functions (structural ones of this kernel, spatial rate
+        functions of its context): their own exception first."""
+        err = getattr(self, "_callback_error", None) or getattr(self.context, "_callback_error", None)
         self._callback_error = None
+        self.context._callback_error = None
         if err is not None:
             raise err
         N.check(rc)

@@ -11,6 +11,7 @@
 #include <readdy/model/topologies/reactions/TopologyReactionActionFactory.h>
 
 #include <algorithm>
+#include <limits>
 #include <cstdlib>
 #include <random>
 #include <set>
@@ -188,7 +189,9 @@ uint64_t seedFromEnvironment() {
 
 }  // namespace
 
-rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx) {
+rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx,
+                      std::vector<std::pair<int, const model::top::reactions::SpatialTopologyReaction *>>
+                              *rate_functions) {
     const auto &types = ctx.particleTypes();
     ParticleTypeId maxId = 0;
     for (const auto &[name, id] : types.typeMapping()) maxId = std::max(maxId, id);
@@ -205,20 +208,27 @@ rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx) {
         for (const auto &[name, id] : types.typeMapping())
             check(rdc_context_set_particle_flavor(c, (int)id, (int)types.infoOf(id).flavor));
         // spatial topology reactions (TopologyRegistry.h:265-281; each reaction sits in one bucket of the
-        // reversal-symmetric map); constant rates only: rate() throws for a rate function
+        // reversal-symmetric map); rate() throws for a reaction with a rate function, which the caller binds
         auto top_id = [](TopologyTypeId t) { return t == EmptyTopologyId ? -1 : (int)t; };
         for (const auto &[key, reactions] : ctx.topologyRegistry().spatialReactionRegistry())
             for (const auto &r : reactions) {
                 double rate = 0;
+                bool function = false;
                 try {
                     rate = r.rate();
                 } catch (const std::runtime_error &) {
-                    throw std::logic_error("CUDA kernel: spatial topology reactions with rate functions are not supported");
+                    if (!rate_functions)
+                        throw std::logic_error("CUDA kernel: a spatial topology reaction with a rate function "
+                                               "needs the kernel to bind it");
+                    rate = 1.0;  // replaced by the function
+                    function = true;
                 }
+                int id = -1;
                 check(rdc_context_add_spatial_topology_reaction(
                         c, (int)r.mode(), (int)r.type1(), top_id(r.top_type1()), (int)r.type2(), top_id(r.top_type2()),
                         (int)r.type_to1(), top_id(r.top_type_to1()), (int)r.type_to2(), top_id(r.top_type_to2()), rate,
-                        r.radius(), (int)r.min_graph_distance(), nullptr));
+                        r.radius(), (int)r.min_graph_distance(), &id));
+                if (function) rate_functions->emplace_back(id, &r);
             }
         check(rdc_context_set_legacy_topology_self_fusion(c, ctx.legacyTopologySelfFusion() ? 1 : 0));
         // each unordered type pair once: the registry files a pair's potentials under both orders
@@ -396,7 +406,7 @@ void CUDAStateModel::reloadTopologies() {
     }
 }
 
-std::unique_ptr<model::top::GraphTopology> CUDAStateModel::deviceTopology(int64_t k) {
+std::unique_ptr<model::top::GraphTopology> CUDAStateModel::deviceTopology(int64_t k, bool keep_view) {
     rdc_system *s = _kernel->sysIfCreated();
     int type = 0;
     int64_t nv = 0, ne = 0;
@@ -408,7 +418,7 @@ std::unique_ptr<model::top::GraphTopology> CUDAStateModel::deviceTopology(int64_
     std::vector<double> x(3 * nv);
     check(rdc_get_topology(s, k, &type, nv, ids.data(), types.data(), &nv, ne, edges.data(), &ne));
     check(rdc_get_topology_positions(s, k, nv, x.data()));
-    _view.clear();
+    if (!keep_view) _view.clear();
     model::top::Graph graph;
     for (int64_t v = 0; v < nv; ++v) {
         graph.addVertex(model::top::VertexData{(std::size_t)ids[v]});
@@ -830,7 +840,16 @@ void CUDAKernel::initialize() {
     model::Kernel::initialize();
     CUDAStateModel::Snapshot keep;
     if (_sys) keep = _state.snapshot();
-    rdc_context *c = toDevice(context(), _rx);
+    std::vector<std::pair<int, const model::top::reactions::SpatialTopologyReaction *>> functions;
+    rdc_context *c = toDevice(context(), _rx, &functions);
+    // the new context's rate functions: bound here, kept once the old system (which uses the old ones) is gone
+    std::vector<std::unique_ptr<SpatialBinding>> spatial;
+    try {
+        spatial = bindSpatialRateFunctions(c, functions);
+    } catch (...) {
+        rdc_context_destroy(c);
+        throw;
+    }
     rdc_system *s = nullptr;
     const int rc = rdc_system_create(&s, c, seedFromEnvironment());
     if (rc != RDC_OK) {
@@ -841,6 +860,7 @@ void CUDAKernel::initialize() {
     if (_ctx) rdc_context_destroy(_ctx);
     _ctx = c;
     _sys = s;
+    _spatial = std::move(spatial);
     registerStructuralReactions();
     _state.restore(keep);
     check(rdc_initialize(_sys));
@@ -916,6 +936,23 @@ struct RemoveEdgeMember {
 template struct MemberOf<AddEdgeMember, &rop::AddEdge::_edge>;
 template struct MemberOf<RemoveEdgeMember, &rop::RemoveEdge::_edge>;
 
+// rdc_spatial_rate_fn: SpatialTopologyReaction::rate(top1, top2) on the device topologies g1 and g2 (the
+// first and second educt's)
+double spatialRate(void *user, rdc_system *, int64_t g1, int64_t g2) {
+    auto *b = static_cast<CUDAKernel::SpatialBinding *>(user);
+    auto &state = b->kernel->cudaStateModel();
+    double rate = std::numeric_limits<double>::quiet_NaN();  // makes the evaluation fail after an exception
+    try {
+        const auto t1 = state.deviceTopology(g1);
+        const auto t2 = state.deviceTopology(g2, true);
+        rate = b->reaction.rate(*t1, *t2);
+    } catch (...) {
+        b->kernel->keepCallbackError(std::current_exception());
+    }
+    state.clearTopologyView();
+    return rate;
+}
+
 // rdc_topology_rate_fn: StructuralTopologyReaction::rate on the device topology k
 double structuralRate(void *user, rdc_system *, int64_t k) {
     auto *b = static_cast<CUDAKernel::StructuralBinding *>(user);
@@ -970,6 +1007,17 @@ void CUDAKernel::registerStructuralReactions() {
                                                        _structural.back().get(),
                                                        r.expects_connected_after_reaction() ? 1 : 0, nullptr));
         }
+}
+
+std::vector<std::unique_ptr<CUDAKernel::SpatialBinding>> CUDAKernel::bindSpatialRateFunctions(
+        rdc_context *c,
+        const std::vector<std::pair<int, const model::top::reactions::SpatialTopologyReaction *>> &functions) {
+    std::vector<std::unique_ptr<SpatialBinding>> bound;
+    for (const auto &[id, r] : functions) {
+        bound.push_back(std::make_unique<SpatialBinding>(SpatialBinding{this, *r}));
+        check(rdc_context_set_spatial_topology_rate_function(c, id, spatialRate, bound.back().get()));
+    }
+    return bound;
 }
 
 void CUDAKernel::rethrowCallbackError() {

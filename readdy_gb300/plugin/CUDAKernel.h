@@ -78,7 +78,7 @@ public:
     // topology k of the device (rdc_get_topologies order) as a host GraphTopology for a structural reaction's
     // functions: local vertex v has persistent index v and holds the device id; until the next call,
     // getParticleForIndex serves its particles without reading the whole system back
-    std::unique_ptr<model::top::GraphTopology> deviceTopology(int64_t k);
+    std::unique_ptr<model::top::GraphTopology> deviceTopology(int64_t k, bool keep_view = false);
     void clearTopologyView() { _view.clear(); }
 
 private:
@@ -183,6 +183,12 @@ public:
         CUDAKernel *kernel;
         model::top::reactions::StructuralTopologyReaction reaction;
     };
+    // a spatial topology reaction with a rate function (SpatialTopologyReaction.h:77-99), registered with
+    // rdc_context_set_spatial_topology_rate_function
+    struct SpatialBinding {
+        CUDAKernel *kernel;
+        model::top::reactions::SpatialTopologyReaction reaction;
+    };
     void keepCallbackError(std::exception_ptr e) {
         if (!_callbackError) _callbackError = std::move(e);
     }
@@ -190,19 +196,26 @@ public:
 
 private:
     void registerStructuralReactions();
+    std::vector<std::unique_ptr<SpatialBinding>> bindSpatialRateFunctions(
+            rdc_context *c,
+            const std::vector<std::pair<int, const model::top::reactions::SpatialTopologyReaction *>> &functions);
 
     rdc_context *_ctx = nullptr;
     rdc_system *_sys = nullptr;
     std::vector<int> _rx;
     std::vector<std::unique_ptr<StructuralBinding>> _structural;
+    std::vector<std::unique_ptr<SpatialBinding>> _spatial;
     std::exception_ptr _callbackError;
     CUDAStateModel _state;
     CUDAActionFactory _actions;
     CUDAObservableFactory _observables;
 };
 
-// model::Context -> a device context; fills rx with the device id of each reference reaction id
-rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx);
+// model::Context -> a device context; fills rx with the device id of each reference reaction id, and
+// rate_functions (when given) with the device id of each spatial topology reaction that has a rate function
+rdc_context *toDevice(const model::Context &ctx, std::vector<int> &rx,
+                      std::vector<std::pair<int, const model::top::reactions::SpatialTopologyReaction *>>
+                              *rate_functions = nullptr);
 
 }  // namespace readdy::kernel::cuda
 

@@ -219,3 +219,47 @@ def structural_system(make, n_small=1, chain=None, seed=1):
     for _ in range(n_small):
         s.add_topology(np.zeros((3, 3)), np.zeros(3, np.int32), [(0, 1), (1, 2)])
     return s
+
+
+def rate_function_system(make, rate, n_pairs=40, seed=1, spacing=6.0):
+    """Isolated pairs of topologies facing each other, for spatial reactions with a rate function: even pairs
+    are single-particle topologies X1 (type 0) and X2 (type 1) 0.5 apart, odd pairs chains X1-X1 and X2-X2 whose
+    facing ends are 0.5 apart (their other particles 1.0 further out, beyond the radius).  All four types are
+    TOPOLOGY flavored; X1 (topology type 0) + X2 (topology type 0) fuse into 2--3 of topology type 1 within
+    1.0 at `rate` (a number or a function of two topology views).  make: rg (the CUDA package) or "oracle".
+    Returns the system (kernel or oracle) with its neighbour list set up."""
+    side = int(np.ceil(n_pairs ** (1 / 3)))
+    L = side * spacing
+    g = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n_pairs]
+    centres = (g + 0.5) * spacing - L / 2
+    box = (L, L, L)
+    if make == "oracle":
+        s = oracle.OracleSystem(list(box), (True, True, True), 1.0, (0.0,) * 4, seed=seed)
+        conf = s
+    else:
+        conf = make.Context(box, (True, True, True), 1.0, (0.0,) * 4)
+    for t in range(4):
+        conf.set_particle_flavor(t, 1)
+    for a, b, l0 in ((0, 0, 1.0), (1, 1, 1.0), (2, 3, 0.5), (0, 2, 1.0), (1, 3, 1.0)):
+        conf.configure_harmonic_bond(a, b, 1.0, l0)
+    conf.add_spatial_topology_reaction(1, (0, 0), (1, 0), (2, 1), (3, 1), rate, 1.0)
+    if make != "oracle":
+        s = make.CUDAKernel(conf, seed=seed)
+    for k, c in enumerate(centres):
+        if k % 2 == 0:
+            s.add_topology(f32(c[None, :]), np.array([0], np.int32), [])
+            s.add_topology(f32(c[None, :] + (0.0, 0.0, 0.5)), np.array([1], np.int32), [])
+        else:
+            s.add_topology(f32(np.stack([c - (0.0, 0.0, 1.0), c])), np.array([0, 0], np.int32), [(0, 1)])
+            s.add_topology(f32(np.stack([c + (0.0, 0.0, 0.5), c + (0.0, 0.0, 1.5)])), np.array([1, 1], np.int32),
+                           [(0, 1)])
+    if make == "oracle":
+        s.nl_setup(1.0)
+    else:
+        s.create_neighbor_list(1.0)
+    return s
+
+
+def only_singles(a, b):
+    """A symmetric rate function: certain for two single-particle topologies, zero otherwise."""
+    return 1e10 if len(a.ids) + len(b.ids) == 2 else 0.0

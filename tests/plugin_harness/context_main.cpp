@@ -42,6 +42,11 @@ int main() {
     top.configureAnglePotential("C", "D", "C", {2.0, 3.0});
     top.configureTorsionPotential("C", "D", "D", "C", {1.0, 3.0, 0.5});
     top.addSpatialReaction("tt: T1(C)+T1(D)->T2(C--D)", 2.0, 1.5);
+    top.addSpatialReaction("tf: T2(C)+T2(D)->T1(C--D)",
+                           [](const readdy::model::top::GraphTopology &, const readdy::model::top::GraphTopology &) {
+                               return 1.0;
+                           },
+                           0.75);
     std::printf("ids A=%d B=%d C=%d D=%d T1=%d T2=%d\n", (int)ctx.particleTypes().idOf("A"),
                 (int)ctx.particleTypes().idOf("B"), (int)ctx.particleTypes().idOf("C"),
                 (int)ctx.particleTypes().idOf("D"), (int)top.idOf("T1"), (int)top.idOf("T2"));

@@ -1,9 +1,10 @@
 // TEST INFRASTRUCTURE ONLY: a host-side stand-in for the part of libreaddy_cuda_core.so that the ReaDDy
 // plugin calls while it sets a system up and runs structural topology reactions, so that the plugin's
 // mapping of ReaDDy's context and recipes onto the C ABI runs without a GPU.
-//  * Structural reactions: it holds one topology (a chain of three TOPOLOGY particles, ids 10 11 12, types
+//  * Topology reactions: it holds one topology (a chain of three TOPOLOGY particles, ids 10 11 12, types
 //    0 0 0, x = 1 2 3), records every rdc_recipe_* call on stdout, and makes rdc_evaluate_topology_reactions
-//    call each registered reaction's rate function and then its reaction function on that topology.
+//    call each registered structural reaction's rate function and then its reaction function on that
+//    topology, and each spatial rate function with that topology as both topologies.
 //  * Context: after fake_abi_log_context(1) it records every rdc_context_* call with its arguments (doubles
 //    in the shortest form that reads back exactly).
 //  * System: after fake_abi_log_context(2) it records the state-model, action and observable calls with
@@ -27,6 +28,12 @@ struct Registered {
     int type, expect_connected;
 };
 std::vector<Registered> g_reactions;
+struct SpatialFn {
+    rdc_spatial_rate_fn rate;
+    void *user;
+};
+std::vector<SpatialFn> g_spatial;  // rate functions of the last context
+std::vector<std::string> g_spatial_reactions;  // the spatial reactions of the last context, as logged
 int g_dummy;
 int g_log_context = 0;  // 1: context calls, 2: system calls
 int g_reaction_ids = 0;
@@ -73,6 +80,8 @@ int rdc_context_create(rdc_context **c, const double *box, const int *pbc, doubl
                        const double *D) {
     *c = reinterpret_cast<rdc_context *>(&g_dummy);
     g_reaction_ids = 0;
+    g_spatial.clear();
+    g_spatial_reactions.clear();
     if (g_log_context == 1) {
         std::printf("context box %s pbc %d %d %d kbt %s D", vec3(box).c_str(), pbc[0], pbc[1], pbc[2], num(kbt).c_str());
         for (int t = 0; t < n_types; ++t) std::printf(" %s", num(D[t]).c_str());
@@ -88,11 +97,19 @@ int rdc_context_add_spatial_topology_reaction(rdc_context *, int mode, int type1
                                               int topology_type2, int type_to1, int topology_type_to1, int type_to2,
                                               int topology_type_to2, double rate, double radius,
                                               int min_graph_distance, int *reaction_id) {
-    if (g_log_context == 1)
-        std::printf("spatial mode %d %d/%d + %d/%d -> %d/%d + %d/%d rate %s radius %s distance %d\n", mode, type1,
-                    topology_type1, type2, topology_type2, type_to1, topology_type_to1, type_to2, topology_type_to2,
-                    num(rate).c_str(), num(radius).c_str(), min_graph_distance);
-    if (reaction_id) *reaction_id = 0;
+    char line[256];
+    std::snprintf(line, sizeof line, "mode %d %d/%d + %d/%d -> %d/%d + %d/%d rate %s radius %s distance %d", mode,
+                  type1, topology_type1, type2, topology_type2, type_to1, topology_type_to1, type_to2,
+                  topology_type_to2, num(rate).c_str(), num(radius).c_str(), min_graph_distance);
+    if (g_log_context == 1) std::printf("spatial %s\n", line);
+    g_spatial_reactions.push_back(line);
+    if (reaction_id) *reaction_id = (int)g_spatial_reactions.size() - 1;
+    return RDC_OK;
+}
+int rdc_context_set_spatial_topology_rate_function(rdc_context *, int reaction_id, rdc_spatial_rate_fn rate,
+                                                   void *user) {
+    if (g_log_context == 1) std::printf("spatial rate function of %s\n", g_spatial_reactions.at(reaction_id).c_str());
+    g_spatial.push_back({rate, user});
     return RDC_OK;
 }
 int rdc_context_set_legacy_topology_self_fusion(rdc_context *, int legacy) {
@@ -258,6 +275,7 @@ int rdc_evaluate_topology_reactions(rdc_system *s, double, int64_t *performed) {
         rdc_recipe *recipe = reinterpret_cast<rdc_recipe *>(&g_dummy);
         r.reaction(r.user, s, 0, recipe);
     }
+    for (const auto &f : g_spatial) std::printf("spatial rate %.6g\n", f.rate(f.user, s, 0, 0));
     if (performed) *performed = 0;
     return RDC_OK;
 }

@@ -50,6 +50,16 @@ int main() {
             2.5);
     fixed.create_child_topologies_after_reaction();
     ctx.topologyRegistry().addStructuralReaction("T1", fixed);
+    // a spatial reaction whose rate is a function of the two topologies: 100 x the first's vertices plus the
+    // second's x coordinates
+    ctx.topologyRegistry().addSpatialReaction(
+            "sp: T1(A)+T1(B)->T1(A--B)",
+            [](const top::GraphTopology &t1, const top::GraphTopology &t2) {
+                double r = 100.0 * (double)t1.graph().vertices().size();
+                for (const auto &v : t2.graph().vertices()) r += t2.particleForVertex(v).pos()[0];
+                return r;
+            },
+            1.2);
     k.initialize();
     k.actions().evaluateTopologyReactions(1.0)->perform();
 

@@ -169,3 +169,48 @@ def test_normal_enzymatic_reaction_with_a_topology_catalyst(rg):
     _, t, _ = k.get_particles()
     assert sorted(t.tolist()) == [0, 2]
     assert len(k.get_topologies()) == 1
+
+
+def _tops(tops):
+    return {(int(tt), frozenset(int(i) for i in ids)) for tt, ids in tops}
+
+
+def test_spatial_rate_function_matches_oracle(rg):
+    """A rate function of the two topologies (SpatialTopologyReaction.h:179-191), certain for pairs of single
+    particles and zero for pairs of chains: exactly the single-particle pairs fuse, on the device as in the
+    oracle, topology for topology."""
+    from tests.helpers import only_singles, rate_function_system
+    k = rate_function_system(rg, only_singles, n_pairs=40)
+    o = rate_function_system("oracle", only_singles, n_pairs=40)
+    assert k.evaluate_topology_reactions(1e-3) == o.evaluate_topology_reactions(1e-3) == 20
+    assert _tops(k.get_topologies()) == _tops(o.topologies())
+    assert sorted((tt, len(ids)) for tt, ids in k.get_topologies()) == [(0, 2)] * 40 + [(1, 2)] * 20
+
+
+def test_spatial_rate_function_equal_to_the_constant_rate(rg):
+    """A rate function that returns the constant draws the same clocks and coins as the constant rate."""
+    from tests.helpers import rate_function_system
+    a = rate_function_system(rg, 700.0, n_pairs=60, seed=4)
+    b = rate_function_system(rg, lambda x, y: 700.0, n_pairs=60, seed=4)
+    na, nb = a.evaluate_topology_reactions(1e-3), b.evaluate_topology_reactions(1e-3)
+    assert na == nb and 0 < na < 60
+    assert _tops(a.get_topologies()) == _tops(b.get_topologies())
+
+
+def test_spatial_rate_function_errors(rg):
+    """A rate below 0 raises; an exception of the function reaches the caller; topology-particle reactions
+    take constant rates only."""
+    from tests.helpers import rate_function_system
+    k = rate_function_system(rg, lambda x, y: -1.0, n_pairs=8)
+    with pytest.raises(RuntimeError):
+        k.evaluate_topology_reactions(1e-3)
+
+    def bad(x, y):
+        raise KeyError("rate failed")
+
+    k = rate_function_system(rg, bad, n_pairs=8)
+    with pytest.raises(KeyError):
+        k.evaluate_topology_reactions(1e-3)
+    ctx = rg.Context((10.0, 10.0, 10.0), (True, True, True), 1.0, (0.0,) * 3)
+    with pytest.raises(ValueError):
+        ctx.add_spatial_topology_reaction(4, (0, 0), (1, None), (0, 0), (2, None), lambda x, y: 1.0, 1.0)

@@ -46,3 +46,46 @@ def test_oracle_topology_fusion_rate_matches_the_coin_probability():
     sizes = [len(i) for _, i in s.topologies()]
     assert sizes.count(2) == done and sizes.count(1) == 2 * (n - done)
     assert list(s.topology_reaction_counts()) == [done]
+
+
+def _tops(s):
+    return sorted((int(tt), tuple(sorted(int(i) for i in ids))) for tt, ids in s.topologies())
+
+
+def test_oracle_spatial_rate_function():
+    """SpatialTopologyReaction's rate function (SpatialTopologyReaction.h:179-191) called with the two
+    topologies of each candidate (CPUEvaluateTopologyReactions.cpp:296-303): certain for pairs of single
+    particles and zero for pairs of chains, so exactly the single-particle pairs fuse."""
+    from tests.helpers import only_singles, rate_function_system
+    s = rate_function_system("oracle", only_singles, n_pairs=40)
+    assert s.evaluate_topology_reactions(1e-3) == 20
+    tops = s.topologies()
+    assert len(tops) == 20 + 40
+    assert sorted((int(tt), len(ids)) for tt, ids in tops) == [(0, 2)] * 40 + [(1, 2)] * 20
+
+
+def test_oracle_spatial_rate_function_equal_to_the_constant_rate():
+    """A rate function that returns the constant gives the constant rate's result, event for event."""
+    from tests.helpers import rate_function_system
+    a = rate_function_system("oracle", 700.0, n_pairs=60, seed=4)
+    b = rate_function_system("oracle", lambda x, y: 700.0, n_pairs=60, seed=4)
+    na, nb = a.evaluate_topology_reactions(1e-3), b.evaluate_topology_reactions(1e-3)
+    assert na == nb and 0 < na < 60
+    assert _tops(a) == _tops(b)
+
+
+def test_oracle_spatial_rate_function_errors():
+    from tests.helpers import rate_function_system
+    s = rate_function_system("oracle", lambda x, y: -1.0, n_pairs=8)
+    with pytest.raises(RuntimeError):
+        s.evaluate_topology_reactions(1e-3)
+
+    def bad(x, y):
+        raise KeyError("rate failed")
+
+    s = rate_function_system("oracle", bad, n_pairs=8)
+    with pytest.raises(KeyError):
+        s.evaluate_topology_reactions(1e-3)
+    o = oracle.OracleSystem([10.0] * 3, (True, True, True), 1.0, (0.0,) * 3)
+    with pytest.raises(RuntimeError):  # topology-particle reactions take constant rates
+        o.add_spatial_topology_reaction(4, (0, 0), (1, None), (0, 0), (2, None), lambda x, y: 1.0, 1.0)

@@ -128,9 +128,13 @@ def test_plugin_structural_reactions_drive_the_recipe_abi(harness_objects, tmp_p
     reaction functions on the topology the C ABI describes: ReaDDy's own Recipe (Recipe.h, Recipe.cpp:55-69,
     with separateVertex's edge removals) becomes the rdc_recipe_* calls step by step, the rate function reads
     the topology's particles through the plugin's state model, and an exception of a reaction's function
-    reaches the caller of the EvaluateTopologyReactions action."""
+    reaches the caller of the EvaluateTopologyReactions action.  A spatial reaction's rate function
+    (SpatialTopologyReaction.h:77-99) is bound the same way and called with the two topologies."""
     lines = _harness(harness_objects, tmp_path, "structural_main.cpp")
     assert "\n".join(lines[:14]) == EXPECTED_STRUCTURAL_LOG
+    # the spatial reaction's rate function on the two topologies (the stand-in passes its one topology as
+    # both): 100 x 3 vertices + x = 1 + 2 + 3 of the second, read through the plugin's state model
+    assert lines[14] == "spatial rate 306"
     assert lines[-1] == "caught rate failed"
 
 
@@ -141,6 +145,8 @@ flavor 1 0
 flavor 2 1
 flavor 3 1
 spatial mode 1 2/0 + 3/0 -> 2/1 + 3/-1 rate 2 radius 1.5 distance 0
+spatial mode 1 2/1 + 3/1 -> 2/0 + 3/-1 rate 1 radius 0.75 distance 0
+spatial rate function of mode 1 2/1 + 3/1 -> 2/0 + 3/-1 rate 1 radius 0.75 distance 0
 legacy self fusion 0
 harmonic repulsion 0 1 k 10 d 1.1
 weak interaction 1 1 k 5 desired 0.7 depth 0.3 cutoff 1.9
