@@ -50,6 +50,17 @@ int main() {
     h->evaluate();
     auto r = o.radialDistribution(1, {0., 0.5, 1.0, 2.0}, {"A"}, {"A", "T"}, 0.25, [](const auto &) {});
     r->evaluate();
+    // ReaDDy's own Topologies observable (Topologies.cpp:61-82) over the plugin's getTopologies and
+    // toDenseParticleIndices
+    auto tobs = o.topologies(1);
+    tobs->evaluate();
+    for (const auto &rec : tobs->getResult()) {
+        std::printf("topology record type %d particles", (int)rec.type);
+        for (auto i : rec.particleIndices) std::printf(" %zu", (std::size_t)i);
+        std::printf(" edges");
+        for (const auto &[a, b] : rec.edges) std::printf(" %zu-%zu", (std::size_t)a, (std::size_t)b);
+        std::printf("\n");
+    }
     // Kernel::initialize again (the CPU kernel's InitializeKernel action calls it): a new system takes over
     // the free particles and the topology with its edges
     k.initialize();

@@ -201,6 +201,7 @@ get virial
 count types
 histogram axis 2 borders 0 1 2.5 types 1
 radial distribution borders 0 0.5 1 2 from 0 to 0 1 density 0.25
+topology record type 0 particles 2 3 4 edges 0-1 1-2
 system create
 add particle (0.5 1.5 -2.5) type 0
 add particle (1 2 3) type 0
@@ -219,7 +220,8 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     ReaDDy's own interfaces: particles are uploaded at once, a topology with the edges added after addTopology
     returned is uploaded at the first action, every action passes its time step or cutoff, BreakBonds its
     configuration's pairs, and the observables their bins and type selections; the observables' results are
-    the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints).  A Virial observable registered
+    the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints); ReaDDy's own Topologies observable
+    sees the topology with dense particle indices and local edges.  A Virial observable registered
     after the system holds particles switches the live system's virial on, and InitializeKernel applies the
     context's flag again, as CPUMiscActions.h:80-89 re-reads the context.  Kernel::initialize moves the free
     particles and the topology, with its edges, to a new system (CPUKernel.cpp:63-83 keeps them), and
