@@ -825,6 +825,45 @@ std::unique_ptr<obs::ReactionCounts> CUDAObservableFactory::reactionCounts(Strid
     return o;
 }
 
+// ---- topology action factory ----------------------------------------------------------------------
+
+namespace {
+[[noreturn]] void noHostTopologyAction() {
+    throw std::logic_error("CUDA kernel: bonded terms, BreakBonds and topology reactions are evaluated on the "
+                           "device; per-topology host actions are not provided");
+}
+}  // namespace
+
+std::unique_ptr<model::top::pot::CalculateHarmonicBondPotential>
+CUDATopologyActionFactory::createCalculateHarmonicBondPotential(const harmonic_bond *) const {
+    noHostTopologyAction();
+}
+std::unique_ptr<model::top::pot::CalculateHarmonicAnglePotential>
+CUDATopologyActionFactory::createCalculateHarmonicAnglePotential(const harmonic_angle *) const {
+    noHostTopologyAction();
+}
+std::unique_ptr<model::top::pot::CalculateCosineDihedralPotential>
+CUDATopologyActionFactory::createCalculateCosineDihedralPotential(const cos_dihedral *) const {
+    noHostTopologyAction();
+}
+CUDATopologyActionFactory::ActionPtr CUDATopologyActionFactory::createChangeParticleType(
+        model::top::GraphTopology *, const model::top::Graph::PersistentVertexIndex &, const ParticleTypeId &) const {
+    noHostTopologyAction();
+}
+CUDATopologyActionFactory::ActionPtr CUDATopologyActionFactory::createChangeParticlePosition(
+        model::top::GraphTopology *, const model::top::Graph::PersistentVertexIndex &, Vec3) const {
+    noHostTopologyAction();
+}
+CUDATopologyActionFactory::ActionPtr CUDATopologyActionFactory::createAppendParticle(
+        model::top::GraphTopology *, const std::vector<model::top::Graph::PersistentVertexIndex> &, ParticleTypeId,
+        const Vec3 &) const {
+    noHostTopologyAction();
+}
+CUDATopologyActionFactory::ActionPtr CUDATopologyActionFactory::createChangeTopologyType(model::top::GraphTopology *,
+                                                                                         const std::string &) const {
+    noHostTopologyAction();
+}
+
 // ---- kernel -----------------------------------------------------------------------------------------
 
 CUDAKernel::CUDAKernel() : model::Kernel("CUDA"), _state(this), _actions(this), _observables(this) {}

@@ -11,6 +11,7 @@
 #include <readdy/model/actions/Actions.h>
 #include <readdy/model/observables/ObservableFactory.h>
 #include <readdy/model/topologies/GraphTopology.h>
+#include <readdy/model/topologies/TopologyActionFactory.h>
 #include <readdy_cuda.h>
 
 #include <exception>
@@ -145,6 +146,29 @@ private:
     CUDAKernel *_kernel;
 };
 
+// The kernel's topology action factory (Kernel.h:177-199).  ReaDDy treats a kernel as supporting topologies
+// when it has one (Kernel::supportsTopologies): Simulation::addTopology and SimulationLoop's topology
+// reactions depend on it.  The plugin evaluates bonded terms, BreakBonds and topology reactions on the device
+// through its own actions, so none of its paths creates the per-topology host actions of this factory; a
+// caller that asks for one gets std::logic_error.
+class CUDATopologyActionFactory : public model::top::TopologyActionFactory {
+public:
+    std::unique_ptr<model::top::pot::CalculateHarmonicBondPotential>
+    createCalculateHarmonicBondPotential(const harmonic_bond *) const override;
+    std::unique_ptr<model::top::pot::CalculateHarmonicAnglePotential>
+    createCalculateHarmonicAnglePotential(const harmonic_angle *) const override;
+    std::unique_ptr<model::top::pot::CalculateCosineDihedralPotential>
+    createCalculateCosineDihedralPotential(const cos_dihedral *) const override;
+    ActionPtr createChangeParticleType(model::top::GraphTopology *, const model::top::Graph::PersistentVertexIndex &,
+                                       const ParticleTypeId &) const override;
+    ActionPtr createChangeParticlePosition(model::top::GraphTopology *, const model::top::Graph::PersistentVertexIndex &,
+                                           Vec3) const override;
+    ActionPtr createAppendParticle(model::top::GraphTopology *,
+                                   const std::vector<model::top::Graph::PersistentVertexIndex> &, ParticleTypeId,
+                                   const Vec3 &) const override;
+    ActionPtr createChangeTopologyType(model::top::GraphTopology *, const std::string &) const override;
+};
+
 class CUDAKernel : public model::Kernel {
 public:
     CUDAKernel();
@@ -156,9 +180,10 @@ public:
     model::actions::ActionFactory &actions() override { return _actions; }
     const model::observables::ObservableFactory &observe() const override { return _observables; }
     model::observables::ObservableFactory &observe() override { return _observables; }
-    // topology reactions and BreakBonds run in the C ABI (no per-operation actions are created)
-    const model::top::TopologyActionFactory *const getTopologyActionFactory() const override { return nullptr; }
-    model::top::TopologyActionFactory *const getTopologyActionFactory() override { return nullptr; }
+    // topology reactions and BreakBonds run in the C ABI (no per-operation actions are created); the factory
+    // is there so that ReaDDy sees topology support (Kernel::supportsTopologies)
+    const model::top::TopologyActionFactory *const getTopologyActionFactory() const override { return &_topologyActions; }
+    model::top::TopologyActionFactory *const getTopologyActionFactory() override { return &_topologyActions; }
     // Kernel::initialize (CPUKernel.cpp:63-83): the context is read again into a new device system, which
     // takes over the particles and topologies (their bonded terms derived again, reaction counts and virial
     // reset, as the CPU kernel resets them); particle ids are renumbered
@@ -209,6 +234,7 @@ private:
     CUDAStateModel _state;
     CUDAActionFactory _actions;
     CUDAObservableFactory _observables;
+    CUDATopologyActionFactory _topologyActions;
 };
 
 // model::Context -> a device context; fills rx with the device id of each reference reaction id, and

@@ -269,7 +269,8 @@ int rdc_get_topology_positions(rdc_system *, int64_t k, int64_t capacity, double
     return RDC_OK;
 }
 
-int rdc_evaluate_topology_reactions(rdc_system *s, double, int64_t *performed) {
+int rdc_evaluate_topology_reactions(rdc_system *s, double dt, int64_t *performed) {
+    if (g_log_context == 2) std::printf("evaluate topology reactions %s\n", num(dt).c_str());
     for (const auto &r : g_reactions) {
         std::printf("rate %.6g\n", r.rate(r.user, s, 0));
         rdc_recipe *recipe = reinterpret_cast<rdc_recipe *>(&g_dummy);

@@ -227,3 +227,33 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     particles and the topology, with its edges, to a new system (CPUKernel.cpp:63-83 keeps them), and
     removeAllParticles leaves none."""
     assert _harness(harness_objects, tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
+
+
+EXPECTED_LOOP_CALLS = """supports topologies 1
+add topology type 0: (0 0 0)/1 (1 0 0)/1 edges 0-1
+system record virial 0
+initialize
+neighbor list create 1.5
+calculate forces
+euler bd 0.01
+neighbor list update
+gillespie 0.01
+evaluate topology reactions 0.01
+neighbor list update
+calculate forces
+euler bd 0.01
+neighbor list update
+gillespie 0.01
+evaluate topology reactions 0.01
+neighbor list update
+calculate forces
+neighbor list clear"""
+
+
+def test_readdy_simulation_loop_drives_the_plugin(harness_objects, tmp_path):
+    """ReaDDy's own SimulationLoop (SimulationLoop.h:256-306) runs two steps through the plugin: ReaDDy sees
+    topology support (Kernel::supportsTopologies, which gates Simulation::addTopology and the loop's topology
+    reactions), and the loop's actions reach the ABI in its order, the neighbour list with the context's
+    largest cutoff (the pair potential's 1.5 over the topology reaction's radius 1.0)."""
+    lines = [l for l in _harness(harness_objects, tmp_path, "loop_main.cpp") if not l.startswith("[console]")]
+    assert lines == EXPECTED_LOOP_CALLS.splitlines()
