@@ -257,3 +257,58 @@ def test_readdy_simulation_loop_drives_the_plugin(harness_objects, tmp_path):
     largest cutoff (the pair potential's 1.5 over the topology reaction's radius 1.0)."""
     lines = [l for l in _harness(harness_objects, tmp_path, "loop_main.cpp") if not l.startswith("[console]")]
     assert lines == EXPECTED_LOOP_CALLS.splitlines()
+
+
+EXPECTED_PROVIDER_RUN = """CUDA kernel available 1
+selected CUDA supports topologies 1
+system create
+initialize
+add particle (0.5 0.5 0.5) type 0
+add topology type 0: (0 0 0)/1 (1 0 0)/1 edges 0-1
+system record virial 0
+initialize
+neighbor list create 1.5
+calculate forces
+count types
+observed 7 particles of A
+euler bd 0.01
+neighbor list update
+gillespie 0.01
+neighbor list update
+calculate forces
+count types
+observed 7 particles of A
+euler bd 0.01
+neighbor list update
+gillespie 0.01
+neighbor list update
+calculate forces
+count types
+observed 7 particles of A
+neighbor list clear"""
+
+
+def test_kernel_provider_loads_the_plugin_and_a_simulation_runs(harness_objects, tmp_path):
+    """The plugin built as libreaddy_kernel_cuda.so (with the stand-in C ABI inside) in a plugin directory:
+    ReaDDy's KernelProvider loads it (KernelProvider.cpp:99-175), readdy::Simulation("CUDA", context) creates
+    the kernel, adds a particle and a topology, registers an NParticles observable and runs two steps; the
+    stand-in's log shows the calls in SimulationLoop's order and the observable evaluated at every step."""
+    h = harness_objects
+    plugins = tmp_path / "plugins"
+    plugins.mkdir()
+    lib = plugins / LIB_NAME
+    assert loader_accepts(str(lib))
+    r = subprocess.run([h["cxx"], "-shared", "-o", str(lib), h["objs"]["plugin"], h["objs"]["fake"], h["objs"]["stubs"],
+                        "-L", h["libdir"], "-lreaddy_ref", "-Wl,-rpath," + h["libdir"]], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    main_obj, exe = str(tmp_path / "provider.o"), str(tmp_path / "provider")
+    r = subprocess.run([h["cxx"], *h["flags"], "-c", os.path.join(ROOT, "tests", "plugin_harness", "provider_main.cpp"),
+                        "-o", main_obj], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    r = subprocess.run([h["cxx"], main_obj, "-L", h["libdir"], "-lreaddy_ref", "-Wl,-rpath," + h["libdir"], "-pthread",
+                        "-ldl", "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    r = subprocess.run([exe, str(plugins)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-2000:])
+    lines = [l for l in r.stdout.strip().splitlines() if not l.startswith("[console]")]
+    assert lines == EXPECTED_PROVIDER_RUN.splitlines()
