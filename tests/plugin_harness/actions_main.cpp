@@ -17,6 +17,10 @@ int main() {
     ctx.boxSize() = {10., 10., 10.};
     ctx.particleTypes().add("A", 1.0);
     ctx.particleTypes().add("T", 1.0, readdy::model::particleflavor::TOPOLOGY);
+    ctx.particleTypes().add("B", 1.0);
+    // ReaDDy numbers reactions in registration order; the device numbers order-1 reactions first
+    const auto fus = ctx.reactions().addFusion("fus", "A", "A", "B", 1.0, 1.0);
+    const auto conv = ctx.reactions().addConversion("conv", "B", "A", 0.5);
     ctx.topologyRegistry().addType("chain");
     ctx.topologyRegistry().configureBondPotential("T", "T", {5.0, 1.0});
     k.initialize();
@@ -44,6 +48,10 @@ int main() {
     a.breakBonds(0.04, cfg)->perform();
     a.clearNeighborList()->perform();
     v->evaluate();
+    auto rc = o.reactionCounts(1, [](const auto &) {});
+    rc->evaluate();
+    const auto &counts = std::get<0>(rc->getResult());
+    std::printf("reaction counts fus %zu conv %zu\n", (std::size_t)counts.at(fus), (std::size_t)counts.at(conv));
     auto n = o.nParticles(1, {"A", "T"}, [](const auto &) {});
     n->evaluate();
     auto h = o.histogramAlongAxis(1, {0., 1., 2.5}, {"T"}, 2, [](const auto &) {});

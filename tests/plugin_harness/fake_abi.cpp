@@ -453,6 +453,11 @@ int rdc_gillespie(rdc_system *, double dt) {
     if (g_log_context == 2) std::printf("gillespie %s\n", num(dt).c_str());
     return RDC_OK;
 }
+int rdc_get_reaction_counts(rdc_system *, int n, int64_t *counts) {
+    if (g_log_context == 2) std::printf("get reaction counts\n");
+    for (int k = 0; k < n; ++k) counts[k] = 100 + k;  // device reaction k performed 100 + k times
+    return RDC_OK;
+}
 int rdc_count_types(rdc_system *, int64_t *counts) {
     if (g_log_context == 2) std::printf("count types\n");
     for (int t = 0; t < 2; ++t) counts[t] = 7 + t;

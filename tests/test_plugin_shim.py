@@ -198,6 +198,8 @@ gillespie 0.03
 break bonds dt 0.04 1-1 threshold 2 rate 0.5
 neighbor list clear
 get virial
+get reaction counts
+reaction counts fus 101 conv 100
 count types
 histogram axis 2 borders 0 1 2.5 types 1
 radial distribution borders 0 0.5 1 2 from 0 to 0 1 density 0.25
@@ -221,7 +223,9 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     returned is uploaded at the first action, every action passes its time step or cutoff, BreakBonds its
     configuration's pairs, and the observables their bins and type selections; the observables' results are
     the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints); ReaDDy's own Topologies observable
-    sees the topology with dense particle indices and local edges.  A Virial observable registered
+    sees the topology with dense particle indices and local edges.  ReactionCounts maps ReaDDy's reaction ids
+    (registration order: fusion 0, conversion 1) onto the device's (order-1 reactions first: conversion 0,
+    fusion 1), whose counts the stand-in gives as 100 + device id.  A Virial observable registered
     after the system holds particles switches the live system's virial on, and InitializeKernel applies the
     context's flag again, as CPUMiscActions.h:80-89 re-reads the context.  Kernel::initialize moves the free
     particles and the topology, with its edges, to a new system (CPUKernel.cpp:63-83 keeps them), and
