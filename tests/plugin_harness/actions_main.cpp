@@ -52,6 +52,21 @@ int main() {
     rc->evaluate();
     const auto &counts = std::get<0>(rc->getResult());
     std::printf("reaction counts fus %zu conv %zu\n", (std::size_t)counts.at(fus), (std::size_t)counts.at(conv));
+    auto fo = o.forces(1, {"A"}, [](const auto &) {});
+    fo->evaluate();
+    for (const auto &f : fo->getResult()) std::printf("force of A %g %g %g\n", f[0], f[1], f[2]);
+    auto po = o.positions(1, {"T"}, [](const auto &) {});
+    po->evaluate();
+    for (const auto &x : po->getResult()) std::printf("position of T %g %g %g\n", x[0], x[1], x[2]);
+    auto pa = o.particles(1, [](const auto &) {});
+    pa->evaluate();
+    const auto &[ptypes, pids, ppos] = pa->getResult();
+    std::printf("particles %zu:", ptypes.size());
+    for (std::size_t i = 0; i < ptypes.size(); ++i) std::printf(" %d/%zu", (int)ptypes[i], (std::size_t)pids[i]);
+    std::printf("\n");
+    auto en = o.energy(1, [](const auto &) {});
+    en->evaluate();
+    std::printf("energy %g\n", en->getResult());
     auto n = o.nParticles(1, {"A", "T"}, [](const auto &) {});
     n->evaluate();
     auto h = o.histogramAlongAxis(1, {0., 1., 2.5}, {"T"}, 2, [](const auto &) {});

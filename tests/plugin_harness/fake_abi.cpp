@@ -453,6 +453,25 @@ int rdc_gillespie(rdc_system *, double dt) {
     if (g_log_context == 2) std::printf("gillespie %s\n", num(dt).c_str());
     return RDC_OK;
 }
+int rdc_get_forces(rdc_system *, int64_t capacity, double *forces3, uint64_t *ids, int64_t *n_out) {
+    // particle i's force is (id, -id, 0.5), in storage order
+    const int64_t n = (int64_t)g_parts.size();
+    if (n_out) *n_out = n;
+    if (capacity < n) return RDC_ERR_CAPACITY;
+    for (int64_t i = 0; i < n; ++i) {
+        if (forces3) {
+            forces3[3 * i] = (double)g_parts[i].id;
+            forces3[3 * i + 1] = -(double)g_parts[i].id;
+            forces3[3 * i + 2] = 0.5;
+        }
+        if (ids) ids[i] = g_parts[i].id;
+    }
+    return RDC_OK;
+}
+int rdc_get_energy(rdc_system *, double *energy) {
+    *energy = 42.5;
+    return RDC_OK;
+}
 int rdc_get_reaction_counts(rdc_system *, int n, int64_t *counts) {
     if (g_log_context == 2) std::printf("get reaction counts\n");
     for (int k = 0; k < n; ++k) counts[k] = 100 + k;  // device reaction k performed 100 + k times

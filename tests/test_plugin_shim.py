@@ -200,6 +200,13 @@ neighbor list clear
 get virial
 get reaction counts
 reaction counts fus 101 conv 100
+force of A 100 -100 0.5
+force of A 101 -101 0.5
+position of T 0 0 0
+position of T 1 0 0
+position of T 2 0 0.25
+particles 5: 0/100 0/101 1/102 1/103 1/104
+energy 42.5
 count types
 histogram axis 2 borders 0 1 2.5 types 1
 radial distribution borders 0 0.5 1 2 from 0 to 0 1 density 0.25
@@ -225,7 +232,8 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     the ABI's (the RadialDistribution bin centres are ReaDDy's midpoints); ReaDDy's own Topologies observable
     sees the topology with dense particle indices and local edges.  ReactionCounts maps ReaDDy's reaction ids
     (registration order: fusion 0, conversion 1) onto the device's (order-1 reactions first: conversion 0,
-    fusion 1), whose counts the stand-in gives as 100 + device id.  A Virial observable registered
+    fusion 1), whose counts the stand-in gives as 100 + device id.  Forces and Positions keep the selected
+    types' particles, Particles all of them with types and ids, Energy the system's energy.  A Virial observable registered
     after the system holds particles switches the live system's virial on, and InitializeKernel applies the
     context's flag again, as CPUMiscActions.h:80-89 re-reads the context.  Kernel::initialize moves the free
     particles and the topology, with its edges, to a new system (CPUKernel.cpp:63-83 keeps them), and
