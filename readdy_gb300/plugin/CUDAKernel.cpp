@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <limits>
+#include <map>
 #include <cstdlib>
 #include <random>
 #include <set>
@@ -390,19 +391,41 @@ void CUDAStateModel::reloadTopologies() {
     if (st != RDC_OK && st != RDC_ERR_CAPACITY) check(st);
     std::vector<uint64_t> edges(2 * ne);
     check(rdc_get_topology_edges(s, nt, eoff.data(), ne, edges.data(), &nt, &ne));
+    // A topology whose particles are the same as before keeps its host object, with the type and graph the
+    // device has now: callers may hold pointers to it (Simulation::addTopology returns one), and the CPU kernel
+    // keeps the topologies that reactions left alone.  The others are created anew; vanished ones are dropped.
+    std::map<std::vector<std::size_t>, std::unique_ptr<model::top::GraphTopology>> previous;
+    for (auto &t : _topologies) {
+        std::vector<std::size_t> key;
+        for (const auto &v : t->graph().vertices()) key.push_back(v->particleIndex);
+        std::sort(key.begin(), key.end());
+        previous.emplace(std::move(key), std::move(t));
+    }
     _topologies.clear();
     for (int64_t k = 0; k < nt; ++k) {
         model::top::Graph graph;
         std::unordered_map<uint64_t, std::size_t> local;
+        std::vector<std::size_t> key;
         for (int64_t v = off[k]; v < off[k + 1]; ++v) {
             local[ids[v]] = (std::size_t)(v - off[k]);
             graph.addVertex(model::top::VertexData{(std::size_t)ids[v]});
+            key.push_back((std::size_t)ids[v]);
         }
         for (int64_t e = eoff[k]; e < eoff[k + 1]; ++e)
             graph.addEdge(graph.vertices().begin_persistent() + local.at(edges[2 * e]),
                           graph.vertices().begin_persistent() + local.at(edges[2 * e + 1]));
-        _topologies.push_back(std::make_unique<model::top::GraphTopology>((TopologyTypeId)types[k], std::move(graph),
-                                                                          _kernel->context(), this));
+        std::sort(key.begin(), key.end());
+        if (auto it = previous.find(key); it != previous.end()) {
+            auto top = std::move(it->second);
+            previous.erase(it);
+            top->type() = (TopologyTypeId)types[k];
+            top->setGraph(std::move(graph));
+            _topologies.push_back(std::move(top));
+        } else {
+            _topologies.push_back(std::make_unique<model::top::GraphTopology>((TopologyTypeId)types[k],
+                                                                              std::move(graph), _kernel->context(),
+                                                                              this));
+        }
     }
 }
 

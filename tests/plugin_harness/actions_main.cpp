@@ -46,6 +46,8 @@ int main() {
     readdy::model::actions::top::BreakConfig cfg;
     cfg.addBreakablePair(1, 1, 2.0, 0.5);
     a.breakBonds(0.04, cfg)->perform();
+    // the topology the caller holds is still the state model's after the reload (its particles are unchanged)
+    std::printf("same topology object after reload %d\n", (int)(k.stateModel().getTopologies().at(0) == t));
     a.clearNeighborList()->perform();
     v->evaluate();
     auto rc = o.reactionCounts(1, [](const auto &) {});

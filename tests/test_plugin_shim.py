@@ -196,6 +196,7 @@ neighbor list update
 uncontrolled approximation 0.02
 gillespie 0.03
 break bonds dt 0.04 1-1 threshold 2 rate 0.5
+same topology object after reload 1
 neighbor list clear
 get virial
 get reaction counts
@@ -235,7 +236,8 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     fusion 1), whose counts the stand-in gives as 100 + device id.  Forces and Positions keep the selected
     types' particles, Particles all of them with types and ids, Energy the system's energy.  A Virial observable registered
     after the system holds particles switches the live system's virial on, and InitializeKernel applies the
-    context's flag again, as CPUMiscActions.h:80-89 re-reads the context.  Kernel::initialize moves the free
+    context's flag again, as CPUMiscActions.h:80-89 re-reads the context.  After BreakBonds reads the
+    topologies back, the topology object the caller got from addTopology is still the state model's.  Kernel::initialize moves the free
     particles and the topology, with its edges, to a new system (CPUKernel.cpp:63-83 keeps them), and
     removeAllParticles leaves none."""
     assert _harness(harness_objects, tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
