@@ -575,8 +575,14 @@ std::unique_ptr<act::CalculateForces> CUDAActionFactory::calculateForces() const
     return std::make_unique<CallAction<act::CalculateForces>>([k] { check(rdc_calculate_forces(k->sys())); });
 }
 std::unique_ptr<act::CreateNeighborList> CUDAActionFactory::createNeighborList(scalar cutoff) const {
-    auto *k = _kernel;
-    return std::make_unique<CallAction<act::CreateNeighborList, scalar>>([k, cutoff] { check(rdc_nl_create(k->sys(), cutoff)); }, cutoff);
+    // the cutoff as the action holds it when performed: SimulationLoop raises it to the context's largest
+    // (SimulationLoop.h:266-268) and ReaDDy's Python API adds its skin through the same reference
+    struct Create : act::CreateNeighborList {
+        CUDAKernel *k;
+        Create(CUDAKernel *k, scalar c) : act::CreateNeighborList(c), k(k) {}
+        void perform() override { check(rdc_nl_create(k->sys(), cutoffDistance())); }
+    };
+    return std::make_unique<Create>(_kernel, cutoff);
 }
 std::unique_ptr<act::UpdateNeighborList> CUDAActionFactory::updateNeighborList() const {
     auto *k = _kernel;

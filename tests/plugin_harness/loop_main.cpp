@@ -30,6 +30,7 @@ int main() {
     t->addEdge(PV{0}, PV{1});
     fake_abi_log_context(2);
     readdy::api::SimulationLoop loop(&k, 0.01);
+    loop.neighborListCutoff() += 0.5;  // a skin, as ReaDDy's Python API adds it (simulation.py:555-556)
     loop.run(2);
     fake_abi_log_context(0);
     return 0;

@@ -247,7 +247,7 @@ EXPECTED_LOOP_CALLS = """supports topologies 1
 add topology type 0: (0 0 0)/1 (1 0 0)/1 edges 0-1
 system record virial 0
 initialize
-neighbor list create 1.5
+neighbor list create 2
 calculate forces
 euler bd 0.01
 neighbor list update
@@ -267,8 +267,9 @@ neighbor list clear"""
 def test_readdy_simulation_loop_drives_the_plugin(harness_objects, tmp_path):
     """ReaDDy's own SimulationLoop (SimulationLoop.h:256-306) runs two steps through the plugin: ReaDDy sees
     topology support (Kernel::supportsTopologies, which gates Simulation::addTopology and the loop's topology
-    reactions), and the loop's actions reach the ABI in its order, the neighbour list with the context's
-    largest cutoff (the pair potential's 1.5 over the topology reaction's radius 1.0)."""
+    reactions), and the loop's actions reach the ABI in its order; the neighbour list takes the cutoff the loop
+    holds when it runs: the context's largest (the pair potential's 1.5 over the topology reaction's radius
+    1.0) plus the skin of 0.5 set through SimulationLoop::neighborListCutoff()."""
     lines = [l for l in _harness(harness_objects, tmp_path, "loop_main.cpp") if not l.startswith("[console]")]
     assert lines == EXPECTED_LOOP_CALLS.splitlines()
 
