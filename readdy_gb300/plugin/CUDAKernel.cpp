@@ -316,6 +316,29 @@ model::Particle CUDAStateModel::getParticleForIndex(std::size_t index) const {
 
 ParticleTypeId CUDAStateModel::getParticleType(std::size_t index) const { return getParticleForIndex(index).type(); }
 
+std::vector<model::Particle> CUDAStateModel::getParticlesForTopology(const model::top::GraphTopology &topology) const {
+    std::vector<model::Particle> out;
+    for (const auto &p : _pending)  // vertices of a pending topology hold their index in its particle list
+        if (p.top.get() == &topology) {
+            for (const auto &v : topology.graph().vertices())
+                if (!v.deactivated()) out.push_back(p.particles.at(v->particleIndex));
+            return out;
+        }
+    const auto h = fetch(_kernel->sysIfCreated());
+    std::unordered_map<uint64_t, std::size_t> at;
+    for (std::size_t i = 0; i < h.ids.size(); ++i) at[h.ids[i]] = i;
+    for (const auto &v : topology.graph().vertices()) {
+        if (v.deactivated()) continue;
+        const auto it = at.find((uint64_t)v->particleIndex);
+        if (it == at.end())
+            throw std::out_of_range("CUDA kernel: no particle with index " + std::to_string(v->particleIndex));
+        const std::size_t i = it->second;
+        out.emplace_back(Vec3(h.pos[3 * i], h.pos[3 * i + 1], h.pos[3 * i + 2]), (ParticleTypeId)h.types[i],
+                         (ParticleId)h.ids[i]);
+    }
+    return out;
+}
+
 void CUDAStateModel::initializeNeighborList(scalar cutoff) { check(rdc_nl_create(_kernel->sys(), cutoff)); }
 void CUDAStateModel::updateNeighborList() { check(rdc_nl_update(_kernel->sys())); }
 void CUDAStateModel::clearNeighborList() { check(rdc_nl_clear(_kernel->sys())); }

@@ -38,6 +38,9 @@ public:
     std::vector<Vec3> getParticlePositions() const override;
     std::vector<model::Particle> getParticles() const override;
     model::Particle getParticleForIndex(std::size_t index) const override;
+    // the particles of a topology by vertex: one read-back of the system (StateModel.cpp:47-55 looks each vertex
+    // up by itself); a topology not uploaded yet gives the particles it was added with
+    std::vector<model::Particle> getParticlesForTopology(const model::top::GraphTopology &topology) const override;
     ParticleTypeId getParticleType(std::size_t index) const override;
     void initializeNeighborList(scalar interactionDistance) override;
     void updateNeighborList() override;

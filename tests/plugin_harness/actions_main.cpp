@@ -31,6 +31,13 @@ int main() {
                                           readdy::model::Particle(2., 0., 0.25, 1)});
     t->addEdge(PV{0}, PV{1});
     t->addEdge(PV{1}, PV{2});
+    auto print_particles = [&](const char *when) {
+        std::printf("topology particles %s:", when);
+        for (const auto &p : k.stateModel().getParticlesForTopology(*t))
+            std::printf(" (%g %g %g)/%d", p.pos()[0], p.pos()[1], p.pos()[2], (int)p.type());
+        std::printf("\n");
+    };
+    print_particles("pending");
     // a Virial observable registered after the system holds particles (the flag reaches the live system)
     auto &o = k.observe();
     auto v = o.virial(1, [](const auto &) {});
@@ -48,6 +55,7 @@ int main() {
     a.breakBonds(0.04, cfg)->perform();
     // the topology the caller holds is still the state model's after the reload (its particles are unchanged)
     std::printf("same topology object after reload %d\n", (int)(k.stateModel().getTopologies().at(0) == t));
+    print_particles("uploaded");
     a.clearNeighborList()->perform();
     v->evaluate();
     auto rc = o.reactionCounts(1, [](const auto &) {});
