@@ -309,6 +309,7 @@ std::vector<model::Particle> CUDAStateModel::getParticles() const {
 // the particle whose device id is `index` (topology vertices hold device ids as their particle index)
 model::Particle CUDAStateModel::getParticleForIndex(std::size_t index) const {
     if (const auto it = _view.find(index); it != _view.end()) return it->second;
+    if (const auto it = _pendingParticles.find(index); it != _pendingParticles.end()) return it->second;
     for (const auto &p : getParticles())
         if (p.id() == index) return p;
     throw std::out_of_range("CUDA kernel: no particle with index " + std::to_string(index));
@@ -318,10 +319,10 @@ ParticleTypeId CUDAStateModel::getParticleType(std::size_t index) const { return
 
 std::vector<model::Particle> CUDAStateModel::getParticlesForTopology(const model::top::GraphTopology &topology) const {
     std::vector<model::Particle> out;
-    for (const auto &p : _pending)  // vertices of a pending topology hold their index in its particle list
+    for (const auto &p : _pending)  // vertices of a pending topology hold placeholder indices
         if (p.top.get() == &topology) {
             for (const auto &v : topology.graph().vertices())
-                if (!v.deactivated()) out.push_back(p.particles.at(v->particleIndex));
+                if (!v.deactivated()) out.push_back(_pendingParticles.at(v->particleIndex));
             return out;
         }
     const auto h = fetch(_kernel->sysIfCreated());
@@ -356,7 +357,10 @@ void CUDAStateModel::addParticles(const std::vector<model::Particle> &ps) {
 model::top::GraphTopology *const CUDAStateModel::addTopology(TopologyTypeId type,
                                                             const std::vector<model::Particle> &particles) {
     model::top::Graph graph;
-    for (std::size_t i = 0; i < particles.size(); ++i) graph.addVertex(model::top::VertexData{i});
+    for (const auto &p : particles) {
+        _pendingParticles.emplace(_nextPending, p);
+        graph.addVertex(model::top::VertexData{_nextPending++});
+    }
     auto top = std::make_unique<model::top::GraphTopology>(type, std::move(graph), _kernel->context(), this);
     auto *raw = top.get();
     _pending.push_back(PendingTopology{std::move(top), particles});
@@ -376,22 +380,25 @@ void CUDAStateModel::flushTopologies() {
             for (int d = 0; d < 3; ++d) x[3 * i + d] = pt.particles[i].pos()[d];
             t[i] = (int)pt.particles[i].type();
         }
-        // edges by the vertices' local particle indices (the position in the list given to addTopology)
+        // edges by the vertices' local indices (the position in the list given to addTopology), from their
+        // placeholders
+        std::unordered_map<std::size_t, int64_t> local;
+        for (std::size_t i = 0; i < n; ++i) local[g.vertices().at(model::top::Graph::PersistentVertexIndex{i})->particleIndex] = (int64_t)i;
         std::vector<int64_t> edges;
         for (const auto &[v1, v2] : g.edges()) {
-            edges.push_back((int64_t)g.vertices().at(v1)->particleIndex);
-            edges.push_back((int64_t)g.vertices().at(v2)->particleIndex);
+            edges.push_back(local.at(g.vertices().at(v1)->particleIndex));
+            edges.push_back(local.at(g.vertices().at(v2)->particleIndex));
         }
         std::vector<uint64_t> ids(n);
         check(rdc_add_topology_typed(s, (int)pt.top->type(), (int64_t)n, x.data(), t.data(),
                                      (int64_t)(edges.size() / 2), edges.data(), ids.data()));
         // from now on a vertex refers to its particle by the device id
         model::top::Graph relabelled;
-        std::unordered_map<std::size_t, std::size_t> local;
         for (std::size_t i = 0; i < n; ++i) relabelled.addVertex(model::top::VertexData{(std::size_t)ids[i]});
         for (const auto &[v1, v2] : g.edges())
-            relabelled.addEdge(relabelled.vertices().begin_persistent() + g.vertices().at(v1)->particleIndex,
-                               relabelled.vertices().begin_persistent() + g.vertices().at(v2)->particleIndex);
+            relabelled.addEdge(relabelled.vertices().begin_persistent() + local.at(g.vertices().at(v1)->particleIndex),
+                               relabelled.vertices().begin_persistent() + local.at(g.vertices().at(v2)->particleIndex));
+        for (const auto &[placeholder, i] : local) _pendingParticles.erase(placeholder);
         pt.top->setGraph(std::move(relabelled));
         _topologies.push_back(std::move(pt.top));
     }
@@ -491,6 +498,7 @@ void CUDAStateModel::removeParticle(const model::Particle &) {
 
 void CUDAStateModel::removeAllParticles() {
     _pending.clear();
+    _pendingParticles.clear();
     _topologies.clear();
     _kernel->dropSystem();
 }

@@ -94,6 +94,11 @@ private:
     std::vector<PendingTopology> _pending;
     std::vector<std::unique_ptr<model::top::GraphTopology>> _topologies;
     std::unordered_map<std::size_t, model::Particle> _view;  // particles of the last deviceTopology
+    // Until its upload, a topology's vertices hold placeholder indices (above any device id) of the particles it
+    // was added with, so that particle lookups by vertex (GraphTopology::particleForVertex) find them.
+    static constexpr std::size_t PENDING_INDEX = std::size_t(1) << 62;
+    std::unordered_map<std::size_t, model::Particle> _pendingParticles;
+    std::size_t _nextPending = PENDING_INDEX;
     mutable scalar _energy = 0;
     scalar _time = 0;
 };

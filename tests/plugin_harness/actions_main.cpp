@@ -38,6 +38,8 @@ int main() {
         std::printf("\n");
     };
     print_particles("pending");
+    std::printf("pending vertex 2 type %d x %g\n", (int)t->particleForVertex(PV{2}).type(),
+                t->particleForVertex(PV{2}).pos()[0]);
     // a Virial observable registered after the system holds particles (the flag reaches the live system)
     auto &o = k.observe();
     auto v = o.virial(1, [](const auto &) {});

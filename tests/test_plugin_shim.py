@@ -186,6 +186,7 @@ def test_plugin_translates_the_context_into_the_abi(harness_objects, tmp_path):
 EXPECTED_SYSTEM_CALLS = """add particle (0.5 1.5 -2.5) type 0
 add particle (1 2 3) type 0
 topology particles pending: (0 0 0)/1 (1 0 0)/1 (2 0 0.25)/1
+pending vertex 2 type 1 x 2
 system record virial 1
 add topology type 0: (0 0 0)/1 (1 0 0)/1 (2 0 0.25)/1 edges 0-1 1-2
 system record virial 1
@@ -240,7 +241,8 @@ def test_plugin_state_model_actions_and_observables_reach_the_abi(harness_object
     after the system holds particles switches the live system's virial on, and InitializeKernel applies the
     context's flag again, as CPUMiscActions.h:80-89 re-reads the context.  After BreakBonds reads the
     topologies back, the topology object the caller got from addTopology is still the state model's, and
-    getParticlesForTopology gives its particles before and after the upload.  Kernel::initialize moves the free
+    getParticlesForTopology gives its particles before and after the upload (before it, the vertices hold
+    placeholder indices that GraphTopology::particleForVertex resolves too).  Kernel::initialize moves the free
     particles and the topology, with its edges, to a new system (CPUKernel.cpp:63-83 keeps them), and
     removeAllParticles leaves none."""
     assert _harness(harness_objects, tmp_path, "actions_main.cpp") == EXPECTED_SYSTEM_CALLS.splitlines()
